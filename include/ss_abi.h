@@ -1,0 +1,166 @@
+/*
+ * ss_abi.h — C-ABI of the GB300-native SuperScanner reconstruction hot path.
+ *
+ * Plain C: pointers, sizes and POD structs only. Every device buffer is a raw
+ * device pointer owned by the caller; every pose is a host array copied into
+ * kernel parameters at call time. All calls are stream-ordered and
+ * asynchronous unless stated otherwise; a device-side status word collects
+ * kernel-detected errors and is returned by ss_grid_sync().
+ *
+ * Reference interfaces replaced (paths inside Pandia3DPublic/SuperScanner):
+ *   GPUVoxelGrid ctor                  src/VoxelGrid/GPUVoxelGrid.h:43, .cpp:10-30
+ *   GPUVoxelGrid::setIntrinsic         src/VoxelGrid/GPUVoxelGrid.h:118-119, .cpp:253-266
+ *   GPUVoxelGrid::integrate            src/VoxelGrid/GPUVoxelGrid.h:98-101, .cpp:41-83
+ *   GPUVoxelGrid::deIntegrate          src/VoxelGrid/GPUVoxelGrid.h:102-105, .cpp:95-136
+ *   GPUVoxelGrid::raycast              src/VoxelGrid/GPUVoxelGrid.h:107-108, .cpp:139-147
+ *   GPUVoxelGrid::cleanMemory          src/VoxelGrid/GPUVoxelGrid.h:116-117, .cpp:185-196
+ *   GPUVoxelGrid::marchingCubesHost    src/VoxelGrid/GPUVoxelGrid.cpp:200-251 (the host
+ *                                       copy of the map; replaced by ss_grid_export_blocks)
+ *   CreatePcdFromDepthView             src/utils/imageutil.cpp:89-111
+ *   CalculateNormalsFromPCDView        src/utils/imageutil.cpp:117-157
+ *   kokkosICP(View,View,tx,ty,type,r)  src/postprocessing/kokkosICP.h:19-21, .cpp:25-210
+ *
+ * Image layout: row-major [rows][cols] (row = i, col = j as in the reference's
+ * depth(i, j)); depth is uint16 millimetres, colour is uint8 x3 interleaved,
+ * point/normal maps are float x3 interleaved. Poses are 4x4 row-major.
+ */
+#ifndef SS_ABI_H
+#define SS_ABI_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Same handle type as cudaStream_t; NULL is the legacy default stream. */
+typedef struct CUstream_st *ss_stream_t;
+
+typedef enum ss_status {
+    SS_OK = 0,
+    SS_ERR_ARG = 1,           /* null pointer, bad size, bad enum */
+    SS_ERR_DIMS = 2,          /* image size differs from the grid's (GPUVoxelGrid.cpp:46-49 only printed) */
+    SS_ERR_TABLE_FULL = 3,    /* no free bucket for a new block (reference: unchecked, GPUVoxelGrid.cpp:497-500) */
+    SS_ERR_LIST_OVERFLOW = 4, /* touched-block list overflow (reference: unchecked, GPUVoxelGrid.cpp:506-508) */
+    SS_ERR_TIMEOUT = 5,       /* a bounded device loop hit its iteration cap */
+    SS_ERR_CUDA = 6,          /* a CUDA runtime call failed */
+    SS_ERR_RANGE = 7,         /* a block coordinate outside the packable range (|c| > 8191 blocks) */
+    SS_ERR_STATE = 8,         /* call order violated (e.g. integrate before set_intrinsic) */
+    SS_ERR_NOMEM = 9          /* device allocation failed */
+} ss_status;
+
+typedef enum ss_storage {
+    SS_STORAGE_F32 = 0,       /* plain form: FP32 sdf + FP32 weight (8 B/voxel) */
+    SS_STORAGE_F16 = 1        /* precision form: FP16 sdf/trunc + uint16 weight (4 B/voxel), FP32 math */
+} ss_storage;
+
+typedef enum ss_icp_type {    /* src/postprocessing/kokkosICP.h:4-8 */
+    SS_ICP_POINT_TO_POINT = 0,
+    SS_ICP_POINT_TO_PLANE = 1
+} ss_icp_type;
+
+typedef struct ss_params {
+    float voxel_length;       /* vl, metres (GPUVoxelGrid.h:48) */
+    float truncation;         /* d_trunc, metres (GPUVoxelGrid.h:47) */
+    int32_t resi;             /* image rows (GPUVoxelGrid.h:50) */
+    int32_t resj;             /* image cols (GPUVoxelGrid.h:51) */
+    uint32_t hash_buckets;    /* power of two; bucket i owns block payload i (like UnorderedMap::value_at) */
+    int32_t storage;          /* ss_storage */
+    int32_t with_color;       /* allocate FP32 r,g,b planes (Voxel::r,g,b, GPUVoxelGrid.h:15-17) */
+    float max_weight;         /* 0 = uncapped, as the reference (GPUVoxelGrid.h:14,62) */
+    float rmin;               /* minimal integrated depth, 0.2 m (GPUVoxelGrid.h:56) */
+    float d_max;              /* raycast range, 10 m (GPUVoxelGrid.h:55) */
+} ss_params;
+
+typedef struct ss_grid ss_grid;
+
+/* Fills the reference defaults of GPUVoxelGrid(c, trunc, voxlength, resi, resj)
+ * (GPUVoxelGrid.cpp:10-30): buckets = next power of two >= c / 512. */
+ss_status ss_params_default(ss_params *p, uint32_t capacity_voxels, float trunc,
+                            float voxel_length, int32_t resi, int32_t resj);
+
+ss_status ss_grid_create(const ss_params *p, ss_grid **out);
+ss_status ss_grid_destroy(ss_grid *g);
+/* Resets the volume to empty (all buckets free, all payload zero). */
+ss_status ss_grid_reset(ss_grid *g, ss_stream_t s);
+
+/* setIntrinsic (GPUVoxelGrid.cpp:253-266): fx, fy, cx, cy of the pinhole model;
+ * the grid uses ci = resi - cy, cj = cx exactly as the reference. */
+ss_status ss_grid_set_intrinsic(ss_grid *g, float fx, float fy, float cx, float cy);
+
+/* integrate / deIntegrate (GPUVoxelGrid.cpp:41-136). depth: [resi][resj] u16 mm,
+ * rgb: [resi][resj][3] u8 or NULL (required when with_color != 0);
+ * extr: camera->world, row-major. No host synchronisation inside. */
+ss_status ss_integrate(ss_grid *g, const uint16_t *depth, const uint8_t *rgb,
+                       const float extr[16], int32_t with_color, ss_stream_t s);
+ss_status ss_deintegrate(ss_grid *g, const uint16_t *depth, const uint8_t *rgb,
+                         const float extr[16], int32_t with_color, ss_stream_t s);
+
+/* raycast (GPUVoxelGrid.cpp:139-147, 561-715): reference semantics — nearest
+ * voxel march from 0.1 m to d_max, world-space points into ray_pcd
+ * [resi][resj][3], colour/255 into ray_color (may be NULL). Misses are 0. */
+ss_status ss_raycast(ss_grid *g, const float extr[16], float *ray_pcd, float *ray_color,
+                     ss_stream_t s);
+
+/* cleanMemory (GPUVoxelGrid.cpp:185-196, 785-805): frees every block whose 512
+ * weights are all zero. */
+ss_status ss_clean_memory(ss_grid *g, ss_stream_t s);
+
+/* Same as ss_integrate / ss_deintegrate (deint != 0), with FMA-contracted
+ * single-precision arithmetic in the voxel update; block allocation keeps
+ * the reference rounding. Used by the per-frame pipeline. No reference
+ * counterpart (an addition of this library). */
+ss_status ss_integrate_fast(ss_grid *g, const uint16_t *depth, const uint8_t *rgb,
+                            const float extr[16], int32_t with_color, int32_t deint,
+                            ss_stream_t s);
+
+/* Synchronises the stream and returns (then clears) the device status word. */
+ss_status ss_grid_sync(ss_grid *g, ss_stream_t s);
+
+/* Synchronises the stream and copies the grid counters: out = {live blocks,
+ * blocks touched by the last call, blocks touched by all calls, calls,
+ * status bits, epoch}. No reference counterpart. */
+ss_status ss_grid_counters(ss_grid *g, ss_stream_t s, int64_t out[6]);
+
+/* Text of the last CUDA error seen by this thread (for SS_ERR_CUDA). */
+const char *ss_last_error(void);
+
+/* Number of allocated blocks (synchronises the stream). */
+ss_status ss_grid_block_count(ss_grid *g, ss_stream_t s, int32_t *count);
+
+/* Canonical dump of the map, sorted by key (the u64 prime hash), into HOST
+ * buffers of room for max_blocks entries: keys, block coords [n][3],
+ * sdf [n][512], weight [n][512], rgb [n][3][512] (NULL to skip any).
+ * Voxel order inside a block is x + 8y + 64z (GPUVoxelGrid.h:28-31). */
+ss_status ss_grid_export_blocks(ss_grid *g, ss_stream_t s, int32_t max_blocks,
+                                uint64_t *keys, int32_t *coords, float *sdf,
+                                float *weight, float *rgb, int32_t *n_out);
+
+/* Loads a dump written by ss_grid_export_blocks (checkpoint / resume). */
+ss_status ss_grid_import_blocks(ss_grid *g, ss_stream_t s, int32_t n, const int32_t *coords,
+                                const float *sdf, const float *weight, const float *rgb);
+
+/* CreatePcdFromDepthView (imageutil.cpp:89-111): pcd [rows][cols][3]. */
+ss_status ss_depth_to_pcd(const uint16_t *depth, int32_t rows, int32_t cols, float fx, float fy,
+                          float cx, float cy, float *pcd, ss_stream_t s);
+
+/* CalculateNormalsFromPCDView (imageutil.cpp:117-157): normals [rows][cols][3]. */
+ss_status ss_normals_from_pcd(const float *pcd, int32_t rows, int32_t cols, float *normals,
+                              ss_stream_t s);
+
+/* kokkosICP(View d1, View d2, tx, ty, type, rmse) (kokkosICP.cpp:25-210):
+ * aligns depth d1 (pose tx) to depth d2 (pose ty); returns the best relative
+ * transform Txy (4x4 row-major, host) and its RMSE. Correspondence search,
+ * reductions and the 3x3 SVD all run on the device; the call synchronises s
+ * once at the end to return the result. Scratch memory is allocated on the
+ * first call per device and reused. */
+ss_status ss_kokkos_icp(const uint16_t *d1, const uint16_t *d2, int32_t rows, int32_t cols,
+                        float fx, float fy, float cx, float cy, const double tx[16],
+                        const double ty[16], int32_t icp_type, double txy_out[16],
+                        float *rmse_out, ss_stream_t s);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SS_ABI_H */

@@ -1,0 +1,170 @@
+"""CPU oracle of the reconstruction hot path — test infrastructure only.
+
+Loads ``oracle/_build/libss_oracle.so`` (built from ss_oracle.cpp by the
+Makefile beside it). Only tests/, __graft_entry__.smoke() and bench.py's CPU
+baseline legs use this module; the product package never imports it.
+Parity status: unpinned by the reference (see ss_oracle.cpp's header).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+_DIR = Path(__file__).resolve().parent
+_LIB_PATH = _DIR / "_build" / "libss_oracle.so"
+
+
+def build(force: bool = False) -> Path:
+    srcs = list(_DIR.glob("*.cpp")) + [_DIR / "Makefile"]
+    if force or not _LIB_PATH.exists() or _LIB_PATH.stat().st_mtime < max(p.stat().st_mtime for p in srcs):
+        subprocess.run(["make", "-s", "-B" if force else "-s", "-C", str(_DIR)], check=True)
+    return _LIB_PATH
+
+
+build()
+_lib = C.CDLL(str(_LIB_PATH))
+_p, _i, _f = C.c_void_p, C.c_int, C.c_float
+for name, res, args in [
+    ("orc_grid_new", _p, [_f, _f, _i, _i, _f]),
+    ("orc_grid_free", None, [_p]),
+    ("orc_grid_set_intrinsic", None, [_p, _f, _f, _f, _f]),
+    ("orc_grid_fuse", _i, [_p, _p, _p, _p, _i, _i]),
+    ("orc_grid_count", _i, [_p]),
+    ("orc_grid_export", _i, [_p, _i, _p, _p, _p, _p, _p]),
+    ("orc_grid_import", None, [_p, _i, _p, _p, _p, _p]),
+    ("orc_grid_clean", _i, [_p]),
+    ("orc_grid_raycast", None, [_p, _p, _p, _p]),
+    ("orc_depth_to_pcd", None, [_p, _i, _i, _f, _f, _f, _f, _p]),
+    ("orc_normals", None, [_p, _i, _i, _p]),
+    ("orc_kokkos_icp", _i, [_p, _p, _i, _i, _f, _f, _f, _f, _p, _p, _i, _p, _p, _p]),
+    ("orc_svd3", None, [_p, _p, _p, _p]),
+    ("orc_inverse4f", None, [_p, _p]),
+    ("orc_mat4_vec4", None, [_p, _p, _p]),
+    ("orc_threads", _i, []),
+]:
+    fn = getattr(_lib, name)
+    fn.restype = res
+    fn.argtypes = args
+
+
+def _ptr(a):
+    return C.c_void_p(a.ctypes.data) if a is not None else C.c_void_p()
+
+
+def _f32(a, shape=None):
+    a = np.ascontiguousarray(a, np.float32)
+    if shape is not None:
+        a = a.reshape(shape)
+    return a
+
+
+class OracleGrid:
+    """Reference-semantics voxel grid (GPUVoxelGrid restated on the CPU)."""
+
+    def __init__(self, vl, trunc, resi, resj, intr=(525.0, 525.0, 319.5, 239.5), max_weight=0.0):
+        self.resi, self.resj = resi, resj
+        self._h = _lib.orc_grid_new(vl, trunc, resi, resj, max_weight)
+        _lib.orc_grid_set_intrinsic(self._h, *map(float, intr))
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            _lib.orc_grid_free(self._h)
+            self._h = None
+
+    def fuse(self, depth, rgb, extr, with_color=True, deint=False) -> int:
+        depth = np.ascontiguousarray(depth, np.uint16)
+        rgb = np.ascontiguousarray(rgb, np.uint8) if (with_color and rgb is not None) else None
+        E = _f32(extr, (16,))
+        return _lib.orc_grid_fuse(self._h, _ptr(depth), _ptr(rgb), _ptr(E), int(with_color and rgb is not None),
+                                  int(deint))
+
+    def integrate(self, depth, rgb, extr, with_color=True):
+        return self.fuse(depth, rgb, extr, with_color, False)
+
+    def deintegrate(self, depth, rgb, extr, with_color=True):
+        return self.fuse(depth, rgb, extr, with_color, True)
+
+    def count(self) -> int:
+        return _lib.orc_grid_count(self._h)
+
+    def export(self) -> dict:
+        n = self.count()
+        keys = np.zeros(n, np.uint64)
+        coords = np.zeros((n, 3), np.int32)
+        sdf = np.zeros((n, 512), np.float32)
+        w = np.zeros((n, 512), np.float32)
+        rgb = np.zeros((n, 3, 512), np.float32)
+        _lib.orc_grid_export(self._h, n, _ptr(keys), _ptr(coords), _ptr(sdf), _ptr(w), _ptr(rgb))
+        return dict(keys=keys, coords=coords, sdf=sdf, w=w, rgb=rgb)
+
+    def import_blocks(self, coords, sdf, w, rgb=None):
+        coords = np.ascontiguousarray(coords, np.int32)
+        _lib.orc_grid_import(self._h, len(coords), _ptr(coords), _ptr(_f32(sdf)), _ptr(_f32(w)),
+                             _ptr(_f32(rgb)) if rgb is not None else C.c_void_p())
+
+    def clean(self) -> int:
+        return _lib.orc_grid_clean(self._h)
+
+    def raycast(self, extr):
+        pcd = np.zeros((self.resi, self.resj, 3), np.float32)
+        col = np.zeros((self.resi, self.resj, 3), np.float32)
+        _lib.orc_grid_raycast(self._h, _ptr(_f32(extr, (16,))), _ptr(pcd), _ptr(col))
+        return pcd, col
+
+
+def depth_to_pcd(depth, intr=(525.0, 525.0, 319.5, 239.5)):
+    depth = np.ascontiguousarray(depth, np.uint16)
+    rows, cols = depth.shape
+    out = np.zeros((rows, cols, 3), np.float32)
+    _lib.orc_depth_to_pcd(_ptr(depth), rows, cols, *map(float, intr), _ptr(out))
+    return out
+
+
+def normals(pcd):
+    pcd = _f32(pcd)
+    rows, cols, _ = pcd.shape
+    out = np.zeros_like(pcd)
+    _lib.orc_normals(_ptr(pcd), rows, cols, _ptr(out))
+    return out
+
+
+def kokkos_icp(d1, d2, tx, ty, icp_type=0, intr=(525.0, 525.0, 319.5, 239.5)):
+    d1 = np.ascontiguousarray(d1, np.uint16)
+    d2 = np.ascontiguousarray(d2, np.uint16)
+    rows, cols = d1.shape
+    tx = np.ascontiguousarray(tx, np.float64)
+    ty = np.ascontiguousarray(ty, np.float64)
+    out = np.zeros(16, np.float64)
+    rmse = np.zeros(1, np.float32)
+    stats = np.zeros((10, 4), np.float64)
+    _lib.orc_kokkos_icp(_ptr(d1), _ptr(d2), rows, cols, *map(float, intr), _ptr(tx), _ptr(ty), int(icp_type),
+                        _ptr(out), _ptr(rmse), _ptr(stats))
+    return out.reshape(4, 4), float(rmse[0]), stats
+
+
+def svd3(H):
+    H = np.ascontiguousarray(H, np.float64)
+    U = np.zeros(9)
+    S = np.zeros(3)
+    V = np.zeros(9)
+    _lib.orc_svd3(_ptr(H), _ptr(U), _ptr(S), _ptr(V))
+    return U.reshape(3, 3), S, V.reshape(3, 3)
+
+
+def inverse4f(E):
+    out = np.zeros(16, np.float32)
+    _lib.orc_inverse4f(_ptr(_f32(E, (16,))), _ptr(out))
+    return out.reshape(4, 4)
+
+
+def mat4_vec4(M, v):
+    out = np.zeros(4, np.float32)
+    _lib.orc_mat4_vec4(_ptr(_f32(M, (16,))), _ptr(_f32(v, (4,))), _ptr(out))
+    return out
+
+
+def threads() -> int:
+    return _lib.orc_threads()

@@ -1,0 +1,91 @@
+"""ctypes binding of libss.so (the C-ABI declared in include/ss_abi.h)."""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+_PKG = Path(__file__).resolve().parent
+LIB_PATH = _PKG / "libss.so"
+
+if not LIB_PATH.exists():
+    raise ImportError(
+        f"{LIB_PATH} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'` "
+        "(there is no CPU fallback for the reconstruction path)")
+
+lib = C.CDLL(str(LIB_PATH))
+
+STATUS = {
+    0: "SS_OK", 1: "SS_ERR_ARG", 2: "SS_ERR_DIMS", 3: "SS_ERR_TABLE_FULL", 4: "SS_ERR_LIST_OVERFLOW",
+    5: "SS_ERR_TIMEOUT", 6: "SS_ERR_CUDA", 7: "SS_ERR_RANGE", 8: "SS_ERR_STATE", 9: "SS_ERR_NOMEM",
+}
+SS_OK, SS_ERR_ARG, SS_ERR_DIMS, SS_ERR_TABLE_FULL, SS_ERR_LIST_OVERFLOW = 0, 1, 2, 3, 4
+SS_ERR_TIMEOUT, SS_ERR_CUDA, SS_ERR_RANGE, SS_ERR_STATE, SS_ERR_NOMEM = 5, 6, 7, 8, 9
+SS_STORAGE_F32, SS_STORAGE_F16 = 0, 1
+
+
+class SSError(RuntimeError):
+    def __init__(self, code: int, where: str):
+        self.code = code
+        detail = lib.ss_last_error().decode(errors="replace") if code == SS_ERR_CUDA else ""
+        super().__init__(f"{where}: {STATUS.get(code, code)} {detail}".strip())
+
+
+def check(code: int, where: str) -> int:
+    if code != SS_OK:
+        raise SSError(code, where)
+    return code
+
+
+class SSParams(C.Structure):
+    _fields_ = [
+        ("voxel_length", C.c_float), ("truncation", C.c_float), ("resi", C.c_int32), ("resj", C.c_int32),
+        ("hash_buckets", C.c_uint32), ("storage", C.c_int32), ("with_color", C.c_int32),
+        ("max_weight", C.c_float), ("rmin", C.c_float), ("d_max", C.c_float),
+    ]
+
+
+_p, _i32, _u32, _f, _st = C.c_void_p, C.c_int32, C.c_uint32, C.c_float, C.c_int
+_F16 = C.POINTER(C.c_float)
+_D16 = C.POINTER(C.c_double)
+
+# name: (restype, argtypes); every symbol the header declares is listed here
+# and checked by tests/test_abi.py.
+SIGNATURES = {
+    "ss_last_error": (C.c_char_p, []),
+    "ss_params_default": (_st, [C.POINTER(SSParams), _u32, _f, _f, _i32, _i32]),
+    "ss_grid_create": (_st, [C.POINTER(SSParams), C.POINTER(_p)]),
+    "ss_grid_destroy": (_st, [_p]),
+    "ss_grid_reset": (_st, [_p, _p]),
+    "ss_grid_set_intrinsic": (_st, [_p, _f, _f, _f, _f]),
+    "ss_integrate": (_st, [_p, _p, _p, _F16, _i32, _p]),
+    "ss_deintegrate": (_st, [_p, _p, _p, _F16, _i32, _p]),
+    "ss_integrate_fast": (_st, [_p, _p, _p, _F16, _i32, _i32, _p]),
+    "ss_raycast": (_st, [_p, _F16, _p, _p, _p]),
+    "ss_clean_memory": (_st, [_p, _p]),
+    "ss_grid_sync": (_st, [_p, _p]),
+    "ss_grid_block_count": (_st, [_p, _p, C.POINTER(_i32)]),
+    "ss_grid_counters": (_st, [_p, _p, C.POINTER(C.c_int64)]),
+    "ss_grid_export_blocks": (_st, [_p, _p, _i32, _p, _p, _p, _p, _p, C.POINTER(_i32)]),
+    "ss_grid_import_blocks": (_st, [_p, _p, _i32, _p, _p, _p, _p]),
+    "ss_depth_to_pcd": (_st, [_p, _i32, _i32, _f, _f, _f, _f, _p, _p]),
+    "ss_normals_from_pcd": (_st, [_p, _i32, _i32, _p, _p]),
+    "ss_kokkos_icp": (_st, [_p, _p, _i32, _i32, _f, _f, _f, _f, _D16, _D16, _i32, _D16,
+                            C.POINTER(C.c_float), _p]),
+}
+
+for _name, (_res, _args) in SIGNATURES.items():
+    _fn = getattr(lib, _name)
+    _fn.restype = _res
+    _fn.argtypes = _args
+
+
+def f32x16(m) -> C.Array:
+    import numpy as np
+    a = np.ascontiguousarray(np.asarray(m, dtype=np.float32).reshape(16))
+    return (C.c_float * 16)(*a.tolist())
+
+
+def f64x16(m) -> C.Array:
+    import numpy as np
+    a = np.ascontiguousarray(np.asarray(m, dtype=np.float64).reshape(16))
+    return (C.c_double * 16)(*a.tolist())

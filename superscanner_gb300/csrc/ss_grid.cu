@@ -1,0 +1,787 @@
+// ss_grid.cu — voxel-hash TSDF: block allocation (hash insertion),
+// integrate / deintegrate, clean, export / import, and their C-ABI.
+//
+// Reference: src/VoxelGrid/GPUVoxelGrid.{h,cpp} of Pandia3DPublic/SuperScanner.
+//
+// Layout in HBM (bucket b of a power-of-two table owns payload b, like
+// Kokkos::UnorderedMap::value_at):
+//   keys   u64[B]          prime-hash key, kEmptyKey, or kTombKey
+//   stamp  u64[B]          epoch of the last call that touched b | packed block coords
+//   vox32  float2[B][512]  (sdf, w)                       plain form, 8 B/voxel
+//   vox16  u32[B][512]     half(sdf/trunc) | u16(w) << 16 precision form, 4 B/voxel
+//   rgb    f32[B][3][512]  colour planes (optional)
+//   list   i32[B]          buckets touched by the current call (deduplicated)
+// One 8^3 block is 4 KB (plain) or 2 KB (precision) contiguous: a warp reads a
+// whole block as 16 fully coalesced 256/128-byte rows.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "ss_grid_impl.cuh"
+
+namespace ss {
+
+static thread_local std::string g_last_error;
+
+void set_last_error(const char *where, cudaError_t e) {
+    g_last_error = std::string(where) + ": " + cudaGetErrorString(e);
+}
+void set_last_error_text(const std::string &s) { g_last_error = s; }
+
+ss_status status_from_bits(int bits) {
+    if (bits & kStTableFull) return SS_ERR_TABLE_FULL;
+    if (bits & kStListOverflow) return SS_ERR_LIST_OVERFLOW;
+    if (bits & kStTimeout) return SS_ERR_TIMEOUT;
+    if (bits & kStRange) return SS_ERR_RANGE;
+    return SS_OK;
+}
+
+Mat34 mat34_from(const float E[16]) {
+    Mat34 m;
+    for (int k = 0; k < 12; k++) m.m[k] = E[k];
+    return m;
+}
+
+// Inverse of a 4x4 float matrix by cofactors in double, rounded to float
+// (GPUVoxelGrid.cpp:55 inverts with Eigen in float; Eigen is not available).
+void inverse4_rounded(const float Ef[16], float out[16]) {
+    double m[16], inv[16];
+    for (int k = 0; k < 16; k++) m[k] = Ef[k];
+    inv[0] = m[5] * m[10] * m[15] - m[5] * m[11] * m[14] - m[9] * m[6] * m[15] + m[9] * m[7] * m[14] +
+             m[13] * m[6] * m[11] - m[13] * m[7] * m[10];
+    inv[4] = -m[4] * m[10] * m[15] + m[4] * m[11] * m[14] + m[8] * m[6] * m[15] - m[8] * m[7] * m[14] -
+             m[12] * m[6] * m[11] + m[12] * m[7] * m[10];
+    inv[8] = m[4] * m[9] * m[15] - m[4] * m[11] * m[13] - m[8] * m[5] * m[15] + m[8] * m[7] * m[13] +
+             m[12] * m[5] * m[11] - m[12] * m[7] * m[9];
+    inv[12] = -m[4] * m[9] * m[14] + m[4] * m[10] * m[13] + m[8] * m[5] * m[14] - m[8] * m[6] * m[13] -
+              m[12] * m[5] * m[10] + m[12] * m[6] * m[9];
+    inv[1] = -m[1] * m[10] * m[15] + m[1] * m[11] * m[14] + m[9] * m[2] * m[15] - m[9] * m[3] * m[14] -
+             m[13] * m[2] * m[11] + m[13] * m[3] * m[10];
+    inv[5] = m[0] * m[10] * m[15] - m[0] * m[11] * m[14] - m[8] * m[2] * m[15] + m[8] * m[3] * m[14] +
+             m[12] * m[2] * m[11] - m[12] * m[3] * m[10];
+    inv[9] = -m[0] * m[9] * m[15] + m[0] * m[11] * m[13] + m[8] * m[1] * m[15] - m[8] * m[3] * m[13] -
+             m[12] * m[1] * m[11] + m[12] * m[3] * m[9];
+    inv[13] = m[0] * m[9] * m[14] - m[0] * m[10] * m[13] - m[8] * m[1] * m[14] + m[8] * m[2] * m[13] +
+              m[12] * m[1] * m[10] - m[12] * m[2] * m[9];
+    inv[2] = m[1] * m[6] * m[15] - m[1] * m[7] * m[14] - m[5] * m[2] * m[15] + m[5] * m[3] * m[14] +
+             m[13] * m[2] * m[7] - m[13] * m[3] * m[6];
+    inv[6] = -m[0] * m[6] * m[15] + m[0] * m[7] * m[14] + m[4] * m[2] * m[15] - m[4] * m[3] * m[14] -
+             m[12] * m[2] * m[7] + m[12] * m[3] * m[6];
+    inv[10] = m[0] * m[5] * m[15] - m[0] * m[7] * m[13] - m[4] * m[1] * m[15] + m[4] * m[3] * m[13] +
+              m[12] * m[1] * m[7] - m[12] * m[3] * m[5];
+    inv[14] = -m[0] * m[5] * m[14] + m[0] * m[6] * m[13] + m[4] * m[1] * m[14] - m[4] * m[2] * m[13] -
+              m[12] * m[1] * m[6] + m[12] * m[2] * m[5];
+    inv[3] = -m[1] * m[6] * m[11] + m[1] * m[7] * m[10] + m[5] * m[2] * m[11] - m[5] * m[3] * m[10] -
+             m[9] * m[2] * m[7] + m[9] * m[3] * m[6];
+    inv[7] = m[0] * m[6] * m[11] - m[0] * m[7] * m[10] - m[4] * m[2] * m[11] + m[4] * m[3] * m[10] +
+             m[8] * m[2] * m[7] - m[8] * m[3] * m[6];
+    inv[11] = -m[0] * m[5] * m[11] + m[0] * m[7] * m[9] + m[4] * m[1] * m[11] - m[4] * m[3] * m[9] -
+              m[8] * m[1] * m[7] + m[8] * m[3] * m[5];
+    inv[15] = m[0] * m[5] * m[10] - m[0] * m[6] * m[9] - m[4] * m[1] * m[10] + m[4] * m[2] * m[9] +
+              m[8] * m[1] * m[6] - m[8] * m[2] * m[5];
+    double det = m[0] * inv[0] + m[1] * inv[4] + m[2] * inv[8] + m[3] * inv[12];
+    for (int k = 0; k < 16; k++) out[k] = (float)(inv[k] / det);
+}
+
+int persistent_ctas(const ss_grid *g, int per_sm) { return g->num_sms * per_sm; }
+
+// ------------------------------------------------------------------ kernels
+
+__global__ void fill_u64_kernel(unsigned long long *p, size_t n, unsigned long long v) {
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x)
+        p[t] = v;
+}
+
+// Block collection (vbCollectionTag, GPUVoxelGrid.cpp:471-514) fused with
+// depthToPcdTag (GPUVoxelGrid.h:303-307). One thread per pixel, one warp per
+// 32 pixels of a row. Per candidate block: __match_any_sync groups the lanes
+// of equal block coordinates, the group leader runs the lock-free
+// find-or-insert, and a 64-bit atomicMax on the block stamp both deduplicates
+// the block for this call (first visitor of the epoch appends it; replaces
+// alreadyIntegrated + the O(capacity) "Reset booleans" pass) and fixes the
+// entry's coordinates canonically for aliased keys. Appends are aggregated
+// per warp (one atomicAdd per warp and candidate round).
+__global__ void __launch_bounds__(256) collect_kernel(GridView g, const uint16_t *__restrict__ depth, Mat34 E) {
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x;  // blockDim = (32, 8): one warp per row segment
+    const int j = blockIdx.x * 32 + threadIdx.x;
+    const int i = blockIdx.y * blockDim.y + threadIdx.y;
+    const uint32_t epoch = *(volatile uint32_t *)&g.ctr->epoch;
+
+    int lox = 0, loy = 0, loz = 0, nx = 0, ny = 0, nz = 0;
+    if (i < g.resi && j < g.resj) {
+        F3 p = get_point(g.in, i, j, depth_m(__ldg(depth + (size_t)i * g.resj + j)));
+        if (p.z > g.rmin) {
+            F3 pt = xform(E, p);
+            F3 t{g.trunc, g.trunc, g.trunc};
+            F3 lo = f3sub(pt, t), hi = f3add(pt, t);
+            lox = idx_rule(lo.x, g.vbl);
+            loy = idx_rule(lo.y, g.vbl);
+            loz = idx_rule(lo.z, g.vbl);
+            nx = idx_rule(hi.x, g.vbl) - lox + 1;
+            ny = idx_rule(hi.y, g.vbl) - loy + 1;
+            nz = idx_rule(hi.z, g.vbl) - loz + 1;
+            if (nx < 1 || ny < 1 || nz < 1 || nx > 8 || ny > 8 || nz > 8) {
+                atomicOr(&g.ctr->status, kStRange);  // non-finite pose or truncation > 3.5 blocks
+                nx = ny = nz = 0;
+            }
+        }
+    }
+    const int total = nx * ny * nz;
+    const unsigned lt = (1u << lane) - 1u;
+    for (int c = 0;; c++) {
+        bool act = c < total;
+        if (!__any_sync(FULL, act)) break;
+        unsigned long long packed = 0, key = 0;
+        if (act) {
+            // x outer, z inner (GPUVoxelGrid.cpp:485-489)
+            const int z = loz + c % nz, y = loy + (c / nz) % ny, x = lox + c / (nz * ny);
+            if (packable(x, y, z)) {
+                packed = pack_coords(x, y, z);
+                key = prime_hash(x, y, z);
+            } else {
+                atomicOr(&g.ctr->status, kStRange);
+                act = false;
+            }
+        }
+        const unsigned am = __ballot_sync(FULL, act);
+        bool append = false;
+        int bucket = -1;
+        if (act) {
+            const unsigned peers = __match_any_sync(am, packed);
+            if (__ffs(peers) - 1 == lane) {
+                bucket = table_find_or_insert(g, key);
+                if (bucket >= 0) {
+                    const unsigned long long mine = ((unsigned long long)epoch << kEpochShift) | packed;
+                    const unsigned long long old = atomicMax(g.stamp + bucket, mine);
+                    append = (uint32_t)(old >> kEpochShift) != epoch;
+                }
+            }
+        }
+        const unsigned ap = __ballot_sync(FULL, append);
+        if (ap) {
+            const int leader = __ffs(ap) - 1;
+            int base = 0;
+            if (lane == leader) base = atomicAdd(&g.ctr->list_count, __popc(ap));
+            base = __shfl_sync(FULL, base, leader);
+            if (append) {
+                const int idx = base + __popc(ap & lt);
+                if (idx <= (int)g.mask) g.list[idx] = bucket;
+                else atomicOr(&g.ctr->status, kStListOverflow);
+            }
+        }
+    }
+}
+
+// One voxel of integrationCore[Color]Tag / deIntegrationCore[Color]Tag
+// (GPUVoxelGrid.cpp:345-469, 516-550). Returns true when the voxel changes;
+// pixel (cori, corj) and the observed sdf come back through the references.
+template <bool kExact>
+__device__ __forceinline__ bool voxel_observe(const GridView &g, const uint16_t *__restrict__ depth, const Mat34 &E,
+                                              const Mat34 &Einv, const F3 &Ez, F3 vm, float &sdf, int &pix) {
+    F3 q;
+    float c0, c1;
+    if (kExact) {
+        q = xform(Einv, vm);
+        c0 = __fadd_rn(__fdiv_rn(__fmul_rn(q.y, g.in.fy), q.z), g.in.ci);  // getCoordinate (GPUVoxelGrid.h:234-237)
+        c1 = __fadd_rn(__fdiv_rn(__fmul_rn(q.x, g.in.fx), q.z), g.in.cj);
+    } else {
+        q.x = fmaf(vm.x, Einv.m[0], fmaf(vm.y, Einv.m[1], fmaf(vm.z, Einv.m[2], Einv.m[3])));
+        q.y = fmaf(vm.x, Einv.m[4], fmaf(vm.y, Einv.m[5], fmaf(vm.z, Einv.m[6], Einv.m[7])));
+        q.z = fmaf(vm.x, Einv.m[8], fmaf(vm.y, Einv.m[9], fmaf(vm.z, Einv.m[10], Einv.m[11])));
+        const float rz = __frcp_rn(q.z);
+        c0 = fmaf(q.y * g.in.fy, rz, g.in.ci);
+        c1 = fmaf(q.x * g.in.fx, rz, g.in.cj);
+    }
+    const int cori = __float2int_rz(c0);
+    const int corj = __float2int_rz(c1);
+    if (!(cori < g.resi && corj < g.resj && cori >= 0 && corj >= 0)) return false;
+    pix = cori * g.resj + corj;
+    const uint16_t dmm = __ldg(depth + pix);
+    F3 vpt;
+    if (kExact) {
+        vpt = get_point(g.in, cori, corj, depth_m(dmm));
+        if (!(vpt.z > g.rmin)) return false;
+        vpt = xform(E, vpt);
+        sdf = f3dot(f3sub(vpt, vm), Ez);
+    } else {
+        const float d = (float)dmm * 1.0e-3f;
+        if (!(d > g.rmin)) return false;
+        const float px = ((float)corj - g.in.cj) * __frcp_rn(g.in.fx) * d;
+        const float py = ((float)cori - g.in.ci) * __frcp_rn(g.in.fy) * d;
+        vpt.x = fmaf(px, E.m[0], fmaf(py, E.m[1], fmaf(d, E.m[2], E.m[3])));
+        vpt.y = fmaf(px, E.m[4], fmaf(py, E.m[5], fmaf(d, E.m[6], E.m[7])));
+        vpt.z = fmaf(px, E.m[8], fmaf(py, E.m[9], fmaf(d, E.m[10], E.m[11])));
+        sdf = (vpt.x - vm.x) * Ez.x + (vpt.y - vm.y) * Ez.y + (vpt.z - vm.z) * Ez.z;
+    }
+    return fabsf(sdf) < g.trunc;
+}
+
+// Running-average update of one voxel (sdf, weight) in FP32.
+template <bool kDeint, bool kExact>
+__device__ __forceinline__ void running_average(float &s, float &w, float obs, float max_weight) {
+    if (!kDeint) {
+        const float w1 = kExact ? __fadd_rn(w, 1.f) : w + 1.f;
+        s = kExact ? __fdiv_rn(__fadd_rn(__fmul_rn(s, w), obs), w1) : __fdividef(fmaf(s, w, obs), w1);
+        w = (max_weight > 0.f && w1 > max_weight) ? max_weight : w1;
+    } else {
+        if (w != 1.f) {
+            const float w1 = kExact ? __fsub_rn(w, 1.f) : w - 1.f;
+            s = kExact ? __fdiv_rn(__fsub_rn(__fmul_rn(s, w), obs), w1) : __fdividef(fmaf(s, w, -obs), w1);
+            w = w1;
+        } else {
+            w = 0.f;
+            s = 0.f;
+        }
+    }
+}
+
+template <bool kDeint, bool kExact>
+__device__ __forceinline__ void color_average(float &c, float w_old, float obs) {
+    if (!kDeint) {
+        c = kExact ? __fdiv_rn(__fadd_rn(__fmul_rn(c, w_old), obs), __fadd_rn(w_old, 1.f))
+                   : __fdividef(fmaf(c, w_old, obs), w_old + 1.f);
+    } else {
+        if (w_old != 1.f) {
+            c = kExact ? __fdiv_rn(__fsub_rn(__fmul_rn(c, w_old), obs), __fsub_rn(w_old, 1.f))
+                       : __fdividef(fmaf(c, w_old, -obs), w_old - 1.f);
+        } else {
+            c = 0.f;
+        }
+    }
+}
+
+// Integrate / deintegrate the touched blocks: one warp per block, 16 voxels
+// per lane (voxel v = lane + 32 r, so every load and store of the warp is one
+// contiguous row of the block). Persistent: warps stride over the device-side
+// list, so the launch needs no host read of the block count (the reference
+// copies it to the host every call, GPUVoxelGrid.cpp:62-63).
+// Voxel centres: the reference computes pzero + (k + 0.5) * vl in double and
+// rounds to float (GPUVoxelGrid.cpp:521); that double sum is exact for
+// |pzero| < 2^20 m, so one fmaf (single rounding of the exact value) gives the
+// identical float.
+template <int kStorage, bool kColor, bool kDeint, bool kExact>
+__global__ void __launch_bounds__(256) fuse_kernel(GridView g, const uint16_t *__restrict__ depth,
+                                                   const uint8_t *__restrict__ rgb, Mat34 E, Mat34 Einv, F3 Ez) {
+    const int lane = threadIdx.x & 31;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    const int n = *(volatile int *)&g.ctr->list_count;
+    const int k = lane & 7, l0 = lane >> 3;
+    const float inv_trunc = 1.0f / g.trunc;
+    for (int t = warp; t < n; t += nwarps) {
+        const int bucket = __ldg(g.list + t);
+        int bx, by, bz;
+        unpack_coords(__ldg(g.stamp + bucket), bx, by, bz);
+        // pzero = vbl * Kvec3f(x, y, z) (GPUVoxelGrid.cpp:501)
+        const float pzx = __fmul_rn(g.vbl, (float)bx), pzy = __fmul_rn(g.vbl, (float)by),
+                    pzz = __fmul_rn(g.vbl, (float)bz);
+        const float cx = __fmaf_rn((float)k + 0.5f, g.vl, pzx);
+#pragma unroll 4
+        for (int r = 0; r < 16; r++) {
+            const int l = l0 + 4 * (r & 1), m = r >> 1;
+            const int v = lane + 32 * r;  // == k + 8 l + 64 m
+            const F3 vm{cx, __fmaf_rn((float)l + 0.5f, g.vl, pzy), __fmaf_rn((float)m + 0.5f, g.vl, pzz)};
+            const size_t vi = (size_t)bucket * kBlockVoxels + v;
+            float s, w;
+            uint32_t word = 0;
+            if (kStorage == SS_STORAGE_F32) {
+                const float2 sw = g.vox32[vi];
+                s = sw.x;
+                w = sw.y;
+            } else {
+                word = g.vox16[vi];
+                s = __half2float(__ushort_as_half((unsigned short)(word & 0xffffu))) * g.trunc;
+                w = (float)(word >> 16);
+            }
+            float obs;
+            int pix;
+            if (!voxel_observe<kExact>(g, depth, E, Einv, Ez, vm, obs, pix)) continue;
+            if (kStorage == SS_STORAGE_F16 && kDeint && w == 0.f) continue;  // u16 weight cannot go negative
+            const float w_old = w;
+            running_average<kDeint, kExact>(s, w, obs, g.max_weight);
+            if (kStorage == SS_STORAGE_F32) {
+                g.vox32[vi] = make_float2(s, w);
+            } else {
+                const float wc = fminf(w, 65535.f);
+                const unsigned short hs = __half_as_ushort(__float2half_rn(s * inv_trunc));
+                g.vox16[vi] = (uint32_t)hs | ((uint32_t)wc << 16);
+            }
+            if (kColor) {
+                const uint8_t *c = rgb + (size_t)pix * 3;
+                float *pl = g.rgb + (size_t)bucket * 3 * kBlockVoxels + v;
+#pragma unroll
+                for (int ch = 0; ch < 3; ch++) {
+                    float cv = pl[ch * kBlockVoxels];
+                    color_average<kDeint, kExact>(cv, w_old, (float)c[ch]);
+                    pl[ch * kBlockVoxels] = cv;
+                }
+            }
+        }
+    }
+}
+
+// Ends a call: remembers and resets the list, advances the epoch.
+__global__ void finalize_kernel(Counters *ctr) {
+    const int n = ctr->list_count;
+    ctr->last_touched = n;
+    ctr->touched_total += (unsigned long long)n;
+    ctr->calls += 1ull;
+    ctr->list_count = 0;
+    ctr->epoch = ctr->epoch + 1u;
+}
+
+// Clears the epoch field of every stamp (run when the epoch counter wraps).
+__global__ void rebase_epoch_kernel(GridView g) {
+    for (size_t b = blockIdx.x * (size_t)blockDim.x + threadIdx.x; b <= g.mask; b += (size_t)gridDim.x * blockDim.x)
+        g.stamp[b] &= ((1ull << kEpochShift) - 1ull);
+    if (blockIdx.x == 0 && threadIdx.x == 0) g.ctr->epoch = 1u;
+}
+
+// cleanTag (GPUVoxelGrid.cpp:785-805): one warp per bucket; a block whose 512
+// weights are all zero is erased (tombstone) and its payload zeroed so the
+// bucket can be reused as a default-constructed block.
+template <int kStorage>
+__global__ void __launch_bounds__(256) clean_kernel(GridView g) {
+    const int lane = threadIdx.x & 31;
+    const size_t warp = (blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5;
+    const size_t nwarps = ((size_t)gridDim.x * blockDim.x) >> 5;
+    for (size_t b = warp; b <= g.mask; b += nwarps) {
+        const unsigned long long key = g.keys[b];
+        if (key == kEmptyKey || key == kTombKey) continue;
+        bool nz = false;
+        for (int r = 0; r < 16; r++) {
+            const size_t vi = b * kBlockVoxels + lane + 32 * r;
+            if (kStorage == SS_STORAGE_F32) nz |= g.vox32[vi].y != 0.f;
+            else nz |= (g.vox16[vi] >> 16) != 0u;
+        }
+        if (__any_sync(0xffffffffu, nz)) continue;
+        for (int r = 0; r < 16; r++) {
+            const size_t vi = b * kBlockVoxels + lane + 32 * r;
+            if (kStorage == SS_STORAGE_F32) g.vox32[vi] = make_float2(0.f, 0.f);
+            else g.vox16[vi] = 0u;
+            if (g.rgb) {
+                float *pl = g.rgb + b * 3 * kBlockVoxels + lane + 32 * r;
+                pl[0] = 0.f;
+                pl[kBlockVoxels] = 0.f;
+                pl[2 * kBlockVoxels] = 0.f;
+            }
+        }
+        if (lane == 0) {
+            g.stamp[b] = 0ull;
+            g.keys[b] = kTombKey;
+            atomicSub(&g.ctr->live_blocks, 1);
+        }
+    }
+}
+
+// Gathers the payload of listed buckets into compact FP32 arrays (export).
+template <int kStorage>
+__global__ void gather_blocks_kernel(GridView g, const int *__restrict__ buckets, int n, float *sdf, float *w,
+                                     float *rgb) {
+    const size_t total = (size_t)n * kBlockVoxels;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x) {
+        const int q = (int)(t / kBlockVoxels), v = (int)(t % kBlockVoxels);
+        const size_t vi = (size_t)buckets[q] * kBlockVoxels + v;
+        if (kStorage == SS_STORAGE_F32) {
+            const float2 sw = g.vox32[vi];
+            if (sdf) sdf[t] = sw.x;
+            if (w) w[t] = sw.y;
+        } else {
+            const uint32_t word = g.vox16[vi];
+            if (sdf) sdf[t] = __half2float(__ushort_as_half((unsigned short)(word & 0xffffu))) * g.trunc;
+            if (w) w[t] = (float)(word >> 16);
+        }
+        if (rgb && g.rgb) {
+            const float *pl = g.rgb + (size_t)buckets[q] * 3 * kBlockVoxels + v;
+            float *o = rgb + (size_t)q * 3 * kBlockVoxels + v;
+            o[0] = pl[0];
+            o[kBlockVoxels] = pl[kBlockVoxels];
+            o[2 * kBlockVoxels] = pl[2 * kBlockVoxels];
+        }
+    }
+}
+
+// Inserts imported blocks and writes their payload (import / resume).
+template <int kStorage>
+__global__ void import_blocks_kernel(GridView g, const int *__restrict__ coords, int n, const float *sdf,
+                                     const float *w, const float *rgb) {
+    const int lane = threadIdx.x & 31;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (int q = warp; q < n; q += nwarps) {
+        const int x = coords[q * 3], y = coords[q * 3 + 1], z = coords[q * 3 + 2];
+        int bucket = -1;
+        if (lane == 0) {
+            if (packable(x, y, z)) {
+                bucket = table_find_or_insert(g, prime_hash(x, y, z));
+                if (bucket >= 0) g.stamp[bucket] = pack_coords(x, y, z);
+            } else {
+                atomicOr(&g.ctr->status, kStRange);
+            }
+        }
+        bucket = __shfl_sync(0xffffffffu, bucket, 0);
+        if (bucket < 0) continue;
+        for (int r = 0; r < 16; r++) {
+            const int v = lane + 32 * r;
+            const size_t src = (size_t)q * kBlockVoxels + v, vi = (size_t)bucket * kBlockVoxels + v;
+            if (kStorage == SS_STORAGE_F32) {
+                g.vox32[vi] = make_float2(sdf[src], w[src]);
+            } else {
+                const float wc = fminf(fmaxf(w[src], 0.f), 65535.f);
+                g.vox16[vi] = (uint32_t)__half_as_ushort(__float2half_rn(sdf[src] / g.trunc)) | ((uint32_t)wc << 16);
+            }
+            if (rgb && g.rgb) {
+                float *pl = g.rgb + (size_t)bucket * 3 * kBlockVoxels + v;
+                const float *s = rgb + (size_t)q * 3 * kBlockVoxels + v;
+                pl[0] = s[0];
+                pl[kBlockVoxels] = s[kBlockVoxels];
+                pl[2 * kBlockVoxels] = s[2 * kBlockVoxels];
+            }
+        }
+    }
+}
+
+// --------------------------------------------------------------- launchers
+
+static ss_status launch_fuse(ss_grid *g, const uint16_t *depth, const uint8_t *rgb, const float extr[16],
+                             bool color, bool deint, bool exact, cudaStream_t s) {
+    float Einv16[16];
+    inverse4_rounded(extr, Einv16);
+    const Mat34 E = mat34_from(extr), Einv = mat34_from(Einv16);
+    // Ez: normalized third column of extr (GPUVoxelGrid.cpp:52-53), Kvec3f::normalize in float
+    const float ex = extr[2], ey = extr[6], ez = extr[10];
+    volatile float len = std::sqrt(ex * ex + ey * ey + ez * ez);
+    const F3 Ez{ex / len, ey / len, ez / len};
+
+    if (g->host_epoch >= kEpochMax) {
+        rebase_epoch_kernel<<<persistent_ctas(g, 4), 256, 0, s>>>(g->v);
+        SS_LAUNCH_CHECK();
+        g->host_epoch = 1;
+    }
+    const dim3 cblk(32, 8), cgrid((g->p.resj + 31) / 32, (g->p.resi + 7) / 8);
+    collect_kernel<<<cgrid, cblk, 0, s>>>(g->v, depth, E);
+    SS_LAUNCH_CHECK();
+    const int ctas = persistent_ctas(g, 8);
+#define SS_FUSE(ST, C, D, X) fuse_kernel<ST, C, D, X><<<ctas, 256, 0, s>>>(g->v, depth, rgb, E, Einv, Ez)
+#define SS_FUSE_X(ST, C, D) \
+    do {                    \
+        if (exact) SS_FUSE(ST, C, D, true); else SS_FUSE(ST, C, D, false); \
+    } while (0)
+#define SS_FUSE_D(ST, C) \
+    do {                 \
+        if (deint) SS_FUSE_X(ST, C, true); else SS_FUSE_X(ST, C, false); \
+    } while (0)
+    if (g->p.storage == SS_STORAGE_F32) {
+        if (color) SS_FUSE_D(SS_STORAGE_F32, true); else SS_FUSE_D(SS_STORAGE_F32, false);
+    } else {
+        if (color) SS_FUSE_D(SS_STORAGE_F16, true); else SS_FUSE_D(SS_STORAGE_F16, false);
+    }
+#undef SS_FUSE_D
+#undef SS_FUSE_X
+#undef SS_FUSE
+    SS_LAUNCH_CHECK();
+    finalize_kernel<<<1, 1, 0, s>>>(g->v.ctr);
+    SS_LAUNCH_CHECK();
+    g->host_epoch++;
+    return SS_OK;
+}
+
+}  // namespace ss
+
+using namespace ss;
+
+extern "C" {
+
+const char *ss_last_error(void) { return g_last_error.c_str(); }
+
+ss_status ss_params_default(ss_params *p, uint32_t capacity_voxels, float trunc, float voxel_length, int32_t resi,
+                            int32_t resj) {
+    if (!p || voxel_length <= 0.f || trunc <= 0.f || resi <= 0 || resj <= 0) return SS_ERR_ARG;
+    uint32_t blocks = capacity_voxels / kBlockVoxels;
+    uint32_t b = 1024;
+    while (b < blocks && b < (1u << 30)) b <<= 1;
+    p->voxel_length = voxel_length;
+    p->truncation = trunc;
+    p->resi = resi;
+    p->resj = resj;
+    p->hash_buckets = b;
+    p->storage = SS_STORAGE_F32;
+    p->with_color = 1;
+    p->max_weight = 0.f;
+    p->rmin = 0.2f;
+    p->d_max = 10.0f;
+    return SS_OK;
+}
+
+ss_status ss_grid_reset(ss_grid *g, ss_stream_t stream) {
+    if (!g) return SS_ERR_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    const size_t B = (size_t)g->p.hash_buckets;
+    fill_u64_kernel<<<persistent_ctas(g, 4), 256, 0, s>>>(g->v.keys, B, kEmptyKey);
+    SS_LAUNCH_CHECK();
+    SS_CUDA_TRY(cudaMemsetAsync(g->v.stamp, 0, B * 8, s));
+    if (g->v.vox32) SS_CUDA_TRY(cudaMemsetAsync(g->v.vox32, 0, B * kBlockVoxels * sizeof(float2), s));
+    if (g->v.vox16) SS_CUDA_TRY(cudaMemsetAsync(g->v.vox16, 0, B * kBlockVoxels * sizeof(uint32_t), s));
+    if (g->v.rgb) SS_CUDA_TRY(cudaMemsetAsync(g->v.rgb, 0, B * 3 * kBlockVoxels * sizeof(float), s));
+    Counters c;
+    std::memset(&c, 0, sizeof(c));
+    c.epoch = 1;
+    SS_CUDA_TRY(cudaMemcpyAsync(g->v.ctr, &c, sizeof(c), cudaMemcpyHostToDevice, s));
+    SS_CUDA_TRY(cudaStreamSynchronize(s));
+    g->host_epoch = 1;
+    return SS_OK;
+}
+
+ss_status ss_grid_create(const ss_params *p, ss_grid **out) {
+    if (!p || !out) return SS_ERR_ARG;
+    *out = nullptr;
+    if (p->hash_buckets < 32 || (p->hash_buckets & (p->hash_buckets - 1)) != 0 || p->hash_buckets > (1u << 30))
+        return SS_ERR_ARG;
+    if (!(p->voxel_length > 0.f) || !(p->truncation > 0.f) || p->resi <= 0 || p->resj <= 0) return SS_ERR_ARG;
+    if (p->storage != SS_STORAGE_F32 && p->storage != SS_STORAGE_F16) return SS_ERR_ARG;
+    ss_grid *g = new ss_grid;
+    g->p = *p;
+    std::memset(&g->v, 0, sizeof(g->v));
+    SS_CUDA_TRY(cudaGetDevice(&g->device));
+    SS_CUDA_TRY(cudaDeviceGetAttribute(&g->num_sms, cudaDevAttrMultiProcessorCount, g->device));
+    const size_t B = (size_t)p->hash_buckets;
+    bool ok = cudaMalloc(&g->v.keys, B * 8) == cudaSuccess && cudaMalloc(&g->v.stamp, B * 8) == cudaSuccess &&
+              cudaMalloc(&g->v.list, B * 4) == cudaSuccess && cudaMalloc(&g->v.ctr, sizeof(Counters)) == cudaSuccess;
+    if (ok && p->storage == SS_STORAGE_F32)
+        ok = cudaMalloc(&g->v.vox32, B * kBlockVoxels * sizeof(float2)) == cudaSuccess;
+    if (ok && p->storage == SS_STORAGE_F16)
+        ok = cudaMalloc(&g->v.vox16, B * kBlockVoxels * sizeof(uint32_t)) == cudaSuccess;
+    if (ok && p->with_color) ok = cudaMalloc(&g->v.rgb, B * 3 * kBlockVoxels * sizeof(float)) == cudaSuccess;
+    if (!ok) {
+        cudaGetLastError();
+        ss_grid_destroy(g);
+        set_last_error_text("ss_grid_create: device allocation failed");
+        return SS_ERR_NOMEM;
+    }
+    g->v.mask = p->hash_buckets - 1;
+    g->v.vl = p->voxel_length;
+    g->v.vbl = kEdge * p->voxel_length;  // GPUVoxelGrid.cpp:15
+    g->v.trunc = p->truncation;
+    g->v.rmin = p->rmin;
+    g->v.d_max = p->d_max;
+    g->v.max_weight = p->max_weight;
+    g->v.resi = p->resi;
+    g->v.resj = p->resj;
+    ss_status st = ss_grid_reset(g, nullptr);
+    if (st != SS_OK) {
+        ss_grid_destroy(g);
+        return st;
+    }
+    *out = g;
+    return SS_OK;
+}
+
+ss_status ss_grid_destroy(ss_grid *g) {
+    if (!g) return SS_ERR_ARG;
+    cudaFree(g->v.keys);
+    cudaFree(g->v.stamp);
+    cudaFree(g->v.list);
+    cudaFree(g->v.ctr);
+    cudaFree(g->v.vox32);
+    cudaFree(g->v.vox16);
+    cudaFree(g->v.rgb);
+    delete g;
+    return SS_OK;
+}
+
+ss_status ss_grid_set_intrinsic(ss_grid *g, float fx, float fy, float cx, float cy) {
+    if (!g || !(fx != 0.f) || !(fy != 0.f)) return SS_ERR_ARG;
+    g->fx = fx;
+    g->fy = fy;
+    g->cx = cx;
+    g->cy = cy;
+    g->v.in.fx = fx;
+    g->v.in.fy = fy;
+    g->v.in.ci = (float)g->p.resi - cy;  // ci = resi - cy (GPUVoxelGrid.cpp:259)
+    g->v.in.cj = cx;                     // cj = cx (GPUVoxelGrid.cpp:260)
+    g->intr_set = true;
+    return SS_OK;
+}
+
+static ss_status fuse_entry(ss_grid *g, const uint16_t *depth, const uint8_t *rgb, const float extr[16],
+                            int32_t with_color, bool deint, ss_stream_t s) {
+    if (!g || !depth || !extr) return SS_ERR_ARG;
+    if (!g->intr_set) return SS_ERR_STATE;
+    const bool color = with_color != 0;
+    if (color && (!rgb || !g->v.rgb)) return SS_ERR_ARG;
+    for (int k = 0; k < 16; k++)
+        if (!std::isfinite(extr[k])) return SS_ERR_ARG;
+    return launch_fuse(g, depth, rgb, extr, color, deint, /*exact=*/true, (cudaStream_t)s);
+}
+
+ss_status ss_integrate(ss_grid *g, const uint16_t *depth, const uint8_t *rgb, const float extr[16],
+                       int32_t with_color, ss_stream_t s) {
+    return fuse_entry(g, depth, rgb, extr, with_color, false, s);
+}
+
+ss_status ss_deintegrate(ss_grid *g, const uint16_t *depth, const uint8_t *rgb, const float extr[16],
+                         int32_t with_color, ss_stream_t s) {
+    return fuse_entry(g, depth, rgb, extr, with_color, true, s);
+}
+
+// Variant used by the per-frame pipeline: same kernels, FMA-contracted fast
+// arithmetic in the voxel update (block allocation stays reference-exact).
+ss_status ss_integrate_fast(ss_grid *g, const uint16_t *depth, const uint8_t *rgb, const float extr[16],
+                            int32_t with_color, int32_t deint, ss_stream_t s) {
+    if (!g || !depth || !extr) return SS_ERR_ARG;
+    if (!g->intr_set) return SS_ERR_STATE;
+    const bool color = with_color != 0;
+    if (color && (!rgb || !g->v.rgb)) return SS_ERR_ARG;
+    return launch_fuse(g, depth, rgb, extr, color, deint != 0, /*exact=*/false, (cudaStream_t)s);
+}
+
+ss_status ss_clean_memory(ss_grid *g, ss_stream_t stream) {
+    if (!g) return SS_ERR_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (g->p.storage == SS_STORAGE_F32) clean_kernel<SS_STORAGE_F32><<<persistent_ctas(g, 8), 256, 0, s>>>(g->v);
+    else clean_kernel<SS_STORAGE_F16><<<persistent_ctas(g, 8), 256, 0, s>>>(g->v);
+    SS_LAUNCH_CHECK();
+    return SS_OK;
+}
+
+ss_status ss_grid_sync(ss_grid *g, ss_stream_t stream) {
+    if (!g) return SS_ERR_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    SS_CUDA_TRY(cudaStreamSynchronize(s));
+    int bits = 0;
+    SS_CUDA_TRY(cudaMemcpy(&bits, &g->v.ctr->status, sizeof(int), cudaMemcpyDeviceToHost));
+    if (bits) {
+        int zero = 0;
+        SS_CUDA_TRY(cudaMemcpy(&g->v.ctr->status, &zero, sizeof(int), cudaMemcpyHostToDevice));
+    }
+    return status_from_bits(bits);
+}
+
+ss_status ss_grid_block_count(ss_grid *g, ss_stream_t stream, int32_t *count) {
+    if (!g || !count) return SS_ERR_ARG;
+    SS_CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
+    SS_CUDA_TRY(cudaMemcpy(count, &g->v.ctr->live_blocks, sizeof(int), cudaMemcpyDeviceToHost));
+    return SS_OK;
+}
+
+// Host copy of the counters (last_touched, touched_total, calls, live blocks).
+ss_status ss_grid_counters(ss_grid *g, ss_stream_t stream, int64_t out[6]) {
+    if (!g || !out) return SS_ERR_ARG;
+    SS_CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
+    Counters c;
+    SS_CUDA_TRY(cudaMemcpy(&c, g->v.ctr, sizeof(c), cudaMemcpyDeviceToHost));
+    out[0] = c.live_blocks;
+    out[1] = c.last_touched;
+    out[2] = (int64_t)c.touched_total;
+    out[3] = (int64_t)c.calls;
+    out[4] = c.status;
+    out[5] = c.epoch;
+    return SS_OK;
+}
+
+ss_status ss_grid_export_blocks(ss_grid *g, ss_stream_t stream, int32_t max_blocks, uint64_t *keys, int32_t *coords,
+                                float *sdf, float *weight, float *rgb, int32_t *n_out) {
+    if (!g || !n_out || max_blocks < 0) return SS_ERR_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    SS_CUDA_TRY(cudaStreamSynchronize(s));
+    const size_t B = (size_t)g->p.hash_buckets;
+    std::vector<unsigned long long> hk(B), hs(B);
+    SS_CUDA_TRY(cudaMemcpy(hk.data(), g->v.keys, B * 8, cudaMemcpyDeviceToHost));
+    SS_CUDA_TRY(cudaMemcpy(hs.data(), g->v.stamp, B * 8, cudaMemcpyDeviceToHost));
+    std::vector<std::pair<unsigned long long, int>> items;
+    for (size_t b = 0; b < B; b++)
+        if (hk[b] != kEmptyKey && hk[b] != kTombKey) items.push_back({hk[b], (int)b});
+    std::sort(items.begin(), items.end());
+    const int n = (int)std::min<size_t>(items.size(), (size_t)max_blocks);
+    *n_out = (int)items.size();
+    if (n == 0) return SS_OK;
+    std::vector<int> buckets(n);
+    for (int q = 0; q < n; q++) {
+        buckets[q] = items[q].second;
+        if (keys) keys[q] = items[q].first;
+        if (coords) {
+            const unsigned long long p = hs[items[q].second] & ((1ull << kEpochShift) - 1ull);
+            coords[q * 3 + 0] = (int)((p >> 28) & 0x3fff) - kCoordBias;
+            coords[q * 3 + 1] = (int)((p >> 14) & 0x3fff) - kCoordBias;
+            coords[q * 3 + 2] = (int)(p & 0x3fff) - kCoordBias;
+        }
+    }
+    if (!sdf && !weight && !rgb) return SS_OK;
+    int *d_buckets = nullptr;
+    float *d_sdf = nullptr, *d_w = nullptr, *d_rgb = nullptr;
+    const size_t nv = (size_t)n * kBlockVoxels;
+    ss_status st = SS_OK;
+    if (cudaMalloc(&d_buckets, n * sizeof(int)) != cudaSuccess || cudaMalloc(&d_sdf, nv * 4) != cudaSuccess ||
+        cudaMalloc(&d_w, nv * 4) != cudaSuccess || (rgb && g->v.rgb && cudaMalloc(&d_rgb, nv * 12) != cudaSuccess)) {
+        cudaGetLastError();
+        st = SS_ERR_NOMEM;
+    }
+    if (st == SS_OK) {
+        cudaMemcpy(d_buckets, buckets.data(), n * sizeof(int), cudaMemcpyHostToDevice);
+        if (g->p.storage == SS_STORAGE_F32)
+            gather_blocks_kernel<SS_STORAGE_F32><<<persistent_ctas(g, 4), 256, 0, s>>>(g->v, d_buckets, n, d_sdf, d_w, d_rgb);
+        else
+            gather_blocks_kernel<SS_STORAGE_F16><<<persistent_ctas(g, 4), 256, 0, s>>>(g->v, d_buckets, n, d_sdf, d_w, d_rgb);
+        cudaError_t e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) {
+            set_last_error("gather_blocks", e);
+            st = SS_ERR_CUDA;
+        }
+    }
+    if (st == SS_OK) {
+        if (sdf) cudaMemcpy(sdf, d_sdf, nv * 4, cudaMemcpyDeviceToHost);
+        if (weight) cudaMemcpy(weight, d_w, nv * 4, cudaMemcpyDeviceToHost);
+        if (rgb) {
+            if (d_rgb) cudaMemcpy(rgb, d_rgb, nv * 12, cudaMemcpyDeviceToHost);
+            else std::memset(rgb, 0, nv * 12);
+        }
+    }
+    cudaFree(d_buckets);
+    cudaFree(d_sdf);
+    cudaFree(d_w);
+    cudaFree(d_rgb);
+    return st;
+}
+
+ss_status ss_grid_import_blocks(ss_grid *g, ss_stream_t stream, int32_t n, const int32_t *coords, const float *sdf,
+                                const float *weight, const float *rgb) {
+    if (!g || n < 0 || (n > 0 && (!coords || !sdf || !weight))) return SS_ERR_ARG;
+    if (n == 0) return SS_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    const size_t nv = (size_t)n * kBlockVoxels;
+    int *d_c = nullptr;
+    float *d_s = nullptr, *d_w = nullptr, *d_rgb = nullptr;
+    ss_status st = SS_OK;
+    if (cudaMalloc(&d_c, (size_t)n * 12) != cudaSuccess || cudaMalloc(&d_s, nv * 4) != cudaSuccess ||
+        cudaMalloc(&d_w, nv * 4) != cudaSuccess || (rgb && cudaMalloc(&d_rgb, nv * 12) != cudaSuccess)) {
+        cudaGetLastError();
+        st = SS_ERR_NOMEM;
+    }
+    if (st == SS_OK) {
+        cudaMemcpy(d_c, coords, (size_t)n * 12, cudaMemcpyHostToDevice);
+        cudaMemcpy(d_s, sdf, nv * 4, cudaMemcpyHostToDevice);
+        cudaMemcpy(d_w, weight, nv * 4, cudaMemcpyHostToDevice);
+        if (rgb) cudaMemcpy(d_rgb, rgb, nv * 12, cudaMemcpyHostToDevice);
+        if (g->p.storage == SS_STORAGE_F32)
+            import_blocks_kernel<SS_STORAGE_F32><<<persistent_ctas(g, 4), 256, 0, s>>>(g->v, d_c, n, d_s, d_w, d_rgb);
+        else
+            import_blocks_kernel<SS_STORAGE_F16><<<persistent_ctas(g, 4), 256, 0, s>>>(g->v, d_c, n, d_s, d_w, d_rgb);
+        cudaError_t e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) {
+            set_last_error("import_blocks", e);
+            st = SS_ERR_CUDA;
+        }
+    }
+    cudaFree(d_c);
+    cudaFree(d_s);
+    cudaFree(d_w);
+    cudaFree(d_rgb);
+    if (st != SS_OK) return st;
+    return ss_grid_sync(g, stream);
+}
+
+}  // extern "C"

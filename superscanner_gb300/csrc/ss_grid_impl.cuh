@@ -1,0 +1,54 @@
+// ss_grid_impl.cuh — host-side grid object shared by the translation units.
+#pragma once
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+
+#include "ss_internal.cuh"
+
+struct ss_grid {
+    ss_params p;
+    ss::GridView v;
+    bool intr_set = false;
+    float fx = 0, fy = 0, cx = 0, cy = 0;
+    uint32_t host_epoch = 1;  // mirror of Counters::epoch for wrap handling
+    int device = 0;
+    int num_sms = 0;
+};
+
+namespace ss {
+
+// Last CUDA error text of this thread (ss_last_error()).
+void set_last_error(const char *where, cudaError_t e);
+void set_last_error_text(const std::string &s);
+
+// Maps device status bits to the ABI status (first error wins).
+ss_status status_from_bits(int bits);
+
+#define SS_CUDA_TRY(call)                                  \
+    do {                                                   \
+        cudaError_t _e = (call);                           \
+        if (_e != cudaSuccess) {                           \
+            ::ss::set_last_error(#call, _e);               \
+            return SS_ERR_CUDA;                            \
+        }                                                  \
+    } while (0)
+
+#define SS_LAUNCH_CHECK()                                  \
+    do {                                                   \
+        cudaError_t _e = cudaGetLastError();               \
+        if (_e != cudaSuccess) {                           \
+            ::ss::set_last_error("kernel launch", _e);     \
+            return SS_ERR_CUDA;                            \
+        }                                                  \
+    } while (0)
+
+Mat34 mat34_from(const float E[16]);
+void inverse4_rounded(const float E[16], float out[16]);
+
+// Blocks of persistent launches (multiple of the SM count).
+int persistent_ctas(const ss_grid *g, int per_sm);
+
+}  // namespace ss

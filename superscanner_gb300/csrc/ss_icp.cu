@@ -1,0 +1,431 @@
+// ss_icp.cu — CreatePcdFromDepthView, CalculateNormalsFromPCDView and
+// kokkosICP (src/utils/imageutil.cpp:89-157, src/postprocessing/kokkosICP.cpp:25-210).
+//
+// The reference runs the 10x10-window correspondence search on the GPU and
+// then copies both point clouds and the correspondences to the host every
+// iteration for centroids, RMSE, H and an Eigen JacobiSVD. Here one kernel
+// per iteration does the search, reduces the 18 sums in double
+// (warp shuffles, then one slot per CTA) and the last CTA to finish reduces
+// the CTA slots in a fixed order, runs a one-sided Jacobi SVD of H in double
+// and writes the next Txy, so the 10 iterations run without a host round trip.
+#include <mutex>
+
+#include "ss_grid_impl.cuh"
+
+namespace ss {
+
+// ------------------------------------------------------------- pcd/normals
+__global__ void depth_to_pcd_kernel(const uint16_t *__restrict__ depth, int rows, int cols, Intr in,
+                                    float *__restrict__ pcd) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y;
+    if (j >= cols || i >= rows) return;
+    const size_t p = (size_t)i * cols + j;
+    const F3 v = get_point(in, i, j, depth_m(__ldg(depth + p)));
+    pcd[p * 3 + 0] = v.x;
+    pcd[p * 3 + 1] = v.y;
+    pcd[p * 3 + 2] = v.z;
+}
+
+__device__ __forceinline__ F3 ld3(const float *__restrict__ a, size_t p) {
+    return {__ldg(a + p * 3), __ldg(a + p * 3 + 1), __ldg(a + p * 3 + 2)};
+}
+
+// Both reference launches in one: default (0,0,1) (imageutil.cpp:123-126),
+// interior pixels with five valid depths get the normalized sum of the four
+// neighbour cross products (:128-154).
+__global__ void normals_kernel(const float *__restrict__ pcd, int rows, int cols, float *__restrict__ out) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y;
+    if (j >= cols || i >= rows) return;
+    const size_t p = (size_t)i * cols + j;
+    F3 n{0.f, 0.f, 1.f};
+    if (i >= 1 && i < rows - 1 && j >= 1 && j < cols - 1) {
+        const F3 c = ld3(pcd, p), up = ld3(pcd, p + cols), dn = ld3(pcd, p - cols), rt = ld3(pcd, p + 1),
+                 lf = ld3(pcd, p - 1);
+        if (c.z != 0 && up.z != 0 && dn.z != 0 && rt.z != 0 && lf.z != 0) {
+            // pcd(i+1,j) = up, pcd(i-1,j) = dn, pcd(i,j+1) = rt, pcd(i,j-1) = lf
+            const F3 n1 = f3cross(f3sub(up, c), f3sub(rt, c));
+            const F3 n2 = f3cross(f3sub(lf, c), f3sub(up, c));
+            const F3 n3 = f3cross(f3sub(rt, c), f3sub(dn, c));
+            const F3 n4 = f3cross(f3sub(dn, c), f3sub(lf, c));
+            n = f3normalized(f3add(f3add(f3add(n1, n2), n3), n4));
+        }
+    }
+    out[p * 3 + 0] = n.x;
+    out[p * 3 + 1] = n.y;
+    out[p * 3 + 2] = n.z;
+}
+
+// ----------------------------------------------------------------- kokkosICP
+constexpr int kIcpSums = 18;  // n_cors, sum x (3), sum y (3), sum x y^T (9), sum tmp^2, n_x
+constexpr int kIcpIters = 10; // n_it (kokkosICP.cpp:54)
+
+struct IcpState {
+    float Txy[16];      // float copy used by the search (EigentoKmat4f(Txy.cast<float>()))
+    double Txy_d[16];   // double Txy_eigen
+    double best[16];    // bestTxy_eigen
+    float lowest;       // lowestRSME
+    float best_fitness;
+    int ticket;
+    int iteration;
+    double stats[kIcpIters * 4];
+};
+
+__device__ void svd3_jacobi(const double *H, double *U, double *S, double *V) {
+    double A[9];
+    for (int k = 0; k < 9; k++) A[k] = H[k];
+    for (int k = 0; k < 9; k++) V[k] = (k % 4 == 0) ? 1.0 : 0.0;
+    for (int sweep = 0; sweep < 60; sweep++) {
+        bool rotated = false;
+        for (int p = 0; p < 2; p++)
+            for (int q = p + 1; q < 3; q++) {
+                double alpha = 0, beta = 0, gamma = 0;
+                for (int i = 0; i < 3; i++) {
+                    alpha += A[i * 3 + p] * A[i * 3 + p];
+                    beta += A[i * 3 + q] * A[i * 3 + q];
+                    gamma += A[i * 3 + p] * A[i * 3 + q];
+                }
+                if (gamma == 0.0 || fabs(gamma) <= 1e-15 * sqrt(alpha * beta)) continue;
+                rotated = true;
+                const double zeta = (beta - alpha) / (2.0 * gamma);
+                const double t = (zeta >= 0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+                const double c = 1.0 / sqrt(1.0 + t * t), s = c * t;
+                for (int i = 0; i < 3; i++) {
+                    const double ap = A[i * 3 + p], aq = A[i * 3 + q];
+                    A[i * 3 + p] = c * ap - s * aq;
+                    A[i * 3 + q] = s * ap + c * aq;
+                    const double vp = V[i * 3 + p], vq = V[i * 3 + q];
+                    V[i * 3 + p] = c * vp - s * vq;
+                    V[i * 3 + q] = s * vp + c * vq;
+                }
+            }
+        if (!rotated) break;
+    }
+    int zero_col = -1;
+    for (int j = 0; j < 3; j++) {
+        const double n = sqrt(A[j] * A[j] + A[3 + j] * A[3 + j] + A[6 + j] * A[6 + j]);
+        S[j] = n;
+        if (n > 1e-300) {
+            for (int i = 0; i < 3; i++) U[i * 3 + j] = A[i * 3 + j] / n;
+        } else {
+            zero_col = j;
+            for (int i = 0; i < 3; i++) U[i * 3 + j] = 0;
+        }
+    }
+    if (zero_col >= 0) {
+        const int a = (zero_col + 1) % 3, b = (zero_col + 2) % 3;
+        const double ua[3] = {U[a], U[3 + a], U[6 + a]}, ub[3] = {U[b], U[3 + b], U[6 + b]};
+        U[zero_col] = ua[1] * ub[2] - ua[2] * ub[1];
+        U[3 + zero_col] = ua[2] * ub[0] - ua[0] * ub[2];
+        U[6 + zero_col] = ua[0] * ub[1] - ua[1] * ub[0];
+    }
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// One kokkosICP iteration: Closest Point Kernel (kokkosICP.cpp:69-115) fused
+// with the host sums (:121-171) and, in the last CTA, the SVD update (:173-185).
+template <int kType>
+__global__ void __launch_bounds__(256) icp_ref_iter_kernel(const float *__restrict__ xp, const float *__restrict__ yp,
+                                                           const float *__restrict__ yn, int rows, int cols, Intr in,
+                                                           IcpState *st, double *partials) {
+    __shared__ double red[8][kIcpSums];
+    __shared__ bool last;
+    const int n_search = 5;
+    const float max_dist = 0.075f;
+    Mat34 T;
+#pragma unroll
+    for (int k = 0; k < 12; k++) T.m[k] = st->Txy[k];
+    double Td[12];
+#pragma unroll
+    for (int k = 0; k < 12; k++) Td[k] = st->Txy_d[k];
+
+    double acc[kIcpSums];
+#pragma unroll
+    for (int k = 0; k < kIcpSums; k++) acc[k] = 0.0;
+
+    const size_t npix = (size_t)rows * cols;
+    for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < npix; p += (size_t)gridDim.x * blockDim.x) {
+        const F3 x = ld3(xp, p);
+        if (x.z == 0) continue;
+        acc[17] += 1.0;  // n_pointsinX
+        const F3 px = xform(T, x);
+        const float c0 = __fadd_rn(__fdiv_rn(__fmul_rn(px.y, in.fy), px.z), in.ci);
+        const float c1 = __fadd_rn(__fdiv_rn(__fmul_rn(px.x, in.fx), px.z), in.cj);
+        const int ci = __float2int_rz(c0), cj = __float2int_rz(c1);
+        if (!(ci > n_search && ci < rows - n_search && cj > n_search && cj < cols - n_search)) continue;
+        float smallest = 1e6f;
+        F3 best{0.f, 0.f, 0.f};
+        for (int k = ci - n_search; k < ci + n_search; k++) {
+            for (int l = cj - n_search; l < cj + n_search; l++) {
+                const size_t q = (size_t)k * cols + l;
+                const F3 py = ld3(yp, q);
+                if (kType == SS_ICP_POINT_TO_POINT) {
+                    if (py.z != 0) {
+                        const float dist = f3len(f3sub(py, px));
+                        if (dist < smallest && dist < max_dist) {
+                            smallest = dist;
+                            best = py;
+                        }
+                    }
+                } else {
+                    const F3 nn = ld3(yn, q);
+                    if (py.z != 0 && nn.x != 0) {
+                        const float d = f3dot(f3sub(py, px), nn);
+                        const float dist = fabsf(d);
+                        if (dist < smallest && dist < max_dist) {
+                            smallest = dist;
+                            best = f3add(px, f3smul(d, nn));
+                        }
+                    }
+                }
+            }
+        }
+        if (best.z == 0) continue;  // x_nearest(i, j).z == 0: no correspondence
+        const double a0 = x.x, a1 = x.y, a2 = x.z, b0 = best.x, b1 = best.y, b2 = best.z;
+        acc[0] += 1.0;
+        acc[1] += a0; acc[2] += a1; acc[3] += a2;
+        acc[4] += b0; acc[5] += b1; acc[6] += b2;
+        acc[7] += a0 * b0;  acc[8] += a0 * b1;  acc[9] += a0 * b2;
+        acc[10] += a1 * b0; acc[11] += a1 * b1; acc[12] += a1 * b2;
+        acc[13] += a2 * b0; acc[14] += a2 * b1; acc[15] += a2 * b2;
+        // RMSE term: || x_nearest4 - Txy_eigen * x4 || in double, squared in float (kokkosICP.cpp:137-138)
+        const double e0 = b0 - (Td[0] * a0 + Td[1] * a1 + Td[2] * a2 + Td[3]);
+        const double e1 = b1 - (Td[4] * a0 + Td[5] * a1 + Td[6] * a2 + Td[7]);
+        const double e2 = b2 - (Td[8] * a0 + Td[9] * a1 + Td[10] * a2 + Td[11]);
+        const float tmp = (float)sqrt(e0 * e0 + e1 * e1 + e2 * e2);
+        acc[16] += (double)(tmp * tmp);
+    }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < kIcpSums; k++) {
+        const double v = warp_sum(acc[k]);
+        if (lane == 0) red[wid][k] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < kIcpSums) {
+        double s = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) s += red[w][threadIdx.x];
+        partials[(size_t)blockIdx.x * kIcpSums + threadIdx.x] = s;
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(&st->ticket, 1) == (int)gridDim.x - 1;
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    __shared__ double tot[kIcpSums];
+    if (threadIdx.x < kIcpSums) {
+        double s = 0.0;
+        for (unsigned b = 0; b < gridDim.x; b++) s += *((volatile double *)partials + (size_t)b * kIcpSums + threadIdx.x);
+        tot[threadIdx.x] = s;
+    }
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    const double n = tot[0];
+    const double cx[3] = {tot[1] / n, tot[2] / n, tot[3] / n}, cy[3] = {tot[4] / n, tot[5] / n, tot[6] / n};
+    float rsme = (float)tot[16];
+    rsme /= (float)n;
+    rsme = sqrtf(rsme);
+    const float fitness = (float)n / (float)tot[17];
+    // H = sum (x - cx)(y - cy)^T = sum x y^T - n cx cy^T
+    double H[9];
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 3; c++) H[r * 3 + c] = tot[7 + r * 3 + c] - n * cx[r] * cy[c];
+    double U[9], S[3], V[9], R[9];
+    svd3_jacobi(H, U, S, V);
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 3; c++) R[r * 3 + c] = V[r * 3] * U[c * 3] + V[r * 3 + 1] * U[c * 3 + 1] + V[r * 3 + 2] * U[c * 3 + 2];
+    double Tn[16];
+    for (int k = 0; k < 16; k++) Tn[k] = (k % 5 == 0) ? 1.0 : 0.0;
+    for (int r = 0; r < 3; r++) {
+        for (int c = 0; c < 3; c++) Tn[r * 4 + c] = R[r * 3 + c];
+        Tn[r * 4 + 3] = cy[r] - (R[r * 3] * cx[0] + R[r * 3 + 1] * cx[1] + R[r * 3 + 2] * cx[2]);
+    }
+    for (int k = 0; k < 16; k++) {
+        st->Txy_d[k] = Tn[k];
+        st->Txy[k] = (float)Tn[k];
+    }
+    const int it = st->iteration;
+    bool became_best = false;
+    if (rsme < st->lowest) {  // kokkosICP.cpp:181-185
+        st->lowest = rsme;
+        for (int k = 0; k < 16; k++) st->best[k] = Tn[k];
+        became_best = true;
+    }
+    if (fitness > st->best_fitness) st->best_fitness = fitness;
+    if (it < kIcpIters) {
+        st->stats[it * 4 + 0] = n;
+        st->stats[it * 4 + 1] = rsme;
+        st->stats[it * 4 + 2] = fitness;
+        st->stats[it * 4 + 3] = became_best ? 1.0 : 0.0;
+    }
+    st->iteration = it + 1;
+    st->ticket = 0;
+}
+
+// Scratch of ss_kokkos_icp, one per device, grown on demand.
+struct IcpWorkspace {
+    float *xp = nullptr, *yp = nullptr, *yn = nullptr;
+    double *partials = nullptr;
+    IcpState *state = nullptr;
+    size_t npix = 0;
+    int ctas = 0;
+};
+static std::mutex g_icp_mutex;
+static IcpWorkspace g_icp_ws[64];
+
+static ss_status icp_workspace(int dev, size_t npix, int ctas, IcpWorkspace **out) {
+    if (dev < 0 || dev >= 64) return SS_ERR_ARG;
+    IcpWorkspace &w = g_icp_ws[dev];
+    if (w.npix < npix) {
+        cudaFree(w.xp);
+        cudaFree(w.yp);
+        cudaFree(w.yn);
+        w.xp = w.yp = w.yn = nullptr;
+        w.npix = 0;
+        if (cudaMalloc(&w.xp, npix * 12) != cudaSuccess || cudaMalloc(&w.yp, npix * 12) != cudaSuccess ||
+            cudaMalloc(&w.yn, npix * 12) != cudaSuccess) {
+            cudaGetLastError();
+            return SS_ERR_NOMEM;
+        }
+        w.npix = npix;
+    }
+    if (w.ctas < ctas || !w.state) {
+        cudaFree(w.partials);
+        cudaFree(w.state);
+        w.partials = nullptr;
+        w.state = nullptr;
+        w.ctas = 0;
+        if (cudaMalloc(&w.partials, (size_t)ctas * kIcpSums * sizeof(double)) != cudaSuccess ||
+            cudaMalloc(&w.state, sizeof(IcpState)) != cudaSuccess) {
+            cudaGetLastError();
+            return SS_ERR_NOMEM;
+        }
+        w.ctas = ctas;
+    }
+    *out = &w;
+    return SS_OK;
+}
+
+static void inverse4d(const double *m, double *out) {
+    double a[4][8];
+    for (int r = 0; r < 4; r++)
+        for (int c = 0; c < 8; c++) a[r][c] = c < 4 ? m[r * 4 + c] : (c - 4 == r ? 1.0 : 0.0);
+    for (int col = 0; col < 4; col++) {
+        int piv = col;
+        for (int r = col + 1; r < 4; r++)
+            if (std::fabs(a[r][col]) > std::fabs(a[piv][col])) piv = r;
+        if (piv != col)
+            for (int c = 0; c < 8; c++) {
+                double t = a[col][c];
+                a[col][c] = a[piv][c];
+                a[piv][c] = t;
+            }
+        const double d = a[col][col];
+        for (int c = 0; c < 8; c++) a[col][c] /= d;
+        for (int r = 0; r < 4; r++) {
+            if (r == col) continue;
+            const double f = a[r][col];
+            for (int c = 0; c < 8; c++) a[r][c] -= f * a[col][c];
+        }
+    }
+    for (int r = 0; r < 4; r++)
+        for (int c = 0; c < 4; c++) out[r * 4 + c] = a[r][c + 4];
+}
+
+// Runs the 10 iterations on prepared point clouds; shared by the entry points.
+ss_status icp_ref_run(const uint16_t *d1, const uint16_t *d2, int rows, int cols, Intr in, const double tx[16],
+                      const double ty[16], int type, float *xp, float *yp, float *yn, double *partials, int ctas,
+                      IcpState *state, double txy_out[16], float *rmse_out, cudaStream_t s) {
+    const dim3 blk(128), grid((cols + 127) / 128, rows);
+    depth_to_pcd_kernel<<<grid, blk, 0, s>>>(d1, rows, cols, in, xp);
+    depth_to_pcd_kernel<<<grid, blk, 0, s>>>(d2, rows, cols, in, yp);
+    normals_kernel<<<grid, blk, 0, s>>>(yp, rows, cols, yn);
+    SS_LAUNCH_CHECK();
+    // Txy = ty^-1 * tx (kokkosICP.cpp:57), float copy for the search
+    double tyi[16], T[16];
+    inverse4d(ty, tyi);
+    for (int r = 0; r < 4; r++)
+        for (int c = 0; c < 4; c++) {
+            double acc = 0;
+            for (int k = 0; k < 4; k++) acc += tyi[r * 4 + k] * tx[k * 4 + c];
+            T[r * 4 + c] = acc;
+        }
+    IcpState h;
+    std::memset(&h, 0, sizeof(h));
+    for (int k = 0; k < 16; k++) {
+        h.Txy_d[k] = T[k];
+        h.Txy[k] = (float)T[k];
+        h.best[k] = (k % 5 == 0) ? 1.0 : 0.0;
+    }
+    h.lowest = 1e6f;
+    h.best_fitness = 0.f;
+    SS_CUDA_TRY(cudaMemcpyAsync(state, &h, sizeof(h), cudaMemcpyHostToDevice, s));
+    for (int it = 0; it < kIcpIters; it++) {
+        if (type == SS_ICP_POINT_TO_POINT)
+            icp_ref_iter_kernel<SS_ICP_POINT_TO_POINT><<<ctas, 256, 0, s>>>(xp, yp, yn, rows, cols, in, state, partials);
+        else
+            icp_ref_iter_kernel<SS_ICP_POINT_TO_PLANE><<<ctas, 256, 0, s>>>(xp, yp, yn, rows, cols, in, state, partials);
+        SS_LAUNCH_CHECK();
+    }
+    SS_CUDA_TRY(cudaMemcpyAsync(&h, state, sizeof(h), cudaMemcpyDeviceToHost, s));
+    SS_CUDA_TRY(cudaStreamSynchronize(s));
+    for (int k = 0; k < 16; k++) txy_out[k] = h.best[k];
+    if (rmse_out) *rmse_out = h.lowest;
+    return SS_OK;
+}
+
+static ss_status icp_check_args(const uint16_t *d1, const uint16_t *d2, int rows, int cols, float fx, float fy,
+                                const double *tx, const double *ty, int type, double *out) {
+    if (!d1 || !d2 || !tx || !ty || !out) return SS_ERR_ARG;
+    if (rows <= 2 * 5 + 1 || cols <= 2 * 5 + 1) return SS_ERR_DIMS;
+    if (type != SS_ICP_POINT_TO_POINT && type != SS_ICP_POINT_TO_PLANE) return SS_ERR_ARG;
+    if (!(fx != 0.f) || !(fy != 0.f)) return SS_ERR_ARG;
+    return SS_OK;
+}
+
+}  // namespace ss
+
+using namespace ss;
+
+extern "C" {
+
+ss_status ss_depth_to_pcd(const uint16_t *depth, int32_t rows, int32_t cols, float fx, float fy, float cx, float cy,
+                          float *pcd, ss_stream_t stream) {
+    if (!depth || !pcd || rows <= 0 || cols <= 0) return SS_ERR_ARG;
+    const Intr in{fx, fy, (float)rows - cy, cx};
+    depth_to_pcd_kernel<<<dim3((cols + 127) / 128, rows), 128, 0, (cudaStream_t)stream>>>(depth, rows, cols, in, pcd);
+    SS_LAUNCH_CHECK();
+    return SS_OK;
+}
+
+ss_status ss_normals_from_pcd(const float *pcd, int32_t rows, int32_t cols, float *normals, ss_stream_t stream) {
+    if (!pcd || !normals || rows <= 0 || cols <= 0) return SS_ERR_ARG;
+    normals_kernel<<<dim3((cols + 127) / 128, rows), 128, 0, (cudaStream_t)stream>>>(pcd, rows, cols, normals);
+    SS_LAUNCH_CHECK();
+    return SS_OK;
+}
+
+ss_status ss_kokkos_icp(const uint16_t *d1, const uint16_t *d2, int32_t rows, int32_t cols, float fx, float fy,
+                        float cx, float cy, const double tx[16], const double ty[16], int32_t icp_type,
+                        double txy_out[16], float *rmse_out, ss_stream_t stream) {
+    ss_status st = icp_check_args(d1, d2, rows, cols, fx, fy, tx, ty, icp_type, txy_out);
+    if (st != SS_OK) return st;
+    int dev = 0, sms = 0;
+    SS_CUDA_TRY(cudaGetDevice(&dev));
+    SS_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int ctas = sms * 4;
+    std::lock_guard<std::mutex> lock(g_icp_mutex);
+    IcpWorkspace *w = nullptr;
+    st = icp_workspace(dev, (size_t)rows * cols, ctas, &w);
+    if (st != SS_OK) return st;
+    const Intr in{fx, fy, (float)rows - cy, cx};  // ci = resi - cy, cj = cx (kokkosICP.cpp:48-49)
+    return icp_ref_run(d1, d2, rows, cols, in, tx, ty, icp_type, w->xp, w->yp, w->yn, w->partials, ctas, w->state,
+                       txy_out, rmse_out, (cudaStream_t)stream);
+}
+
+}  // extern "C"

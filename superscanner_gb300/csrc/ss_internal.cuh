@@ -1,0 +1,228 @@
+// ss_internal.cuh — device-side building blocks shared by the kernels.
+//
+// Reference-order arithmetic: the parity kernels evaluate every expression of
+// the reference (src/VoxelGrid/GPUVoxelGrid.{h,cpp}) with explicit
+// round-to-nearest intrinsics (__fmul_rn, __fadd_rn, __fdiv_rn ...), so nvcc
+// cannot contract them into FMAs and the results are those of the C++
+// expressions evaluated in IEEE single precision, operand by operand.
+#pragma once
+
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/ss_abi.h"
+
+namespace ss {
+
+constexpr int kEdge = 8;          // voxelPerEdge (GPUVoxelGrid.h:6)
+constexpr int kBlockVoxels = 512; // voxelPerBlock (GPUVoxelGrid.h:8)
+
+// Hash-table key domain: the reference's key is an int32 sign-extended to
+// u64, so the upper 32 bits are all-zero or all-one. These two words have
+// upper bits zero and bit 31 set, which no key can have.
+constexpr uint64_t kEmptyKey = 0x00000000FFFFFFFFull;
+constexpr uint64_t kTombKey = 0x00000000FFFFFFFEull;
+
+// Block stamp word: [63:42] epoch of the last call that touched the block,
+// [41:28] x+8192, [27:14] y+8192, [13:0] z+8192.
+constexpr int kCoordBias = 8192;
+constexpr int kEpochShift = 42;
+constexpr uint32_t kEpochMax = (1u << 22) - 1;
+
+// Device status word bits (ORed; mapped to the first ss_status by the host).
+enum : int {
+    kStTableFull = 1 << 0,
+    kStListOverflow = 1 << 1,
+    kStRange = 1 << 2,
+    kStTimeout = 1 << 3,
+};
+
+// Device-resident counters of one grid (one 128-byte line).
+struct Counters {
+    int list_count;                   // touched blocks of the current call
+    int status;                       // kSt* bits
+    uint32_t epoch;                   // current call epoch (1 .. kEpochMax)
+    int work;                         // dynamic work index for persistent kernels
+    int live_blocks;                  // allocated blocks (maintained by insert / clean)
+    int last_touched;                 // list_count of the previous call
+    unsigned long long touched_total; // sum of list_count over all calls
+    unsigned long long calls;         // integrate/deintegrate calls finalized
+    int pad[22];
+};
+static_assert(sizeof(Counters) == 128, "Counters is one 128-byte line");
+
+struct Intr {
+    float fx, fy, ci, cj;  // ci = resi - cy, cj = cx (GPUVoxelGrid.cpp:257-262)
+};
+
+struct Mat34 {
+    float m[12];  // row-major 3x4 affine part of a 4x4 float matrix
+};
+
+// View of one grid passed by value to kernels.
+struct GridView {
+    unsigned long long *keys;   // [buckets] u64 prime-hash keys
+    unsigned long long *stamp;  // [buckets] epoch | packed block coords
+    float2 *vox32;              // [buckets][512] (sdf, w)     SS_STORAGE_F32
+    uint32_t *vox16;            // [buckets][512] half(sdf/trunc) | u16 w << 16   SS_STORAGE_F16
+    float *rgb;                 // [buckets][3][512] or null
+    int *list;                  // [buckets] touched bucket indices
+    Counters *ctr;
+    uint32_t mask;              // buckets - 1
+    float vl, vbl, trunc, rmin, d_max, max_weight;
+    int resi, resj;
+    Intr in;
+};
+
+// ------------------------------------------------------------------ math
+struct F3 {
+    float x, y, z;
+};
+
+__device__ __forceinline__ F3 f3sub(F3 a, F3 b) {
+    return {__fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y), __fsub_rn(a.z, b.z)};
+}
+__device__ __forceinline__ F3 f3add(F3 a, F3 b) {
+    return {__fadd_rn(a.x, b.x), __fadd_rn(a.y, b.y), __fadd_rn(a.z, b.z)};
+}
+__device__ __forceinline__ F3 f3smul(float a, F3 b) {
+    return {__fmul_rn(a, b.x), __fmul_rn(a, b.y), __fmul_rn(a, b.z)};
+}
+// Kvec3f scalar product x*a.x + y*a.y + z*a.z (kokkosFunctions.h:211-214)
+__device__ __forceinline__ float f3dot(F3 a, F3 b) {
+    return __fadd_rn(__fadd_rn(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y)), __fmul_rn(a.z, b.z));
+}
+__device__ __forceinline__ F3 f3cross(F3 a, F3 b) {
+    return {__fsub_rn(__fmul_rn(a.y, b.z), __fmul_rn(a.z, b.y)),
+            __fsub_rn(__fmul_rn(a.z, b.x), __fmul_rn(a.x, b.z)),
+            __fsub_rn(__fmul_rn(a.x, b.y), __fmul_rn(a.y, b.x))};
+}
+__device__ __forceinline__ float f3len(F3 a) { return __fsqrt_rn(f3dot(a, a)); }
+__device__ __forceinline__ F3 f3normalized(F3 a) {
+    float t = f3len(a);
+    return {__fdiv_rn(a.x, t), __fdiv_rn(a.y, t), __fdiv_rn(a.z, t)};
+}
+
+// transformPoint (GPUVoxelGrid.h:240-247): ((p.x*E0 + p.y*E1) + p.z*E2) + E3
+__device__ __forceinline__ F3 xform(const Mat34 &E, F3 p) {
+    F3 o;
+    o.x = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(p.x, E.m[0]), __fmul_rn(p.y, E.m[1])), __fmul_rn(p.z, E.m[2])), E.m[3]);
+    o.y = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(p.x, E.m[4]), __fmul_rn(p.y, E.m[5])), __fmul_rn(p.z, E.m[6])), E.m[7]);
+    o.z = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(p.x, E.m[8]), __fmul_rn(p.y, E.m[9])), __fmul_rn(p.z, E.m[10])), E.m[11]);
+    return o;
+}
+
+// getPoint (GPUVoxelGrid.h:229-232): ((j - cj)/fx*d, (i - ci)/fy*d, d)
+__device__ __forceinline__ F3 get_point(const Intr &in, int i, int j, float d) {
+    return {__fmul_rn(__fdiv_rn(__fsub_rn((float)j, in.cj), in.fx), d),
+            __fmul_rn(__fdiv_rn(__fsub_rn((float)i, in.ci), in.fy), d), d};
+}
+
+// (float)(depth) / 1000 (GPUVoxelGrid.h:306)
+__device__ __forceinline__ float depth_m(uint16_t d) { return __fdiv_rn((float)d, 1000.f); }
+
+// Index rule of getIndeces / getVBIndeces / getVinVBIndeces
+// (GPUVoxelGrid.h:131-221): a >= 0 ? (int)(a/len) : (int)(a/len - 1).
+// __float2int_rz is the (int) cast of the reference's device build.
+__device__ __forceinline__ int idx_rule(float a, float len) {
+    float q = __fdiv_rn(a, len);
+    return a >= 0.f ? __float2int_rz(q) : __float2int_rz(__fsub_rn(q, 1.f));
+}
+
+// getPrimeHash (GPUVoxelGrid.h:124-128), int wrap, sign-extended to u64.
+__device__ __forceinline__ unsigned long long prime_hash(int x, int y, int z) {
+    uint32_t h = 73856093u * (uint32_t)x + 19349669u * (uint32_t)y + 83492791u * (uint32_t)z;
+    return (unsigned long long)(long long)(int32_t)h;
+}
+
+__device__ __forceinline__ bool packable(int x, int y, int z) {
+    return x >= -kCoordBias && x < kCoordBias && y >= -kCoordBias && y < kCoordBias && z >= -kCoordBias &&
+           z < kCoordBias;
+}
+__device__ __forceinline__ unsigned long long pack_coords(int x, int y, int z) {
+    return ((unsigned long long)(uint32_t)(x + kCoordBias) << 28) |
+           ((unsigned long long)(uint32_t)(y + kCoordBias) << 14) | (unsigned long long)(uint32_t)(z + kCoordBias);
+}
+__device__ __forceinline__ void unpack_coords(unsigned long long p, int &x, int &y, int &z) {
+    x = (int)((p >> 28) & 0x3fff) - kCoordBias;
+    y = (int)((p >> 14) & 0x3fff) - kCoordBias;
+    z = (int)(p & 0x3fff) - kCoordBias;
+}
+
+// Home bucket: murmur3 finalizer of the low key word (the prime hash is
+// linear in the coordinates, so neighbouring blocks need mixing).
+__device__ __forceinline__ uint32_t home_bucket(unsigned long long key, uint32_t mask) {
+    uint32_t h = (uint32_t)key;
+    h ^= h >> 16;
+    h *= 0x85ebca6bu;
+    h ^= h >> 13;
+    h *= 0xc2b2ae35u;
+    h ^= h >> 16;
+    return h & mask;
+}
+
+__device__ __forceinline__ unsigned long long ld_relaxed(const unsigned long long *p) {
+    unsigned long long v;
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Lookup only (UnorderedMap::find): bucket index or -1. Tombstones continue
+// the probe, an empty bucket ends it. Read-only kernels see a table that no
+// other kernel is modifying, so plain loads suffice.
+__device__ __forceinline__ int table_find(const GridView &g, unsigned long long key) {
+    uint32_t b = home_bucket(key, g.mask);
+    for (uint32_t probe = 0; probe <= g.mask; probe++) {
+        unsigned long long k = __ldg(g.keys + b);
+        if (k == key) return (int)b;
+        if (k == kEmptyKey) return -1;
+        b = (b + 1) & g.mask;
+    }
+    return -1;
+}
+
+// Lock-free find-or-insert (UnorderedMap::find + insert,
+// GPUVoxelGrid.cpp:493-499). Returns the bucket, or -1 with kStTableFull set.
+// Inserts claim the first tombstone or the terminating empty bucket of the
+// probe sequence with one 64-bit CAS and re-scan when the CAS loses. The
+// payload of a free bucket is always zero (create/reset/clean keep it so), so
+// a claimed bucket is a default-constructed Voxelblock.
+__device__ __forceinline__ int table_find_or_insert(const GridView &g, unsigned long long key) {
+    const uint32_t home = home_bucket(key, g.mask);
+    for (int attempt = 0; attempt < 64; attempt++) {
+        int free_b = -1;
+        unsigned long long free_expect = 0;
+        uint32_t b = home;
+        uint32_t probe = 0;
+        for (; probe <= g.mask; probe++) {
+            unsigned long long k = ld_relaxed(g.keys + b);
+            if (k == key) return (int)b;
+            if (k == kTombKey && free_b < 0) {
+                free_b = (int)b;
+                free_expect = kTombKey;
+            }
+            if (k == kEmptyKey) {
+                if (free_b < 0) {
+                    free_b = (int)b;
+                    free_expect = kEmptyKey;
+                }
+                break;
+            }
+            b = (b + 1) & g.mask;
+        }
+        if (free_b < 0) break;
+        unsigned long long old = atomicCAS(g.keys + free_b, free_expect, key);
+        if (old == free_expect) {
+            atomicAdd(&g.ctr->live_blocks, 1);
+            return free_b;
+        }
+        if (old == key) return free_b;
+    }
+    atomicOr(&g.ctr->status, kStTableFull);
+    return -1;
+}
+
+__device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }
+
+}  // namespace ss
