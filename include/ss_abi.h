@@ -159,6 +159,51 @@ ss_status ss_kokkos_icp(const uint16_t *d1, const uint16_t *d2, int32_t rows, in
                         const double ty[16], int32_t icp_type, double txy_out[16],
                         float *rmse_out, ss_stream_t s);
 
+/* ------------------------------------------------------------------------
+ * The per-frame method (no direct reference counterpart: the reference's
+ * raycast is nearest-voxel with no normals and no step cap, GPUVoxelGrid.h:377,
+ * and its ICP is the host-SVD kokkosICP above).
+ */
+
+/* Trilinear raycast: at most max_steps march steps per ray between t_min and
+ * t_max (camera-frame depth). vertex_depth [resi][resj][4] = (x, y, z world,
+ * depth), normal [resi][resj][4] = (nx, ny, nz, 0) world; misses are zero. */
+ss_status ss_raycast_maps(ss_grid *g, const float extr[16], int32_t max_steps, float t_min,
+                          float t_max, float *vertex_depth, float *normal, ss_stream_t s);
+
+typedef struct ss_pipeline ss_pipeline;
+
+typedef struct ss_pipeline_params {
+    int32_t levels;           /* pyramid levels of the tracker (<= 4) */
+    int32_t iters[4];         /* Gauss-Newton iterations per level, level 0 = full resolution */
+    float dist_thresh[4];     /* correspondence distance gate per level, metres */
+    int32_t raycast_steps;    /* march step cap of the model-view raycast */
+    float t_min, t_max;       /* raycast depth range */
+    int32_t use_graph;        /* replay each tracked frame as one captured CUDA graph */
+    int32_t exact_fusion;     /* reference rounding in the voxel update (else FMA-contracted) */
+} ss_pipeline_params;
+
+ss_status ss_pipeline_params_default(ss_pipeline_params *p);
+/* The pipeline fuses depth only (no colour) into g, which it borrows. */
+ss_status ss_pipeline_create(ss_grid *g, const ss_pipeline_params *p, ss_pipeline **out);
+ss_status ss_pipeline_destroy(ss_pipeline *p);
+/* Sets the device pose (camera -> world) used by the next untracked frame and
+ * as the start of tracking. Synchronises s. */
+ss_status ss_pipeline_set_pose(ss_pipeline *p, const double T[16], ss_stream_t s);
+/* Copies the current pose to the host. Synchronises s. */
+ss_status ss_pipeline_get_pose(ss_pipeline *p, double T[16], ss_stream_t s);
+/* Device input buffer [resi][resj] u16; frames written there need no copy. */
+ss_status ss_pipeline_input(ss_pipeline *p, uint16_t **depth);
+/* Device model maps of the last frame (layout of ss_raycast_maps). */
+ss_status ss_pipeline_maps(ss_pipeline *p, float **vertex_depth, float **normal);
+/* One frame: if track != 0 and a model exists, track the frame against the
+ * last model view, then integrate at the pose and raycast the model view at
+ * it; else integrate at the current pose and raycast. depth may be a device
+ * or host pointer (copied into the input buffer on s). No host sync. */
+ss_status ss_pipeline_frame(ss_pipeline *p, const uint16_t *depth, int32_t track, ss_stream_t s);
+/* Tracker inliers and residual RMS per level of the last tracked frame. */
+ss_status ss_pipeline_stats(ss_pipeline *p, int32_t inliers[4], float rmse[4], ss_stream_t s);
+
 #ifdef __cplusplus
 }
 #endif

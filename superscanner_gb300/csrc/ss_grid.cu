@@ -104,8 +104,13 @@ __global__ void fill_u64_kernel(unsigned long long *p, size_t n, unsigned long l
 // alreadyIntegrated + the O(capacity) "Reset booleans" pass) and fixes the
 // entry's coordinates canonically for aliased keys. Appends are aggregated
 // per warp (one atomicAdd per warp and candidate round).
-__global__ void __launch_bounds__(256) collect_kernel(GridView g, const uint16_t *__restrict__ depth, Mat34 E) {
+__global__ void __launch_bounds__(256) collect_kernel(GridView g, const uint16_t *__restrict__ depth, Mat34 E,
+                                                      const FramePose *__restrict__ pose) {
     const unsigned FULL = 0xffffffffu;
+    if (pose) {
+#pragma unroll
+        for (int k = 0; k < 12; k++) E.m[k] = __ldg(&pose->E.m[k]);
+    }
     const int lane = threadIdx.x;  // blockDim = (32, 8): one warp per row segment
     const int j = blockIdx.x * 32 + threadIdx.x;
     const int i = blockIdx.y * blockDim.y + threadIdx.y;
@@ -265,7 +270,9 @@ __device__ __forceinline__ void color_average(float &c, float w_old, float obs) 
 // identical float.
 template <int kStorage, bool kColor, bool kDeint, bool kExact>
 __global__ void __launch_bounds__(256) fuse_kernel(GridView g, const uint16_t *__restrict__ depth,
-                                                   const uint8_t *__restrict__ rgb, Mat34 E, Mat34 Einv, F3 Ez) {
+                                                   const uint8_t *__restrict__ rgb, Mat34 E, Mat34 Einv, F3 Ez,
+                                                   const FramePose *__restrict__ pose) {
+    if (pose) load_pose(pose, E, Einv, Ez.x, Ez.y, Ez.z);
     const int lane = threadIdx.x & 31;
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -447,26 +454,44 @@ __global__ void import_blocks_kernel(GridView g, const int *__restrict__ coords,
 
 // --------------------------------------------------------------- launchers
 
-static ss_status launch_fuse(ss_grid *g, const uint16_t *depth, const uint8_t *rgb, const float extr[16],
-                             bool color, bool deint, bool exact, cudaStream_t s) {
+FramePose frame_pose_from(const float extr[16]) {
+    FramePose fp;
     float Einv16[16];
     inverse4_rounded(extr, Einv16);
-    const Mat34 E = mat34_from(extr), Einv = mat34_from(Einv16);
+    fp.E = mat34_from(extr);
+    fp.Einv = mat34_from(Einv16);
     // Ez: normalized third column of extr (GPUVoxelGrid.cpp:52-53), Kvec3f::normalize in float
     const float ex = extr[2], ey = extr[6], ez = extr[10];
-    volatile float len = std::sqrt(ex * ex + ey * ey + ez * ez);
-    const F3 Ez{ex / len, ey / len, ez / len};
+    const float len = std::sqrt(ex * ex + ey * ey + ez * ez);
+    fp.Ez[0] = ex / len;
+    fp.Ez[1] = ey / len;
+    fp.Ez[2] = ez / len;
+    fp.pad = 0.f;
+    return fp;
+}
 
-    if (g->host_epoch >= kEpochMax) {
-        rebase_epoch_kernel<<<persistent_ctas(g, 4), 256, 0, s>>>(g->v);
-        SS_LAUNCH_CHECK();
-        g->host_epoch = 1;
+ss_status rebase_epoch(ss_grid *g, cudaStream_t s) {
+    rebase_epoch_kernel<<<persistent_ctas(g, 4), 256, 0, s>>>(g->v);
+    SS_LAUNCH_CHECK();
+    g->host_epoch = 1;
+    return SS_OK;
+}
+
+ss_status launch_fuse(ss_grid *g, const uint16_t *depth, const uint8_t *rgb, const FramePose &hp,
+                      const FramePose *dpose, bool color, bool deint, bool exact, cudaStream_t s,
+                      bool manage_epoch) {
+    const Mat34 E = hp.E, Einv = hp.Einv;
+    const F3 Ez{hp.Ez[0], hp.Ez[1], hp.Ez[2]};
+
+    if (manage_epoch && g->host_epoch >= kEpochMax) {
+        ss_status st = rebase_epoch(g, s);
+        if (st != SS_OK) return st;
     }
     const dim3 cblk(32, 8), cgrid((g->p.resj + 31) / 32, (g->p.resi + 7) / 8);
-    collect_kernel<<<cgrid, cblk, 0, s>>>(g->v, depth, E);
+    collect_kernel<<<cgrid, cblk, 0, s>>>(g->v, depth, E, dpose);
     SS_LAUNCH_CHECK();
     const int ctas = persistent_ctas(g, 8);
-#define SS_FUSE(ST, C, D, X) fuse_kernel<ST, C, D, X><<<ctas, 256, 0, s>>>(g->v, depth, rgb, E, Einv, Ez)
+#define SS_FUSE(ST, C, D, X) fuse_kernel<ST, C, D, X><<<ctas, 256, 0, s>>>(g->v, depth, rgb, E, Einv, Ez, dpose)
 #define SS_FUSE_X(ST, C, D) \
     do {                    \
         if (exact) SS_FUSE(ST, C, D, true); else SS_FUSE(ST, C, D, false); \
@@ -486,7 +511,7 @@ static ss_status launch_fuse(ss_grid *g, const uint16_t *depth, const uint8_t *r
     SS_LAUNCH_CHECK();
     finalize_kernel<<<1, 1, 0, s>>>(g->v.ctr);
     SS_LAUNCH_CHECK();
-    g->host_epoch++;
+    if (manage_epoch) g->host_epoch++;
     return SS_OK;
 }
 
@@ -615,7 +640,7 @@ static ss_status fuse_entry(ss_grid *g, const uint16_t *depth, const uint8_t *rg
     if (color && (!rgb || !g->v.rgb)) return SS_ERR_ARG;
     for (int k = 0; k < 16; k++)
         if (!std::isfinite(extr[k])) return SS_ERR_ARG;
-    return launch_fuse(g, depth, rgb, extr, color, deint, /*exact=*/true, (cudaStream_t)s);
+    return launch_fuse(g, depth, rgb, frame_pose_from(extr), nullptr, color, deint, /*exact=*/true, (cudaStream_t)s);
 }
 
 ss_status ss_integrate(ss_grid *g, const uint16_t *depth, const uint8_t *rgb, const float extr[16],
@@ -636,7 +661,8 @@ ss_status ss_integrate_fast(ss_grid *g, const uint16_t *depth, const uint8_t *rg
     if (!g->intr_set) return SS_ERR_STATE;
     const bool color = with_color != 0;
     if (color && (!rgb || !g->v.rgb)) return SS_ERR_ARG;
-    return launch_fuse(g, depth, rgb, extr, color, deint != 0, /*exact=*/false, (cudaStream_t)s);
+    return launch_fuse(g, depth, rgb, frame_pose_from(extr), nullptr, color, deint != 0, /*exact=*/false,
+                       (cudaStream_t)s);
 }
 
 ss_status ss_clean_memory(ss_grid *g, ss_stream_t stream) {

@@ -46,7 +46,21 @@ ss_status status_from_bits(int bits);
     } while (0)
 
 Mat34 mat34_from(const float E[16]);
+FramePose frame_pose_from(const float extr[16]);
+
+// integrate / deintegrate launch sequence (collect, fuse, finalize); the pose
+// comes from hp, or from device memory when dpose is not null. With
+// manage_epoch the host epoch mirror is advanced here (direct calls); graph
+// replays advance it in the caller instead.
+ss_status launch_fuse(ss_grid *g, const uint16_t *depth, const uint8_t *rgb, const FramePose &hp,
+                      const FramePose *dpose, bool color, bool deint, bool exact, cudaStream_t s,
+                      bool manage_epoch = true);
+// Clears the epoch field of every stamp and restarts the epoch at 1.
+ss_status rebase_epoch(ss_grid *g, cudaStream_t s);
 void inverse4_rounded(const float E[16], float out[16]);
+
+ss_status launch_raycast_maps(ss_grid *g, const Mat34 &T, const FramePose *dpose, int max_steps, float t_min,
+                              float t_max, float4 *vmap, float4 *nmap, cudaStream_t s);
 
 // Blocks of persistent launches (multiple of the SM count).
 int persistent_ctas(const ss_grid *g, int per_sm);

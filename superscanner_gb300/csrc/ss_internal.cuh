@@ -60,6 +60,29 @@ struct Mat34 {
     float m[12];  // row-major 3x4 affine part of a 4x4 float matrix
 };
 
+// Pose of one integrate/raycast call as the kernels consume it. Host-side
+// calls pass it by value; the per-frame pipeline keeps it in device memory
+// (written by the tracker) and passes a pointer, so no host round trip is
+// needed between tracking and fusion.
+struct FramePose {
+    Mat34 E;     // camera -> world, float (the reference's E view)
+    Mat34 Einv;  // world -> camera, float (E_inv)
+    float Ez[3]; // normalized third column of E
+    float pad;
+};
+
+__device__ __forceinline__ void load_pose(const FramePose *p, Mat34 &E, Mat34 &Einv, float &ezx, float &ezy,
+                                          float &ezz) {
+#pragma unroll
+    for (int k = 0; k < 12; k++) {
+        E.m[k] = __ldg(&p->E.m[k]);
+        Einv.m[k] = __ldg(&p->Einv.m[k]);
+    }
+    ezx = __ldg(&p->Ez[0]);
+    ezy = __ldg(&p->Ez[1]);
+    ezz = __ldg(&p->Ez[2]);
+}
+
 // View of one grid passed by value to kernels.
 struct GridView {
     unsigned long long *keys;   // [buckets] u64 prime-hash keys

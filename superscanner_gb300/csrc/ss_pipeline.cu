@@ -1,0 +1,226 @@
+// ss_pipeline.cu — the per-frame reconstruction pipeline:
+//   track (3-level point-to-plane GN against the last model view)
+//   -> integrate at the tracked pose -> raycast the model view at that pose.
+//
+// All state (pose, model maps, hash table) stays in device memory; a frame
+// needs no host synchronisation. With use_graph the whole frame (about 25
+// kernels) is captured once as a CUDA graph and replayed per frame.
+// The reference has no such pipeline object: its integration thread
+// (src/core/integrate.cpp:47-209) calls GPUVoxelGrid::integrate with poses
+// from the keypoint tracker, and raycast is called by the GUI loop
+// (exe/SuperScanner.cpp:343-361).
+#include "ss_grid_impl.cuh"
+#include "ss_track.cuh"
+
+using namespace ss;
+
+struct ss_pipeline {
+    ss_grid *g = nullptr;
+    ss_pipeline_params p{};
+    TrackState *st = nullptr;
+    float2 *partials = nullptr;
+    float4 *vmap = nullptr, *nmap = nullptr;
+    uint16_t *input = nullptr;
+    int ctas = 0;
+    bool have_model = false;
+    cudaStream_t cap = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    unsigned long long frames = 0;
+};
+
+namespace {
+
+ss_status enqueue_fuse_raycast(ss_pipeline *P, cudaStream_t s) {
+    ss_grid *g = P->g;
+    FramePose dummy{};
+    ss_status st = launch_fuse(g, P->input, nullptr, dummy, &P->st->pose, false, false, P->p.exact_fusion != 0, s,
+                               /*manage_epoch=*/false);
+    if (st != SS_OK) return st;
+    return launch_raycast_maps(g, dummy.E, &P->st->pose, P->p.raycast_steps, P->p.t_min, P->p.t_max, P->vmap,
+                               P->nmap, s);
+}
+
+ss_status enqueue_frame(ss_pipeline *P, cudaStream_t s) {
+    ss_grid *g = P->g;
+    TrackLaunch L{};
+    L.depth = P->input;
+    L.rows = g->p.resi;
+    L.cols = g->p.resj;
+    L.in = g->v.in;
+    L.vmap = P->vmap;
+    L.nmap = P->nmap;
+    L.state = P->st;
+    L.partials = P->partials;
+    L.ctas = P->ctas;
+    L.levels = P->p.levels;
+    for (int l = 0; l < kMaxLevels; l++) {
+        L.iters[l] = P->p.iters[l];
+        L.dist[l] = P->p.dist_thresh[l];
+    }
+    L.rmin = g->p.rmin;
+    L.dmax = P->p.t_max;
+    ss_status st = launch_track(L, s);
+    if (st != SS_OK) return st;
+    return enqueue_fuse_raycast(P, s);
+}
+
+// The epoch advances once per executed integrate; rebase before it wraps.
+ss_status epoch_guard(ss_pipeline *P, cudaStream_t s) {
+    ss_grid *g = P->g;
+    if (g->host_epoch + 1 >= kEpochMax) {
+        ss_status st = rebase_epoch(g, s);
+        if (st != SS_OK) return st;
+    }
+    return SS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+ss_status ss_pipeline_params_default(ss_pipeline_params *p) {
+    if (!p) return SS_ERR_ARG;
+    *p = ss_pipeline_params{};
+    p->levels = 3;
+    p->iters[0] = 10;  // 640x480
+    p->iters[1] = 5;   // 320x240
+    p->iters[2] = 4;   // 160x120
+    p->iters[3] = 0;
+    p->dist_thresh[0] = 0.06f;
+    p->dist_thresh[1] = 0.10f;
+    p->dist_thresh[2] = 0.15f;
+    p->dist_thresh[3] = 0.20f;
+    p->raycast_steps = 128;
+    p->t_min = 0.2f;
+    p->t_max = 10.0f;
+    p->use_graph = 1;
+    p->exact_fusion = 0;
+    return SS_OK;
+}
+
+ss_status ss_pipeline_create(ss_grid *g, const ss_pipeline_params *params, ss_pipeline **out) {
+    if (!g || !params || !out) return SS_ERR_ARG;
+    *out = nullptr;
+    if (params->levels < 1 || params->levels > kMaxLevels || params->raycast_steps < 1) return SS_ERR_ARG;
+    if (!g->intr_set) return SS_ERR_STATE;
+    ss_pipeline *P = new ss_pipeline;
+    P->g = g;
+    P->p = *params;
+    P->ctas = g->num_sms * 2;
+    const size_t npix = (size_t)g->p.resi * g->p.resj;
+    bool ok = cudaMalloc(&P->st, sizeof(TrackState)) == cudaSuccess &&
+              cudaMalloc(&P->partials, (size_t)P->ctas * 29 * sizeof(float2)) == cudaSuccess &&
+              cudaMalloc(&P->vmap, npix * sizeof(float4)) == cudaSuccess &&
+              cudaMalloc(&P->nmap, npix * sizeof(float4)) == cudaSuccess &&
+              cudaMalloc(&P->input, npix * sizeof(uint16_t)) == cudaSuccess &&
+              cudaStreamCreateWithFlags(&P->cap, cudaStreamNonBlocking) == cudaSuccess;
+    if (!ok) {
+        cudaGetLastError();
+        ss_pipeline_destroy(P);
+        return SS_ERR_NOMEM;
+    }
+    cudaMemset(P->st, 0, sizeof(TrackState));
+    cudaMemset(P->vmap, 0, npix * sizeof(float4));
+    cudaMemset(P->nmap, 0, npix * sizeof(float4));
+    double I[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
+    cudaMemcpy(P->st->T, I, sizeof(I), cudaMemcpyHostToDevice);
+    SS_CUDA_TRY(cudaDeviceSynchronize());
+    *out = P;
+    return SS_OK;
+}
+
+ss_status ss_pipeline_destroy(ss_pipeline *P) {
+    if (!P) return SS_ERR_ARG;
+    if (P->exec) cudaGraphExecDestroy(P->exec);
+    if (P->graph) cudaGraphDestroy(P->graph);
+    if (P->cap) cudaStreamDestroy(P->cap);
+    cudaFree(P->st);
+    cudaFree(P->partials);
+    cudaFree(P->vmap);
+    cudaFree(P->nmap);
+    cudaFree(P->input);
+    delete P;
+    return SS_OK;
+}
+
+ss_status ss_pipeline_set_pose(ss_pipeline *P, const double T[16], ss_stream_t stream) {
+    if (!P || !T) return SS_ERR_ARG;
+    SS_CUDA_TRY(cudaMemcpyAsync(P->st->T, T, 16 * sizeof(double), cudaMemcpyHostToDevice, (cudaStream_t)stream));
+    SS_CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
+    return SS_OK;
+}
+
+ss_status ss_pipeline_get_pose(ss_pipeline *P, double T[16], ss_stream_t stream) {
+    if (!P || !T) return SS_ERR_ARG;
+    SS_CUDA_TRY(cudaMemcpyAsync(T, P->st->T, 16 * sizeof(double), cudaMemcpyDeviceToHost, (cudaStream_t)stream));
+    SS_CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
+    return SS_OK;
+}
+
+ss_status ss_pipeline_input(ss_pipeline *P, uint16_t **depth) {
+    if (!P || !depth) return SS_ERR_ARG;
+    *depth = P->input;
+    return SS_OK;
+}
+
+ss_status ss_pipeline_maps(ss_pipeline *P, float **vertex_depth, float **normal) {
+    if (!P || !vertex_depth || !normal) return SS_ERR_ARG;
+    *vertex_depth = (float *)P->vmap;
+    *normal = (float *)P->nmap;
+    return SS_OK;
+}
+
+ss_status ss_pipeline_frame(ss_pipeline *P, const uint16_t *depth, int32_t track, ss_stream_t stream) {
+    if (!P || !depth) return SS_ERR_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    ss_grid *g = P->g;
+    const size_t bytes = (size_t)g->p.resi * g->p.resj * sizeof(uint16_t);
+    if (depth != P->input) SS_CUDA_TRY(cudaMemcpyAsync(P->input, depth, bytes, cudaMemcpyDefault, s));
+    ss_status st = epoch_guard(P, s);
+    if (st != SS_OK) return st;
+    if (!track || !P->have_model) {
+        st = launch_pose_prep(P->st, s);
+        if (st == SS_OK) st = enqueue_fuse_raycast(P, s);
+        if (st != SS_OK) return st;
+        P->have_model = true;
+    } else if (P->p.use_graph) {
+        if (!P->exec) {
+            SS_CUDA_TRY(cudaStreamBeginCapture(P->cap, cudaStreamCaptureModeThreadLocal));
+            st = enqueue_frame(P, P->cap);
+            cudaGraph_t graph = nullptr;
+            cudaError_t e = cudaStreamEndCapture(P->cap, &graph);
+            if (st != SS_OK) {
+                if (graph) cudaGraphDestroy(graph);
+                return st;
+            }
+            if (e != cudaSuccess) {
+                set_last_error("cudaStreamEndCapture", e);
+                return SS_ERR_CUDA;
+            }
+            P->graph = graph;
+            SS_CUDA_TRY(cudaGraphInstantiate(&P->exec, P->graph, 0));
+        }
+        SS_CUDA_TRY(cudaGraphLaunch(P->exec, s));
+    } else {
+        st = enqueue_frame(P, s);
+        if (st != SS_OK) return st;
+    }
+    g->host_epoch++;
+    P->frames++;
+    return SS_OK;
+}
+
+ss_status ss_pipeline_stats(ss_pipeline *P, int32_t inliers[4], float rmse[4], ss_stream_t stream) {
+    if (!P || !inliers || !rmse) return SS_ERR_ARG;
+    TrackState h;
+    SS_CUDA_TRY(cudaMemcpyAsync(&h, P->st, sizeof(h), cudaMemcpyDeviceToHost, (cudaStream_t)stream));
+    SS_CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
+    for (int l = 0; l < 4; l++) {
+        inliers[l] = h.inliers[l];
+        rmse[l] = h.rmse[l];
+    }
+    return SS_OK;
+}
+
+}  // extern "C"

@@ -5,6 +5,8 @@
 // of one row, which stay coherent through the block-skip loop). The unit ray
 // table normPcd (createNormPcdTag, :717-722) is recomputed in registers
 // instead of being read from a 3.7 MB image.
+#include <climits>
+
 #include "ss_grid_impl.cuh"
 
 namespace ss {
@@ -176,6 +178,188 @@ __global__ void __launch_bounds__(256) raycast_ref_kernel(GridView g, Mat34 Er, 
     }
 }
 
+
+// ------------------------------------------------------------------------
+// Trilinear raycast (the per-frame pipeline's model view): depth, vertex and
+// normal maps with at most max_steps march steps per ray.
+//
+// Ray of pixel (i, j): direction ((j - cj)/fx, (i - ci)/fy, 1) in the camera
+// (not normalised, so the ray parameter t is the camera-frame depth). Steps:
+//  * the ray point lies in a block that is not allocated: jump to the exit of
+//    that block's box (empty-space skip);
+//  * the trilinear TSDF sample is invalid (a corner voxel unobserved or in a
+//    missing block): advance one voxel;
+//  * the sample is positive: advance max(vl, 0.8 f) (f in metres);
+//  * the sample is negative after a positive one: zero crossing; two
+//    regula-falsi refinements on the bracket, then the hit;
+//  * the sample is negative with no positive predecessor: no hit (back face).
+// Every sample or skip counts as one step. The normal is the normalised
+// gradient of the trilinear interpolant at the hit (world frame, pointing
+// out of the surface). Outputs: vmap[i][j] = (x, y, z world, depth) and
+// nmap[i][j] = (nx, ny, nz, 0); misses are all-zero.
+struct TriSample {
+    bool valid;
+    float f;
+    float gx, gy, gz;  // d f / d (world x, y, z)
+};
+
+struct BlockCache {
+    int x, y, z, bucket;
+};
+
+template <int kStorage>
+__device__ __forceinline__ float2 voxel_sw(const GridView &g, int bucket, int v) {
+    const size_t vi = (size_t)bucket * kBlockVoxels + v;
+    if (kStorage == SS_STORAGE_F32) {
+        return __ldg(g.vox32 + vi);
+    } else {
+        const uint32_t word = __ldg(g.vox16 + vi);
+        return make_float2(__half2float(__ushort_as_half((unsigned short)(word & 0xffffu))) * g.trunc,
+                           (float)(word >> 16));
+    }
+}
+
+__device__ __forceinline__ int cached_lookup(const GridView &g, BlockCache &c, int bx, int by, int bz) {
+    if (bx == c.x && by == c.y && bz == c.z) return c.bucket;
+    c.x = bx;
+    c.y = by;
+    c.z = bz;
+    c.bucket = packable(bx, by, bz) ? table_find(g, prime_hash(bx, by, bz)) : -1;
+    return c.bucket;
+}
+
+template <int kStorage, bool kGrad>
+__device__ __forceinline__ TriSample trilinear(const GridView &g, float px, float py, float pz, float inv_vl,
+                                               BlockCache &c) {
+    TriSample r{false, 0.f, 0.f, 0.f, 0.f};
+    const float ux = fmaf(px, inv_vl, -0.5f), uy = fmaf(py, inv_vl, -0.5f), uz = fmaf(pz, inv_vl, -0.5f);
+    const float fx0 = floorf(ux), fy0 = floorf(uy), fz0 = floorf(uz);
+    const int ix = (int)fx0, iy = (int)fy0, iz = (int)fz0;
+    const float ax = ux - fx0, ay = uy - fy0, az = uz - fz0;
+    float s[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        const int vx = ix + (k & 1), vy = iy + ((k >> 1) & 1), vz = iz + (k >> 2);
+        const int bx = vx >> 3, by = vy >> 3, bz = vz >> 3;  // floor(v / 8)
+        const int b = cached_lookup(g, c, bx, by, bz);
+        if (b < 0) return r;
+        const float2 sw = voxel_sw<kStorage>(g, b, (vx & 7) + 8 * (vy & 7) + 64 * (vz & 7));
+        if (!(sw.y > 0.f)) return r;
+        s[k] = sw.x;
+    }
+    // lerp along x, then y, then z
+    const float s00 = fmaf(ax, s[1] - s[0], s[0]), s10 = fmaf(ax, s[3] - s[2], s[2]);
+    const float s01 = fmaf(ax, s[5] - s[4], s[4]), s11 = fmaf(ax, s[7] - s[6], s[6]);
+    const float s0 = fmaf(ay, s10 - s00, s00), s1 = fmaf(ay, s11 - s01, s01);
+    r.valid = true;
+    r.f = fmaf(az, s1 - s0, s0);
+    if (kGrad) {
+        const float dx00 = s[1] - s[0], dx10 = s[3] - s[2], dx01 = s[5] - s[4], dx11 = s[7] - s[6];
+        const float dx0 = fmaf(ay, dx10 - dx00, dx00), dx1 = fmaf(ay, dx11 - dx01, dx01);
+        r.gx = fmaf(az, dx1 - dx0, dx0) * inv_vl;
+        r.gy = fmaf(az, s11 - s01 - (s10 - s00), s10 - s00) * inv_vl;
+        r.gz = (s1 - s0) * inv_vl;
+    }
+    return r;
+}
+
+template <int kStorage>
+__global__ void __launch_bounds__(256) raycast_maps_kernel(GridView g, Mat34 T, const FramePose *__restrict__ pose,
+                                                           int max_steps, float t_min, float t_max,
+                                                           float4 *__restrict__ vmap, float4 *__restrict__ nmap) {
+    const int j = blockIdx.x * 32 + threadIdx.x;
+    const int i = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= g.resi || j >= g.resj) return;
+    if (pose) {
+#pragma unroll
+        for (int k = 0; k < 12; k++) T.m[k] = __ldg(&pose->E.m[k]);
+    }
+    const float dcx = ((float)j - g.in.cj) / g.in.fx, dcy = ((float)i - g.in.ci) / g.in.fy;
+    const float dx = fmaf(T.m[0], dcx, fmaf(T.m[1], dcy, T.m[2]));
+    const float dy = fmaf(T.m[4], dcx, fmaf(T.m[5], dcy, T.m[6]));
+    const float dz = fmaf(T.m[8], dcx, fmaf(T.m[9], dcy, T.m[10]));
+    const float ox = T.m[3], oy = T.m[7], oz = T.m[11];
+    const float inv_len = rsqrtf(fmaf(dx, dx, fmaf(dy, dy, dz * dz)));  // world length of dt = 1
+    const float vl = g.vl, inv_vl = 1.f / g.vl, inv_vbl = 1.f / g.vbl;
+    const float rdx = 1.f / dx, rdy = 1.f / dy, rdz = 1.f / dz;
+
+    BlockCache cache{INT_MIN, INT_MIN, INT_MIN, -1};
+    float t = t_min, t_prev = 0.f, f_prev = 0.f;
+    bool prev_valid = false, hit = false;
+    int steps = 0;
+    while (steps < max_steps && t < t_max) {
+        const float px = fmaf(t, dx, ox), py = fmaf(t, dy, oy), pz = fmaf(t, dz, oz);
+        const int bx = (int)floorf(px * inv_vbl), by = (int)floorf(py * inv_vbl), bz = (int)floorf(pz * inv_vbl);
+        steps++;
+        if (cached_lookup(g, cache, bx, by, bz) < 0) {
+            // exit of this block's box along the ray
+            const float ex = ((float)(bx + (dx > 0.f)) * g.vbl - ox) * rdx;
+            const float ey = ((float)(by + (dy > 0.f)) * g.vbl - oy) * rdy;
+            const float ez = ((float)(bz + (dz > 0.f)) * g.vbl - oz) * rdz;
+            const float te = fminf(fminf(dx != 0.f ? ex : INFINITY, dy != 0.f ? ey : INFINITY),
+                                   dz != 0.f ? ez : INFINITY);
+            t = fmaxf(te, t) + 1e-4f * vl * inv_len;
+            prev_valid = false;
+            continue;
+        }
+        const TriSample sm = trilinear<kStorage, false>(g, px, py, pz, inv_vl, cache);
+        if (!sm.valid) {
+            prev_valid = false;
+            t += vl * inv_len;
+            continue;
+        }
+        if (sm.f < 0.f) {
+            if (prev_valid && f_prev > 0.f) {
+                float ta = t_prev, fa = f_prev, tb = t, fb = sm.f;
+                for (int r = 0; r < 2; r++) {
+                    const float tc = ta + (tb - ta) * fa / (fa - fb);
+                    const TriSample q = trilinear<kStorage, false>(g, fmaf(tc, dx, ox), fmaf(tc, dy, oy),
+                                                                   fmaf(tc, dz, oz), inv_vl, cache);
+                    if (!q.valid) break;
+                    if (q.f > 0.f) {
+                        ta = tc;
+                        fa = q.f;
+                    } else {
+                        tb = tc;
+                        fb = q.f;
+                    }
+                }
+                t = ta + (tb - ta) * fa / (fa - fb);
+                hit = true;
+            }
+            break;
+        }
+        prev_valid = true;
+        t_prev = t;
+        f_prev = sm.f;
+        t += fmaxf(vl, 0.8f * sm.f) * inv_len;
+    }
+    const size_t pix = (size_t)i * g.resj + j;
+    float4 v = make_float4(0.f, 0.f, 0.f, 0.f), n = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (hit) {
+        const float px = fmaf(t, dx, ox), py = fmaf(t, dy, oy), pz = fmaf(t, dz, oz);
+        const TriSample q = trilinear<kStorage, true>(g, px, py, pz, inv_vl, cache);
+        const float gn = q.valid ? sqrtf(q.gx * q.gx + q.gy * q.gy + q.gz * q.gz) : 0.f;
+        if (gn > 0.f) {
+            v = make_float4(px, py, pz, t);
+            n = make_float4(q.gx / gn, q.gy / gn, q.gz / gn, 0.f);
+        }
+    }
+    vmap[pix] = v;
+    nmap[pix] = n;
+}
+
+ss_status launch_raycast_maps(ss_grid *g, const Mat34 &T, const FramePose *dpose, int max_steps, float t_min,
+                              float t_max, float4 *vmap, float4 *nmap, cudaStream_t s) {
+    const dim3 blk(32, 8), grid((g->p.resj + 31) / 32, (g->p.resi + 7) / 8);
+    if (g->p.storage == SS_STORAGE_F32)
+        raycast_maps_kernel<SS_STORAGE_F32><<<grid, blk, 0, s>>>(g->v, T, dpose, max_steps, t_min, t_max, vmap, nmap);
+    else
+        raycast_maps_kernel<SS_STORAGE_F16><<<grid, blk, 0, s>>>(g->v, T, dpose, max_steps, t_min, t_max, vmap, nmap);
+    SS_LAUNCH_CHECK();
+    return SS_OK;
+}
+
 }  // namespace ss
 
 using namespace ss;
@@ -195,4 +379,14 @@ extern "C" ss_status ss_raycast(ss_grid *g, const float extr[16], float *ray_pcd
         raycast_ref_kernel<SS_STORAGE_F16><<<grid, blk, 0, s>>>(g->v, Er, ray_pcd, ray_color);
     SS_LAUNCH_CHECK();
     return SS_OK;
+}
+
+extern "C" ss_status ss_raycast_maps(ss_grid *g, const float extr[16], int32_t max_steps, float t_min, float t_max,
+                                     float *vertex_depth, float *normal, ss_stream_t stream) {
+    if (!g || !extr || !vertex_depth || !normal || max_steps <= 0 || !(t_max > t_min)) return SS_ERR_ARG;
+    if (!g->intr_set) return SS_ERR_STATE;
+    for (int k = 0; k < 16; k++)
+        if (!std::isfinite(extr[k])) return SS_ERR_ARG;
+    return launch_raycast_maps(g, mat34_from(extr), nullptr, max_steps, t_min, t_max, (float4 *)vertex_depth,
+                               (float4 *)normal, (cudaStream_t)stream);
 }

@@ -1,0 +1,287 @@
+// ss_track.cu — frame-to-model point-to-plane Gauss-Newton tracking.
+//
+// The reference tracks with keypoints and aligns frames in post-processing
+// with kokkosICP (src/postprocessing/kokkosICP.cpp); the per-frame
+// integrate -> raycast -> ICP pipeline tracks each new depth frame against
+// the raycast model view instead (projective association, point-to-plane
+// residual), over a 3-level pyramid of the source depth.
+//
+// One kernel per iteration. Source pixels of level l are the level-0 pixels
+// (i 2^l, j 2^l) back-projected with the level-0 intrinsics (no pyramid
+// images are built). Each thread accumulates the 21 + 6 + 2 normal-equation
+// sums in FP32 with Kahan compensation; warps combine (sum, compensation)
+// pairs with TwoSum through shuffles, CTAs through shared memory, and the
+// last CTA to finish reduces the CTA slots in FP64 in a fixed order, solves
+// the 6x6 system by Cholesky in FP64 and applies the SE(3) update in FP64.
+// No host synchronisation between iterations, levels or frames.
+#include "ss_grid_impl.cuh"
+#include "ss_track.cuh"
+
+namespace ss {
+
+constexpr int kTrackSums = 29;  // JtJ upper triangle (21), Jtr (6), r^2, count
+
+__device__ __forceinline__ void kahan_add(float &s, float &c, float x) {
+    const float y = x - c;
+    const float t = s + y;
+    c = (t - s) - y;
+    s = t;
+}
+
+// (s1 + c1) + (s2 + c2) with the rounding error of s1 + s2 kept (TwoSum).
+__device__ __forceinline__ void pair_add(float &s, float &c, float s2, float c2) {
+    const float t = s + s2;
+    const float bp = t - s;
+    const float e = (s - (t - bp)) + (s2 - bp);
+    s = t;
+    c = c + c2 - e;  // compensation holds the negated error (kahan convention: value = s - c)
+}
+
+__device__ void mat_from_T(const double *T, float *m) {
+    for (int k = 0; k < 12; k++) m[k] = (float)T[k];
+}
+
+// Rigid inverse of a 4x4 double pose: [R^T, -R^T t].
+__device__ void rigid_inverse(const double *T, double *Ti) {
+    for (int r = 0; r < 3; r++) {
+        for (int c = 0; c < 3; c++) Ti[r * 4 + c] = T[c * 4 + r];
+        Ti[r * 4 + 3] = -(T[0 * 4 + r] * T[3] + T[1 * 4 + r] * T[7] + T[2 * 4 + r] * T[11]);
+    }
+    Ti[12] = Ti[13] = Ti[14] = 0.0;
+    Ti[15] = 1.0;
+}
+
+// FramePose of a double pose: float E, float inverse, normalized z column.
+__device__ void write_frame_pose(const double *T, FramePose *fp) {
+    double Ti[16];
+    rigid_inverse(T, Ti);
+    for (int k = 0; k < 12; k++) {
+        fp->E.m[k] = (float)T[k];
+        fp->Einv.m[k] = (float)Ti[k];
+    }
+    const float ex = (float)T[2], ey = (float)T[6], ez = (float)T[10];
+    const float len = sqrtf(ex * ex + ey * ey + ez * ez);
+    fp->Ez[0] = ex / len;
+    fp->Ez[1] = ey / len;
+    fp->Ez[2] = ez / len;
+    fp->pad = 0.f;
+}
+
+// exp of an se(3) twist (omega, upsilon) in FP64, left-multiplied onto T.
+__device__ void se3_left_update(const double *xi, double *T) {
+    const double wx = xi[0], wy = xi[1], wz = xi[2];
+    const double th2 = wx * wx + wy * wy + wz * wz, th = sqrt(th2);
+    double A, B, C;
+    if (th < 1e-8) {
+        A = 1.0 - th2 / 6.0;
+        B = 0.5 - th2 / 24.0;
+        C = 1.0 / 6.0 - th2 / 120.0;
+    } else {
+        A = sin(th) / th;
+        B = (1.0 - cos(th)) / th2;
+        C = (th - sin(th)) / (th2 * th);
+    }
+    const double K[9] = {0, -wz, wy, wz, 0, -wx, -wy, wx, 0};
+    double K2[9];
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 3; c++) K2[r * 3 + c] = K[r * 3] * K[c] + K[r * 3 + 1] * K[3 + c] + K[r * 3 + 2] * K[6 + c];
+    double R[9], V[9];
+    for (int k = 0; k < 9; k++) {
+        const double I = (k % 4 == 0) ? 1.0 : 0.0;
+        R[k] = I + A * K[k] + B * K2[k];
+        V[k] = I + B * K[k] + C * K2[k];
+    }
+    const double t[3] = {V[0] * xi[3] + V[1] * xi[4] + V[2] * xi[5], V[3] * xi[3] + V[4] * xi[4] + V[5] * xi[5],
+                         V[6] * xi[3] + V[7] * xi[4] + V[8] * xi[5]};
+    double N[16];
+    for (int r = 0; r < 3; r++) {
+        for (int c = 0; c < 4; c++)
+            N[r * 4 + c] = R[r * 3] * T[c] + R[r * 3 + 1] * T[4 + c] + R[r * 3 + 2] * T[8 + c] + (c == 3 ? t[r] : 0.0);
+    }
+    for (int k = 0; k < 12; k++) T[k] = N[k];
+    T[12] = T[13] = T[14] = 0.0;
+    T[15] = 1.0;
+}
+
+// Cholesky solve of A x = b (6x6 SPD, FP64). Returns false if A is not SPD.
+__device__ bool cholesky6(const double *A, const double *b, double *x) {
+    double L[36];
+    for (int k = 0; k < 36; k++) L[k] = 0.0;
+    for (int i = 0; i < 6; i++) {
+        for (int j = 0; j <= i; j++) {
+            double s = A[i * 6 + j];
+            for (int k = 0; k < j; k++) s -= L[i * 6 + k] * L[j * 6 + k];
+            if (i == j) {
+                if (!(s > 1e-12)) return false;
+                L[i * 6 + i] = sqrt(s);
+            } else {
+                L[i * 6 + j] = s / L[j * 6 + j];
+            }
+        }
+    }
+    double y[6];
+    for (int i = 0; i < 6; i++) {
+        double s = b[i];
+        for (int k = 0; k < i; k++) s -= L[i * 6 + k] * y[k];
+        y[i] = s / L[i * 6 + i];
+    }
+    for (int i = 5; i >= 0; i--) {
+        double s = y[i];
+        for (int k = i + 1; k < 6; k++) s -= L[k * 6 + i] * x[k];
+        x[i] = s / L[i * 6 + i];
+    }
+    return true;
+}
+
+// Start of a frame: the model maps were raycast at the last pose T, so
+// Tprev = T, and tracking starts from T.
+__global__ void track_begin_kernel(TrackState *st) {
+    if (threadIdx.x != 0) return;
+    double Ti[16];
+    for (int k = 0; k < 16; k++) st->Tprev[k] = st->T[k];
+    rigid_inverse(st->Tprev, Ti);
+    for (int k = 0; k < 12; k++) st->Tprev_inv[k] = (float)Ti[k];
+    mat_from_T(st->T, st->Tf);
+    st->ticket = 0;
+    st->converged_level = -1;
+    for (int l = 0; l < kMaxLevels; l++) {
+        st->inliers[l] = 0;
+        st->rmse[l] = 0.f;
+    }
+}
+
+__global__ void pose_prep_kernel(TrackState *st) {
+    if (threadIdx.x == 0) write_frame_pose(st->T, &st->pose);
+}
+
+__global__ void __launch_bounds__(256) track_iter_kernel(const uint16_t *__restrict__ depth, int rows, int cols,
+                                                         Intr in, const float4 *__restrict__ vmap,
+                                                         const float4 *__restrict__ nmap, TrackState *st,
+                                                         float2 *__restrict__ partials, int level, float dist2,
+                                                         float rmin, float dmax) {
+    if (*(volatile int *)&st->converged_level == level) return;
+    __shared__ float2 red[8][kTrackSums];
+    __shared__ bool last;
+    float T[12], Pi[12];
+#pragma unroll
+    for (int k = 0; k < 12; k++) {
+        T[k] = st->Tf[k];
+        Pi[k] = st->Tprev_inv[k];
+    }
+    float s[kTrackSums], c[kTrackSums];
+#pragma unroll
+    for (int k = 0; k < kTrackSums; k++) s[k] = c[k] = 0.f;
+
+    const int lr = (rows + (1 << level) - 1) >> level, lc = (cols + (1 << level) - 1) >> level;
+    const int npix = lr * lc;
+    const float rfx = 1.f / in.fx, rfy = 1.f / in.fy;
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < npix; p += gridDim.x * blockDim.x) {
+        const int i = (p / lc) << level, j = (p % lc) << level;
+        const float d = (float)__ldg(depth + (size_t)i * cols + j) * 1e-3f;
+        if (!(d > rmin) || !(d < dmax)) continue;
+        const float cx = ((float)j - in.cj) * rfx * d, cy = ((float)i - in.ci) * rfy * d;
+        const float wx = fmaf(T[0], cx, fmaf(T[1], cy, fmaf(T[2], d, T[3])));
+        const float wy = fmaf(T[4], cx, fmaf(T[5], cy, fmaf(T[6], d, T[7])));
+        const float wz = fmaf(T[8], cx, fmaf(T[9], cy, fmaf(T[10], d, T[11])));
+        const float qx = fmaf(Pi[0], wx, fmaf(Pi[1], wy, fmaf(Pi[2], wz, Pi[3])));
+        const float qy = fmaf(Pi[4], wx, fmaf(Pi[5], wy, fmaf(Pi[6], wz, Pi[7])));
+        const float qz = fmaf(Pi[8], wx, fmaf(Pi[9], wy, fmaf(Pi[10], wz, Pi[11])));
+        if (!(qz > 1e-3f)) continue;
+        const float rq = 1.f / qz;
+        const int ii = (int)floorf(fmaf(qy * in.fy, rq, in.ci) + 0.5f);
+        const int jj = (int)floorf(fmaf(qx * in.fx, rq, in.cj) + 0.5f);
+        if (ii < 0 || ii >= rows || jj < 0 || jj >= cols) continue;
+        const float4 n = __ldg(nmap + (size_t)ii * cols + jj);
+        if (n.x == 0.f && n.y == 0.f && n.z == 0.f) continue;
+        const float4 v = __ldg(vmap + (size_t)ii * cols + jj);
+        const float ex = wx - v.x, ey = wy - v.y, ez = wz - v.z;
+        if (ex * ex + ey * ey + ez * ez > dist2) continue;
+        const float r = n.x * ex + n.y * ey + n.z * ez;
+        const float J[6] = {wy * n.z - wz * n.y, wz * n.x - wx * n.z, wx * n.y - wy * n.x, n.x, n.y, n.z};
+        int q = 0;
+#pragma unroll
+        for (int a = 0; a < 6; a++)
+#pragma unroll
+            for (int b = a; b < 6; b++) kahan_add(s[q], c[q], J[a] * J[b]), q++;
+#pragma unroll
+        for (int a = 0; a < 6; a++) kahan_add(s[21 + a], c[21 + a], J[a] * r);
+        kahan_add(s[27], c[27], r * r);
+        s[28] += 1.f;  // counts stay exact far below 2^24
+    }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < kTrackSums; k++) {
+        float a = s[k], b = c[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const float a2 = __shfl_down_sync(0xffffffffu, a, o), b2 = __shfl_down_sync(0xffffffffu, b, o);
+            pair_add(a, b, a2, b2);
+        }
+        if (lane == 0) red[wid][k] = make_float2(a, b);
+    }
+    __syncthreads();
+    if (threadIdx.x < kTrackSums) {
+        float a = 0.f, b = 0.f;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) pair_add(a, b, red[w][threadIdx.x].x, red[w][threadIdx.x].y);
+        partials[(size_t)blockIdx.x * kTrackSums + threadIdx.x] = make_float2(a, b);
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(&st->ticket, 1) == (int)gridDim.x - 1;
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    __shared__ double tot[kTrackSums];
+    if (threadIdx.x < kTrackSums) {
+        double a = 0.0;
+        for (unsigned b = 0; b < gridDim.x; b++) {
+            const float2 v = __ldcg(partials + (size_t)b * kTrackSums + threadIdx.x);
+            a += (double)v.x - (double)v.y;
+        }
+        tot[threadIdx.x] = a;
+    }
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    st->ticket = 0;
+    const double n = tot[28];
+    st->inliers[level] = (int)n;
+    st->rmse[level] = n > 0 ? (float)sqrt(tot[27] / n) : 0.f;
+    if (n < 60.0) return;  // too few correspondences: keep the pose
+    double A[36], b[6], x[6];
+    int q = 0;
+    for (int r = 0; r < 6; r++)
+        for (int cc = r; cc < 6; cc++) {
+            A[r * 6 + cc] = A[cc * 6 + r] = tot[q++];
+        }
+    for (int r = 0; r < 6; r++) b[r] = -tot[21 + r];
+    if (!cholesky6(A, b, x)) return;
+    se3_left_update(x, st->T);
+    mat_from_T(st->T, st->Tf);
+    const double step = sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2] + x[3] * x[3] + x[4] * x[4] + x[5] * x[5]);
+    if (step < 1e-7) st->converged_level = level;
+}
+
+// Host-side launch of one frame's tracking: begin, levels coarse to fine,
+// then the FramePose of the result.
+ss_status launch_track(const TrackLaunch &L, cudaStream_t s) {
+    track_begin_kernel<<<1, 32, 0, s>>>(L.state);
+    SS_LAUNCH_CHECK();
+    for (int level = L.levels - 1; level >= 0; level--) {
+        for (int it = 0; it < L.iters[level]; it++) {
+            track_iter_kernel<<<L.ctas, 256, 0, s>>>(L.depth, L.rows, L.cols, L.in, L.vmap, L.nmap, L.state, L.partials,
+                                                     level, L.dist[level] * L.dist[level], L.rmin, L.dmax);
+            SS_LAUNCH_CHECK();
+        }
+    }
+    pose_prep_kernel<<<1, 32, 0, s>>>(L.state);
+    SS_LAUNCH_CHECK();
+    return SS_OK;
+}
+
+ss_status launch_pose_prep(TrackState *st, cudaStream_t s) {
+    pose_prep_kernel<<<1, 32, 0, s>>>(st);
+    SS_LAUNCH_CHECK();
+    return SS_OK;
+}
+
+}  // namespace ss

@@ -1,0 +1,42 @@
+// ss_track.cuh — device state of the frame-to-model tracker.
+#pragma once
+
+#include "ss_internal.cuh"
+
+namespace ss {
+
+constexpr int kMaxLevels = 4;
+
+// Lives in device memory for the life of a pipeline. T is the current pose
+// estimate (camera -> world, FP64); pose is its float FramePose, consumed by
+// integrate and raycast of the same frame.
+struct TrackState {
+    double T[16];
+    double Tprev[16];    // pose of the model maps (previous frame)
+    float Tf[12];        // float copy of T for the iteration kernel
+    float Tprev_inv[12]; // world -> model camera
+    FramePose pose;
+    int ticket;
+    int converged_level;
+    int inliers[kMaxLevels];
+    float rmse[kMaxLevels];
+};
+
+struct TrackLaunch {
+    const uint16_t *depth;
+    int rows, cols;
+    Intr in;
+    const float4 *vmap, *nmap;
+    TrackState *state;
+    float2 *partials;
+    int ctas;
+    int levels;
+    int iters[kMaxLevels];
+    float dist[kMaxLevels];
+    float rmin, dmax;
+};
+
+ss_status launch_track(const TrackLaunch &L, cudaStream_t s);
+ss_status launch_pose_prep(TrackState *st, cudaStream_t s);
+
+}  // namespace ss
