@@ -192,6 +192,9 @@ ss_status ss_pipeline_destroy(ss_pipeline *p);
 ss_status ss_pipeline_set_pose(ss_pipeline *p, const double T[16], ss_stream_t s);
 /* Copies the current pose to the host. Synchronises s. */
 ss_status ss_pipeline_get_pose(ss_pipeline *p, double T[16], ss_stream_t s);
+/* Enqueues a copy of the current pose into T (pinned host or device memory)
+ * on s without synchronising; valid once s reaches that point. */
+ss_status ss_pipeline_read_pose(ss_pipeline *p, double T[16], ss_stream_t s);
 /* Device input buffer [resi][resj] u16; frames written there need no copy. */
 ss_status ss_pipeline_input(ss_pipeline *p, uint16_t **depth);
 /* Device model maps of the last frame (layout of ss_raycast_maps). */
@@ -201,6 +204,17 @@ ss_status ss_pipeline_maps(ss_pipeline *p, float **vertex_depth, float **normal)
  * it; else integrate at the current pose and raycast. depth may be a device
  * or host pointer (copied into the input buffer on s). No host sync. */
 ss_status ss_pipeline_frame(ss_pipeline *p, const uint16_t *depth, int32_t track, ss_stream_t s);
+/* Copies the model maps into caller buffers (device or host), stream-ordered. */
+ss_status ss_pipeline_copy_maps(ss_pipeline *p, float *vertex_depth, float *normal, ss_stream_t s);
+/* Stage profiling of tracked frames run without the graph: when enabled,
+ * events bracket track, collect, fuse, finalize and raycast of each frame;
+ * ss_pipeline_stage_ms synchronises s and returns the summed milliseconds
+ * per stage, the number of profiled frames and (counters, may be NULL) the
+ * raycast's summed hash finds, voxel loads, march steps and hits (enabling
+ * resets them all). */
+ss_status ss_pipeline_profile(ss_pipeline *p, int32_t enable);
+ss_status ss_pipeline_stage_ms(ss_pipeline *p, double ms[5], int64_t *frames, int64_t counters[4],
+                               ss_stream_t s);
 /* Tracker inliers and residual RMS per level of the last tracked frame. */
 ss_status ss_pipeline_stats(ss_pipeline *p, int32_t inliers[4], float rmse[4], ss_stream_t s);
 

@@ -18,7 +18,7 @@ _LIB_PATH = _DIR / "_build" / "libss_oracle.so"
 
 
 def build(force: bool = False) -> Path:
-    srcs = list(_DIR.glob("*.cpp")) + [_DIR / "Makefile"]
+    srcs = list(_DIR.glob("*.cpp")) + list(_DIR.glob("*.h")) + [_DIR / "Makefile"]
     if force or not _LIB_PATH.exists() or _LIB_PATH.stat().st_mtime < max(p.stat().st_mtime for p in srcs):
         subprocess.run(["make", "-s", "-B" if force else "-s", "-C", str(_DIR)], check=True)
     return _LIB_PATH
@@ -44,6 +44,13 @@ for name, res, args in [
     ("orc_inverse4f", None, [_p, _p]),
     ("orc_mat4_vec4", None, [_p, _p, _p]),
     ("orc_threads", _i, []),
+    ("orm_grid_new", _p, [_f, _f, _i, _i, _f, _f, _f, _f, C.c_double]),
+    ("orm_grid_free", None, [_p]),
+    ("orm_grid_count", _i, [_p]),
+    ("orm_grid_fuse", _i, [_p, _p, _p, _i]),
+    ("orm_grid_export", _i, [_p, _i, _p, _p, _p, _p]),
+    ("orm_raycast", None, [_p, _p, _i, C.c_double, C.c_double, _p, _p, _p]),
+    ("orm_track", _i, [_p, _i, _i, _f, _f, _f, _f, _p, _p, _p, _p, _i, _p, _p, C.c_double, C.c_double]),
 ]:
     fn = getattr(_lib, name)
     fn.restype = res
@@ -168,3 +175,55 @@ def mat4_vec4(M, v):
 
 def threads() -> int:
     return _lib.orc_threads()
+
+
+class MethodGrid64:
+    """FP64 oracle of the per-frame method (FP64 TSDF, trilinear raycast)."""
+
+    def __init__(self, vl, trunc, resi, resj, intr=(525.0, 525.0, 319.5, 239.5), max_weight=0.0):
+        self.resi, self.resj, self.intr = resi, resj, intr
+        self._h = _lib.orm_grid_new(vl, trunc, resi, resj, *map(float, intr), float(max_weight))
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            _lib.orm_grid_free(self._h)
+            self._h = None
+
+    def fuse(self, depth, T, deint=False) -> int:
+        depth = np.ascontiguousarray(depth, np.uint16)
+        T = np.ascontiguousarray(T, np.float64)
+        return _lib.orm_grid_fuse(self._h, _ptr(depth), _ptr(T), int(deint))
+
+    def count(self) -> int:
+        return _lib.orm_grid_count(self._h)
+
+    def export(self) -> dict:
+        n = self.count()
+        keys = np.zeros(n, np.uint64)
+        coords = np.zeros((n, 3), np.int32)
+        sdf = np.zeros((n, 512), np.float64)
+        w = np.zeros((n, 512), np.float64)
+        _lib.orm_grid_export(self._h, n, _ptr(keys), _ptr(coords), _ptr(sdf), _ptr(w))
+        return dict(keys=keys, coords=coords, sdf=sdf, w=w)
+
+    def raycast(self, T, max_steps=128, t_min=0.2, t_max=10.0):
+        vmap = np.zeros((self.resi, self.resj, 4), np.float64)
+        nmap = np.zeros((self.resi, self.resj, 4), np.float64)
+        steps = np.zeros((self.resi, self.resj), np.int32)
+        _lib.orm_raycast(self._h, _ptr(np.ascontiguousarray(T, np.float64)), int(max_steps), float(t_min),
+                         float(t_max), _ptr(vmap), _ptr(nmap), _ptr(steps))
+        return vmap, nmap, steps
+
+
+def track64(depth, vmap, nmap, Tprev, T0, intr=(525.0, 525.0, 319.5, 239.5), levels=3, iters=(10, 5, 4),
+            dist=(0.06, 0.10, 0.15), rmin=0.2, dmax=10.0):
+    """FP64 frame-to-model point-to-plane Gauss-Newton (the method of the GPU tracker)."""
+    depth = np.ascontiguousarray(depth, np.uint16)
+    rows, cols = depth.shape
+    T = np.ascontiguousarray(T0, np.float64).copy()
+    it = np.ascontiguousarray(list(iters) + [0] * (4 - len(iters)), np.int32)
+    ds = np.ascontiguousarray(list(dist) + [0.2] * (4 - len(dist)), np.float64)
+    n = _lib.orm_track(_ptr(depth), rows, cols, *map(float, intr), _ptr(np.ascontiguousarray(vmap, np.float64)),
+                       _ptr(np.ascontiguousarray(nmap, np.float64)), _ptr(np.ascontiguousarray(Tprev, np.float64)),
+                       _ptr(T), int(levels), _ptr(it), _ptr(ds), float(rmin), float(dmax))
+    return T, n

@@ -1,0 +1,455 @@
+// ss_oracle_method.cpp — FP64 oracle of the per-frame method.
+//
+// TEST INFRASTRUCTURE ONLY (see ss_oracle.cpp's header). This is the FP64
+// restatement of the method the GPU pipeline runs (FP64 TSDF, trilinear
+// raycast with at most max_steps steps, frame-to-model point-to-plane
+// Gauss-Newton over a 3-level pyramid), against which the FP32 and FP16 GPU
+// forms state their errors. Block allocation is the reference's (float,
+// GPUVoxelGrid.cpp:471-514, as in ss_oracle.cpp), so both sides fuse into the
+// same set of blocks; everything after allocation is double precision.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <unordered_map>
+#include <vector>
+
+#include "ss_ref_math.h"
+
+namespace {
+
+using namespace orc;
+
+struct Block64 {
+    int vb[3];
+    double sdf[kVox];
+    double w[kVox];
+};
+
+struct Grid64 {
+    float vl, vbl, trunc;  // float parameters of the allocation
+    int resi, resj;
+    float fx, fy, cx, cy, ci, cj;
+    double max_weight;
+    float rmin = 0.2f;
+    std::unordered_map<uint64_t, int> map;
+    std::vector<Block64 *> blocks;
+};
+
+struct D3 {
+    double x, y, z;
+};
+
+inline D3 dxform(const double *T, D3 p) {
+    return {T[0] * p.x + T[1] * p.y + T[2] * p.z + T[3], T[4] * p.x + T[5] * p.y + T[6] * p.z + T[7],
+            T[8] * p.x + T[9] * p.y + T[10] * p.z + T[11]};
+}
+
+void rigid_inverse(const double *T, double *Ti) {
+    for (int r = 0; r < 3; r++) {
+        for (int c = 0; c < 3; c++) Ti[r * 4 + c] = T[c * 4 + r];
+        Ti[r * 4 + 3] = -(T[r] * T[3] + T[4 + r] * T[7] + T[8 + r] * T[11]);
+    }
+    Ti[12] = Ti[13] = Ti[14] = 0;
+    Ti[15] = 1;
+}
+
+// Reference block allocation with the float pose (the GPU fuses with the float
+// cast of the same pose). Returns touched block indices.
+std::vector<int> collect64(Grid64 &g, const uint16_t *depth, const float *E) {
+    std::vector<int> touched;
+    std::unordered_map<int, uint64_t> frame;
+    for (int i = 0; i < g.resi; i++)
+        for (int j = 0; j < g.resj; j++) {
+            const float d = (float)(depth[i * g.resj + j]) / 1000;
+            V3 p{(j - g.cj) / g.fx * d, (i - g.ci) / g.fy * d, d};
+            if (!(p.z > g.rmin)) continue;
+            V3 pt = xform(E, p);
+            V3 lo = sub(pt, V3{g.trunc, g.trunc, g.trunc}), hi = add(pt, V3{g.trunc, g.trunc, g.trunc});
+            for (int x = idx_rule(lo.x, g.vbl); x <= idx_rule(hi.x, g.vbl); x++)
+                for (int y = idx_rule(lo.y, g.vbl); y <= idx_rule(hi.y, g.vbl); y++)
+                    for (int z = idx_rule(lo.z, g.vbl); z <= idx_rule(hi.z, g.vbl); z++) {
+                        if (!packable(x, y, z)) continue;
+                        const uint64_t key = prime_hash(x, y, z), pk = pack_coords(x, y, z);
+                        auto it = g.map.find(key);
+                        int idx;
+                        if (it == g.map.end()) {
+                            idx = (int)g.blocks.size();
+                            Block64 *b = new Block64;
+                            std::memset(b, 0, sizeof(Block64));
+                            g.blocks.push_back(b);
+                            g.map.emplace(key, idx);
+                        } else {
+                            idx = it->second;
+                        }
+                        auto f = frame.find(idx);
+                        if (f == frame.end()) {
+                            frame.emplace(idx, pk);
+                            touched.push_back(idx);
+                        } else if (pk > f->second) {
+                            f->second = pk;
+                        }
+                    }
+        }
+    for (int idx : touched) {
+        I3 v = unpack_coords(frame[idx]);
+        g.blocks[idx]->vb[0] = v.x;
+        g.blocks[idx]->vb[1] = v.y;
+        g.blocks[idx]->vb[2] = v.z;
+    }
+    return touched;
+}
+
+const Block64 *find64(const Grid64 &g, int bx, int by, int bz) {
+    if (!packable(bx, by, bz)) return nullptr;
+    auto it = g.map.find(prime_hash(bx, by, bz));
+    return it == g.map.end() ? nullptr : g.blocks[it->second];
+}
+
+struct Sample {
+    bool valid;
+    double f, gx, gy, gz;
+};
+
+struct Cache {
+    int x = INT32_MIN, y = 0, z = 0;
+    const Block64 *b = nullptr;
+};
+
+inline const Block64 *cached(const Grid64 &g, Cache &c, int bx, int by, int bz) {
+    if (bx != c.x || by != c.y || bz != c.z) {
+        c.x = bx;
+        c.y = by;
+        c.z = bz;
+        c.b = find64(g, bx, by, bz);
+    }
+    return c.b;
+}
+
+inline int floordiv8(int v) { return v >= 0 ? v / 8 : -((-v + 7) / 8); }
+
+Sample trilinear64(const Grid64 &g, double px, double py, double pz, Cache &c) {
+    Sample r{false, 0, 0, 0, 0};
+    const double vl = g.vl;
+    const double ux = px / vl - 0.5, uy = py / vl - 0.5, uz = pz / vl - 0.5;
+    const double fx0 = std::floor(ux), fy0 = std::floor(uy), fz0 = std::floor(uz);
+    const int ix = (int)fx0, iy = (int)fy0, iz = (int)fz0;
+    const double ax = ux - fx0, ay = uy - fy0, az = uz - fz0;
+    double s[8];
+    for (int k = 0; k < 8; k++) {
+        const int vx = ix + (k & 1), vy = iy + ((k >> 1) & 1), vz = iz + (k >> 2);
+        const int bx = floordiv8(vx), by = floordiv8(vy), bz = floordiv8(vz);
+        const Block64 *b = cached(g, c, bx, by, bz);
+        if (!b) return r;
+        const int v = (vx - 8 * bx) + 8 * (vy - 8 * by) + 64 * (vz - 8 * bz);
+        if (!(b->w[v] > 0)) return r;
+        s[k] = b->sdf[v];
+    }
+    const double s00 = s[0] + ax * (s[1] - s[0]), s10 = s[2] + ax * (s[3] - s[2]);
+    const double s01 = s[4] + ax * (s[5] - s[4]), s11 = s[6] + ax * (s[7] - s[6]);
+    const double s0 = s00 + ay * (s10 - s00), s1 = s01 + ay * (s11 - s01);
+    r.valid = true;
+    r.f = s0 + az * (s1 - s0);
+    const double dx00 = s[1] - s[0], dx10 = s[3] - s[2], dx01 = s[5] - s[4], dx11 = s[7] - s[6];
+    const double dx0 = dx00 + ay * (dx10 - dx00), dx1 = dx01 + ay * (dx11 - dx01);
+    r.gx = (dx0 + az * (dx1 - dx0)) / vl;
+    r.gy = ((s10 - s00) + az * ((s11 - s01) - (s10 - s00))) / vl;
+    r.gz = (s1 - s0) / vl;
+    return r;
+}
+
+}  // namespace
+
+extern "C" {
+
+void *orm_grid_new(float vl, float trunc, int resi, int resj, float fx, float fy, float cx, float cy,
+                   double max_weight) {
+    Grid64 *g = new Grid64;
+    g->vl = vl;
+    g->vbl = kEdge * vl;
+    g->trunc = trunc;
+    g->resi = resi;
+    g->resj = resj;
+    g->fx = fx;
+    g->fy = fy;
+    g->cx = cx;
+    g->cy = cy;
+    g->ci = resi - cy;
+    g->cj = cx;
+    g->max_weight = max_weight;
+    g->map.reserve(1 << 18);
+    return g;
+}
+
+void orm_grid_free(void *h) {
+    Grid64 *g = (Grid64 *)h;
+    for (Block64 *b : g->blocks) delete b;
+    delete g;
+}
+
+int orm_grid_count(void *h) { return (int)((Grid64 *)h)->map.size(); }
+
+// FP64 integrate (deint = 0) / deintegrate (deint = 1) at pose T (double).
+int orm_grid_fuse(void *h, const uint16_t *depth, const double *T, int deint) {
+    Grid64 &g = *(Grid64 *)h;
+    float Ef[16];
+    for (int k = 0; k < 16; k++) Ef[k] = (float)T[k];
+    std::vector<int> touched = collect64(g, depth, Ef);
+    double Ti[16];
+    rigid_inverse(T, Ti);
+    const double ezn = std::sqrt(T[2] * T[2] + T[6] * T[6] + T[10] * T[10]);
+    const D3 Ez{T[2] / ezn, T[6] / ezn, T[10] / ezn};
+    const double vl = g.vl, vbl = g.vbl, trunc = g.trunc;
+#pragma omp parallel for schedule(dynamic, 8)
+    for (size_t t = 0; t < touched.size(); t++) {
+        Block64 &b = *g.blocks[touched[t]];
+        for (int v = 0; v < kVox; v++) {
+            const int k = v & 7, l = (v >> 3) & 7, m = v >> 6;
+            const D3 vm{b.vb[0] * vbl + (k + 0.5) * vl, b.vb[1] * vbl + (l + 0.5) * vl, b.vb[2] * vbl + (m + 0.5) * vl};
+            const D3 q = dxform(Ti, vm);
+            const double c0 = q.y * g.fy / q.z + g.ci, c1 = q.x * g.fx / q.z + g.cj;
+            if (!(c0 > -1.0 && c1 > -1.0 && c0 < g.resi && c1 < g.resj)) continue;
+            const int i = (int)c0, j = (int)c1;  // truncation, as the reference's (int) cast
+            if (i < 0 || j < 0 || i >= g.resi || j >= g.resj) continue;
+            const double d = depth[i * g.resj + j] / 1000.0;
+            if (!(d > g.rmin)) continue;
+            const D3 pc{(j - g.cj) / g.fx * d, (i - g.ci) / g.fy * d, d};
+            const D3 pw = dxform(T, pc);
+            const double sdf = (pw.x - vm.x) * Ez.x + (pw.y - vm.y) * Ez.y + (pw.z - vm.z) * Ez.z;
+            if (!(std::fabs(sdf) < trunc)) continue;
+            double &s = b.sdf[v], &w = b.w[v];
+            if (!deint) {
+                s = (s * w + sdf) / (w + 1);
+                w = (g.max_weight > 0 && w + 1 > g.max_weight) ? g.max_weight : w + 1;
+            } else if (w != 0) {
+                if (w != 1) {
+                    s = (s * w - sdf) / (w - 1);
+                    w -= 1;
+                } else {
+                    s = 0;
+                    w = 0;
+                }
+            }
+        }
+    }
+    return (int)touched.size();
+}
+
+// Canonical dump sorted by key (sdf and w in double).
+int orm_grid_export(void *h, int max_blocks, uint64_t *keys, int32_t *coords, double *sdf, double *w) {
+    Grid64 &g = *(Grid64 *)h;
+    std::vector<std::pair<uint64_t, int>> items(g.map.begin(), g.map.end());
+    std::sort(items.begin(), items.end());
+    int n = 0;
+    for (auto &it : items) {
+        if (n >= max_blocks) break;
+        const Block64 &b = *g.blocks[it.second];
+        keys[n] = it.first;
+        for (int k = 0; k < 3; k++) coords[n * 3 + k] = b.vb[k];
+        std::memcpy(sdf + (size_t)n * kVox, b.sdf, sizeof(b.sdf));
+        std::memcpy(w + (size_t)n * kVox, b.w, sizeof(b.w));
+        n++;
+    }
+    return n;
+}
+
+// Trilinear raycast, same step rules as the GPU kernel, in double. vmap
+// [rows][cols][4] = (x, y, z, depth), nmap [rows][cols][4]; misses zero.
+// steps_out (optional) receives the march steps used per pixel.
+void orm_raycast(void *h, const double *T, int max_steps, double t_min, double t_max, double *vmap, double *nmap,
+                 int *steps_out) {
+    const Grid64 &g = *(Grid64 *)h;
+    const double vl = g.vl, vbl = g.vbl;
+#pragma omp parallel for schedule(dynamic, 2)
+    for (int i = 0; i < g.resi; i++) {
+        Cache cache;
+        for (int j = 0; j < g.resj; j++) {
+            const double dcx = (j - (double)g.cj) / g.fx, dcy = (i - (double)g.ci) / g.fy;
+            const double dx = T[0] * dcx + T[1] * dcy + T[2], dy = T[4] * dcx + T[5] * dcy + T[6],
+                         dz = T[8] * dcx + T[9] * dcy + T[10];
+            const double ox = T[3], oy = T[7], oz = T[11];
+            const double inv_len = 1.0 / std::sqrt(dx * dx + dy * dy + dz * dz);
+            double t = t_min, t_prev = 0, f_prev = 0;
+            bool prev_valid = false, hit = false;
+            int steps = 0;
+            while (steps < max_steps && t < t_max) {
+                const double px = ox + t * dx, py = oy + t * dy, pz = oz + t * dz;
+                const int bx = (int)std::floor(px / vbl), by = (int)std::floor(py / vbl), bz = (int)std::floor(pz / vbl);
+                steps++;
+                if (!cached(g, cache, bx, by, bz)) {
+                    double te = INFINITY;
+                    if (dx != 0) te = std::fmin(te, ((bx + (dx > 0)) * vbl - ox) / dx);
+                    if (dy != 0) te = std::fmin(te, ((by + (dy > 0)) * vbl - oy) / dy);
+                    if (dz != 0) te = std::fmin(te, ((bz + (dz > 0)) * vbl - oz) / dz);
+                    t = std::fmax(te, t) + 1e-4 * vl * inv_len;
+                    prev_valid = false;
+                    continue;
+                }
+                const Sample sm = trilinear64(g, px, py, pz, cache);
+                if (!sm.valid) {
+                    prev_valid = false;
+                    t += vl * inv_len;
+                    continue;
+                }
+                if (sm.f < 0) {
+                    if (prev_valid && f_prev > 0) {
+                        double ta = t_prev, fa = f_prev, tb = t, fb = sm.f;
+                        for (int r = 0; r < 2; r++) {
+                            const double tc = ta + (tb - ta) * fa / (fa - fb);
+                            const Sample q = trilinear64(g, ox + tc * dx, oy + tc * dy, oz + tc * dz, cache);
+                            if (!q.valid) break;
+                            if (q.f > 0) {
+                                ta = tc;
+                                fa = q.f;
+                            } else {
+                                tb = tc;
+                                fb = q.f;
+                            }
+                        }
+                        t = ta + (tb - ta) * fa / (fa - fb);
+                        hit = true;
+                    }
+                    break;
+                }
+                prev_valid = true;
+                t_prev = t;
+                f_prev = sm.f;
+                t += std::fmax(vl, 0.8 * sm.f) * inv_len;
+            }
+            const size_t pix = (size_t)i * g.resj + j;
+            double *v = vmap + pix * 4, *n = nmap + pix * 4;
+            for (int k = 0; k < 4; k++) v[k] = n[k] = 0;
+            if (hit) {
+                const double px = ox + t * dx, py = oy + t * dy, pz = oz + t * dz;
+                const Sample q = trilinear64(g, px, py, pz, cache);
+                const double gn = q.valid ? std::sqrt(q.gx * q.gx + q.gy * q.gy + q.gz * q.gz) : 0;
+                if (gn > 0) {
+                    v[0] = px;
+                    v[1] = py;
+                    v[2] = pz;
+                    v[3] = t;
+                    n[0] = q.gx / gn;
+                    n[1] = q.gy / gn;
+                    n[2] = q.gz / gn;
+                }
+            }
+            if (steps_out) steps_out[pix] = steps;
+        }
+    }
+}
+
+static bool chol6(const double *A, const double *b, double *x) {
+    double L[36] = {0};
+    for (int i = 0; i < 6; i++)
+        for (int j = 0; j <= i; j++) {
+            double s = A[i * 6 + j];
+            for (int k = 0; k < j; k++) s -= L[i * 6 + k] * L[j * 6 + k];
+            if (i == j) {
+                if (!(s > 1e-12)) return false;
+                L[i * 6 + i] = std::sqrt(s);
+            } else {
+                L[i * 6 + j] = s / L[j * 6 + j];
+            }
+        }
+    double y[6];
+    for (int i = 0; i < 6; i++) {
+        double s = b[i];
+        for (int k = 0; k < i; k++) s -= L[i * 6 + k] * y[k];
+        y[i] = s / L[i * 6 + i];
+    }
+    for (int i = 5; i >= 0; i--) {
+        double s = y[i];
+        for (int k = i + 1; k < 6; k++) s -= L[k * 6 + i] * x[k];
+        x[i] = s / L[i * 6 + i];
+    }
+    return true;
+}
+
+static void se3_left(const double *xi, double *T) {
+    const double wx = xi[0], wy = xi[1], wz = xi[2];
+    const double th2 = wx * wx + wy * wy + wz * wz, th = std::sqrt(th2);
+    double A, B, C;
+    if (th < 1e-8) {
+        A = 1 - th2 / 6;
+        B = 0.5 - th2 / 24;
+        C = 1.0 / 6 - th2 / 120;
+    } else {
+        A = std::sin(th) / th;
+        B = (1 - std::cos(th)) / th2;
+        C = (th - std::sin(th)) / (th2 * th);
+    }
+    const double K[9] = {0, -wz, wy, wz, 0, -wx, -wy, wx, 0};
+    double K2[9], R[9], V[9];
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 3; c++) K2[r * 3 + c] = K[r * 3] * K[c] + K[r * 3 + 1] * K[3 + c] + K[r * 3 + 2] * K[6 + c];
+    for (int k = 0; k < 9; k++) {
+        const double I = (k % 4 == 0) ? 1 : 0;
+        R[k] = I + A * K[k] + B * K2[k];
+        V[k] = I + B * K[k] + C * K2[k];
+    }
+    const double t[3] = {V[0] * xi[3] + V[1] * xi[4] + V[2] * xi[5], V[3] * xi[3] + V[4] * xi[4] + V[5] * xi[5],
+                         V[6] * xi[3] + V[7] * xi[4] + V[8] * xi[5]};
+    double N[12];
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 4; c++)
+            N[r * 4 + c] = R[r * 3] * T[c] + R[r * 3 + 1] * T[4 + c] + R[r * 3 + 2] * T[8 + c] + (c == 3 ? t[r] : 0);
+    for (int k = 0; k < 12; k++) T[k] = N[k];
+}
+
+// Frame-to-model point-to-plane Gauss-Newton in FP64 (the method of
+// ss_track.cu): source = depth (level-l pixels are the level-0 pixels
+// (i 2^l, j 2^l)), model maps vmap/nmap [rows][cols][4] raycast at Tprev.
+// T is the start pose on input and the result on output. Returns the
+// inliers of the last iteration.
+int orm_track(const uint16_t *depth, int rows, int cols, float fx, float fy, float cx, float cy, const double *vmap,
+              const double *nmap, const double *Tprev, double *T, int levels, const int *iters, const double *dist,
+              double rmin, double dmax) {
+    const double ci = rows - (double)cy, cj = cx;
+    double Pi[16];
+    rigid_inverse(Tprev, Pi);
+    int last_n = 0;
+    for (int level = levels - 1; level >= 0; level--) {
+        const int lr = (rows + (1 << level) - 1) >> level, lc = (cols + (1 << level) - 1) >> level;
+        for (int it = 0; it < iters[level]; it++) {
+            double S[29] = {0};
+            for (int p = 0; p < lr * lc; p++) {
+                const int i = (p / lc) << level, j = (p % lc) << level;
+                const double d = depth[(size_t)i * cols + j] * 1e-3;
+                if (!(d > rmin) || !(d < dmax)) continue;
+                const D3 pc{(j - cj) / fx * d, (i - ci) / fy * d, d};
+                const D3 w = dxform(T, pc);
+                const D3 q = dxform(Pi, w);
+                if (!(q.z > 1e-3)) continue;
+                const int ii = (int)std::floor(q.y * fy / q.z + ci + 0.5), jj = (int)std::floor(q.x * fx / q.z + cj + 0.5);
+                if (ii < 0 || ii >= rows || jj < 0 || jj >= cols) continue;
+                const double *n = nmap + ((size_t)ii * cols + jj) * 4, *v = vmap + ((size_t)ii * cols + jj) * 4;
+                if (n[0] == 0 && n[1] == 0 && n[2] == 0) continue;
+                const double ex = w.x - v[0], ey = w.y - v[1], ez = w.z - v[2];
+                if (ex * ex + ey * ey + ez * ez > dist[level] * dist[level]) continue;
+                const double r = n[0] * ex + n[1] * ey + n[2] * ez;
+                const double J[6] = {w.y * n[2] - w.z * n[1], w.z * n[0] - w.x * n[2], w.x * n[1] - w.y * n[0],
+                                     n[0], n[1], n[2]};
+                int k = 0;
+                for (int a = 0; a < 6; a++)
+                    for (int b = a; b < 6; b++) S[k++] += J[a] * J[b];
+                for (int a = 0; a < 6; a++) S[21 + a] += J[a] * r;
+                S[27] += r * r;
+                S[28] += 1;
+            }
+            last_n = (int)S[28];
+            if (S[28] < 60) break;
+            double A[36], b[6], x[6];
+            int k = 0;
+            for (int r = 0; r < 6; r++)
+                for (int c = r; c < 6; c++) A[r * 6 + c] = A[c * 6 + r] = S[k++];
+            for (int r = 0; r < 6; r++) b[r] = -S[21 + r];
+            if (!chol6(A, b, x)) break;
+            se3_left(x, T);
+            double step = 0;
+            for (int r = 0; r < 6; r++) step += x[r] * x[r];
+            if (std::sqrt(step) < 1e-7) break;
+        }
+    }
+    return last_n;
+}
+
+}  // extern "C"

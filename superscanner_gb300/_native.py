@@ -48,6 +48,14 @@ _p, _i32, _u32, _f, _st = C.c_void_p, C.c_int32, C.c_uint32, C.c_float, C.c_int
 _F16 = C.POINTER(C.c_float)
 _D16 = C.POINTER(C.c_double)
 
+class SSPipelineParams(C.Structure):
+    _fields_ = [
+        ("levels", C.c_int32), ("iters", C.c_int32 * 4), ("dist_thresh", C.c_float * 4),
+        ("raycast_steps", C.c_int32), ("t_min", C.c_float), ("t_max", C.c_float),
+        ("use_graph", C.c_int32), ("exact_fusion", C.c_int32),
+    ]
+
+
 # name: (restype, argtypes); every symbol the header declares is listed here
 # and checked by tests/test_abi.py.
 SIGNATURES = {
@@ -71,6 +79,20 @@ SIGNATURES = {
     "ss_normals_from_pcd": (_st, [_p, _i32, _i32, _p, _p]),
     "ss_kokkos_icp": (_st, [_p, _p, _i32, _i32, _f, _f, _f, _f, _D16, _D16, _i32, _D16,
                             C.POINTER(C.c_float), _p]),
+    "ss_raycast_maps": (_st, [_p, _F16, _i32, _f, _f, _p, _p, _p]),
+    "ss_pipeline_params_default": (_st, [C.POINTER(SSPipelineParams)]),
+    "ss_pipeline_create": (_st, [_p, C.POINTER(SSPipelineParams), C.POINTER(_p)]),
+    "ss_pipeline_destroy": (_st, [_p]),
+    "ss_pipeline_set_pose": (_st, [_p, _D16, _p]),
+    "ss_pipeline_get_pose": (_st, [_p, _D16, _p]),
+    "ss_pipeline_input": (_st, [_p, C.POINTER(_p)]),
+    "ss_pipeline_read_pose": (_st, [_p, _p, _p]),
+    "ss_pipeline_maps": (_st, [_p, C.POINTER(_p), C.POINTER(_p)]),
+    "ss_pipeline_frame": (_st, [_p, _p, _i32, _p]),
+    "ss_pipeline_stats": (_st, [_p, C.POINTER(_i32), C.POINTER(_f), _p]),
+    "ss_pipeline_copy_maps": (_st, [_p, _p, _p, _p]),
+    "ss_pipeline_profile": (_st, [_p, _i32]),
+    "ss_pipeline_stage_ms": (_st, [_p, C.POINTER(C.c_double), C.POINTER(C.c_int64), C.POINTER(C.c_int64), _p]),
 }
 
 for _name, (_res, _args) in SIGNATURES.items():

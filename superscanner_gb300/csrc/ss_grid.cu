@@ -479,7 +479,7 @@ ss_status rebase_epoch(ss_grid *g, cudaStream_t s) {
 
 ss_status launch_fuse(ss_grid *g, const uint16_t *depth, const uint8_t *rgb, const FramePose &hp,
                       const FramePose *dpose, bool color, bool deint, bool exact, cudaStream_t s,
-                      bool manage_epoch) {
+                      bool manage_epoch, cudaEvent_t after_collect, cudaEvent_t after_fuse) {
     const Mat34 E = hp.E, Einv = hp.Einv;
     const F3 Ez{hp.Ez[0], hp.Ez[1], hp.Ez[2]};
 
@@ -490,6 +490,7 @@ ss_status launch_fuse(ss_grid *g, const uint16_t *depth, const uint8_t *rgb, con
     const dim3 cblk(32, 8), cgrid((g->p.resj + 31) / 32, (g->p.resi + 7) / 8);
     collect_kernel<<<cgrid, cblk, 0, s>>>(g->v, depth, E, dpose);
     SS_LAUNCH_CHECK();
+    if (after_collect) SS_CUDA_TRY(cudaEventRecord(after_collect, s));
     const int ctas = persistent_ctas(g, 8);
 #define SS_FUSE(ST, C, D, X) fuse_kernel<ST, C, D, X><<<ctas, 256, 0, s>>>(g->v, depth, rgb, E, Einv, Ez, dpose)
 #define SS_FUSE_X(ST, C, D) \
@@ -509,6 +510,7 @@ ss_status launch_fuse(ss_grid *g, const uint16_t *depth, const uint8_t *rgb, con
 #undef SS_FUSE_X
 #undef SS_FUSE
     SS_LAUNCH_CHECK();
+    if (after_fuse) SS_CUDA_TRY(cudaEventRecord(after_fuse, s));
     finalize_kernel<<<1, 1, 0, s>>>(g->v.ctr);
     SS_LAUNCH_CHECK();
     if (manage_epoch) g->host_epoch++;

@@ -54,13 +54,16 @@ FramePose frame_pose_from(const float extr[16]);
 // replays advance it in the caller instead.
 ss_status launch_fuse(ss_grid *g, const uint16_t *depth, const uint8_t *rgb, const FramePose &hp,
                       const FramePose *dpose, bool color, bool deint, bool exact, cudaStream_t s,
-                      bool manage_epoch = true);
+                      bool manage_epoch = true, cudaEvent_t after_collect = nullptr,
+                      cudaEvent_t after_fuse = nullptr);
 // Clears the epoch field of every stamp and restarts the epoch at 1.
 ss_status rebase_epoch(ss_grid *g, cudaStream_t s);
 void inverse4_rounded(const float E[16], float out[16]);
 
+// counters (optional, device u64[4]): hash finds, voxel loads, march steps, hits
 ss_status launch_raycast_maps(ss_grid *g, const Mat34 &T, const FramePose *dpose, int max_steps, float t_min,
-                              float t_max, float4 *vmap, float4 *nmap, cudaStream_t s);
+                              float t_max, float4 *vmap, float4 *nmap, cudaStream_t s,
+                              unsigned long long *counters = nullptr);
 
 // Blocks of persistent launches (multiple of the SM count).
 int persistent_ctas(const ss_grid *g, int per_sm);

@@ -9,6 +9,8 @@
 // (src/core/integrate.cpp:47-209) calls GPUVoxelGrid::integrate with poses
 // from the keypoint tracker, and raycast is called by the GUI loop
 // (exe/SuperScanner.cpp:343-361).
+#include <vector>
+
 #include "ss_grid_impl.cuh"
 #include "ss_track.cuh"
 
@@ -27,22 +29,46 @@ struct ss_pipeline {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     unsigned long long frames = 0;
+    // stage profiling (non-graph frames only): 6 events per tracked frame
+    bool profile = false;
+    std::vector<cudaEvent_t> events;
+    size_t used = 0;
+    unsigned long long *rc_counters = nullptr;  // raycast traffic counters (device u64[4])
 };
 
 namespace {
+constexpr int kStages = 5;  // track, collect, fuse, finalize, raycast
 
-ss_status enqueue_fuse_raycast(ss_pipeline *P, cudaStream_t s) {
+cudaEvent_t next_event(ss_pipeline *P) {
+    if (P->used == P->events.size()) {
+        cudaEvent_t e;
+        if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+        P->events.push_back(e);
+    }
+    return P->events[P->used++];
+}
+}  // namespace
+
+namespace {
+
+ss_status enqueue_fuse_raycast(ss_pipeline *P, cudaStream_t s, bool prof = false) {
     ss_grid *g = P->g;
     FramePose dummy{};
+    cudaEvent_t e1 = prof ? next_event(P) : nullptr, e2 = prof ? next_event(P) : nullptr;
     ss_status st = launch_fuse(g, P->input, nullptr, dummy, &P->st->pose, false, false, P->p.exact_fusion != 0, s,
-                               /*manage_epoch=*/false);
+                               /*manage_epoch=*/false, e1, e2);
     if (st != SS_OK) return st;
-    return launch_raycast_maps(g, dummy.E, &P->st->pose, P->p.raycast_steps, P->p.t_min, P->p.t_max, P->vmap,
-                               P->nmap, s);
+    if (prof) SS_CUDA_TRY(cudaEventRecord(next_event(P), s));
+    st = launch_raycast_maps(g, dummy.E, &P->st->pose, P->p.raycast_steps, P->p.t_min, P->p.t_max, P->vmap,
+                             P->nmap, s, prof ? P->rc_counters : nullptr);
+    if (st != SS_OK) return st;
+    if (prof) SS_CUDA_TRY(cudaEventRecord(next_event(P), s));
+    return SS_OK;
 }
 
-ss_status enqueue_frame(ss_pipeline *P, cudaStream_t s) {
+ss_status enqueue_frame(ss_pipeline *P, cudaStream_t s, bool prof = false) {
     ss_grid *g = P->g;
+    if (prof) SS_CUDA_TRY(cudaEventRecord(next_event(P), s));
     TrackLaunch L{};
     L.depth = P->input;
     L.rows = g->p.resi;
@@ -62,7 +88,8 @@ ss_status enqueue_frame(ss_pipeline *P, cudaStream_t s) {
     L.dmax = P->p.t_max;
     ss_status st = launch_track(L, s);
     if (st != SS_OK) return st;
-    return enqueue_fuse_raycast(P, s);
+    if (prof) SS_CUDA_TRY(cudaEventRecord(next_event(P), s));
+    return enqueue_fuse_raycast(P, s, prof);
 }
 
 // The epoch advances once per executed integrate; rebase before it wraps.
@@ -114,6 +141,7 @@ ss_status ss_pipeline_create(ss_grid *g, const ss_pipeline_params *params, ss_pi
               cudaMalloc(&P->vmap, npix * sizeof(float4)) == cudaSuccess &&
               cudaMalloc(&P->nmap, npix * sizeof(float4)) == cudaSuccess &&
               cudaMalloc(&P->input, npix * sizeof(uint16_t)) == cudaSuccess &&
+              cudaMalloc(&P->rc_counters, 4 * sizeof(unsigned long long)) == cudaSuccess &&
               cudaStreamCreateWithFlags(&P->cap, cudaStreamNonBlocking) == cudaSuccess;
     if (!ok) {
         cudaGetLastError();
@@ -135,11 +163,13 @@ ss_status ss_pipeline_destroy(ss_pipeline *P) {
     if (P->exec) cudaGraphExecDestroy(P->exec);
     if (P->graph) cudaGraphDestroy(P->graph);
     if (P->cap) cudaStreamDestroy(P->cap);
+    for (cudaEvent_t e : P->events) cudaEventDestroy(e);
     cudaFree(P->st);
     cudaFree(P->partials);
     cudaFree(P->vmap);
     cudaFree(P->nmap);
     cudaFree(P->input);
+    cudaFree(P->rc_counters);
     delete P;
     return SS_OK;
 }
@@ -155,6 +185,12 @@ ss_status ss_pipeline_get_pose(ss_pipeline *P, double T[16], ss_stream_t stream)
     if (!P || !T) return SS_ERR_ARG;
     SS_CUDA_TRY(cudaMemcpyAsync(T, P->st->T, 16 * sizeof(double), cudaMemcpyDeviceToHost, (cudaStream_t)stream));
     SS_CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
+    return SS_OK;
+}
+
+ss_status ss_pipeline_read_pose(ss_pipeline *P, double T[16], ss_stream_t stream) {
+    if (!P || !T) return SS_ERR_ARG;
+    SS_CUDA_TRY(cudaMemcpyAsync(T, P->st->T, 16 * sizeof(double), cudaMemcpyDeviceToHost, (cudaStream_t)stream));
     return SS_OK;
 }
 
@@ -203,11 +239,45 @@ ss_status ss_pipeline_frame(ss_pipeline *P, const uint16_t *depth, int32_t track
         }
         SS_CUDA_TRY(cudaGraphLaunch(P->exec, s));
     } else {
-        st = enqueue_frame(P, s);
+        st = enqueue_frame(P, s, P->profile);
         if (st != SS_OK) return st;
     }
     g->host_epoch++;
     P->frames++;
+    return SS_OK;
+}
+
+ss_status ss_pipeline_profile(ss_pipeline *P, int32_t enable) {
+    if (!P) return SS_ERR_ARG;
+    P->profile = enable != 0;
+    P->used = 0;
+    SS_CUDA_TRY(cudaMemset(P->rc_counters, 0, 4 * sizeof(unsigned long long)));
+    return SS_OK;
+}
+
+ss_status ss_pipeline_stage_ms(ss_pipeline *P, double ms[5], int64_t *frames, int64_t counters[4],
+                               ss_stream_t stream) {
+    if (!P || !ms || !frames) return SS_ERR_ARG;
+    SS_CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
+    for (int k = 0; k < kStages; k++) ms[k] = 0.0;
+    const size_t per = kStages + 1;
+    *frames = (int64_t)(P->used / per);
+    if (counters) SS_CUDA_TRY(cudaMemcpy(counters, P->rc_counters, 4 * sizeof(int64_t), cudaMemcpyDeviceToHost));
+    for (size_t f = 0; f + per <= P->used; f += per) {
+        for (int k = 0; k < kStages; k++) {
+            float t = 0.f;
+            SS_CUDA_TRY(cudaEventElapsedTime(&t, P->events[f + k], P->events[f + k + 1]));
+            ms[k] += t;
+        }
+    }
+    return SS_OK;
+}
+
+ss_status ss_pipeline_copy_maps(ss_pipeline *P, float *vertex_depth, float *normal, ss_stream_t stream) {
+    if (!P || !vertex_depth || !normal) return SS_ERR_ARG;
+    const size_t bytes = (size_t)P->g->p.resi * P->g->p.resj * sizeof(float4);
+    SS_CUDA_TRY(cudaMemcpyAsync(vertex_depth, P->vmap, bytes, cudaMemcpyDefault, (cudaStream_t)stream));
+    SS_CUDA_TRY(cudaMemcpyAsync(normal, P->nmap, bytes, cudaMemcpyDefault, (cudaStream_t)stream));
     return SS_OK;
 }
 

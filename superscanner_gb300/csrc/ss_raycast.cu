@@ -205,6 +205,8 @@ struct TriSample {
 
 struct BlockCache {
     int x, y, z, bucket;
+    unsigned lookups;  // hash-table finds issued (cache misses)
+    unsigned voxels;   // voxel words loaded
 };
 
 template <int kStorage>
@@ -224,6 +226,7 @@ __device__ __forceinline__ int cached_lookup(const GridView &g, BlockCache &c, i
     c.x = bx;
     c.y = by;
     c.z = bz;
+    c.lookups++;
     c.bucket = packable(bx, by, bz) ? table_find(g, prime_hash(bx, by, bz)) : -1;
     return c.bucket;
 }
@@ -244,6 +247,7 @@ __device__ __forceinline__ TriSample trilinear(const GridView &g, float px, floa
         const int b = cached_lookup(g, c, bx, by, bz);
         if (b < 0) return r;
         const float2 sw = voxel_sw<kStorage>(g, b, (vx & 7) + 8 * (vy & 7) + 64 * (vz & 7));
+        c.voxels++;
         if (!(sw.y > 0.f)) return r;
         s[k] = sw.x;
     }
@@ -266,10 +270,15 @@ __device__ __forceinline__ TriSample trilinear(const GridView &g, float px, floa
 template <int kStorage>
 __global__ void __launch_bounds__(256) raycast_maps_kernel(GridView g, Mat34 T, const FramePose *__restrict__ pose,
                                                            int max_steps, float t_min, float t_max,
-                                                           float4 *__restrict__ vmap, float4 *__restrict__ nmap) {
+                                                           float4 *__restrict__ vmap, float4 *__restrict__ nmap,
+                                                           unsigned long long *__restrict__ counters) {
     const int j = blockIdx.x * 32 + threadIdx.x;
     const int i = blockIdx.y * blockDim.y + threadIdx.y;
-    if (i >= g.resi || j >= g.resj) return;
+    const bool inside = i < g.resi && j < g.resj;
+    BlockCache cache{INT_MIN, INT_MIN, INT_MIN, -1, 0u, 0u};
+    int steps = 0;
+    bool hit = false;
+    if (inside) {
     if (pose) {
 #pragma unroll
         for (int k = 0; k < 12; k++) T.m[k] = __ldg(&pose->E.m[k]);
@@ -283,10 +292,8 @@ __global__ void __launch_bounds__(256) raycast_maps_kernel(GridView g, Mat34 T, 
     const float vl = g.vl, inv_vl = 1.f / g.vl, inv_vbl = 1.f / g.vbl;
     const float rdx = 1.f / dx, rdy = 1.f / dy, rdz = 1.f / dz;
 
-    BlockCache cache{INT_MIN, INT_MIN, INT_MIN, -1};
     float t = t_min, t_prev = 0.f, f_prev = 0.f;
-    bool prev_valid = false, hit = false;
-    int steps = 0;
+    bool prev_valid = false;
     while (steps < max_steps && t < t_max) {
         const float px = fmaf(t, dx, ox), py = fmaf(t, dy, oy), pz = fmaf(t, dz, oz);
         const int bx = (int)floorf(px * inv_vbl), by = (int)floorf(py * inv_vbl), bz = (int)floorf(pz * inv_vbl);
@@ -347,15 +354,29 @@ __global__ void __launch_bounds__(256) raycast_maps_kernel(GridView g, Mat34 T, 
     }
     vmap[pix] = v;
     nmap[pix] = n;
+    }
+    if (counters) {  // algorithmic-traffic counters (profiling only), one atomic per warp and field
+        const unsigned full = 0xffffffffu;
+        const unsigned l = __reduce_add_sync(full, cache.lookups), vx = __reduce_add_sync(full, cache.voxels);
+        const unsigned st = __reduce_add_sync(full, (unsigned)steps), h = __reduce_add_sync(full, hit ? 1u : 0u);
+        if ((threadIdx.x & 31) == 0) {
+            atomicAdd(counters + 0, (unsigned long long)l);
+            atomicAdd(counters + 1, (unsigned long long)vx);
+            atomicAdd(counters + 2, (unsigned long long)st);
+            atomicAdd(counters + 3, (unsigned long long)h);
+        }
+    }
 }
 
 ss_status launch_raycast_maps(ss_grid *g, const Mat34 &T, const FramePose *dpose, int max_steps, float t_min,
-                              float t_max, float4 *vmap, float4 *nmap, cudaStream_t s) {
+                              float t_max, float4 *vmap, float4 *nmap, cudaStream_t s, unsigned long long *counters) {
     const dim3 blk(32, 8), grid((g->p.resj + 31) / 32, (g->p.resi + 7) / 8);
     if (g->p.storage == SS_STORAGE_F32)
-        raycast_maps_kernel<SS_STORAGE_F32><<<grid, blk, 0, s>>>(g->v, T, dpose, max_steps, t_min, t_max, vmap, nmap);
+        raycast_maps_kernel<SS_STORAGE_F32>
+            <<<grid, blk, 0, s>>>(g->v, T, dpose, max_steps, t_min, t_max, vmap, nmap, counters);
     else
-        raycast_maps_kernel<SS_STORAGE_F16><<<grid, blk, 0, s>>>(g->v, T, dpose, max_steps, t_min, t_max, vmap, nmap);
+        raycast_maps_kernel<SS_STORAGE_F16>
+            <<<grid, blk, 0, s>>>(g->v, T, dpose, max_steps, t_min, t_max, vmap, nmap, counters);
     SS_LAUNCH_CHECK();
     return SS_OK;
 }

@@ -1,0 +1,114 @@
+"""GPU tests of the per-frame method against its FP64 oracle: trilinear
+raycast depth (<= 1 mm at p99 for both storage forms), one tracking solve,
+and the whole pipeline (graph replay equals direct launches bit for bit;
+poses track the ground truth)."""
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from superscanner_gb300 import GPUVoxelGrid, synth
+from superscanner_gb300.pipeline import Pipeline, raycast_maps
+
+pytestmark = pytest.mark.gpu
+
+INTR = (525.0, 525.0, 319.5, 239.5)
+VL, TRUNC = 0.004, 0.016
+
+
+def seq(n, step=1):
+    sc = synth.Scene(2, 1234)
+    P = sc.trajectory(n * step, 42)[::step]
+    depth, _ = sc.render(P, 480, 640, INTR, noise=True, noise_seed=7, color=False)
+    return P, depth
+
+
+def dev(a):
+    return torch.from_numpy(np.ascontiguousarray(a.view(np.int16))).cuda()
+
+
+def pose_err(T, R):
+    d = np.linalg.inv(R) @ T
+    return np.linalg.norm(d[:3, 3]), np.arccos(np.clip((np.trace(d[:3, :3]) - 1) / 2, -1, 1))
+
+
+@pytest.mark.parametrize("storage", ["f32", "f16"])
+def test_raycast_maps_vs_fp64(storage):
+    P, depth = seq(6, 2)
+    g = GPUVoxelGrid(int(1e9), TRUNC, VL, 480, 640, storage=storage, with_color=False, hash_buckets=1 << 18,
+                     max_weight=255)
+    g.setIntrinsic(*INTR)
+    o = oracle.MethodGrid64(VL, TRUNC, 480, 640, INTR, 255)
+    for k in range(6):
+        g.integrate(None, dev(depth[k]), P[k].astype(np.float32), withColor=False)
+        o.fuse(depth[k], P[k])
+    v, n = raycast_maps(g, P[5].astype(np.float32))
+    g.sync()
+    v = v.cpu().numpy().astype(np.float64)
+    n = n.cpu().numpy()
+    v64, n64, steps = o.raycast(P[5])
+    both = (v[..., 3] > 0) & (v64[..., 3] > 0)
+    assert both.mean() > 0.85
+    assert ((v[..., 3] > 0) == (v64[..., 3] > 0)).mean() > 0.99
+    err = np.abs(v[..., 3][both] - v64[..., 3][both])
+    assert np.median(err) < 1e-4
+    assert np.percentile(err, 99) < 1e-3  # the 1 mm depth bound
+    cos = np.sum(n[both][:, :3] * n64[both][:, :3], axis=-1)
+    assert np.median(cos) > 0.9999
+
+
+def test_tracking_solve_vs_fp64():
+    P, depth = seq(12)
+    g = GPUVoxelGrid(int(1e9), TRUNC, VL, 480, 640, storage="f32", with_color=False, hash_buckets=1 << 18,
+                     max_weight=255)
+    g.setIntrinsic(*INTR)
+    pipe = Pipeline(g, use_graph=False)
+    pipe.set_pose(P[0])
+    for k in range(10):
+        pipe.frame(dev(depth[k]), track=(k > 0))
+    v, n = pipe.maps_tensors()
+    T9 = pipe.pose()
+    torch.cuda.synchronize()
+    pipe.frame(dev(depth[10]), track=True)
+    T10 = pipe.pose()
+    T64, inl = oracle.track64(depth[10], v.cpu().numpy().astype(np.float64), n.cpu().numpy().astype(np.float64),
+                              T9, T9, INTR)
+    dt, dr = pose_err(T10, T64)
+    assert inl > 100000
+    assert dt < 1e-4 and dr < 1e-4
+    inliers, rmse = pipe.stats()
+    assert inliers[0] > 100000
+
+
+def test_pipeline_graph_replay_equals_direct_launches():
+    P, depth = seq(16)
+    poses = {}
+    for graph in (False, True):
+        g = GPUVoxelGrid(int(1e9), TRUNC, VL, 480, 640, storage="f16", with_color=False, hash_buckets=1 << 18,
+                         max_weight=255)
+        g.setIntrinsic(*INTR)
+        pipe = Pipeline(g, use_graph=graph)
+        pipe.set_pose(P[0])
+        out = []
+        for k in range(16):
+            pipe.frame(dev(depth[k]), track=(k > 0))
+            out.append(pipe.pose())
+        g.sync()
+        poses[graph] = np.stack(out)
+    assert np.array_equal(poses[False], poses[True])
+
+
+@pytest.mark.parametrize("storage", ["f32", "f16"])
+def test_pipeline_tracks_ground_truth(storage):
+    P, depth = seq(60)
+    g = GPUVoxelGrid(int(1e9), TRUNC, VL, 480, 640, storage=storage, with_color=False, hash_buckets=1 << 18,
+                     max_weight=255)
+    g.setIntrinsic(*INTR)
+    pipe = Pipeline(g, use_graph=True)
+    pipe.set_pose(P[0])
+    host = torch.from_numpy(depth.view(np.int16)).pin_memory()
+    for k in range(60):
+        pipe.frame(host[k].numpy(), track=(k > 0))
+    g.sync()
+    dt, dr = pose_err(pipe.pose(), P[59])
+    assert dt < 0.01 and np.degrees(dr) < 0.5
