@@ -107,9 +107,11 @@ ss_status ss_raycast(ss_grid *g, const float extr[16], float *ray_pcd, float *ra
 ss_status ss_clean_memory(ss_grid *g, ss_stream_t s);
 
 /* Same as ss_integrate / ss_deintegrate (deint != 0), with FMA-contracted
- * single-precision arithmetic in the voxel update; block allocation keeps
- * the reference rounding. Used by the per-frame pipeline. No reference
- * counterpart (an addition of this library). */
+ * single-precision arithmetic in the voxel update and the voxel observed at
+ * the pixel nearest to its projection (the reference truncates the projected
+ * coordinate, GPUVoxelGrid.cpp:348-349, a half-pixel bias that makes
+ * frame-to-model tracking drift); block allocation keeps the reference
+ * rounding. Used by the per-frame pipeline. No reference counterpart. */
 ss_status ss_integrate_fast(ss_grid *g, const uint16_t *depth, const uint8_t *rgb,
                             const float extr[16], int32_t with_color, int32_t deint,
                             ss_stream_t s);
@@ -180,7 +182,7 @@ typedef struct ss_pipeline_params {
     int32_t raycast_steps;    /* march step cap of the model-view raycast */
     float t_min, t_max;       /* raycast depth range */
     int32_t use_graph;        /* replay each tracked frame as one captured CUDA graph */
-    int32_t exact_fusion;     /* reference rounding in the voxel update (else FMA-contracted) */
+    int32_t exact_fusion;     /* reference voxel update (rounding, truncated pixel) instead of ss_integrate_fast's */
 } ss_pipeline_params;
 
 ss_status ss_pipeline_params_default(ss_pipeline_params *p);

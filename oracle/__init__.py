@@ -47,6 +47,7 @@ for name, res, args in [
     ("orm_grid_new", _p, [_f, _f, _i, _i, _f, _f, _f, _f, C.c_double]),
     ("orm_grid_free", None, [_p]),
     ("orm_grid_count", _i, [_p]),
+    ("orm_grid_set_round_pixel", None, [_p, _i]),
     ("orm_grid_fuse", _i, [_p, _p, _p, _i]),
     ("orm_grid_export", _i, [_p, _i, _p, _p, _p, _p]),
     ("orm_raycast", None, [_p, _p, _i, C.c_double, C.c_double, _p, _p, _p]),
@@ -180,9 +181,11 @@ def threads() -> int:
 class MethodGrid64:
     """FP64 oracle of the per-frame method (FP64 TSDF, trilinear raycast)."""
 
-    def __init__(self, vl, trunc, resi, resj, intr=(525.0, 525.0, 319.5, 239.5), max_weight=0.0):
+    def __init__(self, vl, trunc, resi, resj, intr=(525.0, 525.0, 319.5, 239.5), max_weight=0.0,
+                 round_pixel=True):
         self.resi, self.resj, self.intr = resi, resj, intr
         self._h = _lib.orm_grid_new(vl, trunc, resi, resj, *map(float, intr), float(max_weight))
+        _lib.orm_grid_set_round_pixel(self._h, 1 if round_pixel else 0)
 
     def __del__(self):
         if getattr(self, "_h", None):

@@ -11,6 +11,7 @@
 #include <cmath>
 #include <cstring>
 #include <unordered_map>
+#include <unordered_set>
 #include <vector>
 
 #include "ss_ref_math.h"
@@ -31,9 +32,17 @@ struct Grid64 {
     float fx, fy, cx, cy, ci, cj;
     double max_weight;
     float rmin = 0.2f;
+    int round_pixel = 1;  // 1: nearest pixel of the voxel's projection; 0: truncation (GPUVoxelGrid.cpp:348)
     std::unordered_map<uint64_t, int> map;
     std::vector<Block64 *> blocks;
+    std::unordered_set<uint64_t> supers;  // super-blocks (8^3 blocks) holding an allocated block
 };
+
+inline int floordiv8(int v) { return v >= 0 ? v / 8 : -((-v + 7) / 8); }
+inline uint64_t super_key(int sx, int sy, int sz) {
+    return ((uint64_t)(uint32_t)(sx + 1024) << 22) | ((uint64_t)(uint32_t)(sy + 1024) << 11) |
+           (uint64_t)(uint32_t)(sz + 1024);
+}
 
 struct D3 {
     double x, y, z;
@@ -78,6 +87,7 @@ std::vector<int> collect64(Grid64 &g, const uint16_t *depth, const float *E) {
                             std::memset(b, 0, sizeof(Block64));
                             g.blocks.push_back(b);
                             g.map.emplace(key, idx);
+                            g.supers.insert(super_key(floordiv8(x), floordiv8(y), floordiv8(z)));
                         } else {
                             idx = it->second;
                         }
@@ -124,8 +134,6 @@ inline const Block64 *cached(const Grid64 &g, Cache &c, int bx, int by, int bz) 
     }
     return c.b;
 }
-
-inline int floordiv8(int v) { return v >= 0 ? v / 8 : -((-v + 7) / 8); }
 
 Sample trilinear64(const Grid64 &g, double px, double py, double pz, Cache &c) {
     Sample r{false, 0, 0, 0, 0};
@@ -188,6 +196,8 @@ void orm_grid_free(void *h) {
 
 int orm_grid_count(void *h) { return (int)((Grid64 *)h)->map.size(); }
 
+void orm_grid_set_round_pixel(void *h, int on) { ((Grid64 *)h)->round_pixel = on; }
+
 // FP64 integrate (deint = 0) / deintegrate (deint = 1) at pose T (double).
 int orm_grid_fuse(void *h, const uint16_t *depth, const double *T, int deint) {
     Grid64 &g = *(Grid64 *)h;
@@ -208,7 +218,8 @@ int orm_grid_fuse(void *h, const uint16_t *depth, const double *T, int deint) {
             const D3 q = dxform(Ti, vm);
             const double c0 = q.y * g.fy / q.z + g.ci, c1 = q.x * g.fx / q.z + g.cj;
             if (!(c0 > -1.0 && c1 > -1.0 && c0 < g.resi && c1 < g.resj)) continue;
-            const int i = (int)c0, j = (int)c1;  // truncation, as the reference's (int) cast
+            const int i = g.round_pixel ? (int)std::floor(c0 + 0.5) : (int)c0;
+            const int j = g.round_pixel ? (int)std::floor(c1 + 0.5) : (int)c1;
             if (i < 0 || j < 0 || i >= g.resi || j >= g.resj) continue;
             const double d = depth[i * g.resj + j] / 1000.0;
             if (!(d > g.rmin)) continue;
@@ -275,6 +286,17 @@ void orm_raycast(void *h, const double *T, int max_steps, double t_min, double t
                 const double px = ox + t * dx, py = oy + t * dy, pz = oz + t * dz;
                 const int bx = (int)std::floor(px / vbl), by = (int)std::floor(py / vbl), bz = (int)std::floor(pz / vbl);
                 steps++;
+                const int sx = floordiv8(bx), sy = floordiv8(by), sz = floordiv8(bz);
+                if (!g.supers.count(super_key(sx, sy, sz))) {
+                    const double sbl = 8 * vbl;
+                    double te = INFINITY;
+                    if (dx != 0) te = std::fmin(te, ((sx + (dx > 0)) * sbl - ox) / dx);
+                    if (dy != 0) te = std::fmin(te, ((sy + (dy > 0)) * sbl - oy) / dy);
+                    if (dz != 0) te = std::fmin(te, ((sz + (dz > 0)) * sbl - oz) / dz);
+                    t = std::fmax(te, t) + 1e-4 * vl * inv_len;
+                    prev_valid = false;
+                    continue;
+                }
                 if (!cached(g, cache, bx, by, bz)) {
                     double te = INFINITY;
                     if (dx != 0) te = std::fmin(te, ((bx + (dx > 0)) * vbl - ox) / dx);

@@ -80,12 +80,30 @@ def build_synth(force: bool = False) -> Path:
     return SYNTH_LIB
 
 
+SHIM_SRC = ROOT / "tests" / "cpp" / "shim_roundtrip.cpp"
+SHIM_BIN = BUILD / "shim_roundtrip"
+
+
+def build_shim_test(force: bool = False) -> Path:
+    """C++ program that drives the reference-shaped shim header over libss.so."""
+    deps = [SHIM_SRC, INCLUDE / "ss_gpu_voxel_grid.hpp", INCLUDE / "ss_abi.h", LIB]
+    if not force and SHIM_BIN.exists() and SHIM_BIN.stat().st_mtime >= _newest(deps):
+        return SHIM_BIN
+    cuda = Path(_nvcc()).resolve().parent.parent
+    BUILD.mkdir(exist_ok=True)
+    _run(["g++", "-O2", "-std=c++17", "-I", str(INCLUDE), "-I", str(cuda / "include"), str(SHIM_SRC),
+          "-o", str(SHIM_BIN), "-L", str(PKG), "-lss", "-L", str(cuda / "lib64"), "-lcudart",
+          f"-Wl,-rpath,{PKG}", f"-Wl,-rpath,{cuda / 'lib64'}"])
+    return SHIM_BIN
+
+
 def build_native(force: bool = False, verbose: bool = False) -> None:
     with cf.ThreadPoolExecutor(max_workers=2) as ex:
         a = ex.submit(build_cuda, force, verbose)
         b = ex.submit(build_synth, force)
         a.result()
         b.result()
+    build_shim_test(force)
 
 
 if __name__ == "__main__":

@@ -158,7 +158,13 @@ __global__ void __launch_bounds__(256) collect_kernel(GridView g, const uint16_t
         if (act) {
             const unsigned peers = __match_any_sync(am, packed);
             if (__ffs(peers) - 1 == lane) {
-                bucket = table_find_or_insert(g, key);
+                bool inserted = false;
+                bucket = table_find_or_insert(g, key, &inserted);
+                if (inserted) {
+                    int x, y, z;
+                    unpack_coords(packed, x, y, z);
+                    super_insert(g, x, y, z);
+                }
                 if (bucket >= 0) {
                     const unsigned long long mine = ((unsigned long long)epoch << kEpochShift) | packed;
                     const unsigned long long old = atomicMax(g.stamp + bucket, mine);
@@ -201,8 +207,10 @@ __device__ __forceinline__ bool voxel_observe(const GridView &g, const uint16_t 
         c0 = fmaf(q.y * g.in.fy, rz, g.in.ci);
         c1 = fmaf(q.x * g.in.fx, rz, g.in.cj);
     }
-    const int cori = __float2int_rz(c0);
-    const int corj = __float2int_rz(c1);
+    // exact: the reference's (int) cast (GPUVoxelGrid.cpp:348-349), which picks the pixel half a pixel
+    // off the projection; fast: the nearest pixel (the truncation makes frame-to-model tracking drift)
+    const int cori = kExact ? __float2int_rz(c0) : __float2int_rd(c0 + 0.5f);
+    const int corj = kExact ? __float2int_rz(c1) : __float2int_rd(c1 + 0.5f);
     if (!(cori < g.resi && corj < g.resj && cori >= 0 && corj >= 0)) return false;
     pix = cori * g.resj + corj;
     const uint16_t dmm = __ldg(depth + pix);
@@ -385,6 +393,17 @@ __global__ void __launch_bounds__(256) clean_kernel(GridView g) {
     }
 }
 
+// Re-derives the super-block set from the live blocks (after clean).
+__global__ void super_rebuild_kernel(GridView g) {
+    for (size_t b = blockIdx.x * (size_t)blockDim.x + threadIdx.x; b <= g.mask; b += (size_t)gridDim.x * blockDim.x) {
+        const unsigned long long key = g.keys[b];
+        if (key == kEmptyKey || key == kTombKey) continue;
+        int x, y, z;
+        unpack_coords(g.stamp[b] & ((1ull << kEpochShift) - 1ull), x, y, z);
+        super_insert(g, x, y, z);
+    }
+}
+
 // Gathers the payload of listed buckets into compact FP32 arrays (export).
 template <int kStorage>
 __global__ void gather_blocks_kernel(GridView g, const int *__restrict__ buckets, int n, float *sdf, float *w,
@@ -425,7 +444,10 @@ __global__ void import_blocks_kernel(GridView g, const int *__restrict__ coords,
         if (lane == 0) {
             if (packable(x, y, z)) {
                 bucket = table_find_or_insert(g, prime_hash(x, y, z));
-                if (bucket >= 0) g.stamp[bucket] = pack_coords(x, y, z);
+                if (bucket >= 0) {
+                    g.stamp[bucket] = pack_coords(x, y, z);
+                    super_insert(g, x, y, z);
+                }
             } else {
                 atomicOr(&g.ctr->status, kStRange);
             }
@@ -549,6 +571,7 @@ ss_status ss_grid_reset(ss_grid *g, ss_stream_t stream) {
     cudaStream_t s = (cudaStream_t)stream;
     const size_t B = (size_t)g->p.hash_buckets;
     fill_u64_kernel<<<persistent_ctas(g, 4), 256, 0, s>>>(g->v.keys, B, kEmptyKey);
+    fill_u64_kernel<<<persistent_ctas(g, 1), 256, 0, s>>>(g->v.sbkeys, (size_t)g->v.sbmask + 1, kSuperEmpty);
     SS_LAUNCH_CHECK();
     SS_CUDA_TRY(cudaMemsetAsync(g->v.stamp, 0, B * 8, s));
     if (g->v.vox32) SS_CUDA_TRY(cudaMemsetAsync(g->v.vox32, 0, B * kBlockVoxels * sizeof(float2), s));
@@ -578,6 +601,10 @@ ss_status ss_grid_create(const ss_params *p, ss_grid **out) {
     const size_t B = (size_t)p->hash_buckets;
     bool ok = cudaMalloc(&g->v.keys, B * 8) == cudaSuccess && cudaMalloc(&g->v.stamp, B * 8) == cudaSuccess &&
               cudaMalloc(&g->v.list, B * 4) == cudaSuccess && cudaMalloc(&g->v.ctr, sizeof(Counters)) == cudaSuccess;
+    // super-block set: one entry per 512 blocks of capacity, at least 4096 (load factor <= 1/8 of a 2^20 table)
+    const size_t SB = std::max<size_t>(4096, B / 32);
+    if (ok) ok = cudaMalloc(&g->v.sbkeys, SB * 8) == cudaSuccess;
+    g->v.sbmask = (uint32_t)(SB - 1);
     if (ok && p->storage == SS_STORAGE_F32)
         ok = cudaMalloc(&g->v.vox32, B * kBlockVoxels * sizeof(float2)) == cudaSuccess;
     if (ok && p->storage == SS_STORAGE_F16)
@@ -616,6 +643,7 @@ ss_status ss_grid_destroy(ss_grid *g) {
     cudaFree(g->v.vox32);
     cudaFree(g->v.vox16);
     cudaFree(g->v.rgb);
+    cudaFree(g->v.sbkeys);
     delete g;
     return SS_OK;
 }
@@ -656,7 +684,8 @@ ss_status ss_deintegrate(ss_grid *g, const uint16_t *depth, const uint8_t *rgb, 
 }
 
 // Variant used by the per-frame pipeline: same kernels, FMA-contracted fast
-// arithmetic in the voxel update (block allocation stays reference-exact).
+// arithmetic and nearest-pixel association in the voxel update (block
+// allocation stays reference-exact).
 ss_status ss_integrate_fast(ss_grid *g, const uint16_t *depth, const uint8_t *rgb, const float extr[16],
                             int32_t with_color, int32_t deint, ss_stream_t s) {
     if (!g || !depth || !extr) return SS_ERR_ARG;
@@ -672,6 +701,9 @@ ss_status ss_clean_memory(ss_grid *g, ss_stream_t stream) {
     cudaStream_t s = (cudaStream_t)stream;
     if (g->p.storage == SS_STORAGE_F32) clean_kernel<SS_STORAGE_F32><<<persistent_ctas(g, 8), 256, 0, s>>>(g->v);
     else clean_kernel<SS_STORAGE_F16><<<persistent_ctas(g, 8), 256, 0, s>>>(g->v);
+    SS_LAUNCH_CHECK();
+    fill_u64_kernel<<<persistent_ctas(g, 1), 256, 0, s>>>(g->v.sbkeys, (size_t)g->v.sbmask + 1, kSuperEmpty);
+    super_rebuild_kernel<<<persistent_ctas(g, 4), 256, 0, s>>>(g->v);
     SS_LAUNCH_CHECK();
     return SS_OK;
 }

@@ -206,10 +206,10 @@ __global__ void __launch_bounds__(256) icp_ref_iter_kernel(const float *__restri
         if (lane == 0) red[wid][k] = v;
     }
     __syncthreads();
-    if (threadIdx.x < kIcpSums) {
+    if (threadIdx.x < kIcpSums) {  // value-major slots: partials[value][cta]
         double s = 0.0;
         for (int w = 0; w < (int)(blockDim.x >> 5); w++) s += red[w][threadIdx.x];
-        partials[(size_t)blockIdx.x * kIcpSums + threadIdx.x] = s;
+        partials[(size_t)threadIdx.x * gridDim.x + blockIdx.x] = s;
     }
     __threadfence();
     __syncthreads();
@@ -217,11 +217,13 @@ __global__ void __launch_bounds__(256) icp_ref_iter_kernel(const float *__restri
     __syncthreads();
     if (!last) return;
     __threadfence();
+    // last CTA: one warp per sum, lanes stride over the CTA slots, fixed shuffle tree (deterministic)
     __shared__ double tot[kIcpSums];
-    if (threadIdx.x < kIcpSums) {
+    for (int v = wid; v < kIcpSums; v += (int)(blockDim.x >> 5)) {
         double s = 0.0;
-        for (unsigned b = 0; b < gridDim.x; b++) s += *((volatile double *)partials + (size_t)b * kIcpSums + threadIdx.x);
-        tot[threadIdx.x] = s;
+        for (unsigned b = lane; b < gridDim.x; b += 32) s += __ldcg(partials + (size_t)v * gridDim.x + b);
+        s = warp_sum(s);
+        if (lane == 0) tot[v] = s;
     }
     __syncthreads();
     if (threadIdx.x != 0) return;

@@ -92,6 +92,8 @@ struct GridView {
     float *rgb;                 // [buckets][3][512] or null
     int *list;                  // [buckets] touched bucket indices
     Counters *ctr;
+    unsigned long long *sbkeys; // [sb_buckets] occupied super-blocks (8^3 blocks) for empty-space skipping
+    uint32_t sbmask;            // sb_buckets - 1
     uint32_t mask;              // buckets - 1
     float vl, vbl, trunc, rmin, d_max, max_weight;
     int resi, resj;
@@ -211,7 +213,8 @@ __device__ __forceinline__ int table_find(const GridView &g, unsigned long long 
 // probe sequence with one 64-bit CAS and re-scan when the CAS loses. The
 // payload of a free bucket is always zero (create/reset/clean keep it so), so
 // a claimed bucket is a default-constructed Voxelblock.
-__device__ __forceinline__ int table_find_or_insert(const GridView &g, unsigned long long key) {
+__device__ __forceinline__ int table_find_or_insert(const GridView &g, unsigned long long key,
+                                                    bool *inserted = nullptr) {
     const uint32_t home = home_bucket(key, g.mask);
     for (int attempt = 0; attempt < 64; attempt++) {
         int free_b = -1;
@@ -238,12 +241,56 @@ __device__ __forceinline__ int table_find_or_insert(const GridView &g, unsigned 
         unsigned long long old = atomicCAS(g.keys + free_b, free_expect, key);
         if (old == free_expect) {
             atomicAdd(&g.ctr->live_blocks, 1);
+            if (inserted) *inserted = true;
             return free_b;
         }
         if (old == key) return free_b;
     }
     atomicOr(&g.ctr->status, kStTableFull);
     return -1;
+}
+
+// ---------------------------------------------------------- super-blocks
+// A super-block is 8x8x8 blocks (coordinates b >> 3); the set of super-blocks
+// holding at least one allocated block lets a ray skip 8 blocks at a time
+// through empty space. Kept as a small open-addressing set of packed
+// coordinates; inserts are idempotent, entries are only removed by a rebuild.
+constexpr int kSuperShift = 3;
+constexpr unsigned long long kSuperEmpty = ~0ull;
+
+__device__ __forceinline__ unsigned long long super_key(int sx, int sy, int sz) {
+    return ((unsigned long long)(uint32_t)(sx + 1024) << 22) | ((unsigned long long)(uint32_t)(sy + 1024) << 11) |
+           (unsigned long long)(uint32_t)(sz + 1024);
+}
+__device__ __forceinline__ uint32_t super_home(unsigned long long key, uint32_t mask) {
+    uint32_t h = (uint32_t)(key ^ (key >> 29)) * 0x9E3779B1u;
+    h ^= h >> 15;
+    return h & mask;
+}
+__device__ __forceinline__ void super_insert(const GridView &g, int bx, int by, int bz) {
+    const unsigned long long key = super_key(bx >> kSuperShift, by >> kSuperShift, bz >> kSuperShift);
+    uint32_t b = super_home(key, g.sbmask);
+    for (uint32_t probe = 0; probe <= g.sbmask; probe++) {
+        const unsigned long long k = ld_relaxed(g.sbkeys + b);
+        if (k == key) return;
+        if (k == kSuperEmpty) {
+            const unsigned long long old = atomicCAS(g.sbkeys + b, kSuperEmpty, key);
+            if (old == kSuperEmpty || old == key) return;
+        }
+        b = (b + 1) & g.sbmask;
+    }
+    atomicOr(&g.ctr->status, kStTableFull);
+}
+__device__ __forceinline__ bool super_occupied(const GridView &g, int sx, int sy, int sz) {
+    const unsigned long long key = super_key(sx, sy, sz);
+    uint32_t b = super_home(key, g.sbmask);
+    for (uint32_t probe = 0; probe <= g.sbmask; probe++) {
+        const unsigned long long k = __ldg(g.sbkeys + b);
+        if (k == key) return true;
+        if (k == kSuperEmpty) return false;
+        b = (b + 1) & g.sbmask;
+    }
+    return false;
 }
 
 __device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }

@@ -185,6 +185,8 @@ __global__ void __launch_bounds__(256) raycast_ref_kernel(GridView g, Mat34 Er, 
 //
 // Ray of pixel (i, j): direction ((j - cj)/fx, (i - ci)/fy, 1) in the camera
 // (not normalised, so the ray parameter t is the camera-frame depth). Steps:
+//  * the ray point lies in a super-block (8^3 blocks) without any allocated
+//    block: jump to the exit of that super-block's box;
 //  * the ray point lies in a block that is not allocated: jump to the exit of
 //    that block's box (empty-space skip);
 //  * the trilinear TSDF sample is invalid (a corner voxel unobserved or in a
@@ -294,10 +296,32 @@ __global__ void __launch_bounds__(256) raycast_maps_kernel(GridView g, Mat34 T, 
 
     float t = t_min, t_prev = 0.f, f_prev = 0.f;
     bool prev_valid = false;
+    const float sbl = g.vbl * (float)(1 << kSuperShift);
+    int csx = INT_MIN, csy = INT_MIN, csz = INT_MIN;
+    bool cocc = false;
     while (steps < max_steps && t < t_max) {
         const float px = fmaf(t, dx, ox), py = fmaf(t, dy, oy), pz = fmaf(t, dz, oz);
         const int bx = (int)floorf(px * inv_vbl), by = (int)floorf(py * inv_vbl), bz = (int)floorf(pz * inv_vbl);
         steps++;
+        const int sx = bx >> kSuperShift, sy = by >> kSuperShift, sz = bz >> kSuperShift;
+        if (sx != csx || sy != csy || sz != csz) {
+            csx = sx;
+            csy = sy;
+            csz = sz;
+            cocc = super_occupied(g, sx, sy, sz);
+            cache.lookups++;
+        }
+        if (!cocc) {
+            // exit of this empty super-block's box along the ray
+            const float ex = ((float)(sx + (dx > 0.f)) * sbl - ox) * rdx;
+            const float ey = ((float)(sy + (dy > 0.f)) * sbl - oy) * rdy;
+            const float ez = ((float)(sz + (dz > 0.f)) * sbl - oz) * rdz;
+            const float te = fminf(fminf(dx != 0.f ? ex : INFINITY, dy != 0.f ? ey : INFINITY),
+                                   dz != 0.f ? ez : INFINITY);
+            t = fmaxf(te, t) + 1e-4f * vl * inv_len;
+            prev_valid = false;
+            continue;
+        }
         if (cached_lookup(g, cache, bx, by, bz) < 0) {
             // exit of this block's box along the ray
             const float ex = ((float)(bx + (dx > 0.f)) * g.vbl - ox) * rdx;

@@ -220,10 +220,10 @@ __global__ void __launch_bounds__(256) track_iter_kernel(const uint16_t *__restr
         if (lane == 0) red[wid][k] = make_float2(a, b);
     }
     __syncthreads();
-    if (threadIdx.x < kTrackSums) {
+    if (threadIdx.x < kTrackSums) {  // value-major slots: partials[value][cta]
         float a = 0.f, b = 0.f;
         for (int w = 0; w < (int)(blockDim.x >> 5); w++) pair_add(a, b, red[w][threadIdx.x].x, red[w][threadIdx.x].y);
-        partials[(size_t)blockIdx.x * kTrackSums + threadIdx.x] = make_float2(a, b);
+        partials[(size_t)threadIdx.x * gridDim.x + blockIdx.x] = make_float2(a, b);
     }
     __threadfence();
     __syncthreads();
@@ -231,14 +231,17 @@ __global__ void __launch_bounds__(256) track_iter_kernel(const uint16_t *__restr
     __syncthreads();
     if (!last) return;
     __threadfence();
+    // last CTA: one warp per value, lanes stride over the CTA slots (coalesced), FP64 shuffle tree
     __shared__ double tot[kTrackSums];
-    if (threadIdx.x < kTrackSums) {
+    for (int v = wid; v < kTrackSums; v += (int)(blockDim.x >> 5)) {
         double a = 0.0;
-        for (unsigned b = 0; b < gridDim.x; b++) {
-            const float2 v = __ldcg(partials + (size_t)b * kTrackSums + threadIdx.x);
-            a += (double)v.x - (double)v.y;
+        for (unsigned b = lane; b < gridDim.x; b += 32) {
+            const float2 q = __ldcg(partials + (size_t)v * gridDim.x + b);
+            a += (double)q.x - (double)q.y;
         }
-        tot[threadIdx.x] = a;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+        if (lane == 0) tot[v] = a;
     }
     __syncthreads();
     if (threadIdx.x != 0) return;

@@ -51,7 +51,12 @@ struct Rng {
 inline double u01(uint64_t key) { return ((double)(splitmix(key) >> 11) + 0.5) * (1.0 / 9007199254740992.0); }
 
 // Trajectory of the camera centre: a smooth closed curve around the room
-// centre (radius ~ a quarter of the smaller horizontal extent).
+// centre (radius 0.16 of the smaller horizontal extent, one loop per 500
+// frames) at 0.3 of the room height. The camera turns 0.6 deg per frame about
+// the vertical and looks 25 +- 8 deg downwards, so every view holds a wall,
+// the floor and the objects standing on it (a view of one flat wall and one
+// sphere leaves a rotation that point-to-plane ICP cannot observe).
+// Per-frame motion: <= 6 mm and < 1 deg.
 void traj_point(const Scene &s, int t, int n, double phase, double *p, double *yaw, double *pitch) {
     const double cx = 0.5 * (s.room_lo[0] + s.room_hi[0]), cy = 0.5 * (s.room_lo[1] + s.room_hi[1]);
     const double h = s.room_hi[2] - s.room_lo[2];
@@ -60,9 +65,9 @@ void traj_point(const Scene &s, int t, int n, double phase, double *p, double *y
     const double w = 2.0 * M_PI / 500.0;  // one loop per 500 frames
     p[0] = cx + rad * std::cos(w * t + phase);
     p[1] = cy + 0.8 * rad * std::sin(w * t + phase);
-    p[2] = s.room_lo[2] + 0.45 * h + 0.05 * h * std::sin(2.3 * w * t);
-    *yaw = phase + (0.6 * M_PI / 180.0) * t;                       // 0.6 deg / frame
-    *pitch = (8.0 * M_PI / 180.0) * std::sin(1.7 * w * t + phase); // +-8 deg
+    p[2] = s.room_lo[2] + 0.30 * h + 0.04 * h * std::sin(2.3 * w * t);
+    *yaw = phase + (0.6 * M_PI / 180.0) * t;
+    *pitch = -(25.0 * M_PI / 180.0) + (8.0 * M_PI / 180.0) * std::sin(1.7 * w * t + phase);
     (void)n;
 }
 
@@ -152,6 +157,9 @@ void make_scene(Scene &s, int kind, uint64_t seed) {
         const double rho = std::sqrt(dx * dx + dy * dy);
         return std::fabs(rho - rad) > r + 0.45 && rho > r + 0.25;
     };
+    // Objects along the walls give every view structure in three directions
+    // (a view of only a wall and the floor cannot fix the motion along their
+    // intersection): spheres and boxes are spread over the four walls in turn.
     int tries = 0;
     while ((int)s.prims.size() < ns && tries < 100000) {
         tries++;
@@ -159,6 +167,13 @@ void make_scene(Scene &s, int kind, uint64_t seed) {
         p.kind = 0;
         p.r = rng.range(0.1, 0.4);
         for (int k = 0; k < 3; k++) p.c[k] = rng.range(p.r + 0.05, L[k] - p.r - 0.05);
+        const int idx = (int)s.prims.size();
+        if (idx % 2 == 0) {  // every other sphere rests on the floor near a wall
+            const int wall = (idx / 2) % 4;
+            const int ax = wall / 2;
+            p.c[ax] = (wall & 1) ? L[ax] - p.r - rng.range(0.05, 0.5) : p.r + rng.range(0.05, 0.5);
+            p.c[2] = p.r;
+        }
         if (!clear_of_path(p.c, p.r)) continue;
         for (int c = 0; c < 3; c++) p.col[c] = (uint8_t)rng.range(30, 255);
         s.prims.push_back(p);
@@ -171,7 +186,14 @@ void make_scene(Scene &s, int kind, uint64_t seed) {
         double half[3], c[3];
         for (int k = 0; k < 3; k++) half[k] = rng.range(0.08, 0.3);
         for (int k = 0; k < 3; k++) c[k] = rng.range(half[k] + 0.05, L[k] - half[k] - 0.05);
-        if (kind == 1 || rng.uni() < 0.5) c[2] = half[2];  // many boxes stand on the floor
+        if (nbox % 4 != 3) {  // three boxes in four stand on the floor against a wall
+            const int wall = nbox % 4;
+            const int ax = wall / 2;
+            c[ax] = (wall & 1) ? L[ax] - half[ax] : half[ax];
+            c[2] = half[2];
+        } else if (kind == 1 || rng.uni() < 0.5) {
+            c[2] = half[2];
+        }
         const double rr = std::sqrt(half[0] * half[0] + half[1] * half[1]);
         if (!clear_of_path(c, rr)) continue;
         for (int k = 0; k < 3; k++) {

@@ -98,6 +98,13 @@ class GPUVoxelGrid:
         """deIntegrate (GPUVoxelGrid.cpp:95-136)."""
         self._fuse(lib.ss_deintegrate, "deIntegrate", rgb, depth, extr, withColor, stream)
 
+    def integrate_fast(self, depth, extr, deint: bool = False, rgb=None, stream=None) -> None:
+        """The per-frame method's fusion (ss_integrate_fast): FMA arithmetic, nearest-pixel association."""
+        d = _dev_ptr(depth, 2, (self.resi, self.resj), "depth")
+        r = _dev_ptr(rgb, 1, (self.resi, self.resj, 3), "rgb") if rgb is not None else C.c_void_p()
+        check(lib.ss_integrate_fast(self._h, d, r, f32x16(extr), 1 if rgb is not None else 0, 1 if deint else 0,
+                                    _stream_ptr(stream)), "integrate_fast")
+
     def raycast(self, extr, stream=None, with_color: bool = True):
         """raycast (GPUVoxelGrid.cpp:139-147): fills rayPcd and rayColorPcd."""
         col = C.c_void_p(self.rayColorPcd.data_ptr()) if with_color else C.c_void_p()

@@ -23,3 +23,14 @@ def pytest_collection_modifyitems(config, items):
 
 
 INTR = (525.0, 525.0, 319.5, 239.5)
+
+
+def _ensure_built():
+    lib = ROOT / "superscanner_gb300" / "libss.so"
+    shim = ROOT / "superscanner_gb300" / "_build" / "shim_roundtrip"
+    if not lib.exists() or not shim.exists():
+        import __graft_entry__
+        __graft_entry__.build()
+
+
+_ensure_built()
