@@ -56,6 +56,10 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-error-check", action="store_true")
+    ap.add_argument("--buckets", type=int, default=BUCKETS,
+                    help="hash buckets (profiler captures use a smaller table to keep device memory small)")
+    ap.add_argument("--only", choices=["all", "chosen"], default="all",
+                    help="chosen: time the chosen form alone (for profiler captures)")
     return ap.parse_args()
 
 
@@ -139,13 +143,14 @@ class ClockSampler:
 
 # ----------------------------------------------------------------- GPU arm
 
-def run_form(torch, form: str, depth_dev, P, W: int, K: int, stream, barrier, profile=False, sampler=None):
+def run_form(torch, form: str, depth_dev, P, W: int, K: int, stream, barrier, profile=False, sampler=None,
+             buckets=BUCKETS):
     from superscanner_gb300 import GPUVoxelGrid
     from superscanner_gb300.pipeline import Pipeline
     storage, graph = {"plain": ("f32", False), "chosen": ("f16", True)}[form]
     if profile:
         graph = False
-    grid = GPUVoxelGrid(int(1e9), TRUNC, VL, ROWS, COLS, storage=storage, with_color=False, hash_buckets=BUCKETS,
+    grid = GPUVoxelGrid(int(1e9), TRUNC, VL, ROWS, COLS, storage=storage, with_color=False, hash_buckets=buckets,
                         max_weight=MAX_WEIGHT)
     grid.setIntrinsic(*INTR)
     pipe = Pipeline(grid, use_graph=graph, iters=ITERS, raycast_steps=STEPS_CAP)
@@ -341,9 +346,14 @@ def main_ours(args):
     sampler = ClockSampler(local) if rank == 0 else None
     if sampler:
         sampler.start()
-    chosen = run_form(torch, "chosen", depth_dev, P, W, K, stream, barrier, sampler=sampler)
+    chosen = run_form(torch, "chosen", depth_dev, P, W, K, stream, barrier, sampler=sampler, buckets=args.buckets)
     if sampler:
         sampler.stop()
+    if args.only == "chosen":
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": round(world * K / (chosen["ms"] * 1e-3), 2),
+                              "unit": "frames/s", "steps": K, "warmup": W, "only": "chosen"}), flush=True)
+        return
     plain = run_form(torch, "plain", depth_dev, P, W, K, stream, barrier)
     prof = run_form(torch, "chosen", depth_dev, P, W, K, stream, lambda: None, profile=True)
 
@@ -390,7 +400,7 @@ def main_ours(args):
     cpu = None
     if rank == 0:
         import oracle
-        sample_frames = 20
+        sample_frames = min(20, n - 1)
         times = cpu_reference_frames(depth, P, 1, sample_frames)
         cpu = {"value": round(sample_frames / sum(times), 4), "unit": "frames/s", "cores": oracle.threads(),
                "kind": "port",
