@@ -169,9 +169,14 @@ ss_status ss_kokkos_icp(const uint16_t *d1, const uint16_t *d2, int32_t rows, in
 
 /* Trilinear raycast: at most max_steps march steps per ray between t_min and
  * t_max (camera-frame depth). vertex_depth [resi][resj][4] = (x, y, z world,
- * depth), normal [resi][resj][4] = (nx, ny, nz, 0) world; misses are zero. */
+ * depth), normal [resi][resj][4] = (nx, ny, nz, 0) world; misses are zero.
+ * hint_depth (may be NULL): a u16-mm depth image taken at this pose; a ray
+ * whose pixel has depth d starts at d - hint_margin and marches from t_min
+ * again if that finds no surface (the reference's commented-out "cheat"
+ * raycast, GPUVoxelGrid.cpp:150-158, 571-582, starts at d - 0.1 m). */
 ss_status ss_raycast_maps(ss_grid *g, const float extr[16], int32_t max_steps, float t_min,
-                          float t_max, float *vertex_depth, float *normal, ss_stream_t s);
+                          float t_max, const uint16_t *hint_depth, float hint_margin,
+                          float *vertex_depth, float *normal, ss_stream_t s);
 
 typedef struct ss_pipeline ss_pipeline;
 
@@ -183,6 +188,7 @@ typedef struct ss_pipeline_params {
     float t_min, t_max;       /* raycast depth range */
     int32_t use_graph;        /* replay each tracked frame as one captured CUDA graph */
     int32_t exact_fusion;     /* reference voxel update (rounding, truncated pixel) instead of ss_integrate_fast's */
+    float hint_margin;        /* > 0: the model-view raycast starts at the fused frame's depth - hint_margin */
 } ss_pipeline_params;
 
 ss_status ss_pipeline_params_default(ss_pipeline_params *p);

@@ -50,7 +50,7 @@ for name, res, args in [
     ("orm_grid_set_round_pixel", None, [_p, _i]),
     ("orm_grid_fuse", _i, [_p, _p, _p, _i]),
     ("orm_grid_export", _i, [_p, _i, _p, _p, _p, _p]),
-    ("orm_raycast", None, [_p, _p, _i, C.c_double, C.c_double, _p, _p, _p]),
+    ("orm_raycast", None, [_p, _p, _i, C.c_double, C.c_double, _p, C.c_double, _p, _p, _p]),
     ("orm_track", _i, [_p, _i, _i, _f, _f, _f, _f, _p, _p, _p, _p, _i, _p, _p, C.c_double, C.c_double]),
 ]:
     fn = getattr(_lib, name)
@@ -209,12 +209,13 @@ class MethodGrid64:
         _lib.orm_grid_export(self._h, n, _ptr(keys), _ptr(coords), _ptr(sdf), _ptr(w))
         return dict(keys=keys, coords=coords, sdf=sdf, w=w)
 
-    def raycast(self, T, max_steps=128, t_min=0.2, t_max=10.0):
+    def raycast(self, T, max_steps=128, t_min=0.2, t_max=10.0, hint=None, hint_margin=0.0):
         vmap = np.zeros((self.resi, self.resj, 4), np.float64)
         nmap = np.zeros((self.resi, self.resj, 4), np.float64)
         steps = np.zeros((self.resi, self.resj), np.int32)
+        hint = np.ascontiguousarray(hint, np.uint16) if hint is not None else None
         _lib.orm_raycast(self._h, _ptr(np.ascontiguousarray(T, np.float64)), int(max_steps), float(t_min),
-                         float(t_max), _ptr(vmap), _ptr(nmap), _ptr(steps))
+                         float(t_max), _ptr(hint), float(hint_margin), _ptr(vmap), _ptr(nmap), _ptr(steps))
         return vmap, nmap, steps
 
 

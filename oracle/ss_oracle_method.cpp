@@ -263,13 +263,77 @@ int orm_grid_export(void *h, int max_blocks, uint64_t *keys, int32_t *coords, do
     return n;
 }
 
-// Trilinear raycast, same step rules as the GPU kernel, in double. vmap
-// [rows][cols][4] = (x, y, z, depth), nmap [rows][cols][4]; misses zero.
-// steps_out (optional) receives the march steps used per pixel.
-void orm_raycast(void *h, const double *T, int max_steps, double t_min, double t_max, double *vmap, double *nmap,
-                 int *steps_out) {
+// One march of the trilinear raycast from t0 (same step rules as the GPU
+// kernel, in double); returns true on a zero crossing with t = hit depth.
+static bool march64(const Grid64 &g, Cache &cache, double ox, double oy, double oz, double dx, double dy, double dz,
+                    double inv_len, double t0, double t_max, int max_steps, int &steps, double &t) {
+    const double vl = g.vl, vbl = g.vbl, sbl = 8 * vbl;
+    t = t0;
+    double t_prev = 0, f_prev = 0;
+    bool prev_valid = false;
+    while (steps < max_steps && t < t_max) {
+        const double px = ox + t * dx, py = oy + t * dy, pz = oz + t * dz;
+        const int bx = (int)std::floor(px / vbl), by = (int)std::floor(py / vbl), bz = (int)std::floor(pz / vbl);
+        steps++;
+        const int sx = floordiv8(bx), sy = floordiv8(by), sz = floordiv8(bz);
+        if (!g.supers.count(super_key(sx, sy, sz))) {
+            double te = INFINITY;
+            if (dx != 0) te = std::fmin(te, ((sx + (dx > 0)) * sbl - ox) / dx);
+            if (dy != 0) te = std::fmin(te, ((sy + (dy > 0)) * sbl - oy) / dy);
+            if (dz != 0) te = std::fmin(te, ((sz + (dz > 0)) * sbl - oz) / dz);
+            t = std::fmax(te, t) + 1e-4 * vl * inv_len;
+            prev_valid = false;
+            continue;
+        }
+        if (!cached(g, cache, bx, by, bz)) {
+            double te = INFINITY;
+            if (dx != 0) te = std::fmin(te, ((bx + (dx > 0)) * vbl - ox) / dx);
+            if (dy != 0) te = std::fmin(te, ((by + (dy > 0)) * vbl - oy) / dy);
+            if (dz != 0) te = std::fmin(te, ((bz + (dz > 0)) * vbl - oz) / dz);
+            t = std::fmax(te, t) + 1e-4 * vl * inv_len;
+            prev_valid = false;
+            continue;
+        }
+        const Sample sm = trilinear64(g, px, py, pz, cache);
+        if (!sm.valid) {
+            prev_valid = false;
+            t += vl * inv_len;
+            continue;
+        }
+        if (sm.f < 0) {
+            if (!(prev_valid && f_prev > 0)) return false;
+            double ta = t_prev, fa = f_prev, tb = t, fb = sm.f;
+            for (int r = 0; r < 2; r++) {
+                const double tc = ta + (tb - ta) * fa / (fa - fb);
+                const Sample q = trilinear64(g, ox + tc * dx, oy + tc * dy, oz + tc * dz, cache);
+                if (!q.valid) break;
+                if (q.f > 0) {
+                    ta = tc;
+                    fa = q.f;
+                } else {
+                    tb = tc;
+                    fb = q.f;
+                }
+            }
+            t = ta + (tb - ta) * fa / (fa - fb);
+            return true;
+        }
+        prev_valid = true;
+        t_prev = t;
+        f_prev = sm.f;
+        t += std::fmax(vl, 0.8 * sm.f) * inv_len;
+    }
+    return false;
+}
+
+// Trilinear raycast in double. vmap [rows][cols][4] = (x, y, z, depth), nmap
+// [rows][cols][4]; misses zero. hint (optional) is a u16-mm depth image at
+// this pose: rays with depth d start at d - hint_margin and march from t_min
+// again when that finds no crossing. steps_out (optional) receives the march
+// steps used per pixel.
+void orm_raycast(void *h, const double *T, int max_steps, double t_min, double t_max, const uint16_t *hint,
+                 double hint_margin, double *vmap, double *nmap, int *steps_out) {
     const Grid64 &g = *(Grid64 *)h;
-    const double vl = g.vl, vbl = g.vbl;
 #pragma omp parallel for schedule(dynamic, 2)
     for (int i = 0; i < g.resi; i++) {
         Cache cache;
@@ -279,65 +343,21 @@ void orm_raycast(void *h, const double *T, int max_steps, double t_min, double t
                          dz = T[8] * dcx + T[9] * dcy + T[10];
             const double ox = T[3], oy = T[7], oz = T[11];
             const double inv_len = 1.0 / std::sqrt(dx * dx + dy * dy + dz * dz);
-            double t = t_min, t_prev = 0, f_prev = 0;
-            bool prev_valid = false, hit = false;
-            int steps = 0;
-            while (steps < max_steps && t < t_max) {
-                const double px = ox + t * dx, py = oy + t * dy, pz = oz + t * dz;
-                const int bx = (int)std::floor(px / vbl), by = (int)std::floor(py / vbl), bz = (int)std::floor(pz / vbl);
-                steps++;
-                const int sx = floordiv8(bx), sy = floordiv8(by), sz = floordiv8(bz);
-                if (!g.supers.count(super_key(sx, sy, sz))) {
-                    const double sbl = 8 * vbl;
-                    double te = INFINITY;
-                    if (dx != 0) te = std::fmin(te, ((sx + (dx > 0)) * sbl - ox) / dx);
-                    if (dy != 0) te = std::fmin(te, ((sy + (dy > 0)) * sbl - oy) / dy);
-                    if (dz != 0) te = std::fmin(te, ((sz + (dz > 0)) * sbl - oz) / dz);
-                    t = std::fmax(te, t) + 1e-4 * vl * inv_len;
-                    prev_valid = false;
-                    continue;
-                }
-                if (!cached(g, cache, bx, by, bz)) {
-                    double te = INFINITY;
-                    if (dx != 0) te = std::fmin(te, ((bx + (dx > 0)) * vbl - ox) / dx);
-                    if (dy != 0) te = std::fmin(te, ((by + (dy > 0)) * vbl - oy) / dy);
-                    if (dz != 0) te = std::fmin(te, ((bz + (dz > 0)) * vbl - oz) / dz);
-                    t = std::fmax(te, t) + 1e-4 * vl * inv_len;
-                    prev_valid = false;
-                    continue;
-                }
-                const Sample sm = trilinear64(g, px, py, pz, cache);
-                if (!sm.valid) {
-                    prev_valid = false;
-                    t += vl * inv_len;
-                    continue;
-                }
-                if (sm.f < 0) {
-                    if (prev_valid && f_prev > 0) {
-                        double ta = t_prev, fa = f_prev, tb = t, fb = sm.f;
-                        for (int r = 0; r < 2; r++) {
-                            const double tc = ta + (tb - ta) * fa / (fa - fb);
-                            const Sample q = trilinear64(g, ox + tc * dx, oy + tc * dy, oz + tc * dz, cache);
-                            if (!q.valid) break;
-                            if (q.f > 0) {
-                                ta = tc;
-                                fa = q.f;
-                            } else {
-                                tb = tc;
-                                fb = q.f;
-                            }
-                        }
-                        t = ta + (tb - ta) * fa / (fa - fb);
-                        hit = true;
-                    }
-                    break;
-                }
-                prev_valid = true;
-                t_prev = t;
-                f_prev = sm.f;
-                t += std::fmax(vl, 0.8 * sm.f) * inv_len;
-            }
             const size_t pix = (size_t)i * g.resj + j;
+            int steps = 0;
+            double t = t_min;
+            bool hit;
+            const double th = hint ? hint[pix] * 1e-3 - hint_margin : 0.0;
+            if (hint && th > t_min) {
+                hit = march64(g, cache, ox, oy, oz, dx, dy, dz, inv_len, th, t_max, max_steps, steps, t);
+                if (!hit) {
+                    int steps2 = 0;
+                    hit = march64(g, cache, ox, oy, oz, dx, dy, dz, inv_len, t_min, t_max, max_steps, steps2, t);
+                    steps += steps2;
+                }
+            } else {
+                hit = march64(g, cache, ox, oy, oz, dx, dy, dz, inv_len, t_min, t_max, max_steps, steps, t);
+            }
             double *v = vmap + pix * 4, *n = nmap + pix * 4;
             for (int k = 0; k < 4; k++) v[k] = n[k] = 0;
             if (hit) {

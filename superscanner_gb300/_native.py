@@ -52,7 +52,7 @@ class SSPipelineParams(C.Structure):
     _fields_ = [
         ("levels", C.c_int32), ("iters", C.c_int32 * 4), ("dist_thresh", C.c_float * 4),
         ("raycast_steps", C.c_int32), ("t_min", C.c_float), ("t_max", C.c_float),
-        ("use_graph", C.c_int32), ("exact_fusion", C.c_int32),
+        ("use_graph", C.c_int32), ("exact_fusion", C.c_int32), ("hint_margin", C.c_float),
     ]
 
 
@@ -79,7 +79,7 @@ SIGNATURES = {
     "ss_normals_from_pcd": (_st, [_p, _i32, _i32, _p, _p]),
     "ss_kokkos_icp": (_st, [_p, _p, _i32, _i32, _f, _f, _f, _f, _D16, _D16, _i32, _D16,
                             C.POINTER(C.c_float), _p]),
-    "ss_raycast_maps": (_st, [_p, _F16, _i32, _f, _f, _p, _p, _p]),
+    "ss_raycast_maps": (_st, [_p, _F16, _i32, _f, _f, _p, _f, _p, _p, _p]),
     "ss_pipeline_params_default": (_st, [C.POINTER(SSPipelineParams)]),
     "ss_pipeline_create": (_st, [_p, C.POINTER(SSPipelineParams), C.POINTER(_p)]),
     "ss_pipeline_destroy": (_st, [_p]),

@@ -267,11 +267,13 @@ __device__ __forceinline__ void color_average(float &c, float w_old, float obs) 
     }
 }
 
-// Integrate / deintegrate the touched blocks: one warp per block, 16 voxels
-// per lane (voxel v = lane + 32 r, so every load and store of the warp is one
-// contiguous row of the block). Persistent: warps stride over the device-side
-// list, so the launch needs no host read of the block count (the reference
-// copies it to the host every call, GPUVoxelGrid.cpp:62-63).
+// Integrate / deintegrate the touched blocks. A work item is a quarter of a
+// block (128 voxels): one warp, 4 voxels per lane, voxel v = lane + 32 r, so
+// every load and store of the warp is one contiguous row of the block and the
+// 4 voxels of a lane are independent (their loads and depth gathers overlap).
+// Persistent: warps stride over 4 x (device-side list length) items, so the
+// launch needs no host read of the block count (the reference copies it to
+// the host every call, GPUVoxelGrid.cpp:62-63).
 // Voxel centres: the reference computes pzero + (k + 0.5) * vl in double and
 // rounds to float (GPUVoxelGrid.cpp:521); that double sum is exact for
 // |pzero| < 2^20 m, so one fmaf (single rounding of the exact value) gives the
@@ -284,37 +286,38 @@ __global__ void __launch_bounds__(256) fuse_kernel(GridView g, const uint16_t *_
     const int lane = threadIdx.x & 31;
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    const int n = *(volatile int *)&g.ctr->list_count;
+    const int n = 4 * *(volatile int *)&g.ctr->list_count;
     const int k = lane & 7, l0 = lane >> 3;
     const float inv_trunc = 1.0f / g.trunc;
     for (int t = warp; t < n; t += nwarps) {
-        const int bucket = __ldg(g.list + t);
+        const int bucket = __ldg(g.list + (t >> 2));
+        const int r0 = (t & 3) * 4;
         int bx, by, bz;
         unpack_coords(__ldg(g.stamp + bucket), bx, by, bz);
         // pzero = vbl * Kvec3f(x, y, z) (GPUVoxelGrid.cpp:501)
         const float pzx = __fmul_rn(g.vbl, (float)bx), pzy = __fmul_rn(g.vbl, (float)by),
                     pzz = __fmul_rn(g.vbl, (float)bz);
         const float cx = __fmaf_rn((float)k + 0.5f, g.vl, pzx);
-#pragma unroll 4
-        for (int r = 0; r < 16; r++) {
+#pragma unroll
+        for (int rr = 0; rr < 4; rr++) {
+            const int r = r0 + rr;
             const int l = l0 + 4 * (r & 1), m = r >> 1;
             const int v = lane + 32 * r;  // == k + 8 l + 64 m
             const F3 vm{cx, __fmaf_rn((float)l + 0.5f, g.vl, pzy), __fmaf_rn((float)m + 0.5f, g.vl, pzz)};
             const size_t vi = (size_t)bucket * kBlockVoxels + v;
+            float obs;
+            int pix;
+            if (!voxel_observe<kExact>(g, depth, E, Einv, Ez, vm, obs, pix)) continue;
             float s, w;
-            uint32_t word = 0;
             if (kStorage == SS_STORAGE_F32) {
                 const float2 sw = g.vox32[vi];
                 s = sw.x;
                 w = sw.y;
             } else {
-                word = g.vox16[vi];
+                const uint32_t word = g.vox16[vi];
                 s = __half2float(__ushort_as_half((unsigned short)(word & 0xffffu))) * g.trunc;
                 w = (float)(word >> 16);
             }
-            float obs;
-            int pix;
-            if (!voxel_observe<kExact>(g, depth, E, Einv, Ez, vm, obs, pix)) continue;
             if (kStorage == SS_STORAGE_F16 && kDeint && w == 0.f) continue;  // u16 weight cannot go negative
             const float w_old = w;
             running_average<kDeint, kExact>(s, w, obs, g.max_weight);

@@ -63,7 +63,8 @@ void inverse4_rounded(const float E[16], float out[16]);
 // counters (optional, device u64[4]): hash finds, voxel loads, march steps, hits
 ss_status launch_raycast_maps(ss_grid *g, const Mat34 &T, const FramePose *dpose, int max_steps, float t_min,
                               float t_max, float4 *vmap, float4 *nmap, cudaStream_t s,
-                              unsigned long long *counters = nullptr);
+                              unsigned long long *counters = nullptr, const uint16_t *hint = nullptr,
+                              float hint_margin = 0.f);
 
 // Blocks of persistent launches (multiple of the SM count).
 int persistent_ctas(const ss_grid *g, int per_sm);

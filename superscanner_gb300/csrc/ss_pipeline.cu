@@ -59,8 +59,10 @@ ss_status enqueue_fuse_raycast(ss_pipeline *P, cudaStream_t s, bool prof = false
                                /*manage_epoch=*/false, e1, e2);
     if (st != SS_OK) return st;
     if (prof) SS_CUDA_TRY(cudaEventRecord(next_event(P), s));
+    const bool hint = P->p.hint_margin > 0.f;
     st = launch_raycast_maps(g, dummy.E, &P->st->pose, P->p.raycast_steps, P->p.t_min, P->p.t_max, P->vmap,
-                             P->nmap, s, prof ? P->rc_counters : nullptr);
+                             P->nmap, s, prof ? P->rc_counters : nullptr, hint ? P->input : nullptr,
+                             P->p.hint_margin);
     if (st != SS_OK) return st;
     if (prof) SS_CUDA_TRY(cudaEventRecord(next_event(P), s));
     return SS_OK;
@@ -123,6 +125,7 @@ ss_status ss_pipeline_params_default(ss_pipeline_params *p) {
     p->t_max = 10.0f;
     p->use_graph = 1;
     p->exact_fusion = 0;
+    p->hint_margin = 0.f;
     return SS_OK;
 }
 

@@ -195,6 +195,9 @@ __global__ void __launch_bounds__(256) raycast_ref_kernel(GridView g, Mat34 Er, 
 //  * the sample is negative after a positive one: zero crossing; two
 //    regula-falsi refinements on the bracket, then the hit;
 //  * the sample is negative with no positive predecessor: no hit (back face).
+// With a depth hint (the frame just fused at this pose), a ray whose pixel has
+// a valid depth d starts at d - margin, and marches again from t_min when that
+// finds no crossing; steps of both marches count against max_steps each.
 // Every sample or skip counts as one step. The normal is the normalised
 // gradient of the trilinear interpolant at the hit (world frame, pointing
 // out of the surface). Outputs: vmap[i][j] = (x, y, z world, depth) and
@@ -242,16 +245,34 @@ __device__ __forceinline__ TriSample trilinear(const GridView &g, float px, floa
     const int ix = (int)fx0, iy = (int)fy0, iz = (int)fz0;
     const float ax = ux - fx0, ay = uy - fy0, az = uz - fz0;
     float s[8];
-#pragma unroll
-    for (int k = 0; k < 8; k++) {
-        const int vx = ix + (k & 1), vy = iy + ((k >> 1) & 1), vz = iz + (k >> 2);
-        const int bx = vx >> 3, by = vy >> 3, bz = vz >> 3;  // floor(v / 8)
-        const int b = cached_lookup(g, c, bx, by, bz);
+    if ((ix & 7) != 7 && (iy & 7) != 7 && (iz & 7) != 7) {
+        // all 8 corners in one block: one lookup, fixed offsets +1, +8, +64
+        const int b = cached_lookup(g, c, ix >> 3, iy >> 3, iz >> 3);
         if (b < 0) return r;
-        const float2 sw = voxel_sw<kStorage>(g, b, (vx & 7) + 8 * (vy & 7) + 64 * (vz & 7));
-        c.voxels++;
-        if (!(sw.y > 0.f)) return r;
-        s[k] = sw.x;
+        const int v0 = (ix & 7) + 8 * (iy & 7) + 64 * (iz & 7);
+        float2 sw[8];
+#pragma unroll
+        for (int k = 0; k < 8; k++) sw[k] = voxel_sw<kStorage>(g, b, v0 + (k & 1) + 8 * ((k >> 1) & 1) + 64 * (k >> 2));
+        c.voxels += 8;
+        bool ok = true;
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            ok &= sw[k].y > 0.f;
+            s[k] = sw[k].x;
+        }
+        if (!ok) return r;
+    } else {
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            const int vx = ix + (k & 1), vy = iy + ((k >> 1) & 1), vz = iz + (k >> 2);
+            const int bx = vx >> 3, by = vy >> 3, bz = vz >> 3;  // floor(v / 8)
+            const int b = cached_lookup(g, c, bx, by, bz);
+            if (b < 0) return r;
+            const float2 sw = voxel_sw<kStorage>(g, b, (vx & 7) + 8 * (vy & 7) + 64 * (vz & 7));
+            c.voxels++;
+            if (!(sw.y > 0.f)) return r;
+            s[k] = sw.x;
+        }
     }
     // lerp along x, then y, then z
     const float s00 = fmaf(ax, s[1] - s[0], s[0]), s10 = fmaf(ax, s[3] - s[2], s[2]);
@@ -269,11 +290,90 @@ __device__ __forceinline__ TriSample trilinear(const GridView &g, float px, floa
     return r;
 }
 
+// One ray march from t0; returns true on a zero crossing (t = hit depth).
+template <int kStorage>
+__device__ __forceinline__ bool march(const GridView &g, float ox, float oy, float oz, float dx, float dy, float dz,
+                                      float inv_len, float t0, float t_max, int max_steps, int &steps, float &t,
+                                      BlockCache &cache) {
+    const float vl = g.vl, inv_vl = 1.f / g.vl, inv_vbl = 1.f / g.vbl;
+    const float rdx = 1.f / dx, rdy = 1.f / dy, rdz = 1.f / dz;
+    const float sbl = g.vbl * (float)(1 << kSuperShift);
+    t = t0;
+    float t_prev = 0.f, f_prev = 0.f;
+    bool prev_valid = false;
+    int csx = INT_MIN, csy = INT_MIN, csz = INT_MIN;
+    bool cocc = false;
+    while (steps < max_steps && t < t_max) {
+        const float px = fmaf(t, dx, ox), py = fmaf(t, dy, oy), pz = fmaf(t, dz, oz);
+        const int bx = (int)floorf(px * inv_vbl), by = (int)floorf(py * inv_vbl), bz = (int)floorf(pz * inv_vbl);
+        steps++;
+        const int sx = bx >> kSuperShift, sy = by >> kSuperShift, sz = bz >> kSuperShift;
+        if (sx != csx || sy != csy || sz != csz) {
+            csx = sx;
+            csy = sy;
+            csz = sz;
+            cocc = super_occupied(g, sx, sy, sz);
+            cache.lookups++;
+        }
+        if (!cocc) {  // exit of this empty super-block's box along the ray
+            const float ex = ((float)(sx + (dx > 0.f)) * sbl - ox) * rdx;
+            const float ey = ((float)(sy + (dy > 0.f)) * sbl - oy) * rdy;
+            const float ez = ((float)(sz + (dz > 0.f)) * sbl - oz) * rdz;
+            const float te = fminf(fminf(dx != 0.f ? ex : INFINITY, dy != 0.f ? ey : INFINITY),
+                                   dz != 0.f ? ez : INFINITY);
+            t = fmaxf(te, t) + 1e-4f * vl * inv_len;
+            prev_valid = false;
+            continue;
+        }
+        if (cached_lookup(g, cache, bx, by, bz) < 0) {  // exit of this empty block's box
+            const float ex = ((float)(bx + (dx > 0.f)) * g.vbl - ox) * rdx;
+            const float ey = ((float)(by + (dy > 0.f)) * g.vbl - oy) * rdy;
+            const float ez = ((float)(bz + (dz > 0.f)) * g.vbl - oz) * rdz;
+            const float te = fminf(fminf(dx != 0.f ? ex : INFINITY, dy != 0.f ? ey : INFINITY),
+                                   dz != 0.f ? ez : INFINITY);
+            t = fmaxf(te, t) + 1e-4f * vl * inv_len;
+            prev_valid = false;
+            continue;
+        }
+        const TriSample sm = trilinear<kStorage, false>(g, px, py, pz, inv_vl, cache);
+        if (!sm.valid) {
+            prev_valid = false;
+            t += vl * inv_len;
+            continue;
+        }
+        if (sm.f < 0.f) {
+            if (!(prev_valid && f_prev > 0.f)) return false;  // back face
+            float ta = t_prev, fa = f_prev, tb = t, fb = sm.f;
+            for (int r = 0; r < 2; r++) {
+                const float tc = ta + (tb - ta) * fa / (fa - fb);
+                const TriSample q = trilinear<kStorage, false>(g, fmaf(tc, dx, ox), fmaf(tc, dy, oy),
+                                                               fmaf(tc, dz, oz), inv_vl, cache);
+                if (!q.valid) break;
+                if (q.f > 0.f) {
+                    ta = tc;
+                    fa = q.f;
+                } else {
+                    tb = tc;
+                    fb = q.f;
+                }
+            }
+            t = ta + (tb - ta) * fa / (fa - fb);
+            return true;
+        }
+        prev_valid = true;
+        t_prev = t;
+        f_prev = sm.f;
+        t += fmaxf(vl, 0.8f * sm.f) * inv_len;
+    }
+    return false;
+}
+
 template <int kStorage>
 __global__ void __launch_bounds__(256) raycast_maps_kernel(GridView g, Mat34 T, const FramePose *__restrict__ pose,
                                                            int max_steps, float t_min, float t_max,
                                                            float4 *__restrict__ vmap, float4 *__restrict__ nmap,
-                                                           unsigned long long *__restrict__ counters) {
+                                                           unsigned long long *__restrict__ counters,
+                                                           const uint16_t *__restrict__ hint, float hint_margin) {
     const int j = blockIdx.x * 32 + threadIdx.x;
     const int i = blockIdx.y * blockDim.y + threadIdx.y;
     const bool inside = i < g.resi && j < g.resj;
@@ -291,79 +391,21 @@ __global__ void __launch_bounds__(256) raycast_maps_kernel(GridView g, Mat34 T, 
     const float dz = fmaf(T.m[8], dcx, fmaf(T.m[9], dcy, T.m[10]));
     const float ox = T.m[3], oy = T.m[7], oz = T.m[11];
     const float inv_len = rsqrtf(fmaf(dx, dx, fmaf(dy, dy, dz * dz)));  // world length of dt = 1
-    const float vl = g.vl, inv_vl = 1.f / g.vl, inv_vbl = 1.f / g.vbl;
-    const float rdx = 1.f / dx, rdy = 1.f / dy, rdz = 1.f / dz;
+    const float inv_vl = 1.f / g.vl;
 
-    float t = t_min, t_prev = 0.f, f_prev = 0.f;
-    bool prev_valid = false;
-    const float sbl = g.vbl * (float)(1 << kSuperShift);
-    int csx = INT_MIN, csy = INT_MIN, csz = INT_MIN;
-    bool cocc = false;
-    while (steps < max_steps && t < t_max) {
-        const float px = fmaf(t, dx, ox), py = fmaf(t, dy, oy), pz = fmaf(t, dz, oz);
-        const int bx = (int)floorf(px * inv_vbl), by = (int)floorf(py * inv_vbl), bz = (int)floorf(pz * inv_vbl);
-        steps++;
-        const int sx = bx >> kSuperShift, sy = by >> kSuperShift, sz = bz >> kSuperShift;
-        if (sx != csx || sy != csy || sz != csz) {
-            csx = sx;
-            csy = sy;
-            csz = sz;
-            cocc = super_occupied(g, sx, sy, sz);
-            cache.lookups++;
+    float t = t_min;
+    const float t_hint = hint ? (float)__ldg(hint + (size_t)i * g.resj + j) * 1e-3f - hint_margin : 0.f;
+    if (hint && t_hint > t_min) {
+        // start near the depth this frame observed along the same ray; if that
+        // march finds no crossing, march the whole ray
+        hit = march<kStorage>(g, ox, oy, oz, dx, dy, dz, inv_len, t_hint, t_max, max_steps, steps, t, cache);
+        if (!hit) {
+            int steps2 = 0;
+            hit = march<kStorage>(g, ox, oy, oz, dx, dy, dz, inv_len, t_min, t_max, max_steps, steps2, t, cache);
+            steps += steps2;
         }
-        if (!cocc) {
-            // exit of this empty super-block's box along the ray
-            const float ex = ((float)(sx + (dx > 0.f)) * sbl - ox) * rdx;
-            const float ey = ((float)(sy + (dy > 0.f)) * sbl - oy) * rdy;
-            const float ez = ((float)(sz + (dz > 0.f)) * sbl - oz) * rdz;
-            const float te = fminf(fminf(dx != 0.f ? ex : INFINITY, dy != 0.f ? ey : INFINITY),
-                                   dz != 0.f ? ez : INFINITY);
-            t = fmaxf(te, t) + 1e-4f * vl * inv_len;
-            prev_valid = false;
-            continue;
-        }
-        if (cached_lookup(g, cache, bx, by, bz) < 0) {
-            // exit of this block's box along the ray
-            const float ex = ((float)(bx + (dx > 0.f)) * g.vbl - ox) * rdx;
-            const float ey = ((float)(by + (dy > 0.f)) * g.vbl - oy) * rdy;
-            const float ez = ((float)(bz + (dz > 0.f)) * g.vbl - oz) * rdz;
-            const float te = fminf(fminf(dx != 0.f ? ex : INFINITY, dy != 0.f ? ey : INFINITY),
-                                   dz != 0.f ? ez : INFINITY);
-            t = fmaxf(te, t) + 1e-4f * vl * inv_len;
-            prev_valid = false;
-            continue;
-        }
-        const TriSample sm = trilinear<kStorage, false>(g, px, py, pz, inv_vl, cache);
-        if (!sm.valid) {
-            prev_valid = false;
-            t += vl * inv_len;
-            continue;
-        }
-        if (sm.f < 0.f) {
-            if (prev_valid && f_prev > 0.f) {
-                float ta = t_prev, fa = f_prev, tb = t, fb = sm.f;
-                for (int r = 0; r < 2; r++) {
-                    const float tc = ta + (tb - ta) * fa / (fa - fb);
-                    const TriSample q = trilinear<kStorage, false>(g, fmaf(tc, dx, ox), fmaf(tc, dy, oy),
-                                                                   fmaf(tc, dz, oz), inv_vl, cache);
-                    if (!q.valid) break;
-                    if (q.f > 0.f) {
-                        ta = tc;
-                        fa = q.f;
-                    } else {
-                        tb = tc;
-                        fb = q.f;
-                    }
-                }
-                t = ta + (tb - ta) * fa / (fa - fb);
-                hit = true;
-            }
-            break;
-        }
-        prev_valid = true;
-        t_prev = t;
-        f_prev = sm.f;
-        t += fmaxf(vl, 0.8f * sm.f) * inv_len;
+    } else {
+        hit = march<kStorage>(g, ox, oy, oz, dx, dy, dz, inv_len, t_min, t_max, max_steps, steps, t, cache);
     }
     const size_t pix = (size_t)i * g.resj + j;
     float4 v = make_float4(0.f, 0.f, 0.f, 0.f), n = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -393,14 +435,15 @@ __global__ void __launch_bounds__(256) raycast_maps_kernel(GridView g, Mat34 T, 
 }
 
 ss_status launch_raycast_maps(ss_grid *g, const Mat34 &T, const FramePose *dpose, int max_steps, float t_min,
-                              float t_max, float4 *vmap, float4 *nmap, cudaStream_t s, unsigned long long *counters) {
+                              float t_max, float4 *vmap, float4 *nmap, cudaStream_t s, unsigned long long *counters,
+                              const uint16_t *hint, float hint_margin) {
     const dim3 blk(32, 8), grid((g->p.resj + 31) / 32, (g->p.resi + 7) / 8);
     if (g->p.storage == SS_STORAGE_F32)
-        raycast_maps_kernel<SS_STORAGE_F32>
-            <<<grid, blk, 0, s>>>(g->v, T, dpose, max_steps, t_min, t_max, vmap, nmap, counters);
+        raycast_maps_kernel<SS_STORAGE_F32><<<grid, blk, 0, s>>>(g->v, T, dpose, max_steps, t_min, t_max, vmap, nmap,
+                                                                 counters, hint, hint_margin);
     else
-        raycast_maps_kernel<SS_STORAGE_F16>
-            <<<grid, blk, 0, s>>>(g->v, T, dpose, max_steps, t_min, t_max, vmap, nmap, counters);
+        raycast_maps_kernel<SS_STORAGE_F16><<<grid, blk, 0, s>>>(g->v, T, dpose, max_steps, t_min, t_max, vmap, nmap,
+                                                                 counters, hint, hint_margin);
     SS_LAUNCH_CHECK();
     return SS_OK;
 }
@@ -427,11 +470,12 @@ extern "C" ss_status ss_raycast(ss_grid *g, const float extr[16], float *ray_pcd
 }
 
 extern "C" ss_status ss_raycast_maps(ss_grid *g, const float extr[16], int32_t max_steps, float t_min, float t_max,
-                                     float *vertex_depth, float *normal, ss_stream_t stream) {
+                                     const uint16_t *hint_depth, float hint_margin, float *vertex_depth,
+                                     float *normal, ss_stream_t stream) {
     if (!g || !extr || !vertex_depth || !normal || max_steps <= 0 || !(t_max > t_min)) return SS_ERR_ARG;
     if (!g->intr_set) return SS_ERR_STATE;
     for (int k = 0; k < 16; k++)
         if (!std::isfinite(extr[k])) return SS_ERR_ARG;
     return launch_raycast_maps(g, mat34_from(extr), nullptr, max_steps, t_min, t_max, (float4 *)vertex_depth,
-                               (float4 *)normal, (cudaStream_t)stream);
+                               (float4 *)normal, (cudaStream_t)stream, nullptr, hint_depth, hint_margin);
 }

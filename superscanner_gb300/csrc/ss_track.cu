@@ -72,10 +72,14 @@ __device__ void se3_left_update(const double *xi, double *T) {
     const double wx = xi[0], wy = xi[1], wz = xi[2];
     const double th2 = wx * wx + wy * wy + wz * wz, th = sqrt(th2);
     double A, B, C;
-    if (th < 1e-8) {
-        A = 1.0 - th2 / 6.0;
-        B = 0.5 - th2 / 24.0;
-        C = 1.0 / 6.0 - th2 / 120.0;
+    if (th < 0.05) {
+        // Maclaurin series of sin(t)/t, (1-cos t)/t^2, (t-sin t)/t^3 to t^8: the first
+        // omitted term is below 3e-21 for t < 0.05, so this is exact in double and
+        // avoids the FP64 sin/cos on the (serial) solve path.
+        const double t2 = th2;
+        A = 1.0 + t2 * (-1.0 / 6 + t2 * (1.0 / 120 + t2 * (-1.0 / 5040 + t2 * (1.0 / 362880))));
+        B = 0.5 + t2 * (-1.0 / 24 + t2 * (1.0 / 720 + t2 * (-1.0 / 40320 + t2 * (1.0 / 3628800))));
+        C = 1.0 / 6 + t2 * (-1.0 / 120 + t2 * (1.0 / 5040 + t2 * (-1.0 / 362880 + t2 * (1.0 / 39916800))));
     } else {
         A = sin(th) / th;
         B = (1.0 - cos(th)) / th2;
@@ -104,31 +108,40 @@ __device__ void se3_left_update(const double *xi, double *T) {
 }
 
 // Cholesky solve of A x = b (6x6 SPD, FP64). Returns false if A is not SPD.
+// Column-oriented (right-looking) so the updates of one column are independent
+// and pipeline; one reciprocal square root per column instead of a division
+// per element.
 __device__ bool cholesky6(const double *A, const double *b, double *x) {
-    double L[36];
-    for (int k = 0; k < 36; k++) L[k] = 0.0;
-    for (int i = 0; i < 6; i++) {
-        for (int j = 0; j <= i; j++) {
-            double s = A[i * 6 + j];
-            for (int k = 0; k < j; k++) s -= L[i * 6 + k] * L[j * 6 + k];
-            if (i == j) {
-                if (!(s > 1e-12)) return false;
-                L[i * 6 + i] = sqrt(s);
-            } else {
-                L[i * 6 + j] = s / L[j * 6 + j];
-            }
-        }
+    double L[36], inv[6];
+#pragma unroll
+    for (int k = 0; k < 36; k++) L[k] = A[k];
+#pragma unroll
+    for (int j = 0; j < 6; j++) {
+        const double d = L[j * 6 + j];
+        if (!(d > 1e-12)) return false;
+        const double r = rsqrt(d);
+        inv[j] = r;
+#pragma unroll
+        for (int i = j; i < 6; i++) L[i * 6 + j] *= r;  // L[j][j] = sqrt(d)
+#pragma unroll
+        for (int c = j + 1; c < 6; c++)
+#pragma unroll
+            for (int i = c; i < 6; i++) L[i * 6 + c] -= L[i * 6 + j] * L[c * 6 + j];
     }
     double y[6];
+#pragma unroll
     for (int i = 0; i < 6; i++) {
         double s = b[i];
+#pragma unroll
         for (int k = 0; k < i; k++) s -= L[i * 6 + k] * y[k];
-        y[i] = s / L[i * 6 + i];
+        y[i] = s * inv[i];
     }
+#pragma unroll
     for (int i = 5; i >= 0; i--) {
         double s = y[i];
+#pragma unroll
         for (int k = i + 1; k < 6; k++) s -= L[k * 6 + i] * x[k];
-        x[i] = s / L[i * 6 + i];
+        x[i] = s * inv[i];
     }
     return true;
 }
@@ -231,17 +244,23 @@ __global__ void __launch_bounds__(256) track_iter_kernel(const uint16_t *__restr
     __syncthreads();
     if (!last) return;
     __threadfence();
-    // last CTA: one warp per value, lanes stride over the CTA slots (coalesced), FP64 shuffle tree
+    // last CTA: one warp per value, lanes stride over the CTA slots (coalesced);
+    // (sum, compensation) pairs combine by TwoSum in FP32 and only the final
+    // value is widened to FP64 for the solve (FP64 is scarce on this part and
+    // a serial FP64 chain here stalls the whole GPU).
     __shared__ double tot[kTrackSums];
     for (int v = wid; v < kTrackSums; v += (int)(blockDim.x >> 5)) {
-        double a = 0.0;
-        for (unsigned b = lane; b < gridDim.x; b += 32) {
-            const float2 q = __ldcg(partials + (size_t)v * gridDim.x + b);
-            a += (double)q.x - (double)q.y;
+        float a = 0.f, b = 0.f;
+        for (unsigned q = lane; q < gridDim.x; q += 32) {
+            const float2 pq = __ldcg(partials + (size_t)v * gridDim.x + q);
+            pair_add(a, b, pq.x, pq.y);
         }
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
-        if (lane == 0) tot[v] = a;
+        for (int o = 16; o > 0; o >>= 1) {
+            const float a2 = __shfl_down_sync(0xffffffffu, a, o), b2 = __shfl_down_sync(0xffffffffu, b, o);
+            pair_add(a, b, a2, b2);
+        }
+        if (lane == 0) tot[v] = (double)a - (double)b;
     }
     __syncthreads();
     if (threadIdx.x != 0) return;

@@ -18,13 +18,14 @@ from .voxel_grid import GPUVoxelGrid, _stream_ptr
 
 
 def raycast_maps(grid: GPUVoxelGrid, extr, max_steps: int = 128, t_min: float = 0.2, t_max: float = 10.0,
-                 stream=None):
+                 hint_depth=None, hint_margin: float = 0.0, stream=None):
     """Trilinear raycast: (vertex_depth [H,W,4], normal [H,W,4]) CUDA tensors."""
     vmap = torch.empty((grid.resi, grid.resj, 4), dtype=torch.float32, device=grid.device)
     nmap = torch.empty_like(vmap)
-    check(lib.ss_raycast_maps(grid.handle, f32x16(extr), int(max_steps), float(t_min), float(t_max),
-                              C.c_void_p(vmap.data_ptr()), C.c_void_p(nmap.data_ptr()), _stream_ptr(stream)),
-          "raycast_maps")
+    hint = C.c_void_p(hint_depth.data_ptr()) if hint_depth is not None else C.c_void_p()
+    check(lib.ss_raycast_maps(grid.handle, f32x16(extr), int(max_steps), float(t_min), float(t_max), hint,
+                              float(hint_margin), C.c_void_p(vmap.data_ptr()), C.c_void_p(nmap.data_ptr()),
+                              _stream_ptr(stream)), "raycast_maps")
     return vmap, nmap
 
 
@@ -37,7 +38,7 @@ FORMS = {
 class Pipeline:
     def __init__(self, grid: GPUVoxelGrid, *, use_graph: bool = True, levels: int = 3, iters=(10, 5, 4),
                  dist=(0.06, 0.10, 0.15), raycast_steps: int = 128, t_min: float = 0.2, t_max: float = 10.0,
-                 exact_fusion: bool = False):
+                 exact_fusion: bool = False, hint_margin: float = 0.04):
         p = SSPipelineParams()
         check(lib.ss_pipeline_params_default(C.byref(p)), "pipeline_params_default")
         p.levels = levels
@@ -48,6 +49,7 @@ class Pipeline:
         p.t_min, p.t_max = float(t_min), float(t_max)
         p.use_graph = 1 if use_graph else 0
         p.exact_fusion = 1 if exact_fusion else 0
+        p.hint_margin = float(hint_margin)
         self.grid = grid
         self._h = C.c_void_p()
         check(lib.ss_pipeline_create(grid.handle, C.byref(p), C.byref(self._h)), "pipeline_create")

@@ -32,8 +32,8 @@ def pose_err(T, R):
     return np.linalg.norm(d[:3, 3]), np.arccos(np.clip((np.trace(d[:3, :3]) - 1) / 2, -1, 1))
 
 
-@pytest.mark.parametrize("storage", ["f32", "f16"])
-def test_raycast_maps_vs_fp64(storage):
+@pytest.mark.parametrize("storage,margin", [("f32", 0.0), ("f16", 0.0), ("f16", 0.04)])
+def test_raycast_maps_vs_fp64(storage, margin):
     P, depth = seq(6, 2)
     g = GPUVoxelGrid(int(1e9), TRUNC, VL, 480, 640, storage=storage, with_color=False, hash_buckets=1 << 18,
                      max_weight=255)
@@ -42,11 +42,12 @@ def test_raycast_maps_vs_fp64(storage):
     for k in range(6):
         g.integrate_fast(dev(depth[k]), P[k].astype(np.float32))
         o.fuse(depth[k], P[k])
-    v, n = raycast_maps(g, P[5].astype(np.float32))
+    hint = dev(depth[5]) if margin > 0 else None
+    v, n = raycast_maps(g, P[5].astype(np.float32), hint_depth=hint, hint_margin=margin)
     g.sync()
     v = v.cpu().numpy().astype(np.float64)
     n = n.cpu().numpy()
-    v64, n64, steps = o.raycast(P[5])
+    v64, n64, steps = o.raycast(P[5], hint=depth[5] if margin > 0 else None, hint_margin=margin)
     both = (v[..., 3] > 0) & (v64[..., 3] > 0)
     assert both.mean() > 0.85
     assert ((v[..., 3] > 0) == (v64[..., 3] > 0)).mean() > 0.99
