@@ -171,9 +171,10 @@ ss_status ss_kokkos_icp(const uint16_t *d1, const uint16_t *d2, int32_t rows, in
  * t_max (camera-frame depth). vertex_depth [resi][resj][4] = (x, y, z world,
  * depth), normal [resi][resj][4] = (nx, ny, nz, 0) world; misses are zero.
  * hint_depth (may be NULL): a u16-mm depth image taken at this pose; a ray
- * whose pixel has depth d starts at d - hint_margin and marches from t_min
- * again if that finds no surface (the reference's commented-out "cheat"
- * raycast, GPUVoxelGrid.cpp:150-158, 571-582, starts at d - 0.1 m). */
+ * whose pixel has depth d searches only [d - hint_margin, d + hint_margin],
+ * a ray without depth starts at the smallest depth of its 32-pixel row
+ * segment minus hint_margin (the reference's commented-out "cheat" raycast,
+ * GPUVoxelGrid.cpp:150-158, 571-582, starts at d - 0.1 m). */
 ss_status ss_raycast_maps(ss_grid *g, const float extr[16], int32_t max_steps, float t_min,
                           float t_max, const uint16_t *hint_depth, float hint_margin,
                           float *vertex_depth, float *normal, ss_stream_t s);

@@ -328,8 +328,9 @@ static bool march64(const Grid64 &g, Cache &cache, double ox, double oy, double 
 
 // Trilinear raycast in double. vmap [rows][cols][4] = (x, y, z, depth), nmap
 // [rows][cols][4]; misses zero. hint (optional) is a u16-mm depth image at
-// this pose: rays with depth d start at d - hint_margin and march from t_min
-// again when that finds no crossing. steps_out (optional) receives the march
+// this pose: a ray whose pixel has depth d searches [d - m, d + m]; a ray
+// without depth starts at the smallest depth of its 32-pixel row segment
+// minus m and marches on (m = hint_margin). steps_out (optional) receives the march
 // steps used per pixel.
 void orm_raycast(void *h, const double *T, int max_steps, double t_min, double t_max, const uint16_t *hint,
                  double hint_margin, double *vmap, double *nmap, int *steps_out) {
@@ -347,14 +348,22 @@ void orm_raycast(void *h, const double *T, int max_steps, double t_min, double t
             int steps = 0;
             double t = t_min;
             bool hit;
-            const double th = hint ? hint[pix] * 1e-3 - hint_margin : 0.0;
-            if (hint && th > t_min) {
-                hit = march64(g, cache, ox, oy, oz, dx, dy, dz, inv_len, th, t_max, max_steps, steps, t);
-                if (!hit) {
-                    int steps2 = 0;
-                    hit = march64(g, cache, ox, oy, oz, dx, dy, dz, inv_len, t_min, t_max, max_steps, steps2, t);
-                    steps += steps2;
+            // hint: own depth, else the smallest valid depth of the 32-pixel row segment
+            // (one GPU warp) holding this pixel
+            unsigned hmm = hint ? hint[pix] : 0u;
+            if (hint && hmm == 0) {
+                const int j0 = j / 32 * 32, j1 = std::min(j0 + 32, g.resj);
+                unsigned m = 0xffffffffu;
+                for (int q = j0; q < j1; q++) {
+                    const unsigned v = hint[(size_t)i * g.resj + q];
+                    if (v && v < m) m = v;
                 }
+                hmm = m != 0xffffffffu ? m : 0u;
+            }
+            const double th = hint ? hmm * 1e-3 - hint_margin : 0.0;
+            if (hint && th > t_min) {
+                const double t_end = hint[pix] ? std::fmin(t_max, th + 2 * hint_margin) : t_max;
+                hit = march64(g, cache, ox, oy, oz, dx, dy, dz, inv_len, th, t_end, max_steps, steps, t);
             } else {
                 hit = march64(g, cache, ox, oy, oz, dx, dy, dz, inv_len, t_min, t_max, max_steps, steps, t);
             }

@@ -195,9 +195,14 @@ __global__ void __launch_bounds__(256) raycast_ref_kernel(GridView g, Mat34 Er, 
 //  * the sample is negative after a positive one: zero crossing; two
 //    regula-falsi refinements on the bracket, then the hit;
 //  * the sample is negative with no positive predecessor: no hit (back face).
-// With a depth hint (the frame just fused at this pose), a ray whose pixel has
-// a valid depth d starts at d - margin, and marches again from t_min when that
-// finds no crossing; steps of both marches count against max_steps each.
+// With a depth hint (the frame just fused at this pose, so the same rays), a
+// ray whose pixel has depth d searches only [d - margin, d + margin]; a pixel
+// without depth (dropout) starts at the smallest depth of its warp's 32-pixel
+// row segment minus margin and marches on as usual. Where the fused frame saw
+// d, a crossing outside that window contradicts the frame just fused (it
+// shows up at silhouettes, through gaps of the thin band the trilinear
+// validity test leaves there), so the window loses no consistent surface and
+// keeps every lane of a warp within a few steps of the others.
 // Every sample or skip counts as one step. The normal is the normalised
 // gradient of the trilinear interpolant at the hit (world frame, pointing
 // out of the surface). Outputs: vmap[i][j] = (x, y, z world, depth) and
@@ -380,6 +385,15 @@ __global__ void __launch_bounds__(256) raycast_maps_kernel(GridView g, Mat34 T, 
     BlockCache cache{INT_MIN, INT_MIN, INT_MIN, -1, 0u, 0u};
     int steps = 0;
     bool hit = false;
+    // Depth hint of this ray: the fused frame's depth at this pixel, or, where
+    // that is missing (dropout), the smallest depth of the 32 pixels of this
+    // warp's row segment, so that no lane of the warp marches the whole ray.
+    unsigned hint_mm = 0;
+    if (hint) {
+        const unsigned own = inside ? (unsigned)__ldg(hint + (size_t)i * g.resj + j) : 0u;
+        const unsigned wmin = __reduce_min_sync(0xffffffffu, own ? own : 0xffffffffu);
+        hint_mm = own ? own : (wmin != 0xffffffffu ? wmin : 0u);
+    }
     if (inside) {
     if (pose) {
 #pragma unroll
@@ -394,16 +408,13 @@ __global__ void __launch_bounds__(256) raycast_maps_kernel(GridView g, Mat34 T, 
     const float inv_vl = 1.f / g.vl;
 
     float t = t_min;
-    const float t_hint = hint ? (float)__ldg(hint + (size_t)i * g.resj + j) * 1e-3f - hint_margin : 0.f;
+    const float t_hint = (float)hint_mm * 1e-3f - hint_margin;
     if (hint && t_hint > t_min) {
-        // start near the depth this frame observed along the same ray; if that
-        // march finds no crossing, march the whole ray
-        hit = march<kStorage>(g, ox, oy, oz, dx, dy, dz, inv_len, t_hint, t_max, max_steps, steps, t, cache);
-        if (!hit) {
-            int steps2 = 0;
-            hit = march<kStorage>(g, ox, oy, oz, dx, dy, dz, inv_len, t_min, t_max, max_steps, steps2, t, cache);
-            steps += steps2;
-        }
+        // a pixel with its own depth d searches [d - margin, d + margin]; a
+        // dropout pixel starts at its warp's smallest depth and marches on
+        const bool own = __ldg(hint + (size_t)i * g.resj + j) != 0;
+        const float t_end = own ? fminf(t_max, t_hint + 2.f * hint_margin) : t_max;
+        hit = march<kStorage>(g, ox, oy, oz, dx, dy, dz, inv_len, t_hint, t_end, max_steps, steps, t, cache);
     } else {
         hit = march<kStorage>(g, ox, oy, oz, dx, dy, dz, inv_len, t_min, t_max, max_steps, steps, t, cache);
     }
