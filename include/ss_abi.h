@@ -161,6 +161,19 @@ ss_status ss_kokkos_icp(const uint16_t *d1, const uint16_t *d2, int32_t rows, in
                         const double ty[16], int32_t icp_type, double txy_out[16],
                         float *rmse_out, ss_stream_t s);
 
+/* No counterpart in the reference. Same computation, arguments and results as
+ * ss_kokkos_icp, but it allocates nothing: for callers that cannot call
+ * cudaMalloc while tracking (a real-time thread, or a process whose device
+ * memory belongs to its own pool allocator). Its scratch is a fixed 11.2 MB
+ * device array that every GPU loading the library holds until exit; rows *
+ * cols above 640 x 480 return SS_ERR_DIMS. The first call on a device looks up
+ * the array's address and should come before any stream capture. Calls share
+ * the array: calls that overlap on the GPU race and must be serialised. */
+ss_status ss_kokkos_icp_noalloc(const uint16_t *d1, const uint16_t *d2, int32_t rows, int32_t cols,
+                                float fx, float fy, float cx, float cy, const double tx[16],
+                                const double ty[16], int32_t icp_type, double txy_out[16],
+                                float *rmse_out, ss_stream_t s);
+
 /* ------------------------------------------------------------------------
  * The per-frame method (no direct reference counterpart: the reference's
  * raycast is nearest-voxel with no normals and no step cap, GPUVoxelGrid.h:377,

@@ -79,6 +79,8 @@ SIGNATURES = {
     "ss_normals_from_pcd": (_st, [_p, _i32, _i32, _p, _p]),
     "ss_kokkos_icp": (_st, [_p, _p, _i32, _i32, _f, _f, _f, _f, _D16, _D16, _i32, _D16,
                             C.POINTER(C.c_float), _p]),
+    "ss_kokkos_icp_noalloc": (_st, [_p, _p, _i32, _i32, _f, _f, _f, _f, _D16, _D16, _i32, _D16,
+                                    C.POINTER(C.c_float), _p]),
     "ss_raycast_maps": (_st, [_p, _F16, _i32, _f, _f, _p, _f, _p, _p, _p]),
     "ss_pipeline_params_default": (_st, [C.POINTER(SSPipelineParams)]),
     "ss_pipeline_create": (_st, [_p, C.POINTER(SSPipelineParams), C.POINTER(_p)]),

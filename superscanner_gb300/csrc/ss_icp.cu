@@ -390,11 +390,84 @@ static ss_status icp_check_args(const uint16_t *d1, const uint16_t *d2, int rows
     return SS_OK;
 }
 
+// ------------------------------------------------- allocation-free variant
+// Scratch of ss_kokkos_icp_noalloc: the same three point / normal images, CTA
+// slots and solver state that ss_kokkos_icp takes from its lazily allocated
+// workspace, but in one statically sized device array that exists as soon as
+// the library is loaded, so the entry point never calls cudaMalloc. Every GPU
+// that loads the library holds these bytes until the process exits.
+constexpr size_t kNoAllocMaxPixels = 640 * 480;  // largest rows * cols accepted
+constexpr int kNoAllocCtas = 608;                // fixed upper bound of the iteration grid
+constexpr size_t kAlign256(size_t n) { return (n + 255) / 256 * 256; }
+constexpr size_t kNoAllocImage = kAlign256(kNoAllocMaxPixels * 3 * sizeof(float));
+constexpr size_t kNoAllocPartials = kAlign256((size_t)kNoAllocCtas * kIcpSums * sizeof(double));
+constexpr size_t kNoAllocBytes = 3 * kNoAllocImage + kNoAllocPartials + kAlign256(sizeof(IcpState));
+
+static __device__ __align__(256) unsigned char g_icp_noalloc_scratch[kNoAllocBytes];
+
+// Device address of the array on each device (the host-side symbol is only a
+// stand-in and must never be handed to a kernel). Filled on the first call
+// made with that device current.
+static std::mutex g_noalloc_mutex;
+static unsigned char *g_noalloc_addr[64] = {};
+
+static ss_status noalloc_scratch(int dev, unsigned char **out) {
+    if (dev < 0 || dev >= 64) return SS_ERR_ARG;
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_addr[dev]) {
+        void *ptr = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&ptr, g_icp_noalloc_scratch);
+        if (e != cudaSuccess || !ptr) {
+            set_last_error("cudaGetSymbolAddress(g_icp_noalloc_scratch)", e);
+            return SS_ERR_CUDA;
+        }
+        g_noalloc_addr[dev] = (unsigned char *)ptr;
+    }
+    *out = g_noalloc_addr[dev];
+    return SS_OK;
+}
+
 }  // namespace ss
 
 using namespace ss;
 
 extern "C" {
+
+// Same computation and arguments as ss_kokkos_icp, for callers that cannot
+// allocate device memory while they run: a tracking thread with a real-time
+// budget (cudaMalloc may synchronise the device and take milliseconds), or a
+// process whose device memory is handed out by its own pool allocator that
+// must stay the only allocator. Images larger than 640 x 480 pixels are
+// rejected with SS_ERR_DIMS. The first call on each device looks up the
+// scratch array's device address (cudaGetSymbolAddress); make that first call
+// before any stream capture. All calls share the one array and it keeps the
+// last call's contents: the per-call state is re-initialised by every call,
+// and two calls whose work overlaps on the GPU (different streams, or
+// different host threads) race on it, so serialise them.
+ss_status ss_kokkos_icp_noalloc(const uint16_t *d1, const uint16_t *d2, int32_t rows, int32_t cols, float fx,
+                                float fy, float cx, float cy, const double tx[16], const double ty[16],
+                                int32_t icp_type, double txy_out[16], float *rmse_out, ss_stream_t stream) {
+    ss_status st = icp_check_args(d1, d2, rows, cols, fx, fy, tx, ty, icp_type, txy_out);
+    if (st != SS_OK) return st;
+    if ((size_t)rows * (size_t)cols > kNoAllocMaxPixels) {
+        set_last_error_text("ss_kokkos_icp_noalloc: rows * cols exceeds the 640 x 480 scratch");
+        return SS_ERR_DIMS;
+    }
+    int dev = 0, sms = 0;
+    SS_CUDA_TRY(cudaGetDevice(&dev));
+    SS_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int ctas = sms * 4 < kNoAllocCtas ? sms * 4 : kNoAllocCtas;
+    unsigned char *base = nullptr;
+    st = noalloc_scratch(dev, &base);
+    if (st != SS_OK) return st;
+    float *xp = (float *)base, *yp = (float *)(base + kNoAllocImage), *yn = (float *)(base + 2 * kNoAllocImage);
+    double *partials = (double *)(base + 3 * kNoAllocImage);
+    IcpState *state = (IcpState *)(base + 3 * kNoAllocImage + kNoAllocPartials);
+    const Intr in{fx, fy, (float)rows - cy, cx};
+    return icp_ref_run(d1, d2, rows, cols, in, tx, ty, icp_type, xp, yp, yn, partials, ctas, state, txy_out,
+                       rmse_out, (cudaStream_t)stream);
+}
+
 
 ss_status ss_depth_to_pcd(const uint16_t *depth, int32_t rows, int32_t cols, float fx, float fy, float cx, float cy,
                           float *pcd, ss_stream_t stream) {

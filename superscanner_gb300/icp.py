@@ -29,3 +29,16 @@ def kokkos_icp(d1, d2, tx, ty, ICPType: int = PointToPoint, intrinsic=PRIMESENSE
                             float(fx), float(fy), float(cx), float(cy), f64x16(tx), f64x16(ty), int(ICPType), out,
                             C.byref(rmse), _stream_ptr(stream)), "kokkosICP")
     return np.array(out[:], dtype=np.float64).reshape(4, 4), float(rmse.value)
+
+
+def kokkos_icp_noalloc(d1, d2, tx, ty, ICPType: int = PointToPoint, intrinsic=PRIMESENSE, stream=None):
+    """kokkos_icp through ss_kokkos_icp_noalloc: no device allocation, scratch in a
+    fixed static device array (images up to 640 x 480; overlapping calls race)."""
+    rows, cols = d1.shape
+    out = (C.c_double * 16)()
+    rmse = C.c_float()
+    fx, fy, cx, cy = intrinsic
+    check(lib.ss_kokkos_icp_noalloc(_dev_ptr(d1, 2, (rows, cols), "d1"), _dev_ptr(d2, 2, (rows, cols), "d2"), rows,
+                                    cols, float(fx), float(fy), float(cx), float(cy), f64x16(tx), f64x16(ty),
+                                    int(ICPType), out, C.byref(rmse), _stream_ptr(stream)), "kokkosICP (no alloc)")
+    return np.array(out[:], dtype=np.float64).reshape(4, 4), float(rmse.value)
