@@ -150,12 +150,14 @@ def run_form(torch, form: str, depth_dev, P, W: int, K: int, stream, barrier, pr
     from superscanner_gb300 import GPUVoxelGrid
     from superscanner_gb300.pipeline import Pipeline
     storage, graph = {"plain": ("f32", False), "chosen": ("f16", True)}[form]
+    persistent = form == "chosen"
     if profile:
         graph = False
     grid = GPUVoxelGrid(int(1e9), TRUNC, VL, ROWS, COLS, storage=storage, with_color=False, hash_buckets=buckets,
                         max_weight=MAX_WEIGHT)
     grid.setIntrinsic(*INTR)
-    pipe = Pipeline(grid, use_graph=graph, iters=ITERS, raycast_steps=STEPS_CAP, hint_margin=HINT_MARGIN)
+    pipe = Pipeline(grid, use_graph=graph, iters=ITERS, raycast_steps=STEPS_CAP, hint_margin=HINT_MARGIN,
+                    persistent_track=persistent)
     with torch.cuda.stream(stream):
         pipe.set_pose(P[0], stream)
         pipe.frame(depth_dev[0], track=False, stream=stream)
@@ -197,7 +199,8 @@ def run_e2e(torch, host_depth_pinned, P, W: int, K: int, stream):
     grid = GPUVoxelGrid(int(1e9), TRUNC, VL, ROWS, COLS, storage="f16", with_color=False, hash_buckets=BUCKETS,
                         max_weight=MAX_WEIGHT)
     grid.setIntrinsic(*INTR)
-    pipe = Pipeline(grid, use_graph=True, iters=ITERS, raycast_steps=STEPS_CAP, hint_margin=HINT_MARGIN)
+    pipe = Pipeline(grid, use_graph=True, iters=ITERS, raycast_steps=STEPS_CAP, hint_margin=HINT_MARGIN,
+                    persistent_track=True)
     n = 1 + W + K
     poses = torch.zeros((n, 4, 4), dtype=torch.float64).pin_memory()
     with torch.cuda.stream(stream):
@@ -221,11 +224,72 @@ def run_e2e(torch, host_depth_pinned, P, W: int, K: int, stream):
     return dict(ms=ev0.elapsed_time(ev1), wall_s=wall, poses=poses.numpy().copy(), grid=grid, pipe=pipe)
 
 
+def se3_delta(rng, deg=2.0, cm=3.0):
+    """Seeded SE(3) correction: rotation up to deg about a random axis, translation up to cm."""
+    ax = rng.normal(size=3)
+    ax /= np.linalg.norm(ax)
+    a = np.radians(rng.uniform(0, deg))
+    K = np.array([[0, -ax[2], ax[1]], [ax[2], 0, -ax[0]], [-ax[1], ax[0], 0]])
+    D = np.eye(4)
+    D[:3, :3] = np.eye(3) + np.sin(a) * K + (1 - np.cos(a)) * K @ K
+    v = rng.normal(size=3)
+    D[:3, 3] = v / np.linalg.norm(v) * rng.uniform(0, cm / 100)
+    return D
+
+
+def run_refusion(torch, depth, P, stream, n_kf: int = 200):
+    """Config 4: the volume of the sequence (keyframes fused with seeded
+    rectangular occlusions, 20-100 % coverage), then n_kf keyframes re-fused
+    at poses corrected by seeded SE(3) deltas (<= 2 deg / 3 cm): one batched
+    ss_refuse_batch call vs the 2 n_kf sequential calls, same volume state."""
+    from superscanner_gb300 import GPUVoxelGrid, synth
+    n = len(depth)
+    n_kf = min(n_kf, n)
+    masks = synth.occlusion_masks(n_kf, ROWS, COLS, seed=99)
+    dep = depth.copy()
+    dep[:n_kf] = np.where(masks, dep[:n_kf], 0)
+    cover = masks.mean(axis=(1, 2))
+    dev = torch.from_numpy(dep.view(np.int16)).cuda()
+    rng = np.random.default_rng(31)
+    T_new = np.stack([se3_delta(rng) @ P[k] for k in range(n_kf)])
+    res = {}
+    dumps = {}
+    for mode in ("sequential", "batched"):
+        g = GPUVoxelGrid(int(1e9), TRUNC, VL, ROWS, COLS, storage="f16", with_color=False, hash_buckets=BUCKETS,
+                         max_weight=MAX_WEIGHT)
+        g.setIntrinsic(*INTR)
+        with torch.cuda.stream(stream):
+            for k in range(n):
+                g.integrate_fast(dev[k], P[k].astype(np.float32), stream=stream)
+            torch.cuda.synchronize()
+            ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            ev0.record(stream)
+            if mode == "batched":
+                g.refuse_batch([dev[k] for k in range(n_kf)], P[:n_kf], T_new, stream=stream)
+            else:
+                for k in range(n_kf):
+                    g.integrate_fast(dev[k], P[k].astype(np.float32), deint=True, stream=stream)
+                    g.integrate_fast(dev[k], T_new[k].astype(np.float32), stream=stream)
+            ev1.record(stream)
+            torch.cuda.synchronize()
+        g.sync(stream)
+        ms = ev0.elapsed_time(ev1)
+        res[mode] = {"ms": round(ms, 3), "keyframes_per_s": round(n_kf / (ms * 1e-3), 1)}
+        dumps[mode] = g.export_blocks(with_color=False)
+        g.close()
+    a, b = dumps["sequential"], dumps["batched"]
+    res["bit_identical"] = bool(np.array_equal(a["keys"], b["keys"]) and np.array_equal(a["w"], b["w"])
+                                and np.array_equal(a["sdf"], b["sdf"]))
+    res["speedup"] = round(res["sequential"]["ms"] / res["batched"]["ms"], 2)
+    res["keyframes"] = n_kf
+    res["coverage_min_max"] = [round(float(cover.min()), 3), round(float(cover.max()), 3)]
+    return res
+
+
 def roofline(stage_ms: dict, frames: int, touched: int, rc: dict, vox_bytes: int, peak: float, peak_kind: str):
     """Per-launch algorithmic bytes / time for every stage; the dominant one is reported."""
     npix = ROWS * COLS
     f = max(frames, 1)
-    n_it = sum(ITERS)
     track_px = sum(((ROWS + (1 << l) - 1) >> l) * ((COLS + (1 << l) - 1) >> l) * it for l, it in enumerate(ITERS))
     stages = {
         # touched blocks x 512 voxels x (read + write), plus the depth image the voxels project into
@@ -233,8 +297,9 @@ def roofline(stage_ms: dict, frames: int, touched: int, rc: dict, vox_bytes: int
         # hash finds (8-byte keys), voxel words, two float4 output maps
         "raycast_maps_kernel": ((rc["lookups"] * 8 + rc["voxels"] * vox_bytes) / f + 32 * npix,
                                 stage_ms["raycast"] / f, 1),
-        # per iteration: source depth (2 B) + model vertex and normal (2 x 16 B) per source pixel
-        "track_iter_kernel": (track_px * 34 / n_it, stage_ms["track"] / f / n_it, n_it),
+        # all Gauss-Newton iterations of a frame in one cooperative launch: per iteration
+        # and source pixel, depth (2 B) + model vertex and normal (2 x 16 B)
+        "track_frame_kernel": (track_px * 34, stage_ms["track"] / f, 1),
         # depth + per touched block a key probe, a stamp atomic and a list append
         "collect_kernel": (2 * npix + touched / f * 20, stage_ms["collect"] / f, 1),
     }
@@ -385,6 +450,8 @@ def main_ours(args):
             traffic = None
     roof["traffic"] = traffic
 
+    refusion = run_refusion(torch, depth, P, stream) if rank == 0 else None
+
     # accuracy: tracked poses vs ground truth, chosen vs plain, depth vs the FP64 oracle
     gt = P[n - 1]
     def pose_err(T, R):
@@ -433,6 +500,7 @@ def main_ours(args):
                     "d2h_bytes_per_step": 16 * 8, "wall_s": round(e2e["wall_s"], 4)},
             "gpu_launches": KERNELS_PER_FRAME * K,
             "accuracy": accuracy,
+            "refusion": refusion,
             "clocks": clocks,
         }
         print(json.dumps(line), flush=True)

@@ -116,6 +116,18 @@ ss_status ss_integrate_fast(ss_grid *g, const uint16_t *depth, const uint8_t *rg
                             const float extr[16], int32_t with_color, int32_t deint,
                             ss_stream_t s);
 
+/* Loop-closure re-fusion of n keyframes (n <= 256): for k = 0..n-1 in order,
+ * deintegrate depth k at T_old[k], then integrate it at T_new[k] — the
+ * reference's deIntegrate + integrate pair per re-fused frame
+ * (src/core/integrate.cpp:109-113, src/postprocessing/postprocessing.cpp:64-76)
+ * — as one collection launch and one persistent apply launch. depths: host
+ * array of n device pointers to [resi][resj] u16 images; T_old, T_new: n x 16
+ * row-major floats (host). Depth only. exact != 0 uses ss_integrate's
+ * arithmetic, else ss_integrate_fast's; the volume equals the 2n sequential
+ * calls bit for bit. */
+ss_status ss_refuse_batch(ss_grid *g, int32_t n, const uint16_t *const *depths, const float *T_old,
+                          const float *T_new, int32_t exact, ss_stream_t s);
+
 /* Synchronises the stream and returns (then clears) the device status word. */
 ss_status ss_grid_sync(ss_grid *g, ss_stream_t s);
 
@@ -203,6 +215,7 @@ typedef struct ss_pipeline_params {
     int32_t use_graph;        /* replay each tracked frame as one captured CUDA graph */
     int32_t exact_fusion;     /* reference voxel update (rounding, truncated pixel) instead of ss_integrate_fast's */
     float hint_margin;        /* > 0: the model-view raycast starts at the fused frame's depth - hint_margin */
+    int32_t persistent_track; /* all tracker iterations in one cooperative launch (else one launch each) */
 } ss_pipeline_params;
 
 ss_status ss_pipeline_params_default(ss_pipeline_params *p);

@@ -53,6 +53,7 @@ class SSPipelineParams(C.Structure):
         ("levels", C.c_int32), ("iters", C.c_int32 * 4), ("dist_thresh", C.c_float * 4),
         ("raycast_steps", C.c_int32), ("t_min", C.c_float), ("t_max", C.c_float),
         ("use_graph", C.c_int32), ("exact_fusion", C.c_int32), ("hint_margin", C.c_float),
+        ("persistent_track", C.c_int32),
     ]
 
 
@@ -70,6 +71,7 @@ SIGNATURES = {
     "ss_integrate_fast": (_st, [_p, _p, _p, _F16, _i32, _i32, _p]),
     "ss_raycast": (_st, [_p, _F16, _p, _p, _p]),
     "ss_clean_memory": (_st, [_p, _p]),
+    "ss_refuse_batch": (_st, [_p, _i32, _p, _p, _p, _i32, _p]),
     "ss_grid_sync": (_st, [_p, _p]),
     "ss_grid_block_count": (_st, [_p, _p, C.POINTER(_i32)]),
     "ss_grid_counters": (_st, [_p, _p, C.POINTER(C.c_int64)]),

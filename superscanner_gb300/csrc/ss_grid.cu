@@ -647,6 +647,9 @@ ss_status ss_grid_destroy(ss_grid *g) {
     cudaFree(g->v.vox16);
     cudaFree(g->v.rgb);
     cudaFree(g->v.sbkeys);
+    cudaFree(g->phase_mask);
+    cudaFree(g->batch_poses);
+    cudaFree((void *)g->batch_depths);
     delete g;
     return SS_OK;
 }

@@ -16,9 +16,16 @@ struct ss_grid {
     uint32_t host_epoch = 1;  // mirror of Counters::epoch for wrap handling
     int device = 0;
     int num_sms = 0;
+    // batched re-fusion scratch, allocated on the first ss_refuse_batch call
+    uint32_t *phase_mask = nullptr;        // [buckets][kMaxPhases / 32]
+    ss::FramePose *batch_poses = nullptr;  // [kMaxPhases]
+    const uint16_t **batch_depths = nullptr;  // [kMaxPhases / 2] device pointers
 };
 
 namespace ss {
+
+constexpr int kMaxPhases = 512;  // 2 x keyframes of one ss_refuse_batch call
+constexpr int kPhaseWords = kMaxPhases / 32;
 
 // Last CUDA error text of this thread (ss_last_error()).
 void set_last_error(const char *where, cudaError_t e);

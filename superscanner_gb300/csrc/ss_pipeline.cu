@@ -24,6 +24,7 @@ struct ss_pipeline {
     float4 *vmap = nullptr, *nmap = nullptr;
     uint16_t *input = nullptr;
     int ctas = 0;
+    int track_ctas = 0;  // co-resident CTAs of the persistent tracker
     bool have_model = false;
     cudaStream_t cap = nullptr;
     cudaGraph_t graph = nullptr;
@@ -80,7 +81,8 @@ ss_status enqueue_frame(ss_pipeline *P, cudaStream_t s, bool prof = false) {
     L.nmap = P->nmap;
     L.state = P->st;
     L.partials = P->partials;
-    L.ctas = P->ctas;
+    L.persistent = P->p.persistent_track != 0;
+    L.ctas = L.persistent ? P->track_ctas : P->ctas;
     L.levels = P->p.levels;
     for (int l = 0; l < kMaxLevels; l++) {
         L.iters[l] = P->p.iters[l];
@@ -126,6 +128,7 @@ ss_status ss_pipeline_params_default(ss_pipeline_params *p) {
     p->use_graph = 1;
     p->exact_fusion = 0;
     p->hint_margin = 0.f;
+    p->persistent_track = 0;
     return SS_OK;
 }
 
@@ -138,9 +141,11 @@ ss_status ss_pipeline_create(ss_grid *g, const ss_pipeline_params *params, ss_pi
     P->g = g;
     P->p = *params;
     P->ctas = g->num_sms * 2;
+    P->track_ctas = persistent_track_ctas(g->num_sms);
+    const int slot_ctas = P->ctas > P->track_ctas ? P->ctas : P->track_ctas;
     const size_t npix = (size_t)g->p.resi * g->p.resj;
     bool ok = cudaMalloc(&P->st, sizeof(TrackState)) == cudaSuccess &&
-              cudaMalloc(&P->partials, (size_t)P->ctas * 29 * sizeof(float2)) == cudaSuccess &&
+              cudaMalloc(&P->partials, 2 * (size_t)slot_ctas * 29 * sizeof(float2)) == cudaSuccess &&
               cudaMalloc(&P->vmap, npix * sizeof(float4)) == cudaSuccess &&
               cudaMalloc(&P->nmap, npix * sizeof(float4)) == cudaSuccess &&
               cudaMalloc(&P->input, npix * sizeof(uint16_t)) == cudaSuccess &&

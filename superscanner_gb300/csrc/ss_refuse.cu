@@ -1,0 +1,318 @@
+// ss_refuse.cu — batched loop-closure re-fusion: for keyframes k = 0..n-1 in
+// order, deintegrate depth k at its old pose and integrate it at its new one
+// (the reference does these as 2n separate deIntegrate / integrate calls,
+// src/core/integrate.cpp:109-113 and src/postprocessing/postprocessing.cpp:64-76,
+// each with a block collection, a D2H count read and a device fence).
+//
+// Two launches for the whole batch:
+//  1. refuse_collect_kernel, grid (tiles, phases): phase 2k deintegrates and
+//     2k+1 integrates keyframe k. Each pixel's candidate blocks are found or
+//     inserted as in collect_kernel; the first visitor of the batch appends
+//     the block to the list, and every phase ORs its bit into the block's
+//     512-bit phase mask.
+//  2. refuse_apply_kernel, persistent: warps pull quarter-block items from an
+//     atomic counter (blocks carry very different numbers of phases when
+//     keyframes are partly occluded), keep their 4 voxels per lane in
+//     registers and apply the block's phases in ascending order.
+// Every voxel thus sees exactly the updates of the 2n sequential calls, in
+// the same order, with the same arithmetic, so the volume is bit-identical to
+// them (precision form included: the value is re-quantised to half after
+// every phase as a sequential store would). Only the aliasing rule differs:
+// an aliased entry takes the largest packed coordinate of the whole batch.
+#include "ss_grid_impl.cuh"
+
+namespace ss {
+
+__global__ void __launch_bounds__(256) refuse_collect_kernel(GridView g, const uint16_t *const *__restrict__ depths,
+                                                             const FramePose *__restrict__ poses,
+                                                             uint32_t *__restrict__ phase_mask) {
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x;
+    const int j = blockIdx.x * 32 + threadIdx.x;
+    const int i = blockIdx.y * blockDim.y + threadIdx.y;
+    const int phase = blockIdx.z;
+    const uint16_t *depth = depths[phase >> 1];
+    Mat34 E;
+#pragma unroll
+    for (int k = 0; k < 12; k++) E.m[k] = __ldg(&poses[phase].E.m[k]);
+    const uint32_t epoch = *(volatile uint32_t *)&g.ctr->epoch;
+
+    int lox = 0, loy = 0, loz = 0, nx = 0, ny = 0, nz = 0;
+    if (i < g.resi && j < g.resj) {
+        const F3 p = get_point(g.in, i, j, depth_m(__ldg(depth + (size_t)i * g.resj + j)));
+        if (p.z > g.rmin) {
+            const F3 pt = xform(E, p);
+            const F3 t{g.trunc, g.trunc, g.trunc};
+            const F3 lo = f3sub(pt, t), hi = f3add(pt, t);
+            lox = idx_rule(lo.x, g.vbl);
+            loy = idx_rule(lo.y, g.vbl);
+            loz = idx_rule(lo.z, g.vbl);
+            nx = idx_rule(hi.x, g.vbl) - lox + 1;
+            ny = idx_rule(hi.y, g.vbl) - loy + 1;
+            nz = idx_rule(hi.z, g.vbl) - loz + 1;
+            if (nx < 1 || ny < 1 || nz < 1 || nx > 8 || ny > 8 || nz > 8) {
+                atomicOr(&g.ctr->status, kStRange);
+                nx = ny = nz = 0;
+            }
+        }
+    }
+    const int total = nx * ny * nz;
+    const unsigned lt = (1u << lane) - 1u;
+    const uint32_t bit = 1u << (phase & 31);
+    const int word = phase >> 5;
+    for (int c = 0;; c++) {
+        bool act = c < total;
+        if (!__any_sync(FULL, act)) break;
+        unsigned long long packed = 0, key = 0;
+        if (act) {
+            const int z = loz + c % nz, y = loy + (c / nz) % ny, x = lox + c / (nz * ny);
+            if (packable(x, y, z)) {
+                packed = pack_coords(x, y, z);
+                key = prime_hash(x, y, z);
+            } else {
+                atomicOr(&g.ctr->status, kStRange);
+                act = false;
+            }
+        }
+        const unsigned am = __ballot_sync(FULL, act);
+        bool append = false;
+        int bucket = -1;
+        if (act) {
+            const unsigned peers = __match_any_sync(am, packed);
+            if (__ffs(peers) - 1 == lane) {
+                bool inserted = false;
+                bucket = table_find_or_insert(g, key, &inserted);
+                if (inserted) {
+                    int x, y, z;
+                    unpack_coords(packed, x, y, z);
+                    super_insert(g, x, y, z);
+                }
+                if (bucket >= 0) {
+                    const unsigned long long mine = ((unsigned long long)epoch << kEpochShift) | packed;
+                    const unsigned long long old = atomicMax(g.stamp + bucket, mine);
+                    append = (uint32_t)(old >> kEpochShift) != epoch;
+                    atomicOr(phase_mask + (size_t)bucket * kPhaseWords + word, bit);
+                }
+            }
+        }
+        const unsigned ap = __ballot_sync(FULL, append);
+        if (ap) {
+            const int leader = __ffs(ap) - 1;
+            int base = 0;
+            if (lane == leader) base = atomicAdd(&g.ctr->list_count, __popc(ap));
+            base = __shfl_sync(FULL, base, leader);
+            if (append) {
+                const int idx = base + __popc(ap & lt);
+                if (idx <= (int)g.mask) g.list[idx] = bucket;
+                else atomicOr(&g.ctr->status, kStListOverflow);
+            }
+        }
+    }
+}
+
+// The per-voxel observation and update of ss_grid.cu's fuse path.
+template <bool kExact>
+__device__ bool voxel_observe_b(const GridView &g, const uint16_t *__restrict__ depth, const FramePose &fp, F3 vm,
+                                float &sdf) {
+    F3 q;
+    float c0, c1;
+    const Mat34 &E = fp.E, &Einv = fp.Einv;
+    if (kExact) {
+        q = xform(Einv, vm);
+        c0 = __fadd_rn(__fdiv_rn(__fmul_rn(q.y, g.in.fy), q.z), g.in.ci);
+        c1 = __fadd_rn(__fdiv_rn(__fmul_rn(q.x, g.in.fx), q.z), g.in.cj);
+    } else {
+        q.x = fmaf(vm.x, Einv.m[0], fmaf(vm.y, Einv.m[1], fmaf(vm.z, Einv.m[2], Einv.m[3])));
+        q.y = fmaf(vm.x, Einv.m[4], fmaf(vm.y, Einv.m[5], fmaf(vm.z, Einv.m[6], Einv.m[7])));
+        q.z = fmaf(vm.x, Einv.m[8], fmaf(vm.y, Einv.m[9], fmaf(vm.z, Einv.m[10], Einv.m[11])));
+        const float rz = __frcp_rn(q.z);
+        c0 = fmaf(q.y * g.in.fy, rz, g.in.ci);
+        c1 = fmaf(q.x * g.in.fx, rz, g.in.cj);
+    }
+    const int cori = kExact ? __float2int_rz(c0) : __float2int_rd(c0 + 0.5f);
+    const int corj = kExact ? __float2int_rz(c1) : __float2int_rd(c1 + 0.5f);
+    if (!(cori < g.resi && corj < g.resj && cori >= 0 && corj >= 0)) return false;
+    const uint16_t dmm = __ldg(depth + cori * g.resj + corj);
+    F3 vpt;
+    if (kExact) {
+        vpt = get_point(g.in, cori, corj, depth_m(dmm));
+        if (!(vpt.z > g.rmin)) return false;
+        vpt = xform(E, vpt);
+        sdf = f3dot(f3sub(vpt, vm), F3{fp.Ez[0], fp.Ez[1], fp.Ez[2]});
+    } else {
+        const float d = (float)dmm * 1.0e-3f;
+        if (!(d > g.rmin)) return false;
+        const float px = ((float)corj - g.in.cj) * __frcp_rn(g.in.fx) * d;
+        const float py = ((float)cori - g.in.ci) * __frcp_rn(g.in.fy) * d;
+        vpt.x = fmaf(px, E.m[0], fmaf(py, E.m[1], fmaf(d, E.m[2], E.m[3])));
+        vpt.y = fmaf(px, E.m[4], fmaf(py, E.m[5], fmaf(d, E.m[6], E.m[7])));
+        vpt.z = fmaf(px, E.m[8], fmaf(py, E.m[9], fmaf(d, E.m[10], E.m[11])));
+        sdf = (vpt.x - vm.x) * fp.Ez[0] + (vpt.y - vm.y) * fp.Ez[1] + (vpt.z - vm.z) * fp.Ez[2];
+    }
+    return fabsf(sdf) < g.trunc;
+}
+
+template <int kStorage, bool kExact>
+__global__ void __launch_bounds__(256) refuse_apply_kernel(GridView g, const uint16_t *const *__restrict__ depths,
+                                                           const FramePose *__restrict__ poses,
+                                                           const uint32_t *__restrict__ phase_mask) {
+    const int lane = threadIdx.x & 31;
+    const int n = 4 * *(volatile int *)&g.ctr->list_count;
+    const int k = lane & 7, l0 = lane >> 3;
+    const float inv_trunc = 1.0f / g.trunc;
+    for (;;) {
+        int t = 0;
+        if (lane == 0) t = atomicAdd(&g.ctr->work, 1);
+        t = __shfl_sync(0xffffffffu, t, 0);
+        if (t >= n) break;
+        const int bucket = __ldg(g.list + (t >> 2));
+        const int r0 = (t & 3) * 4;
+        int bx, by, bz;
+        unpack_coords(__ldg(g.stamp + bucket) & ((1ull << kEpochShift) - 1ull), bx, by, bz);
+        const float pzx = __fmul_rn(g.vbl, (float)bx), pzy = __fmul_rn(g.vbl, (float)by),
+                    pzz = __fmul_rn(g.vbl, (float)bz);
+        const float cx = __fmaf_rn((float)k + 0.5f, g.vl, pzx);
+        F3 vm[4];
+        float s[4], w[4];
+        bool changed[4];
+#pragma unroll
+        for (int rr = 0; rr < 4; rr++) {
+            const int r = r0 + rr, l = l0 + 4 * (r & 1), m = r >> 1;
+            vm[rr] = F3{cx, __fmaf_rn((float)l + 0.5f, g.vl, pzy), __fmaf_rn((float)m + 0.5f, g.vl, pzz)};
+            const size_t vi = (size_t)bucket * kBlockVoxels + lane + 32 * r;
+            if (kStorage == SS_STORAGE_F32) {
+                const float2 sw = g.vox32[vi];
+                s[rr] = sw.x;
+                w[rr] = sw.y;
+            } else {
+                const uint32_t word = g.vox16[vi];
+                s[rr] = __half2float(__ushort_as_half((unsigned short)(word & 0xffffu))) * g.trunc;
+                w[rr] = (float)(word >> 16);
+            }
+            changed[rr] = false;
+        }
+        const uint32_t *mask = phase_mask + (size_t)bucket * kPhaseWords;
+        for (int wi = 0; wi < kPhaseWords; wi++) {
+            uint32_t bits = __ldg(mask + wi);
+            while (bits) {
+                const int phase = wi * 32 + __ffs(bits) - 1;
+                bits &= bits - 1;
+                const bool deint = (phase & 1) == 0;
+                const FramePose fp = poses[phase];
+                const uint16_t *depth = depths[phase >> 1];
+#pragma unroll
+                for (int rr = 0; rr < 4; rr++) {
+                    float obs;
+                    if (!voxel_observe_b<kExact>(g, depth, fp, vm[rr], obs)) continue;
+                    if (kStorage == SS_STORAGE_F16 && deint && w[rr] == 0.f) continue;
+                    float sv = s[rr], wv = w[rr];
+                    if (deint) {
+                        if (wv != 1.f) {
+                            const float w1 = kExact ? __fsub_rn(wv, 1.f) : wv - 1.f;
+                            sv = kExact ? __fdiv_rn(__fsub_rn(__fmul_rn(sv, wv), obs), w1)
+                                        : __fdividef(fmaf(sv, wv, -obs), w1);
+                            wv = w1;
+                        } else {
+                            wv = 0.f;
+                            sv = 0.f;
+                        }
+                    } else {
+                        const float w1 = kExact ? __fadd_rn(wv, 1.f) : wv + 1.f;
+                        sv = kExact ? __fdiv_rn(__fadd_rn(__fmul_rn(sv, wv), obs), w1) : __fdividef(fmaf(sv, wv, obs), w1);
+                        wv = (g.max_weight > 0.f && w1 > g.max_weight) ? g.max_weight : w1;
+                    }
+                    if (kStorage == SS_STORAGE_F16) {  // the value a sequential call would have stored
+                        sv = __half2float(__float2half_rn(sv * inv_trunc)) * g.trunc;
+                        wv = fminf(wv, 65535.f);
+                    }
+                    s[rr] = sv;
+                    w[rr] = wv;
+                    changed[rr] = true;
+                }
+            }
+        }
+#pragma unroll
+        for (int rr = 0; rr < 4; rr++) {
+            if (!changed[rr]) continue;
+            const size_t vi = (size_t)bucket * kBlockVoxels + lane + 32 * (r0 + rr);
+            if (kStorage == SS_STORAGE_F32) {
+                g.vox32[vi] = make_float2(s[rr], w[rr]);
+            } else {
+                const unsigned short hs = __half_as_ushort(__float2half_rn(s[rr] * inv_trunc));
+                g.vox16[vi] = (uint32_t)hs | ((uint32_t)w[rr] << 16);
+            }
+        }
+    }
+}
+
+// Clears the phase masks of the listed blocks, then ends the call like finalize_kernel.
+__global__ void refuse_finalize_kernel(GridView g, uint32_t *phase_mask) {
+    const int n = *(volatile int *)&g.ctr->list_count;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n * kPhaseWords; t += gridDim.x * blockDim.x)
+        phase_mask[(size_t)g.list[t / kPhaseWords] * kPhaseWords + t % kPhaseWords] = 0u;
+}
+
+__global__ void refuse_counters_kernel(Counters *ctr) {
+    const int n = ctr->list_count;
+    ctr->last_touched = n;
+    ctr->touched_total += (unsigned long long)n;
+    ctr->calls += 1ull;
+    ctr->list_count = 0;
+    ctr->work = 0;
+    ctr->epoch = ctr->epoch + 1u;
+}
+
+}  // namespace ss
+
+using namespace ss;
+
+extern "C" ss_status ss_refuse_batch(ss_grid *g, int32_t n, const uint16_t *const *depths, const float *T_old,
+                                     const float *T_new, int32_t exact, ss_stream_t stream) {
+    if (!g || n < 0 || (n > 0 && (!depths || !T_old || !T_new))) return SS_ERR_ARG;
+    if (!g->intr_set) return SS_ERR_STATE;
+    if (2 * n > kMaxPhases) return SS_ERR_DIMS;
+    if (n == 0) return SS_OK;
+    for (int k = 0; k < n; k++) {
+        if (!depths[k]) return SS_ERR_ARG;
+        for (int q = 0; q < 16; q++)
+            if (!std::isfinite(T_old[k * 16 + q]) || !std::isfinite(T_new[k * 16 + q])) return SS_ERR_ARG;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    if (!g->phase_mask) {
+        const size_t B = (size_t)g->p.hash_buckets;
+        if (cudaMalloc(&g->phase_mask, B * kPhaseWords * sizeof(uint32_t)) != cudaSuccess ||
+            cudaMalloc(&g->batch_poses, kMaxPhases * sizeof(FramePose)) != cudaSuccess ||
+            cudaMalloc(&g->batch_depths, (kMaxPhases / 2) * sizeof(uint16_t *)) != cudaSuccess) {
+            cudaGetLastError();
+            return SS_ERR_NOMEM;
+        }
+        SS_CUDA_TRY(cudaMemsetAsync(g->phase_mask, 0, B * kPhaseWords * sizeof(uint32_t), s));
+    }
+    if (g->host_epoch >= kEpochMax) {
+        ss_status st = rebase_epoch(g, s);
+        if (st != SS_OK) return st;
+    }
+    FramePose hp[kMaxPhases];
+    for (int k = 0; k < n; k++) {
+        hp[2 * k] = frame_pose_from(T_old + 16 * k);
+        hp[2 * k + 1] = frame_pose_from(T_new + 16 * k);
+    }
+    SS_CUDA_TRY(cudaMemcpyAsync(g->batch_poses, hp, 2 * n * sizeof(FramePose), cudaMemcpyHostToDevice, s));
+    SS_CUDA_TRY(cudaMemcpyAsync(g->batch_depths, depths, n * sizeof(uint16_t *), cudaMemcpyHostToDevice, s));
+    SS_CUDA_TRY(cudaMemsetAsync(&g->v.ctr->work, 0, sizeof(int), s));
+    const dim3 cblk(32, 8), cgrid((g->p.resj + 31) / 32, (g->p.resi + 7) / 8, 2 * n);
+    refuse_collect_kernel<<<cgrid, cblk, 0, s>>>(g->v, g->batch_depths, g->batch_poses, g->phase_mask);
+    SS_LAUNCH_CHECK();
+    const int ctas = persistent_ctas(g, 8);
+    const bool f32 = g->p.storage == SS_STORAGE_F32;
+    if (f32 && exact) refuse_apply_kernel<SS_STORAGE_F32, true><<<ctas, 256, 0, s>>>(g->v, g->batch_depths, g->batch_poses, g->phase_mask);
+    else if (f32) refuse_apply_kernel<SS_STORAGE_F32, false><<<ctas, 256, 0, s>>>(g->v, g->batch_depths, g->batch_poses, g->phase_mask);
+    else if (exact) refuse_apply_kernel<SS_STORAGE_F16, true><<<ctas, 256, 0, s>>>(g->v, g->batch_depths, g->batch_poses, g->phase_mask);
+    else refuse_apply_kernel<SS_STORAGE_F16, false><<<ctas, 256, 0, s>>>(g->v, g->batch_depths, g->batch_poses, g->phase_mask);
+    SS_LAUNCH_CHECK();
+    refuse_finalize_kernel<<<persistent_ctas(g, 2), 256, 0, s>>>(g->v, g->phase_mask);
+    refuse_counters_kernel<<<1, 1, 0, s>>>(g->v.ctr);
+    SS_LAUNCH_CHECK();
+    g->host_epoch++;
+    return SS_OK;
+}

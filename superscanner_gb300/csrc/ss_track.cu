@@ -156,6 +156,7 @@ __global__ void track_begin_kernel(TrackState *st) {
     for (int k = 0; k < 12; k++) st->Tprev_inv[k] = (float)Ti[k];
     mat_from_T(st->T, st->Tf);
     st->ticket = 0;
+    st->barrier = 0u;
     st->converged_level = -1;
     for (int l = 0; l < kMaxLevels; l++) {
         st->inliers[l] = 0;
@@ -167,28 +168,16 @@ __global__ void pose_prep_kernel(TrackState *st) {
     if (threadIdx.x == 0) write_frame_pose(st->T, &st->pose);
 }
 
-__global__ void __launch_bounds__(256) track_iter_kernel(const uint16_t *__restrict__ depth, int rows, int cols,
-                                                         Intr in, const float4 *__restrict__ vmap,
-                                                         const float4 *__restrict__ nmap, TrackState *st,
-                                                         float2 *__restrict__ partials, int level, float dist2,
-                                                         float rmin, float dmax) {
-    if (*(volatile int *)&st->converged_level == level) return;
-    __shared__ float2 red[8][kTrackSums];
-    __shared__ bool last;
-    float T[12], Pi[12];
-#pragma unroll
-    for (int k = 0; k < 12; k++) {
-        T[k] = st->Tf[k];
-        Pi[k] = st->Tprev_inv[k];
-    }
-    float s[kTrackSums], c[kTrackSums];
-#pragma unroll
-    for (int k = 0; k < kTrackSums; k++) s[k] = c[k] = 0.f;
-
+// Accumulates this thread's share of one Gauss-Newton iteration at a level
+// into Kahan (sum, compensation) pairs.
+__device__ __forceinline__ void track_accumulate(const uint16_t *__restrict__ depth, int rows, int cols, Intr in,
+                                                 const float4 *__restrict__ vmap, const float4 *__restrict__ nmap,
+                                                 const float *T, const float *Pi, int level, float dist2, float rmin,
+                                                 float dmax, int tid, int nthreads, float *s, float *c) {
     const int lr = (rows + (1 << level) - 1) >> level, lc = (cols + (1 << level) - 1) >> level;
     const int npix = lr * lc;
     const float rfx = 1.f / in.fx, rfy = 1.f / in.fy;
-    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < npix; p += gridDim.x * blockDim.x) {
+    for (int p = tid; p < npix; p += nthreads) {
         const int i = (p / lc) << level, j = (p % lc) << level;
         const float d = (float)__ldg(depth + (size_t)i * cols + j) * 1e-3f;
         if (!(d > rmin) || !(d < dmax)) continue;
@@ -221,6 +210,12 @@ __global__ void __launch_bounds__(256) track_iter_kernel(const uint16_t *__restr
         kahan_add(s[27], c[27], r * r);
         s[28] += 1.f;  // counts stay exact far below 2^24
     }
+}
+
+// Reduces the CTA's pairs (warp shuffles with TwoSum, then shared memory)
+// and writes them to the value-major slots: slots[value][cta].
+__device__ __forceinline__ void track_cta_to_slots(float *s, float *c, float2 (*red)[kTrackSums],
+                                                   float2 *__restrict__ slots) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
     for (int k = 0; k < kTrackSums; k++) {
@@ -233,26 +228,20 @@ __global__ void __launch_bounds__(256) track_iter_kernel(const uint16_t *__restr
         if (lane == 0) red[wid][k] = make_float2(a, b);
     }
     __syncthreads();
-    if (threadIdx.x < kTrackSums) {  // value-major slots: partials[value][cta]
+    if (threadIdx.x < kTrackSums) {
         float a = 0.f, b = 0.f;
         for (int w = 0; w < (int)(blockDim.x >> 5); w++) pair_add(a, b, red[w][threadIdx.x].x, red[w][threadIdx.x].y);
-        partials[(size_t)threadIdx.x * gridDim.x + blockIdx.x] = make_float2(a, b);
+        slots[(size_t)threadIdx.x * gridDim.x + blockIdx.x] = make_float2(a, b);
     }
-    __threadfence();
-    __syncthreads();
-    if (threadIdx.x == 0) last = atomicAdd(&st->ticket, 1) == (int)gridDim.x - 1;
-    __syncthreads();
-    if (!last) return;
-    __threadfence();
-    // last CTA: one warp per value, lanes stride over the CTA slots (coalesced);
-    // (sum, compensation) pairs combine by TwoSum in FP32 and only the final
-    // value is widened to FP64 for the solve (FP64 is scarce on this part and
-    // a serial FP64 chain here stalls the whole GPU).
-    __shared__ double tot[kTrackSums];
+}
+
+// Reduces all CTA slots (one warp per value, TwoSum in FP32, fixed order) into tot (FP64).
+__device__ __forceinline__ void track_slots_to_totals(const float2 *__restrict__ slots, double *tot) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     for (int v = wid; v < kTrackSums; v += (int)(blockDim.x >> 5)) {
         float a = 0.f, b = 0.f;
         for (unsigned q = lane; q < gridDim.x; q += 32) {
-            const float2 pq = __ldcg(partials + (size_t)v * gridDim.x + q);
+            const float2 pq = __ldcg(slots + (size_t)v * gridDim.x + q);
             pair_add(a, b, pq.x, pq.y);
         }
 #pragma unroll
@@ -262,13 +251,12 @@ __global__ void __launch_bounds__(256) track_iter_kernel(const uint16_t *__restr
         }
         if (lane == 0) tot[v] = (double)a - (double)b;
     }
-    __syncthreads();
-    if (threadIdx.x != 0) return;
-    st->ticket = 0;
-    const double n = tot[28];
-    st->inliers[level] = (int)n;
-    st->rmse[level] = n > 0 ? (float)sqrt(tot[27] / n) : 0.f;
-    if (n < 60.0) return;  // too few correspondences: keep the pose
+}
+
+// FP64 solve of the normal equations and left SE(3) update of T; returns the
+// step norm (negative when the system was not solved).
+__device__ double track_solve(const double *tot, double *T) {
+    if (tot[28] < 60.0) return -1.0;  // too few correspondences: keep the pose
     double A[36], b[6], x[6];
     int q = 0;
     for (int r = 0; r < 6; r++)
@@ -276,11 +264,147 @@ __global__ void __launch_bounds__(256) track_iter_kernel(const uint16_t *__restr
             A[r * 6 + cc] = A[cc * 6 + r] = tot[q++];
         }
     for (int r = 0; r < 6; r++) b[r] = -tot[21 + r];
-    if (!cholesky6(A, b, x)) return;
-    se3_left_update(x, st->T);
-    mat_from_T(st->T, st->Tf);
-    const double step = sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2] + x[3] * x[3] + x[4] * x[4] + x[5] * x[5]);
-    if (step < 1e-7) st->converged_level = level;
+    if (!cholesky6(A, b, x)) return -1.0;
+    se3_left_update(x, T);
+    return sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2] + x[3] * x[3] + x[4] * x[4] + x[5] * x[5]);
+}
+
+__global__ void __launch_bounds__(256) track_iter_kernel(const uint16_t *__restrict__ depth, int rows, int cols,
+                                                         Intr in, const float4 *__restrict__ vmap,
+                                                         const float4 *__restrict__ nmap, TrackState *st,
+                                                         float2 *__restrict__ partials, int level, float dist2,
+                                                         float rmin, float dmax) {
+    if (*(volatile int *)&st->converged_level == level) return;
+    __shared__ float2 red[8][kTrackSums];
+    __shared__ bool last;
+    __shared__ double tot[kTrackSums];
+    float T[12], Pi[12];
+#pragma unroll
+    for (int k = 0; k < 12; k++) {
+        T[k] = st->Tf[k];
+        Pi[k] = st->Tprev_inv[k];
+    }
+    float s[kTrackSums], c[kTrackSums];
+#pragma unroll
+    for (int k = 0; k < kTrackSums; k++) s[k] = c[k] = 0.f;
+    track_accumulate(depth, rows, cols, in, vmap, nmap, T, Pi, level, dist2, rmin, dmax,
+                     blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x, s, c);
+    track_cta_to_slots(s, c, red, partials);
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(&st->ticket, 1) == (int)gridDim.x - 1;
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    // last CTA: FP32 TwoSum over the slots, FP64 only for the solve (FP64 is
+    // scarce on this part and a serial FP64 chain here stalls the whole GPU)
+    track_slots_to_totals(partials, tot);
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    st->ticket = 0;
+    const double n = tot[28];
+    st->inliers[level] = (int)n;
+    st->rmse[level] = n > 0 ? (float)sqrt(tot[27] / n) : 0.f;
+    const double step = track_solve(tot, st->T);
+    if (step >= 0.0) mat_from_T(st->T, st->Tf);
+    if (step >= 0.0 && step < 1e-7) st->converged_level = level;
+}
+
+// Bounded grid barrier of the cooperative tracker: arrival count, spin with
+// back-off up to a cap (about a second), then an error flag instead of a hang.
+__device__ __forceinline__ bool grid_barrier(TrackState *st, unsigned target) {
+    __syncthreads();
+    __shared__ int ok;
+    if (threadIdx.x == 0) {
+        __threadfence();
+        atomicAdd(&st->barrier, 1u);
+        ok = 1;
+        unsigned seen;
+        int spins = 0;
+        do {
+            asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(seen) : "l"(&st->barrier) : "memory");
+            if (seen >= target) break;
+            __nanosleep(64);
+        } while (++spins < (1 << 24));
+        if (seen < target) {
+            atomicOr(&st->status, kStTimeout);
+            ok = 0;
+        }
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+// All Gauss-Newton iterations of one frame in one cooperative launch. Every
+// CTA reduces all CTA slots and solves redundantly (bit-identical results in
+// every CTA), so one grid barrier per iteration suffices; the slots are double
+// buffered so a CTA that runs ahead never overwrites slots still being read.
+__global__ void __launch_bounds__(256) track_frame_kernel(const uint16_t *__restrict__ depth, int rows, int cols,
+                                                          Intr in, const float4 *__restrict__ vmap,
+                                                          const float4 *__restrict__ nmap, TrackState *st,
+                                                          float2 *__restrict__ slots, TrackLaunch L) {
+    __shared__ float2 red[8][kTrackSums];
+    __shared__ double tot[kTrackSums];
+    __shared__ double Td[16];
+    __shared__ float Tf[12], Pi[12];
+    __shared__ int done_level;
+    if (threadIdx.x < 16) Td[threadIdx.x] = st->T[threadIdx.x];
+    if (threadIdx.x < 12) {
+        Tf[threadIdx.x] = st->Tf[threadIdx.x];
+        Pi[threadIdx.x] = st->Tprev_inv[threadIdx.x];
+    }
+    if (threadIdx.x == 0) done_level = -1;
+    __syncthreads();
+    unsigned barriers = 0;
+    int parity = 0;
+    for (int level = L.levels - 1; level >= 0; level--) {
+        const float dist2 = L.dist[level] * L.dist[level];
+        for (int it = 0; it < L.iters[level]; it++) {
+            if (done_level == level) break;  // converged: identical decision in every CTA
+            float s[kTrackSums], c[kTrackSums];
+#pragma unroll
+            for (int k = 0; k < kTrackSums; k++) s[k] = c[k] = 0.f;
+            float T[12], P[12];
+#pragma unroll
+            for (int k = 0; k < 12; k++) {
+                T[k] = Tf[k];
+                P[k] = Pi[k];
+            }
+            track_accumulate(depth, rows, cols, in, vmap, nmap, T, P, level, dist2, L.rmin, L.dmax,
+                             blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x, s, c);
+            float2 *buf = slots + (size_t)parity * kTrackSums * gridDim.x;
+            track_cta_to_slots(s, c, red, buf);
+            if (!grid_barrier(st, (++barriers) * gridDim.x)) return;
+            track_slots_to_totals(buf, tot);
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                const double step = track_solve(tot, Td);
+                if (step >= 0.0)
+                    for (int k = 0; k < 12; k++) Tf[k] = (float)Td[k];
+                if (step >= 0.0 && step < 1e-7) done_level = level;
+                if (blockIdx.x == 0) {
+                    const double n = tot[28];
+                    st->inliers[level] = (int)n;
+                    st->rmse[level] = n > 0 ? (float)sqrt(tot[27] / n) : 0.f;
+                }
+            }
+            __syncthreads();
+            parity ^= 1;
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        for (int k = 0; k < 16; k++) st->T[k] = Td[k];
+        for (int k = 0; k < 12; k++) st->Tf[k] = Tf[k];
+    }
+}
+
+int persistent_track_ctas(int num_sms) {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, track_frame_kernel, 256, 0) != cudaSuccess) {
+        cudaGetLastError();
+        per_sm = 1;
+    }
+    return num_sms * (per_sm >= 2 ? 2 : (per_sm < 1 ? 1 : per_sm));
 }
 
 // Host-side launch of one frame's tracking: begin, levels coarse to fine,
@@ -288,6 +412,30 @@ __global__ void __launch_bounds__(256) track_iter_kernel(const uint16_t *__restr
 ss_status launch_track(const TrackLaunch &L, cudaStream_t s) {
     track_begin_kernel<<<1, 32, 0, s>>>(L.state);
     SS_LAUNCH_CHECK();
+    if (L.persistent) {
+        const uint16_t *depth = L.depth;
+        int rows = L.rows, cols = L.cols;
+        Intr in = L.in;
+        const float4 *vmap = L.vmap, *nmap = L.nmap;
+        TrackState *st = L.state;
+        float2 *slots = L.partials;
+        // cooperative launch (all CTAs co-resident, so the grid barrier cannot wait
+        // on a CTA that is not running); the attribute form is stream-capturable
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(L.ctas);
+        cfg.blockDim = dim3(256);
+        cfg.dynamicSmemBytes = 0;
+        cfg.stream = s;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeCooperative;
+        attr[0].val.cooperative = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        SS_CUDA_TRY(cudaLaunchKernelEx(&cfg, track_frame_kernel, depth, rows, cols, in, vmap, nmap, st, slots, L));
+        pose_prep_kernel<<<1, 32, 0, s>>>(L.state);
+        SS_LAUNCH_CHECK();
+        return SS_OK;
+    }
     for (int level = L.levels - 1; level >= 0; level--) {
         for (int it = 0; it < L.iters[level]; it++) {
             track_iter_kernel<<<L.ctas, 256, 0, s>>>(L.depth, L.rows, L.cols, L.in, L.vmap, L.nmap, L.state, L.partials,

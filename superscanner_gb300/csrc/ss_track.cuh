@@ -20,6 +20,8 @@ struct TrackState {
     int converged_level;
     int inliers[kMaxLevels];
     float rmse[kMaxLevels];
+    unsigned int barrier;  // arrivals at the persistent tracker's grid barrier (zeroed per frame)
+    int status;            // kSt* bits of the persistent tracker
 };
 
 struct TrackLaunch {
@@ -34,9 +36,12 @@ struct TrackLaunch {
     int iters[kMaxLevels];
     float dist[kMaxLevels];
     float rmin, dmax;
+    bool persistent;  // one cooperative launch for all iterations (else one launch per iteration)
 };
 
 ss_status launch_track(const TrackLaunch &L, cudaStream_t s);
+// CTAs of the persistent tracker on this device (co-resident, <= 2 per SM).
+int persistent_track_ctas(int num_sms);
 ss_status launch_pose_prep(TrackState *st, cudaStream_t s);
 
 }  // namespace ss

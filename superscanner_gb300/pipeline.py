@@ -2,9 +2,10 @@
 the last model view (3-level point-to-plane Gauss-Newton), integrate it at
 the tracked pose, raycast the new model view (trilinear, <= 128 steps).
 
-Forms: ``plain`` = FP32 TSDF, every kernel launched one by one;
-``chosen`` = FP16 TSDF + uint16 weights, each tracked frame replayed as one
-CUDA graph. Both keep all state on the device (no host sync per frame).
+Forms: ``plain`` = FP32 TSDF, every kernel launched one by one (one launch
+per tracker iteration); ``chosen`` = FP16 TSDF + uint16 weights, all tracker
+iterations in one persistent cooperative launch, each tracked frame replayed
+as one CUDA graph. Both keep all state on the device (no host sync per frame).
 """
 from __future__ import annotations
 
@@ -30,15 +31,15 @@ def raycast_maps(grid: GPUVoxelGrid, extr, max_steps: int = 128, t_min: float = 
 
 
 FORMS = {
-    "plain": dict(storage="f32", use_graph=False),
-    "chosen": dict(storage="f16", use_graph=True),
+    "plain": dict(storage="f32", use_graph=False, persistent_track=False),
+    "chosen": dict(storage="f16", use_graph=True, persistent_track=True),
 }
 
 
 class Pipeline:
     def __init__(self, grid: GPUVoxelGrid, *, use_graph: bool = True, levels: int = 3, iters=(10, 5, 4),
                  dist=(0.06, 0.10, 0.15), raycast_steps: int = 128, t_min: float = 0.2, t_max: float = 10.0,
-                 exact_fusion: bool = False, hint_margin: float = 0.04):
+                 exact_fusion: bool = False, hint_margin: float = 0.04, persistent_track: bool | None = None):
         p = SSPipelineParams()
         check(lib.ss_pipeline_params_default(C.byref(p)), "pipeline_params_default")
         p.levels = levels
@@ -50,6 +51,7 @@ class Pipeline:
         p.use_graph = 1 if use_graph else 0
         p.exact_fusion = 1 if exact_fusion else 0
         p.hint_margin = float(hint_margin)
+        p.persistent_track = int(use_graph if persistent_track is None else persistent_track)
         self.grid = grid
         self._h = C.c_void_p()
         check(lib.ss_pipeline_create(grid.handle, C.byref(p), C.byref(self._h)), "pipeline_create")

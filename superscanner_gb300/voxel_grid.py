@@ -105,6 +105,18 @@ class GPUVoxelGrid:
         check(lib.ss_integrate_fast(self._h, d, r, f32x16(extr), 1 if rgb is not None else 0, 1 if deint else 0,
                                     _stream_ptr(stream)), "integrate_fast")
 
+    def refuse_batch(self, depths, T_old, T_new, exact: bool = False, stream=None) -> None:
+        """Re-fuse keyframes: for each k, deintegrate depths[k] at T_old[k] and integrate it at T_new[k]
+        (in order), in one collection and one persistent apply launch."""
+        n = len(depths)
+        for d in depths:
+            _dev_ptr(d, 2, (self.resi, self.resj), "depth")
+        ptrs = (C.c_void_p * n)(*[d.data_ptr() for d in depths])
+        to = np.ascontiguousarray(np.asarray(T_old, np.float32).reshape(n, 16))
+        tn = np.ascontiguousarray(np.asarray(T_new, np.float32).reshape(n, 16))
+        check(lib.ss_refuse_batch(self._h, n, ptrs, C.c_void_p(to.ctypes.data), C.c_void_p(tn.ctypes.data),
+                                  1 if exact else 0, _stream_ptr(stream)), "refuse_batch")
+
     def raycast(self, extr, stream=None, with_color: bool = True):
         """raycast (GPUVoxelGrid.cpp:139-147): fills rayPcd and rayColorPcd."""
         col = C.c_void_p(self.rayColorPcd.data_ptr()) if with_color else C.c_void_p()

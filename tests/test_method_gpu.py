@@ -81,14 +81,15 @@ def test_tracking_solve_vs_fp64():
     assert inliers[0] > 100000
 
 
-def test_pipeline_graph_replay_equals_direct_launches():
+@pytest.mark.parametrize("persistent", [False, True])
+def test_pipeline_graph_replay_equals_direct_launches(persistent):
     P, depth = seq(16)
     poses = {}
     for graph in (False, True):
         g = GPUVoxelGrid(int(1e9), TRUNC, VL, 480, 640, storage="f16", with_color=False, hash_buckets=1 << 18,
                          max_weight=255)
         g.setIntrinsic(*INTR)
-        pipe = Pipeline(g, use_graph=graph)
+        pipe = Pipeline(g, use_graph=graph, persistent_track=persistent)
         pipe.set_pose(P[0])
         out = []
         for k in range(16):
@@ -113,3 +114,28 @@ def test_pipeline_tracks_ground_truth(storage):
     g.sync()
     dt, dr = pose_err(pipe.pose(), P[59])
     assert dt < 0.005 and np.degrees(dr) < 0.3
+
+
+def test_persistent_tracker_matches_per_iteration_launches():
+    """One cooperative launch for all Gauss-Newton iterations gives the poses of
+    one launch per iteration (the CTA count differs, so FP32 sums round
+    differently: within 1e-5 m / 1e-5 rad over 24 frames)."""
+    P, depth = seq(24)
+    out = {}
+    for persistent in (False, True):
+        g = GPUVoxelGrid(int(1e9), TRUNC, VL, 480, 640, storage="f32", with_color=False, hash_buckets=1 << 18,
+                         max_weight=255)
+        g.setIntrinsic(*INTR)
+        pipe = Pipeline(g, use_graph=False, persistent_track=persistent)
+        pipe.set_pose(P[0])
+        poses = []
+        for k in range(24):
+            pipe.frame(dev(depth[k]), track=(k > 0))
+            poses.append(pipe.pose())
+        g.sync()
+        out[persistent] = poses
+        inliers, _ = pipe.stats()
+        assert inliers[0] > 100000
+    for a, b in zip(out[False], out[True]):
+        dt, dr = pose_err(a, b)
+        assert dt < 1e-5 and dr < 1e-5
