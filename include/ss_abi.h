@@ -150,6 +150,12 @@ ss_status ss_grid_export_blocks(ss_grid *g, ss_stream_t s, int32_t max_blocks,
                                 uint64_t *keys, int32_t *coords, float *sdf,
                                 float *weight, float *rgb, int32_t *n_out);
 
+/* Bucket index of each block, in the order of ss_grid_export_blocks (key
+ * order): maps payload-layout buffers such as raycast voxel gradients back to
+ * blocks. No reference counterpart. */
+ss_status ss_grid_export_buckets(ss_grid *g, ss_stream_t s, int32_t max_blocks, int32_t *buckets,
+                                 int32_t *n_out);
+
 /* Loads a dump written by ss_grid_export_blocks (checkpoint / resume). */
 ss_status ss_grid_import_blocks(ss_grid *g, ss_stream_t s, int32_t n, const int32_t *coords,
                                 const float *sdf, const float *weight, const float *rgb);
@@ -203,6 +209,26 @@ ss_status ss_kokkos_icp_noalloc(const uint16_t *d1, const uint16_t *d2, int32_t 
 ss_status ss_raycast_maps(ss_grid *g, const float extr[16], int32_t max_steps, float t_min,
                           float t_max, const uint16_t *hint_depth, float hint_margin,
                           float *vertex_depth, float *normal, ss_stream_t s);
+
+/* Differentiable raycast (no reference counterpart). Renders the model view at
+ * pose T (camera -> world, row-major doubles) with the trilinear march (at most
+ * max_steps steps) refined by Newton steps to the root of the trilinear field,
+ * and returns the loss against depth_obs ([resi][resj] u16 mm, device):
+ *   L = sum over valid pixels of r^2 + lambda_n (r n.d)^2,  r = t* - d_obs,
+ * (the second term is the squared distance of the observed point to the
+ * rendered tangent plane; valid: hit, observation present, |r| < r_max,
+ * surface facing the ray). valid_pixels and depth_out ([resi][resj] floats,
+ * device, the rendered depth) may be NULL. Synchronises s. */
+ss_status ss_raycast_loss(ss_grid *g, const double T[16], const uint16_t *depth_obs, float lambda_n,
+                          float r_max, int32_t max_steps, double *loss, int64_t *valid_pixels,
+                          float *depth_out, ss_stream_t s);
+/* Its adjoint, recomputing the march: grad_pose = dL/d(omega, upsilon) for the
+ * left increment T <- exp(xi) T; grad_voxels (device, [buckets][512] floats,
+ * the TSDF payload layout, may be NULL) += dL/d(voxel TSDF value in metres).
+ * The caller zeroes grad_voxels. Synchronises s. */
+ss_status ss_raycast_loss_grad(ss_grid *g, const double T[16], const uint16_t *depth_obs, float lambda_n,
+                               float r_max, int32_t max_steps, double *loss, double grad_pose[6],
+                               float *grad_voxels, int64_t *valid_pixels, ss_stream_t s);
 
 typedef struct ss_pipeline ss_pipeline;
 

@@ -51,6 +51,10 @@ for name, res, args in [
     ("orm_grid_fuse", _i, [_p, _p, _p, _i]),
     ("orm_grid_export", _i, [_p, _i, _p, _p, _p, _p]),
     ("orm_raycast", None, [_p, _p, _i, C.c_double, C.c_double, _p, C.c_double, _p, _p, _p]),
+    ("orm_track_debug", None, [_p, C.c_double]),
+    ("orm_grid_import", None, [_p, _i, _p, _p, _p]),
+    ("orm_grid_add_voxel", _i, [_p, _i, _i, _i, _i, C.c_double]),
+    ("orm_raycast_loss", C.c_double, [_p, _p, _p, C.c_double, C.c_double, _i, C.c_double, C.c_double, _p]),
     ("orm_track", _i, [_p, _i, _i, _f, _f, _f, _f, _p, _p, _p, _p, _i, _p, _p, C.c_double, C.c_double]),
 ]:
     fn = getattr(_lib, name)
@@ -199,6 +203,22 @@ class MethodGrid64:
 
     def count(self) -> int:
         return _lib.orm_grid_count(self._h)
+
+    def import_blocks(self, coords, sdf, w):
+        coords = np.ascontiguousarray(coords, np.int32)
+        _lib.orm_grid_import(self._h, len(coords), _ptr(coords), _ptr(_f32(sdf)), _ptr(_f32(w)))
+
+    def add_voxel(self, coords, v, delta) -> bool:
+        return bool(_lib.orm_grid_add_voxel(self._h, int(coords[0]), int(coords[1]), int(coords[2]), int(v),
+                                            float(delta)))
+
+    def raycast_loss(self, T, obs, lambda_n=1.0, r_max=0.05, max_steps=128, t_min=0.2, t_max=10.0):
+        valid = np.zeros(1, np.int64)
+        obs = np.ascontiguousarray(obs, np.uint16)
+        loss = _lib.orm_raycast_loss(self._h, _ptr(np.ascontiguousarray(T, np.float64)), _ptr(obs),
+                                     float(lambda_n), float(r_max), int(max_steps), float(t_min), float(t_max),
+                                     _ptr(valid))
+        return loss, int(valid[0])
 
     def export(self) -> dict:
         n = self.count()

@@ -388,6 +388,110 @@ void orm_raycast(void *h, const double *T, int max_steps, double t_min, double t
     }
 }
 
+// Loads blocks (coords, sdf and weight per voxel) into an FP64 grid.
+void orm_grid_import(void *h, int n, const int32_t *coords, const float *sdf, const float *w) {
+    Grid64 &g = *(Grid64 *)h;
+    for (int q = 0; q < n; q++) {
+        const int x = coords[q * 3], y = coords[q * 3 + 1], z = coords[q * 3 + 2];
+        const uint64_t key = prime_hash(x, y, z);
+        auto it = g.map.find(key);
+        int idx;
+        if (it == g.map.end()) {
+            idx = (int)g.blocks.size();
+            Block64 *b = new Block64;
+            std::memset(b, 0, sizeof(Block64));
+            g.blocks.push_back(b);
+            g.map.emplace(key, idx);
+            g.supers.insert(super_key(floordiv8(x), floordiv8(y), floordiv8(z)));
+        } else {
+            idx = it->second;
+        }
+        Block64 &b = *g.blocks[idx];
+        b.vb[0] = x;
+        b.vb[1] = y;
+        b.vb[2] = z;
+        for (int v = 0; v < kVox; v++) {
+            b.sdf[v] = sdf[(size_t)q * kVox + v];
+            b.w[v] = w[(size_t)q * kVox + v];
+        }
+    }
+}
+
+// Adds delta to the TSDF value of voxel v of block (x, y, z); returns 0 if the block is absent.
+int orm_grid_add_voxel(void *h, int x, int y, int z, int v, double delta) {
+    Grid64 &g = *(Grid64 *)h;
+    auto it = g.map.find(prime_hash(x, y, z));
+    if (it == g.map.end()) return 0;
+    g.blocks[it->second]->sdf[v] += delta;
+    return 1;
+}
+
+// Loss of the differentiable raycast (the GPU's ss_raycast_loss) in FP64:
+// trilinear march from t_min, Newton steps to the root of the trilinear field,
+// L = sum of r^2 + lambda (r n.d)^2 over valid pixels (r = t* - d_obs).
+double orm_raycast_loss(void *h, const double *T, const uint16_t *obs, double lambda_n, double r_max,
+                        int max_steps, double t_min, double t_max, long long *valid_out) {
+    const Grid64 &g = *(Grid64 *)h;
+    double total = 0;
+    long long valid = 0;
+#pragma omp parallel for schedule(dynamic, 2) reduction(+ : total, valid)
+    for (int i = 0; i < g.resi; i++) {
+        Cache cache;
+        for (int j = 0; j < g.resj; j++) {
+            const double dcx = (j - (double)g.cj) / g.fx, dcy = (i - (double)g.ci) / g.fy;
+            const double dx = T[0] * dcx + T[1] * dcy + T[2], dy = T[4] * dcx + T[5] * dcy + T[6],
+                         dz = T[8] * dcx + T[9] * dcy + T[10];
+            const double ox = T[3], oy = T[7], oz = T[11];
+            const double inv_len = 1.0 / std::sqrt(dx * dx + dy * dy + dz * dz);
+            int steps = 0;
+            double t = t_min;
+            if (!march64(g, cache, ox, oy, oz, dx, dy, dz, inv_len, t_min, t_max, max_steps, steps, t)) continue;
+            Sample q{false, 0, 0, 0, 0};
+            bool ok = true;
+            for (int it = 0; it < 6; it++) {
+                q = trilinear64(g, ox + t * dx, oy + t * dy, oz + t * dz, cache);
+                if (!q.valid) {
+                    ok = false;
+                    break;
+                }
+                const double gd = q.gx * dx + q.gy * dy + q.gz * dz;
+                if (!(gd < 0)) {
+                    ok = false;
+                    break;
+                }
+                const double dt = -q.f / gd;
+                if (std::fabs(dt) > 2 * g.vl * inv_len) {
+                    ok = false;
+                    break;
+                }
+                t += dt;
+                if (std::fabs(dt) < 1e-7 * t) break;
+            }
+            if (!ok) continue;
+            q = trilinear64(g, ox + t * dx, oy + t * dy, oz + t * dz, cache);
+            if (!q.valid) continue;
+            const double d_obs = obs[(size_t)i * g.resj + j] * 1e-3;
+            if (!(d_obs > g.rmin)) continue;
+            const double gn = std::sqrt(q.gx * q.gx + q.gy * q.gy + q.gz * q.gz);
+            const double c = (q.gx * dx + q.gy * dy + q.gz * dz) / gn;
+            const double r = t - d_obs;
+            if (!(std::fabs(r) < r_max && c < -0.05)) continue;
+            total += r * r + lambda_n * (r * c) * (r * c);
+            valid++;
+        }
+    }
+    if (valid_out) *valid_out = valid;
+    return total;
+}
+
+static double *g_track_log = nullptr;  // optional per-iteration step norms [level][16] (tests)
+static double g_track_eps = 1e-7;        // convergence threshold on the step norm
+
+void orm_track_debug(double *log, double eps) {
+    g_track_log = log;
+    g_track_eps = eps;
+}
+
 static bool chol6(const double *A, const double *b, double *x) {
     double L[36] = {0};
     for (int i = 0; i < 6; i++)
@@ -497,7 +601,8 @@ int orm_track(const uint16_t *depth, int rows, int cols, float fx, float fy, flo
             se3_left(x, T);
             double step = 0;
             for (int r = 0; r < 6; r++) step += x[r] * x[r];
-            if (std::sqrt(step) < 1e-7) break;
+            if (g_track_log) g_track_log[level * 16 + it] = std::sqrt(step);
+            if (std::sqrt(step) < g_track_eps) break;
         }
     }
     return last_n;

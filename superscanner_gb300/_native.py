@@ -76,6 +76,7 @@ SIGNATURES = {
     "ss_grid_block_count": (_st, [_p, _p, C.POINTER(_i32)]),
     "ss_grid_counters": (_st, [_p, _p, C.POINTER(C.c_int64)]),
     "ss_grid_export_blocks": (_st, [_p, _p, _i32, _p, _p, _p, _p, _p, C.POINTER(_i32)]),
+    "ss_grid_export_buckets": (_st, [_p, _p, _i32, _p, C.POINTER(_i32)]),
     "ss_grid_import_blocks": (_st, [_p, _p, _i32, _p, _p, _p, _p]),
     "ss_depth_to_pcd": (_st, [_p, _i32, _i32, _f, _f, _f, _f, _p, _p]),
     "ss_normals_from_pcd": (_st, [_p, _i32, _i32, _p, _p]),
@@ -84,6 +85,9 @@ SIGNATURES = {
     "ss_kokkos_icp_noalloc": (_st, [_p, _p, _i32, _i32, _f, _f, _f, _f, _D16, _D16, _i32, _D16,
                                     C.POINTER(C.c_float), _p]),
     "ss_raycast_maps": (_st, [_p, _F16, _i32, _f, _f, _p, _f, _p, _p, _p]),
+    "ss_raycast_loss": (_st, [_p, _D16, _p, _f, _f, _i32, C.POINTER(C.c_double), C.POINTER(C.c_int64), _p, _p]),
+    "ss_raycast_loss_grad": (_st, [_p, _D16, _p, _f, _f, _i32, C.POINTER(C.c_double), C.POINTER(C.c_double), _p,
+                                   C.POINTER(C.c_int64), _p]),
     "ss_pipeline_params_default": (_st, [C.POINTER(SSPipelineParams)]),
     "ss_pipeline_create": (_st, [_p, C.POINTER(SSPipelineParams), C.POINTER(_p)]),
     "ss_pipeline_destroy": (_st, [_p]),

@@ -813,6 +813,23 @@ ss_status ss_grid_export_blocks(ss_grid *g, ss_stream_t stream, int32_t max_bloc
     return st;
 }
 
+ss_status ss_grid_export_buckets(ss_grid *g, ss_stream_t stream, int32_t max_blocks, int32_t *buckets,
+                                 int32_t *n_out) {
+    if (!g || !n_out || max_blocks < 0) return SS_ERR_ARG;
+    SS_CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
+    const size_t B = (size_t)g->p.hash_buckets;
+    std::vector<unsigned long long> hk(B);
+    SS_CUDA_TRY(cudaMemcpy(hk.data(), g->v.keys, B * 8, cudaMemcpyDeviceToHost));
+    std::vector<std::pair<unsigned long long, int>> items;
+    for (size_t b = 0; b < B; b++)
+        if (hk[b] != kEmptyKey && hk[b] != kTombKey) items.push_back({hk[b], (int)b});
+    std::sort(items.begin(), items.end());
+    *n_out = (int)items.size();
+    for (int q = 0; q < (int)items.size() && q < max_blocks; q++)
+        if (buckets) buckets[q] = items[q].second;
+    return SS_OK;
+}
+
 ss_status ss_grid_import_blocks(ss_grid *g, ss_stream_t stream, int32_t n, const int32_t *coords, const float *sdf,
                                 const float *weight, const float *rgb) {
     if (!g || n < 0 || (n > 0 && (!coords || !sdf || !weight))) return SS_ERR_ARG;

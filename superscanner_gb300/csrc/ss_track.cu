@@ -335,6 +335,23 @@ __device__ __forceinline__ bool grid_barrier(TrackState *st, unsigned target) {
     return ok != 0;
 }
 
+#ifdef SS_TRACK_TIMING
+// Phase timestamps of CTA 0 (global timer, ns) for tuning builds only.
+__device__ unsigned long long g_track_timing[32 * 6];
+#define SS_TT(slot, phase)                                                                     \
+    do {                                                                                       \
+        if (blockIdx.x == 0 && threadIdx.x == 0 && (slot) < 32) {                              \
+            unsigned long long t_;                                                             \
+            asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t_));                             \
+            g_track_timing[(slot) * 6 + (phase)] = t_;                                         \
+        }                                                                                      \
+    } while (0)
+#else
+#define SS_TT(slot, phase) \
+    do {                   \
+    } while (0)
+#endif
+
 // All Gauss-Newton iterations of one frame in one cooperative launch. Every
 // CTA reduces all CTA slots and solves redundantly (bit-identical results in
 // every CTA), so one grid barrier per iteration suffices; the slots are double
@@ -361,6 +378,7 @@ __global__ void __launch_bounds__(256) track_frame_kernel(const uint16_t *__rest
         const float dist2 = L.dist[level] * L.dist[level];
         for (int it = 0; it < L.iters[level]; it++) {
             if (done_level == level) break;  // converged: identical decision in every CTA
+            SS_TT(barriers, 0);
             float s[kTrackSums], c[kTrackSums];
 #pragma unroll
             for (int k = 0; k < kTrackSums; k++) s[k] = c[k] = 0.f;
@@ -372,11 +390,15 @@ __global__ void __launch_bounds__(256) track_frame_kernel(const uint16_t *__rest
             }
             track_accumulate(depth, rows, cols, in, vmap, nmap, T, P, level, dist2, L.rmin, L.dmax,
                              blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x, s, c);
+            SS_TT(barriers, 1);
             float2 *buf = slots + (size_t)parity * kTrackSums * gridDim.x;
             track_cta_to_slots(s, c, red, buf);
+            SS_TT(barriers, 2);
             if (!grid_barrier(st, (++barriers) * gridDim.x)) return;
+            SS_TT(barriers - 1, 3);
             track_slots_to_totals(buf, tot);
             __syncthreads();
+            SS_TT(barriers - 1, 4);
             if (threadIdx.x == 0) {
                 const double step = track_solve(tot, Td);
                 if (step >= 0.0)
@@ -389,6 +411,7 @@ __global__ void __launch_bounds__(256) track_frame_kernel(const uint16_t *__rest
                 }
             }
             __syncthreads();
+            SS_TT(barriers - 1, 5);
             parity ^= 1;
         }
     }
@@ -397,6 +420,12 @@ __global__ void __launch_bounds__(256) track_frame_kernel(const uint16_t *__rest
         for (int k = 0; k < 12; k++) st->Tf[k] = Tf[k];
     }
 }
+
+#ifdef SS_TRACK_TIMING
+extern "C" int ss_debug_track_timing(unsigned long long *out) {
+    return (int)cudaMemcpyFromSymbol(out, g_track_timing, sizeof(g_track_timing));
+}
+#endif
 
 int persistent_track_ctas(int num_sms) {
     int per_sm = 0;

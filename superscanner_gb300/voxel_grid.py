@@ -162,6 +162,15 @@ class GPUVoxelGrid:
                                         ptr(w), ptr(rgb), C.byref(n)), "export_blocks")
         return dict(keys=keys, coords=coords, sdf=sdf, w=w, rgb=rgb)
 
+    def export_buckets(self, stream=None) -> np.ndarray:
+        """Bucket index of each block in export_blocks' (key) order."""
+        n = C.c_int32()
+        check(lib.ss_grid_export_buckets(self._h, _stream_ptr(stream), 0, None, C.byref(n)), "export_buckets")
+        out = np.zeros(n.value, np.int32)
+        check(lib.ss_grid_export_buckets(self._h, _stream_ptr(stream), n.value, C.c_void_p(out.ctypes.data),
+                                          C.byref(n)), "export_buckets")
+        return out
+
     def import_blocks(self, coords, sdf, w, rgb=None, stream=None) -> None:
         coords = np.ascontiguousarray(coords, np.int32)
         sdf = np.ascontiguousarray(sdf, np.float32)
