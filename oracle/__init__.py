@@ -54,6 +54,7 @@ for name, res, args in [
     ("orm_track_debug", None, [_p, C.c_double]),
     ("orm_grid_import", None, [_p, _i, _p, _p, _p]),
     ("orm_grid_add_voxel", _i, [_p, _i, _i, _i, _i, C.c_double]),
+    ("orm_raycast_loss_grad", C.c_double, [_p, _p, _p, C.c_double, C.c_double, _i, C.c_double, C.c_double, _p, _p]),
     ("orm_raycast_loss", C.c_double, [_p, _p, _p, C.c_double, C.c_double, _i, C.c_double, C.c_double, _p]),
     ("orm_track", _i, [_p, _i, _i, _f, _f, _f, _f, _p, _p, _p, _p, _i, _p, _p, C.c_double, C.c_double]),
 ]:
@@ -63,7 +64,9 @@ for name, res, args in [
 
 
 def _ptr(a):
-    return C.c_void_p(a.ctypes.data) if a is not None else C.c_void_p()
+    # numpy's ctypes view holds a reference to the array, so a temporary
+    # (a converted copy) stays alive for the duration of the foreign call
+    return a.ctypes if a is not None else C.c_void_p()
 
 
 def _f32(a, shape=None):
@@ -219,6 +222,17 @@ class MethodGrid64:
                                      float(lambda_n), float(r_max), int(max_steps), float(t_min), float(t_max),
                                      _ptr(valid))
         return loss, int(valid[0])
+
+    def raycast_loss_grad(self, T, obs, lambda_n=1.0, r_max=0.05, max_steps=128, t_min=0.2, t_max=10.0,
+                          voxels=False):
+        """(loss, dL/dxi [6]) or, with voxels=True, (loss, dL/dxi, dL/ds [blocks, 512] in export order)."""
+        grad = np.zeros(6)
+        gvox = np.zeros((self.count(), 512)) if voxels else None
+        obs = np.ascontiguousarray(obs, np.uint16)
+        loss = _lib.orm_raycast_loss_grad(self._h, _ptr(np.ascontiguousarray(T, np.float64)), _ptr(obs),
+                                          float(lambda_n), float(r_max), int(max_steps), float(t_min), float(t_max),
+                                          _ptr(grad), _ptr(gvox))
+        return (loss, grad, gvox) if voxels else (loss, grad)
 
     def export(self) -> dict:
         n = self.count()

@@ -484,6 +484,145 @@ double orm_raycast_loss(void *h, const double *T, const uint16_t *obs, double la
     return total;
 }
 
+struct Cell64 {
+    bool valid;
+    double f, g[3], Hxy, Hxz, Hyz, a, b, c;
+    const Block64 *blk[8];
+    int vox[8];
+};
+
+static Cell64 cell64(const Grid64 &g, double px, double py, double pz, Cache &cache) {
+    Cell64 r;
+    r.valid = false;
+    const double vl = g.vl;
+    const double ux = px / vl - 0.5, uy = py / vl - 0.5, uz = pz / vl - 0.5;
+    const double fx0 = std::floor(ux), fy0 = std::floor(uy), fz0 = std::floor(uz);
+    const int ix = (int)fx0, iy = (int)fy0, iz = (int)fz0;
+    r.a = ux - fx0;
+    r.b = uy - fy0;
+    r.c = uz - fz0;
+    double s[8];
+    for (int k = 0; k < 8; k++) {
+        const int vx = ix + (k & 1), vy = iy + ((k >> 1) & 1), vz = iz + (k >> 2);
+        const int bx = floordiv8(vx), by = floordiv8(vy), bz = floordiv8(vz);
+        const Block64 *b = cached(g, cache, bx, by, bz);
+        if (!b) return r;
+        const int v = (vx - 8 * bx) + 8 * (vy - 8 * by) + 64 * (vz - 8 * bz);
+        if (!(b->w[v] > 0)) return r;
+        s[k] = b->sdf[v];
+        r.blk[k] = b;
+        r.vox[k] = v;
+    }
+    double f = 0, ga = 0, gb = 0, gc = 0, hab = 0, hac = 0, hbc = 0;
+    for (int k = 0; k < 8; k++) {
+        const double wx = (k & 1) ? r.a : 1 - r.a, wy = ((k >> 1) & 1) ? r.b : 1 - r.b, wz = (k >> 2) ? r.c : 1 - r.c;
+        const double sx = (k & 1) ? 1 : -1, sy = ((k >> 1) & 1) ? 1 : -1, sz = (k >> 2) ? 1 : -1;
+        f += s[k] * wx * wy * wz;
+        ga += s[k] * sx * wy * wz;
+        gb += s[k] * wx * sy * wz;
+        gc += s[k] * wx * wy * sz;
+        hab += s[k] * sx * sy * wz;
+        hac += s[k] * sx * wy * sz;
+        hbc += s[k] * wx * sy * sz;
+    }
+    r.f = f;
+    r.g[0] = ga / vl;
+    r.g[1] = gb / vl;
+    r.g[2] = gc / vl;
+    r.Hxy = hab / (vl * vl);
+    r.Hxz = hac / (vl * vl);
+    r.Hyz = hbc / (vl * vl);
+    r.valid = true;
+    return r;
+}
+
+// Adjoint of orm_raycast_loss in FP64 (same formulas as the GPU adjoint):
+// grad[6] = dL/d(omega, upsilon) of the left increment; gvox (optional,
+// [blocks][512], zeroed by the caller) accumulates
+// dL/d(voxel TSDF value), blocks in the order of orm_grid_export (sorted by
+// key). Sequential.
+double orm_raycast_loss_grad(void *h, const double *T, const uint16_t *obs, double lambda_n, double r_max,
+                             int max_steps, double t_min, double t_max, double *grad, double *gvox) {
+    const Grid64 &g = *(Grid64 *)h;
+    double total = 0;
+    for (int k = 0; k < 6; k++) grad[k] = 0;
+    std::unordered_map<const Block64 *, size_t> index_of;
+    if (gvox) {
+        std::vector<std::pair<uint64_t, int>> items(g.map.begin(), g.map.end());
+        std::sort(items.begin(), items.end());
+        for (size_t q = 0; q < items.size(); q++) index_of.emplace(g.blocks[items[q].second], q);
+    }
+    for (int i = 0; i < g.resi; i++) {
+        Cache cache;
+        for (int j = 0; j < g.resj; j++) {
+            const double dcx = (j - (double)g.cj) / g.fx, dcy = (i - (double)g.ci) / g.fy;
+            const double d[3] = {T[0] * dcx + T[1] * dcy + T[2], T[4] * dcx + T[5] * dcy + T[6],
+                                 T[8] * dcx + T[9] * dcy + T[10]};
+            const double ox = T[3], oy = T[7], oz = T[11];
+            const double inv_len = 1.0 / std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+            int steps = 0;
+            double t = t_min;
+            if (!march64(g, cache, ox, oy, oz, d[0], d[1], d[2], inv_len, t_min, t_max, max_steps, steps, t)) continue;
+            Cell64 cs;
+            bool ok = true;
+            for (int it = 0; it < 6; it++) {
+                cs = cell64(g, ox + t * d[0], oy + t * d[1], oz + t * d[2], cache);
+                if (!cs.valid) {
+                    ok = false;
+                    break;
+                }
+                const double gd = cs.g[0] * d[0] + cs.g[1] * d[1] + cs.g[2] * d[2];
+                if (!(gd < 0)) {
+                    ok = false;
+                    break;
+                }
+                const double dt = -cs.f / gd;
+                if (std::fabs(dt) > 2 * g.vl * inv_len) {
+                    ok = false;
+                    break;
+                }
+                t += dt;
+                if (std::fabs(dt) < 1e-7 * t) break;
+            }
+            if (!ok) continue;
+            cs = cell64(g, ox + t * d[0], oy + t * d[1], oz + t * d[2], cache);
+            if (!cs.valid) continue;
+            const double d_obs = obs[(size_t)i * g.resj + j] * 1e-3;
+            if (!(d_obs > g.rmin)) continue;
+            const double gn = std::sqrt(cs.g[0] * cs.g[0] + cs.g[1] * cs.g[1] + cs.g[2] * cs.g[2]);
+            const double n[3] = {cs.g[0] / gn, cs.g[1] / gn, cs.g[2] / gn};
+            const double c = n[0] * d[0] + n[1] * d[1] + n[2] * d[2];
+            const double r = t - d_obs;
+            if (!(std::fabs(r) < r_max && c < -0.05)) continue;
+            total += r * r + lambda_n * (r * c) * (r * c);
+            const double p[3] = {ox + t * d[0], oy + t * d[1], oz + t * d[2]};
+            const double a = 2 * r * (1 + lambda_n * c * c), b = 2 * lambda_n * r * r * c;
+            const double gd = cs.g[0] * d[0] + cs.g[1] * d[1] + cs.g[2] * d[2];
+            double m[3];
+            for (int q = 0; q < 3; q++) m[q] = (d[q] - n[q] * c) / gn;
+            const double hh[3] = {cs.Hxy * m[1] + cs.Hxz * m[2], cs.Hxy * m[0] + cs.Hyz * m[2], cs.Hxz * m[0] + cs.Hyz * m[1]};
+            const double e = (a + b * (hh[0] * d[0] + hh[1] * d[1] + hh[2] * d[2])) / gd;
+            const double pg[3] = {p[1] * cs.g[2] - p[2] * cs.g[1], p[2] * cs.g[0] - p[0] * cs.g[2], p[0] * cs.g[1] - p[1] * cs.g[0]};
+            const double ph[3] = {p[1] * hh[2] - p[2] * hh[1], p[2] * hh[0] - p[0] * hh[2], p[0] * hh[1] - p[1] * hh[0]};
+            const double dn[3] = {d[1] * n[2] - d[2] * n[1], d[2] * n[0] - d[0] * n[2], d[0] * n[1] - d[1] * n[0]};
+            for (int q = 0; q < 3; q++) {
+                grad[q] += -e * pg[q] + b * (ph[q] + dn[q]);
+                grad[3 + q] += -e * cs.g[q] + b * hh[q];
+            }
+            if (gvox) {
+                for (int k = 0; k < 8; k++) {
+                    const double wx = (k & 1) ? cs.a : 1 - cs.a, wy = ((k >> 1) & 1) ? cs.b : 1 - cs.b;
+                    const double wz = (k >> 2) ? cs.c : 1 - cs.c;
+                    const double sx = (k & 1) ? 1 : -1, sy = ((k >> 1) & 1) ? 1 : -1, sz = (k >> 2) ? 1 : -1;
+                    const double mdw = (m[0] * sx * wy * wz + m[1] * wx * sy * wz + m[2] * wx * wy * sz) / g.vl;
+                    gvox[index_of.at(cs.blk[k]) * kVox + cs.vox[k]] += -e * (wx * wy * wz) + b * mdw;
+                }
+            }
+        }
+    }
+    return total;
+}
+
 static double *g_track_log = nullptr;  // optional per-iteration step norms [level][16] (tests)
 static double g_track_eps = 1e-7;        // convergence threshold on the step norm
 
