@@ -74,6 +74,18 @@ typedef struct ss_params {
 
 typedef struct ss_grid ss_grid;
 
+/* Launch shapes of a grid's kernels (no reference counterpart), chosen by
+ * the autotuner (superscanner_gb300/autotune.py) or left at the defaults.
+ * Pixel kernels run 32 x rows thread tiles (one warp per 32 pixels of a
+ * row); persistent kernels run ctas_per_sm x SM-count CTAs of 256 threads. */
+typedef struct ss_launch_config {
+    int32_t collect_rows;       /* block collection tile rows, 1..8 (default 8) */
+    int32_t raycast_rows;       /* model-view raycast tile rows, 1..8 (default 8) */
+    int32_t fuse_ctas_per_sm;   /* integrate / deintegrate, 1..32 (default 8) */
+    int32_t refuse_ctas_per_sm; /* batched re-fusion apply, 1..32 (default 8) */
+    int32_t track_ctas_per_sm;  /* persistent tracker, 1..2, capped by occupancy (default 2) */
+} ss_launch_config;
+
 /* Fills the reference defaults of GPUVoxelGrid(c, trunc, voxlength, resi, resj)
  * (GPUVoxelGrid.cpp:10-30): buckets = next power of two >= c / 512. */
 ss_status ss_params_default(ss_params *p, uint32_t capacity_voxels, float trunc,
@@ -81,6 +93,10 @@ ss_status ss_params_default(ss_params *p, uint32_t capacity_voxels, float trunc,
 
 ss_status ss_grid_create(const ss_params *p, ss_grid **out);
 ss_status ss_grid_destroy(ss_grid *g);
+ss_status ss_grid_get_launch_config(const ss_grid *g, ss_launch_config *c);
+/* Takes effect for later launches; a pipeline reads it when it is created. */
+ss_status ss_grid_set_launch_config(ss_grid *g, const ss_launch_config *c);
+
 /* Resets the volume to empty (all buckets free, all payload zero). */
 ss_status ss_grid_reset(ss_grid *g, ss_stream_t s);
 

@@ -48,6 +48,11 @@ _p, _i32, _u32, _f, _st = C.c_void_p, C.c_int32, C.c_uint32, C.c_float, C.c_int
 _F16 = C.POINTER(C.c_float)
 _D16 = C.POINTER(C.c_double)
 
+class SSLaunchConfig(C.Structure):
+    _fields_ = [("collect_rows", C.c_int32), ("raycast_rows", C.c_int32), ("fuse_ctas_per_sm", C.c_int32),
+                ("refuse_ctas_per_sm", C.c_int32), ("track_ctas_per_sm", C.c_int32)]
+
+
 class SSPipelineParams(C.Structure):
     _fields_ = [
         ("levels", C.c_int32), ("iters", C.c_int32 * 4), ("dist_thresh", C.c_float * 4),
@@ -65,6 +70,8 @@ SIGNATURES = {
     "ss_grid_create": (_st, [C.POINTER(SSParams), C.POINTER(_p)]),
     "ss_grid_destroy": (_st, [_p]),
     "ss_grid_reset": (_st, [_p, _p]),
+    "ss_grid_get_launch_config": (_st, [_p, C.POINTER(SSLaunchConfig)]),
+    "ss_grid_set_launch_config": (_st, [_p, C.POINTER(SSLaunchConfig)]),
     "ss_grid_set_intrinsic": (_st, [_p, _f, _f, _f, _f]),
     "ss_integrate": (_st, [_p, _p, _p, _F16, _i32, _p]),
     "ss_deintegrate": (_st, [_p, _p, _p, _F16, _i32, _p]),

@@ -512,11 +512,12 @@ ss_status launch_fuse(ss_grid *g, const uint16_t *depth, const uint8_t *rgb, con
         ss_status st = rebase_epoch(g, s);
         if (st != SS_OK) return st;
     }
-    const dim3 cblk(32, 8), cgrid((g->p.resj + 31) / 32, (g->p.resi + 7) / 8);
+    const int cr = g->lc.collect_rows;
+    const dim3 cblk(32, cr), cgrid((g->p.resj + 31) / 32, (g->p.resi + cr - 1) / cr);
     collect_kernel<<<cgrid, cblk, 0, s>>>(g->v, depth, E, dpose);
     SS_LAUNCH_CHECK();
     if (after_collect) SS_CUDA_TRY(cudaEventRecord(after_collect, s));
-    const int ctas = persistent_ctas(g, 8);
+    const int ctas = persistent_ctas(g, g->lc.fuse_ctas_per_sm);
 #define SS_FUSE(ST, C, D, X) fuse_kernel<ST, C, D, X><<<ctas, 256, 0, s>>>(g->v, depth, rgb, E, Einv, Ez, dpose)
 #define SS_FUSE_X(ST, C, D) \
     do {                    \
@@ -566,6 +567,22 @@ ss_status ss_params_default(ss_params *p, uint32_t capacity_voxels, float trunc,
     p->max_weight = 0.f;
     p->rmin = 0.2f;
     p->d_max = 10.0f;
+    return SS_OK;
+}
+
+ss_status ss_grid_get_launch_config(const ss_grid *g, ss_launch_config *c) {
+    if (!g || !c) return SS_ERR_ARG;
+    *c = g->lc;
+    return SS_OK;
+}
+
+ss_status ss_grid_set_launch_config(ss_grid *g, const ss_launch_config *c) {
+    if (!g || !c) return SS_ERR_ARG;
+    if (c->collect_rows < 1 || c->collect_rows > 8 || c->raycast_rows < 1 || c->raycast_rows > 8 ||
+        c->fuse_ctas_per_sm < 1 || c->fuse_ctas_per_sm > 32 || c->refuse_ctas_per_sm < 1 ||
+        c->refuse_ctas_per_sm > 32 || c->track_ctas_per_sm < 1 || c->track_ctas_per_sm > 2)
+        return SS_ERR_ARG;
+    g->lc = *c;
     return SS_OK;
 }
 

@@ -13,6 +13,7 @@ struct ss_grid {
     ss::GridView v;
     bool intr_set = false;
     float fx = 0, fy = 0, cx = 0, cy = 0;
+    ss_launch_config lc{8, 8, 8, 8, 2};  // launch shapes (autotuner)
     uint32_t host_epoch = 1;  // mirror of Counters::epoch for wrap handling
     int device = 0;
     int num_sms = 0;

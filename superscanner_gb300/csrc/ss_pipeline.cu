@@ -141,8 +141,8 @@ ss_status ss_pipeline_create(ss_grid *g, const ss_pipeline_params *params, ss_pi
     P->g = g;
     P->p = *params;
     P->ctas = g->num_sms * 2;
-    P->track_ctas = persistent_track_ctas(g->num_sms);
-    const int slot_ctas = P->ctas > P->track_ctas ? P->ctas : P->track_ctas;
+    P->track_ctas = persistent_track_ctas(g->num_sms, g->lc.track_ctas_per_sm);
+    const int slot_ctas = P->ctas > 2 * g->num_sms ? P->ctas : 2 * g->num_sms;
     const size_t npix = (size_t)g->p.resi * g->p.resj;
     bool ok = cudaMalloc(&P->st, sizeof(TrackState)) == cudaSuccess &&
               cudaMalloc(&P->partials, 2 * (size_t)slot_ctas * 29 * sizeof(float2)) == cudaSuccess &&

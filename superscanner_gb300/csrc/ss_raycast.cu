@@ -283,7 +283,8 @@ __global__ void __launch_bounds__(256) raycast_maps_kernel(GridView g, Mat34 T, 
 ss_status launch_raycast_maps(ss_grid *g, const Mat34 &T, const FramePose *dpose, int max_steps, float t_min,
                               float t_max, float4 *vmap, float4 *nmap, cudaStream_t s, unsigned long long *counters,
                               const uint16_t *hint, float hint_margin) {
-    const dim3 blk(32, 8), grid((g->p.resj + 31) / 32, (g->p.resi + 7) / 8);
+    const int rr = g->lc.raycast_rows;
+    const dim3 blk(32, rr), grid((g->p.resj + 31) / 32, (g->p.resi + rr - 1) / rr);
     if (g->p.storage == SS_STORAGE_F32)
         raycast_maps_kernel<SS_STORAGE_F32><<<grid, blk, 0, s>>>(g->v, T, dpose, max_steps, t_min, t_max, vmap, nmap,
                                                                  counters, hint, hint_margin);

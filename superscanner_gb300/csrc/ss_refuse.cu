@@ -303,7 +303,7 @@ extern "C" ss_status ss_refuse_batch(ss_grid *g, int32_t n, const uint16_t *cons
     const dim3 cblk(32, 8), cgrid((g->p.resj + 31) / 32, (g->p.resi + 7) / 8, 2 * n);
     refuse_collect_kernel<<<cgrid, cblk, 0, s>>>(g->v, g->batch_depths, g->batch_poses, g->phase_mask);
     SS_LAUNCH_CHECK();
-    const int ctas = persistent_ctas(g, 8);
+    const int ctas = persistent_ctas(g, g->lc.refuse_ctas_per_sm);
     const bool f32 = g->p.storage == SS_STORAGE_F32;
     if (f32 && exact) refuse_apply_kernel<SS_STORAGE_F32, true><<<ctas, 256, 0, s>>>(g->v, g->batch_depths, g->batch_poses, g->phase_mask);
     else if (f32) refuse_apply_kernel<SS_STORAGE_F32, false><<<ctas, 256, 0, s>>>(g->v, g->batch_depths, g->batch_poses, g->phase_mask);

@@ -427,13 +427,14 @@ extern "C" int ss_debug_track_timing(unsigned long long *out) {
 }
 #endif
 
-int persistent_track_ctas(int num_sms) {
+int persistent_track_ctas(int num_sms, int want_per_sm) {
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, track_frame_kernel, 256, 0) != cudaSuccess) {
         cudaGetLastError();
         per_sm = 1;
     }
-    return num_sms * (per_sm >= 2 ? 2 : (per_sm < 1 ? 1 : per_sm));
+    if (per_sm > want_per_sm) per_sm = want_per_sm;
+    return num_sms * (per_sm < 1 ? 1 : per_sm);
 }
 
 // Host-side launch of one frame's tracking: begin, levels coarse to fine,

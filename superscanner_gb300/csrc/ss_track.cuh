@@ -40,8 +40,8 @@ struct TrackLaunch {
 };
 
 ss_status launch_track(const TrackLaunch &L, cudaStream_t s);
-// CTAs of the persistent tracker on this device (co-resident, <= 2 per SM).
-int persistent_track_ctas(int num_sms);
+// CTAs of the persistent tracker on this device (co-resident, <= want_per_sm per SM).
+int persistent_track_ctas(int num_sms, int want_per_sm);
 ss_status launch_pose_prep(TrackState *st, cudaStream_t s);
 
 }  // namespace ss

@@ -15,7 +15,7 @@ import ctypes as C
 import numpy as np
 import torch
 
-from ._native import (SS_STORAGE_F16, SS_STORAGE_F32, SSParams, check, f32x16, lib)
+from ._native import (SS_STORAGE_F16, SS_STORAGE_F32, SSLaunchConfig, SSParams, check, f32x16, lib)
 
 _STORAGE = {"f32": SS_STORAGE_F32, "f16": SS_STORAGE_F16}
 
@@ -129,6 +129,19 @@ class GPUVoxelGrid:
         check(lib.ss_clean_memory(self._h, _stream_ptr(stream)), "cleanMemory")
 
     # -- additions of the C-ABI
+    LAUNCH_FIELDS = ("collect_rows", "raycast_rows", "fuse_ctas_per_sm", "refuse_ctas_per_sm", "track_ctas_per_sm")
+
+    def launch_config(self) -> dict:
+        c = SSLaunchConfig()
+        check(lib.ss_grid_get_launch_config(self._h, C.byref(c)), "get_launch_config")
+        return {f: getattr(c, f) for f in self.LAUNCH_FIELDS}
+
+    def set_launch_config(self, **kw) -> None:
+        cur = self.launch_config()
+        cur.update(kw)
+        c = SSLaunchConfig(*[int(cur[f]) for f in self.LAUNCH_FIELDS])
+        check(lib.ss_grid_set_launch_config(self._h, C.byref(c)), "set_launch_config")
+
     def sync(self, stream=None) -> None:
         check(lib.ss_grid_sync(self._h, _stream_ptr(stream)), "sync")
 
