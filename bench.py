@@ -175,10 +175,13 @@ def run_form(torch, form: str, depth_dev, P, W: int, K: int, stream, barrier, pr
             sampler.mark(True)
         torch.cuda.synchronize()
         ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        # NVTX range: lets ncu --nvtx-include select exactly the timed frames of one form
+        torch.cuda.nvtx.range_push(f"{form}_{'stages' if profile else 'timed'}")
         ev0.record(stream)
         for k in range(1 + W, 1 + W + K):
             pipe.frame(depth_dev[k], stream=stream)
         ev1.record(stream)
+        torch.cuda.nvtx.range_pop()
         torch.cuda.synchronize()
         if sampler:
             sampler.mark(False)
@@ -455,14 +458,18 @@ def main_ours(args):
 
     dom, roof, table = roofline(prof["stage_ms"], prof["prof_frames"], prof["touched"], prof["rc"], 4, peak,
                                 peak_kind)
+    # DRAM bytes per launch of the dominant kernel from the committed ncu capture
+    # (dram__bytes_read.sum + dram__bytes_write.sum, same workload); null without one
     traffic = None
-    tf = ROOT / "profiles" / "ncu_traffic.json"
+    tf = ROOT / "profiles" / "dram_traffic_chosen_640x480_4mm.json"
     if tf.exists():
         try:
-            traffic = json.loads(tf.read_text()).get(dom)
-        except (ValueError, OSError):
+            traffic = json.loads(tf.read_text())["bytes_per_launch"].get(dom)
+        except (ValueError, OSError, KeyError):
             traffic = None
     roof["traffic"] = traffic
+    if traffic is not None:
+        roof["traffic_source"] = "ncu capture, " + tf.name
 
     refusion = run_refusion(torch, depth, P, stream, launch=tuned) if rank == 0 else None
 
