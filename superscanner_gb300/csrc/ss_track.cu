@@ -6,16 +6,20 @@
 // the raycast model view instead (projective association, point-to-plane
 // residual), over a 3-level pyramid of the source depth.
 //
-// One kernel per iteration. Source pixels of level l are the level-0 pixels
-// (i 2^l, j 2^l) back-projected with the level-0 intrinsics (no pyramid
-// images are built). Each thread accumulates the 21 + 6 + 2 normal-equation
-// sums in FP32 with Kahan compensation; warps combine (sum, compensation)
-// pairs with TwoSum through shuffles, CTAs through shared memory, and the
-// last CTA to finish reduces the CTA slots in FP64 in a fixed order, solves
-// the 6x6 system by Cholesky in FP64 and applies the SE(3) update in FP64.
-// No host synchronisation between iterations, levels or frames.
+// Source pixels of level l are the level-0 pixels (i 2^l, j 2^l)
+// back-projected with the level-0 intrinsics (no pyramid images are built).
+// Each thread accumulates the 21 + 6 + 2 normal-equation sums in FP32 with
+// Kahan compensation; warps combine (sum, compensation) pairs with TwoSum
+// through shuffles, CTAs through shared memory, and the CTA slots are reduced
+// the same way in a fixed order. One warp then solves the 6x6 system and
+// applies the SE(3) update in FP64 (ss_track_solve.cuh). Two launch forms:
+// one cooperative launch per frame (every CTA reduces and solves redundantly,
+// one grid barrier per iteration), or one launch per iteration (the last CTA
+// to finish solves). No host synchronisation between iterations, levels or
+// frames.
 #include "ss_grid_impl.cuh"
 #include "ss_track.cuh"
+#include "ss_track_solve.cuh"
 
 namespace ss {
 
@@ -65,85 +69,6 @@ __device__ void write_frame_pose(const double *T, FramePose *fp) {
     fp->Ez[1] = ey / len;
     fp->Ez[2] = ez / len;
     fp->pad = 0.f;
-}
-
-// exp of an se(3) twist (omega, upsilon) in FP64, left-multiplied onto T.
-__device__ void se3_left_update(const double *xi, double *T) {
-    const double wx = xi[0], wy = xi[1], wz = xi[2];
-    const double th2 = wx * wx + wy * wy + wz * wz, th = sqrt(th2);
-    double A, B, C;
-    if (th < 0.05) {
-        // Maclaurin series of sin(t)/t, (1-cos t)/t^2, (t-sin t)/t^3 to t^8: the first
-        // omitted term is below 3e-21 for t < 0.05, so this is exact in double and
-        // avoids the FP64 sin/cos on the (serial) solve path.
-        const double t2 = th2;
-        A = 1.0 + t2 * (-1.0 / 6 + t2 * (1.0 / 120 + t2 * (-1.0 / 5040 + t2 * (1.0 / 362880))));
-        B = 0.5 + t2 * (-1.0 / 24 + t2 * (1.0 / 720 + t2 * (-1.0 / 40320 + t2 * (1.0 / 3628800))));
-        C = 1.0 / 6 + t2 * (-1.0 / 120 + t2 * (1.0 / 5040 + t2 * (-1.0 / 362880 + t2 * (1.0 / 39916800))));
-    } else {
-        A = sin(th) / th;
-        B = (1.0 - cos(th)) / th2;
-        C = (th - sin(th)) / (th2 * th);
-    }
-    const double K[9] = {0, -wz, wy, wz, 0, -wx, -wy, wx, 0};
-    double K2[9];
-    for (int r = 0; r < 3; r++)
-        for (int c = 0; c < 3; c++) K2[r * 3 + c] = K[r * 3] * K[c] + K[r * 3 + 1] * K[3 + c] + K[r * 3 + 2] * K[6 + c];
-    double R[9], V[9];
-    for (int k = 0; k < 9; k++) {
-        const double I = (k % 4 == 0) ? 1.0 : 0.0;
-        R[k] = I + A * K[k] + B * K2[k];
-        V[k] = I + B * K[k] + C * K2[k];
-    }
-    const double t[3] = {V[0] * xi[3] + V[1] * xi[4] + V[2] * xi[5], V[3] * xi[3] + V[4] * xi[4] + V[5] * xi[5],
-                         V[6] * xi[3] + V[7] * xi[4] + V[8] * xi[5]};
-    double N[16];
-    for (int r = 0; r < 3; r++) {
-        for (int c = 0; c < 4; c++)
-            N[r * 4 + c] = R[r * 3] * T[c] + R[r * 3 + 1] * T[4 + c] + R[r * 3 + 2] * T[8 + c] + (c == 3 ? t[r] : 0.0);
-    }
-    for (int k = 0; k < 12; k++) T[k] = N[k];
-    T[12] = T[13] = T[14] = 0.0;
-    T[15] = 1.0;
-}
-
-// Cholesky solve of A x = b (6x6 SPD, FP64). Returns false if A is not SPD.
-// Column-oriented (right-looking) so the updates of one column are independent
-// and pipeline; one reciprocal square root per column instead of a division
-// per element.
-__device__ bool cholesky6(const double *A, const double *b, double *x) {
-    double L[36], inv[6];
-#pragma unroll
-    for (int k = 0; k < 36; k++) L[k] = A[k];
-#pragma unroll
-    for (int j = 0; j < 6; j++) {
-        const double d = L[j * 6 + j];
-        if (!(d > 1e-12)) return false;
-        const double r = rsqrt(d);
-        inv[j] = r;
-#pragma unroll
-        for (int i = j; i < 6; i++) L[i * 6 + j] *= r;  // L[j][j] = sqrt(d)
-#pragma unroll
-        for (int c = j + 1; c < 6; c++)
-#pragma unroll
-            for (int i = c; i < 6; i++) L[i * 6 + c] -= L[i * 6 + j] * L[c * 6 + j];
-    }
-    double y[6];
-#pragma unroll
-    for (int i = 0; i < 6; i++) {
-        double s = b[i];
-#pragma unroll
-        for (int k = 0; k < i; k++) s -= L[i * 6 + k] * y[k];
-        y[i] = s * inv[i];
-    }
-#pragma unroll
-    for (int i = 5; i >= 0; i--) {
-        double s = y[i];
-#pragma unroll
-        for (int k = i + 1; k < 6; k++) s -= L[k * 6 + i] * x[k];
-        x[i] = s * inv[i];
-    }
-    return true;
 }
 
 // Start of a frame: the model maps were raycast at the last pose T, so
@@ -235,39 +160,45 @@ __device__ __forceinline__ void track_cta_to_slots(float *s, float *c, float2 (*
     }
 }
 
-// Reduces all CTA slots (one warp per value, TwoSum in FP32, fixed order) into tot (FP64).
-__device__ __forceinline__ void track_slots_to_totals(const float2 *__restrict__ slots, double *tot) {
+// Reduces all CTA slots into (sum, compensation) pairs, TwoSum in FP32 in a
+// fixed order: warp w takes values w, w + 8, w + 16, w + 24 (256 threads), each
+// lane a strided share of the CTAs; all loads of a chunk are issued before its
+// additions.
+__device__ __forceinline__ void track_slots_to_pairs(const float2 *__restrict__ slots, float2 *tot) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    for (int v = wid; v < kTrackSums; v += (int)(blockDim.x >> 5)) {
-        float a = 0.f, b = 0.f;
-        for (unsigned q = lane; q < gridDim.x; q += 32) {
-            const float2 pq = __ldcg(slots + (size_t)v * gridDim.x + q);
-            pair_add(a, b, pq.x, pq.y);
+    constexpr int kPer = (kTrackSums + 7) / 8;
+    const unsigned n = gridDim.x;
+    float a[kPer], b[kPer];
+#pragma unroll
+    for (int u = 0; u < kPer; u++) a[u] = b[u] = 0.f;
+#pragma unroll 2
+    for (unsigned q = lane; q < n; q += 32) {
+        float2 p[kPer];
+#pragma unroll
+        for (int u = 0; u < kPer; u++) {
+            const int v = wid + 8 * u;
+            p[u] = v < kTrackSums ? __ldcg(slots + (size_t)v * n + q) : make_float2(0.f, 0.f);
         }
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            const float a2 = __shfl_down_sync(0xffffffffu, a, o), b2 = __shfl_down_sync(0xffffffffu, b, o);
-            pair_add(a, b, a2, b2);
+        for (int u = 0; u < kPer; u++) pair_add(a[u], b[u], p[u].x, p[u].y);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+        for (int u = 0; u < kPer; u++) {
+            const float a2 = __shfl_down_sync(0xffffffffu, a[u], o), b2 = __shfl_down_sync(0xffffffffu, b[u], o);
+            pair_add(a[u], b[u], a2, b2);
         }
-        if (lane == 0) tot[v] = (double)a - (double)b;
+    }
+    if (lane == 0) {
+#pragma unroll
+        for (int u = 0; u < kPer; u++)
+            if (wid + 8 * u < kTrackSums) tot[wid + 8 * u] = make_float2(a[u], b[u]);
     }
 }
 
-// FP64 solve of the normal equations and left SE(3) update of T; returns the
-// step norm (negative when the system was not solved).
-__device__ double track_solve(const double *tot, double *T) {
-    if (tot[28] < 60.0) return -1.0;  // too few correspondences: keep the pose
-    double A[36], b[6], x[6];
-    int q = 0;
-    for (int r = 0; r < 6; r++)
-        for (int cc = r; cc < 6; cc++) {
-            A[r * 6 + cc] = A[cc * 6 + r] = tot[q++];
-        }
-    for (int r = 0; r < 6; r++) b[r] = -tot[21 + r];
-    if (!cholesky6(A, b, x)) return -1.0;
-    se3_left_update(x, T);
-    return sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2] + x[3] * x[3] + x[4] * x[4] + x[5] * x[5]);
-}
+// Value of a (sum, compensation) pair.
+__device__ __forceinline__ float pair_value(float2 p) { return p.x - p.y; }
 
 __global__ void __launch_bounds__(256) track_iter_kernel(const uint16_t *__restrict__ depth, int rows, int cols,
                                                          Intr in, const float4 *__restrict__ vmap,
@@ -277,7 +208,7 @@ __global__ void __launch_bounds__(256) track_iter_kernel(const uint16_t *__restr
     if (*(volatile int *)&st->converged_level == level) return;
     __shared__ float2 red[8][kTrackSums];
     __shared__ bool last;
-    __shared__ double tot[kTrackSums];
+    __shared__ float2 tot[kTrackSums];
     float T[12], Pi[12];
 #pragma unroll
     for (int k = 0; k < 12; k++) {
@@ -296,18 +227,21 @@ __global__ void __launch_bounds__(256) track_iter_kernel(const uint16_t *__restr
     __syncthreads();
     if (!last) return;
     __threadfence();
-    // last CTA: FP32 TwoSum over the slots, FP64 only for the solve (FP64 is
-    // scarce on this part and a serial FP64 chain here stalls the whole GPU)
-    track_slots_to_totals(partials, tot);
+    // last CTA: reduce the slots, then one warp solves in FP64
+    track_slots_to_pairs(partials, tot);
     __syncthreads();
-    if (threadIdx.x != 0) return;
-    st->ticket = 0;
-    const double n = tot[28];
-    st->inliers[level] = (int)n;
-    st->rmse[level] = n > 0 ? (float)sqrt(tot[27] / n) : 0.f;
-    const double step = track_solve(tot, st->T);
-    if (step >= 0.0) mat_from_T(st->T, st->Tf);
-    if (step >= 0.0 && step < 1e-7) st->converged_level = level;
+    const float n = pair_value(tot[28]);
+    if (threadIdx.x < 32) {
+        if (threadIdx.x == 0) st->ticket = 0;
+        double x[6];
+        if (n >= 60.f && warp_solve6(tot, x)) {  // too few correspondences: keep the pose
+            const float step2 = warp_se3_left_update(x, st->T, st->T, st->Tf);
+            if (threadIdx.x == 0 && step2 < 1e-14f) st->converged_level = level;
+        }
+    } else if (threadIdx.x == 32) {
+        st->inliers[level] = (int)n;
+        st->rmse[level] = n > 0.f ? sqrtf(fmaxf(pair_value(tot[27]), 0.f) / n) : 0.f;
+    }
 }
 
 // Bounded grid barrier of the cooperative tracker: arrival count, spin with
@@ -361,7 +295,7 @@ __global__ void __launch_bounds__(256) track_frame_kernel(const uint16_t *__rest
                                                           const float4 *__restrict__ nmap, TrackState *st,
                                                           float2 *__restrict__ slots, TrackLaunch L) {
     __shared__ float2 red[8][kTrackSums];
-    __shared__ double tot[kTrackSums];
+    __shared__ float2 tot[kTrackSums];
     __shared__ double Td[16];
     __shared__ float Tf[12], Pi[12];
     __shared__ int done_level;
@@ -396,19 +330,19 @@ __global__ void __launch_bounds__(256) track_frame_kernel(const uint16_t *__rest
             SS_TT(barriers, 2);
             if (!grid_barrier(st, (++barriers) * gridDim.x)) return;
             SS_TT(barriers - 1, 3);
-            track_slots_to_totals(buf, tot);
+            track_slots_to_pairs(buf, tot);
             __syncthreads();
             SS_TT(barriers - 1, 4);
-            if (threadIdx.x == 0) {
-                const double step = track_solve(tot, Td);
-                if (step >= 0.0)
-                    for (int k = 0; k < 12; k++) Tf[k] = (float)Td[k];
-                if (step >= 0.0 && step < 1e-7) done_level = level;
-                if (blockIdx.x == 0) {
-                    const double n = tot[28];
-                    st->inliers[level] = (int)n;
-                    st->rmse[level] = n > 0 ? (float)sqrt(tot[27] / n) : 0.f;
+            const float n = pair_value(tot[28]);
+            if (threadIdx.x < 32) {
+                double x[6];
+                if (n >= 60.f && warp_solve6(tot, x)) {  // too few correspondences: keep the pose
+                    const float step2 = warp_se3_left_update(x, Td, Td, Tf);
+                    if (threadIdx.x == 0 && step2 < 1e-14f) done_level = level;
                 }
+            } else if (blockIdx.x == 0 && threadIdx.x == 32) {
+                st->inliers[level] = (int)n;
+                st->rmse[level] = n > 0.f ? sqrtf(fmaxf(pair_value(tot[27]), 0.f) / n) : 0.f;
             }
             __syncthreads();
             SS_TT(barriers - 1, 5);

@@ -1,0 +1,189 @@
+// ss_track_solve.cuh — FP64 solve of the tracker's 6x6 normal equations and
+// the SE(3) pose update, by one warp.
+//
+// On this part an FP64 warp instruction occupies its SM sub-partition's FP64
+// pipe for ~64 cycles whether one lane or 32 are active, so a one-thread solve
+// costs ~64 cycles per FP64 operation (~140 operations for a Cholesky solve
+// with square roots, ~130 more for the SE(3) exponential and pose product).
+// Here every lane owns one entry, so each step of the factorisation, the back
+// substitution and the pose update is one or two warp instructions, and no
+// square root is taken:
+//
+// * elimination: symmetric Gaussian elimination without pivoting on the
+//   augmented upper triangle [A | b] (27 lanes), i.e. the square-root-free
+//   (LDL^T) form of Cholesky. Each step updates the trailing rows in
+//   fraction-free form, a_ij <- p' a_ij - a_ki (a_kj 2^-e), with the pivot
+//   p = p' 2^e split exactly into p' in [1, 2) and a power of two by integer
+//   operations: the same rows as LDL^T, each scaled by a factor in [1, 2), so
+//   no division sits on the elimination's critical path;
+// * back substitution with the reciprocals of the six pivots, computed
+//   together: an FP32 seed refined by two Newton-Raphson steps in FP64
+//   (r <- r + r (1 - m r); the relative error squares each step, 2^-23 ->
+//   2^-46 -> below FP64 rounding);
+// * SE(3) exponential by Maclaurin series of sin t / t, (1 - cos t) / t^2,
+//   (t - sin t) / t^3 (one series per lane), R and V entries one per lane,
+//   then the pose product R T + V upsilon one entry per lane.
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace ss {
+
+constexpr int kAugLanes = 27;  // entries (i, j) of [A | b], 0 <= i <= j <= 6, i < 6
+constexpr double kPivotMin = 1e-12;
+
+// lane of entry (i, j) of the augmented upper triangle (rows of 7, 6, ..., 2)
+__device__ __forceinline__ int aug_lane(int i, int j) { return 7 * i - ((i * (i - 1)) >> 1) + (j - i); }
+
+// entry (i, j) of lane (lanes >= kAugLanes get j > 6)
+__device__ __forceinline__ void aug_entry(int lane, int &i, int &j) {
+    i = 0;
+#pragma unroll
+    for (int r = 1; r < 6; r++)
+        if (lane >= aug_lane(r, r)) i = r;
+    j = i + (lane - aug_lane(i, i));
+}
+
+// x = m 2^e with m in [1, 2) (sign kept), for finite normal x; integer operations only.
+__device__ __forceinline__ double split_pow2(double x, int &e) {
+    const int hi = __double2hiint(x), lo = __double2loint(x);
+    e = ((hi >> 20) & 0x7ff) - 1023;
+    return __hiloint2double((hi & 0x800fffff) | 0x3ff00000, lo);
+}
+
+// x 2^-e, exact by exponent arithmetic (zero and subnormal inputs, and
+// results below the normal range, give zero).
+__device__ __forceinline__ double scale_pow2(double x, int e) {
+    const int hi = __double2hiint(x), lo = __double2loint(x);
+    const int ex = (hi >> 20) & 0x7ff;
+    const int nx = ex - e;
+    if (ex == 0 || nx <= 0) return 0.0;
+    if (nx >= 0x7ff) return __hiloint2double((hi & 0x80000000) | 0x7ff00000, 0);
+    return __hiloint2double((hi & 0x800fffff) | (nx << 20), lo);
+}
+
+// 1 / x for finite normal x > 0: FP32 seed on the mantissa, two Newton-Raphson steps in FP64.
+__device__ __forceinline__ double rcp_pos(double x) {
+    int e;
+    const double m = split_pow2(x, e);
+    float sf;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(sf) : "f"((float)m));
+    double r = (double)sf;
+    double t = fma(-m, r, 1.0);
+    r = fma(r, t, r);
+    t = fma(-m, r, 1.0);
+    r = fma(r, t, r);
+    return scale_pow2(r, e);
+}
+
+// Solves A x = b in FP64 with the calling warp (all 32 lanes, converged).
+// pairs[0..20]: the upper triangle of A row-major, pairs[21..26]: J^T r (b = -J^T r),
+// each an FP32 (sum, compensation) pair with value sum - compensation.
+// Every lane returns the same x and the same verdict (false: a pivot <= kPivotMin).
+__device__ __forceinline__ bool warp_solve6(const float2 *pairs, double x[6]) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    int i, j;
+    aug_entry(lane, i, j);
+    const bool live = lane < kAugLanes;
+    double a = 0.0;
+    if (live) {
+        const int q = (j < 6) ? 6 * i - ((i * (i - 1)) >> 1) + (j - i) : 21 + i;
+        const float2 p = pairs[q];
+        a = (double)p.x - (double)p.y;
+        if (j == 6) a = -a;
+    }
+    bool ok = true;
+#pragma unroll
+    for (int k = 0; k < 5; k++) {
+        const double p = __shfl_sync(full, a, aug_lane(k, k));
+        ok = ok && (p > kPivotMin);
+        int e;
+        const double ph = split_pow2(p, e);
+        const bool upd = live && i > k;
+        const double ahat = (live && i == k) ? scale_pow2(a, e) : a;  // row k times 2^-e
+        const double aki = __shfl_sync(full, a, upd ? aug_lane(k, i) : 0);
+        const double akj = __shfl_sync(full, ahat, upd ? aug_lane(k, j) : 0);
+        if (upd) a = fma(ph, a, -(aki * akj));
+    }
+    ok = ok && (__shfl_sync(full, a, aug_lane(5, 5)) > kPivotMin);
+    // reciprocals of the six pivots (diagonal lanes), then back substitution on lanes (i, 6)
+    const bool diag = live && i == j;
+    const double r = rcp_pos(diag && a > kPivotMin ? a : 1.0);
+    const bool rhs = live && j == 6;
+    double u[6];
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+        const bool mine = rhs && k > i;
+        const double v = __shfl_sync(full, a, mine ? aug_lane(i, k) : 0);
+        u[k] = mine ? v : 0.0;
+    }
+    const double rii = __shfl_sync(full, r, rhs ? aug_lane(i, i) : 0);
+    double c = a;
+#pragma unroll
+    for (int k = 5; k >= 0; k--) {
+        x[k] = __shfl_sync(full, c * rii, aug_lane(k, 6));
+        c = fma(-u[k], x[k], c);
+    }
+    return ok;
+}
+
+// T <- exp(xi) T (left increment, xi = (omega, upsilon)) in FP64 with the calling
+// warp. Tin: 12 doubles (rows of [R | t]); Tout (12 doubles) and Tfout (12 floats)
+// are written by lanes 0..11 and may alias Tin only if the caller syncs the warp
+// before reading them. Returns |xi|^2 (FP32, every lane).
+__device__ __forceinline__ float warp_se3_left_update(const double xi[6], const double *Tin, double *Tout,
+                                                      float *Tfout) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const double wx = xi[0], wy = xi[1], wz = xi[2];
+    const double th2 = fma(wx, wx, fma(wy, wy, wz * wz));
+    // lane s = lane % 3 evaluates series s: A = sin t / t, B = (1 - cos t) / t^2, C = (t - sin t) / t^3
+    const int s = lane % 3;
+    double coef;
+    if (th2 < 0.0025) {
+        // Maclaurin series to t^8: the first omitted term is below 3e-21 for t < 0.05
+        const double c4 = s == 0 ? 1.0 / 362880 : (s == 1 ? 1.0 / 3628800 : 1.0 / 39916800);
+        const double c3 = s == 0 ? -1.0 / 5040 : (s == 1 ? -1.0 / 40320 : -1.0 / 362880);
+        const double c2 = s == 0 ? 1.0 / 120 : (s == 1 ? 1.0 / 720 : 1.0 / 5040);
+        const double c1 = s == 0 ? -1.0 / 6 : (s == 1 ? -1.0 / 24 : -1.0 / 120);
+        const double c0 = s == 0 ? 1.0 : (s == 1 ? 0.5 : 1.0 / 6);
+        coef = fma(fma(fma(fma(c4, th2, c3), th2, c2), th2, c1), th2, c0);
+    } else {
+        const double th = sqrt(th2), sn = sin(th), cs = cos(th);
+        coef = s == 0 ? sn / th : (s == 1 ? (1.0 - cs) / th2 : (th - sn) / (th2 * th));
+    }
+    const double A = __shfl_sync(full, coef, 0), B = __shfl_sync(full, coef, 1), C = __shfl_sync(full, coef, 2);
+    // lanes 0..8: R = I + A K + B K^2; lanes 9..17: V = I + B K + C K^2 (K = [omega]x,
+    // K^2 = w w^T - t^2 I); entry (r, c) = ((lane % 9) / 3, lane % 3)
+    const int e9 = lane % 9, r = e9 / 3, cc = e9 % 3;
+    const double wr = r == 0 ? wx : (r == 1 ? wy : wz), wc = cc == 0 ? wx : (cc == 1 ? wy : wz);
+    const int wk = 3 - r - cc;  // index of the omega component in K[r][c] for r != c
+    const double wkv = wk == 0 ? wx : (wk == 1 ? wy : wz);
+    // K[r][c] = -eps(r, c, k) w_k: K01 = -wz, K02 = wy, K10 = wz, K12 = -wx, K20 = -wy, K21 = wx
+    const bool pos = (r == 1 && cc == 0) || (r == 0 && cc == 2) || (r == 2 && cc == 1);
+    const double kv = r == cc ? 0.0 : (pos ? wkv : -wkv);
+    const double k2 = fma(wr, wc, r == cc ? -th2 : 0.0);
+    const bool isR = lane < 9;
+    const double m = fma(isR ? B : C, k2, fma(isR ? A : B, kv, r == cc ? 1.0 : 0.0));
+    // lanes 0..11: N(r, c) = sum_m R(r, m) T(m, c); lanes 12..14: t_r = sum_m V(r, m) upsilon_m
+    const bool nl = lane < 12, tl = lane >= 12 && lane < 15;
+    const int nr = nl ? (lane >> 2) : (tl ? lane - 12 : 0), nc = lane & 3;
+    const double m0 = __shfl_sync(full, m, (tl ? 9 : 0) + 3 * nr + 0);
+    const double m1 = __shfl_sync(full, m, (tl ? 9 : 0) + 3 * nr + 1);
+    const double m2 = __shfl_sync(full, m, (tl ? 9 : 0) + 3 * nr + 2);
+    const double o0 = nl ? Tin[nc] : xi[3], o1 = nl ? Tin[4 + nc] : xi[4], o2 = nl ? Tin[8 + nc] : xi[5];
+    double nv = fma(m0, o0, fma(m1, o1, m2 * o2));
+    const double tr = __shfl_sync(full, nv, 12 + (nr < 3 ? nr : 0));
+    if (nl && nc == 3) nv += tr;
+    if (nl) {
+        Tout[lane] = nv;
+        Tfout[lane] = (float)nv;
+    }
+    float n2 = 0.f;
+#pragma unroll
+    for (int k = 0; k < 6; k++) n2 = fmaf((float)xi[k], (float)xi[k], n2);
+    return n2;
+}
+
+}  // namespace ss
