@@ -94,7 +94,12 @@ __global__ void pose_prep_kernel(TrackState *st) {
 }
 
 // Accumulates this thread's share of one Gauss-Newton iteration at a level
-// into Kahan (sum, compensation) pairs.
+// into Kahan (sum, compensation) pairs. The thread's pixels are visited in
+// groups of kTrackGroup: all depth loads of a group, then all model-map loads,
+// then the sums, so the two dependent memory round trips of a pixel overlap
+// with those of the others (same pixel order as one at a time).
+constexpr int kTrackGroup = 4;
+
 __device__ __forceinline__ void track_accumulate(const uint16_t *__restrict__ depth, int rows, int cols, Intr in,
                                                  const float4 *__restrict__ vmap, const float4 *__restrict__ nmap,
                                                  const float *T, const float *Pi, int level, float dist2, float rmin,
@@ -102,56 +107,98 @@ __device__ __forceinline__ void track_accumulate(const uint16_t *__restrict__ de
     const int lr = (rows + (1 << level) - 1) >> level, lc = (cols + (1 << level) - 1) >> level;
     const int npix = lr * lc;
     const float rfx = 1.f / in.fx, rfy = 1.f / in.fy;
-    for (int p = tid; p < npix; p += nthreads) {
-        const int i = (p / lc) << level, j = (p % lc) << level;
-        const float d = (float)__ldg(depth + (size_t)i * cols + j) * 1e-3f;
-        if (!(d > rmin) || !(d < dmax)) continue;
-        const float cx = ((float)j - in.cj) * rfx * d, cy = ((float)i - in.ci) * rfy * d;
-        const float wx = fmaf(T[0], cx, fmaf(T[1], cy, fmaf(T[2], d, T[3])));
-        const float wy = fmaf(T[4], cx, fmaf(T[5], cy, fmaf(T[6], d, T[7])));
-        const float wz = fmaf(T[8], cx, fmaf(T[9], cy, fmaf(T[10], d, T[11])));
-        const float qx = fmaf(Pi[0], wx, fmaf(Pi[1], wy, fmaf(Pi[2], wz, Pi[3])));
-        const float qy = fmaf(Pi[4], wx, fmaf(Pi[5], wy, fmaf(Pi[6], wz, Pi[7])));
-        const float qz = fmaf(Pi[8], wx, fmaf(Pi[9], wy, fmaf(Pi[10], wz, Pi[11])));
-        if (!(qz > 1e-3f)) continue;
-        const float rq = 1.f / qz;
-        const int ii = (int)floorf(fmaf(qy * in.fy, rq, in.ci) + 0.5f);
-        const int jj = (int)floorf(fmaf(qx * in.fx, rq, in.cj) + 0.5f);
-        if (ii < 0 || ii >= rows || jj < 0 || jj >= cols) continue;
-        const float4 n = __ldg(nmap + (size_t)ii * cols + jj);
-        if (n.x == 0.f && n.y == 0.f && n.z == 0.f) continue;
-        const float4 v = __ldg(vmap + (size_t)ii * cols + jj);
-        const float ex = wx - v.x, ey = wy - v.y, ez = wz - v.z;
-        if (ex * ex + ey * ey + ez * ez > dist2) continue;
-        const float r = n.x * ex + n.y * ey + n.z * ez;
-        const float J[6] = {wy * n.z - wz * n.y, wz * n.x - wx * n.z, wx * n.y - wy * n.x, n.x, n.y, n.z};
-        int q = 0;
+    for (int base = tid; base < npix; base += kTrackGroup * nthreads) {
+        float d[kTrackGroup];
+        int pi[kTrackGroup], pj[kTrackGroup];
 #pragma unroll
-        for (int a = 0; a < 6; a++)
+        for (int g = 0; g < kTrackGroup; g++) {
+            const int p = base + g * nthreads;
+            pi[g] = (p / lc) << level;
+            pj[g] = (p % lc) << level;
+            d[g] = p < npix ? (float)__ldg(depth + (size_t)pi[g] * cols + pj[g]) * 1e-3f : 0.f;
+        }
+        float wv[kTrackGroup][3];
+        float4 n[kTrackGroup], v[kTrackGroup];
+        bool ok[kTrackGroup];
 #pragma unroll
-            for (int b = a; b < 6; b++) kahan_add(s[q], c[q], J[a] * J[b]), q++;
+        for (int g = 0; g < kTrackGroup; g++) {
+            const float dd = d[g];
+            const float cx = ((float)pj[g] - in.cj) * rfx * dd, cy = ((float)pi[g] - in.ci) * rfy * dd;
+            const float wx = fmaf(T[0], cx, fmaf(T[1], cy, fmaf(T[2], dd, T[3])));
+            const float wy = fmaf(T[4], cx, fmaf(T[5], cy, fmaf(T[6], dd, T[7])));
+            const float wz = fmaf(T[8], cx, fmaf(T[9], cy, fmaf(T[10], dd, T[11])));
+            const float qx = fmaf(Pi[0], wx, fmaf(Pi[1], wy, fmaf(Pi[2], wz, Pi[3])));
+            const float qy = fmaf(Pi[4], wx, fmaf(Pi[5], wy, fmaf(Pi[6], wz, Pi[7])));
+            const float qz = fmaf(Pi[8], wx, fmaf(Pi[9], wy, fmaf(Pi[10], wz, Pi[11])));
+            wv[g][0] = wx;
+            wv[g][1] = wy;
+            wv[g][2] = wz;
+            bool good = (dd > rmin) && (dd < dmax) && (qz > 1e-3f);
+            int ii = 0, jj = 0;
+            if (good) {
+                const float rq = 1.f / qz;
+                ii = (int)floorf(fmaf(qy * in.fy, rq, in.ci) + 0.5f);
+                jj = (int)floorf(fmaf(qx * in.fx, rq, in.cj) + 0.5f);
+                good = ii >= 0 && ii < rows && jj >= 0 && jj < cols;
+            }
+            ok[g] = good;
+            const size_t m = good ? (size_t)ii * cols + jj : 0;
+            n[g] = good ? __ldg(nmap + m) : make_float4(0.f, 0.f, 0.f, 0.f);
+            v[g] = good ? __ldg(vmap + m) : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
 #pragma unroll
-        for (int a = 0; a < 6; a++) kahan_add(s[21 + a], c[21 + a], J[a] * r);
-        kahan_add(s[27], c[27], r * r);
-        s[28] += 1.f;  // counts stay exact far below 2^24
+        for (int g = 0; g < kTrackGroup; g++) {
+            if (!ok[g]) continue;
+            const float4 nn = n[g], vv = v[g];
+            if (nn.x == 0.f && nn.y == 0.f && nn.z == 0.f) continue;
+            const float wx = wv[g][0], wy = wv[g][1], wz = wv[g][2];
+            const float ex = wx - vv.x, ey = wy - vv.y, ez = wz - vv.z;
+            if (ex * ex + ey * ey + ez * ez > dist2) continue;
+            const float r = nn.x * ex + nn.y * ey + nn.z * ez;
+            const float J[6] = {wy * nn.z - wz * nn.y, wz * nn.x - wx * nn.z, wx * nn.y - wy * nn.x, nn.x, nn.y, nn.z};
+            int q = 0;
+#pragma unroll
+            for (int a = 0; a < 6; a++)
+#pragma unroll
+                for (int b = a; b < 6; b++) kahan_add(s[q], c[q], J[a] * J[b]), q++;
+#pragma unroll
+            for (int a = 0; a < 6; a++) kahan_add(s[21 + a], c[21 + a], J[a] * r);
+            kahan_add(s[27], c[27], r * r);
+            s[28] += 1.f;  // counts stay exact far below 2^24
+        }
     }
 }
 
-// Reduces the CTA's pairs (warp shuffles with TwoSum, then shared memory)
-// and writes them to the value-major slots: slots[value][cta].
+// Reduces the CTA's pairs and writes them to the value-major slots:
+// slots[value][cta]. Within a warp, a transpose-reduce (recursive halving):
+// at offset o each lane keeps the half of its remaining values selected by
+// lane bit o and trades the other half with lane ^ o, adding with TwoSum, so
+// after offsets 16, 8, 4, 2, 1 lane l holds the warp's pair of value l (31
+// exchanges per lane instead of 5 per value). Warps then combine through
+// shared memory in a fixed order.
 __device__ __forceinline__ void track_cta_to_slots(float *s, float *c, float2 (*red)[kTrackSums],
                                                    float2 *__restrict__ slots) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    float vs[32], vc[32];
 #pragma unroll
-    for (int k = 0; k < kTrackSums; k++) {
-        float a = s[k], b = c[k];
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            const float a2 = __shfl_down_sync(0xffffffffu, a, o), b2 = __shfl_down_sync(0xffffffffu, b, o);
-            pair_add(a, b, a2, b2);
-        }
-        if (lane == 0) red[wid][k] = make_float2(a, b);
+    for (int k = 0; k < 32; k++) {
+        vs[k] = k < kTrackSums ? s[k] : 0.f;
+        vc[k] = k < kTrackSums ? c[k] : 0.f;
     }
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) {
+        const bool upper = (lane & o) != 0;
+#pragma unroll
+        for (int k = 0; k < o; k++) {
+            const float ss = upper ? vs[k] : vs[k + o], sc = upper ? vc[k] : vc[k + o];
+            float ks = upper ? vs[k + o] : vs[k], kc = upper ? vc[k + o] : vc[k];
+            const float rs = __shfl_xor_sync(0xffffffffu, ss, o), rc = __shfl_xor_sync(0xffffffffu, sc, o);
+            pair_add(ks, kc, rs, rc);
+            vs[k] = ks;
+            vc[k] = kc;
+        }
+    }
+    if (lane < kTrackSums) red[wid][lane] = make_float2(vs[0], vc[0]);
     __syncthreads();
     if (threadIdx.x < kTrackSums) {
         float a = 0.f, b = 0.f;
