@@ -265,12 +265,28 @@ int orm_grid_export(void *h, int max_blocks, uint64_t *keys, int32_t *coords, do
 
 // One march of the trilinear raycast from t0 (same step rules as the GPU
 // kernel, in double); returns true on a zero crossing with t = hit depth.
-static bool march64(const Grid64 &g, Cache &cache, double ox, double oy, double oz, double dx, double dy, double dz,
-                    double inv_len, double t0, double t_max, int max_steps, int &steps, double &t) {
+static double refine64(const Grid64 &g, Cache &cache, double ox, double oy, double oz, double dx, double dy,
+                       double dz, double ta, double fa, double tb, double fb) {
+    for (int r = 0; r < 2; r++) {
+        const double tc = ta + (tb - ta) * fa / (fa - fb);
+        const Sample q = trilinear64(g, ox + tc * dx, oy + tc * dy, oz + tc * dz, cache);
+        if (!q.valid) break;
+        if (q.f > 0) {
+            ta = tc;
+            fa = q.f;
+        } else {
+            tb = tc;
+            fb = q.f;
+        }
+    }
+    return ta + (tb - ta) * fa / (fa - fb);
+}
+
+static bool march64_from(const Grid64 &g, Cache &cache, double ox, double oy, double oz, double dx, double dy,
+                         double dz, double inv_len, double t0, double t_max, int max_steps, int &steps, double &t,
+                         bool prev_valid, double t_prev, double f_prev) {
     const double vl = g.vl, vbl = g.vbl, sbl = 8 * vbl;
     t = t0;
-    double t_prev = 0, f_prev = 0;
-    bool prev_valid = false;
     while (steps < max_steps && t < t_max) {
         const double px = ox + t * dx, py = oy + t * dy, pz = oz + t * dz;
         const int bx = (int)std::floor(px / vbl), by = (int)std::floor(py / vbl), bz = (int)std::floor(pz / vbl);
@@ -302,20 +318,7 @@ static bool march64(const Grid64 &g, Cache &cache, double ox, double oy, double 
         }
         if (sm.f < 0) {
             if (!(prev_valid && f_prev > 0)) return false;
-            double ta = t_prev, fa = f_prev, tb = t, fb = sm.f;
-            for (int r = 0; r < 2; r++) {
-                const double tc = ta + (tb - ta) * fa / (fa - fb);
-                const Sample q = trilinear64(g, ox + tc * dx, oy + tc * dy, oz + tc * dz, cache);
-                if (!q.valid) break;
-                if (q.f > 0) {
-                    ta = tc;
-                    fa = q.f;
-                } else {
-                    tb = tc;
-                    fb = q.f;
-                }
-            }
-            t = ta + (tb - ta) * fa / (fa - fb);
+            t = refine64(g, cache, ox, oy, oz, dx, dy, dz, t_prev, f_prev, t, sm.f);
             return true;
         }
         prev_valid = true;
@@ -326,12 +329,47 @@ static bool march64(const Grid64 &g, Cache &cache, double ox, double oy, double 
     return false;
 }
 
+static bool march64(const Grid64 &g, Cache &cache, double ox, double oy, double oz, double dx, double dy, double dz,
+                    double inv_len, double t0, double t_max, int max_steps, int &steps, double &t) {
+    return march64_from(g, cache, ox, oy, oz, dx, dy, dz, inv_len, t0, t_max, max_steps, steps, t, false, 0, 0);
+}
+
+// Search from a depth hint td within [t_lo, t_hi] (the GPU raycast's
+// ray_search, seek mode): unobserved at td: no hit; positive: forward to t_hi;
+// negative: back to a positive sample (unobserved or below t_lo: no hit).
+static bool seek64(const Grid64 &g, Cache &cache, double ox, double oy, double oz, double dx, double dy, double dz,
+                   double inv_len, double td, double t_lo, double t_hi, int max_steps, int &steps, double &t) {
+    const double vl = g.vl;
+    steps++;
+    const Sample s0 = trilinear64(g, ox + td * dx, oy + td * dy, oz + td * dz, cache);
+    if (!s0.valid) return false;
+    if (s0.f >= 0)
+        return march64_from(g, cache, ox, oy, oz, dx, dy, dz, inv_len, td + std::fmax(vl, 0.8 * s0.f) * inv_len, t_hi,
+                            max_steps, steps, t, true, td, s0.f);
+    double tb = td, fb = s0.f;
+    while (true) {
+        const double ta = tb - std::fmax(vl, -0.8 * fb) * inv_len;
+        if (ta < t_lo || !(steps < max_steps)) return false;
+        steps++;
+        const Sample s = trilinear64(g, ox + ta * dx, oy + ta * dy, oz + ta * dz, cache);
+        if (!s.valid) return false;
+        if (s.f > 0) {
+            t = refine64(g, cache, ox, oy, oz, dx, dy, dz, ta, s.f, tb, fb);
+            return true;
+        }
+        tb = ta;
+        fb = s.f;
+    }
+}
+
 // Trilinear raycast in double. vmap [rows][cols][4] = (x, y, z, depth), nmap
 // [rows][cols][4]; misses zero. hint (optional) is a u16-mm depth image at
-// this pose: a ray whose pixel has depth d searches [d - m, d + m]; a ray
-// without depth starts at the smallest depth of its 32-pixel row segment
-// minus m and marches on (m = hint_margin). steps_out (optional) receives the march
-// steps used per pixel.
+// this pose: a ray whose pixel has depth d searches [d - m, d + m] starting
+// at d (seek64: forward from a positive sample, back to a positive sample
+// from a negative one, no hit from an unobserved one); a ray without depth
+// takes as d the smaller depth of the nearest pixels with depth to its left
+// and right in its 32-pixel row segment (m = hint_margin). steps_out
+// (optional) receives the march steps used per pixel.
 void orm_raycast(void *h, const double *T, int max_steps, double t_min, double t_max, const uint16_t *hint,
                  double hint_margin, double *vmap, double *nmap, int *steps_out) {
     const Grid64 &g = *(Grid64 *)h;
@@ -348,22 +386,20 @@ void orm_raycast(void *h, const double *T, int max_steps, double t_min, double t
             int steps = 0;
             double t = t_min;
             bool hit;
-            // hint: own depth, else the smallest valid depth of the 32-pixel row segment
-            // (one GPU warp) holding this pixel
+            // hint: own depth, else the smaller depth of the nearest pixels with depth
+            // to the left and right within the 32-pixel row segment (one GPU warp)
             unsigned hmm = hint ? hint[pix] : 0u;
             if (hint && hmm == 0) {
                 const int j0 = j / 32 * 32, j1 = std::min(j0 + 32, g.resj);
-                unsigned m = 0xffffffffu;
-                for (int q = j0; q < j1; q++) {
-                    const unsigned v = hint[(size_t)i * g.resj + q];
-                    if (v && v < m) m = v;
-                }
-                hmm = m != 0xffffffffu ? m : 0u;
+                unsigned dl = 0, dr = 0;
+                for (int q = j - 1; q >= j0 && !dl; q--) dl = hint[(size_t)i * g.resj + q];
+                for (int q = j + 1; q < j1 && !dr; q++) dr = hint[(size_t)i * g.resj + q];
+                hmm = dl && dr ? std::min(dl, dr) : (dl ? dl : dr);
             }
             const double th = hint ? hmm * 1e-3 - hint_margin : 0.0;
             if (hint && th > t_min) {
-                const double t_end = hint[pix] ? std::fmin(t_max, th + 2 * hint_margin) : t_max;
-                hit = march64(g, cache, ox, oy, oz, dx, dy, dz, inv_len, th, t_end, max_steps, steps, t);
+                hit = seek64(g, cache, ox, oy, oz, dx, dy, dz, inv_len, th + hint_margin, th,
+                             std::fmin(t_max, th + 2 * hint_margin), max_steps, steps, t);
             } else {
                 hit = march64(g, cache, ox, oy, oz, dx, dy, dz, inv_len, t_min, t_max, max_steps, steps, t);
             }

@@ -197,13 +197,20 @@ __global__ void __launch_bounds__(256) raycast_ref_kernel(GridView g, Mat34 Er, 
 //    regula-falsi refinements on the bracket, then the hit;
 //  * the sample is negative with no positive predecessor: no hit (back face).
 // With a depth hint (the frame just fused at this pose, so the same rays), a
-// ray whose pixel has depth d searches only [d - margin, d + margin]; a pixel
-// without depth (dropout) starts at the smallest depth of its warp's 32-pixel
-// row segment minus margin and marches on as usual. Where the fused frame saw
-// d, a crossing outside that window contradicts the frame just fused (it
-// shows up at silhouettes, through gaps of the thin band the trilinear
-// validity test leaves there), so the window loses no consistent surface and
-// keeps every lane of a warp within a few steps of the others.
+// ray whose pixel has depth d searches only [d - margin, d + margin], and
+// starts at d: one sample there; in front of the surface (f >= 0) the march
+// goes on forward, behind it (f < 0) it steps back by max(vl, 0.8 |f|) until a
+// positive sample brackets the crossing (an unobserved sample, or leaving the
+// window, first: no hit); an unobserved sample at d (a gap of the band at a
+// silhouette) is no hit. A pixel without depth (dropout) takes as d the
+// smaller depth of the nearest pixels with depth to its left and right in its
+// warp's 32-pixel row segment. Where the fused frame saw d, a crossing
+// outside the window contradicts the frame just fused, so the window loses no
+// consistent surface; starting at d skips the unobserved voxels in front of
+// the band, which a plain march would cross one voxel at a time, and keeps
+// the lanes of a warp within a few steps of each other (marching the window
+// where the sample at d is unobserved recovers 0.3 % of the hits on the
+// synthetic room sequence at 2.3x the warp time).
 // Every sample or skip counts as one step. The normal is the normalised
 // gradient of the trilinear interpolant at the hit (world frame, pointing
 // out of the surface). Outputs: vmap[i][j] = (x, y, z world, depth) and
@@ -221,13 +228,18 @@ __global__ void __launch_bounds__(256) raycast_maps_kernel(GridView g, Mat34 T, 
     int steps = 0;
     bool hit = false;
     // Depth hint of this ray: the fused frame's depth at this pixel, or, where
-    // that is missing (dropout), the smallest depth of the 32 pixels of this
-    // warp's row segment, so that no lane of the warp marches the whole ray.
+    // that is missing (dropout), the smaller depth of the nearest pixels with
+    // depth to its left and right within this warp's 32-pixel row segment.
     unsigned hint_mm = 0;
     if (hint) {
+        const unsigned full = 0xffffffffu;
+        const int lane = threadIdx.x & 31;
         const unsigned own = inside ? (unsigned)__ldg(hint + (size_t)i * g.resj + j) : 0u;
-        const unsigned wmin = __reduce_min_sync(0xffffffffu, own ? own : 0xffffffffu);
-        hint_mm = own ? own : (wmin != 0xffffffffu ? wmin : 0u);
+        const unsigned have = __ballot_sync(full, own != 0u);
+        const unsigned left = have & ((1u << lane) - 1u), right = lane < 31 ? have & (full << (lane + 1)) : 0u;
+        const int li = left ? 31 - __clz(left) : lane, ri = right ? __ffs(right) - 1 : lane;
+        const unsigned dl = __shfl_sync(full, own, li), dr = __shfl_sync(full, own, ri);
+        hint_mm = own ? own : (left && right ? min(dl, dr) : (left ? dl : (right ? dr : 0u)));
     }
     if (inside) {
     if (pose) {
@@ -245,11 +257,9 @@ __global__ void __launch_bounds__(256) raycast_maps_kernel(GridView g, Mat34 T, 
     float t = t_min;
     const float t_hint = (float)hint_mm * 1e-3f - hint_margin;
     if (hint && t_hint > t_min) {
-        // a pixel with its own depth d searches [d - margin, d + margin]; a
-        // dropout pixel starts at its warp's smallest depth and marches on
-        const bool own = __ldg(hint + (size_t)i * g.resj + j) != 0;
-        const float t_end = own ? fminf(t_max, t_hint + 2.f * hint_margin) : t_max;
-        hit = march<kStorage>(g, ox, oy, oz, dx, dy, dz, inv_len, t_hint, t_end, max_steps, steps, t, cache);
+        // seek from the hint d within [d - margin, d + margin]
+        hit = ray_search<kStorage>(g, ox, oy, oz, dx, dy, dz, inv_len, kRaySeek, t_hint + hint_margin, t_hint,
+                                   fminf(t_max, t_hint + 2.f * hint_margin), max_steps, steps, t, cache);
     } else {
         hit = march<kStorage>(g, ox, oy, oz, dx, dy, dz, inv_len, t_min, t_max, max_steps, steps, t, cache);
     }

@@ -42,6 +42,12 @@ __device__ __forceinline__ int cached_lookup(const GridView &g, BlockCache &c, i
     return c.bucket;
 }
 
+// Uncached find of a neighbouring block (counted as a lookup).
+__device__ __forceinline__ int block_find(const GridView &g, BlockCache &c, int bx, int by, int bz) {
+    c.lookups++;
+    return packable(bx, by, bz) ? table_find(g, prime_hash(bx, by, bz)) : -1;
+}
+
 template <int kStorage, bool kGrad>
 __device__ __forceinline__ TriSample trilinear(const GridView &g, float px, float py, float pz, float inv_vl,
                                                BlockCache &c) {
@@ -68,17 +74,38 @@ __device__ __forceinline__ TriSample trilinear(const GridView &g, float px, floa
         }
         if (!ok) return r;
     } else {
+        // the cell straddles block faces: each distinct block is looked up once
+        // (corner (a, b, c) lies in block offset (a sx, b sy, c sz))
+        const int bx0 = ix >> 3, by0 = iy >> 3, bz0 = iz >> 3;
+        const bool sx = (ix & 7) == 7, sy = (iy & 7) == 7, sz = (iz & 7) == 7;
+        int bk[8];
+        bk[0] = cached_lookup(g, c, bx0, by0, bz0);
+        if (bk[0] < 0) return r;
+        bk[1] = sx ? block_find(g, c, bx0 + 1, by0, bz0) : bk[0];
+        bk[2] = sy ? block_find(g, c, bx0, by0 + 1, bz0) : bk[0];
+        bk[4] = sz ? block_find(g, c, bx0, by0, bz0 + 1) : bk[0];
+        bk[3] = (sx && sy) ? block_find(g, c, bx0 + 1, by0 + 1, bz0) : (sx ? bk[1] : bk[2]);
+        bk[5] = (sx && sz) ? block_find(g, c, bx0 + 1, by0, bz0 + 1) : (sx ? bk[1] : bk[4]);
+        bk[6] = (sy && sz) ? block_find(g, c, bx0, by0 + 1, bz0 + 1) : (sy ? bk[2] : bk[4]);
+        bk[7] = (sx && sy && sz) ? block_find(g, c, bx0 + 1, by0 + 1, bz0 + 1)
+                                 : (sx && sy ? bk[3] : (sx && sz ? bk[5] : (sy && sz ? bk[6] : (sx ? bk[1] : (sy ? bk[2] : bk[4])))));
+        bool ok = true;
+#pragma unroll
+        for (int k = 0; k < 8; k++) ok &= bk[k] >= 0;
+        if (!ok) return r;
+        float2 sw[8];
 #pragma unroll
         for (int k = 0; k < 8; k++) {
             const int vx = ix + (k & 1), vy = iy + ((k >> 1) & 1), vz = iz + (k >> 2);
-            const int bx = vx >> 3, by = vy >> 3, bz = vz >> 3;  // floor(v / 8)
-            const int b = cached_lookup(g, c, bx, by, bz);
-            if (b < 0) return r;
-            const float2 sw = voxel_sw<kStorage>(g, b, (vx & 7) + 8 * (vy & 7) + 64 * (vz & 7));
-            c.voxels++;
-            if (!(sw.y > 0.f)) return r;
-            s[k] = sw.x;
+            sw[k] = voxel_sw<kStorage>(g, bk[k], (vx & 7) + 8 * (vy & 7) + 64 * (vz & 7));
         }
+        c.voxels += 8;
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            ok &= sw[k].y > 0.f;
+            s[k] = sw[k].x;
+        }
+        if (!ok) return r;
     }
     // lerp along x, then y, then z
     const float s00 = fmaf(ax, s[1] - s[0], s[0]), s10 = fmaf(ax, s[3] - s[2], s[2]);
@@ -96,82 +123,148 @@ __device__ __forceinline__ TriSample trilinear(const GridView &g, float px, floa
     return r;
 }
 
-// One ray march from t0; returns true on a zero crossing (t = hit depth).
+// Regula falsi on a bracket (ta, fa > 0) .. (tb, fb < 0) of the trilinear
+// field along the ray: two refinements, then the secant root.
 template <int kStorage>
-__device__ __forceinline__ bool march(const GridView &g, float ox, float oy, float oz, float dx, float dy, float dz,
-                                      float inv_len, float t0, float t_max, int max_steps, int &steps, float &t,
-                                      BlockCache &cache) {
+__device__ __forceinline__ float refine_crossing(const GridView &g, float ox, float oy, float oz, float dx, float dy,
+                                                 float dz, float ta, float fa, float tb, float fb, BlockCache &cache) {
+    const float inv_vl = 1.f / g.vl;
+    for (int r = 0; r < 2; r++) {
+        const float tc = ta + (tb - ta) * fa / (fa - fb);
+        const TriSample q =
+            trilinear<kStorage, false>(g, fmaf(tc, dx, ox), fmaf(tc, dy, oy), fmaf(tc, dz, oz), inv_vl, cache);
+        if (!q.valid) break;
+        if (q.f > 0.f) {
+            ta = tc;
+            fa = q.f;
+        } else {
+            tb = tc;
+            fb = q.f;
+        }
+    }
+    return ta + (tb - ta) * fa / (fa - fb);
+}
+
+constexpr int kRayForward = 0;  // march forward from t0 to t_hi
+constexpr int kRaySeek = 1;     // search near a depth hint t0 within [t_lo, t_hi]
+
+// Ray search, one loop with one trilinear sample per iteration for every
+// mode, so lanes of a warp in different modes still share the sampling code:
+//  forward: in a super-block without allocated blocks, or a block that is not
+//    allocated, jump to the exit of its box; an invalid sample (unobserved
+//    corner) advances one voxel; a positive one advances max(vl, 0.8 f); a
+//    negative one after a positive one brackets the crossing, a negative one
+//    without a positive predecessor is a back face (no hit);
+//  seek (window [t_lo, t_hi]): one sample at the hint t0; unobserved: no
+//    hit; positive: forward from there to t_hi (that sample is the
+//    predecessor); negative:
+//  back: steps back by max(vl, 0.8 |f|) until a positive sample brackets the
+//    crossing (an unobserved sample, or passing t_lo, first: no hit).
+// Forward marching ends at t_hi. Every sample or skip counts as one step. A
+// bracket is refined by two regula-falsi steps, then the secant root is the
+// hit (t).
+template <int kStorage>
+__device__ __forceinline__ bool ray_search(const GridView &g, float ox, float oy, float oz, float dx, float dy,
+                                           float dz, float inv_len, int mode, float t0, float t_lo, float t_hi,
+                                           int max_steps, int &steps, float &t, BlockCache &cache) {
+    constexpr int kBack = 2;
     const float vl = g.vl, inv_vl = 1.f / g.vl, inv_vbl = 1.f / g.vbl;
     const float rdx = 1.f / dx, rdy = 1.f / dy, rdz = 1.f / dz;
     const float sbl = g.vbl * (float)(1 << kSuperShift);
     t = t0;
-    float t_prev = 0.f, f_prev = 0.f;
-    bool prev_valid = false;
+    bool prev_valid = false, found = false;
+    float t_prev = 0.f, f_prev = 0.f;  // forward: last valid sample; back: last (negative) sample
+    float ta = 0.f, fa = 0.f, tb = 0.f, fb = 0.f;  // bracket: f(ta) > 0 > f(tb)
     int csx = INT_MIN, csy = INT_MIN, csz = INT_MIN;
     bool cocc = false;
-    while (steps < max_steps && t < t_max) {
+    while (steps < max_steps) {
+        if (mode == kRayForward && !(t < t_hi)) break;
         const float px = fmaf(t, dx, ox), py = fmaf(t, dy, oy), pz = fmaf(t, dz, oz);
-        const int bx = (int)floorf(px * inv_vbl), by = (int)floorf(py * inv_vbl), bz = (int)floorf(pz * inv_vbl);
         steps++;
-        const int sx = bx >> kSuperShift, sy = by >> kSuperShift, sz = bz >> kSuperShift;
-        if (sx != csx || sy != csy || sz != csz) {
-            csx = sx;
-            csy = sy;
-            csz = sz;
-            cocc = super_occupied(g, sx, sy, sz);
-            cache.lookups++;
-        }
-        if (!cocc) {  // exit of this empty super-block's box along the ray
-            const float ex = ((float)(sx + (dx > 0.f)) * sbl - ox) * rdx;
-            const float ey = ((float)(sy + (dy > 0.f)) * sbl - oy) * rdy;
-            const float ez = ((float)(sz + (dz > 0.f)) * sbl - oz) * rdz;
-            const float te = fminf(fminf(dx != 0.f ? ex : INFINITY, dy != 0.f ? ey : INFINITY),
-                                   dz != 0.f ? ez : INFINITY);
-            t = fmaxf(te, t) + 1e-4f * vl * inv_len;
-            prev_valid = false;
-            continue;
-        }
-        if (cached_lookup(g, cache, bx, by, bz) < 0) {  // exit of this empty block's box
-            const float ex = ((float)(bx + (dx > 0.f)) * g.vbl - ox) * rdx;
-            const float ey = ((float)(by + (dy > 0.f)) * g.vbl - oy) * rdy;
-            const float ez = ((float)(bz + (dz > 0.f)) * g.vbl - oz) * rdz;
-            const float te = fminf(fminf(dx != 0.f ? ex : INFINITY, dy != 0.f ? ey : INFINITY),
-                                   dz != 0.f ? ez : INFINITY);
-            t = fmaxf(te, t) + 1e-4f * vl * inv_len;
-            prev_valid = false;
-            continue;
+        if (mode == kRayForward) {
+            const int bx = (int)floorf(px * inv_vbl), by = (int)floorf(py * inv_vbl), bz = (int)floorf(pz * inv_vbl);
+            const int sx = bx >> kSuperShift, sy = by >> kSuperShift, sz = bz >> kSuperShift;
+            if (sx != csx || sy != csy || sz != csz) {
+                csx = sx;
+                csy = sy;
+                csz = sz;
+                cocc = super_occupied(g, sx, sy, sz);
+                cache.lookups++;
+            }
+            const bool empty_super = !cocc;
+            if (empty_super || cached_lookup(g, cache, bx, by, bz) < 0) {
+                // exit of the empty super-block's (or block's) box along the ray
+                const float box = empty_super ? sbl : g.vbl;
+                const int cx = empty_super ? sx : bx, cy = empty_super ? sy : by, cz = empty_super ? sz : bz;
+                const float ex = ((float)(cx + (dx > 0.f)) * box - ox) * rdx;
+                const float ey = ((float)(cy + (dy > 0.f)) * box - oy) * rdy;
+                const float ez = ((float)(cz + (dz > 0.f)) * box - oz) * rdz;
+                const float te = fminf(fminf(dx != 0.f ? ex : INFINITY, dy != 0.f ? ey : INFINITY),
+                                       dz != 0.f ? ez : INFINITY);
+                t = fmaxf(te, t) + 1e-4f * vl * inv_len;
+                prev_valid = false;
+                continue;
+            }
         }
         const TriSample sm = trilinear<kStorage, false>(g, px, py, pz, inv_vl, cache);
-        if (!sm.valid) {
-            prev_valid = false;
-            t += vl * inv_len;
-            continue;
-        }
-        if (sm.f < 0.f) {
-            if (!(prev_valid && f_prev > 0.f)) return false;  // back face
-            float ta = t_prev, fa = f_prev, tb = t, fb = sm.f;
-            for (int r = 0; r < 2; r++) {
-                const float tc = ta + (tb - ta) * fa / (fa - fb);
-                const TriSample q = trilinear<kStorage, false>(g, fmaf(tc, dx, ox), fmaf(tc, dy, oy),
-                                                               fmaf(tc, dz, oz), inv_vl, cache);
-                if (!q.valid) break;
-                if (q.f > 0.f) {
-                    ta = tc;
-                    fa = q.f;
-                } else {
-                    tb = tc;
-                    fb = q.f;
-                }
+        if (mode == kRayForward) {
+            if (!sm.valid) {
+                prev_valid = false;
+                t += vl * inv_len;
+                continue;
             }
-            t = ta + (tb - ta) * fa / (fa - fb);
-            return true;
+            if (sm.f < 0.f) {
+                found = prev_valid && f_prev > 0.f;  // else a back face
+                ta = t_prev;
+                fa = f_prev;
+                tb = t;
+                fb = sm.f;
+                break;
+            }
+            prev_valid = true;
+            t_prev = t;
+            f_prev = sm.f;
+            t += fmaxf(vl, 0.8f * sm.f) * inv_len;
+        } else if (mode == kRaySeek) {
+            if (!sm.valid) break;  // unobserved at the hint (a gap in the band): no hit
+            t_prev = t;
+            f_prev = sm.f;
+            if (sm.f >= 0.f) {
+                mode = kRayForward;
+                prev_valid = true;
+                t += fmaxf(vl, 0.8f * sm.f) * inv_len;
+            } else {
+                mode = kBack;
+                t -= fmaxf(vl, -0.8f * sm.f) * inv_len;
+                if (t < t_lo) break;
+            }
+        } else {  // back
+            if (sm.valid && sm.f > 0.f) {
+                found = true;
+                ta = t;
+                fa = sm.f;
+                tb = t_prev;
+                fb = f_prev;
+                break;
+            }
+            if (!sm.valid) break;
+            t_prev = t;
+            f_prev = sm.f;
+            t -= fmaxf(vl, -0.8f * sm.f) * inv_len;
+            if (t < t_lo) break;
         }
-        prev_valid = true;
-        t_prev = t;
-        f_prev = sm.f;
-        t += fmaxf(vl, 0.8f * sm.f) * inv_len;
     }
-    return false;
+    if (found) t = refine_crossing<kStorage>(g, ox, oy, oz, dx, dy, dz, ta, fa, tb, fb, cache);
+    return found;
+}
+
+// One forward ray march from t0 to t_max; returns true on a zero crossing (t = hit depth).
+template <int kStorage>
+__device__ __forceinline__ bool march(const GridView &g, float ox, float oy, float oz, float dx, float dy, float dz,
+                                      float inv_len, float t0, float t_max, int max_steps, int &steps, float &t,
+                                      BlockCache &cache) {
+    return ray_search<kStorage>(g, ox, oy, oz, dx, dy, dz, inv_len, kRayForward, t0, t0, t_max, max_steps, steps, t,
+                                cache);
 }
 
 }  // namespace ss
