@@ -209,8 +209,10 @@ __device__ __forceinline__ void track_cta_to_slots(float *s, float *c, float2 (*
 
 // Reduces all CTA slots into (sum, compensation) pairs, TwoSum in FP32 in a
 // fixed order: warp w takes values w, w + 8, w + 16, w + 24 (256 threads), each
-// lane a strided share of the CTAs; all loads of a chunk are issued before its
-// additions.
+// lane a strided share of the CTAs. The loads of up to kSlotChunks x 32 CTAs
+// are all issued before the first addition (one L2 round trip).
+constexpr int kSlotChunks = 8;
+
 __device__ __forceinline__ void track_slots_to_pairs(const float2 *__restrict__ slots, float2 *tot) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     constexpr int kPer = (kTrackSums + 7) / 8;
@@ -218,16 +220,21 @@ __device__ __forceinline__ void track_slots_to_pairs(const float2 *__restrict__ 
     float a[kPer], b[kPer];
 #pragma unroll
     for (int u = 0; u < kPer; u++) a[u] = b[u] = 0.f;
-#pragma unroll 2
-    for (unsigned q = lane; q < n; q += 32) {
-        float2 p[kPer];
+    for (unsigned q0 = 0; q0 < n; q0 += 32u * kSlotChunks) {
+        float2 p[kSlotChunks][kPer];
 #pragma unroll
-        for (int u = 0; u < kPer; u++) {
-            const int v = wid + 8 * u;
-            p[u] = v < kTrackSums ? __ldcg(slots + (size_t)v * n + q) : make_float2(0.f, 0.f);
+        for (int ch = 0; ch < kSlotChunks; ch++) {
+            const unsigned q = q0 + lane + 32u * ch;
+#pragma unroll
+            for (int u = 0; u < kPer; u++) {
+                const int v = wid + 8 * u;
+                p[ch][u] = (q < n && v < kTrackSums) ? __ldcg(slots + (size_t)v * n + q) : make_float2(0.f, 0.f);
+            }
         }
 #pragma unroll
-        for (int u = 0; u < kPer; u++) pair_add(a[u], b[u], p[u].x, p[u].y);
+        for (int ch = 0; ch < kSlotChunks; ch++)
+#pragma unroll
+            for (int u = 0; u < kPer; u++) pair_add(a[u], b[u], p[ch][u].x, p[ch][u].y);
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -333,10 +340,23 @@ __device__ unsigned long long g_track_timing[32 * 6];
     } while (0)
 #endif
 
-// All Gauss-Newton iterations of one frame in one cooperative launch. Every
-// CTA reduces all CTA slots and solves redundantly (bit-identical results in
+// Rigid inverse of T (FP64) as floats by one warp: lanes 0..11 write Ti[lane].
+__device__ __forceinline__ void warp_rigid_inverse_f(const double *T, float *Ti) {
+    const int lane = threadIdx.x & 31;
+    if (lane < 12) {
+        const int r = lane >> 2, c = lane & 3;
+        Ti[lane] = c < 3 ? (float)T[c * 4 + r] : (float)(-(T[r] * T[3] + T[4 + r] * T[7] + T[8 + r] * T[11]));
+    }
+}
+
+// All Gauss-Newton iterations of one frame in one cooperative launch, with
+// the frame's start (model pose = current pose, its inverse) and end (the
+// FramePose of the result for integrate and raycast) folded in. Every CTA
+// reduces all CTA slots and solves redundantly (bit-identical results in
 // every CTA), so one grid barrier per iteration suffices; the slots are double
 // buffered so a CTA that runs ahead never overwrites slots still being read.
+// Every CTA leaves through the same exit, also after a barrier timeout; the
+// last one to leave zeroes the barrier counter for the next frame.
 __global__ void __launch_bounds__(256) track_frame_kernel(const uint16_t *__restrict__ depth, int rows, int cols,
                                                           Intr in, const float4 *__restrict__ vmap,
                                                           const float4 *__restrict__ nmap, TrackState *st,
@@ -347,15 +367,26 @@ __global__ void __launch_bounds__(256) track_frame_kernel(const uint16_t *__rest
     __shared__ float Tf[12], Pi[12];
     __shared__ int done_level;
     if (threadIdx.x < 16) Td[threadIdx.x] = st->T[threadIdx.x];
-    if (threadIdx.x < 12) {
-        Tf[threadIdx.x] = st->Tf[threadIdx.x];
-        Pi[threadIdx.x] = st->Tprev_inv[threadIdx.x];
-    }
     if (threadIdx.x == 0) done_level = -1;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        // the model maps were raycast at the current pose: Tprev = T
+        warp_rigid_inverse_f(Td, Pi);
+        if (threadIdx.x < 12) Tf[threadIdx.x] = (float)Td[threadIdx.x];
+        if (blockIdx.x == 0) {
+            if (threadIdx.x < 16) st->Tprev[threadIdx.x] = Td[threadIdx.x];
+            if (threadIdx.x < 12) st->Tprev_inv[threadIdx.x] = Pi[threadIdx.x];
+            if (threadIdx.x < kMaxLevels) {
+                st->inliers[threadIdx.x] = 0;
+                st->rmse[threadIdx.x] = 0.f;
+            }
+        }
+    }
     __syncthreads();
     unsigned barriers = 0;
     int parity = 0;
-    for (int level = L.levels - 1; level >= 0; level--) {
+    bool alive = true;
+    for (int level = L.levels - 1; level >= 0 && alive; level--) {
         const float dist2 = L.dist[level] * L.dist[level];
         for (int it = 0; it < L.iters[level]; it++) {
             if (done_level == level) break;  // converged: identical decision in every CTA
@@ -375,7 +406,10 @@ __global__ void __launch_bounds__(256) track_frame_kernel(const uint16_t *__rest
             float2 *buf = slots + (size_t)parity * kTrackSums * gridDim.x;
             track_cta_to_slots(s, c, red, buf);
             SS_TT(barriers, 2);
-            if (!grid_barrier(st, (++barriers) * gridDim.x)) return;
+            if (!grid_barrier(st, (++barriers) * gridDim.x)) {
+                alive = false;
+                break;
+            }
             SS_TT(barriers - 1, 3);
             track_slots_to_pairs(buf, tot);
             __syncthreads();
@@ -396,9 +430,31 @@ __global__ void __launch_bounds__(256) track_frame_kernel(const uint16_t *__rest
             parity ^= 1;
         }
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        for (int k = 0; k < 16; k++) st->T[k] = Td[k];
-        for (int k = 0; k < 12; k++) st->Tf[k] = Tf[k];
+    if (blockIdx.x == 0 && threadIdx.x < 32) {
+        // the result and its FramePose (float pose, float inverse, unit z column)
+        const int lane = threadIdx.x;
+        if (lane < 16) st->T[lane] = Td[lane];
+        if (lane < 12) {
+            st->Tf[lane] = Tf[lane];
+            st->pose.E.m[lane] = (float)Td[lane];
+        }
+        warp_rigid_inverse_f(Td, st->pose.Einv.m);
+        const float ex = (float)Td[2], ey = (float)Td[6], ez = (float)Td[10];
+        const float len = sqrtf(ex * ex + ey * ey + ez * ez);
+        if (lane == 0) {
+            st->pose.Ez[0] = ex / len;
+            st->pose.Ez[1] = ey / len;
+            st->pose.Ez[2] = ez / len;
+            st->pose.pad = 0.f;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(&st->exits, 1u) == gridDim.x - 1) {
+            st->barrier = 0u;
+            st->exits = 0u;
+        }
     }
 }
 
@@ -418,11 +474,10 @@ int persistent_track_ctas(int num_sms, int want_per_sm) {
     return num_sms * (per_sm < 1 ? 1 : per_sm);
 }
 
-// Host-side launch of one frame's tracking: begin, levels coarse to fine,
-// then the FramePose of the result.
+// Host-side launch of one frame's tracking: one cooperative launch, or begin,
+// one launch per iteration (levels coarse to fine), then the FramePose of the
+// result.
 ss_status launch_track(const TrackLaunch &L, cudaStream_t s) {
-    track_begin_kernel<<<1, 32, 0, s>>>(L.state);
-    SS_LAUNCH_CHECK();
     if (L.persistent) {
         const uint16_t *depth = L.depth;
         int rows = L.rows, cols = L.cols;
@@ -443,10 +498,10 @@ ss_status launch_track(const TrackLaunch &L, cudaStream_t s) {
         cfg.attrs = attr;
         cfg.numAttrs = 1;
         SS_CUDA_TRY(cudaLaunchKernelEx(&cfg, track_frame_kernel, depth, rows, cols, in, vmap, nmap, st, slots, L));
-        pose_prep_kernel<<<1, 32, 0, s>>>(L.state);
-        SS_LAUNCH_CHECK();
         return SS_OK;
     }
+    track_begin_kernel<<<1, 32, 0, s>>>(L.state);
+    SS_LAUNCH_CHECK();
     for (int level = L.levels - 1; level >= 0; level--) {
         for (int it = 0; it < L.iters[level]; it++) {
             track_iter_kernel<<<L.ctas, 256, 0, s>>>(L.depth, L.rows, L.cols, L.in, L.vmap, L.nmap, L.state, L.partials,

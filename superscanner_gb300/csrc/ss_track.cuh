@@ -20,8 +20,9 @@ struct TrackState {
     int converged_level;
     int inliers[kMaxLevels];
     float rmse[kMaxLevels];
-    unsigned int barrier;  // arrivals at the persistent tracker's grid barrier (zeroed per frame)
+    unsigned int barrier;  // arrivals at the persistent tracker's grid barrier (0 between frames)
     int status;            // kSt* bits of the persistent tracker
+    unsigned int exits;    // CTAs of the persistent tracker that have left (the last resets both counters)
 };
 
 struct TrackLaunch {

@@ -5,18 +5,20 @@
 // pipe for ~64 cycles whether one lane or 32 are active, so a one-thread solve
 // costs ~64 cycles per FP64 operation (~140 operations for a Cholesky solve
 // with square roots, ~130 more for the SE(3) exponential and pose product).
-// Here every lane owns one entry, so each step of the factorisation, the back
-// substitution and the pose update is one or two warp instructions, and no
-// square root is taken:
+// Here every lane owns one entry, so each step of the elimination and of the
+// pose update is one or two warp instructions, and no square root is taken:
 //
-// * elimination: symmetric Gaussian elimination without pivoting on the
-//   augmented upper triangle [A | b] (27 lanes), i.e. the square-root-free
-//   (LDL^T) form of Cholesky. Each step updates the trailing rows in
-//   fraction-free form, a_ij <- p' a_ij - a_ki (a_kj 2^-e), with the pivot
-//   p = p' 2^e split exactly into p' in [1, 2) and a power of two by integer
-//   operations: the same rows as LDL^T, each scaled by a factor in [1, 2), so
-//   no division sits on the elimination's critical path;
-// * back substitution with the reciprocals of the six pivots, computed
+// * elimination: Gauss-Jordan elimination without pivoting on the augmented
+//   upper triangle [A | b] (27 lanes). The pivots are those of the
+//   square-root-free (LDL^T) form of Cholesky (row k of the trailing matrix
+//   is updated exactly as in LDL^T, and the trailing matrix stays symmetric,
+//   so a_ik = a_ki serves the rows below the pivot); the rows above the pivot
+//   are cleared too, so no back substitution is needed. Each step updates
+//   every other row in fraction-free form, a_ij <- p' a_ij - a_ik (a_kj 2^-e),
+//   with the pivot p = p' 2^e split exactly into p' in [1, 2) and a power of
+//   two by integer operations: each row is scaled by a factor in [1, 2) per
+//   step, and no division sits on the elimination's critical path;
+// * x_i = c_i / u_ii with the reciprocals of the six pivots computed
 //   together: an FP32 seed refined by two Newton-Raphson steps in FP64
 //   (r <- r + r (1 - m r); the relative error squares each step, 2^-23 ->
 //   2^-46 -> below FP64 rounding);
@@ -95,36 +97,27 @@ __device__ __forceinline__ bool warp_solve6(const float2 *pairs, double x[6]) {
     }
     bool ok = true;
 #pragma unroll
-    for (int k = 0; k < 5; k++) {
+    for (int k = 0; k < 6; k++) {
         const double p = __shfl_sync(full, a, aug_lane(k, k));
         ok = ok && (p > kPivotMin);
         int e;
         const double ph = split_pow2(p, e);
-        const bool upd = live && i > k;
+        const bool upd = live && i != k;
         const double ahat = (live && i == k) ? scale_pow2(a, e) : a;  // row k times 2^-e
-        const double aki = __shfl_sync(full, a, upd ? aug_lane(k, i) : 0);
-        const double akj = __shfl_sync(full, ahat, upd ? aug_lane(k, j) : 0);
-        if (upd) a = fma(ph, a, -(aki * akj));
+        // a_ik of this lane's row (upper triangle: (i, k) above the pivot, (k, i) below)
+        const double aik = __shfl_sync(full, a, !upd ? 0 : (i < k ? aug_lane(i, k) : aug_lane(k, i)));
+        // a_kj 2^-e of this lane's column (columns left of the pivot are cleared: 0)
+        const double akj = __shfl_sync(full, ahat, (upd && j >= k) ? aug_lane(k, j) : 0);
+        if (upd) a = fma(ph, a, -(aik * (j >= k ? akj : 0.0)));
     }
-    ok = ok && (__shfl_sync(full, a, aug_lane(5, 5)) > kPivotMin);
-    // reciprocals of the six pivots (diagonal lanes), then back substitution on lanes (i, 6)
+    // row i is now u_ii x_i = c_i: reciprocals on the diagonal lanes, x_i on lanes (i, 6)
     const bool diag = live && i == j;
     const double r = rcp_pos(diag && a > kPivotMin ? a : 1.0);
     const bool rhs = live && j == 6;
-    double u[6];
-#pragma unroll
-    for (int k = 0; k < 6; k++) {
-        const bool mine = rhs && k > i;
-        const double v = __shfl_sync(full, a, mine ? aug_lane(i, k) : 0);
-        u[k] = mine ? v : 0.0;
-    }
     const double rii = __shfl_sync(full, r, rhs ? aug_lane(i, i) : 0);
-    double c = a;
+    const double xl = a * rii;
 #pragma unroll
-    for (int k = 5; k >= 0; k--) {
-        x[k] = __shfl_sync(full, c * rii, aug_lane(k, 6));
-        c = fma(-u[k], x[k], c);
-    }
+    for (int k = 0; k < 6; k++) x[k] = __shfl_sync(full, xl, aug_lane(k, 6));
     return ok;
 }
 
