@@ -40,15 +40,16 @@ VL, TRUNC = 0.004, 0.016
 BUCKETS = 1 << 20
 MAX_WEIGHT = 255.0
 STEPS_CAP = 128
-HINT_MARGIN = 0.04  # model-view rays start 40 mm before the just-fused frame's depth (full march as fallback)
+HINT_MARGIN = 0.04  # model-view rays search within 40 mm of the just-fused frame's depth
 ITERS = (10, 5, 4)
 SCENE_SEED, TRAJ_SEED, NOISE_SEED = 1234, 42, 7
 METRIC = "frames/s 640x480@4mm, chosen vs plain form at <=1mm depth err; % HBM peak"
 WORKLOAD = ("synthetic 4x4x3 m room, 40 primitives, 640x480 noisy uint16 depth (sigma 1.2 mm + 1.9 mm (z-0.4)^2, "
             "5% dropout), 4 mm voxels, trunc 16 mm, 2^20 buckets, max weight 255; per frame: 3-level "
-            "point-to-plane ICP (10/5/4 it) -> integrate -> trilinear raycast (<=128 steps, started 40 mm before the "
-            "fused frame's depth)")
-KERNELS_PER_FRAME = 1 + sum(ITERS) + 1 + 3 + 1  # track begin, GN iterations, pose prep, collect/fuse/finalize, raycast
+            "point-to-plane ICP (10/5/4 it) -> integrate -> trilinear raycast (<=128 steps, searched within 40 mm of "
+            "the fused frame's depth)")
+# kernels per frame of the chosen form: the cooperative tracker (all GN iterations), collect/fuse/finalize, raycast
+KERNELS_PER_FRAME = 1 + 3 + 1
 
 
 def parse():
@@ -58,6 +59,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-error-check", action="store_true")
+    ap.add_argument("--precision-frames", type=int, default=20,
+                    help="frames of the perturbed-start precision comparison against the FP64 oracle (0: skip)")
     ap.add_argument("--buckets", type=int, default=BUCKETS,
                     help="hash buckets (profiler captures use a smaller table to keep device memory small)")
     ap.add_argument("--only", choices=["all", "chosen"], default="all",
@@ -295,6 +298,105 @@ def run_refusion(torch, depth, P, stream, n_kf: int = 200, launch=None):
     return res
 
 
+def rand_perturb(rng, max_deg=5.0, max_m=0.05):
+    """Seeded SE(3) perturbation: rotation about a uniformly random axis by an
+    angle ~ U(0, max_deg), translation along a uniformly random direction by a
+    length ~ U(0, max_m)."""
+    from superscanner_gb300.raydiff import se3_exp
+    ax = rng.normal(size=3)
+    ax /= np.linalg.norm(ax)
+    d = rng.normal(size=3)
+    d /= np.linalg.norm(d)
+    return se3_exp(np.concatenate([ax * np.deg2rad(rng.uniform(0, max_deg)), d * rng.uniform(0, max_m)]))
+
+
+def pose_delta(T, R):
+    """(translation mm, rotation deg) of T relative to R."""
+    d = np.linalg.inv(R) @ T
+    return (float(np.linalg.norm(d[:3, 3]) * 1e3),
+            float(np.rad2deg(np.arccos(np.clip((np.trace(d[:3, :3]) - 1) / 2, -1, 1)))))
+
+
+def run_precision_form(torch, depth, P, stream, n_frames=20, launch=None):
+    """Config 3: the chosen form (FP16 TSDF + u16 weights, FP32 accumulation,
+    Kahan/TwoSum J^T J, FP64 solve) and the FP64 oracle pipeline run the same
+    frames, each frame's ICP starting from its own previous pose perturbed by
+    the same seeded U(<= 5 deg, <= 5 cm) delta. Per frame: pose of each vs the
+    other and vs ground truth, model depth (raycast at the previous pose)
+    chosen vs FP64; at the end the TSDF, chosen vs FP64, in truncation units."""
+    import oracle
+    from superscanner_gb300 import GPUVoxelGrid
+    from superscanner_gb300.pipeline import Pipeline
+    n_frames = min(n_frames, len(depth))
+    rng = np.random.default_rng(77)
+    deltas = [rand_perturb(rng) for _ in range(n_frames)]
+    dev = torch.from_numpy(np.ascontiguousarray(depth[:n_frames]).view(np.int16)).cuda()
+    g = GPUVoxelGrid(int(1e9), TRUNC, VL, ROWS, COLS, storage="f16", with_color=False, hash_buckets=BUCKETS,
+                     max_weight=MAX_WEIGHT)
+    g.setIntrinsic(*INTR)
+    if launch:
+        g.set_launch_config(**launch)
+    pipe = Pipeline(g, use_graph=True, iters=ITERS, raycast_steps=STEPS_CAP, hint_margin=HINT_MARGIN,
+                    persistent_track=True)
+    o = oracle.MethodGrid64(VL, TRUNC, ROWS, COLS, INTR, MAX_WEIGHT)
+    with torch.cuda.stream(stream):
+        pipe.set_pose(P[0], stream)
+        pipe.frame(dev[0], track=False, stream=stream)
+    o.fuse(depth[0], P[0])
+    Tg, T64 = P[0].copy(), P[0].copy()
+    frames = []
+    for k in range(1, n_frames):
+        # model maps at the previous pose: FP64 raycast vs the chosen form's maps
+        vm, nm, _ = o.raycast(T64, STEPS_CAP, 0.2, 10.0, hint=depth[k - 1], hint_margin=HINT_MARGIN)
+        v, _ = pipe.maps_tensors(stream)
+        torch.cuda.synchronize()
+        dg = v[..., 3].cpu().numpy().astype(np.float64)
+        both = (dg > 0) & (vm[..., 3] > 0)
+        derr = np.abs(dg[both] - vm[..., 3][both]) * 1e3
+        start_g = Tg @ deltas[k]
+        with torch.cuda.stream(stream):
+            pipe.set_start(start_g, stream)
+            pipe.frame(dev[k], stream=stream)
+        Tg = pipe.pose(stream)
+        T64, _ = oracle.track64(depth[k], vm, nm, T64, T64 @ deltas[k], INTR, levels=len(ITERS), iters=ITERS)
+        o.fuse(depth[k], T64)
+        frames.append({"start_err_mm_deg": [round(x, 2) for x in pose_delta(start_g, P[k])],
+                       "chosen_vs_fp64_mm_deg": [round(x, 4) for x in pose_delta(Tg, T64)],
+                       "chosen_vs_gt_mm_deg": [round(x, 3) for x in pose_delta(Tg, P[k])],
+                       "fp64_vs_gt_mm_deg": [round(x, 3) for x in pose_delta(T64, P[k])],
+                       "depth_p99_mm": round(float(np.percentile(derr, 99)), 4),
+                       "depth_max_mm": round(float(derr.max()), 3)})
+    g.sync(stream)
+    a, b = g.export_blocks(with_color=False), o.export()
+    row64 = {tuple(c): q for q, c in enumerate(b["coords"].tolist())}
+    qa = [q for q, c in enumerate(a["coords"].tolist()) if tuple(c) in row64]
+    qb = [row64[tuple(a["coords"][q].tolist())] for q in qa]
+    wa, wb = a["w"][qa], b["w"][qb]
+    obs = (wa > 0) & (wb > 0)
+    same = obs & (wa == wb)  # fused from the same observations (a 0.01 mm pose difference can flip a voxel's pixel)
+    dsdf = np.abs(a["sdf"][qa].astype(np.float64) - b["sdf"][qb])[same] / TRUNC
+    pipe.close()
+    g.close()
+    agree = np.array([f["chosen_vs_fp64_mm_deg"] for f in frames])
+    return {
+        "frames": n_frames, "perturbation": "U(<=5 deg, <=5 cm) per frame, seed 77",
+        "max_chosen_vs_fp64_mm_deg": [round(float(agree[:, 0].max()), 4), round(float(agree[:, 1].max()), 5)],
+        "max_chosen_vs_gt_mm_deg": [round(max(f["chosen_vs_gt_mm_deg"][0] for f in frames), 3),
+                                    round(max(f["chosen_vs_gt_mm_deg"][1] for f in frames), 4)],
+        "max_start_err_mm_deg": [round(max(f["start_err_mm_deg"][0] for f in frames), 1),
+                                 round(max(f["start_err_mm_deg"][1] for f in frames), 2)],
+        "depth_vs_fp64_max_p99_mm": round(max(f["depth_p99_mm"] for f in frames), 4),
+        "depth_vs_fp64_max_mm": round(max(f["depth_max_mm"] for f in frames), 3),
+        "tsdf_vs_fp64_trunc_units": {"voxels_same_weight": int(same.sum()),
+                                     "frac_observed_same_weight": round(float(same.sum() / max(obs.sum(), 1)), 5),
+                                     "median": float("%.3g" % np.median(dsdf)),
+                                     "p99": float("%.3g" % np.percentile(dsdf, 99)),
+                                     "max": float("%.3g" % dsdf.max()),
+                                     "frac_le_1e-3": round(float((dsdf <= 1e-3).mean()), 5)},
+        "per_frame": frames,
+    }
+
+
 def roofline(stage_ms: dict, frames: int, touched: int, rc: dict, vox_bytes: int, peak: float, peak_kind: str):
     """Per-launch algorithmic bytes / time for every stage; the dominant one is reported."""
     npix = ROWS * COLS
@@ -472,6 +574,8 @@ def main_ours(args):
         roof["traffic_source"] = "ncu capture, " + tf.name
 
     refusion = run_refusion(torch, depth, P, stream, launch=tuned) if rank == 0 else None
+    precision = (run_precision_form(torch, depth, P, stream, n_frames=args.precision_frames, launch=tuned)
+                 if rank == 0 and args.precision_frames > 1 else None)
 
     # accuracy: tracked poses vs ground truth, chosen vs plain, depth vs the FP64 oracle
     gt = P[n - 1]
@@ -525,6 +629,7 @@ def main_ours(args):
             "gpu_launches": KERNELS_PER_FRAME * K,
             "accuracy": accuracy,
             "refusion": refusion,
+            "precision_form": precision,
             "clocks": clocks,
         }
         print(json.dumps(line), flush=True)

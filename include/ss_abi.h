@@ -267,6 +267,11 @@ ss_status ss_pipeline_destroy(ss_pipeline *p);
 /* Sets the device pose (camera -> world) used by the next untracked frame and
  * as the start of tracking. Synchronises s. */
 ss_status ss_pipeline_set_pose(ss_pipeline *p, const double T[16], ss_stream_t s);
+/* One-shot ICP start pose (camera -> world, row-major) for the next tracked
+ * frame: tracking starts from T instead of the current pose, while the model
+ * maps stay those raycast at the current pose. Synchronises s. No reference
+ * counterpart (the per-frame pipeline has none). */
+ss_status ss_pipeline_set_start(ss_pipeline *p, const double T[16], ss_stream_t s);
 /* Copies the current pose to the host. Synchronises s. */
 ss_status ss_pipeline_get_pose(ss_pipeline *p, double T[16], ss_stream_t s);
 /* Enqueues a copy of the current pose into T (pinned host or device memory)

@@ -100,6 +100,7 @@ SIGNATURES = {
     "ss_pipeline_destroy": (_st, [_p]),
     "ss_pipeline_set_pose": (_st, [_p, _D16, _p]),
     "ss_pipeline_get_pose": (_st, [_p, _D16, _p]),
+    "ss_pipeline_set_start": (_st, [_p, _D16, _p]),
     "ss_pipeline_input": (_st, [_p, C.POINTER(_p)]),
     "ss_pipeline_read_pose": (_st, [_p, _p, _p]),
     "ss_pipeline_maps": (_st, [_p, C.POINTER(_p), C.POINTER(_p)]),

@@ -11,6 +11,8 @@
 // (exe/SuperScanner.cpp:343-361).
 #include <vector>
 
+#include <cmath>
+
 #include "ss_grid_impl.cuh"
 #include "ss_track.cuh"
 
@@ -186,6 +188,18 @@ ss_status ss_pipeline_set_pose(ss_pipeline *P, const double T[16], ss_stream_t s
     if (!P || !T) return SS_ERR_ARG;
     SS_CUDA_TRY(cudaMemcpyAsync(P->st->T, T, 16 * sizeof(double), cudaMemcpyHostToDevice, (cudaStream_t)stream));
     SS_CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
+    return SS_OK;
+}
+
+ss_status ss_pipeline_set_start(ss_pipeline *P, const double T[16], ss_stream_t stream) {
+    if (!P || !T) return SS_ERR_ARG;
+    for (int k = 0; k < 16; k++)
+        if (!std::isfinite(T[k])) return SS_ERR_ARG;
+    static const int one = 1;
+    cudaStream_t s = (cudaStream_t)stream;
+    SS_CUDA_TRY(cudaMemcpyAsync(P->st->Tstart, T, 16 * sizeof(double), cudaMemcpyHostToDevice, s));
+    SS_CUDA_TRY(cudaMemcpyAsync(&P->st->has_start, &one, sizeof(int), cudaMemcpyHostToDevice, s));
+    SS_CUDA_TRY(cudaStreamSynchronize(s));
     return SS_OK;
 }
 

@@ -72,13 +72,17 @@ __device__ void write_frame_pose(const double *T, FramePose *fp) {
 }
 
 // Start of a frame: the model maps were raycast at the last pose T, so
-// Tprev = T, and tracking starts from T.
+// Tprev = T, and tracking starts from T (or from Tstart when one was set).
 __global__ void track_begin_kernel(TrackState *st) {
     if (threadIdx.x != 0) return;
     double Ti[16];
     for (int k = 0; k < 16; k++) st->Tprev[k] = st->T[k];
     rigid_inverse(st->Tprev, Ti);
     for (int k = 0; k < 12; k++) st->Tprev_inv[k] = (float)Ti[k];
+    if (st->has_start) {  // ICP start other than the model pose (one-shot)
+        for (int k = 0; k < 16; k++) st->T[k] = st->Tstart[k];
+        st->has_start = 0;
+    }
     mat_from_T(st->T, st->Tf);
     st->ticket = 0;
     st->barrier = 0u;
@@ -350,8 +354,9 @@ __device__ __forceinline__ void warp_rigid_inverse_f(const double *T, float *Ti)
 }
 
 // All Gauss-Newton iterations of one frame in one cooperative launch, with
-// the frame's start (model pose = current pose, its inverse) and end (the
-// FramePose of the result for integrate and raycast) folded in. Every CTA
+// the frame's start (model pose = current pose, its inverse; ICP start = the
+// one-shot start pose or the model pose) and end (the FramePose of the result
+// for integrate and raycast) folded in. Every CTA
 // reduces all CTA slots and solves redundantly (bit-identical results in
 // every CTA), so one grid barrier per iteration suffices; the slots are double
 // buffered so a CTA that runs ahead never overwrites slots still being read.
@@ -372,7 +377,6 @@ __global__ void __launch_bounds__(256) track_frame_kernel(const uint16_t *__rest
     if (threadIdx.x < 32) {
         // the model maps were raycast at the current pose: Tprev = T
         warp_rigid_inverse_f(Td, Pi);
-        if (threadIdx.x < 12) Tf[threadIdx.x] = (float)Td[threadIdx.x];
         if (blockIdx.x == 0) {
             if (threadIdx.x < 16) st->Tprev[threadIdx.x] = Td[threadIdx.x];
             if (threadIdx.x < 12) st->Tprev_inv[threadIdx.x] = Pi[threadIdx.x];
@@ -382,6 +386,12 @@ __global__ void __launch_bounds__(256) track_frame_kernel(const uint16_t *__rest
             }
         }
     }
+    __syncthreads();
+    // ICP start: the one-shot start pose when set (read by every CTA before its
+    // first barrier arrival; the last CTA to leave clears it), else the model pose
+    if (*(volatile int *)&st->has_start && threadIdx.x < 16) Td[threadIdx.x] = st->Tstart[threadIdx.x];
+    __syncthreads();
+    if (threadIdx.x < 12) Tf[threadIdx.x] = (float)Td[threadIdx.x];
     __syncthreads();
     unsigned barriers = 0;
     int parity = 0;
@@ -454,6 +464,7 @@ __global__ void __launch_bounds__(256) track_frame_kernel(const uint16_t *__rest
         if (atomicAdd(&st->exits, 1u) == gridDim.x - 1) {
             st->barrier = 0u;
             st->exits = 0u;
+            st->has_start = 0;
         }
     }
 }

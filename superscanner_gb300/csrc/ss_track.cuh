@@ -23,6 +23,8 @@ struct TrackState {
     unsigned int barrier;  // arrivals at the persistent tracker's grid barrier (0 between frames)
     int status;            // kSt* bits of the persistent tracker
     unsigned int exits;    // CTAs of the persistent tracker that have left (the last resets both counters)
+    int has_start;         // one-shot: the next tracked frame starts its ICP from Tstart
+    double Tstart[16];
 };
 
 struct TrackLaunch {

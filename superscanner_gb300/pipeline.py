@@ -77,6 +77,10 @@ class Pipeline:
     def set_pose(self, T, stream=None):
         check(lib.ss_pipeline_set_pose(self._h, f64x16(T), _stream_ptr(stream)), "pipeline_set_pose")
 
+    def set_start(self, T, stream=None):
+        """One-shot ICP start pose for the next tracked frame (the model maps stay at the current pose)."""
+        check(lib.ss_pipeline_set_start(self._h, f64x16(T), _stream_ptr(stream)), "pipeline_set_start")
+
     def pose(self, stream=None) -> np.ndarray:
         out = (C.c_double * 16)()
         check(lib.ss_pipeline_get_pose(self._h, out, _stream_ptr(stream)), "pipeline_get_pose")

@@ -139,3 +139,48 @@ def test_persistent_tracker_matches_per_iteration_launches():
     for a, b in zip(out[False], out[True]):
         dt, dr = pose_err(a, b)
         assert dt < 1e-5 and dr < 1e-5
+
+
+@pytest.mark.parametrize("persistent", [True, False])
+def test_perturbed_start_matches_fp64_tracker(persistent):
+    """ICP from a start perturbed by up to 5 deg / 5 cm (the precision form's
+    protocol): the GPU tracker and the FP64 oracle tracker, given the same
+    fused frames, model pose and start, agree to 0.05 mm / 0.001 deg and both
+    land within 1 mm / 0.05 deg of the ground truth."""
+    from superscanner_gb300.raydiff import se3_exp
+    P, depth = seq(13)
+    o = oracle.MethodGrid64(VL, TRUNC, 480, 640, INTR, 255)
+    for k in range(12):
+        o.fuse(depth[k], P[k])
+    vm, nm, _ = o.raycast(P[11], hint=depth[11], hint_margin=0.04)
+    rng = np.random.default_rng(5)
+    for trial in range(3):
+        ax = rng.normal(size=3)
+        ax /= np.linalg.norm(ax)
+        d = rng.normal(size=3)
+        d /= np.linalg.norm(d)
+        D = se3_exp(np.concatenate([ax * np.deg2rad(rng.uniform(2.5, 5.0)), d * rng.uniform(0.025, 0.05)]))
+        start = P[11] @ D
+        T64, _ = oracle.track64(depth[12], vm, nm, P[11], start, INTR)
+        # a fresh GPU pipeline (tracking fuses frame 12) tracks it from the same start against its maps at P[11]
+        g2 = GPUVoxelGrid(int(1e9), TRUNC, VL, 480, 640, storage="f16", with_color=False, hash_buckets=1 << 18,
+                          max_weight=255)
+        g2.setIntrinsic(*INTR)
+        p2 = Pipeline(g2, use_graph=False, hint_margin=0.04, persistent_track=persistent)
+        for k in range(12):
+            p2.set_pose(P[k])
+            p2.frame(dev(depth[k]), track=False)
+        p2.set_start(start)
+        p2.frame(dev(depth[12]))
+        Tg = p2.pose()
+        g2.sync()
+        t_gf, r_gf = pose_err(Tg, T64)
+        t_g, r_g = pose_err(Tg, P[12])
+        t_f, r_f = pose_err(T64, P[12])
+        t_s, r_s = pose_err(start, P[12])
+        print(f"start {t_s * 1e3:.1f} mm {np.rad2deg(r_s):.2f} deg -> gpu {t_g * 1e3:.3f} mm, fp64 {t_f * 1e3:.3f} mm,"
+              f" gpu vs fp64 {t_gf * 1e3:.4f} mm {np.rad2deg(r_gf):.5f} deg")
+        assert t_gf < 5e-5 and np.rad2deg(r_gf) < 1e-3
+        assert t_g < 1e-3 and np.rad2deg(r_g) < 0.05
+        p2.close()
+        g2.close()
