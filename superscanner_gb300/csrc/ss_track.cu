@@ -173,6 +173,93 @@ __device__ __forceinline__ void track_accumulate(const uint16_t *__restrict__ de
     }
 }
 
+// The persistent tracker keeps each thread's source points of a level in
+// shared memory across the level's iterations (a pixel's camera-frame point
+// does not depend on the pose): up to kCamCache pixels per thread.
+constexpr int kCamCache = 8;
+
+// Camera-frame points (x, y, d, valid) of this thread's pixels at a level,
+// the same pixels in the same order as track_accumulate.
+__device__ __forceinline__ void track_fill_cam(const uint16_t *__restrict__ depth, int rows, int cols, Intr in,
+                                               int level, float rmin, float dmax, int tid, int nthreads, int m_count,
+                                               float4 (*cam)[256]) {
+    const int lc = (cols + (1 << level) - 1) >> level;
+    const int npix = ((rows + (1 << level) - 1) >> level) * lc;
+    const float rfx = 1.f / in.fx, rfy = 1.f / in.fy;
+#pragma unroll
+    for (int m = 0; m < kCamCache; m++) {
+        if (m >= m_count) break;
+        const int p = tid + m * nthreads;
+        float4 cp = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (p < npix) {
+            const int i = (p / lc) << level, j = (p % lc) << level;
+            const float d = (float)__ldg(depth + (size_t)i * cols + j) * 1e-3f;
+            if ((d > rmin) && (d < dmax))
+                cp = make_float4(((float)j - in.cj) * rfx * d, ((float)i - in.ci) * rfy * d, d, 1.f);
+        }
+        cam[m][threadIdx.x] = cp;
+    }
+}
+
+// track_accumulate over the cached camera points (groups of kTrackGroup:
+// all model-map loads of a group before its sums).
+__device__ __forceinline__ void track_accumulate_cam(const float4 (*cam)[256], int m_count, int rows, int cols,
+                                                     Intr in, const float4 *__restrict__ vmap,
+                                                     const float4 *__restrict__ nmap, const float *T, const float *Pi,
+                                                     float dist2, float *s, float *c) {
+    for (int m0 = 0; m0 < m_count; m0 += kTrackGroup) {
+        float wv[kTrackGroup][3];
+        float4 n[kTrackGroup], v[kTrackGroup];
+        bool ok[kTrackGroup];
+#pragma unroll
+        for (int g = 0; g < kTrackGroup; g++) {
+            const float4 cp = (m0 + g < m_count) ? cam[m0 + g][threadIdx.x] : make_float4(0.f, 0.f, 0.f, 0.f);
+            const float cx = cp.x, cy = cp.y, dd = cp.z;
+            const float wx = fmaf(T[0], cx, fmaf(T[1], cy, fmaf(T[2], dd, T[3])));
+            const float wy = fmaf(T[4], cx, fmaf(T[5], cy, fmaf(T[6], dd, T[7])));
+            const float wz = fmaf(T[8], cx, fmaf(T[9], cy, fmaf(T[10], dd, T[11])));
+            const float qx = fmaf(Pi[0], wx, fmaf(Pi[1], wy, fmaf(Pi[2], wz, Pi[3])));
+            const float qy = fmaf(Pi[4], wx, fmaf(Pi[5], wy, fmaf(Pi[6], wz, Pi[7])));
+            const float qz = fmaf(Pi[8], wx, fmaf(Pi[9], wy, fmaf(Pi[10], wz, Pi[11])));
+            wv[g][0] = wx;
+            wv[g][1] = wy;
+            wv[g][2] = wz;
+            bool good = (cp.w != 0.f) && (qz > 1e-3f);
+            int ii = 0, jj = 0;
+            if (good) {
+                const float rq = 1.f / qz;
+                ii = (int)floorf(fmaf(qy * in.fy, rq, in.ci) + 0.5f);
+                jj = (int)floorf(fmaf(qx * in.fx, rq, in.cj) + 0.5f);
+                good = ii >= 0 && ii < rows && jj >= 0 && jj < cols;
+            }
+            ok[g] = good;
+            const size_t mi = good ? (size_t)ii * cols + jj : 0;
+            n[g] = good ? __ldg(nmap + mi) : make_float4(0.f, 0.f, 0.f, 0.f);
+            v[g] = good ? __ldg(vmap + mi) : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+#pragma unroll
+        for (int g = 0; g < kTrackGroup; g++) {
+            if (!ok[g]) continue;
+            const float4 nn = n[g], vv = v[g];
+            if (nn.x == 0.f && nn.y == 0.f && nn.z == 0.f) continue;
+            const float wx = wv[g][0], wy = wv[g][1], wz = wv[g][2];
+            const float ex = wx - vv.x, ey = wy - vv.y, ez = wz - vv.z;
+            if (ex * ex + ey * ey + ez * ez > dist2) continue;
+            const float r = nn.x * ex + nn.y * ey + nn.z * ez;
+            const float J[6] = {wy * nn.z - wz * nn.y, wz * nn.x - wx * nn.z, wx * nn.y - wy * nn.x, nn.x, nn.y, nn.z};
+            int q = 0;
+#pragma unroll
+            for (int a = 0; a < 6; a++)
+#pragma unroll
+                for (int b = a; b < 6; b++) kahan_add(s[q], c[q], J[a] * J[b]), q++;
+#pragma unroll
+            for (int a = 0; a < 6; a++) kahan_add(s[21 + a], c[21 + a], J[a] * r);
+            kahan_add(s[27], c[27], r * r);
+            s[28] += 1.f;  // counts stay exact far below 2^24
+        }
+    }
+}
+
 // Reduces the CTA's pairs and writes them to the value-major slots:
 // slots[value][cta]. Within a warp, a transpose-reduce (recursive halving):
 // at offset o each lane keeps the half of its remaining values selected by
@@ -371,6 +458,7 @@ __global__ void __launch_bounds__(256) track_frame_kernel(const uint16_t *__rest
     __shared__ double Td[16];
     __shared__ float Tf[12], Pi[12];
     __shared__ int done_level;
+    __shared__ float4 cam[kCamCache][256];
     if (threadIdx.x < 16) Td[threadIdx.x] = st->T[threadIdx.x];
     if (threadIdx.x == 0) done_level = -1;
     __syncthreads();
@@ -396,8 +484,13 @@ __global__ void __launch_bounds__(256) track_frame_kernel(const uint16_t *__rest
     unsigned barriers = 0;
     int parity = 0;
     bool alive = true;
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x, nthreads = gridDim.x * blockDim.x;
     for (int level = L.levels - 1; level >= 0 && alive; level--) {
         const float dist2 = L.dist[level] * L.dist[level];
+        const int npix = ((rows + (1 << level) - 1) >> level) * ((cols + (1 << level) - 1) >> level);
+        const int m_count = (npix + nthreads - 1) / nthreads;
+        const bool cached = m_count <= kCamCache;  // else the points are recomputed every iteration
+        if (cached) track_fill_cam(depth, rows, cols, in, level, L.rmin, L.dmax, tid, nthreads, m_count, cam);
         for (int it = 0; it < L.iters[level]; it++) {
             if (done_level == level) break;  // converged: identical decision in every CTA
             SS_TT(barriers, 0);
@@ -410,8 +503,11 @@ __global__ void __launch_bounds__(256) track_frame_kernel(const uint16_t *__rest
                 T[k] = Tf[k];
                 P[k] = Pi[k];
             }
-            track_accumulate(depth, rows, cols, in, vmap, nmap, T, P, level, dist2, L.rmin, L.dmax,
-                             blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x, s, c);
+            if (cached)
+                track_accumulate_cam(cam, m_count, rows, cols, in, vmap, nmap, T, P, dist2, s, c);
+            else
+                track_accumulate(depth, rows, cols, in, vmap, nmap, T, P, level, dist2, L.rmin, L.dmax, tid, nthreads,
+                                 s, c);
             SS_TT(barriers, 1);
             float2 *buf = slots + (size_t)parity * kTrackSums * gridDim.x;
             track_cta_to_slots(s, c, red, buf);
