@@ -61,6 +61,8 @@ def parse():
     ap.add_argument("--no-error-check", action="store_true")
     ap.add_argument("--precision-frames", type=int, default=20,
                     help="frames of the perturbed-start precision comparison against the FP64 oracle (0: skip)")
+    ap.add_argument("--refine-frames", type=int, default=50,
+                    help="frames of the gradient-based pose refinement through the raycast adjoint (0: skip)")
     ap.add_argument("--buckets", type=int, default=BUCKETS,
                     help="hash buckets (profiler captures use a smaller table to keep device memory small)")
     ap.add_argument("--only", choices=["all", "chosen"], default="all",
@@ -397,6 +399,57 @@ def run_precision_form(torch, depth, P, stream, n_frames=20, launch=None):
     }
 
 
+def run_pose_refinement(torch, depth, P, stream, n_frames=50):
+    """Config 5 use: the volume of the sequence fused at its poses (FP16,
+    4 mm), then n_frames seeded frames whose poses are perturbed by up to
+    3 deg / 4 cm and refined by BFGS on the raycast adjoint's pose gradient
+    (superscanner_gb300.raydiff.refine_pose: residual gates 0.2 / 0.1 /
+    0.05 m, the march recomputed at every evaluation)."""
+    from superscanner_gb300 import GPUVoxelGrid
+    from superscanner_gb300.raydiff import raycast_loss_grad, refine_pose
+    n = len(depth)
+    dev = torch.from_numpy(np.ascontiguousarray(depth).view(np.int16)).cuda()
+    g = GPUVoxelGrid(int(1e9), TRUNC, VL, ROWS, COLS, storage="f16", with_color=False, hash_buckets=BUCKETS,
+                     max_weight=MAX_WEIGHT)
+    g.setIntrinsic(*INTR)
+    with torch.cuda.stream(stream):
+        for k in range(n):
+            g.integrate_fast(dev[k], P[k].astype(np.float32), stream=stream)
+    torch.cuda.synchronize()
+    rng = np.random.default_rng(55)
+    ks = rng.choice(np.arange(1, n), min(n_frames, n - 1), replace=False)
+    res, evals, iters = [], 0, []
+    t0 = time.time()
+    for k in ks:
+        T0 = P[k] @ rand_perturb(rng, 3.0, 0.04)
+        T, info = refine_pose(g, T0, dev[k], stream=stream)
+        evals += info["evals"]
+        iters.append(info["iters"])
+        res.append(pose_delta(T0, P[k]) + pose_delta(T, P[k]))
+    wall = time.time() - t0
+    res = np.array(res)
+    # GPU time of one loss + adjoint evaluation (pose gradient, 640x480, <= 128 steps)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        raycast_loss_grad(g, P[ks[0]], dev[ks[0]], stream=stream)
+        ev0.record(stream)
+        for _ in range(10):
+            raycast_loss_grad(g, P[ks[0]], dev[ks[0]], stream=stream)
+        ev1.record(stream)
+    torch.cuda.synchronize()
+    g.close()
+    conv = (res[:, 2] < 1.0) & (res[:, 3] < 0.05)
+    return {
+        "frames": int(len(ks)), "perturbation": "U(<=3 deg, <=4 cm), seed 55",
+        "start_err_median_mm_deg": [round(float(np.median(res[:, 0])), 2), round(float(np.median(res[:, 1])), 3)],
+        "final_err_median_mm_deg": [round(float(np.median(res[:, 2])), 4), round(float(np.median(res[:, 3])), 5)],
+        "final_err_max_mm_deg": [round(float(res[:, 2].max()), 3), round(float(res[:, 3].max()), 4)],
+        "converged_lt_1mm_0.05deg": round(float(conv.mean()), 3),
+        "iters_median": int(np.median(iters)), "evals": int(evals), "wall_s": round(wall, 2),
+        "loss_grad_ms": round(ev0.elapsed_time(ev1) / 10, 3),
+    }
+
+
 def roofline(stage_ms: dict, frames: int, touched: int, rc: dict, vox_bytes: int, peak: float, peak_kind: str):
     """Per-launch algorithmic bytes / time for every stage; the dominant one is reported."""
     npix = ROWS * COLS
@@ -576,6 +629,8 @@ def main_ours(args):
     refusion = run_refusion(torch, depth, P, stream, launch=tuned) if rank == 0 else None
     precision = (run_precision_form(torch, depth, P, stream, n_frames=args.precision_frames, launch=tuned)
                  if rank == 0 and args.precision_frames > 1 else None)
+    refinement = (run_pose_refinement(torch, depth, P, stream, n_frames=args.refine_frames)
+                  if rank == 0 and args.refine_frames > 0 else None)
 
     # accuracy: tracked poses vs ground truth, chosen vs plain, depth vs the FP64 oracle
     gt = P[n - 1]
@@ -630,6 +685,7 @@ def main_ours(args):
             "accuracy": accuracy,
             "refusion": refusion,
             "precision_form": precision,
+            "pose_refinement": refinement,
             "clocks": clocks,
         }
         print(json.dumps(line), flush=True)
