@@ -1,0 +1,89 @@
+// ss_fuse.cuh — the per-voxel observation and running-average update of
+// integrate / deintegrate, shared by the per-frame fuse kernel (ss_grid.cu)
+// and the batched re-fusion (ss_refuse.cu), so that a batched re-fusion gives
+// bit for bit the volume of the sequential calls.
+#pragma once
+
+#include "ss_internal.cuh"
+
+namespace ss {
+
+// One voxel of integrationCore[Color]Tag / deIntegrationCore[Color]Tag
+// (GPUVoxelGrid.cpp:345-469, 516-550). Returns true when the voxel changes;
+// pixel (cori, corj) and the observed sdf come back through the references.
+template <bool kExact>
+__device__ __forceinline__ bool voxel_observe(const GridView &g, const uint16_t *__restrict__ depth, const Mat34 &E,
+                                              const Mat34 &Einv, const F3 &Ez, F3 vm, float &sdf, int &pix) {
+    F3 q;
+    float c0, c1;
+    if (kExact) {
+        q = xform(Einv, vm);
+        c0 = __fadd_rn(__fdiv_rn(__fmul_rn(q.y, g.in.fy), q.z), g.in.ci);  // getCoordinate (GPUVoxelGrid.h:234-237)
+        c1 = __fadd_rn(__fdiv_rn(__fmul_rn(q.x, g.in.fx), q.z), g.in.cj);
+    } else {
+        q.x = fmaf(vm.x, Einv.m[0], fmaf(vm.y, Einv.m[1], fmaf(vm.z, Einv.m[2], Einv.m[3])));
+        q.y = fmaf(vm.x, Einv.m[4], fmaf(vm.y, Einv.m[5], fmaf(vm.z, Einv.m[6], Einv.m[7])));
+        q.z = fmaf(vm.x, Einv.m[8], fmaf(vm.y, Einv.m[9], fmaf(vm.z, Einv.m[10], Einv.m[11])));
+        float rz;  // the pixel choice only needs the projection to ~1 ulp
+        asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(rz) : "f"(q.z));
+        c0 = fmaf(q.y * g.in.fy, rz, g.in.ci);
+        c1 = fmaf(q.x * g.in.fx, rz, g.in.cj);
+    }
+    // exact: the reference's (int) cast (GPUVoxelGrid.cpp:348-349), which picks the pixel half a pixel
+    // off the projection; fast: the nearest pixel (the truncation makes frame-to-model tracking drift)
+    const int cori = kExact ? __float2int_rz(c0) : __float2int_rd(c0 + 0.5f);
+    const int corj = kExact ? __float2int_rz(c1) : __float2int_rd(c1 + 0.5f);
+    if (!(cori < g.resi && corj < g.resj && cori >= 0 && corj >= 0)) return false;
+    pix = cori * g.resj + corj;
+    const uint16_t dmm = __ldg(depth + pix);
+    if (kExact) {
+        F3 vpt = get_point(g.in, cori, corj, depth_m(dmm));
+        if (!(vpt.z > g.rmin)) return false;
+        vpt = xform(E, vpt);
+        sdf = f3dot(f3sub(vpt, vm), Ez);
+    } else {
+        const float d = (float)dmm * 1.0e-3f;
+        if (!(d > g.rmin)) return false;
+        // (E p - vm) . Ez with p the pixel's point at depth d: for a rigid E
+        // this is d - q.z (q = E^-1 vm), the projective distance along the
+        // camera axis; a voxel behind the camera gets d + |q.z| > trunc
+        sdf = d - q.z;
+    }
+    return fabsf(sdf) < g.trunc;
+}
+
+// Running-average update of one voxel (sdf, weight) in FP32.
+template <bool kDeint, bool kExact>
+__device__ __forceinline__ void running_average(float &s, float &w, float obs, float max_weight) {
+    if (!kDeint) {
+        const float w1 = kExact ? __fadd_rn(w, 1.f) : w + 1.f;
+        s = kExact ? __fdiv_rn(__fadd_rn(__fmul_rn(s, w), obs), w1) : __fdividef(fmaf(s, w, obs), w1);
+        w = (max_weight > 0.f && w1 > max_weight) ? max_weight : w1;
+    } else {
+        if (w != 1.f) {
+            const float w1 = kExact ? __fsub_rn(w, 1.f) : w - 1.f;
+            s = kExact ? __fdiv_rn(__fsub_rn(__fmul_rn(s, w), obs), w1) : __fdividef(fmaf(s, w, -obs), w1);
+            w = w1;
+        } else {
+            w = 0.f;
+            s = 0.f;
+        }
+    }
+}
+
+template <bool kDeint, bool kExact>
+__device__ __forceinline__ void color_average(float &c, float w_old, float obs) {
+    if (!kDeint) {
+        c = kExact ? __fdiv_rn(__fadd_rn(__fmul_rn(c, w_old), obs), __fadd_rn(w_old, 1.f))
+                   : __fdividef(fmaf(c, w_old, obs), w_old + 1.f);
+    } else {
+        if (w_old != 1.f) {
+            c = kExact ? __fdiv_rn(__fsub_rn(__fmul_rn(c, w_old), obs), __fsub_rn(w_old, 1.f))
+                       : __fdividef(fmaf(c, w_old, -obs), w_old - 1.f);
+        } else {
+            c = 0.f;
+        }
+    }
+}
+
+}  // namespace ss

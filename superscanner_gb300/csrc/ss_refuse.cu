@@ -19,6 +19,7 @@
 // them (precision form included: the value is re-quantised to half after
 // every phase as a sequential store would). Only the aliasing rule differs:
 // an aliased entry takes the largest packed coordinate of the whole batch.
+#include "ss_fuse.cuh"
 #include "ss_grid_impl.cuh"
 
 namespace ss {
@@ -110,48 +111,6 @@ __global__ void __launch_bounds__(256) refuse_collect_kernel(GridView g, const u
     }
 }
 
-// The per-voxel observation and update of ss_grid.cu's fuse path.
-template <bool kExact>
-__device__ bool voxel_observe_b(const GridView &g, const uint16_t *__restrict__ depth, const FramePose &fp, F3 vm,
-                                float &sdf) {
-    F3 q;
-    float c0, c1;
-    const Mat34 &E = fp.E, &Einv = fp.Einv;
-    if (kExact) {
-        q = xform(Einv, vm);
-        c0 = __fadd_rn(__fdiv_rn(__fmul_rn(q.y, g.in.fy), q.z), g.in.ci);
-        c1 = __fadd_rn(__fdiv_rn(__fmul_rn(q.x, g.in.fx), q.z), g.in.cj);
-    } else {
-        q.x = fmaf(vm.x, Einv.m[0], fmaf(vm.y, Einv.m[1], fmaf(vm.z, Einv.m[2], Einv.m[3])));
-        q.y = fmaf(vm.x, Einv.m[4], fmaf(vm.y, Einv.m[5], fmaf(vm.z, Einv.m[6], Einv.m[7])));
-        q.z = fmaf(vm.x, Einv.m[8], fmaf(vm.y, Einv.m[9], fmaf(vm.z, Einv.m[10], Einv.m[11])));
-        const float rz = __frcp_rn(q.z);
-        c0 = fmaf(q.y * g.in.fy, rz, g.in.ci);
-        c1 = fmaf(q.x * g.in.fx, rz, g.in.cj);
-    }
-    const int cori = kExact ? __float2int_rz(c0) : __float2int_rd(c0 + 0.5f);
-    const int corj = kExact ? __float2int_rz(c1) : __float2int_rd(c1 + 0.5f);
-    if (!(cori < g.resi && corj < g.resj && cori >= 0 && corj >= 0)) return false;
-    const uint16_t dmm = __ldg(depth + cori * g.resj + corj);
-    F3 vpt;
-    if (kExact) {
-        vpt = get_point(g.in, cori, corj, depth_m(dmm));
-        if (!(vpt.z > g.rmin)) return false;
-        vpt = xform(E, vpt);
-        sdf = f3dot(f3sub(vpt, vm), F3{fp.Ez[0], fp.Ez[1], fp.Ez[2]});
-    } else {
-        const float d = (float)dmm * 1.0e-3f;
-        if (!(d > g.rmin)) return false;
-        const float px = ((float)corj - g.in.cj) * __frcp_rn(g.in.fx) * d;
-        const float py = ((float)cori - g.in.ci) * __frcp_rn(g.in.fy) * d;
-        vpt.x = fmaf(px, E.m[0], fmaf(py, E.m[1], fmaf(d, E.m[2], E.m[3])));
-        vpt.y = fmaf(px, E.m[4], fmaf(py, E.m[5], fmaf(d, E.m[6], E.m[7])));
-        vpt.z = fmaf(px, E.m[8], fmaf(py, E.m[9], fmaf(d, E.m[10], E.m[11])));
-        sdf = (vpt.x - vm.x) * fp.Ez[0] + (vpt.y - vm.y) * fp.Ez[1] + (vpt.z - vm.z) * fp.Ez[2];
-    }
-    return fabsf(sdf) < g.trunc;
-}
-
 template <int kStorage, bool kExact>
 __global__ void __launch_bounds__(256) refuse_apply_kernel(GridView g, const uint16_t *const *__restrict__ depths,
                                                            const FramePose *__restrict__ poses,
@@ -203,24 +162,16 @@ __global__ void __launch_bounds__(256) refuse_apply_kernel(GridView g, const uin
 #pragma unroll
                 for (int rr = 0; rr < 4; rr++) {
                     float obs;
-                    if (!voxel_observe_b<kExact>(g, depth, fp, vm[rr], obs)) continue;
+                    int pix;
+                    if (!voxel_observe<kExact>(g, depth, fp.E, fp.Einv, F3{fp.Ez[0], fp.Ez[1], fp.Ez[2]}, vm[rr], obs,
+                                               pix))
+                        continue;
                     if (kStorage == SS_STORAGE_F16 && deint && w[rr] == 0.f) continue;
                     float sv = s[rr], wv = w[rr];
-                    if (deint) {
-                        if (wv != 1.f) {
-                            const float w1 = kExact ? __fsub_rn(wv, 1.f) : wv - 1.f;
-                            sv = kExact ? __fdiv_rn(__fsub_rn(__fmul_rn(sv, wv), obs), w1)
-                                        : __fdividef(fmaf(sv, wv, -obs), w1);
-                            wv = w1;
-                        } else {
-                            wv = 0.f;
-                            sv = 0.f;
-                        }
-                    } else {
-                        const float w1 = kExact ? __fadd_rn(wv, 1.f) : wv + 1.f;
-                        sv = kExact ? __fdiv_rn(__fadd_rn(__fmul_rn(sv, wv), obs), w1) : __fdividef(fmaf(sv, wv, obs), w1);
-                        wv = (g.max_weight > 0.f && w1 > g.max_weight) ? g.max_weight : w1;
-                    }
+                    if (deint)
+                        running_average<true, kExact>(sv, wv, obs, g.max_weight);
+                    else
+                        running_average<false, kExact>(sv, wv, obs, g.max_weight);
                     if (kStorage == SS_STORAGE_F16) {  // the value a sequential call would have stored
                         sv = __half2float(__float2half_rn(sv * inv_trunc)) * g.trunc;
                         wv = fminf(wv, 65535.f);

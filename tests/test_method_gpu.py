@@ -58,6 +58,36 @@ def test_raycast_maps_vs_fp64(storage, margin):
     assert np.median(cos) > 0.9999
 
 
+@pytest.mark.parametrize("storage", ["f32", "f16"])
+def test_fast_fusion_vs_fp64(storage):
+    """The method's fusion (nearest pixel, running average in FP32) against
+    the FP64 oracle's at the same poses: the same blocks, the same weight on
+    at least 99.9 % of observed voxels, and where the weights agree the TSDF
+    within 1e-3 of the truncation at p99 (FP16: within its half-precision
+    step of sdf / truncation, 2^-11, plus that)."""
+    P, depth = seq(8, 2)
+    g = GPUVoxelGrid(int(1e9), TRUNC, VL, 480, 640, storage=storage, with_color=False, hash_buckets=1 << 18,
+                     max_weight=255)
+    g.setIntrinsic(*INTR)
+    o = oracle.MethodGrid64(VL, TRUNC, 480, 640, INTR, 255)
+    for k in range(8):
+        g.integrate_fast(dev(depth[k]), P[k].astype(np.float32))
+        o.fuse(depth[k], P[k])
+    g.sync()
+    a, b = g.export_blocks(with_color=False), o.export()
+    assert np.array_equal(np.sort(a["keys"]), np.sort(b["keys"]))
+    row = {tuple(c): q for q, c in enumerate(b["coords"].tolist())}
+    qb = [row[tuple(c)] for c in a["coords"].tolist()]
+    wa, wb = a["w"], b["w"][qb]
+    obs = (wa > 0) | (wb > 0)
+    same = obs & (wa == wb)
+    frac = same.sum() / obs.sum()
+    err = np.abs(a["sdf"].astype(np.float64) - b["sdf"][qb])[same] / TRUNC
+    print(storage, "same weight", frac, "sdf err p99", np.percentile(err, 99), "max", err.max())
+    assert frac >= 0.999
+    assert np.percentile(err, 99) <= (1e-3 if storage == "f32" else 1e-3 + 2.0 ** -11)
+
+
 def test_tracking_solve_vs_fp64():
     P, depth = seq(12)
     g = GPUVoxelGrid(int(1e9), TRUNC, VL, 480, 640, storage="f32", with_color=False, hash_buckets=1 << 18,
