@@ -97,90 +97,136 @@ __global__ void fill_u64_kernel(unsigned long long *p, size_t n, unsigned long l
 }
 
 // Block collection (vbCollectionTag, GPUVoxelGrid.cpp:471-514) fused with
-// depthToPcdTag (GPUVoxelGrid.h:303-307). One thread per pixel, one warp per
-// 32 pixels of a row. Per candidate block: __match_any_sync groups the lanes
-// of equal block coordinates, the group leader runs the lock-free
-// find-or-insert, and a 64-bit atomicMax on the block stamp both deduplicates
-// the block for this call (first visitor of the epoch appends it; replaces
-// alreadyIntegrated + the O(capacity) "Reset booleans" pass) and fixes the
-// entry's coordinates canonically for aliased keys. Appends are aggregated
-// per warp (one atomicAdd per warp and candidate round).
+// depthToPcdTag (GPUVoxelGrid.h:303-307). One thread per pixel, a CTA per
+// 32 x rows pixel tile, in two phases:
+//  1. every pixel enumerates the blocks its truncation band overlaps (x
+//     outer, z inner, GPUVoxelGrid.cpp:485-489) into a shared-memory hash set
+//     of packed block coordinates, so the tile's candidates are deduplicated
+//     on chip (512 slots per tile row, at most half of them used: with a
+//     truncation up to half a block a pixel has at most 8 candidates; a list
+//     of up to 128 distinct blocks per tile row; a candidate the set or the
+//     list cannot hold goes straight to phase 2's global steps);
+//  2. the tile's distinct blocks, in parallel: lock-free find-or-insert, then
+//     a 64-bit atomicMax on the block stamp, which both deduplicates the
+//     block for this call across tiles (first visitor of the epoch appends
+//     it; replaces alreadyIntegrated + the O(capacity) "Reset booleans" pass)
+//     and fixes the entry's coordinates canonically for aliased keys; appends
+//     are aggregated per warp.
+// The set of allocated blocks is the union of every pixel's candidates, as in
+// the reference; only the number of global probes and atomics changes (one
+// per distinct block per tile instead of one per distinct block per warp and
+// candidate index).
+constexpr unsigned long long kSetEmpty = ~0ull;
+constexpr int kSetSlotsPerRow = 512;
+
+// One candidate block straight through the global table (find-or-insert,
+// stamp, append): for candidates the tile's set cannot hold.
+__device__ void collect_block_global(const GridView &g, unsigned long long packed, uint32_t epoch) {
+    int x, y, z;
+    unpack_coords(packed, x, y, z);
+    bool inserted = false;
+    const int bucket = table_find_or_insert(g, prime_hash(x, y, z), &inserted);
+    if (inserted) super_insert(g, x, y, z);
+    if (bucket < 0) return;
+    const unsigned long long old = atomicMax(g.stamp + bucket, ((unsigned long long)epoch << kEpochShift) | packed);
+    if ((uint32_t)(old >> kEpochShift) == epoch) return;
+    const int idx = atomicAdd(&g.ctr->list_count, 1);
+    if (idx <= (int)g.mask) g.list[idx] = bucket;
+    else atomicOr(&g.ctr->status, kStListOverflow);
+}
+
 __global__ void __launch_bounds__(256) collect_kernel(GridView g, const uint16_t *__restrict__ depth, Mat34 E,
                                                       const FramePose *__restrict__ pose) {
+    extern __shared__ unsigned long long cset[];  // [slots] packed coords, then [slots / 4] list entries
+    __shared__ int ccount;
     const unsigned FULL = 0xffffffffu;
+    const int slots = kSetSlotsPerRow * blockDim.y;
+    unsigned long long *clist = cset + slots;
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x, nthreads = blockDim.x * blockDim.y;
+    for (int q = tid; q < slots; q += nthreads) cset[q] = kSetEmpty;
+    if (tid == 0) ccount = 0;
     if (pose) {
 #pragma unroll
         for (int k = 0; k < 12; k++) E.m[k] = __ldg(&pose->E.m[k]);
     }
-    const int lane = threadIdx.x;  // blockDim = (32, 8): one warp per row segment
     const int j = blockIdx.x * 32 + threadIdx.x;
     const int i = blockIdx.y * blockDim.y + threadIdx.y;
     const uint32_t epoch = *(volatile uint32_t *)&g.ctr->epoch;
+    __syncthreads();
 
-    int lox = 0, loy = 0, loz = 0, nx = 0, ny = 0, nz = 0;
+    // phase 1: this pixel's candidate blocks into the tile's set
     if (i < g.resi && j < g.resj) {
         F3 p = get_point(g.in, i, j, depth_m(__ldg(depth + (size_t)i * g.resj + j)));
         if (p.z > g.rmin) {
             F3 pt = xform(E, p);
             F3 t{g.trunc, g.trunc, g.trunc};
             F3 lo = f3sub(pt, t), hi = f3add(pt, t);
-            lox = idx_rule(lo.x, g.vbl);
-            loy = idx_rule(lo.y, g.vbl);
-            loz = idx_rule(lo.z, g.vbl);
-            nx = idx_rule(hi.x, g.vbl) - lox + 1;
-            ny = idx_rule(hi.y, g.vbl) - loy + 1;
-            nz = idx_rule(hi.z, g.vbl) - loz + 1;
+            const int lox = idx_rule(lo.x, g.vbl), loy = idx_rule(lo.y, g.vbl), loz = idx_rule(lo.z, g.vbl);
+            const int nx = idx_rule(hi.x, g.vbl) - lox + 1, ny = idx_rule(hi.y, g.vbl) - loy + 1,
+                      nz = idx_rule(hi.z, g.vbl) - loz + 1;
             if (nx < 1 || ny < 1 || nz < 1 || nx > 8 || ny > 8 || nz > 8) {
                 atomicOr(&g.ctr->status, kStRange);  // non-finite pose or truncation > 3.5 blocks
-                nx = ny = nz = 0;
+            } else {
+                for (int c = 0; c < nx * ny * nz; c++) {
+                    const int z = loz + c % nz, y = loy + (c / nz) % ny, x = lox + c / (nz * ny);
+                    if (!packable(x, y, z)) {
+                        atomicOr(&g.ctr->status, kStRange);
+                        continue;
+                    }
+                    const unsigned long long packed = pack_coords(x, y, z);
+                    uint32_t h = (uint32_t)((packed * 0x9E3779B97F4A7C15ull) >> 40) & (uint32_t)(slots - 1);
+                    bool placed = false;
+                    for (int probe = 0; probe < slots / 2 && !placed; probe++) {
+                        const unsigned long long old = atomicCAS(cset + h, kSetEmpty, packed);
+                        if (old == kSetEmpty) {
+                            const int at = atomicAdd(&ccount, 1);
+                            if (at < slots / 4) {
+                                clist[at] = packed;
+                            } else {  // list full (truncations over half a block): this thread does it
+                                collect_block_global(g, packed, epoch);
+                            }
+                            placed = true;
+                        } else if (old == packed) {
+                            placed = true;
+                        }
+                        h = (h + 1) & (uint32_t)(slots - 1);
+                    }
+                    if (!placed) collect_block_global(g, packed, epoch);  // set too crowded: same, directly
+                }
             }
         }
     }
-    const int total = nx * ny * nz;
+    __syncthreads();
+
+    // phase 2: the tile's distinct blocks
+    const int n = min(ccount, slots / 4);
+    const int lane = tid & 31, wid = tid >> 5, nw = (nthreads + 31) >> 5;
     const unsigned lt = (1u << lane) - 1u;
-    for (int c = 0;; c++) {
-        bool act = c < total;
-        if (!__any_sync(FULL, act)) break;
-        unsigned long long packed = 0, key = 0;
-        if (act) {
-            // x outer, z inner (GPUVoxelGrid.cpp:485-489)
-            const int z = loz + c % nz, y = loy + (c / nz) % ny, x = lox + c / (nz * ny);
-            if (packable(x, y, z)) {
-                packed = pack_coords(x, y, z);
-                key = prime_hash(x, y, z);
-            } else {
-                atomicOr(&g.ctr->status, kStRange);
-                act = false;
-            }
-        }
-        const unsigned am = __ballot_sync(FULL, act);
+    for (int base = wid * 32; base < n; base += nw * 32) {
+        const int e = base + lane;
         bool append = false;
         int bucket = -1;
-        if (act) {
-            const unsigned peers = __match_any_sync(am, packed);
-            if (__ffs(peers) - 1 == lane) {
-                bool inserted = false;
-                bucket = table_find_or_insert(g, key, &inserted);
-                if (inserted) {
-                    int x, y, z;
-                    unpack_coords(packed, x, y, z);
-                    super_insert(g, x, y, z);
-                }
-                if (bucket >= 0) {
-                    const unsigned long long mine = ((unsigned long long)epoch << kEpochShift) | packed;
-                    const unsigned long long old = atomicMax(g.stamp + bucket, mine);
-                    append = (uint32_t)(old >> kEpochShift) != epoch;
-                }
+        if (e < n) {
+            const unsigned long long packed = clist[e];
+            int x, y, z;
+            unpack_coords(packed, x, y, z);
+            bool inserted = false;
+            bucket = table_find_or_insert(g, prime_hash(x, y, z), &inserted);
+            if (inserted) super_insert(g, x, y, z);
+            if (bucket >= 0) {
+                const unsigned long long mine = ((unsigned long long)epoch << kEpochShift) | packed;
+                const unsigned long long old = atomicMax(g.stamp + bucket, mine);
+                append = (uint32_t)(old >> kEpochShift) != epoch;
             }
         }
         const unsigned ap = __ballot_sync(FULL, append);
         if (ap) {
             const int leader = __ffs(ap) - 1;
-            int base = 0;
-            if (lane == leader) base = atomicAdd(&g.ctr->list_count, __popc(ap));
-            base = __shfl_sync(FULL, base, leader);
+            int b0 = 0;
+            if (lane == leader) b0 = atomicAdd(&g.ctr->list_count, __popc(ap));
+            b0 = __shfl_sync(FULL, b0, leader);
             if (append) {
-                const int idx = base + __popc(ap & lt);
+                const int idx = b0 + __popc(ap & lt);
                 if (idx <= (int)g.mask) g.list[idx] = bucket;
                 else atomicOr(&g.ctr->status, kStListOverflow);
             }
@@ -435,7 +481,9 @@ ss_status launch_fuse(ss_grid *g, const uint16_t *depth, const uint8_t *rgb, con
     }
     const int cr = g->lc.collect_rows;
     const dim3 cblk(32, cr), cgrid((g->p.resj + 31) / 32, (g->p.resi + cr - 1) / cr);
-    collect_kernel<<<cgrid, cblk, 0, s>>>(g->v, depth, E, dpose);
+    // shared set of packed coordinates + the list of its distinct entries
+    const size_t csmem = (size_t)kSetSlotsPerRow * cr * sizeof(unsigned long long) * 5 / 4;  // <= 40 KB
+    collect_kernel<<<cgrid, cblk, csmem, s>>>(g->v, depth, E, dpose);
     SS_LAUNCH_CHECK();
     if (after_collect) SS_CUDA_TRY(cudaEventRecord(after_collect, s));
     const int ctas = persistent_ctas(g, g->lc.fuse_ctas_per_sm);
