@@ -114,8 +114,7 @@ __global__ void fill_u64_kernel(unsigned long long *p, size_t n, unsigned long l
 //     are aggregated per warp.
 // The set of allocated blocks is the union of every pixel's candidates, as in
 // the reference; only the number of global probes and atomics changes (one
-// per distinct block per tile instead of one per distinct block per warp and
-// candidate index).
+// per distinct block per tile).
 constexpr unsigned long long kSetEmpty = ~0ull;
 constexpr int kSetSlotsPerRow = 512;
 
@@ -154,53 +153,67 @@ __global__ void __launch_bounds__(256) collect_kernel(GridView g, const uint16_t
     const uint32_t epoch = *(volatile uint32_t *)&g.ctr->epoch;
     __syncthreads();
 
-    // phase 1: this pixel's candidate blocks into the tile's set
+    // phase 1: this pixel's candidate blocks into the tile's set. The warp
+    // steps through candidates together (an odometer over x outer, z inner);
+    // lanes with equal blocks are grouped and only each group's leader inserts.
+    int lox = 0, loy = 0, loz = 0, nx = 0, ny = 0, nz = 0;
     if (i < g.resi && j < g.resj) {
         F3 p = get_point(g.in, i, j, depth_m(__ldg(depth + (size_t)i * g.resj + j)));
         if (p.z > g.rmin) {
             F3 pt = xform(E, p);
             F3 t{g.trunc, g.trunc, g.trunc};
             F3 lo = f3sub(pt, t), hi = f3add(pt, t);
-            const int lox = idx_rule(lo.x, g.vbl), loy = idx_rule(lo.y, g.vbl), loz = idx_rule(lo.z, g.vbl);
-            const int nx = idx_rule(hi.x, g.vbl) - lox + 1, ny = idx_rule(hi.y, g.vbl) - loy + 1,
-                      nz = idx_rule(hi.z, g.vbl) - loz + 1;
+            lox = idx_rule(lo.x, g.vbl);
+            loy = idx_rule(lo.y, g.vbl);
+            loz = idx_rule(lo.z, g.vbl);
+            nx = idx_rule(hi.x, g.vbl) - lox + 1;
+            ny = idx_rule(hi.y, g.vbl) - loy + 1;
+            nz = idx_rule(hi.z, g.vbl) - loz + 1;
             if (nx < 1 || ny < 1 || nz < 1 || nx > 8 || ny > 8 || nz > 8) {
                 atomicOr(&g.ctr->status, kStRange);  // non-finite pose or truncation > 3.5 blocks
-            } else {
-                for (int c = 0; c < nx * ny * nz; c++) {
-                    const int z = loz + c % nz, y = loy + (c / nz) % ny, x = lox + c / (nz * ny);
-                    if (!packable(x, y, z)) {
-                        atomicOr(&g.ctr->status, kStRange);
-                        continue;
-                    }
-                    const unsigned long long packed = pack_coords(x, y, z);
-                    uint32_t h = (uint32_t)((packed * 0x9E3779B97F4A7C15ull) >> 40) & (uint32_t)(slots - 1);
-                    bool placed = false;
-                    for (int probe = 0; probe < slots / 2 && !placed; probe++) {
-                        const unsigned long long old = atomicCAS(cset + h, kSetEmpty, packed);
-                        if (old == kSetEmpty) {
-                            const int at = atomicAdd(&ccount, 1);
-                            if (at < slots / 4) {
-                                clist[at] = packed;
-                            } else {  // list full (truncations over half a block): this thread does it
-                                collect_block_global(g, packed, epoch);
-                            }
-                            placed = true;
-                        } else if (old == packed) {
-                            placed = true;
-                        }
-                        h = (h + 1) & (uint32_t)(slots - 1);
-                    }
-                    if (!placed) collect_block_global(g, packed, epoch);  // set too crowded: same, directly
+                nx = ny = nz = 0;
+            }
+        }
+    }
+    const int total = nx * ny * nz;
+    const int lane = tid & 31;
+    int x = lox, y = loy, z = loz;
+    for (int c = 0; __any_sync(FULL, c < total); c++) {
+        unsigned long long packed = kSetEmpty;
+        if (c < total) {
+            if (packable(x, y, z)) packed = pack_coords(x, y, z);
+            else atomicOr(&g.ctr->status, kStRange);
+            if (++z == loz + nz) {
+                z = loz;
+                if (++y == loy + ny) {
+                    y = loy;
+                    ++x;
                 }
             }
         }
+        const unsigned peers = __match_any_sync(FULL, packed);
+        if (packed == kSetEmpty || __ffs(peers) - 1 != lane) continue;
+        uint32_t h = (uint32_t)((packed * 0x9E3779B97F4A7C15ull) >> 40) & (uint32_t)(slots - 1);
+        bool placed = false;
+        for (int probe = 0; probe < slots / 2 && !placed; probe++) {
+            const unsigned long long old = atomicCAS(cset + h, kSetEmpty, packed);
+            if (old == kSetEmpty) {
+                const int at = atomicAdd(&ccount, 1);
+                if (at < slots / 4) clist[at] = packed;
+                else collect_block_global(g, packed, epoch);  // list full (truncations over half a block)
+                placed = true;
+            } else if (old == packed) {
+                placed = true;
+            }
+            h = (h + 1) & (uint32_t)(slots - 1);
+        }
+        if (!placed) collect_block_global(g, packed, epoch);  // set too crowded: same, directly
     }
     __syncthreads();
 
     // phase 2: the tile's distinct blocks
     const int n = min(ccount, slots / 4);
-    const int lane = tid & 31, wid = tid >> 5, nw = (nthreads + 31) >> 5;
+    const int wid = tid >> 5, nw = (nthreads + 31) >> 5;
     const unsigned lt = (1u << lane) - 1u;
     for (int base = wid * 32; base < n; base += nw * 32) {
         const int e = base + lane;
