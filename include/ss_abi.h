@@ -144,6 +144,54 @@ ss_status ss_integrate_fast(ss_grid *g, const uint16_t *depth, const uint8_t *rg
 ss_status ss_refuse_batch(ss_grid *g, int32_t n, const uint16_t *const *depths, const float *T_old,
                           const float *T_new, int32_t exact, ss_stream_t s);
 
+/* ---- integration scheduling (src/core/integrate.cpp:47-236) ------------ */
+
+/* Pose (camera -> world, row-major) of six world DoFs (rx, ry, rz, tx, ty,
+ * tz): trans(t) Rz(rz) Ry(ry) Rx(rx) (getT, src/utils/matrixutil.h:61-63). */
+ss_status ss_dofs_to_pose(const double dofs[6], double T[16]);
+/* The DoFs of a pose (MattoDof, src/utils/matrixutil.cpp:37-49). */
+ss_status ss_pose_to_dofs(const double T[16], double dofs[6]);
+/* updateReintegrationBuffer's order (integrate.cpp:218-236): the indices of
+ * n integrated frames sorted by descending pose change (diff,
+ * integrate.cpp:205-211: |(rotation DoF deltas, 2 x translation deltas)|
+ * between world and integrated DoFs, n x 6 each), stable, keeping those with
+ * a change >= treint; order[0..*count). Host only. */
+ss_status ss_reintegration_order(int32_t n, const double *world_dofs, const double *integrated_dofs, double treint,
+                                 int32_t *order, int32_t *count);
+
+/* The integration thread's frame buffers and schedule
+ * (pandia_integration::integrateThreadFunction, integrate.cpp:47-200) as a
+ * host object over one grid. Frames are identified by caller ids; their
+ * depth images (device, [resi][resj] u16) stay the caller's and must live
+ * until the frame is deintegrated. Not thread-safe (the reference guards it
+ * with integrationlock). treint: the re-integration threshold (the
+ * reference's config: 0.04); max_batch: re-integrations per step, fused as
+ * one ss_refuse_batch; exact != 0: ss_integrate's arithmetic. */
+typedef struct ss_scheduler ss_scheduler;
+ss_status ss_scheduler_create(ss_grid *g, double treint, int32_t max_batch, int32_t exact, ss_scheduler **out);
+ss_status ss_scheduler_destroy(ss_scheduler *s);
+/* integrationBuffer.push_back: a new frame and its world DoFs. */
+ss_status ss_scheduler_push_integrate(ss_scheduler *s, int64_t id, const uint16_t *depth, const double dofs[6]);
+/* The frame's world DoFs changed (pose optimisation, Frame::setWorlddofs). */
+ss_status ss_scheduler_set_dofs(ss_scheduler *s, int64_t id, const double dofs[6]);
+/* deintegrationBuffer.push_back; a frame not yet integrated is just dropped,
+ * and the frame leaves the re-integration queue. */
+ss_status ss_scheduler_push_deintegrate(ss_scheduler *s, int64_t id);
+/* updateReintegrationBuffer: refills the re-integration queue (queued: its
+ * length). */
+ss_status ss_scheduler_update(ss_scheduler *s, int32_t *queued);
+/* The ids in queue which (0 integrate, 1 re-integrate, 2 deintegrate), up to
+ * cap of them; count: the queue's length. */
+ss_status ss_scheduler_queue(ss_scheduler *s, int32_t which, int32_t cap, int64_t *ids, int32_t *count);
+/* One pass of the thread loop: all pending integrations, up to max_batch
+ * queued re-integrations (one batched re-fusion), all pending
+ * deintegrations; done[3] = the counts. Stream-ordered, no host sync. */
+ss_status ss_scheduler_step(ss_scheduler *s, ss_stream_t st, int32_t done[3]);
+/* The stop drain (integrate.cpp:160-197): everything queued. */
+ss_status ss_scheduler_drain(ss_scheduler *s, ss_stream_t st, int32_t done[3]);
+/* Whether frame id is fused, and the DoFs it is fused at. */
+ss_status ss_scheduler_frame(ss_scheduler *s, int64_t id, int32_t *integrated, double integrated_dofs[6]);
+
 /* Synchronises the stream and returns (then clears) the device status word. */
 ss_status ss_grid_sync(ss_grid *g, ss_stream_t s);
 

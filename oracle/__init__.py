@@ -265,3 +265,52 @@ def track64(depth, vmap, nmap, Tprev, T0, intr=(525.0, 525.0, 319.5, 239.5), lev
                        _ptr(np.ascontiguousarray(nmap, np.float64)), _ptr(np.ascontiguousarray(Tprev, np.float64)),
                        _ptr(T), int(levels), _ptr(it), _ptr(ds), float(rmin), float(dmax))
     return T, n
+
+
+# ---- integration scheduling (src/core/integrate.cpp:47-236), numpy restatement ----
+
+def dofs_to_pose(x):
+    """getT (src/utils/matrixutil.h:61-63): trans(x[3:6]) @ Rz(x[2]) @ Ry(x[1]) @ Rx(x[0]), as the product."""
+    x = np.asarray(x, np.float64)
+    def rx(a):
+        c, s = np.cos(a), np.sin(a)
+        return np.array([[1, 0, 0, 0], [0, c, -s, 0], [0, s, c, 0], [0, 0, 0, 1.0]])
+    def ry(a):
+        c, s = np.cos(a), np.sin(a)
+        return np.array([[c, 0, s, 0], [0, 1, 0, 0], [-s, 0, c, 0], [0, 0, 0, 1.0]])
+    def rz(a):
+        c, s = np.cos(a), np.sin(a)
+        return np.array([[c, -s, 0, 0], [s, c, 0, 0], [0, 0, 1, 0], [0, 0, 0, 1.0]])
+    t = np.eye(4)
+    t[:3, 3] = x[3:6]
+    return t @ rz(x[2]) @ ry(x[1]) @ rx(x[0])
+
+
+def pose_to_dofs(T):
+    """MattoDof (src/utils/matrixutil.cpp:37-49)."""
+    T = np.asarray(T, np.float64)
+    return np.array([np.arctan2(T[2, 1], T[2, 2]), -np.arcsin(T[2, 0]), np.arctan2(T[1, 0], T[0, 0]),
+                     T[0, 3], T[1, 3], T[2, 3]])
+
+
+def pose_change(world, integrated):
+    """diff (src/core/integrate.cpp:205-211): |(d rotation DoFs, 2 d translation DoFs)|."""
+    d = np.asarray(world, np.float64) - np.asarray(integrated, np.float64)
+    s = 0.0
+    for k in range(6):  # squared norm summed in element order
+        v = (1.0 if k < 3 else 2.0) * float(d[k])
+        s += v * v
+    return float(np.sqrt(s))
+
+
+def reintegration_order(world, integrated, treint):
+    """updateReintegrationBuffer (integrate.cpp:218-236): stable sort by descending
+    diff (std::list::sort), then the prefix with diff >= treint."""
+    d = [pose_change(w, i) for w, i in zip(world, integrated)]
+    idx = sorted(range(len(d)), key=lambda k: -d[k])  # Python's sort is stable
+    out = []
+    for k in idx:
+        if d[k] < treint:
+            break
+        out.append(k)
+    return out

@@ -79,6 +79,19 @@ SIGNATURES = {
     "ss_raycast": (_st, [_p, _F16, _p, _p, _p]),
     "ss_clean_memory": (_st, [_p, _p]),
     "ss_refuse_batch": (_st, [_p, _i32, _p, _p, _p, _i32, _p]),
+    "ss_dofs_to_pose": (_st, [_D16, _D16]),
+    "ss_pose_to_dofs": (_st, [_D16, _D16]),
+    "ss_reintegration_order": (_st, [_i32, _p, _p, C.c_double, _p, C.POINTER(_i32)]),
+    "ss_scheduler_create": (_st, [_p, C.c_double, _i32, _i32, _p]),
+    "ss_scheduler_destroy": (_st, [_p]),
+    "ss_scheduler_push_integrate": (_st, [_p, C.c_int64, _p, _D16]),
+    "ss_scheduler_set_dofs": (_st, [_p, C.c_int64, _D16]),
+    "ss_scheduler_push_deintegrate": (_st, [_p, C.c_int64]),
+    "ss_scheduler_update": (_st, [_p, C.POINTER(_i32)]),
+    "ss_scheduler_queue": (_st, [_p, _i32, _i32, _p, C.POINTER(_i32)]),
+    "ss_scheduler_step": (_st, [_p, _p, C.POINTER(_i32)]),
+    "ss_scheduler_drain": (_st, [_p, _p, C.POINTER(_i32)]),
+    "ss_scheduler_frame": (_st, [_p, C.c_int64, C.POINTER(_i32), _D16]),
     "ss_grid_sync": (_st, [_p, _p]),
     "ss_grid_block_count": (_st, [_p, _p, C.POINTER(_i32)]),
     "ss_grid_counters": (_st, [_p, _p, C.POINTER(C.c_int64)]),
