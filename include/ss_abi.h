@@ -192,6 +192,16 @@ ss_status ss_scheduler_drain(ss_scheduler *s, ss_stream_t st, int32_t done[3]);
 /* Whether frame id is fused, and the DoFs it is fused at. */
 ss_status ss_scheduler_frame(ss_scheduler *s, int64_t id, int32_t *integrated, double integrated_dofs[6]);
 
+/* Mesh of the TSDF's zero level set, extracted on the GPU (replaces the host
+ * copy into Open3D of marchingCubesHost, GPUVoxelGrid.cpp:200-251): marching
+ * tetrahedra over every cell of 8 observed voxel centres (6 tetrahedra per
+ * cell along its main diagonal; no cracks between cells), triangles facing
+ * from negative to positive sdf, world coordinates. triangles: device float
+ * [max_triangles][3][3]; count: the mesh's triangle count, which may exceed
+ * max_triangles (then only the first max_triangles were written: call again
+ * with a larger buffer). Synchronises s. */
+ss_status ss_grid_extract_mesh(ss_grid *g, int64_t max_triangles, float *triangles, int64_t *count, ss_stream_t s);
+
 /* Synchronises the stream and returns (then clears) the device status word. */
 ss_status ss_grid_sync(ss_grid *g, ss_stream_t s);
 

@@ -784,3 +784,94 @@ int orm_track(const uint16_t *depth, int rows, int cols, float fx, float fy, flo
 }
 
 }  // extern "C"
+
+// ---- mesh of the zero level set (the GPU's ss_grid_extract_mesh) in FP64 ----
+// Marching tetrahedra: each cell of 8 observed voxel centres is split into
+// the 6 tetrahedra along the diagonal from corner 0 to corner 7 (corner
+// n = dx + 2 dy + 4 dz); sdf < 0 is inside; edge vertices by linear
+// interpolation; triangles face from the inside corners to the outside ones.
+namespace {
+const int kTet64[6][4] = {{0, 1, 3, 7}, {0, 1, 5, 7}, {0, 2, 3, 7}, {0, 2, 6, 7}, {0, 4, 5, 7}, {0, 4, 6, 7}};
+
+struct P3 {
+    double x, y, z;
+};
+
+P3 edge64(const P3 &p, double sp, const P3 &q, double sq) {
+    const double t = sp / (sp - sq);
+    return {p.x + t * (q.x - p.x), p.y + t * (q.y - p.y), p.z + t * (q.z - p.z)};
+}
+
+void emit64(std::vector<double> &out, P3 a, P3 b, P3 c, const P3 &dir) {
+    const double ux = b.x - a.x, uy = b.y - a.y, uz = b.z - a.z, vx = c.x - a.x, vy = c.y - a.y, vz = c.z - a.z;
+    const double nx = uy * vz - uz * vy, ny = uz * vx - ux * vz, nz = ux * vy - uy * vx;
+    if (nx * dir.x + ny * dir.y + nz * dir.z < 0) std::swap(b, c);
+    for (const P3 *q : {&a, &b, &c}) {
+        out.push_back(q->x);
+        out.push_back(q->y);
+        out.push_back(q->z);
+    }
+}
+
+void tetra64(std::vector<double> &out, const P3 *p, const double *s, const int *t) {
+    int in[4], outc[4], ni = 0, no = 0;
+    for (int k = 0; k < 4; k++) {
+        if (s[t[k]] < 0) in[ni++] = t[k];
+        else outc[no++] = t[k];
+    }
+    if (ni == 0 || ni == 4) return;
+    P3 ci{0, 0, 0}, co{0, 0, 0};
+    for (int k = 0; k < ni; k++) ci = {ci.x + p[in[k]].x, ci.y + p[in[k]].y, ci.z + p[in[k]].z};
+    for (int k = 0; k < no; k++) co = {co.x + p[outc[k]].x, co.y + p[outc[k]].y, co.z + p[outc[k]].z};
+    const P3 dir{co.x / no - ci.x / ni, co.y / no - ci.y / ni, co.z / no - ci.z / ni};
+    if (ni == 1 || ni == 3) {
+        const int a = ni == 1 ? in[0] : outc[0];
+        const int *r = ni == 1 ? outc : in;
+        emit64(out, edge64(p[a], s[a], p[r[0]], s[r[0]]), edge64(p[a], s[a], p[r[1]], s[r[1]]),
+               edge64(p[a], s[a], p[r[2]], s[r[2]]), dir);
+    } else {
+        const int a = in[0], b = in[1], c = outc[0], d = outc[1];
+        const P3 ac = edge64(p[a], s[a], p[c], s[c]), ad = edge64(p[a], s[a], p[d], s[d]);
+        const P3 bd = edge64(p[b], s[b], p[d], s[d]), bc = edge64(p[b], s[b], p[c], s[c]);
+        emit64(out, ac, ad, bd, dir);
+        emit64(out, ac, bd, bc, dir);
+    }
+}
+}  // namespace
+
+// Triangles (9 doubles each) into tris (up to cap); returns the total count.
+extern "C" long long orm_extract_mesh(void *h, long long cap, double *tris) {
+    const Grid64 &g = *(Grid64 *)h;
+    std::vector<double> out;
+    Cache cache;
+    for (const Block64 *blk : g.blocks) {
+        const int bx = blk->vb[0], by = blk->vb[1], bz = blk->vb[2];
+        for (int c = 0; c < kVox; c++) {
+            const int i = c & 7, j = (c >> 3) & 7, k = c >> 6;
+            P3 p[8];
+            double s[8];
+            bool ok = true;
+            for (int n = 0; n < 8 && ok; n++) {
+                const int vi = i + (n & 1), vj = j + ((n >> 1) & 1), vk = k + (n >> 2);
+                const Block64 *b = cached(g, cache, bx + (vi >> 3), by + (vj >> 3), bz + (vk >> 3));
+                if (!b) {
+                    ok = false;
+                    break;
+                }
+                const int v = (vi & 7) + 8 * (vj & 7) + 64 * (vk & 7);
+                if (!(b->w[v] > 0)) {
+                    ok = false;
+                    break;
+                }
+                s[n] = b->sdf[v];
+                p[n] = {((double)(bx * 8 + vi) + 0.5) * g.vl, ((double)(by * 8 + vj) + 0.5) * g.vl,
+                        ((double)(bz * 8 + vk) + 0.5) * g.vl};
+            }
+            if (!ok) continue;
+            for (int t = 0; t < 6; t++) tetra64(out, p, s, kTet64[t]);
+        }
+    }
+    const long long n = (long long)out.size() / 9;
+    if (tris) std::memcpy(tris, out.data(), (size_t)std::min(n, cap) * 9 * sizeof(double));
+    return n;
+}

@@ -647,6 +647,7 @@ ss_status ss_grid_destroy(ss_grid *g) {
     cudaFree(g->v.rgb);
     cudaFree(g->v.sbkeys);
     cudaFree(g->phase_mask);
+    cudaFree(g->mesh_count);
     cudaFree(g->batch_poses);
     cudaFree((void *)g->batch_depths);
     delete g;

@@ -21,6 +21,7 @@ struct ss_grid {
     uint32_t *phase_mask = nullptr;        // [buckets][kMaxPhases / 32]
     ss::FramePose *batch_poses = nullptr;  // [kMaxPhases]
     const uint16_t **batch_depths = nullptr;  // [kMaxPhases / 2] device pointers
+    unsigned long long *mesh_count = nullptr;  // triangle counter of ss_grid_extract_mesh (first call)
 };
 
 namespace ss {
