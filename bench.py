@@ -631,6 +631,16 @@ def main_ours(args):
             print(json.dumps({"metric": METRIC, "value": round(world * K / (chosen["ms"] * 1e-3), 2),
                               "unit": "frames/s", "steps": K, "warmup": W, "only": "chosen"}), flush=True)
         return
+    mesh = None
+    if rank == 0:  # mesh export of the chosen form's volume (GPU marching tetrahedra)
+        from superscanner_gb300.mesh import extract_triangles
+        extract_triangles(chosen["grid"], stream=stream)
+        t0 = time.perf_counter()
+        tris = extract_triangles(chosen["grid"], stream=stream)
+        mesh = {"triangles": int(tris.shape[0]), "live_blocks": int(chosen["live"]),
+                "ms": round((time.perf_counter() - t0) * 1e3, 3),
+                "note": "two calls (count, then extract) incl. host sync; world-space triangle soup"}
+        del tris
     plain = run_form(torch, "plain", depth_dev, P, W, K, stream, barrier)
     prof = run_form(torch, "chosen", depth_dev, P, W, K, stream, lambda: None, profile=True, launch=tuned)
 
@@ -727,6 +737,7 @@ def main_ours(args):
             "gpu_launches": KERNELS_PER_FRAME * K,
             "accuracy": accuracy,
             "refusion": refusion,
+            "mesh": mesh,
             "precision_form": precision,
             "pose_refinement": refinement,
             "clocks": clocks,
