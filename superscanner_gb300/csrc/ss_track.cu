@@ -8,10 +8,11 @@
 //
 // Source pixels of level l are the level-0 pixels (i 2^l, j 2^l)
 // back-projected with the level-0 intrinsics (no pyramid images are built).
-// Each thread accumulates the 21 + 6 + 2 normal-equation sums in FP32 with
-// Kahan compensation; warps combine (sum, compensation) pairs with TwoSum
-// through shuffles, CTAs through shared memory, and the CTA slots are reduced
-// the same way in a fixed order. One warp then solves the 6x6 system and
+// Each thread accumulates the 21 + 6 + 2 normal-equation sums in FP32 (four
+// pixels' terms by FMA, then one Kahan-compensated add per group); warps
+// combine (sum, compensation) pairs with TwoSum through shuffles, CTAs
+// through shared memory, and the CTA slots are reduced the same way in a
+// fixed order. One warp then solves the 6x6 system and
 // applies the SE(3) update in FP64 (ss_track_solve.cuh). Two launch forms:
 // one cooperative launch per frame (every CTA reduces and solves redundantly,
 // one grid barrier per iteration), or one launch per iteration (the last CTA
@@ -101,7 +102,9 @@ __global__ void pose_prep_kernel(TrackState *st) {
 // into Kahan (sum, compensation) pairs. The thread's pixels are visited in
 // groups of kTrackGroup: all depth loads of a group, then all model-map loads,
 // then the sums, so the two dependent memory round trips of a pixel overlap
-// with those of the others (same pixel order as one at a time).
+// with those of the others. A group's terms are summed with plain FMAs, then
+// added to the Kahan pairs once per group (the running sums stay compensated;
+// a group adds at most kTrackGroup - 1 roundings).
 constexpr int kTrackGroup = 4;
 
 __device__ __forceinline__ void track_accumulate(const uint16_t *__restrict__ depth, int rows, int cols, Intr in,
@@ -150,6 +153,10 @@ __device__ __forceinline__ void track_accumulate(const uint16_t *__restrict__ de
             n[g] = good ? __ldg(nmap + m) : make_float4(0.f, 0.f, 0.f, 0.f);
             v[g] = good ? __ldg(vmap + m) : make_float4(0.f, 0.f, 0.f, 0.f);
         }
+        float t[kTrackSums - 1];
+#pragma unroll
+        for (int q = 0; q < kTrackSums - 1; q++) t[q] = 0.f;
+        bool any = false;
 #pragma unroll
         for (int g = 0; g < kTrackGroup; g++) {
             if (!ok[g]) continue;
@@ -164,11 +171,16 @@ __device__ __forceinline__ void track_accumulate(const uint16_t *__restrict__ de
 #pragma unroll
             for (int a = 0; a < 6; a++)
 #pragma unroll
-                for (int b = a; b < 6; b++) kahan_add(s[q], c[q], J[a] * J[b]), q++;
+                for (int b = a; b < 6; b++) t[q] = fmaf(J[a], J[b], t[q]), q++;
 #pragma unroll
-            for (int a = 0; a < 6; a++) kahan_add(s[21 + a], c[21 + a], J[a] * r);
-            kahan_add(s[27], c[27], r * r);
+            for (int a = 0; a < 6; a++) t[21 + a] = fmaf(J[a], r, t[21 + a]);
+            t[27] = fmaf(r, r, t[27]);
             s[28] += 1.f;  // counts stay exact far below 2^24
+            any = true;
+        }
+        if (any) {
+#pragma unroll
+            for (int q = 0; q < kTrackSums - 1; q++) kahan_add(s[q], c[q], t[q]);
         }
     }
 }
@@ -202,7 +214,9 @@ __device__ __forceinline__ void track_fill_cam(const uint16_t *__restrict__ dept
 }
 
 // track_accumulate over the cached camera points (groups of kTrackGroup:
-// all model-map loads of a group before its sums).
+// all model-map loads of a group before its sums). A group's terms are summed
+// with plain FMAs, then added to the Kahan pairs once per group (the running
+// sums stay compensated; a group adds at most kTrackGroup - 1 roundings).
 __device__ __forceinline__ void track_accumulate_cam(const float4 (*cam)[256], int m_count, int rows, int cols,
                                                      Intr in, const float4 *__restrict__ vmap,
                                                      const float4 *__restrict__ nmap, const float *T, const float *Pi,
@@ -237,6 +251,10 @@ __device__ __forceinline__ void track_accumulate_cam(const float4 (*cam)[256], i
             n[g] = good ? __ldg(nmap + mi) : make_float4(0.f, 0.f, 0.f, 0.f);
             v[g] = good ? __ldg(vmap + mi) : make_float4(0.f, 0.f, 0.f, 0.f);
         }
+        float t[kTrackSums - 1];
+#pragma unroll
+        for (int q = 0; q < kTrackSums - 1; q++) t[q] = 0.f;
+        bool any = false;
 #pragma unroll
         for (int g = 0; g < kTrackGroup; g++) {
             if (!ok[g]) continue;
@@ -251,11 +269,16 @@ __device__ __forceinline__ void track_accumulate_cam(const float4 (*cam)[256], i
 #pragma unroll
             for (int a = 0; a < 6; a++)
 #pragma unroll
-                for (int b = a; b < 6; b++) kahan_add(s[q], c[q], J[a] * J[b]), q++;
+                for (int b = a; b < 6; b++) t[q] = fmaf(J[a], J[b], t[q]), q++;
 #pragma unroll
-            for (int a = 0; a < 6; a++) kahan_add(s[21 + a], c[21 + a], J[a] * r);
-            kahan_add(s[27], c[27], r * r);
+            for (int a = 0; a < 6; a++) t[21 + a] = fmaf(J[a], r, t[21 + a]);
+            t[27] = fmaf(r, r, t[27]);
             s[28] += 1.f;  // counts stay exact far below 2^24
+            any = true;
+        }
+        if (any) {
+#pragma unroll
+            for (int q = 0; q < kTrackSums - 1; q++) kahan_add(s[q], c[q], t[q]);
         }
     }
 }
