@@ -202,6 +202,11 @@ ss_status ss_scheduler_frame(ss_scheduler *s, int64_t id, int32_t *integrated, d
  * with a larger buffer). Synchronises s. */
 ss_status ss_grid_extract_mesh(ss_grid *g, int64_t max_triangles, float *triangles, int64_t *count, ss_stream_t s);
 
+/* Frame ingest help (src/cameras/DataCam.cpp:10-100 reads depth PNGs): undoes
+ * the PNG row filters (types 0..4) of rows x (1 + row_bytes) filtered bytes
+ * into rows x row_bytes (bpp: bytes per pixel). Host memory, host code. */
+ss_status ss_png_unfilter(const uint8_t *filtered, int32_t rows, int32_t row_bytes, int32_t bpp, uint8_t *out);
+
 /* Synchronises the stream and returns (then clears) the device status word. */
 ss_status ss_grid_sync(ss_grid *g, ss_stream_t s);
 
