@@ -18,6 +18,10 @@ struct BlockCache {
     int x, y, z, bucket;
     unsigned lookups;  // hash-table finds issued (cache misses)
     unsigned voxels;   // voxel words loaded
+    // the last sampled cell (its lowest voxel) and its 8 corner values
+    int cx = INT_MIN, cy = INT_MIN, cz = INT_MIN;
+    bool cok = false;
+    float cs[8];
 };
 
 template <int kStorage>
@@ -57,8 +61,13 @@ __device__ __forceinline__ TriSample trilinear(const GridView &g, float px, floa
     const int ix = (int)fx0, iy = (int)fy0, iz = (int)fz0;
     const float ax = ux - fx0, ay = uy - fy0, az = uz - fz0;
     float s[8];
-    if ((ix & 7) != 7 && (iy & 7) != 7 && (iz & 7) != 7) {
+    if (ix == c.cx && iy == c.cy && iz == c.cz) {  // same cell as the last sample: its corners again
+        if (!c.cok) return r;
+#pragma unroll
+        for (int k = 0; k < 8; k++) s[k] = c.cs[k];
+    } else if ((ix & 7) != 7 && (iy & 7) != 7 && (iz & 7) != 7) {
         // all 8 corners in one block: one lookup, fixed offsets +1, +8, +64
+        c.cx = ix, c.cy = iy, c.cz = iz, c.cok = false;
         const int b = cached_lookup(g, c, ix >> 3, iy >> 3, iz >> 3);
         if (b < 0) return r;
         const int v0 = (ix & 7) + 8 * (iy & 7) + 64 * (iz & 7);
@@ -71,11 +80,14 @@ __device__ __forceinline__ TriSample trilinear(const GridView &g, float px, floa
         for (int k = 0; k < 8; k++) {
             ok &= sw[k].y > 0.f;
             s[k] = sw[k].x;
+            c.cs[k] = s[k];
         }
+        c.cok = ok;
         if (!ok) return r;
     } else {
         // the cell straddles block faces: each distinct block is looked up once
         // (corner (a, b, c) lies in block offset (a sx, b sy, c sz))
+        c.cx = ix, c.cy = iy, c.cz = iz, c.cok = false;
         const int bx0 = ix >> 3, by0 = iy >> 3, bz0 = iz >> 3;
         const bool sx = (ix & 7) == 7, sy = (iy & 7) == 7, sz = (iz & 7) == 7;
         int bk[8];
@@ -104,7 +116,9 @@ __device__ __forceinline__ TriSample trilinear(const GridView &g, float px, floa
         for (int k = 0; k < 8; k++) {
             ok &= sw[k].y > 0.f;
             s[k] = sw[k].x;
+            c.cs[k] = s[k];
         }
+        c.cok = ok;
         if (!ok) return r;
     }
     // lerp along x, then y, then z
