@@ -272,6 +272,16 @@ __global__ void __launch_bounds__(256) fuse_kernel(GridView g, const uint16_t *_
     for (int t = warp; t < n; t += nwarps) {
         const int bucket = __ldg(g.list + (t >> 2));
         const int r0 = (t & 3) * 4;
+        // this lane's 4 voxel words, loaded before they are known to be
+        // observed: their loads overlap the stamp load and the depth gathers
+        float2 sw32[4];
+        uint32_t sw16[4];
+#pragma unroll
+        for (int rr = 0; rr < 4; rr++) {
+            const size_t vi = (size_t)bucket * kBlockVoxels + lane + 32 * (r0 + rr);
+            if (kStorage == SS_STORAGE_F32) sw32[rr] = g.vox32[vi];
+            else sw16[rr] = g.vox16[vi];
+        }
         int bx, by, bz;
         unpack_coords(__ldg(g.stamp + bucket), bx, by, bz);
         // pzero = vbl * Kvec3f(x, y, z) (GPUVoxelGrid.cpp:501)
@@ -290,11 +300,10 @@ __global__ void __launch_bounds__(256) fuse_kernel(GridView g, const uint16_t *_
             if (!voxel_observe<kExact>(g, depth, E, Einv, Ez, vm, obs, pix)) continue;
             float s, w;
             if (kStorage == SS_STORAGE_F32) {
-                const float2 sw = g.vox32[vi];
-                s = sw.x;
-                w = sw.y;
+                s = sw32[rr].x;
+                w = sw32[rr].y;
             } else {
-                const uint32_t word = g.vox16[vi];
+                const uint32_t word = sw16[rr];
                 s = __half2float(__ushort_as_half((unsigned short)(word & 0xffffu))) * g.trunc;
                 w = (float)(word >> 16);
             }
