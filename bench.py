@@ -361,11 +361,13 @@ def run_precision_form(torch, depth, P, stream, n_frames=20, launch=None):
     Kahan/TwoSum J^T J, FP64 solve) and the FP64 oracle pipeline run the same
     frames, each frame's ICP starting from its own previous pose perturbed by
     the same seeded U(<= 5 deg, <= 5 cm) delta. Per frame: pose of each vs the
-    other and vs ground truth, model depth (raycast at the previous pose)
-    chosen vs FP64; at the end the TSDF, chosen vs FP64, in truncation units."""
+    other and vs ground truth; model depth chosen vs FP64, each raycast at its
+    own previous pose (pose and TSDF differences together) and the chosen
+    volume raycast at the FP64 pose (TSDF differences alone); at the end the
+    TSDF, chosen vs FP64, in truncation units."""
     import oracle
     from superscanner_gb300 import GPUVoxelGrid
-    from superscanner_gb300.pipeline import Pipeline
+    from superscanner_gb300.pipeline import Pipeline, raycast_maps
     n_frames = min(n_frames, len(depth))
     rng = np.random.default_rng(77)
     deltas = [rand_perturb(rng) for _ in range(n_frames)]
@@ -388,10 +390,15 @@ def run_precision_form(torch, depth, P, stream, n_frames=20, launch=None):
         # model maps at the previous pose: FP64 raycast vs the chosen form's maps
         vm, nm, _ = o.raycast(T64, STEPS_CAP, 0.2, 10.0, hint=depth[k - 1], hint_margin=HINT_MARGIN)
         v, _ = pipe.maps_tensors(stream)
+        vs, _ = raycast_maps(g, T64.astype(np.float32), STEPS_CAP, 0.2, 10.0, hint_depth=dev[k - 1],
+                             hint_margin=HINT_MARGIN, stream=stream)
         torch.cuda.synchronize()
         dg = v[..., 3].cpu().numpy().astype(np.float64)
         both = (dg > 0) & (vm[..., 3] > 0)
         derr = np.abs(dg[both] - vm[..., 3][both]) * 1e3
+        ds = vs[..., 3].cpu().numpy().astype(np.float64)
+        both = (ds > 0) & (vm[..., 3] > 0)
+        serr = np.abs(ds[both] - vm[..., 3][both]) * 1e3
         start_g = Tg @ deltas[k]
         with torch.cuda.stream(stream):
             pipe.set_start(start_g, stream)
@@ -404,7 +411,9 @@ def run_precision_form(torch, depth, P, stream, n_frames=20, launch=None):
                        "chosen_vs_gt_mm_deg": [round(x, 3) for x in pose_delta(Tg, P[k])],
                        "fp64_vs_gt_mm_deg": [round(x, 3) for x in pose_delta(T64, P[k])],
                        "depth_p99_mm": round(float(np.percentile(derr, 99)), 4),
-                       "depth_max_mm": round(float(derr.max()), 3)})
+                       "depth_max_mm": round(float(derr.max()), 3),
+                       "same_pose_depth_p99_mm": round(float(np.percentile(serr, 99)), 4),
+                       "same_pose_depth_max_mm": round(float(serr.max()), 3)})
     g.sync(stream)
     a, b = g.export_blocks(with_color=False), o.export()
     row64 = {tuple(c): q for q, c in enumerate(b["coords"].tolist())}
@@ -426,6 +435,8 @@ def run_precision_form(torch, depth, P, stream, n_frames=20, launch=None):
                                  round(max(f["start_err_mm_deg"][1] for f in frames), 2)],
         "depth_vs_fp64_max_p99_mm": round(max(f["depth_p99_mm"] for f in frames), 4),
         "depth_vs_fp64_max_mm": round(max(f["depth_max_mm"] for f in frames), 3),
+        "same_pose_depth_vs_fp64_max_p99_mm": round(max(f["same_pose_depth_p99_mm"] for f in frames), 4),
+        "same_pose_depth_vs_fp64_max_mm": round(max(f["same_pose_depth_max_mm"] for f in frames), 3),
         "tsdf_vs_fp64_trunc_units": {"voxels_same_weight": int(same.sum()),
                                      "frac_observed_same_weight": round(float(same.sum() / max(obs.sum(), 1)), 5),
                                      "median": float("%.3g" % np.median(dsdf)),
