@@ -23,6 +23,7 @@ struct ss_pipeline {
     ss_pipeline_params p{};
     TrackState *st = nullptr;
     float2 *partials = nullptr;
+    unsigned long long *acc = nullptr;  // persistent tracker's fixed-point accumulators
     float4 *vmap = nullptr, *nmap = nullptr;
     uint16_t *input = nullptr;
     int ctas = 0;
@@ -83,6 +84,7 @@ ss_status enqueue_frame(ss_pipeline *P, cudaStream_t s, bool prof = false) {
     L.nmap = P->nmap;
     L.state = P->st;
     L.partials = P->partials;
+    L.acc = P->acc;
     L.persistent = P->p.persistent_track != 0;
     L.ctas = L.persistent ? P->track_ctas : P->ctas;
     L.levels = P->p.levels;
@@ -148,6 +150,7 @@ ss_status ss_pipeline_create(ss_grid *g, const ss_pipeline_params *params, ss_pi
     const size_t npix = (size_t)g->p.resi * g->p.resj;
     bool ok = cudaMalloc(&P->st, sizeof(TrackState)) == cudaSuccess &&
               cudaMalloc(&P->partials, 2 * (size_t)slot_ctas * 29 * sizeof(float2)) == cudaSuccess &&
+              cudaMalloc(&P->acc, kTrackAccWords * sizeof(unsigned long long)) == cudaSuccess &&
               cudaMalloc(&P->vmap, npix * sizeof(float4)) == cudaSuccess &&
               cudaMalloc(&P->nmap, npix * sizeof(float4)) == cudaSuccess &&
               cudaMalloc(&P->input, npix * sizeof(uint16_t)) == cudaSuccess &&
@@ -159,6 +162,7 @@ ss_status ss_pipeline_create(ss_grid *g, const ss_pipeline_params *params, ss_pi
         return SS_ERR_NOMEM;
     }
     cudaMemset(P->st, 0, sizeof(TrackState));
+    cudaMemset(P->acc, 0, kTrackAccWords * sizeof(unsigned long long));
     cudaMemset(P->vmap, 0, npix * sizeof(float4));
     cudaMemset(P->nmap, 0, npix * sizeof(float4));
     double I[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
@@ -176,6 +180,7 @@ ss_status ss_pipeline_destroy(ss_pipeline *P) {
     for (cudaEvent_t e : P->events) cudaEventDestroy(e);
     cudaFree(P->st);
     cudaFree(P->partials);
+    cudaFree(P->acc);
     cudaFree(P->vmap);
     cudaFree(P->nmap);
     cudaFree(P->input);

@@ -11,13 +11,13 @@
 // Each thread accumulates the 21 + 6 + 2 normal-equation sums in FP32 (four
 // pixels' terms by FMA, then one Kahan-compensated add per group); warps
 // combine (sum, compensation) pairs with TwoSum through shuffles, CTAs
-// through shared memory, and the CTA slots are reduced the same way in a
-// fixed order. One warp then solves the 6x6 system and
-// applies the SE(3) update in FP64 (ss_track_solve.cuh). Two launch forms:
-// one cooperative launch per frame (every CTA reduces and solves redundantly,
-// one grid barrier per iteration), or one launch per iteration (the last CTA
-// to finish solves). No host synchronisation between iterations, levels or
-// frames.
+// through shared memory. One warp then solves the 6x6 system and applies the
+// SE(3) update in FP64 (ss_track_solve.cuh). Two launch forms: one
+// cooperative launch per frame (CTA totals added exactly in fixed point with
+// integer atomics, one grid barrier per iteration, every CTA solves
+// redundantly), or one launch per iteration (CTA slots reduced with TwoSum in
+// a fixed order by the last CTA to finish, which solves). No host
+// synchronisation between iterations, levels or frames.
 #include "ss_grid_impl.cuh"
 #include "ss_track.cuh"
 #include "ss_track_solve.cuh"
@@ -283,15 +283,14 @@ __device__ __forceinline__ void track_accumulate_cam(const float4 (*cam)[256], i
     }
 }
 
-// Reduces the CTA's pairs and writes them to the value-major slots:
-// slots[value][cta]. Within a warp, a transpose-reduce (recursive halving):
-// at offset o each lane keeps the half of its remaining values selected by
-// lane bit o and trades the other half with lane ^ o, adding with TwoSum, so
-// after offsets 16, 8, 4, 2, 1 lane l holds the warp's pair of value l (31
-// exchanges per lane instead of 5 per value). Warps then combine through
-// shared memory in a fixed order.
-__device__ __forceinline__ void track_cta_to_slots(float *s, float *c, float2 (*red)[kTrackSums],
-                                                   float2 *__restrict__ slots) {
+// Reduces the CTA's pairs: thread v < kTrackSums returns the CTA's pair of
+// value v. Within a warp, a transpose-reduce (recursive halving): at offset o
+// each lane keeps the half of its remaining values selected by lane bit o and
+// trades the other half with lane ^ o, adding with TwoSum, so after offsets
+// 16, 8, 4, 2, 1 lane l holds the warp's pair of value l (31 exchanges per
+// lane instead of 5 per value). Warps then combine through shared memory in a
+// fixed order.
+__device__ __forceinline__ float2 track_cta_pairs(float *s, float *c, float2 (*red)[kTrackSums]) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     float vs[32], vc[32];
 #pragma unroll
@@ -314,11 +313,82 @@ __device__ __forceinline__ void track_cta_to_slots(float *s, float *c, float2 (*
     }
     if (lane < kTrackSums) red[wid][lane] = make_float2(vs[0], vc[0]);
     __syncthreads();
-    if (threadIdx.x < kTrackSums) {
-        float a = 0.f, b = 0.f;
+    float a = 0.f, b = 0.f;
+    if (threadIdx.x < kTrackSums)
         for (int w = 0; w < (int)(blockDim.x >> 5); w++) pair_add(a, b, red[w][threadIdx.x].x, red[w][threadIdx.x].y);
-        slots[(size_t)threadIdx.x * gridDim.x + blockIdx.x] = make_float2(a, b);
+    return make_float2(a, b);
+}
+
+// The CTA's pairs into the value-major slots: slots[value][cta].
+__device__ __forceinline__ void track_cta_to_slots(float *s, float *c, float2 (*red)[kTrackSums],
+                                                   float2 *__restrict__ slots) {
+    const float2 p = track_cta_pairs(s, c, red);
+    if (threadIdx.x < kTrackSums) slots[(size_t)threadIdx.x * gridDim.x + blockIdx.x] = p;
+}
+
+// Cross-CTA sums of the persistent tracker in fixed point: each CTA's pair
+// (sum - compensation) is converted exactly, up to a resolution of
+// 2^-kTrackFixShift, to a signed integer below 2^96 in magnitude, split into
+// three 32-bit chunks (two unsigned, the top one signed) and added with
+// 64-bit integer atomics, so the total is exact and does not depend on the
+// order in which CTAs arrive (the pose is bit-reproducible). A CTA value of
+// magnitude >= 2^47 (or NaN) is not added; it increments the overflow count
+// (value kTrackSums) instead, and the iteration keeps its pose.
+constexpr int kTrackFixShift = 48;
+constexpr double kTrackFixScale = 1.0 / (double)(1ull << kTrackFixShift);
+
+// f 2^kTrackFixShift truncated toward zero, for |f| < 2^47; false otherwise.
+__device__ __forceinline__ bool fixed_of_float(float f, __int128 &q) {
+    if (!(fabsf(f) < 0x1p47f)) return false;
+    const unsigned u = __float_as_uint(f);
+    const int ex = (int)((u >> 23) & 0xffu);
+    if (ex == 0) {  // zero or subnormal: below the resolution
+        q = 0;
+        return true;
     }
+    const unsigned long long m = (u & 0x7fffffu) | 0x800000u;  // f = m 2^(ex - 150)
+    const int sh = ex - 150 + kTrackFixShift;                  // <= 71: m 2^sh < 2^95
+    __int128 mag = 0;
+    if (sh >= 0)
+        mag = (__int128)m << sh;
+    else if (sh > -24)
+        mag = (__int128)(m >> -sh);
+    q = (u >> 31) ? -mag : mag;
+    return true;
+}
+
+__device__ __forceinline__ void track_cta_to_acc(float *s, float *c, float2 (*red)[kTrackSums],
+                                                 unsigned long long *__restrict__ acc) {
+    const float2 p = track_cta_pairs(s, c, red);
+    if (threadIdx.x < kTrackSums) {
+        __int128 qs, qc;
+        if (fixed_of_float(p.x, qs) && fixed_of_float(p.y, qc)) {
+            const __int128 v = qs - qc;
+            unsigned long long *w = acc + (size_t)threadIdx.x * kTrackAccChunks * kTrackAccStride;
+            atomicAdd(w, (unsigned long long)v & 0xffffffffull);
+            atomicAdd(w + kTrackAccStride, (unsigned long long)(v >> 32) & 0xffffffffull);
+            atomicAdd(w + 2 * kTrackAccStride, (unsigned long long)(long long)(v >> 64));
+        } else {
+            atomicAdd(acc + (size_t)kTrackSums * kTrackAccChunks * kTrackAccStride, 1ull);
+        }
+    }
+}
+
+// Value v < kTrackAccValues of a completed accumulator buffer, in FP64: the
+// chunk sums recombined exactly into a 128-bit integer, then one conversion
+// (at most two roundings).
+__device__ __forceinline__ double track_acc_value(const unsigned long long *__restrict__ acc, int v) {
+    const unsigned long long *w = acc + (size_t)v * kTrackAccChunks * kTrackAccStride;
+    const unsigned long long s0 = __ldcg(w), s1 = __ldcg(w + kTrackAccStride), s2 = __ldcg(w + 2 * kTrackAccStride);
+    const __int128 t = (__int128)(long long)s2 * ((__int128)1 << 64) + ((__int128)s1 << 32) + (__int128)s0;
+    const long long hi = (long long)(t >> 64);
+    const unsigned long long lo = (unsigned long long)t;
+    double d;
+    if (hi == ((long long)lo >> 63))
+        d = (double)(long long)lo;  // fits in 64 bits: one rounding
+    else
+        d = (double)hi * 0x1p64 + (double)lo;  // |t| >= 2^63: two roundings, relative 2^-52
+    return d * kTrackFixScale;
 }
 
 // Reduces all CTA slots into (sum, compensation) pairs, TwoSum in FP32 in a
@@ -466,18 +536,21 @@ __device__ __forceinline__ void warp_rigid_inverse_f(const double *T, float *Ti)
 // All Gauss-Newton iterations of one frame in one cooperative launch, with
 // the frame's start (model pose = current pose, its inverse; ICP start = the
 // one-shot start pose or the model pose) and end (the FramePose of the result
-// for integrate and raycast) folded in. Every CTA
-// reduces all CTA slots and solves redundantly (bit-identical results in
-// every CTA), so one grid barrier per iteration suffices; the slots are double
-// buffered so a CTA that runs ahead never overwrites slots still being read.
-// Every CTA leaves through the same exit, also after a barrier timeout; the
-// last one to leave zeroes the barrier counter for the next frame.
+// for integrate and raycast) folded in. Each CTA adds its sums to the
+// fixed-point accumulators of the iteration; after the one grid barrier of
+// the iteration every CTA reads the totals and solves redundantly
+// (bit-identical results in every CTA). Iterations rotate through three
+// accumulator buffers: the buffer of iteration k + 2 was last read before
+// barrier k, and CTA 0 zeroes it after barrier k, before it arrives at
+// barrier k + 1, after which the CTAs add into it. Every CTA leaves through
+// the same exit, also after a barrier timeout; the last one to leave zeroes
+// the barrier counter and all accumulators for the next frame.
 __global__ void __launch_bounds__(256) track_frame_kernel(const uint16_t *__restrict__ depth, int rows, int cols,
                                                           Intr in, const float4 *__restrict__ vmap,
                                                           const float4 *__restrict__ nmap, TrackState *st,
-                                                          float2 *__restrict__ slots, TrackLaunch L) {
+                                                          unsigned long long *__restrict__ acc, TrackLaunch L) {
     __shared__ float2 red[8][kTrackSums];
-    __shared__ float2 tot[kTrackSums];
+    __shared__ int last_out;
     __shared__ double Td[16];
     __shared__ float Tf[12], Pi[12];
     __shared__ int done_level;
@@ -505,7 +578,7 @@ __global__ void __launch_bounds__(256) track_frame_kernel(const uint16_t *__rest
     if (threadIdx.x < 12) Tf[threadIdx.x] = (float)Td[threadIdx.x];
     __syncthreads();
     unsigned barriers = 0;
-    int parity = 0;
+    int abuf = 0;  // accumulator buffer of this iteration
     bool alive = true;
     const int tid = blockIdx.x * blockDim.x + threadIdx.x, nthreads = gridDim.x * blockDim.x;
     for (int level = L.levels - 1; level >= 0 && alive; level--) {
@@ -532,31 +605,37 @@ __global__ void __launch_bounds__(256) track_frame_kernel(const uint16_t *__rest
                 track_accumulate(depth, rows, cols, in, vmap, nmap, T, P, level, dist2, L.rmin, L.dmax, tid, nthreads,
                                  s, c);
             SS_TT(barriers, 1);
-            float2 *buf = slots + (size_t)parity * kTrackSums * gridDim.x;
-            track_cta_to_slots(s, c, red, buf);
+            unsigned long long *buf = acc + (size_t)abuf * kTrackAccBufWords;
+            track_cta_to_acc(s, c, red, buf);
             SS_TT(barriers, 2);
             if (!grid_barrier(st, (++barriers) * gridDim.x)) {
                 alive = false;
                 break;
             }
             SS_TT(barriers - 1, 3);
-            track_slots_to_pairs(buf, tot);
-            __syncthreads();
-            SS_TT(barriers - 1, 4);
-            const float n = pair_value(tot[28]);
             if (threadIdx.x < 32) {
+                const int lane = threadIdx.x;
+                const double v = lane < kTrackAccValues ? track_acc_value(buf, lane) : 0.0;
+                const double n = __shfl_sync(0xffffffffu, v, kTrackSums - 1);
+                const double r2 = __shfl_sync(0xffffffffu, v, kTrackSums - 2);
+                const bool overflow = __shfl_sync(0xffffffffu, v, kTrackSums) != 0.0;
                 double x[6];
-                if (n >= 60.f && warp_solve6(tot, x)) {  // too few correspondences: keep the pose
+                // too few correspondences, or a sum out of range: keep the pose
+                if (n >= 60.0 && !overflow && warp_solve6_lanes(v, x)) {
                     const float step2 = warp_se3_left_update(x, Td, Td, Tf);
-                    if (threadIdx.x == 0 && step2 < 1e-14f) done_level = level;
+                    if (lane == 0 && step2 < 1e-14f) done_level = level;
                 }
-            } else if (blockIdx.x == 0 && threadIdx.x == 32) {
-                st->inliers[level] = (int)n;
-                st->rmse[level] = n > 0.f ? sqrtf(fmaxf(pair_value(tot[27]), 0.f) / n) : 0.f;
+                if (blockIdx.x == 0 && lane == 0) {
+                    st->inliers[level] = (int)n;
+                    st->rmse[level] = n > 0.0 ? sqrtf(fmaxf((float)r2, 0.f) / (float)n) : 0.f;
+                }
+            } else if (blockIdx.x == 0 && threadIdx.x < 32 + kTrackAccValues * kTrackAccChunks) {
+                const int nb = abuf == 0 ? kTrackAccBuffers - 1 : abuf - 1;  // buffer of iteration + 2
+                acc[(size_t)nb * kTrackAccBufWords + (size_t)(threadIdx.x - 32) * kTrackAccStride] = 0ull;
             }
             __syncthreads();
             SS_TT(barriers - 1, 5);
-            parity ^= 1;
+            abuf = abuf == kTrackAccBuffers - 1 ? 0 : abuf + 1;
         }
     }
     if (blockIdx.x == 0 && threadIdx.x < 32) {
@@ -580,12 +659,17 @@ __global__ void __launch_bounds__(256) track_frame_kernel(const uint16_t *__rest
     __syncthreads();
     if (threadIdx.x == 0) {
         __threadfence();
-        if (atomicAdd(&st->exits, 1u) == gridDim.x - 1) {
+        last_out = atomicAdd(&st->exits, 1u) == gridDim.x - 1;
+        if (last_out) {
             st->barrier = 0u;
             st->exits = 0u;
             st->has_start = 0;
         }
     }
+    __syncthreads();
+    if (last_out)  // every other CTA has finished its reads
+        for (int w = threadIdx.x; w < kTrackAccBuffers * kTrackAccValues * kTrackAccChunks; w += blockDim.x)
+            acc[(size_t)w * kTrackAccStride] = 0ull;
 }
 
 #ifdef SS_TRACK_TIMING
@@ -614,7 +698,7 @@ ss_status launch_track(const TrackLaunch &L, cudaStream_t s) {
         Intr in = L.in;
         const float4 *vmap = L.vmap, *nmap = L.nmap;
         TrackState *st = L.state;
-        float2 *slots = L.partials;
+        unsigned long long *acc = L.acc;
         // cooperative launch (all CTAs co-resident, so the grid barrier cannot wait
         // on a CTA that is not running); the attribute form is stream-capturable
         cudaLaunchConfig_t cfg = {};
@@ -627,7 +711,7 @@ ss_status launch_track(const TrackLaunch &L, cudaStream_t s) {
         attr[0].val.cooperative = 1;
         cfg.attrs = attr;
         cfg.numAttrs = 1;
-        SS_CUDA_TRY(cudaLaunchKernelEx(&cfg, track_frame_kernel, depth, rows, cols, in, vmap, nmap, st, slots, L));
+        SS_CUDA_TRY(cudaLaunchKernelEx(&cfg, track_frame_kernel, depth, rows, cols, in, vmap, nmap, st, acc, L));
         return SS_OK;
     }
     track_begin_kernel<<<1, 32, 0, s>>>(L.state);

@@ -27,6 +27,16 @@ struct TrackState {
     double Tstart[16];
 };
 
+// Fixed-point accumulators of the persistent tracker's cross-CTA sums: three
+// buffers (iterations rotate through them) of 30 values (29 sums and an
+// overflow count) x 3 chunks, one 128-byte line per word.
+constexpr int kTrackAccValues = 30;
+constexpr int kTrackAccChunks = 3;
+constexpr int kTrackAccStride = 16;  // u64 words between accumulator words
+constexpr int kTrackAccBuffers = 3;
+constexpr int kTrackAccBufWords = kTrackAccValues * kTrackAccChunks * kTrackAccStride;
+constexpr int kTrackAccWords = kTrackAccBuffers * kTrackAccBufWords;
+
 struct TrackLaunch {
     const uint16_t *depth;
     int rows, cols;
@@ -34,6 +44,7 @@ struct TrackLaunch {
     const float4 *vmap, *nmap;
     TrackState *state;
     float2 *partials;
+    unsigned long long *acc;  // fixed-point accumulators of the persistent tracker (kTrackAccWords, zeroed)
     int ctas;
     int levels;
     int iters[kMaxLevels];

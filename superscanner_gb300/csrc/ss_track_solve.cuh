@@ -78,23 +78,51 @@ __device__ __forceinline__ double rcp_pos(double x) {
     return scale_pow2(r, e);
 }
 
+// Index q of the normal-equation sum behind this lane's entry (i, j) of
+// [A | b]: 0..20 the upper triangle of A row-major, 21..26 J^T r.
+__device__ __forceinline__ int aug_sum_index(int i, int j) {
+    return (j < 6) ? 6 * i - ((i * (i - 1)) >> 1) + (j - i) : 21 + i;
+}
+
+// Gauss-Jordan core: lane (i, j) < kAugLanes holds entry (i, j) of [A | b]
+// in a (b = -J^T r), other lanes 0.
+__device__ __forceinline__ bool warp_solve6_aug(double a, double x[6]);
+
 // Solves A x = b in FP64 with the calling warp (all 32 lanes, converged).
 // pairs[0..20]: the upper triangle of A row-major, pairs[21..26]: J^T r (b = -J^T r),
 // each an FP32 (sum, compensation) pair with value sum - compensation.
 // Every lane returns the same x and the same verdict (false: a pivot <= kPivotMin).
 __device__ __forceinline__ bool warp_solve6(const float2 *pairs, double x[6]) {
+    const int lane = threadIdx.x & 31;
+    int i, j;
+    aug_entry(lane, i, j);
+    double a = 0.0;
+    if (lane < kAugLanes) {
+        const float2 p = pairs[aug_sum_index(i, j)];
+        a = (double)p.x - (double)p.y;
+        if (j == 6) a = -a;
+    }
+    return warp_solve6_aug(a, x);
+}
+
+// The same with the sums already in FP64, lane q < 27 of the warp holding sum q.
+__device__ __forceinline__ bool warp_solve6_lanes(double sum, double x[6]) {
+    const int lane = threadIdx.x & 31;
+    int i, j;
+    aug_entry(lane, i, j);
+    const bool live = lane < kAugLanes;
+    double a = __shfl_sync(0xffffffffu, sum, live ? aug_sum_index(i, j) : 0);
+    if (!live) a = 0.0;
+    if (j == 6) a = -a;
+    return warp_solve6_aug(a, x);
+}
+
+__device__ __forceinline__ bool warp_solve6_aug(double a, double x[6]) {
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     int i, j;
     aug_entry(lane, i, j);
     const bool live = lane < kAugLanes;
-    double a = 0.0;
-    if (live) {
-        const int q = (j < 6) ? 6 * i - ((i * (i - 1)) >> 1) + (j - i) : 21 + i;
-        const float2 p = pairs[q];
-        a = (double)p.x - (double)p.y;
-        if (j == 6) a = -a;
-    }
     bool ok = true;
 #pragma unroll
     for (int k = 0; k < 6; k++) {
