@@ -335,7 +335,7 @@ __device__ __forceinline__ void track_cta_to_slots(float *s, float *c, float2 (*
 // magnitude >= 2^47 (or NaN) is not added; it increments the overflow count
 // (value kTrackSums) instead, and the iteration keeps its pose.
 constexpr int kTrackFixShift = 48;
-constexpr double kTrackFixScale = 1.0 / (double)(1ull << kTrackFixShift);
+constexpr double kTrackFixUnit = (double)(1ull << kTrackFixShift);  // 1.0 in accumulator units
 
 // f 2^kTrackFixShift truncated toward zero, for |f| < 2^47; false otherwise.
 __device__ __forceinline__ bool fixed_of_float(float f, __int128 &q) {
@@ -374,21 +374,18 @@ __device__ __forceinline__ void track_cta_to_acc(float *s, float *c, float2 (*re
     }
 }
 
-// Value v < kTrackAccValues of a completed accumulator buffer, in FP64: the
-// chunk sums recombined exactly into a 128-bit integer, then one conversion
-// (at most two roundings).
+// Value v < kTrackAccValues of a completed accumulator buffer in FP64, in
+// units of 2^-kTrackFixShift (the caller scales or compares in those units):
+// the chunk sums recombined exactly into a 128-bit integer t = h 2^64 + l
+// with l signed, then fma(h, 2^64, l), exact for |t| < 2^63 and otherwise
+// within two roundings (relative 2^-52).
 __device__ __forceinline__ double track_acc_value(const unsigned long long *__restrict__ acc, int v) {
     const unsigned long long *w = acc + (size_t)v * kTrackAccChunks * kTrackAccStride;
     const unsigned long long s0 = __ldcg(w), s1 = __ldcg(w + kTrackAccStride), s2 = __ldcg(w + 2 * kTrackAccStride);
     const __int128 t = (__int128)(long long)s2 * ((__int128)1 << 64) + ((__int128)s1 << 32) + (__int128)s0;
-    const long long hi = (long long)(t >> 64);
-    const unsigned long long lo = (unsigned long long)t;
-    double d;
-    if (hi == ((long long)lo >> 63))
-        d = (double)(long long)lo;  // fits in 64 bits: one rounding
-    else
-        d = (double)hi * 0x1p64 + (double)lo;  // |t| >= 2^63: two roundings, relative 2^-52
-    return d * kTrackFixScale;
+    const long long l = (long long)(unsigned long long)t;  // t mod 2^64, signed
+    const long long h = (long long)((t - (__int128)l) >> 64);
+    return fma((double)h, 0x1p64, (double)l);
 }
 
 // Reduces all CTA slots into (sum, compensation) pairs, TwoSum in FP32 in a
@@ -509,18 +506,32 @@ __device__ __forceinline__ bool grid_barrier(TrackState *st, unsigned target) {
 
 #ifdef SS_TRACK_TIMING
 // Phase timestamps of CTA 0 (global timer, ns) for tuning builds only.
-__device__ unsigned long long g_track_timing[32 * 6];
+__device__ unsigned long long g_track_timing[32 * 8];
 #define SS_TT(slot, phase)                                                                     \
     do {                                                                                       \
         if (blockIdx.x == 0 && threadIdx.x == 0 && (slot) < 32) {                              \
             unsigned long long t_;                                                             \
             asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t_));                             \
-            g_track_timing[(slot) * 6 + (phase)] = t_;                                         \
+            g_track_timing[(slot) * 8 + (phase)] = t_;                                         \
         }                                                                                      \
+    } while (0)
+// Every CTA's arrival at (kind 0) and departure from (kind 1) each barrier.
+constexpr int kTimingCtas = 512;
+__device__ unsigned long long g_track_cta_timing[2 * 32 * kTimingCtas];
+#define SS_TC(slot, kind)                                                                                  \
+    do {                                                                                                   \
+        if (threadIdx.x == 0 && (slot) < 32 && blockIdx.x < kTimingCtas) {                                 \
+            unsigned long long t_;                                                                         \
+            asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t_));                                         \
+            g_track_cta_timing[((kind) * 32 + (slot)) * kTimingCtas + blockIdx.x] = t_;                    \
+        }                                                                                                  \
     } while (0)
 #else
 #define SS_TT(slot, phase) \
     do {                   \
+    } while (0)
+#define SS_TC(slot, kind) \
+    do {                  \
     } while (0)
 #endif
 
@@ -608,26 +619,35 @@ __global__ void __launch_bounds__(256) track_frame_kernel(const uint16_t *__rest
             unsigned long long *buf = acc + (size_t)abuf * kTrackAccBufWords;
             track_cta_to_acc(s, c, red, buf);
             SS_TT(barriers, 2);
+            SS_TC(barriers, 0);
             if (!grid_barrier(st, (++barriers) * gridDim.x)) {
                 alive = false;
                 break;
             }
             SS_TT(barriers - 1, 3);
+            SS_TC(barriers - 1, 1);
             if (threadIdx.x < 32) {
                 const int lane = threadIdx.x;
+                // sums in units of 2^-48: the solve is invariant under that common
+                // power-of-two scale, so only the thresholds are scaled
                 const double v = lane < kTrackAccValues ? track_acc_value(buf, lane) : 0.0;
                 const double n = __shfl_sync(0xffffffffu, v, kTrackSums - 1);
                 const double r2 = __shfl_sync(0xffffffffu, v, kTrackSums - 2);
-                const bool overflow = __shfl_sync(0xffffffffu, v, kTrackSums) != 0.0;
+                const double of = __shfl_sync(0xffffffffu, v, kTrackSums);
+                SS_TT(barriers - 1, 4);
                 double x[6];
                 // too few correspondences, or a sum out of range: keep the pose
-                if (n >= 60.0 && !overflow && warp_solve6_lanes(v, x)) {
+                if (above_pos(n, 59.5 * kTrackFixUnit) && __double_as_longlong(of) == 0 &&
+                    warp_solve6_lanes(v, x, kPivotMin * kTrackFixUnit)) {
+                    SS_TT(barriers - 1, 6);
                     const float step2 = warp_se3_left_update(x, Td, Td, Tf);
                     if (lane == 0 && step2 < 1e-14f) done_level = level;
+                    SS_TT(barriers - 1, 7);
                 }
                 if (blockIdx.x == 0 && lane == 0) {
-                    st->inliers[level] = (int)n;
-                    st->rmse[level] = n > 0.0 ? sqrtf(fmaxf((float)r2, 0.f) / (float)n) : 0.f;
+                    const float nf = (float)n;  // exact: a count below 2^24 times 2^48
+                    st->inliers[level] = (int)(nf * (float)(1.0 / kTrackFixUnit));
+                    st->rmse[level] = nf > 0.f ? sqrtf(fmaxf((float)r2, 0.f) / nf) : 0.f;
                 }
             } else if (blockIdx.x == 0 && threadIdx.x < 32 + kTrackAccValues * kTrackAccChunks) {
                 const int nb = abuf == 0 ? kTrackAccBuffers - 1 : abuf - 1;  // buffer of iteration + 2
@@ -675,6 +695,9 @@ __global__ void __launch_bounds__(256) track_frame_kernel(const uint16_t *__rest
 #ifdef SS_TRACK_TIMING
 extern "C" int ss_debug_track_timing(unsigned long long *out) {
     return (int)cudaMemcpyFromSymbol(out, g_track_timing, sizeof(g_track_timing));
+}
+extern "C" int ss_debug_track_cta_timing(unsigned long long *out) {
+    return (int)cudaMemcpyFromSymbol(out, g_track_cta_timing, sizeof(g_track_cta_timing));
 }
 #endif
 

@@ -85,8 +85,16 @@ __device__ __forceinline__ int aug_sum_index(int i, int j) {
 }
 
 // Gauss-Jordan core: lane (i, j) < kAugLanes holds entry (i, j) of [A | b]
-// in a (b = -J^T r), other lanes 0.
-__device__ __forceinline__ bool warp_solve6_aug(double a, double x[6]);
+// in a (b = -J^T r), other lanes 0. A pivot must exceed pivot_min.
+__device__ __forceinline__ bool warp_solve6_aug(double a, double x[6], double pivot_min = kPivotMin);
+
+// x > y for y >= 0 finite, x not NaN or +inf (false for those), by integer
+// comparison of the bit patterns (which order like the values for x, y >= 0;
+// negative x has the sign bit and compares below): no FP64 instruction.
+__device__ __forceinline__ bool above_pos(double x, double y) {
+    const long long bx = __double_as_longlong(x);
+    return bx > __double_as_longlong(y) && bx < 0x7ff0000000000000ll;
+}
 
 // Solves A x = b in FP64 with the calling warp (all 32 lanes, converged).
 // pairs[0..20]: the upper triangle of A row-major, pairs[21..26]: J^T r (b = -J^T r),
@@ -105,8 +113,11 @@ __device__ __forceinline__ bool warp_solve6(const float2 *pairs, double x[6]) {
     return warp_solve6_aug(a, x);
 }
 
-// The same with the sums already in FP64, lane q < 27 of the warp holding sum q.
-__device__ __forceinline__ bool warp_solve6_lanes(double sum, double x[6]) {
+// The same with the sums already in FP64, lane q < 27 of the warp holding sum
+// q, all of them scaled by one power of two 2^s: the elimination's pivot
+// splits, row scalings and reciprocals are exact under such a scaling, so x
+// comes out bit for bit as for the unscaled sums when pivot_min is scaled too.
+__device__ __forceinline__ bool warp_solve6_lanes(double sum, double x[6], double pivot_min = kPivotMin) {
     const int lane = threadIdx.x & 31;
     int i, j;
     aug_entry(lane, i, j);
@@ -114,10 +125,10 @@ __device__ __forceinline__ bool warp_solve6_lanes(double sum, double x[6]) {
     double a = __shfl_sync(0xffffffffu, sum, live ? aug_sum_index(i, j) : 0);
     if (!live) a = 0.0;
     if (j == 6) a = -a;
-    return warp_solve6_aug(a, x);
+    return warp_solve6_aug(a, x, pivot_min);
 }
 
-__device__ __forceinline__ bool warp_solve6_aug(double a, double x[6]) {
+__device__ __forceinline__ bool warp_solve6_aug(double a, double x[6], double pivot_min) {
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     int i, j;
@@ -127,7 +138,7 @@ __device__ __forceinline__ bool warp_solve6_aug(double a, double x[6]) {
 #pragma unroll
     for (int k = 0; k < 6; k++) {
         const double p = __shfl_sync(full, a, aug_lane(k, k));
-        ok = ok && (p > kPivotMin);
+        ok = ok && above_pos(p, pivot_min);
         int e;
         const double ph = split_pow2(p, e);
         const bool upd = live && i != k;
@@ -140,7 +151,7 @@ __device__ __forceinline__ bool warp_solve6_aug(double a, double x[6]) {
     }
     // row i is now u_ii x_i = c_i: reciprocals on the diagonal lanes, x_i on lanes (i, 6)
     const bool diag = live && i == j;
-    const double r = rcp_pos(diag && a > kPivotMin ? a : 1.0);
+    const double r = rcp_pos(diag && above_pos(a, pivot_min) ? a : 1.0);
     const bool rhs = live && j == 6;
     const double rii = __shfl_sync(full, r, rhs ? aug_lane(i, i) : 0);
     const double xl = a * rii;
@@ -162,7 +173,7 @@ __device__ __forceinline__ float warp_se3_left_update(const double xi[6], const 
     // lane s = lane % 3 evaluates series s: A = sin t / t, B = (1 - cos t) / t^2, C = (t - sin t) / t^3
     const int s = lane % 3;
     double coef;
-    if (th2 < 0.0025) {
+    if (!above_pos(th2, 0.0025)) {  // th2 <= 0.0025 (th2 >= 0)
         // Maclaurin series to t^8: the first omitted term is below 3e-21 for t < 0.05
         const double c4 = s == 0 ? 1.0 / 362880 : (s == 1 ? 1.0 / 3628800 : 1.0 / 39916800);
         const double c3 = s == 0 ? -1.0 / 5040 : (s == 1 ? -1.0 / 40320 : -1.0 / 362880);
@@ -201,9 +212,14 @@ __device__ __forceinline__ float warp_se3_left_update(const double xi[6], const 
         Tout[lane] = nv;
         Tfout[lane] = (float)nv;
     }
-    float n2 = 0.f;
-#pragma unroll
-    for (int k = 0; k < 6; k++) n2 = fmaf((float)xi[k], (float)xi[k], n2);
+    // |xi|^2 in FP32: lane k < 6 converts xi[k], then a sum over 8 lanes
+    const int k6 = lane & 7;
+    const double xk = k6 == 0 ? xi[0] : k6 == 1 ? xi[1] : k6 == 2 ? xi[2] : k6 == 3 ? xi[3] : k6 == 4 ? xi[4] : xi[5];
+    const float xf = k6 < 6 ? (float)xk : 0.f;
+    float n2 = xf * xf;
+    n2 += __shfl_xor_sync(full, n2, 1);
+    n2 += __shfl_xor_sync(full, n2, 2);
+    n2 += __shfl_xor_sync(full, n2, 4);
     return n2;
 }
 
