@@ -23,8 +23,9 @@
 //   (r <- r + r (1 - m r); the relative error squares each step, 2^-23 ->
 //   2^-46 -> below FP64 rounding);
 // * SE(3) exponential by Maclaurin series of sin t / t, (1 - cos t) / t^2,
-//   (t - sin t) / t^3 (one series per lane), R and V entries one per lane,
-//   then the pose product R T + V upsilon one entry per lane.
+//   (t - sin t) / t^3 (one series per lane, as many terms as th2 needs), and
+//   the pose product R T + V upsilon from one set of lane-parallel dot
+//   products (K T, omega^T T, K upsilon, ...), one entry per lane.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -160,61 +161,90 @@ __device__ __forceinline__ bool warp_solve6_aug(double a, double x[6], double pi
     return ok;
 }
 
+// Series coefficient s of the SE(3) exponential at th2 = |omega|^2:
+// s = 0: A = sin t / t, 1: B = (1 - cos t) / t^2, 2: C = (t - sin t) / t^3.
+// Maclaurin series cut where the first omitted term of A (the largest of
+// the three) is below 1e-17: 2 terms for th2 < 3.4e-8, 3 below 3.7e-5, 4
+// below 1.38e-3, 5 below 2.5e-3; sin and cos beyond. Each branch also
+// evaluates the caller's independent product k2 = fma(p, q, -(th2 y)) so that
+// its FP64 instructions overlap the series' dependent chain.
+__device__ __forceinline__ double se3_series(int s, double th2, double p, double q, double y, double &k2) {
+    const double c4 = s == 0 ? 1.0 / 362880 : (s == 1 ? 1.0 / 3628800 : 1.0 / 39916800);
+    const double c3 = s == 0 ? -1.0 / 5040 : (s == 1 ? -1.0 / 40320 : -1.0 / 362880);
+    const double c2 = s == 0 ? 1.0 / 120 : (s == 1 ? 1.0 / 720 : 1.0 / 5040);
+    const double c1 = s == 0 ? -1.0 / 6 : (s == 1 ? -1.0 / 24 : -1.0 / 120);
+    const double c0 = s == 0 ? 1.0 : (s == 1 ? 0.5 : 1.0 / 6);
+    if (!above_pos(th2, 3.4e-8)) {
+        k2 = fma(p, q, -(th2 * y));
+        return fma(c1, th2, c0);
+    }
+    if (!above_pos(th2, 3.7e-5)) {
+        k2 = fma(p, q, -(th2 * y));
+        return fma(fma(c2, th2, c1), th2, c0);
+    }
+    if (!above_pos(th2, 1.38e-3)) {
+        k2 = fma(p, q, -(th2 * y));
+        return fma(fma(fma(c3, th2, c2), th2, c1), th2, c0);
+    }
+    k2 = fma(p, q, -(th2 * y));
+    if (!above_pos(th2, 0.0025)) return fma(fma(fma(fma(c4, th2, c3), th2, c2), th2, c1), th2, c0);
+    const double th = sqrt(th2), sn = sin(th), cs = cos(th);
+    return s == 0 ? sn / th : (s == 1 ? (1.0 - cs) / th2 : (th - sn) / (th2 * th));
+}
+
 // T <- exp(xi) T (left increment, xi = (omega, upsilon)) in FP64 with the calling
 // warp. Tin: 12 doubles (rows of [R | t]); Tout (12 doubles) and Tfout (12 floats)
 // are written by lanes 0..11 and may alias Tin only if the caller syncs the warp
 // before reading them. Returns |xi|^2 (FP32, every lane).
+//
+// With K = [omega]x, K^2 = omega omega^T - th2 I and exp(xi) = [R | V upsilon],
+// R = I + A K + B K^2, V = I + B K + C K^2:
+//   R T = T + A (K T) + B (omega (omega^T T) - th2 T),
+//   V upsilon = upsilon + B (K upsilon) + C (omega (omega . upsilon) - th2 upsilon),
+// so one set of three-term dot products (K T, omega^T T, K upsilon,
+// omega . upsilon and th2 in different lanes) feeds everything, and the
+// dependent FP64 chain is: dot products (3), the series overlapped with the
+// K^2 terms (1 to 4), two FMAs, one add.
 __device__ __forceinline__ float warp_se3_left_update(const double xi[6], const double *Tin, double *Tout,
                                                       float *Tfout) {
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
-    const double wx = xi[0], wy = xi[1], wz = xi[2];
-    const double th2 = fma(wx, wx, fma(wy, wy, wz * wz));
-    // lane s = lane % 3 evaluates series s: A = sin t / t, B = (1 - cos t) / t^2, C = (t - sin t) / t^3
-    const int s = lane % 3;
-    double coef;
-    if (!above_pos(th2, 0.0025)) {  // th2 <= 0.0025 (th2 >= 0)
-        // Maclaurin series to t^8: the first omitted term is below 3e-21 for t < 0.05
-        const double c4 = s == 0 ? 1.0 / 362880 : (s == 1 ? 1.0 / 3628800 : 1.0 / 39916800);
-        const double c3 = s == 0 ? -1.0 / 5040 : (s == 1 ? -1.0 / 40320 : -1.0 / 362880);
-        const double c2 = s == 0 ? 1.0 / 120 : (s == 1 ? 1.0 / 720 : 1.0 / 5040);
-        const double c1 = s == 0 ? -1.0 / 6 : (s == 1 ? -1.0 / 24 : -1.0 / 120);
-        const double c0 = s == 0 ? 1.0 : (s == 1 ? 0.5 : 1.0 / 6);
-        coef = fma(fma(fma(fma(c4, th2, c3), th2, c2), th2, c1), th2, c0);
-    } else {
-        const double th = sqrt(th2), sn = sin(th), cs = cos(th);
-        coef = s == 0 ? sn / th : (s == 1 ? (1.0 - cs) / th2 : (th - sn) / (th2 * th));
-    }
+    const double wx = xi[0], wy = xi[1], wz = xi[2], ux = xi[3], uy = xi[4], uz = xi[5];
+    // lanes 0..11: (r, c) = (lane / 4, lane % 4) of K T; 12..15: column c of omega^T T;
+    // 16..18: row r of K upsilon; 19: omega . upsilon; 20: th2
+    const bool nl = lane < 12, ul = lane >= 16 && lane < 19;
+    const int r = nl ? (lane >> 2) : (ul ? lane - 16 : 0), c = lane & 3;
+    // row r of K: (0, -wz, wy), (wz, 0, -wx), (-wy, wx, 0)
+    const bool krow = nl || ul;
+    const double a0 = krow ? (r == 0 ? 0.0 : (r == 1 ? wz : -wy)) : wx;
+    const double a1 = krow ? (r == 0 ? -wz : (r == 1 ? 0.0 : wx)) : wy;
+    const double a2 = krow ? (r == 0 ? wy : (r == 1 ? -wx : 0.0)) : wz;
+    const bool tcol = lane < 16;
+    const double b0 = tcol ? Tin[c] : (lane == 20 ? wx : ux);
+    const double b1 = tcol ? Tin[4 + c] : (lane == 20 ? wy : uy);
+    const double b2 = tcol ? Tin[8 + c] : (lane == 20 ? wz : uz);
+    const double d = fma(a2, b2, fma(a1, b1, a0 * b0));
+    const double th2 = __shfl_sync(full, d, 20);
+    const double wu = __shfl_sync(full, d, 19);
+    const double wtt = __shfl_sync(full, d, 12 + c);
+    // K^2 term of this lane: omega_r X - th2 Y, with (X, Y) = ((omega^T T)_c, T_rc) or (omega . upsilon, upsilon_r)
+    const double wr = r == 0 ? wx : (r == 1 ? wy : wz);
+    const double Y = nl ? Tin[4 * r + c] : (r == 0 ? ux : (r == 1 ? uy : uz));
+    const double X = nl ? wtt : wu;
+    double k2;
+    const double coef = se3_series(lane % 3, th2, wr, X, Y, k2);
     const double A = __shfl_sync(full, coef, 0), B = __shfl_sync(full, coef, 1), C = __shfl_sync(full, coef, 2);
-    // lanes 0..8: R = I + A K + B K^2; lanes 9..17: V = I + B K + C K^2 (K = [omega]x,
-    // K^2 = w w^T - t^2 I); entry (r, c) = ((lane % 9) / 3, lane % 3)
-    const int e9 = lane % 9, r = e9 / 3, cc = e9 % 3;
-    const double wr = r == 0 ? wx : (r == 1 ? wy : wz), wc = cc == 0 ? wx : (cc == 1 ? wy : wz);
-    const int wk = 3 - r - cc;  // index of the omega component in K[r][c] for r != c
-    const double wkv = wk == 0 ? wx : (wk == 1 ? wy : wz);
-    // K[r][c] = -eps(r, c, k) w_k: K01 = -wz, K02 = wy, K10 = wz, K12 = -wx, K20 = -wy, K21 = wx
-    const bool pos = (r == 1 && cc == 0) || (r == 0 && cc == 2) || (r == 2 && cc == 1);
-    const double kv = r == cc ? 0.0 : (pos ? wkv : -wkv);
-    const double k2 = fma(wr, wc, r == cc ? -th2 : 0.0);
-    const bool isR = lane < 9;
-    const double m = fma(isR ? B : C, k2, fma(isR ? A : B, kv, r == cc ? 1.0 : 0.0));
-    // lanes 0..11: N(r, c) = sum_m R(r, m) T(m, c); lanes 12..14: t_r = sum_m V(r, m) upsilon_m
-    const bool nl = lane < 12, tl = lane >= 12 && lane < 15;
-    const int nr = nl ? (lane >> 2) : (tl ? lane - 12 : 0), nc = lane & 3;
-    const double m0 = __shfl_sync(full, m, (tl ? 9 : 0) + 3 * nr + 0);
-    const double m1 = __shfl_sync(full, m, (tl ? 9 : 0) + 3 * nr + 1);
-    const double m2 = __shfl_sync(full, m, (tl ? 9 : 0) + 3 * nr + 2);
-    const double o0 = nl ? Tin[nc] : xi[3], o1 = nl ? Tin[4 + nc] : xi[4], o2 = nl ? Tin[8 + nc] : xi[5];
-    double nv = fma(m0, o0, fma(m1, o1, m2 * o2));
-    const double tr = __shfl_sync(full, nv, 12 + (nr < 3 ? nr : 0));
-    if (nl && nc == 3) nv += tr;
+    // lanes 0..11: (R T)_rc = T_rc + A (K T)_rc + B (K^2 T)_rc; lanes 16..18: (V upsilon)_r
+    double nv = fma(nl ? B : C, k2, fma(nl ? A : B, d, Y));
+    const double tr = __shfl_sync(full, nv, 16 + (nl ? r : 0));
+    if (nl && c == 3) nv += tr;
     if (nl) {
         Tout[lane] = nv;
         Tfout[lane] = (float)nv;
     }
     // |xi|^2 in FP32: lane k < 6 converts xi[k], then a sum over 8 lanes
     const int k6 = lane & 7;
-    const double xk = k6 == 0 ? xi[0] : k6 == 1 ? xi[1] : k6 == 2 ? xi[2] : k6 == 3 ? xi[3] : k6 == 4 ? xi[4] : xi[5];
+    const double xk = k6 == 0 ? wx : k6 == 1 ? wy : k6 == 2 ? wz : k6 == 3 ? ux : k6 == 4 ? uy : uz;
     const float xf = k6 < 6 ? (float)xk : 0.f;
     float n2 = xf * xf;
     n2 += __shfl_xor_sync(full, n2, 1);
