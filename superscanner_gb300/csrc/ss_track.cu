@@ -332,10 +332,24 @@ __device__ __forceinline__ void track_cta_to_slots(float *s, float *c, float2 (*
 // three 32-bit chunks (two unsigned, the top one signed) and added with
 // 64-bit integer atomics, so the total is exact and does not depend on the
 // order in which CTAs arrive (the pose is bit-reproducible). A CTA value of
-// magnitude >= 2^47 (or NaN) is not added; it increments the overflow count
+// magnitude >= 2^47 (or NaN) is not added; it counts in the overflow word
 // (value kTrackSums) instead, and the iteration keeps its pose.
+//
+// Each atomic also adds 2^48, so every word counts its own contributions
+// and no separate grid barrier is needed: a reader waits until each of its
+// words has grown by gridDim.x contributions since it last read that buffer
+// (a CTA's chunks add less than 2^41 per use, so the count field is exact).
+// The words only grow during a frame (wrapping mod 2^64); readers take the
+// difference to the value they read at the buffer's previous use. That is
+// safe with three buffers in rotation: a CTA adds to iteration k + 3's use
+// of a buffer only after it has read iteration k + 2, which needs every
+// CTA's iteration-(k + 2) contribution, which each CTA makes only after it
+// has read iteration k. The last CTA to leave zeroes the words for the next
+// frame.
 constexpr int kTrackFixShift = 48;
 constexpr double kTrackFixUnit = (double)(1ull << kTrackFixShift);  // 1.0 in accumulator units
+constexpr int kTrackCountShift = 48;
+constexpr unsigned long long kTrackCountOne = 1ull << kTrackCountShift;
 
 // f 2^kTrackFixShift truncated toward zero, for |f| < 2^47; false otherwise.
 __device__ __forceinline__ bool fixed_of_float(float f, __int128 &q) {
@@ -357,35 +371,87 @@ __device__ __forceinline__ bool fixed_of_float(float f, __int128 &q) {
     return true;
 }
 
+// The CTA's totals into the counted words of one buffer: lane v < kTrackSums
+// of warp 0 adds value v, lane kTrackSums the CTA's overflow count; every
+// one of the buffer's words receives exactly one atomic per CTA.
 __device__ __forceinline__ void track_cta_to_acc(float *s, float *c, float2 (*red)[kTrackSums],
                                                  unsigned long long *__restrict__ acc) {
     const float2 p = track_cta_pairs(s, c, red);
-    if (threadIdx.x < kTrackSums) {
-        __int128 qs, qc;
-        if (fixed_of_float(p.x, qs) && fixed_of_float(p.y, qc)) {
-            const __int128 v = qs - qc;
-            unsigned long long *w = acc + (size_t)threadIdx.x * kTrackAccChunks * kTrackAccStride;
-            atomicAdd(w, (unsigned long long)v & 0xffffffffull);
-            atomicAdd(w + kTrackAccStride, (unsigned long long)(v >> 32) & 0xffffffffull);
-            atomicAdd(w + 2 * kTrackAccStride, (unsigned long long)(long long)(v >> 64));
-        } else {
-            atomicAdd(acc + (size_t)kTrackSums * kTrackAccChunks * kTrackAccStride, 1ull);
+    if (threadIdx.x < 32) {
+        const int v = threadIdx.x;
+        __int128 qs = 0, qc = 0;
+        const bool ok = v < kTrackSums && fixed_of_float(p.x, qs) && fixed_of_float(p.y, qc);
+        const unsigned bad = __ballot_sync(0xffffffffu, v < kTrackSums && !ok);
+        if (v < kTrackAccValues) {
+            unsigned long long c0 = 0, c1 = 0, c2 = 0;
+            if (ok) {
+                const __int128 q = qs - qc;
+                c0 = (unsigned long long)q & 0xffffffffull;
+                c1 = (unsigned long long)(q >> 32) & 0xffffffffull;
+                c2 = (unsigned long long)(long long)(q >> 64);
+            }
+            if (v == kTrackSums) c0 = (unsigned long long)__popc(bad);
+            unsigned long long *w = acc + (size_t)v * kTrackAccChunks * kTrackAccStride;
+            atomicAdd(w, c0 + kTrackCountOne);
+            atomicAdd(w + kTrackAccStride, c1 + kTrackCountOne);
+            atomicAdd(w + 2 * kTrackAccStride, c2 + kTrackCountOne);
         }
     }
 }
 
-// Value v < kTrackAccValues of a completed accumulator buffer in FP64, in
-// units of 2^-kTrackFixShift (the caller scales or compares in those units):
-// the chunk sums recombined exactly into a 128-bit integer t = h 2^64 + l
-// with l signed, then fma(h, 2^64, l), exact for |t| < 2^63 and otherwise
-// within two roundings (relative 2^-52).
-__device__ __forceinline__ double track_acc_value(const unsigned long long *__restrict__ acc, int v) {
-    const unsigned long long *w = acc + (size_t)v * kTrackAccChunks * kTrackAccStride;
-    const unsigned long long s0 = __ldcg(w), s1 = __ldcg(w + kTrackAccStride), s2 = __ldcg(w + 2 * kTrackAccStride);
-    const __int128 t = (__int128)(long long)s2 * ((__int128)1 << 64) + ((__int128)s1 << 32) + (__int128)s0;
-    const long long l = (long long)(unsigned long long)t;  // t mod 2^64, signed
-    const long long h = (long long)((t - (__int128)l) >> 64);
-    return fma((double)h, 0x1p64, (double)l);
+__device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long *p) {
+    unsigned long long v;
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Warp 0: waits until all words of a buffer hold gridDim.x new contributions
+// (relaxed loads, back-off, at most 2^22 polls: about a second), then returns
+// in lane v < kTrackAccValues value v of this use in FP64, in units of
+// 2^-kTrackFixShift (the chunk increments recombined exactly into a 128-bit
+// integer t = h 2^64 + l with l signed, then fma(h, 2^64, l): exact for
+// |t| < 2^63, else within two roundings). prev: the buffer's 90 words as read
+// at its previous use (shared), updated here. False on timeout.
+__device__ __forceinline__ bool track_acc_wait(const unsigned long long *__restrict__ acc, unsigned long long *prev,
+                                               double &value) {
+    const int v = threadIdx.x & 31;
+    const bool mine = v < kTrackAccValues;
+    const unsigned long long *w = acc + (size_t)(mine ? v : 0) * kTrackAccChunks * kTrackAccStride;
+    const unsigned long long p0 = mine ? prev[3 * v] : 0ull, p1 = mine ? prev[3 * v + 1] : 0ull,
+                             p2 = mine ? prev[3 * v + 2] : 0ull;
+    const unsigned long long want = (unsigned long long)gridDim.x;
+    unsigned long long w0 = 0, w1 = 0, w2 = 0;
+    bool done = false;
+    int spins = 0;
+    do {
+        if (mine) {
+            w0 = ld_relaxed_u64(w);
+            w1 = ld_relaxed_u64(w + kTrackAccStride);
+            w2 = ld_relaxed_u64(w + 2 * kTrackAccStride);
+        }
+        const unsigned long long half = 1ull << (kTrackCountShift - 1);
+        const bool complete = !mine || (((w0 - p0 + half) >> kTrackCountShift) == want &&
+                                        ((w1 - p1 + half) >> kTrackCountShift) == want &&
+                                        ((w2 - p2 + half) >> kTrackCountShift) == want);
+        done = __all_sync(0xffffffffu, complete);
+        if (done) break;
+        __nanosleep(32);
+    } while (++spins < (1 << 22));
+    if (!done) return false;
+    value = 0.0;
+    if (mine) {
+        prev[3 * v] = w0;
+        prev[3 * v + 1] = w1;
+        prev[3 * v + 2] = w2;
+        const unsigned long long counted = want << kTrackCountShift;
+        const long long s0 = (long long)(w0 - p0 - counted), s1 = (long long)(w1 - p1 - counted),
+                        s2 = (long long)(w2 - p2 - counted);
+        const __int128 t = (__int128)s2 * ((__int128)1 << 64) + (__int128)s1 * ((__int128)1 << 32) + (__int128)s0;
+        const long long l = (long long)(unsigned long long)t;  // t mod 2^64, signed
+        const long long h = (long long)((t - (__int128)l) >> 64);
+        value = fma((double)h, 0x1p64, (double)l);
+    }
+    return true;
 }
 
 // Reduces all CTA slots into (sum, compensation) pairs, TwoSum in FP32 in a
@@ -479,31 +545,6 @@ __global__ void __launch_bounds__(256) track_iter_kernel(const uint16_t *__restr
     }
 }
 
-// Bounded grid barrier of the cooperative tracker: arrival count, spin with
-// back-off up to a cap (about a second), then an error flag instead of a hang.
-__device__ __forceinline__ bool grid_barrier(TrackState *st, unsigned target) {
-    __syncthreads();
-    __shared__ int ok;
-    if (threadIdx.x == 0) {
-        __threadfence();
-        atomicAdd(&st->barrier, 1u);
-        ok = 1;
-        unsigned seen;
-        int spins = 0;
-        do {
-            asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(seen) : "l"(&st->barrier) : "memory");
-            if (seen >= target) break;
-            __nanosleep(64);
-        } while (++spins < (1 << 24));
-        if (seen < target) {
-            atomicOr(&st->status, kStTimeout);
-            ok = 0;
-        }
-    }
-    __syncthreads();
-    return ok != 0;
-}
-
 #ifdef SS_TRACK_TIMING
 // Phase timestamps of CTA 0 (global timer, ns) for tuning builds only.
 __device__ unsigned long long g_track_timing[32 * 8];
@@ -548,14 +589,12 @@ __device__ __forceinline__ void warp_rigid_inverse_f(const double *T, float *Ti)
 // the frame's start (model pose = current pose, its inverse; ICP start = the
 // one-shot start pose or the model pose) and end (the FramePose of the result
 // for integrate and raycast) folded in. Each CTA adds its sums to the
-// fixed-point accumulators of the iteration; after the one grid barrier of
-// the iteration every CTA reads the totals and solves redundantly
-// (bit-identical results in every CTA). Iterations rotate through three
-// accumulator buffers: the buffer of iteration k + 2 was last read before
-// barrier k, and CTA 0 zeroes it after barrier k, before it arrives at
-// barrier k + 1, after which the CTAs add into it. Every CTA leaves through
-// the same exit, also after a barrier timeout; the last one to leave zeroes
-// the barrier counter and all accumulators for the next frame.
+// counted fixed-point accumulators of the iteration (three buffers in
+// rotation); warp 0 of every CTA waits until the iteration's words are
+// complete, reads the totals and solves redundantly (bit-identical results
+// in every CTA), so no other grid-wide synchronisation is needed. Every CTA
+// leaves through the same exit, also after a wait timeout; the last one to
+// leave zeroes the accumulators for the next frame.
 __global__ void __launch_bounds__(256) track_frame_kernel(const uint16_t *__restrict__ depth, int rows, int cols,
                                                           Intr in, const float4 *__restrict__ vmap,
                                                           const float4 *__restrict__ nmap, TrackState *st,
@@ -564,10 +603,16 @@ __global__ void __launch_bounds__(256) track_frame_kernel(const uint16_t *__rest
     __shared__ int last_out;
     __shared__ double Td[16];
     __shared__ float Tf[12], Pi[12];
-    __shared__ int done_level;
+    __shared__ int done_level, abort_run;
+    __shared__ unsigned long long prevw[kTrackAccBuffers][kTrackAccValues * kTrackAccChunks];
     __shared__ float4 cam[kCamCache][256];
     if (threadIdx.x < 16) Td[threadIdx.x] = st->T[threadIdx.x];
-    if (threadIdx.x == 0) done_level = -1;
+    if (threadIdx.x == 0) {
+        done_level = -1;
+        abort_run = 0;
+    }
+    for (int w = threadIdx.x; w < kTrackAccBuffers * kTrackAccValues * kTrackAccChunks; w += blockDim.x)
+        (&prevw[0][0])[w] = 0ull;  // the words are zero at the start of a frame
     __syncthreads();
     if (threadIdx.x < 32) {
         // the model maps were raycast at the current pose: Tprev = T
@@ -620,17 +665,19 @@ __global__ void __launch_bounds__(256) track_frame_kernel(const uint16_t *__rest
             track_cta_to_acc(s, c, red, buf);
             SS_TT(barriers, 2);
             SS_TC(barriers, 0);
-            if (!grid_barrier(st, (++barriers) * gridDim.x)) {
-                alive = false;
-                break;
-            }
-            SS_TT(barriers - 1, 3);
-            SS_TC(barriers - 1, 1);
-            if (threadIdx.x < 32) {
+            barriers++;
+            double v = 0.0;
+            if (threadIdx.x < 32 && !track_acc_wait(buf, prevw[abuf], v)) {
+                if (threadIdx.x == 0) {
+                    abort_run = 1;
+                    atomicOr(&st->status, kStTimeout);
+                }
+            } else if (threadIdx.x < 32) {
+                SS_TT(barriers - 1, 3);
+                SS_TC(barriers - 1, 1);
                 const int lane = threadIdx.x;
                 // sums in units of 2^-48: the solve is invariant under that common
                 // power-of-two scale, so only the thresholds are scaled
-                const double v = lane < kTrackAccValues ? track_acc_value(buf, lane) : 0.0;
                 const double n = __shfl_sync(0xffffffffu, v, kTrackSums - 1);
                 const double r2 = __shfl_sync(0xffffffffu, v, kTrackSums - 2);
                 const double of = __shfl_sync(0xffffffffu, v, kTrackSums);
@@ -649,12 +696,13 @@ __global__ void __launch_bounds__(256) track_frame_kernel(const uint16_t *__rest
                     st->inliers[level] = (int)(nf * (float)(1.0 / kTrackFixUnit));
                     st->rmse[level] = nf > 0.f ? sqrtf(fmaxf((float)r2, 0.f) / nf) : 0.f;
                 }
-            } else if (blockIdx.x == 0 && threadIdx.x < 32 + kTrackAccValues * kTrackAccChunks) {
-                const int nb = abuf == 0 ? kTrackAccBuffers - 1 : abuf - 1;  // buffer of iteration + 2
-                acc[(size_t)nb * kTrackAccBufWords + (size_t)(threadIdx.x - 32) * kTrackAccStride] = 0ull;
             }
             __syncthreads();
             SS_TT(barriers - 1, 5);
+            if (abort_run) {
+                alive = false;
+                break;
+            }
             abuf = abuf == kTrackAccBuffers - 1 ? 0 : abuf + 1;
         }
     }
