@@ -340,14 +340,21 @@ ss_status ss_pipeline_get_pose(ss_pipeline *p, double T[16], ss_stream_t s);
 /* Enqueues a copy of the current pose into T (pinned host or device memory)
  * on s without synchronising; valid once s reaches that point. */
 ss_status ss_pipeline_read_pose(ss_pipeline *p, double T[16], ss_stream_t s);
-/* Device input buffer [resi][resj] u16; frames written there need no copy. */
+/* Device input buffer [resi][resj] u16; frames written there need no copy.
+ * It is also one of the two buffers host frames are uploaded into, so a
+ * caller that writes frames there should pass only such frames. */
 ss_status ss_pipeline_input(ss_pipeline *p, uint16_t **depth);
 /* Device model maps of the last frame (layout of ss_raycast_maps). */
 ss_status ss_pipeline_maps(ss_pipeline *p, float **vertex_depth, float **normal);
 /* One frame: if track != 0 and a model exists, track the frame against the
  * last model view, then integrate at the pose and raycast the model view at
  * it; else integrate at the current pose and raycast. depth may be a device
- * or host pointer (copied into the input buffer on s). No host sync. */
+ * or host pointer. A host frame (pinned for an asynchronous upload) is
+ * uploaded on an internal copy stream into one of two input buffers as soon
+ * as the frame before last has finished with it, overlapping the previous
+ * frame's kernels; s waits for the upload, so the frame must be complete
+ * when this is called and stay unchanged until s has passed it. Another
+ * device pointer is copied on s. No host sync. */
 ss_status ss_pipeline_frame(ss_pipeline *p, const uint16_t *depth, int32_t track, ss_stream_t s);
 /* Copies the model maps into caller buffers (device or host), stream-ordered. */
 ss_status ss_pipeline_copy_maps(ss_pipeline *p, float *vertex_depth, float *normal, ss_stream_t s);

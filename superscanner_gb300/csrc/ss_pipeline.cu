@@ -25,13 +25,20 @@ struct ss_pipeline {
     float2 *partials = nullptr;
     unsigned long long *acc = nullptr;  // persistent tracker's fixed-point accumulators
     float4 *vmap = nullptr, *nmap = nullptr;
-    uint16_t *input = nullptr;
+    // Two input buffers: a host frame is uploaded into one on the copy stream
+    // while the previous frame's kernels still read the other.
+    uint16_t *input = nullptr;  // inbuf[0], the buffer ss_pipeline_input hands out
+    uint16_t *inbuf[2] = {nullptr, nullptr};
+    int next_buf = 0;
+    cudaStream_t copy = nullptr;
+    cudaEvent_t ev_done[2] = {nullptr, nullptr};    // the last frame that read inbuf[b] has finished
+    cudaEvent_t ev_copied[2] = {nullptr, nullptr};  // the upload into inbuf[b] has finished
     int ctas = 0;
     int track_ctas = 0;  // co-resident CTAs of the persistent tracker
     bool have_model = false;
     cudaStream_t cap = nullptr;
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t exec = nullptr;
+    cudaGraph_t graph[2] = {nullptr, nullptr};  // one tracked frame reading inbuf[b]
+    cudaGraphExec_t exec[2] = {nullptr, nullptr};
     unsigned long long frames = 0;
     // stage profiling (non-graph frames only): 6 events per tracked frame
     bool profile = false;
@@ -55,28 +62,28 @@ cudaEvent_t next_event(ss_pipeline *P) {
 
 namespace {
 
-ss_status enqueue_fuse_raycast(ss_pipeline *P, cudaStream_t s, bool prof = false) {
+ss_status enqueue_fuse_raycast(ss_pipeline *P, const uint16_t *in, cudaStream_t s, bool prof = false) {
     ss_grid *g = P->g;
     FramePose dummy{};
     cudaEvent_t e1 = prof ? next_event(P) : nullptr, e2 = prof ? next_event(P) : nullptr;
-    ss_status st = launch_fuse(g, P->input, nullptr, dummy, &P->st->pose, false, false, P->p.exact_fusion != 0, s,
+    ss_status st = launch_fuse(g, in, nullptr, dummy, &P->st->pose, false, false, P->p.exact_fusion != 0, s,
                                /*manage_epoch=*/false, e1, e2);
     if (st != SS_OK) return st;
     if (prof) SS_CUDA_TRY(cudaEventRecord(next_event(P), s));
     const bool hint = P->p.hint_margin > 0.f;
     st = launch_raycast_maps(g, dummy.E, &P->st->pose, P->p.raycast_steps, P->p.t_min, P->p.t_max, P->vmap,
-                             P->nmap, s, prof ? P->rc_counters : nullptr, hint ? P->input : nullptr,
+                             P->nmap, s, prof ? P->rc_counters : nullptr, hint ? in : nullptr,
                              P->p.hint_margin);
     if (st != SS_OK) return st;
     if (prof) SS_CUDA_TRY(cudaEventRecord(next_event(P), s));
     return SS_OK;
 }
 
-ss_status enqueue_frame(ss_pipeline *P, cudaStream_t s, bool prof = false) {
+ss_status enqueue_frame(ss_pipeline *P, const uint16_t *in, cudaStream_t s, bool prof = false) {
     ss_grid *g = P->g;
     if (prof) SS_CUDA_TRY(cudaEventRecord(next_event(P), s));
     TrackLaunch L{};
-    L.depth = P->input;
+    L.depth = in;
     L.rows = g->p.resi;
     L.cols = g->p.resj;
     L.in = g->v.in;
@@ -97,7 +104,7 @@ ss_status enqueue_frame(ss_pipeline *P, cudaStream_t s, bool prof = false) {
     ss_status st = launch_track(L, s);
     if (st != SS_OK) return st;
     if (prof) SS_CUDA_TRY(cudaEventRecord(next_event(P), s));
-    return enqueue_fuse_raycast(P, s, prof);
+    return enqueue_fuse_raycast(P, in, s, prof);
 }
 
 // The epoch advances once per executed integrate; rebase before it wraps.
@@ -153,9 +160,16 @@ ss_status ss_pipeline_create(ss_grid *g, const ss_pipeline_params *params, ss_pi
               cudaMalloc(&P->acc, kTrackAccWords * sizeof(unsigned long long)) == cudaSuccess &&
               cudaMalloc(&P->vmap, npix * sizeof(float4)) == cudaSuccess &&
               cudaMalloc(&P->nmap, npix * sizeof(float4)) == cudaSuccess &&
-              cudaMalloc(&P->input, npix * sizeof(uint16_t)) == cudaSuccess &&
+              cudaMalloc(&P->inbuf[0], npix * sizeof(uint16_t)) == cudaSuccess &&
+              cudaMalloc(&P->inbuf[1], npix * sizeof(uint16_t)) == cudaSuccess &&
+              cudaStreamCreateWithFlags(&P->copy, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaEventCreateWithFlags(&P->ev_done[0], cudaEventDisableTiming) == cudaSuccess &&
+              cudaEventCreateWithFlags(&P->ev_done[1], cudaEventDisableTiming) == cudaSuccess &&
+              cudaEventCreateWithFlags(&P->ev_copied[0], cudaEventDisableTiming) == cudaSuccess &&
+              cudaEventCreateWithFlags(&P->ev_copied[1], cudaEventDisableTiming) == cudaSuccess &&
               cudaMalloc(&P->rc_counters, 4 * sizeof(unsigned long long)) == cudaSuccess &&
               cudaStreamCreateWithFlags(&P->cap, cudaStreamNonBlocking) == cudaSuccess;
+    P->input = P->inbuf[0];
     if (!ok) {
         cudaGetLastError();
         ss_pipeline_destroy(P);
@@ -174,16 +188,22 @@ ss_status ss_pipeline_create(ss_grid *g, const ss_pipeline_params *params, ss_pi
 
 ss_status ss_pipeline_destroy(ss_pipeline *P) {
     if (!P) return SS_ERR_ARG;
-    if (P->exec) cudaGraphExecDestroy(P->exec);
-    if (P->graph) cudaGraphDestroy(P->graph);
+    for (int b = 0; b < 2; b++) {
+        if (P->exec[b]) cudaGraphExecDestroy(P->exec[b]);
+        if (P->graph[b]) cudaGraphDestroy(P->graph[b]);
+        if (P->ev_done[b]) cudaEventDestroy(P->ev_done[b]);
+        if (P->ev_copied[b]) cudaEventDestroy(P->ev_copied[b]);
+    }
     if (P->cap) cudaStreamDestroy(P->cap);
+    if (P->copy) cudaStreamDestroy(P->copy);
     for (cudaEvent_t e : P->events) cudaEventDestroy(e);
     cudaFree(P->st);
     cudaFree(P->partials);
     cudaFree(P->acc);
     cudaFree(P->vmap);
     cudaFree(P->nmap);
-    cudaFree(P->input);
+    cudaFree(P->inbuf[0]);
+    cudaFree(P->inbuf[1]);
     cudaFree(P->rc_counters);
     delete P;
     return SS_OK;
@@ -217,7 +237,15 @@ ss_status ss_pipeline_get_pose(ss_pipeline *P, double T[16], ss_stream_t stream)
 
 ss_status ss_pipeline_read_pose(ss_pipeline *P, double T[16], ss_stream_t stream) {
     if (!P || !T) return SS_ERR_ARG;
-    SS_CUDA_TRY(cudaMemcpyAsync(T, P->st->T, 16 * sizeof(double), cudaMemcpyDeviceToHost, (cudaStream_t)stream));
+    cudaStream_t s = (cudaStream_t)stream;
+    // pinned host memory mapped into the device's address space: one small
+    // kernel stores the pose there (a copy-engine transfer of 128 bytes
+    // between two frames' kernels costs several microseconds of hand-off)
+    cudaPointerAttributes attr{};
+    if (cudaPointerGetAttributes(&attr, T) == cudaSuccess && attr.type == cudaMemoryTypeHost && attr.devicePointer)
+        return launch_pose_out(P->st, (double *)attr.devicePointer, s);
+    cudaGetLastError();
+    SS_CUDA_TRY(cudaMemcpyAsync(T, P->st->T, 16 * sizeof(double), cudaMemcpyDefault, s));
     return SS_OK;
 }
 
@@ -239,18 +267,43 @@ ss_status ss_pipeline_frame(ss_pipeline *P, const uint16_t *depth, int32_t track
     cudaStream_t s = (cudaStream_t)stream;
     ss_grid *g = P->g;
     const size_t bytes = (size_t)g->p.resi * g->p.resj * sizeof(uint16_t);
-    if (depth != P->input) SS_CUDA_TRY(cudaMemcpyAsync(P->input, depth, bytes, cudaMemcpyDefault, s));
+    // The input buffer of this frame. A frame already in one of them (written
+    // through ss_pipeline_input) is read in place. A host frame is uploaded on
+    // the copy stream into the buffer the frame before last read, as soon as
+    // that frame has finished, so the upload overlaps the last frame's
+    // kernels; s waits for the upload. Another device pointer is copied on s
+    // (earlier work on s may be producing it).
+    int b;
+    if (depth == P->inbuf[0] || depth == P->inbuf[1]) {
+        b = depth == P->inbuf[0] ? 0 : 1;
+    } else {
+        b = P->next_buf;
+        P->next_buf ^= 1;
+        cudaPointerAttributes attr{};
+        const bool host = cudaPointerGetAttributes(&attr, depth) == cudaSuccess &&
+                          (attr.type == cudaMemoryTypeHost || attr.type == cudaMemoryTypeUnregistered);
+        cudaGetLastError();
+        if (host) {
+            SS_CUDA_TRY(cudaStreamWaitEvent(P->copy, P->ev_done[b], 0));
+            SS_CUDA_TRY(cudaMemcpyAsync(P->inbuf[b], depth, bytes, cudaMemcpyDefault, P->copy));
+            SS_CUDA_TRY(cudaEventRecord(P->ev_copied[b], P->copy));
+            SS_CUDA_TRY(cudaStreamWaitEvent(s, P->ev_copied[b], 0));
+        } else {
+            SS_CUDA_TRY(cudaMemcpyAsync(P->inbuf[b], depth, bytes, cudaMemcpyDefault, s));
+        }
+    }
+    const uint16_t *in = P->inbuf[b];
     ss_status st = epoch_guard(P, s);
     if (st != SS_OK) return st;
     if (!track || !P->have_model) {
         st = launch_pose_prep(P->st, s);
-        if (st == SS_OK) st = enqueue_fuse_raycast(P, s);
+        if (st == SS_OK) st = enqueue_fuse_raycast(P, in, s);
         if (st != SS_OK) return st;
         P->have_model = true;
     } else if (P->p.use_graph) {
-        if (!P->exec) {
+        if (!P->exec[b]) {
             SS_CUDA_TRY(cudaStreamBeginCapture(P->cap, cudaStreamCaptureModeThreadLocal));
-            st = enqueue_frame(P, P->cap);
+            st = enqueue_frame(P, in, P->cap);
             cudaGraph_t graph = nullptr;
             cudaError_t e = cudaStreamEndCapture(P->cap, &graph);
             if (st != SS_OK) {
@@ -261,14 +314,15 @@ ss_status ss_pipeline_frame(ss_pipeline *P, const uint16_t *depth, int32_t track
                 set_last_error("cudaStreamEndCapture", e);
                 return SS_ERR_CUDA;
             }
-            P->graph = graph;
-            SS_CUDA_TRY(cudaGraphInstantiate(&P->exec, P->graph, 0));
+            P->graph[b] = graph;
+            SS_CUDA_TRY(cudaGraphInstantiate(&P->exec[b], P->graph[b], 0));
         }
-        SS_CUDA_TRY(cudaGraphLaunch(P->exec, s));
+        SS_CUDA_TRY(cudaGraphLaunch(P->exec[b], s));
     } else {
-        st = enqueue_frame(P, s, P->profile);
+        st = enqueue_frame(P, in, s, P->profile);
         if (st != SS_OK) return st;
     }
+    SS_CUDA_TRY(cudaEventRecord(P->ev_done[b], s));
     g->host_epoch++;
     P->frames++;
     return SS_OK;

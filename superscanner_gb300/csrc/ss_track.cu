@@ -805,4 +805,16 @@ ss_status launch_pose_prep(TrackState *st, cudaStream_t s) {
     return SS_OK;
 }
 
+// The pose (16 doubles) stored through a device-mapped pointer (pinned host
+// memory): a per-frame readback without a copy-engine transfer.
+__global__ void pose_out_kernel(const TrackState *st, double *dst) {
+    if (threadIdx.x < 16) dst[threadIdx.x] = st->T[threadIdx.x];
+}
+
+ss_status launch_pose_out(const TrackState *st, double *dst, cudaStream_t s) {
+    pose_out_kernel<<<1, 32, 0, s>>>(st, dst);
+    SS_LAUNCH_CHECK();
+    return SS_OK;
+}
+
 }  // namespace ss

@@ -57,5 +57,7 @@ ss_status launch_track(const TrackLaunch &L, cudaStream_t s);
 // CTAs of the persistent tracker on this device (co-resident, <= want_per_sm per SM).
 int persistent_track_ctas(int num_sms, int want_per_sm);
 ss_status launch_pose_prep(TrackState *st, cudaStream_t s);
+// Stores the pose T into dst (a device address, e.g. of mapped pinned host memory).
+ss_status launch_pose_out(const TrackState *st, double *dst, cudaStream_t s);
 
 }  // namespace ss

@@ -214,3 +214,40 @@ def test_perturbed_start_matches_fp64_tracker(persistent):
         assert t_g < 1e-3 and np.rad2deg(r_g) < 0.05
         p2.close()
         g2.close()
+
+
+def test_host_frames_and_pose_readback():
+    """Pinned host frames (uploaded on the copy stream into two alternating
+    input buffers) track bit for bit like the same frames on the device, and
+    the per-frame asynchronous pose readback into pinned host memory (stored
+    by a kernel through the mapped pointer) and into device memory (a copy)
+    both equal the pose."""
+    P, depth = seq(8)
+    poses = {}
+    for source in ("device", "host"):
+        g = GPUVoxelGrid(int(1e9), TRUNC, VL, 480, 640, storage="f16", with_color=False, hash_buckets=1 << 18,
+                         max_weight=255)
+        g.setIntrinsic(*INTR)
+        pipe = Pipeline(g, use_graph=True, persistent_track=True, hint_margin=0.04)
+        stream = torch.cuda.Stream()
+        host = torch.from_numpy(np.ascontiguousarray(depth.view(np.int16))).pin_memory()
+        on_dev = dev(depth)
+        out_host = torch.zeros((8, 16), dtype=torch.float64).pin_memory()
+        out_dev = torch.zeros((8, 16), dtype=torch.float64, device="cuda")
+        with torch.cuda.stream(stream):
+            pipe.set_pose(P[0], stream)
+            for k in range(8):
+                frame = host[k].data_ptr() if source == "host" else on_dev[k]
+                pipe.frame(frame, track=k > 0, stream=stream)
+                pipe.read_pose_async(out_host[k].data_ptr(), stream)
+                pipe.read_pose_async(out_dev[k].data_ptr(), stream)
+        torch.cuda.synchronize()
+        last = pipe.pose(stream)
+        ph, pd = out_host.numpy().reshape(8, 4, 4), out_dev.cpu().numpy().reshape(8, 4, 4)
+        assert np.array_equal(ph, pd)
+        assert np.array_equal(ph[-1], last)
+        poses[source] = ph
+        assert pose_err(ph[-1], P[7])[0] < 0.01
+        pipe.close()
+        g.close()
+    assert np.array_equal(poses["host"], poses["device"])
