@@ -1,0 +1,192 @@
+// ss_collect.cuh — block collection of one 32 x rows pixel tile
+// (depthToPcdTag + vbCollectionTag, GPUVoxelGrid.h:303-307,
+// GPUVoxelGrid.cpp:471-514), shared by the per-call collection
+// (collect_kernel, ss_grid.cu) and the batched re-fusion's
+// (refuse_collect_kernel, ss_refuse.cu). One thread per pixel, two phases:
+//  1. every pixel enumerates the blocks its truncation band overlaps (x
+//     outer, z inner, GPUVoxelGrid.cpp:485-489) into a shared-memory hash set,
+//     so the tile's candidates are deduplicated on chip: the warp steps
+//     through candidates together, groups equal ones (__match_any_sync) and
+//     each group's leader inserts with one 32-bit CAS. A key is the block's
+//     offset from the camera's block, 10 bits per axis ([-512, 511] blocks,
+//     +-16 m at 32 mm blocks); 128 slots per tile row (a tile row at 4 m and
+//     4 mm voxels meets about 20 distinct blocks). Most candidates are in the
+//     set already, so a plain load of the slot precedes the CAS (shared
+//     atomics, not arithmetic, bound this phase). A candidate outside the
+//     key range, or one the set cannot place, is visited directly;
+//  2. each warp compacts its slice of the set (ballots, no atomics) and
+//     visits its distinct blocks; the visits that append a block to the
+//     call's list are aggregated per warp.
+// The set of allocated blocks is the union of every pixel's candidates, as in
+// the reference; only the number of global probes and atomics changes (one
+// per distinct block per tile). 8 bytes of shared memory per slot (set and
+// per-warp lists): 4 KB per 4-row tile.
+//
+// A visitor is a callable bool (int bx, int by, int bz, int &bucket): it finds
+// or inserts the block, marks it, and returns true when this visit is the
+// one that appends bucket to the list.
+#pragma once
+
+#include "ss_internal.cuh"
+
+namespace ss {
+
+constexpr unsigned kSetEmpty = 0xffffffffu;
+constexpr int kSetSlotsPerRow = 128;
+constexpr int kSetOff = 512;  // key offsets per axis: [-kSetOff, kSetOff) blocks
+
+// Dynamic shared memory of a tile of `rows` pixel rows.
+inline size_t tile_set_bytes(int rows) { return (size_t)kSetSlotsPerRow * rows * 2 * sizeof(unsigned); }
+
+// The camera's block (the origin of the set's keys) of pose E.
+__device__ __forceinline__ void camera_block(const GridView &g, const Mat34 &E, int &cbx, int &cby, int &cbz) {
+    cbx = (int)floorf(E.m[3] / g.vbl);
+    cby = (int)floorf(E.m[7] / g.vbl);
+    cbz = (int)floorf(E.m[11] / g.vbl);
+}
+
+// One visit outside the tile's set, with its own append.
+template <class Visit>
+__device__ __forceinline__ void visit_one(const GridView &g, int bx, int by, int bz, Visit &visit) {
+    int bucket = -1;
+    if (!visit(bx, by, bz, bucket)) return;
+    const int idx = atomicAdd(&g.ctr->list_count, 1);
+    if (idx <= (int)g.mask) g.list[idx] = bucket;
+    else atomicOr(&g.ctr->status, kStListOverflow);
+}
+
+// Phase 1 for pixel (i, j) of the tile (every thread of the CTA calls it; the
+// set must be cleared and the CTA synced before).
+template <class Visit>
+__device__ __forceinline__ void tile_fill_set(const GridView &g, const uint16_t *__restrict__ depth, const Mat34 &E,
+                                              int i, int j, unsigned *cset, int slots, int cbx, int cby, int cbz,
+                                              Visit &visit) {
+    const unsigned FULL = 0xffffffffu;
+    int lox = 0, loy = 0, loz = 0, nx = 0, ny = 0, nz = 0;
+    if (i < g.resi && j < g.resj) {
+        F3 p = get_point(g.in, i, j, depth_m(__ldg(depth + (size_t)i * g.resj + j)));
+        if (p.z > g.rmin) {
+            F3 pt = xform(E, p);
+            F3 t{g.trunc, g.trunc, g.trunc};
+            F3 lo = f3sub(pt, t), hi = f3add(pt, t);
+            lox = idx_rule(lo.x, g.vbl);
+            loy = idx_rule(lo.y, g.vbl);
+            loz = idx_rule(lo.z, g.vbl);
+            nx = idx_rule(hi.x, g.vbl) - lox + 1;
+            ny = idx_rule(hi.y, g.vbl) - loy + 1;
+            nz = idx_rule(hi.z, g.vbl) - loz + 1;
+            if (nx < 1 || ny < 1 || nz < 1 || nx > 8 || ny > 8 || nz > 8) {
+                atomicOr(&g.ctr->status, kStRange);  // non-finite pose or truncation > 3.5 blocks
+                nx = ny = nz = 0;
+            }
+        }
+    }
+    const int total = nx * ny * nz;
+    const int lane = (threadIdx.y * blockDim.x + threadIdx.x) & 31;
+    const uint32_t hmask = (uint32_t)(slots - 1);
+    const int hshift = __clz(slots) + 1;  // 32 - log2(slots)
+    // an odometer over x outer, z inner
+    int x = lox, y = loy, z = loz;
+    for (int c = 0; __any_sync(FULL, c < total); c++) {
+        unsigned key = kSetEmpty;
+        bool direct = false;
+        int cx = 0, cy = 0, cz = 0;
+        if (c < total) {
+            cx = x;
+            cy = y;
+            cz = z;
+            if (packable(x, y, z)) {
+                const unsigned ox = (unsigned)(x - cbx + kSetOff), oy = (unsigned)(y - cby + kSetOff),
+                               oz = (unsigned)(z - cbz + kSetOff);
+                if (ox < 2u * kSetOff && oy < 2u * kSetOff && oz < 2u * kSetOff) key = (ox << 20) | (oy << 10) | oz;
+                else direct = true;
+            } else {
+                atomicOr(&g.ctr->status, kStRange);
+            }
+            if (++z == loz + nz) {
+                z = loz;
+                if (++y == loy + ny) {
+                    y = loy;
+                    ++x;
+                }
+            }
+        }
+        if (direct) visit_one(g, cx, cy, cz, visit);  // outside the key range
+        const unsigned peers = __match_any_sync(FULL, key);
+        if (key == kSetEmpty || __ffs(peers) - 1 != lane) continue;
+        // most candidates are already in the set (another warp or an earlier
+        // step put them there): a plain load finds those without an atomic
+        uint32_t h = (key * 0x9E3779B1u) >> hshift;  // the product's top bits (multiplicative hashing)
+        bool placed = false;
+        for (int probe = 0; probe < slots / 2 && !placed; probe++) {
+            h &= hmask;
+            unsigned cur = ((volatile unsigned *)cset)[h];
+            if (cur == kSetEmpty) cur = atomicCAS(cset + h, kSetEmpty, key);
+            placed = cur == kSetEmpty || cur == key;
+            h++;
+        }
+        if (!placed) visit_one(g, cx, cy, cz, visit);  // set too crowded
+    }
+}
+
+// Phase 2 (every thread of the CTA calls it after a CTA barrier that follows
+// phase 1): warp w compacts slots [w per, (w + 1) per) into its list and
+// visits its distinct blocks, appending with one atomic per warp step.
+template <class Visit>
+__device__ __forceinline__ void tile_flush_set(const GridView &g, unsigned *cset, int slots, int cbx, int cby,
+                                               int cbz, Visit &visit) {
+    const unsigned FULL = 0xffffffffu;
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x, nthreads = blockDim.x * blockDim.y;
+    const int lane = tid & 31, wid = tid >> 5, nw = nthreads >> 5, per = slots / nw;
+    const unsigned lt = (1u << lane) - 1u;
+    unsigned *wlist = cset + slots + wid * per;
+    int cnt = 0;
+    for (int r = 0; r < per; r += 32) {
+        const unsigned key = cset[wid * per + r + lane];
+        const bool present = key != kSetEmpty;
+        const unsigned b = __ballot_sync(FULL, present);
+        if (present) wlist[cnt + __popc(b & lt)] = key;
+        cnt += __popc(b);
+    }
+    __syncwarp();
+    for (int base = 0; base < cnt; base += 32) {
+        const int e = base + lane;
+        bool append = false;
+        int bucket = -1;
+        if (e < cnt) {
+            const unsigned key = wlist[e];
+            append = visit(cbx + (int)(key >> 20) - kSetOff, cby + (int)((key >> 10) & 1023u) - kSetOff,
+                           cbz + (int)(key & 1023u) - kSetOff, bucket);
+        }
+        const unsigned ap = __ballot_sync(FULL, append);
+        if (ap) {
+            const int leader = __ffs(ap) - 1;
+            int b0 = 0;
+            if (lane == leader) b0 = atomicAdd(&g.ctr->list_count, __popc(ap));
+            b0 = __shfl_sync(FULL, b0, leader);
+            if (append) {
+                const int idx = b0 + __popc(ap & lt);
+                if (idx <= (int)g.mask) g.list[idx] = bucket;
+                else atomicOr(&g.ctr->status, kStListOverflow);
+            }
+        }
+    }
+}
+
+// Find or insert a block, then stamp it with this call's epoch: the first
+// visitor of the epoch appends it (replaces alreadyIntegrated and the
+// O(capacity) "Reset booleans" pass); the 64-bit atomicMax on (epoch, packed
+// coordinates) also fixes an aliased entry's coordinates canonically (the
+// largest packed coordinate of the call).
+__device__ __forceinline__ bool find_and_stamp(const GridView &g, uint32_t epoch, int bx, int by, int bz,
+                                               int &bucket) {
+    bool inserted = false;
+    bucket = table_find_or_insert(g, prime_hash(bx, by, bz), &inserted);
+    if (inserted) super_insert(g, bx, by, bz);
+    if (bucket < 0) return false;
+    const unsigned long long old =
+        atomicMax(g.stamp + bucket, ((unsigned long long)epoch << kEpochShift) | pack_coords(bx, by, bz));
+    return (uint32_t)(old >> kEpochShift) != epoch;
+}
+
+}  // namespace ss

@@ -20,6 +20,7 @@
 #include <string>
 #include <vector>
 
+#include "ss_collect.cuh"
 #include "ss_fuse.cuh"
 #include "ss_grid_impl.cuh"
 
@@ -96,39 +97,11 @@ __global__ void fill_u64_kernel(unsigned long long *p, size_t n, unsigned long l
         p[t] = v;
 }
 
-// Block collection (vbCollectionTag, GPUVoxelGrid.cpp:471-514) fused with
-// depthToPcdTag (GPUVoxelGrid.h:303-307). One thread per pixel, a CTA per
-// 32 x rows pixel tile, in two phases:
-//  1. every pixel enumerates the blocks its truncation band overlaps (x
-//     outer, z inner, GPUVoxelGrid.cpp:485-489) into a shared-memory hash set,
-//     so the tile's candidates are deduplicated on chip: the warp steps
-//     through candidates together, groups equal ones (__match_any_sync) and
-//     each group's leader inserts with one 32-bit CAS. A key is the block's
-//     offset from the camera's block, 10 bits per axis ([-512, 511] blocks,
-//     +-16 m at 32 mm blocks); 128 slots per tile row (a tile row at 4 m and
-//     4 mm voxels meets about 20 distinct blocks). Most candidates are in the
-//     set already, so a plain load of the slot precedes the CAS (shared
-//     atomics, not arithmetic, bound this phase). A candidate outside the
-//     key range, or one the set cannot place, goes straight to the global
-//     steps of phase 2;
-//  2. each warp compacts its slice of the set (ballots, no atomics) and
-//     handles its distinct blocks: lock-free find-or-insert, then a 64-bit
-//     atomicMax on the block stamp, which both deduplicates the block for
-//     this call across tiles (first visitor of the epoch appends it; replaces
-//     alreadyIntegrated + the O(capacity) "Reset booleans" pass) and fixes the
-//     entry's coordinates canonically for aliased keys; appends are
-//     aggregated per warp.
-// The set of allocated blocks is the union of every pixel's candidates, as in
-// the reference; only the number of global probes and atomics changes (one
-// per distinct block per tile). 8 bytes of shared memory per slot (set and
-// per-warp lists): 4 KB per 4-row tile. Registers are capped at 32 so that
-// every tile of a 640x480 frame is resident at once (16 tiles of 4 rows per
-// SM); the few bytes this spills cost less than a second wave of tiles
-// (collect 0.024 -> 0.022 ms per frame).
-constexpr unsigned kSetEmpty = 0xffffffffu;
-constexpr int kSetSlotsPerRow = 128;
-constexpr int kSetOff = 512;  // key offsets per axis: [-kSetOff, kSetOff) blocks
-
+// Block collection of one call (vbCollectionTag, GPUVoxelGrid.cpp:471-514,
+// fused with depthToPcdTag; the two tile phases are in ss_collect.cuh).
+// Registers are capped at 32 so that every tile of a 640x480 frame is
+// resident at once (16 tiles of 4 rows per SM); the few bytes this spills
+// cost less than a second wave of tiles (collect 0.024 -> 0.022 ms per frame).
 #ifdef SS_COLLECT_TIMING
 // Phase timestamps of every CTA (global timer, ns) for tuning builds only:
 // start, candidates computed, set filled, tile synced, end.
@@ -152,26 +125,18 @@ extern "C" int ss_debug_collect_timing(unsigned long long *out) {
     } while (0)
 #endif
 
-// One candidate block straight through the global table (find-or-insert,
-// stamp, append): for candidates the tile's set cannot hold.
-__device__ void collect_block_global(const GridView &g, unsigned long long packed, uint32_t epoch) {
-    int x, y, z;
-    unpack_coords(packed, x, y, z);
-    bool inserted = false;
-    const int bucket = table_find_or_insert(g, prime_hash(x, y, z), &inserted);
-    if (inserted) super_insert(g, x, y, z);
-    if (bucket < 0) return;
-    const unsigned long long old = atomicMax(g.stamp + bucket, ((unsigned long long)epoch << kEpochShift) | packed);
-    if ((uint32_t)(old >> kEpochShift) == epoch) return;
-    const int idx = atomicAdd(&g.ctr->list_count, 1);
-    if (idx <= (int)g.mask) g.list[idx] = bucket;
-    else atomicOr(&g.ctr->status, kStListOverflow);
-}
+// A block visited by the per-call collection: find or insert, stamp.
+struct CollectVisit {
+    GridView g;
+    uint32_t epoch;
+    __device__ __forceinline__ bool operator()(int bx, int by, int bz, int &bucket) {
+        return find_and_stamp(g, epoch, bx, by, bz, bucket);
+    }
+};
 
 __global__ void __launch_bounds__(256, 8) collect_kernel(GridView g, const uint16_t *__restrict__ depth, Mat34 E,
-                                                      const FramePose *__restrict__ pose) {
+                                                         const FramePose *__restrict__ pose) {
     extern __shared__ unsigned cset[];  // [slots] keys, then [slots] per-warp lists
-    const unsigned FULL = 0xffffffffu;
     const int slots = kSetSlotsPerRow * blockDim.y;
     const int tid = threadIdx.y * blockDim.x + threadIdx.x, nthreads = blockDim.x * blockDim.y;
     for (int q = tid; q < slots; q += nthreads) cset[q] = kSetEmpty;
@@ -179,129 +144,17 @@ __global__ void __launch_bounds__(256, 8) collect_kernel(GridView g, const uint1
 #pragma unroll
         for (int k = 0; k < 12; k++) E.m[k] = __ldg(&pose->E.m[k]);
     }
-    const int j = blockIdx.x * 32 + threadIdx.x;
-    const int i = blockIdx.y * blockDim.y + threadIdx.y;
-    const uint32_t epoch = *(volatile uint32_t *)&g.ctr->epoch;
-    // the camera's block: the origin of the set's keys
-    const int cbx = (int)floorf(E.m[3] / g.vbl), cby = (int)floorf(E.m[7] / g.vbl), cbz = (int)floorf(E.m[11] / g.vbl);
+    CollectVisit visit{g, *(volatile uint32_t *)&g.ctr->epoch};
+    int cbx, cby, cbz;
+    camera_block(g, E, cbx, cby, cbz);
     SS_CT(0);
     __syncthreads();
-
-    int lox = 0, loy = 0, loz = 0, nx = 0, ny = 0, nz = 0;
-    if (i < g.resi && j < g.resj) {
-        F3 p = get_point(g.in, i, j, depth_m(__ldg(depth + (size_t)i * g.resj + j)));
-        if (p.z > g.rmin) {
-            F3 pt = xform(E, p);
-            F3 t{g.trunc, g.trunc, g.trunc};
-            F3 lo = f3sub(pt, t), hi = f3add(pt, t);
-            lox = idx_rule(lo.x, g.vbl);
-            loy = idx_rule(lo.y, g.vbl);
-            loz = idx_rule(lo.z, g.vbl);
-            nx = idx_rule(hi.x, g.vbl) - lox + 1;
-            ny = idx_rule(hi.y, g.vbl) - loy + 1;
-            nz = idx_rule(hi.z, g.vbl) - loz + 1;
-            if (nx < 1 || ny < 1 || nz < 1 || nx > 8 || ny > 8 || nz > 8) {
-                atomicOr(&g.ctr->status, kStRange);  // non-finite pose or truncation > 3.5 blocks
-                nx = ny = nz = 0;
-            }
-        }
-    }
-    const int total = nx * ny * nz;
-    const int lane = tid & 31;
-    const unsigned lt = (1u << lane) - 1u;
-    const uint32_t hmask = (uint32_t)(slots - 1);
-    const int hshift = __clz(slots) + 1;  // 32 - log2(slots)
-    SS_CT(1);
-    // phase 1 (an odometer over x outer, z inner)
-    int x = lox, y = loy, z = loz;
-    for (int c = 0; __any_sync(FULL, c < total); c++) {
-        unsigned key = kSetEmpty;
-        bool direct = false;
-        int cx = 0, cy = 0, cz = 0;
-        if (c < total) {
-            cx = x;
-            cy = y;
-            cz = z;
-            if (packable(x, y, z)) {
-                const unsigned ox = (unsigned)(x - cbx + kSetOff), oy = (unsigned)(y - cby + kSetOff),
-                               oz = (unsigned)(z - cbz + kSetOff);
-                if (ox < 2u * kSetOff && oy < 2u * kSetOff && oz < 2u * kSetOff) key = (ox << 20) | (oy << 10) | oz;
-                else direct = true;
-            } else {
-                atomicOr(&g.ctr->status, kStRange);
-            }
-            if (++z == loz + nz) {
-                z = loz;
-                if (++y == loy + ny) {
-                    y = loy;
-                    ++x;
-                }
-            }
-        }
-        if (direct) collect_block_global(g, pack_coords(cx, cy, cz), epoch);  // outside the key range
-        const unsigned peers = __match_any_sync(FULL, key);
-        if (key == kSetEmpty || __ffs(peers) - 1 != lane) continue;
-        // most candidates are already in the set (another warp or an earlier
-        // step put them there): a plain load finds those without an atomic
-        uint32_t h = (key * 0x9E3779B1u) >> hshift;  // the product's top bits (multiplicative hashing)
-        bool placed = false;
-        for (int probe = 0; probe < slots / 2 && !placed; probe++) {
-            h &= hmask;
-            unsigned cur = ((volatile unsigned *)cset)[h];
-            if (cur == kSetEmpty) cur = atomicCAS(cset + h, kSetEmpty, key);
-            placed = cur == kSetEmpty || cur == key;
-            h++;
-        }
-        if (!placed) collect_block_global(g, pack_coords(cx, cy, cz), epoch);  // set too crowded
-    }
+    tile_fill_set(g, depth, E, blockIdx.y * blockDim.y + threadIdx.y, blockIdx.x * 32 + threadIdx.x, cset, slots, cbx,
+                  cby, cbz, visit);
     SS_CT(2);
     __syncthreads();
     SS_CT(3);
-
-    // phase 2: warp w compacts slots [w per, (w + 1) per) into its list, then
-    // finds / inserts, stamps and appends its distinct blocks
-    const int wid = tid >> 5, nw = nthreads >> 5, per = slots / nw;
-    unsigned *wlist = cset + slots + wid * per;
-    int cnt = 0;
-    for (int r = 0; r < per; r += 32) {
-        const unsigned key = cset[wid * per + r + lane];
-        const bool present = key != kSetEmpty;
-        const unsigned b = __ballot_sync(FULL, present);
-        if (present) wlist[cnt + __popc(b & lt)] = key;
-        cnt += __popc(b);
-    }
-    __syncwarp();
-    for (int base = 0; base < cnt; base += 32) {
-        const int e = base + lane;
-        bool append = false;
-        int bucket = -1;
-        if (e < cnt) {
-            const unsigned key = wlist[e];
-            const int bx = cbx + (int)(key >> 20) - kSetOff, by = cby + (int)((key >> 10) & 1023u) - kSetOff,
-                      bz = cbz + (int)(key & 1023u) - kSetOff;
-            const unsigned long long packed = pack_coords(bx, by, bz);
-            bool inserted = false;
-            bucket = table_find_or_insert(g, prime_hash(bx, by, bz), &inserted);
-            if (inserted) super_insert(g, bx, by, bz);
-            if (bucket >= 0) {
-                const unsigned long long mine = ((unsigned long long)epoch << kEpochShift) | packed;
-                const unsigned long long old = atomicMax(g.stamp + bucket, mine);
-                append = (uint32_t)(old >> kEpochShift) != epoch;
-            }
-        }
-        const unsigned ap = __ballot_sync(FULL, append);
-        if (ap) {
-            const int leader = __ffs(ap) - 1;
-            int b0 = 0;
-            if (lane == leader) b0 = atomicAdd(&g.ctr->list_count, __popc(ap));
-            b0 = __shfl_sync(FULL, b0, leader);
-            if (append) {
-                const int idx = b0 + __popc(ap & lt);
-                if (idx <= (int)g.mask) g.list[idx] = bucket;
-                else atomicOr(&g.ctr->status, kStListOverflow);
-            }
-        }
-    }
+    tile_flush_set(g, cset, slots, cbx, cby, cbz, visit);
     SS_CT(4);
 }
 
@@ -562,7 +415,7 @@ ss_status launch_fuse(ss_grid *g, const uint16_t *depth, const uint8_t *rgb, con
     const int cr = g->lc.collect_rows;
     const dim3 cblk(32, cr), cgrid((g->p.resj + 31) / 32, (g->p.resi + cr - 1) / cr);
     // shared set of packed coordinates + the list of its distinct entries
-    const size_t csmem = (size_t)kSetSlotsPerRow * cr * 2 * sizeof(unsigned);  // <= 8 KB
+    const size_t csmem = tile_set_bytes(cr);  // <= 8 KB
     collect_kernel<<<cgrid, cblk, csmem, s>>>(g->v, depth, E, dpose);
     SS_LAUNCH_CHECK();
     if (after_collect) SS_CUDA_TRY(cudaEventRecord(after_collect, s));

@@ -6,8 +6,9 @@
 //
 // Two launches for the whole batch:
 //  1. refuse_collect_kernel, grid (tiles, phases): phase 2k deintegrates and
-//     2k+1 integrates keyframe k. Each pixel's candidate blocks are found or
-//     inserted as in collect_kernel; the first visitor of the batch appends
+//     2k+1 integrates keyframe k. Each tile's candidate blocks are
+//     deduplicated in shared memory and found or inserted as in
+//     collect_kernel (ss_collect.cuh); the first visitor of the batch appends
 //     the block to the list, and every phase ORs its bit into the block's
 //     512-bit phase mask.
 //  2. refuse_apply_kernel, persistent: warps pull quarter-block items from an
@@ -19,96 +20,53 @@
 // them (precision form included: the value is re-quantised to half after
 // every phase as a sequential store would). Only the aliasing rule differs:
 // an aliased entry takes the largest packed coordinate of the whole batch.
+#include "ss_collect.cuh"
 #include "ss_fuse.cuh"
 #include "ss_grid_impl.cuh"
 
 namespace ss {
 
-__global__ void __launch_bounds__(256) refuse_collect_kernel(GridView g, const uint16_t *const *__restrict__ depths,
-                                                             const FramePose *__restrict__ poses,
-                                                             uint32_t *__restrict__ phase_mask) {
-    const unsigned FULL = 0xffffffffu;
-    const int lane = threadIdx.x;
-    const int j = blockIdx.x * 32 + threadIdx.x;
-    const int i = blockIdx.y * blockDim.y + threadIdx.y;
+// A block visited by the batched collection in one phase: find or insert,
+// set the phase's bit in the block's mask (a plain load first: other tiles of
+// the phase have mostly set it already), stamp with the batch's epoch.
+struct RefuseVisit {
+    GridView g;
+    uint32_t epoch;
+    uint32_t *phase_mask;
+    int word;
+    uint32_t bit;
+    __device__ __forceinline__ bool operator()(int bx, int by, int bz, int &bucket) {
+        const bool append = find_and_stamp(g, epoch, bx, by, bz, bucket);
+        if (bucket >= 0) {
+            uint32_t *w = phase_mask + (size_t)bucket * kPhaseWords + word;
+            if (!(*(volatile uint32_t *)w & bit)) atomicOr(w, bit);
+        }
+        return append;
+    }
+};
+
+// Grid (tiles, tiles, phases): the tile phases of collect_kernel (ss_collect.cuh)
+// for the depth and pose of one phase. Registers capped as in collect_kernel.
+__global__ void __launch_bounds__(256, 8) refuse_collect_kernel(GridView g, const uint16_t *const *__restrict__ depths,
+                                                                const FramePose *__restrict__ poses,
+                                                                uint32_t *__restrict__ phase_mask) {
+    extern __shared__ unsigned cset[];  // [slots] keys, then [slots] per-warp lists
+    const int slots = kSetSlotsPerRow * blockDim.y;
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x, nthreads = blockDim.x * blockDim.y;
+    for (int q = tid; q < slots; q += nthreads) cset[q] = kSetEmpty;
     const int phase = blockIdx.z;
     const uint16_t *depth = depths[phase >> 1];
     Mat34 E;
 #pragma unroll
     for (int k = 0; k < 12; k++) E.m[k] = __ldg(&poses[phase].E.m[k]);
-    const uint32_t epoch = *(volatile uint32_t *)&g.ctr->epoch;
-
-    int lox = 0, loy = 0, loz = 0, nx = 0, ny = 0, nz = 0;
-    if (i < g.resi && j < g.resj) {
-        const F3 p = get_point(g.in, i, j, depth_m(__ldg(depth + (size_t)i * g.resj + j)));
-        if (p.z > g.rmin) {
-            const F3 pt = xform(E, p);
-            const F3 t{g.trunc, g.trunc, g.trunc};
-            const F3 lo = f3sub(pt, t), hi = f3add(pt, t);
-            lox = idx_rule(lo.x, g.vbl);
-            loy = idx_rule(lo.y, g.vbl);
-            loz = idx_rule(lo.z, g.vbl);
-            nx = idx_rule(hi.x, g.vbl) - lox + 1;
-            ny = idx_rule(hi.y, g.vbl) - loy + 1;
-            nz = idx_rule(hi.z, g.vbl) - loz + 1;
-            if (nx < 1 || ny < 1 || nz < 1 || nx > 8 || ny > 8 || nz > 8) {
-                atomicOr(&g.ctr->status, kStRange);
-                nx = ny = nz = 0;
-            }
-        }
-    }
-    const int total = nx * ny * nz;
-    const unsigned lt = (1u << lane) - 1u;
-    const uint32_t bit = 1u << (phase & 31);
-    const int word = phase >> 5;
-    for (int c = 0;; c++) {
-        bool act = c < total;
-        if (!__any_sync(FULL, act)) break;
-        unsigned long long packed = 0, key = 0;
-        if (act) {
-            const int z = loz + c % nz, y = loy + (c / nz) % ny, x = lox + c / (nz * ny);
-            if (packable(x, y, z)) {
-                packed = pack_coords(x, y, z);
-                key = prime_hash(x, y, z);
-            } else {
-                atomicOr(&g.ctr->status, kStRange);
-                act = false;
-            }
-        }
-        const unsigned am = __ballot_sync(FULL, act);
-        bool append = false;
-        int bucket = -1;
-        if (act) {
-            const unsigned peers = __match_any_sync(am, packed);
-            if (__ffs(peers) - 1 == lane) {
-                bool inserted = false;
-                bucket = table_find_or_insert(g, key, &inserted);
-                if (inserted) {
-                    int x, y, z;
-                    unpack_coords(packed, x, y, z);
-                    super_insert(g, x, y, z);
-                }
-                if (bucket >= 0) {
-                    const unsigned long long mine = ((unsigned long long)epoch << kEpochShift) | packed;
-                    const unsigned long long old = atomicMax(g.stamp + bucket, mine);
-                    append = (uint32_t)(old >> kEpochShift) != epoch;
-                    atomicOr(phase_mask + (size_t)bucket * kPhaseWords + word, bit);
-                }
-            }
-        }
-        const unsigned ap = __ballot_sync(FULL, append);
-        if (ap) {
-            const int leader = __ffs(ap) - 1;
-            int base = 0;
-            if (lane == leader) base = atomicAdd(&g.ctr->list_count, __popc(ap));
-            base = __shfl_sync(FULL, base, leader);
-            if (append) {
-                const int idx = base + __popc(ap & lt);
-                if (idx <= (int)g.mask) g.list[idx] = bucket;
-                else atomicOr(&g.ctr->status, kStListOverflow);
-            }
-        }
-    }
+    RefuseVisit visit{g, *(volatile uint32_t *)&g.ctr->epoch, phase_mask, phase >> 5, 1u << (phase & 31)};
+    int cbx, cby, cbz;
+    camera_block(g, E, cbx, cby, cbz);
+    __syncthreads();
+    tile_fill_set(g, depth, E, blockIdx.y * blockDim.y + threadIdx.y, blockIdx.x * 32 + threadIdx.x, cset, slots, cbx,
+                  cby, cbz, visit);
+    __syncthreads();
+    tile_flush_set(g, cset, slots, cbx, cby, cbz, visit);
 }
 
 template <int kStorage, bool kExact>
@@ -251,8 +209,10 @@ extern "C" ss_status ss_refuse_batch(ss_grid *g, int32_t n, const uint16_t *cons
     SS_CUDA_TRY(cudaMemcpyAsync(g->batch_poses, hp, 2 * n * sizeof(FramePose), cudaMemcpyHostToDevice, s));
     SS_CUDA_TRY(cudaMemcpyAsync(g->batch_depths, depths, n * sizeof(uint16_t *), cudaMemcpyHostToDevice, s));
     SS_CUDA_TRY(cudaMemsetAsync(&g->v.ctr->work, 0, sizeof(int), s));
-    const dim3 cblk(32, 8), cgrid((g->p.resj + 31) / 32, (g->p.resi + 7) / 8, 2 * n);
-    refuse_collect_kernel<<<cgrid, cblk, 0, s>>>(g->v, g->batch_depths, g->batch_poses, g->phase_mask);
+    constexpr int kRows = 4;
+    const dim3 cblk(32, kRows), cgrid((g->p.resj + 31) / 32, (g->p.resi + kRows - 1) / kRows, 2 * n);
+    refuse_collect_kernel<<<cgrid, cblk, tile_set_bytes(kRows), s>>>(g->v, g->batch_depths, g->batch_poses,
+                                                                     g->phase_mask);
     SS_LAUNCH_CHECK();
     const int ctas = persistent_ctas(g, g->lc.refuse_ctas_per_sm);
     const bool f32 = g->p.storage == SS_STORAGE_F32;
