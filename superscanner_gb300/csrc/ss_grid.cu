@@ -523,8 +523,10 @@ ss_status ss_grid_create(const ss_params *p, ss_grid **out) {
     const size_t B = (size_t)p->hash_buckets;
     bool ok = cudaMalloc(&g->v.keys, B * 8) == cudaSuccess && cudaMalloc(&g->v.stamp, B * 8) == cudaSuccess &&
               cudaMalloc(&g->v.list, B * 4) == cudaSuccess && cudaMalloc(&g->v.ctr, sizeof(Counters)) == cudaSuccess;
-    // super-block set: one entry per 512 blocks of capacity, at least 4096 (load factor <= 1/8 of a 2^20 table)
-    const size_t SB = std::max<size_t>(4096, B / 32);
+    // super-block set: as many entries as the table has buckets, so it cannot
+    // fill before the table does (scattered depths put every block in a
+    // super-block of its own); at least 4096
+    const size_t SB = std::max<size_t>(4096, B);
     if (ok) ok = cudaMalloc(&g->v.sbkeys, SB * 8) == cudaSuccess;
     g->v.sbmask = (uint32_t)(SB - 1);
     if (ok && p->storage == SS_STORAGE_F32)

@@ -252,3 +252,25 @@ def test_f16_storage_tracks_f32():
     assert np.array_equal(da["keys"], db["keys"])
     assert np.array_equal(da["w"], db["w"])
     assert np.abs(da["sdf"] - db["sdf"]).max() <= 1e-3 * 0.02
+
+
+def test_scattered_and_far_depths_match_oracle():
+    """Block collection off its common path: random depths from 0.4 m to 40 m
+    per pixel (blocks beyond the tile set's +-20 m key range take the direct
+    global path; tiles meet more distinct blocks than their set holds), on a
+    ragged image. Block set, coordinates, weights and TSDF as the oracle."""
+    rows, cols = 61, 93
+    intr = scaled_intr(rows, cols)
+    rng = np.random.default_rng(3)
+    depth = rng.integers(400, 40000, size=(2, rows, cols)).astype(np.uint16)
+    depth[1, :, : cols // 2] = 0  # a frame with a blank half
+    P = [np.eye(4), np.eye(4)]
+    P[1][:3, 3] = [0.3, -0.2, 0.1]
+    g, o = make_pair(rows, cols, intr, buckets=1 << 18, color=False)
+    for k in range(2):
+        E = P[k].astype(np.float32)
+        g.integrate(None, dev(depth[k]), E, withColor=False)
+        o.integrate(depth[k], np.zeros((rows, cols, 3), np.uint8), E, with_color=False)
+    g.sync()
+    assert g.block_count() > 20000
+    assert compare(g, o, 0.02, color=False) == 1.0

@@ -62,3 +62,37 @@ def test_batched_refusion_equals_sequential(storage, exact):
     assert np.array_equal(a["keys"], b["keys"]) and np.array_equal(a["coords"], b["coords"])
     assert np.array_equal(a["w"], b["w"])
     assert np.array_equal(a["sdf"], b["sdf"])
+
+
+def test_batched_refusion_scattered_depths():
+    """The batched collection off its common path (random depths up to 40 m:
+    blocks beyond the tile set's key range, crowded tile sets) still gives the
+    volume of the sequential calls bit for bit."""
+    rows, cols = 48, 64
+    rng = np.random.default_rng(11)
+    depth = rng.integers(400, 40000, size=(6, rows, cols)).astype(np.uint16)
+    dev = [torch.from_numpy(np.ascontiguousarray(d.view(np.int16))).cuda() for d in depth]
+    intr = (52.5, 52.5, (cols - 1) / 2.0, (rows - 1) / 2.0)
+    P = np.stack([np.eye(4)] * 6)
+    P[:, 0, 3] = np.linspace(0, 0.2, 6)
+    T_new = np.stack([delta(rng) @ P[k] for k in range(6)])
+    out = []
+    for batched in (False, True):
+        g = GPUVoxelGrid(int(1e9), 0.016, 0.004, rows, cols, storage="f16", with_color=False, hash_buckets=1 << 19,
+                         max_weight=255)
+        g.setIntrinsic(*intr)
+        for k in range(6):
+            g.integrate_fast(dev[k], P[k].astype(np.float32))
+        if batched:
+            g.refuse_batch(dev, P, T_new)
+        else:
+            for k in range(6):
+                g.integrate_fast(dev[k], P[k].astype(np.float32), deint=True)
+                g.integrate_fast(dev[k], T_new[k].astype(np.float32))
+        g.sync()
+        out.append(g.export_blocks(with_color=False))
+        g.close()
+    a, b = out
+    assert len(a["keys"]) > 10000
+    assert np.array_equal(a["keys"], b["keys"]) and np.array_equal(a["coords"], b["coords"])
+    assert np.array_equal(a["w"], b["w"]) and np.array_equal(a["sdf"], b["sdf"])
