@@ -215,6 +215,31 @@ __global__ void __launch_bounds__(256) raycast_ref_kernel(GridView g, Mat34 Er, 
 // gradient of the trilinear interpolant at the hit (world frame, pointing
 // out of the surface). Outputs: vmap[i][j] = (x, y, z world, depth) and
 // nmap[i][j] = (nx, ny, nz, 0); misses are all-zero.
+#ifdef SS_RAYCAST_TIMING
+// Per-warp SM cycles of the hint, the search (with its refinement) and the
+// final sample and stores, and the warps' largest and summed step counts,
+// for tuning builds only.
+__device__ unsigned long long g_raycast_timing[8];
+#define SS_RT_NOW(v) long long v = clock64()
+#define SS_RT_ADD(slot, val)                                                                 \
+    do {                                                                                     \
+        if ((threadIdx.x & 31) == 0) atomicAdd(&g_raycast_timing[slot], (unsigned long long)(val)); \
+    } while (0)
+extern "C" int ss_debug_raycast_timing(unsigned long long *out, int reset) {
+    int e = (int)cudaMemcpyFromSymbol(out, g_raycast_timing, sizeof(g_raycast_timing));
+    if (reset) {
+        unsigned long long z[8] = {};
+        cudaMemcpyToSymbol(g_raycast_timing, z, sizeof(z));
+    }
+    return e;
+}
+#else
+#define SS_RT_NOW(v)
+#define SS_RT_ADD(slot, val) \
+    do {                     \
+    } while (0)
+#endif
+
 template <int kStorage>
 __global__ void __launch_bounds__(256) raycast_maps_kernel(GridView g, Mat34 T, const FramePose *__restrict__ pose,
                                                            int max_steps, float t_min, float t_max,
@@ -227,6 +252,7 @@ __global__ void __launch_bounds__(256) raycast_maps_kernel(GridView g, Mat34 T, 
     BlockCache cache{INT_MIN, INT_MIN, INT_MIN, -1, 0u, 0u};
     int steps = 0;
     bool hit = false;
+    SS_RT_NOW(rt0);
     // Depth hint of this ray: the fused frame's depth at this pixel, or, where
     // that is missing (dropout), the smaller depth of the nearest pixels with
     // depth to its left and right within this warp's 32-pixel row segment.
@@ -241,6 +267,8 @@ __global__ void __launch_bounds__(256) raycast_maps_kernel(GridView g, Mat34 T, 
         const unsigned dl = __shfl_sync(full, own, li), dr = __shfl_sync(full, own, ri);
         hint_mm = own ? own : (left && right ? min(dl, dr) : (left ? dl : (right ? dr : 0u)));
     }
+    SS_RT_NOW(rt1);
+    long long rt2 = 0;
     if (inside) {
     if (pose) {
 #pragma unroll
@@ -263,6 +291,9 @@ __global__ void __launch_bounds__(256) raycast_maps_kernel(GridView g, Mat34 T, 
     } else {
         hit = march<kStorage>(g, ox, oy, oz, dx, dy, dz, inv_len, t_min, t_max, max_steps, steps, t, cache);
     }
+#ifdef SS_RAYCAST_TIMING
+    rt2 = clock64();
+#endif
     const size_t pix = (size_t)i * g.resj + j;
     float4 v = make_float4(0.f, 0.f, 0.f, 0.f), n = make_float4(0.f, 0.f, 0.f, 0.f);
     if (hit) {
@@ -277,6 +308,21 @@ __global__ void __launch_bounds__(256) raycast_maps_kernel(GridView g, Mat34 T, 
     vmap[pix] = v;
     nmap[pix] = n;
     }
+#ifdef SS_RAYCAST_TIMING
+    {
+        const long long rt3 = clock64();
+        const unsigned full = 0xffffffffu;
+        // lanes outside the image leave rt2 at 0: take the warp's latest search end
+        const long long e2 = (long long)__reduce_max_sync(full, (unsigned)(rt2 ? rt2 - rt1 : 0));
+        SS_RT_ADD(0, rt1 - rt0);
+        SS_RT_ADD(1, e2);
+        SS_RT_ADD(2, rt3 - rt1 - e2);
+        const unsigned smax = __reduce_max_sync(full, (unsigned)steps), ssum = __reduce_add_sync(full, (unsigned)steps);
+        SS_RT_ADD(3, smax);
+        SS_RT_ADD(4, ssum);
+        SS_RT_ADD(5, 1);
+    }
+#endif
     if (counters) {  // algorithmic-traffic counters (profiling only), one atomic per warp and field
         const unsigned full = 0xffffffffu;
         const unsigned l = __reduce_add_sync(full, cache.lookups), vx = __reduce_add_sync(full, cache.voxels);
