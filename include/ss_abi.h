@@ -207,6 +207,26 @@ ss_status ss_grid_extract_mesh(ss_grid *g, int64_t max_triangles, float *triangl
  * into rows x row_bytes (bpp: bytes per pixel). Host memory, host code. */
 ss_status ss_png_unfilter(const uint8_t *filtered, int32_t rows, int32_t row_bytes, int32_t bpp, uint8_t *out);
 
+/* Colour frames (DataCam.cpp:30-46 reads color/<NNNNNN>.jpg first, 66-69
+ * resizes them with cv::resize's default, bilinear). A JPEG decoder on the GPU
+ * (nvJPEG, loaded at run time: ss_jpeg_create returns SS_ERR_STATE when the
+ * CUDA toolkit's libnvjpeg is absent). One decoder per host thread. */
+typedef struct ss_jpeg ss_jpeg;
+ss_status ss_jpeg_create(ss_jpeg **out);
+ss_status ss_jpeg_destroy(ss_jpeg *j);
+/* Image size of a JPEG held in host memory (1 or 3 components). */
+ss_status ss_jpeg_info(ss_jpeg *j, const uint8_t *data, size_t size, int32_t *rows, int32_t *cols);
+/* Decodes a JPEG (host memory) into rgb: device [rows][cols][3] u8, RGB,
+ * bilinearly resized when the image's size differs (source coordinate
+ * (d + 0.5) src / dst - 0.5, clamped to the border). Enqueued on s (the
+ * entropy decoding runs on the calling thread). SS_ERR_ARG for a stream that
+ * is not a JPEG nvJPEG supports. */
+ss_status ss_jpeg_decode_rgb(ss_jpeg *j, const uint8_t *data, size_t size, uint8_t *rgb, int32_t rows, int32_t cols,
+                             ss_stream_t s);
+/* The same bilinear resize of a device RGB image (e.g. a PNG colour frame). */
+ss_status ss_resize_rgb(const uint8_t *src, int32_t src_rows, int32_t src_cols, uint8_t *dst, int32_t rows,
+                        int32_t cols, ss_stream_t s);
+
 /* Synchronises the stream and returns (then clears) the device status word. */
 ss_status ss_grid_sync(ss_grid *g, ss_stream_t s);
 

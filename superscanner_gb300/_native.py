@@ -81,6 +81,11 @@ SIGNATURES = {
     "ss_refuse_batch": (_st, [_p, _i32, _p, _p, _p, _i32, _p]),
     "ss_grid_extract_mesh": (_st, [_p, C.c_int64, _p, C.POINTER(C.c_int64), _p]),
     "ss_png_unfilter": (_st, [_p, _i32, _i32, _i32, _p]),
+    "ss_jpeg_create": (_st, [C.POINTER(_p)]),
+    "ss_jpeg_destroy": (_st, [_p]),
+    "ss_jpeg_info": (_st, [_p, _p, C.c_size_t, C.POINTER(_i32), C.POINTER(_i32)]),
+    "ss_jpeg_decode_rgb": (_st, [_p, _p, C.c_size_t, _p, _i32, _i32, _p]),
+    "ss_resize_rgb": (_st, [_p, _i32, _i32, _p, _i32, _i32, _p]),
     "ss_dofs_to_pose": (_st, [_D16, _D16]),
     "ss_pose_to_dofs": (_st, [_D16, _D16]),
     "ss_reintegration_order": (_st, [_i32, _p, _p, C.c_double, _p, C.POINTER(_i32)]),

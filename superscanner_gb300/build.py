@@ -65,7 +65,7 @@ def build_cuda(force: bool = False, verbose: bool = False) -> Path:
             if verbose:
                 print(" ".join(cmd), file=sys.stderr)
     tmp = LIB.with_suffix(".so.tmp")
-    _run([nvcc, *ARCH, "-shared", "-cudart", "static", "-o", str(tmp), *map(str, objs)])
+    _run([nvcc, *ARCH, "-shared", "-cudart", "static", "-o", str(tmp), *map(str, objs), "-ldl"])
     os.replace(tmp, LIB)
     return LIB
 

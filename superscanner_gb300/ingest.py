@@ -1,11 +1,12 @@
 """Frame ingest in the reference's on-disk layout (src/cameras/DataCam.cpp:10-100,
 src/utils/coreutil.cpp:381-457): ``<root>/depth/<NNNNNN>.png`` (16-bit grey,
-millimetres; a plain number as fallback), ``<root>/color/<NNNNNN>.png``
-(8-bit RGB; JPEG colour needs an image library that this package does not
-use), ``intrinsic.txt`` (width, height, then the 3x3 intrinsic matrix, one
-row per line). Frames whose size differs from the target are resized with
-nearest-neighbour sampling, as the reference does with OpenCV INTER_NEAREST.
-Frames are returned in pinned host memory, ready for the pipeline's
+millimetres; a plain number as fallback), ``<root>/color/<NNNNNN>.jpg`` or
+``.png`` (8-bit RGB; JPEG decoded on the GPU by ``ss_jpeg_decode_rgb``),
+``intrinsic.txt`` (width, height, then the 3x3 intrinsic matrix, one row per
+line). Depth frames whose size differs from the target are resized with
+nearest-neighbour sampling, as the reference does with OpenCV INTER_NEAREST;
+colour frames bilinearly, as its cv::resize default (INTER_LINEAR). Depth
+frames are returned in pinned host memory, ready for the pipeline's
 asynchronous upload (``Pipeline.frame``)."""
 from __future__ import annotations
 
@@ -119,6 +120,68 @@ def resize_nearest(img: np.ndarray, rows: int, cols: int) -> np.ndarray:
     return img[ii][:, jj]
 
 
+def resize_bilinear(img: np.ndarray, rows: int, cols: int) -> np.ndarray:
+    """[H, W, C] uint8 resized bilinearly with cv::resize's INTER_LINEAR
+    geometry (source coordinate (d + 0.5) src / dst - 0.5, clamped to the
+    first and last pixel), rounded to nearest; the host twin of
+    ss_resize_rgb."""
+    h, w = img.shape[:2]
+    if (h, w) == (rows, cols):
+        return img
+
+    def axis(n_dst, n_src):
+        f = (np.arange(n_dst) + 0.5) * (n_src / n_dst) - 0.5
+        i0 = np.floor(f).astype(np.int64)
+        a = f - i0
+        a[i0 < 0] = 0.0
+        i0 = np.maximum(i0, 0)
+        a[i0 >= n_src - 1] = 0.0
+        i0 = np.minimum(i0, n_src - 1)
+        return i0, np.minimum(i0 + 1, n_src - 1), a
+
+    y0, y1, ay = axis(rows, h)
+    x0, x1, ax = axis(cols, w)
+    f = img.astype(np.float64)
+    top = f[y0][:, x0] + ax[None, :, None] * (f[y0][:, x1] - f[y0][:, x0])
+    bot = f[y1][:, x0] + ax[None, :, None] * (f[y1][:, x1] - f[y1][:, x0])
+    out = top + ay[:, None, None] * (bot - top)
+    return np.clip(np.rint(out), 0, 255).astype(np.uint8)
+
+
+class JpegDecoder:
+    """JPEG -> RGB on the GPU (ss_jpeg_*, nvJPEG); one per host thread."""
+
+    def __init__(self):
+        self._h = C.c_void_p()
+        check(lib.ss_jpeg_create(C.byref(self._h)), "jpeg_create")
+
+    def close(self):
+        if self._h:
+            lib.ss_jpeg_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def info(self, data: bytes) -> tuple[int, int]:
+        r, c = C.c_int32(), C.c_int32()
+        check(lib.ss_jpeg_info(self._h, data, len(data), C.byref(r), C.byref(c)), "jpeg_info")
+        return r.value, c.value
+
+    def decode(self, data: bytes, rows: int | None = None, cols: int | None = None, stream=None) -> torch.Tensor:
+        """CUDA uint8 tensor [rows, cols, 3] (the image's own size by default)."""
+        if rows is None or cols is None:
+            rows, cols = self.info(data)
+        out = torch.empty((rows, cols, 3), dtype=torch.uint8, device="cuda")
+        sp = C.c_void_p(stream.cuda_stream) if stream is not None else C.c_void_p()
+        check(lib.ss_jpeg_decode_rgb(self._h, data, len(data), C.c_void_p(out.data_ptr()), rows, cols, sp),
+              "jpeg_decode_rgb")
+        return out
+
+
 def frame_name(k: int) -> str:
     """getPicNumberString (coreutil.cpp:449-457): zero-padded to 6 digits."""
     return str(k).rjust(6, "0")
@@ -131,6 +194,7 @@ class FrameReader:
     def __init__(self, root, rows: int = 480, cols: int = 640):
         self.root = Path(root)
         self.rows, self.cols = rows, cols
+        self._jpeg = None
 
     def _find(self, sub: str, k: int, ext: str):
         for name in (frame_name(k), str(k)):
@@ -153,9 +217,25 @@ class FrameReader:
         t.numpy()[:] = img.view(np.int16)
         return t
 
-    def color(self, k: int):
-        p = self._find("color", k, "png")
-        if p is None:
-            return None  # JPEG colour: not decoded here
-        img = read_png(p)
-        return np.ascontiguousarray(resize_nearest(img, self.rows, self.cols))
+    def color(self, k: int, device: bool = False):
+        """RGB frame k resized to rows x cols (None when there is none): the
+        reference's order color/<NNNNNN>.jpg, color/<NNNNNN>.png, color/<k>.jpg
+        (DataCam.cpp:30-46). A JPEG is decoded and resized on the GPU; a CUDA
+        tensor if device, else a host array."""
+        zp, plain = self.root / "color" / frame_name(k), self.root / "color" / str(k)
+        for p in (zp.with_suffix(".jpg"), zp.with_suffix(".png"), plain.with_suffix(".jpg")):
+            if not p.exists():
+                continue
+            if p.suffix == ".jpg":
+                if self._jpeg is None:
+                    self._jpeg = JpegDecoder()
+                t = self._jpeg.decode(p.read_bytes(), self.rows, self.cols)
+                return t if device else t.cpu().numpy()
+            img = read_png(p)
+            if img.dtype != np.uint8:
+                raise ValueError(f"{p}: 8-bit colour expected")
+            if img.ndim == 2:
+                img = np.repeat(img[..., None], 3, axis=2)
+            img = np.ascontiguousarray(resize_bilinear(img[..., :3], self.rows, self.cols))
+            return torch.from_numpy(img).cuda() if device else img
+        return None

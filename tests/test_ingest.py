@@ -4,6 +4,7 @@ zero-padded frame names with their plain fallback, nearest-neighbour resize."""
 import numpy as np
 import pytest
 
+from superscanner_gb300._native import SSError
 from superscanner_gb300.ingest import FrameReader, frame_name, read_intrinsic, read_png, resize_nearest, write_png
 
 
@@ -76,3 +77,85 @@ def test_ingested_frames_drive_the_pipeline(tmp_path):
         g.close()
     for a, b in zip(poses["png"], poses["device"]):
         assert np.array_equal(a, b)
+
+
+def _smooth_rgb(rows, cols, seed=0):
+    yy, xx = np.mgrid[0:rows, 0:cols].astype(np.float64)
+    rng = np.random.default_rng(seed)
+    img = np.stack([128 + 90 * np.sin(xx / 17.0 + 0.3), 128 + 80 * np.cos(yy / 13.0),
+                    60 + 0.9 * xx + 0.5 * yy], -1) + rng.normal(0, 1.5, (rows, cols, 3))
+    return np.clip(np.rint(img), 0, 255).astype(np.uint8)
+
+
+def test_jpeg_test_encoder_is_sane():
+    """The test-side JPEG encoder: SOI / EOI, its segments in order, and a
+    reconstruction close to the input (4:4:4 at quality 95)."""
+    import jpeg_encode
+    img = _smooth_rgb(45, 70)
+    data, rec = jpeg_encode.encode(img, 95, subsample=False)
+    assert data[:2] == b"\xff\xd8" and data[-2:] == b"\xff\xd9"
+    for m in (b"\xff\xdb", b"\xff\xc0", b"\xff\xc4", b"\xff\xda"):
+        assert m in data
+    mse = np.mean((rec.astype(np.float64) - img) ** 2)
+    assert 10 * np.log10(255.0 ** 2 / mse) > 35.0
+
+
+def test_resize_bilinear_known_answers():
+    """cv::resize INTER_LINEAR geometry: 2 -> 4 pixels gives 0, 25, 75, 100
+    (source coordinates -0.25 clamped, 0.25, 0.75, 1.25 clamped); equal sizes
+    are returned unchanged; a constant image stays constant."""
+    from superscanner_gb300.ingest import resize_bilinear
+    img = np.zeros((2, 2, 3), np.uint8)
+    img[:, 1] = 100
+    out = resize_bilinear(img, 2, 4)
+    assert out[0, :, 0].tolist() == [0, 25, 75, 100]
+    assert resize_bilinear(img, 2, 2) is img
+    flat = np.full((7, 9, 3), 77, np.uint8)
+    assert (resize_bilinear(flat, 13, 5) == 77).all()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("subsample", [False, True])
+def test_jpeg_decodes_on_gpu(subsample):
+    """nvJPEG through ss_jpeg_decode_rgb reproduces the test encoder's
+    reconstruction (4:4:4: within the IDCT's rounding; 4:2:0: the decoder may
+    interpolate chroma where the reconstruction replicates it)."""
+    import jpeg_encode
+    from superscanner_gb300.ingest import JpegDecoder
+    img = _smooth_rgb(61, 83, seed=1)
+    data, rec = jpeg_encode.encode(img, 90, subsample=subsample)
+    dec = JpegDecoder()
+    assert dec.info(data) == (61, 83)
+    out = dec.decode(data).cpu().numpy()
+    d = np.abs(out.astype(np.int32) - rec)
+    if subsample:
+        assert d.mean() < 1.5 and d.max() <= 16
+    else:  # one level in Y and in Cr can become 1 + 1.402 in R
+        assert d.mean() < 0.3 and d.max() <= 3
+    with pytest.raises(SSError):
+        dec.decode(b"\xff\xd8" + bytes(range(200)))
+    dec.close()
+
+
+@pytest.mark.gpu
+def test_jpeg_colour_frames_resized_on_gpu(tmp_path):
+    """A colour JPEG of another size is decoded and resized on the GPU like
+    the host resize of the decoded image (to one level); the frame reader
+    takes color/<NNNNNN>.jpg before .png, on the host or the device."""
+    import jpeg_encode
+    from superscanner_gb300.ingest import JpegDecoder, resize_bilinear
+    img = _smooth_rgb(50, 70, seed=2)
+    data, _ = jpeg_encode.encode(img, 92)
+    dec = JpegDecoder()
+    native = dec.decode(data).cpu().numpy()
+    for rows, cols in ((120, 160), (24, 31)):
+        gpu = dec.decode(data, rows, cols).cpu().numpy()
+        assert np.abs(gpu.astype(np.int32) - resize_bilinear(native, rows, cols)).max() <= 1
+    (tmp_path / "color").mkdir()
+    (tmp_path / "color" / "000000.jpg").write_bytes(data)
+    write_png(tmp_path / "color" / "000000.png", np.zeros((50, 70, 3), np.uint8))
+    r = FrameReader(tmp_path, rows=120, cols=160)
+    host = r.color(0)
+    assert host.shape == (120, 160, 3) and host.dtype == np.uint8
+    assert np.abs(host.astype(np.int32) - resize_bilinear(native, 120, 160)).max() <= 1
+    assert np.array_equal(r.color(0, device=True).cpu().numpy(), host)
