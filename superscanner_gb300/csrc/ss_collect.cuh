@@ -3,11 +3,14 @@
 // GPUVoxelGrid.cpp:471-514), shared by the per-call collection
 // (collect_kernel, ss_grid.cu) and the batched re-fusion's
 // (refuse_collect_kernel, ss_refuse.cu). One thread per pixel, two phases:
-//  1. every pixel enumerates the blocks its truncation band overlaps (x
-//     outer, z inner, GPUVoxelGrid.cpp:485-489) into a shared-memory hash set,
-//     so the tile's candidates are deduplicated on chip: the warp steps
-//     through candidates together, groups equal ones (__match_any_sync) and
-//     each group's leader inserts with one 32-bit CAS. A key is the block's
+//  1. every pixel's candidates, the cube of blocks its truncation band
+//     overlaps (GPUVoxelGrid.cpp:485-489), go into a shared-memory hash set,
+//     so the tile's candidates are deduplicated on chip: the lanes of a warp
+//     are grouped by cube (__match_any_sync on corner and extent; neighbouring
+//     pixels mostly share one), and the distinct cubes' blocks are spread
+//     over the lanes, 32 per step, each inserted with at most one 32-bit CAS
+//     (typically one or two steps per warp instead of one per candidate of a
+//     pixel). A key is the block's
 //     offset from the camera's block, 10 bits per axis ([-512, 511] blocks,
 //     +-16 m at 32 mm blocks); 128 slots per tile row (a tile row at 4 m and
 //     4 mm voxels meets about 20 distinct blocks). Most candidates are in the
@@ -20,7 +23,7 @@
 // The set of allocated blocks is the union of every pixel's candidates, as in
 // the reference; only the number of global probes and atomics changes (one
 // per distinct block per tile). 8 bytes of shared memory per slot (set and
-// per-warp lists): 4 KB per 4-row tile.
+// per-warp lists) and 512 bytes per warp for its cubes: 6 KB per 4-row tile.
 //
 // A visitor is a callable bool (int bx, int by, int bz, int &bucket): it finds
 // or inserts the block, marks it, and returns true when this visit is the
@@ -35,8 +38,11 @@ constexpr unsigned kSetEmpty = 0xffffffffu;
 constexpr int kSetSlotsPerRow = 128;
 constexpr int kSetOff = 512;  // key offsets per axis: [-kSetOff, kSetOff) blocks
 
-// Dynamic shared memory of a tile of `rows` pixel rows.
-inline size_t tile_set_bytes(int rows) { return (size_t)kSetSlotsPerRow * rows * 2 * sizeof(unsigned); }
+// Dynamic shared memory of a tile of `rows` pixel rows (rows warps): the
+// set, the per-warp lists, and per warp 32 cube entries of 16 bytes.
+inline size_t tile_set_bytes(int rows) {
+    return (size_t)kSetSlotsPerRow * rows * 2 * sizeof(unsigned) + (size_t)rows * 32 * sizeof(int4);
+}
 
 // The camera's block (the origin of the set's keys) of pose E.
 __device__ __forceinline__ void camera_block(const GridView &g, const Mat34 &E, int &cbx, int &cby, int &cbz) {
@@ -82,40 +88,62 @@ __device__ __forceinline__ void tile_fill_set(const GridView &g, const uint16_t 
         }
     }
     const int total = nx * ny * nz;
-    const int lane = (threadIdx.y * blockDim.x + threadIdx.x) & 31;
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    const int lane = tid & 31, wid = tid >> 5;
+    const unsigned lt = (1u << lane) - 1u;
     const uint32_t hmask = (uint32_t)(slots - 1);
     const int hshift = __clz(slots) + 1;  // 32 - log2(slots)
-    // an odometer over x outer, z inner
-    int x = lox, y = loy, z = loz;
-    for (int c = 0; __any_sync(FULL, c < total); c++) {
+    // Neighbouring pixels mostly share their whole cube of candidates: lanes
+    // are grouped by cube (corner and extent), each group's leader enters its
+    // cube in the warp's table, and the cubes' blocks are then spread over the
+    // lanes, 32 per step (x outer, z inner within a cube).
+    const bool small = abs(lox) < (1 << 16) && abs(loy) < (1 << 16) && abs(loz) < (1 << 16);
+    unsigned long long cube = ~0ull - (unsigned long long)lane;  // no cube, or one not grouped: its own key
+    if (total > 0 && small)
+        cube = ((unsigned long long)(lox & 0x1ffff) << 46) | ((unsigned long long)(loy & 0x1ffff) << 29) |
+               ((unsigned long long)(loz & 0x1ffff) << 12) | (unsigned long long)((nx - 1) | (ny - 1) << 4 | (nz - 1) << 8);
+    const unsigned peers = __match_any_sync(FULL, cube);
+    const bool leader = total > 0 && __ffs(peers) - 1 == lane;
+    const unsigned lmask = __ballot_sync(FULL, leader);
+    int incl = leader ? total : 0;  // inclusive scan of the leaders' block counts
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(FULL, incl, o);
+        if (lane >= o) incl += t;
+    }
+    const int work = __shfl_sync(FULL, incl, 31);
+    int4 *cubes = reinterpret_cast<int4 *>(cset + 2 * slots) + wid * 32;
+    const int nlead = __popc(lmask);
+    if (leader)
+        cubes[__popc(lmask & lt)] = make_int4(lox, loy, loz, ((incl - total) << 12) | (nx - 1) | (ny - 1) << 4 | (nz - 1) << 8);
+    __syncwarp();
+    for (int base = 0; base < work; base += 32) {
+        const int w = base + lane;
         unsigned key = kSetEmpty;
         bool direct = false;
         int cx = 0, cy = 0, cz = 0;
-        if (c < total) {
-            cx = x;
-            cy = y;
-            cz = z;
-            if (packable(x, y, z)) {
-                const unsigned ox = (unsigned)(x - cbx + kSetOff), oy = (unsigned)(y - cby + kSetOff),
-                               oz = (unsigned)(z - cbz + kSetOff);
+        if (w < work) {
+            int r = 0;  // the last cube whose first item is <= w
+            while (r + 1 < nlead && (cubes[r + 1].w >> 12) <= w) r++;
+            const int4 cb = cubes[r];
+            const int c = w - (cb.w >> 12);
+            const int ey = ((cb.w >> 4) & 15) + 1, ez = ((cb.w >> 8) & 15) + 1;
+            cz = cb.z + c % ez;
+            cy = cb.y + (c / ez) % ey;
+            cx = cb.x + c / (ez * ey);
+            if (packable(cx, cy, cz)) {
+                const unsigned ox = (unsigned)(cx - cbx + kSetOff), oy = (unsigned)(cy - cby + kSetOff),
+                               oz = (unsigned)(cz - cbz + kSetOff);
                 if (ox < 2u * kSetOff && oy < 2u * kSetOff && oz < 2u * kSetOff) key = (ox << 20) | (oy << 10) | oz;
                 else direct = true;
             } else {
                 atomicOr(&g.ctr->status, kStRange);
             }
-            if (++z == loz + nz) {
-                z = loz;
-                if (++y == loy + ny) {
-                    y = loy;
-                    ++x;
-                }
-            }
         }
         if (direct) visit_one(g, cx, cy, cz, visit);  // outside the key range
-        const unsigned peers = __match_any_sync(FULL, key);
-        if (key == kSetEmpty || __ffs(peers) - 1 != lane) continue;
-        // most candidates are already in the set (another warp or an earlier
-        // step put them there): a plain load finds those without an atomic
+        if (key == kSetEmpty) continue;
+        // most blocks are already in the set (another warp or step put them
+        // there): a plain load finds those without an atomic
         uint32_t h = (key * 0x9E3779B1u) >> hshift;  // the product's top bits (multiplicative hashing)
         bool placed = false;
         for (int probe = 0; probe < slots / 2 && !placed; probe++) {
