@@ -75,12 +75,13 @@ __device__ __forceinline__ void tile_fill_set(const GridView &g, const uint16_t 
             F3 pt = xform(E, p);
             F3 t{g.trunc, g.trunc, g.trunc};
             F3 lo = f3sub(pt, t), hi = f3add(pt, t);
-            lox = idx_rule(lo.x, g.vbl);
-            loy = idx_rule(lo.y, g.vbl);
-            loz = idx_rule(lo.z, g.vbl);
-            nx = idx_rule(hi.x, g.vbl) - lox + 1;
-            ny = idx_rule(hi.y, g.vbl) - loy + 1;
-            nz = idx_rule(hi.z, g.vbl) - loz + 1;
+            const float rvbl = __frcp_rn(g.vbl);
+            lox = idx_rule_r(lo.x, g.vbl, rvbl);
+            loy = idx_rule_r(lo.y, g.vbl, rvbl);
+            loz = idx_rule_r(lo.z, g.vbl, rvbl);
+            nx = idx_rule_r(hi.x, g.vbl, rvbl) - lox + 1;
+            ny = idx_rule_r(hi.y, g.vbl, rvbl) - loy + 1;
+            nz = idx_rule_r(hi.z, g.vbl, rvbl) - loz + 1;
             if (nx < 1 || ny < 1 || nz < 1 || nx > 8 || ny > 8 || nz > 8) {
                 atomicOr(&g.ctr->status, kStRange);  // non-finite pose or truncation > 3.5 blocks
                 nx = ny = nz = 0;

@@ -155,6 +155,22 @@ __device__ __forceinline__ int idx_rule(float a, float len) {
     return a >= 0.f ? __float2int_rz(q) : __float2int_rz(__fsub_rn(q, 1.f));
 }
 
+// idx_rule with the quotient taken as q1 = a * rlen, rlen = RN(1 / len), where
+// that gives the same result: q1 is within 3.02 u |q1| of the IEEE quotient
+// q = RN(a / len) (u = 2^-24: three roundings), and RN(q - 1) within a
+// further u (|q1| + 1) of q - 1, so when q1 lies more than 5 u (|q1| + 1)
+// from every integer, no integer separates q from q1 or RN(q - 1) from
+// RN(q1 - 1), and the truncations agree. Otherwise (and for zero, huge or
+// non-finite values) the IEEE division decides. One multiply instead of a
+// division in all but a few cases per million.
+__device__ __forceinline__ int idx_rule_r(float a, float len, float rlen) {
+    const float q1 = __fmul_rn(a, rlen);
+    const float margin = 3.0e-7f * (fabsf(q1) + 1.f);  // > 5 * 2^-24 (|q1| + 1)
+    if (fabsf(q1 - rintf(q1)) > margin)
+        return a >= 0.f ? __float2int_rz(q1) : __float2int_rz(__fsub_rn(q1, 1.f));
+    return idx_rule(a, len);
+}
+
 // getPrimeHash (GPUVoxelGrid.h:124-128), int wrap, sign-extended to u64.
 __device__ __forceinline__ unsigned long long prime_hash(int x, int y, int z) {
     uint32_t h = 73856093u * (uint32_t)x + 19349669u * (uint32_t)y + 83492791u * (uint32_t)z;
