@@ -52,6 +52,42 @@ __device__ __forceinline__ bool voxel_observe(const GridView &g, const uint16_t 
     return fabsf(sdf) < g.trunc;
 }
 
+// The fast path's observation of a voxel from its camera-frame point q =
+// Einv vm: the nearest pixel (within the image), its depth d > rmin, and the
+// projective sdf d - q.z within the truncation (the expression of
+// voxel_observe<false> after its projection).
+__device__ __forceinline__ bool observe_fast(const GridView &g, const uint16_t *__restrict__ depth, F3 q, float &sdf,
+                                             int &pix) {
+    float rz;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(rz) : "f"(q.z));
+    const int cori = __float2int_rd(fmaf(q.y * g.in.fy, rz, g.in.ci) + 0.5f);
+    const int corj = __float2int_rd(fmaf(q.x * g.in.fx, rz, g.in.cj) + 0.5f);
+    if (!(cori < g.resi && corj < g.resj && cori >= 0 && corj >= 0)) return false;
+    pix = cori * g.resj + corj;
+    const float d = (float)__ldg(depth + pix) * 1.0e-3f;
+    if (!(d > g.rmin)) return false;
+    sdf = d - q.z;
+    return fabsf(sdf) < g.trunc;
+}
+
+// Camera-frame points of a lane's four voxels r0 .. r0 + 3 (r0 even: voxel
+// (l0, m0) of vm0, then (l0 + 4, m0), (l0, m0 + 1), (l0 + 4, m0 + 1)) for the
+// fast path: the first as Einv vm0, the others by adding the transformed
+// voxel steps (4 vl along y, vl along z), with rounded operations that are
+// never contracted, so every kernel computes the same values (the per-frame
+// fusion and the batched re-fusion stay bit-identical).
+__device__ __forceinline__ void quad_points_fast(const Mat34 &Einv, F3 vm0, float vl, F3 q[4]) {
+    q[0].x = fmaf(vm0.x, Einv.m[0], fmaf(vm0.y, Einv.m[1], fmaf(vm0.z, Einv.m[2], Einv.m[3])));
+    q[0].y = fmaf(vm0.x, Einv.m[4], fmaf(vm0.y, Einv.m[5], fmaf(vm0.z, Einv.m[6], Einv.m[7])));
+    q[0].z = fmaf(vm0.x, Einv.m[8], fmaf(vm0.y, Einv.m[9], fmaf(vm0.z, Einv.m[10], Einv.m[11])));
+    const float sy = __fmul_rn(4.f, vl);
+    const F3 dy{__fmul_rn(Einv.m[1], sy), __fmul_rn(Einv.m[5], sy), __fmul_rn(Einv.m[9], sy)};
+    const F3 dz{__fmul_rn(Einv.m[2], vl), __fmul_rn(Einv.m[6], vl), __fmul_rn(Einv.m[10], vl)};
+    q[1] = F3{__fadd_rn(q[0].x, dy.x), __fadd_rn(q[0].y, dy.y), __fadd_rn(q[0].z, dy.z)};
+    q[2] = F3{__fadd_rn(q[0].x, dz.x), __fadd_rn(q[0].y, dz.y), __fadd_rn(q[0].z, dz.z)};
+    q[3] = F3{__fadd_rn(q[2].x, dy.x), __fadd_rn(q[2].y, dy.y), __fadd_rn(q[2].z, dy.z)};
+}
+
 // Running-average update of one voxel (sdf, weight) in FP32.
 template <bool kDeint, bool kExact>
 __device__ __forceinline__ void running_average(float &s, float &w, float obs, float max_weight) {

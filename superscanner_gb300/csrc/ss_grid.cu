@@ -199,6 +199,10 @@ __global__ void __launch_bounds__(256) fuse_kernel(GridView g, const uint16_t *_
         const float pzx = __fmul_rn(g.vbl, (float)bx), pzy = __fmul_rn(g.vbl, (float)by),
                     pzz = __fmul_rn(g.vbl, (float)bz);
         const float cx = __fmaf_rn((float)k + 0.5f, g.vl, pzx);
+        F3 qf[4];  // fast path: the four camera-frame points (ss_fuse.cuh)
+        if (!kExact)
+            quad_points_fast(Einv, F3{cx, __fmaf_rn((float)l0 + 0.5f, g.vl, pzy), __fmaf_rn((float)(r0 >> 1) + 0.5f, g.vl, pzz)},
+                             g.vl, qf);
 #pragma unroll
         for (int rr = 0; rr < 4; rr++) {
             const int r = r0 + rr;
@@ -208,7 +212,9 @@ __global__ void __launch_bounds__(256) fuse_kernel(GridView g, const uint16_t *_
             const size_t vi = (size_t)bucket * kBlockVoxels + v;
             float obs;
             int pix;
-            if (!voxel_observe<kExact>(g, depth, E, Einv, Ez, vm, obs, pix)) continue;
+            if (kExact ? !voxel_observe<true>(g, depth, E, Einv, Ez, vm, obs, pix)
+                       : !observe_fast(g, depth, qf[rr], obs, pix))
+                continue;
             float s, w;
             if (kStorage == SS_STORAGE_F32) {
                 s = sw32[rr].x;

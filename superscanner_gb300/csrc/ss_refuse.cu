@@ -117,12 +117,15 @@ __global__ void __launch_bounds__(256) refuse_apply_kernel(GridView g, const uin
                 const bool deint = (phase & 1) == 0;
                 const FramePose fp = poses[phase];
                 const uint16_t *depth = depths[phase >> 1];
+                F3 qf[4];  // fast path: the four camera-frame points, as fuse_kernel computes them
+                if (!kExact) quad_points_fast(fp.Einv, vm[0], g.vl, qf);
 #pragma unroll
                 for (int rr = 0; rr < 4; rr++) {
                     float obs;
                     int pix;
-                    if (!voxel_observe<kExact>(g, depth, fp.E, fp.Einv, F3{fp.Ez[0], fp.Ez[1], fp.Ez[2]}, vm[rr], obs,
-                                               pix))
+                    if (kExact ? !voxel_observe<true>(g, depth, fp.E, fp.Einv, F3{fp.Ez[0], fp.Ez[1], fp.Ez[2]}, vm[rr],
+                                                      obs, pix)
+                               : !observe_fast(g, depth, qf[rr], obs, pix))
                         continue;
                     if (kStorage == SS_STORAGE_F16 && deint && w[rr] == 0.f) continue;
                     float sv = s[rr], wv = w[rr];
