@@ -50,8 +50,9 @@ WORKLOAD = ("synthetic 4x4x3 m room, 40 primitives, 640x480 noisy uint16 depth (
             "5% dropout), 4 mm voxels, trunc 16 mm, 2^20 buckets, max weight 255; per frame: 3-level "
             "point-to-plane ICP (10/5/4 it) -> integrate -> trilinear raycast (<=128 steps, searched within 40 mm of "
             "the fused frame's depth)")
-# kernels per frame of the chosen form: the cooperative tracker (all GN iterations), collect/fuse/finalize, raycast
-KERNELS_PER_FRAME = 1 + 3 + 1
+# kernels per frame of the chosen form: the cooperative tracker (all GN iterations), collect, fuse, raycast (which
+# also ends the integrate call)
+KERNELS_PER_FRAME = 1 + 2 + 1
 
 
 def parse():

@@ -249,14 +249,7 @@ __global__ void __launch_bounds__(256) fuse_kernel(GridView g, const uint16_t *_
 }
 
 // Ends a call: remembers and resets the list, advances the epoch.
-__global__ void finalize_kernel(Counters *ctr) {
-    const int n = ctr->list_count;
-    ctr->last_touched = n;
-    ctr->touched_total += (unsigned long long)n;
-    ctr->calls += 1ull;
-    ctr->list_count = 0;
-    ctr->epoch = ctr->epoch + 1u;
-}
+__global__ void finalize_kernel(Counters *ctr) { end_call(ctr); }
 
 // Clears the epoch field of every stamp (run when the epoch counter wraps).
 __global__ void rebase_epoch_kernel(GridView g) {
@@ -410,7 +403,7 @@ ss_status rebase_epoch(ss_grid *g, cudaStream_t s) {
 
 ss_status launch_fuse(ss_grid *g, const uint16_t *depth, const uint8_t *rgb, const FramePose &hp,
                       const FramePose *dpose, bool color, bool deint, bool exact, cudaStream_t s,
-                      bool manage_epoch, cudaEvent_t after_collect, cudaEvent_t after_fuse) {
+                      bool manage_epoch, cudaEvent_t after_collect, cudaEvent_t after_fuse, bool finalize) {
     const Mat34 E = hp.E, Einv = hp.Einv;
     const F3 Ez{hp.Ez[0], hp.Ez[1], hp.Ez[2]};
 
@@ -445,8 +438,10 @@ ss_status launch_fuse(ss_grid *g, const uint16_t *depth, const uint8_t *rgb, con
 #undef SS_FUSE
     SS_LAUNCH_CHECK();
     if (after_fuse) SS_CUDA_TRY(cudaEventRecord(after_fuse, s));
-    finalize_kernel<<<1, 1, 0, s>>>(g->v.ctr);
-    SS_LAUNCH_CHECK();
+    if (finalize) {
+        finalize_kernel<<<1, 1, 0, s>>>(g->v.ctr);
+        SS_LAUNCH_CHECK();
+    }
     if (manage_epoch) g->host_epoch++;
     return SS_OK;
 }

@@ -57,23 +57,38 @@ ss_status status_from_bits(int bits);
 Mat34 mat34_from(const float E[16]);
 FramePose frame_pose_from(const float extr[16]);
 
+// The end of an integrate / deintegrate call (one thread): remembers and
+// resets the block list, advances the epoch.
+__device__ __forceinline__ void end_call(Counters *ctr) {
+    const int n = ctr->list_count;
+    ctr->last_touched = n;
+    ctr->touched_total += (unsigned long long)n;
+    ctr->calls += 1ull;
+    ctr->list_count = 0;
+    ctr->epoch = ctr->epoch + 1u;
+}
+
 // integrate / deintegrate launch sequence (collect, fuse, finalize); the pose
 // comes from hp, or from device memory when dpose is not null. With
 // manage_epoch the host epoch mirror is advanced here (direct calls); graph
-// replays advance it in the caller instead.
+// replays advance it in the caller instead. Without finalize the caller ends
+// the call in a later kernel of the same stream (end_call) before the next
+// collection.
 ss_status launch_fuse(ss_grid *g, const uint16_t *depth, const uint8_t *rgb, const FramePose &hp,
                       const FramePose *dpose, bool color, bool deint, bool exact, cudaStream_t s,
                       bool manage_epoch = true, cudaEvent_t after_collect = nullptr,
-                      cudaEvent_t after_fuse = nullptr);
+                      cudaEvent_t after_fuse = nullptr, bool finalize = true);
 // Clears the epoch field of every stamp and restarts the epoch at 1.
 ss_status rebase_epoch(ss_grid *g, cudaStream_t s);
 void inverse4_rounded(const float E[16], float out[16]);
 
-// counters (optional, device u64[4]): hash finds, voxel loads, march steps, hits
+// counters (optional, device u64[4]): hash finds, voxel loads, march steps, hits.
+// end (optional): the integrate call whose end the raycast's first thread
+// performs (end_call), in place of a finalize launch.
 ss_status launch_raycast_maps(ss_grid *g, const Mat34 &T, const FramePose *dpose, int max_steps, float t_min,
                               float t_max, float4 *vmap, float4 *nmap, cudaStream_t s,
                               unsigned long long *counters = nullptr, const uint16_t *hint = nullptr,
-                              float hint_margin = 0.f);
+                              float hint_margin = 0.f, Counters *end = nullptr);
 
 // Blocks of persistent launches (multiple of the SM count).
 int persistent_ctas(const ss_grid *g, int per_sm);

@@ -66,14 +66,15 @@ ss_status enqueue_fuse_raycast(ss_pipeline *P, const uint16_t *in, cudaStream_t 
     ss_grid *g = P->g;
     FramePose dummy{};
     cudaEvent_t e1 = prof ? next_event(P) : nullptr, e2 = prof ? next_event(P) : nullptr;
+    // the integrate call ends in the raycast's first thread (no finalize launch)
     ss_status st = launch_fuse(g, in, nullptr, dummy, &P->st->pose, false, false, P->p.exact_fusion != 0, s,
-                               /*manage_epoch=*/false, e1, e2);
+                               /*manage_epoch=*/false, e1, e2, /*finalize=*/false);
     if (st != SS_OK) return st;
     if (prof) SS_CUDA_TRY(cudaEventRecord(next_event(P), s));
     const bool hint = P->p.hint_margin > 0.f;
     st = launch_raycast_maps(g, dummy.E, &P->st->pose, P->p.raycast_steps, P->p.t_min, P->p.t_max, P->vmap,
                              P->nmap, s, prof ? P->rc_counters : nullptr, hint ? in : nullptr,
-                             P->p.hint_margin);
+                             P->p.hint_margin, g->v.ctr);
     if (st != SS_OK) return st;
     if (prof) SS_CUDA_TRY(cudaEventRecord(next_event(P), s));
     return SS_OK;

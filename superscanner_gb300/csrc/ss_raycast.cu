@@ -245,7 +245,9 @@ __global__ void __launch_bounds__(256) raycast_maps_kernel(GridView g, Mat34 T, 
                                                            int max_steps, float t_min, float t_max,
                                                            float4 *__restrict__ vmap, float4 *__restrict__ nmap,
                                                            unsigned long long *__restrict__ counters,
-                                                           const uint16_t *__restrict__ hint, float hint_margin) {
+                                                           const uint16_t *__restrict__ hint, float hint_margin,
+                                                           Counters *end) {
+    if (end && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0 && threadIdx.y == 0) end_call(end);
     const int j = blockIdx.x * 32 + threadIdx.x;
     const int i = blockIdx.y * blockDim.y + threadIdx.y;
     const bool inside = i < g.resi && j < g.resj;
@@ -338,15 +340,15 @@ __global__ void __launch_bounds__(256) raycast_maps_kernel(GridView g, Mat34 T, 
 
 ss_status launch_raycast_maps(ss_grid *g, const Mat34 &T, const FramePose *dpose, int max_steps, float t_min,
                               float t_max, float4 *vmap, float4 *nmap, cudaStream_t s, unsigned long long *counters,
-                              const uint16_t *hint, float hint_margin) {
+                              const uint16_t *hint, float hint_margin, Counters *end) {
     const int rr = g->lc.raycast_rows;
     const dim3 blk(32, rr), grid((g->p.resj + 31) / 32, (g->p.resi + rr - 1) / rr);
     if (g->p.storage == SS_STORAGE_F32)
         raycast_maps_kernel<SS_STORAGE_F32><<<grid, blk, 0, s>>>(g->v, T, dpose, max_steps, t_min, t_max, vmap, nmap,
-                                                                 counters, hint, hint_margin);
+                                                                 counters, hint, hint_margin, end);
     else
         raycast_maps_kernel<SS_STORAGE_F16><<<grid, blk, 0, s>>>(g->v, T, dpose, max_steps, t_min, t_max, vmap, nmap,
-                                                                 counters, hint, hint_margin);
+                                                                 counters, hint, hint_margin, end);
     SS_LAUNCH_CHECK();
     return SS_OK;
 }
