@@ -70,7 +70,7 @@ __device__ __forceinline__ void tile_fill_set(const GridView &g, const uint16_t 
     const unsigned FULL = 0xffffffffu;
     int lox = 0, loy = 0, loz = 0, nx = 0, ny = 0, nz = 0;
     if (i < g.resi && j < g.resj) {
-        F3 p = get_point(g.in, i, j, depth_m(__ldg(depth + (size_t)i * g.resj + j)));
+        F3 p = get_point_t(g, i, j, depth_m(__ldg(depth + (size_t)i * g.resj + j)));
         if (p.z > g.rmin) {
             F3 pt = xform(E, p);
             F3 t{g.trunc, g.trunc, g.trunc};

@@ -522,7 +522,9 @@ ss_status ss_grid_create(const ss_params *p, ss_grid **out) {
     SS_CUDA_TRY(cudaGetDevice(&g->device));
     SS_CUDA_TRY(cudaDeviceGetAttribute(&g->num_sms, cudaDevAttrMultiProcessorCount, g->device));
     const size_t B = (size_t)p->hash_buckets;
-    bool ok = cudaMalloc(&g->v.keys, B * 8) == cudaSuccess && cudaMalloc(&g->v.stamp, B * 8) == cudaSuccess &&
+    bool ok = cudaMalloc((void **)&g->v.ray_u, (size_t)p->resj * sizeof(float)) == cudaSuccess &&
+              cudaMalloc((void **)&g->v.ray_v, (size_t)p->resi * sizeof(float)) == cudaSuccess &&
+              cudaMalloc(&g->v.keys, B * 8) == cudaSuccess && cudaMalloc(&g->v.stamp, B * 8) == cudaSuccess &&
               cudaMalloc(&g->v.list, B * 4) == cudaSuccess && cudaMalloc(&g->v.ctr, sizeof(Counters)) == cudaSuccess;
     // super-block set: as many entries as the table has buckets, so it cannot
     // fill before the table does (scattered depths put every block in a
@@ -569,6 +571,8 @@ ss_status ss_grid_destroy(ss_grid *g) {
     cudaFree(g->v.vox16);
     cudaFree(g->v.rgb);
     cudaFree(g->v.sbkeys);
+    cudaFree((void *)g->v.ray_u);
+    cudaFree((void *)g->v.ray_v);
     cudaFree(g->phase_mask);
     cudaFree(g->mesh_count);
     cudaFree(g->batch_poses);
@@ -587,6 +591,12 @@ ss_status ss_grid_set_intrinsic(ss_grid *g, float fx, float fy, float cx, float 
     g->v.in.fy = fy;
     g->v.in.ci = (float)g->p.resi - cy;  // ci = resi - cy (GPUVoxelGrid.cpp:259)
     g->v.in.cj = cx;                     // cj = cx (GPUVoxelGrid.cpp:260)
+    // getPoint's quotients per column and row (float operations, as on the device)
+    std::vector<float> u(g->p.resj), v(g->p.resi);
+    for (int j = 0; j < g->p.resj; j++) u[j] = ((float)j - g->v.in.cj) / fx;
+    for (int i = 0; i < g->p.resi; i++) v[i] = ((float)i - g->v.in.ci) / fy;
+    SS_CUDA_TRY(cudaMemcpy((void *)g->v.ray_u, u.data(), u.size() * sizeof(float), cudaMemcpyHostToDevice));
+    SS_CUDA_TRY(cudaMemcpy((void *)g->v.ray_v, v.data(), v.size() * sizeof(float), cudaMemcpyHostToDevice));
     g->intr_set = true;
     return SS_OK;
 }

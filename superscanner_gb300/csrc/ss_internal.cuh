@@ -98,6 +98,10 @@ struct GridView {
     float vl, vbl, trunc, rmin, d_max, max_weight;
     int resi, resj;
     Intr in;
+    // getPoint's per-column and per-row quotients (j - cj) / fx and
+    // (i - ci) / fy in IEEE float, computed on the host when the intrinsics
+    // are set (the same roundings as the device expression)
+    const float *ray_u, *ray_v;  // [resj], [resi]
 };
 
 // ------------------------------------------------------------------ math
@@ -136,6 +140,11 @@ __device__ __forceinline__ F3 xform(const Mat34 &E, F3 p) {
     o.y = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(p.x, E.m[4]), __fmul_rn(p.y, E.m[5])), __fmul_rn(p.z, E.m[6])), E.m[7]);
     o.z = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(p.x, E.m[8]), __fmul_rn(p.y, E.m[9])), __fmul_rn(p.z, E.m[10])), E.m[11]);
     return o;
+}
+
+// getPoint from the grid's quotient tables: bit-identical to get_point.
+__device__ __forceinline__ F3 get_point_t(const GridView &g, int i, int j, float d) {
+    return {__fmul_rn(__ldg(g.ray_u + j), d), __fmul_rn(__ldg(g.ray_v + i), d), d};
 }
 
 // getPoint (GPUVoxelGrid.h:229-232): ((j - cj)/fx*d, (i - ci)/fy*d, d)
