@@ -274,3 +274,19 @@ def test_scattered_and_far_depths_match_oracle():
     g.sync()
     assert g.block_count() > 20000
     assert compare(g, o, 0.02, color=False) == 1.0
+
+
+@pytest.mark.parametrize("rows", [1, 2, 3, 4, 7, 8])
+def test_collection_tile_rows_match_oracle(rows):
+    """Block collection with every tile height the launch configuration
+    allows (set size 128 slots per row, one warp per row, power of two or
+    not): block set, coordinates and TSDF as the oracle."""
+    P, depth, rgb, intr = frames(n=3)
+    g, o = make_pair(480, 640, intr, color=False)
+    g.set_launch_config(collect_rows=rows)
+    for k in range(len(P)):
+        E = P[k].astype(np.float32)
+        g.integrate(None, dev(depth[k]), E, withColor=False)
+        o.integrate(depth[k], rgb[k], E, with_color=False)
+    g.sync()
+    assert compare(g, o, 0.02, color=False) == 1.0
