@@ -68,8 +68,9 @@ def parse():
                     help="frames of the gradient-based pose refinement through the raycast adjoint (0: skip)")
     ap.add_argument("--buckets", type=int, default=BUCKETS,
                     help="hash buckets (profiler captures use a smaller table to keep device memory small)")
-    ap.add_argument("--only", choices=["all", "chosen"], default="all",
-                    help="chosen: time the chosen form alone (for profiler captures)")
+    ap.add_argument("--only", choices=["all", "chosen", "refusion"], default="all",
+                    help="chosen: time the chosen form alone; refusion: time the batched re-fusion alone, "
+                         "three calls with the poses swapped between calls (both for profiler captures)")
     return ap.parse_args()
 
 
@@ -287,11 +288,13 @@ def se3_delta(rng, deg=2.0, cm=3.0):
     return D
 
 
-def run_refusion(torch, depth, P, stream, n_kf: int = 200, launch=None):
+def run_refusion(torch, depth, P, stream, n_kf: int = 200, launch=None, modes=("sequential", "batched"), calls=1):
     """Config 4: the volume of the sequence (keyframes fused with seeded
     rectangular occlusions, 20-100 % coverage), then n_kf keyframes re-fused
     at poses corrected by seeded SE(3) deltas (<= 2 deg / 3 cm): one batched
-    ss_refuse_batch call vs the 2 n_kf sequential calls, same volume state."""
+    ss_refuse_batch call vs the 2 n_kf sequential calls, same volume state.
+    With calls > 1 the re-fusion is repeated on the same volume, old and new
+    poses swapped between calls, and each call is timed."""
     from superscanner_gb300 import GPUVoxelGrid, synth
     n = len(depth)
     n_kf = min(n_kf, n)
@@ -304,7 +307,7 @@ def run_refusion(torch, depth, P, stream, n_kf: int = 200, launch=None):
     T_new = np.stack([se3_delta(rng) @ P[k] for k in range(n_kf)])
     res = {}
     dumps = {}
-    for mode in ("sequential", "batched"):
+    for mode in modes:
         g = GPUVoxelGrid(int(1e9), TRUNC, VL, ROWS, COLS, storage="f16", with_color=False, hash_buckets=BUCKETS,
                          max_weight=MAX_WEIGHT)
         g.setIntrinsic(*INTR)
@@ -314,27 +317,35 @@ def run_refusion(torch, depth, P, stream, n_kf: int = 200, launch=None):
             for k in range(n):
                 g.integrate_fast(dev[k], P[k].astype(np.float32), stream=stream)
             torch.cuda.synchronize()
-            ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            ev0.record(stream)
-            if mode == "batched":
-                g.refuse_batch([dev[k] for k in range(n_kf)], P[:n_kf], T_new, stream=stream)
-            else:
-                for k in range(n_kf):
-                    g.integrate_fast(dev[k], P[k].astype(np.float32), deint=True, stream=stream)
-                    g.integrate_fast(dev[k], T_new[k].astype(np.float32), stream=stream)
-            ev1.record(stream)
-            torch.cuda.synchronize()
+            call_ms = []
+            for c in range(calls):
+                old, new = (P[:n_kf], T_new) if c % 2 == 0 else (T_new, P[:n_kf])
+                ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                ev0.record(stream)
+                if mode == "batched":
+                    g.refuse_batch([dev[k] for k in range(n_kf)], old, new, stream=stream)
+                else:
+                    for k in range(n_kf):
+                        g.integrate_fast(dev[k], old[k].astype(np.float32), deint=True, stream=stream)
+                        g.integrate_fast(dev[k], new[k].astype(np.float32), stream=stream)
+                ev1.record(stream)
+                torch.cuda.synchronize()
+                call_ms.append(ev0.elapsed_time(ev1))
         g.sync(stream)
-        ms = ev0.elapsed_time(ev1)
+        ms = call_ms[0]
         res[mode] = {"ms": round(ms, 3), "keyframes_per_s": round(n_kf / (ms * 1e-3), 1)}
+        if calls > 1:
+            res[mode]["ms_per_call"] = [round(x, 3) for x in call_ms]
         dumps[mode] = g.export_blocks(with_color=False)
         g.close()
+    res["keyframes"] = n_kf
+    res["coverage_min_max"] = [round(float(cover.min()), 3), round(float(cover.max()), 3)]
+    if len(dumps) < 2:
+        return res
     a, b = dumps["sequential"], dumps["batched"]
     res["bit_identical"] = bool(np.array_equal(a["keys"], b["keys"]) and np.array_equal(a["w"], b["w"])
                                 and np.array_equal(a["sdf"], b["sdf"]))
     res["speedup"] = round(res["sequential"]["ms"] / res["batched"]["ms"], 2)
-    res["keyframes"] = n_kf
-    res["coverage_min_max"] = [round(float(cover.min()), 3), round(float(cover.max()), 3)]
     return res
 
 
@@ -623,6 +634,11 @@ def main_ours(args):
     depth_dev = torch.from_numpy(depth.view(np.int16)).cuda()
     stream = torch.cuda.Stream()
     peak, peak_kind = measured_peaks()
+    if args.only == "refusion":
+        if rank == 0:
+            res = run_refusion(torch, depth, P, stream, modes=("batched",), calls=3)
+            print(json.dumps({"metric": "refusion_ms_per_call", "impl": "ours", "refusion": res}))
+        return
 
     # chosen form: launch shapes from the autotuner, timed on the first frames (untimed setup)
     from superscanner_gb300.autotune import autotune
