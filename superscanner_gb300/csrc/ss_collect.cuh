@@ -44,11 +44,12 @@ inline size_t tile_set_bytes(int rows) {
     return (size_t)kSetSlotsPerRow * rows * 2 * sizeof(unsigned) + (size_t)rows * 32 * sizeof(int4);
 }
 
-// The camera's block (the origin of the set's keys) of pose E.
+// The camera's block, about (the origin of the set's keys) of pose E: any
+// value works as long as every thread of the tile computes the same one.
 __device__ __forceinline__ void camera_block(const GridView &g, const Mat34 &E, int &cbx, int &cby, int &cbz) {
-    cbx = (int)floorf(E.m[3] / g.vbl);
-    cby = (int)floorf(E.m[7] / g.vbl);
-    cbz = (int)floorf(E.m[11] / g.vbl);
+    cbx = (int)floorf(E.m[3] * g.rvbl);
+    cby = (int)floorf(E.m[7] * g.rvbl);
+    cbz = (int)floorf(E.m[11] * g.rvbl);
 }
 
 // One visit outside the tile's set, with its own append.
@@ -75,7 +76,7 @@ __device__ __forceinline__ void tile_fill_set(const GridView &g, const uint16_t 
             F3 pt = xform(E, p);
             F3 t{g.trunc, g.trunc, g.trunc};
             F3 lo = f3sub(pt, t), hi = f3add(pt, t);
-            const float rvbl = __frcp_rn(g.vbl);
+            const float rvbl = g.rvbl;
             lox = idx_rule_r(lo.x, g.vbl, rvbl);
             loy = idx_rule_r(lo.y, g.vbl, rvbl);
             loz = idx_rule_r(lo.z, g.vbl, rvbl);
@@ -97,7 +98,10 @@ __device__ __forceinline__ void tile_fill_set(const GridView &g, const uint16_t 
     // Neighbouring pixels mostly share their whole cube of candidates: lanes
     // are grouped by cube (corner and extent), each group's leader enters its
     // cube in the warp's table, and the cubes' blocks are then spread over the
-    // lanes, 32 per step (x outer, z inner within a cube).
+    // lanes, 32 per step. A cube is enumerated over its extents rounded up to
+    // powers of two (x outer, z inner), so an item's offsets are shifts and
+    // masks; items past an extent are skipped (none while the truncation band
+    // spans at most two blocks per axis, the usual case).
     const bool small = abs(lox) < (1 << 16) && abs(loy) < (1 << 16) && abs(loz) < (1 << 16);
     unsigned long long cube = ~0ull - (unsigned long long)lane;  // no cube, or one not grouped: its own key
     if (total > 0 && small)
@@ -106,39 +110,48 @@ __device__ __forceinline__ void tile_fill_set(const GridView &g, const uint16_t 
     const unsigned peers = __match_any_sync(FULL, cube);
     const bool leader = total > 0 && __ffs(peers) - 1 == lane;
     const unsigned lmask = __ballot_sync(FULL, leader);
-    int incl = leader ? total : 0;  // inclusive scan of the leaders' block counts
+    // log2 of the padded extents: 1 -> 0, 2 -> 1, 3-4 -> 2, 5-8 -> 3
+    const int ly = 32 - __clz(max(ny - 1, 0)), lz = 32 - __clz(max(nz - 1, 0));
+    const int padded = leader ? (1 << (32 - __clz(max(nx - 1, 0)) + ly + lz)) : 0;
+    int incl = padded;  // inclusive scan of the leaders' padded block counts
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
         const int t = __shfl_up_sync(FULL, incl, o);
         if (lane >= o) incl += t;
     }
     const int work = __shfl_sync(FULL, incl, 31);
+    const int first = incl - padded;  // a leader's first item
     int4 *cubes = reinterpret_cast<int4 *>(cset + 2 * slots) + wid * 32;
-    const int nlead = __popc(lmask);
     if (leader)
-        cubes[__popc(lmask & lt)] = make_int4(lox, loy, loz, ((incl - total) << 12) | (nx - 1) | (ny - 1) << 4 | (nz - 1) << 8);
+        cubes[__popc(lmask & lt)] =
+            make_int4(lox, loy, loz, first << 16 | lz << 11 | ly << 9 | (nz - 1) << 6 | (ny - 1) << 3 | (nx - 1));
     __syncwarp();
     for (int base = 0; base < work; base += 32) {
+        // the cube of item w: the leaders that started before this step, plus
+        // those starting in it at or before w (one bit per starting item)
+        const unsigned starts =
+            __reduce_or_sync(FULL, leader && first >= base && first < base + 32 ? 1u << (first - base) : 0u);
+        const int before = __popc(__ballot_sync(FULL, leader && first < base));
         const int w = base + lane;
         unsigned key = kSetEmpty;
         bool direct = false;
         int cx = 0, cy = 0, cz = 0;
         if (w < work) {
-            int r = 0;  // the last cube whose first item is <= w
-            while (r + 1 < nlead && (cubes[r + 1].w >> 12) <= w) r++;
-            const int4 cb = cubes[r];
-            const int c = w - (cb.w >> 12);
-            const int ey = ((cb.w >> 4) & 15) + 1, ez = ((cb.w >> 8) & 15) + 1;
-            cz = cb.z + c % ez;
-            cy = cb.y + (c / ez) % ey;
-            cx = cb.x + c / (ez * ey);
-            if (packable(cx, cy, cz)) {
-                const unsigned ox = (unsigned)(cx - cbx + kSetOff), oy = (unsigned)(cy - cby + kSetOff),
-                               oz = (unsigned)(cz - cbz + kSetOff);
-                if (ox < 2u * kSetOff && oy < 2u * kSetOff && oz < 2u * kSetOff) key = (ox << 20) | (oy << 10) | oz;
-                else direct = true;
-            } else {
-                atomicOr(&g.ctr->status, kStRange);
+            const int4 cb = cubes[before + __popc(starts & (0xffffffffu >> (31 - lane))) - 1];
+            const int c = w - (cb.w >> 16), sz = (cb.w >> 11) & 3, sy = (cb.w >> 9) & 3;
+            const int dz = c & ((1 << sz) - 1), dy = (c >> sz) & ((1 << sy) - 1), dx = c >> (sz + sy);
+            if (dx <= (cb.w & 7) && dy <= ((cb.w >> 3) & 7) && dz <= ((cb.w >> 6) & 7)) {
+                cx = cb.x + dx;
+                cy = cb.y + dy;
+                cz = cb.z + dz;
+                if (packable(cx, cy, cz)) {
+                    const unsigned ox = (unsigned)(cx - cbx + kSetOff), oy = (unsigned)(cy - cby + kSetOff),
+                                   oz = (unsigned)(cz - cbz + kSetOff);
+                    if (ox < 2u * kSetOff && oy < 2u * kSetOff && oz < 2u * kSetOff) key = (ox << 20) | (oy << 10) | oz;
+                    else direct = true;
+                } else {
+                    atomicOr(&g.ctr->status, kStRange);
+                }
             }
         }
         if (direct) visit_one(g, cx, cy, cz, visit);  // outside the key range
@@ -206,16 +219,39 @@ __device__ __forceinline__ void tile_flush_set(const GridView &g, unsigned *cset
 // visitor of the epoch appends it (replaces alreadyIntegrated and the
 // O(capacity) "Reset booleans" pass); the 64-bit atomicMax on (epoch, packed
 // coordinates) also fixes an aliased entry's coordinates canonically (the
-// largest packed coordinate of the call).
-__device__ __forceinline__ bool find_and_stamp(const GridView &g, uint32_t epoch, int bx, int by, int bz,
-                                               int &bucket) {
-    bool inserted = false;
-    bucket = table_find_or_insert(g, prime_hash(bx, by, bz), &inserted);
-    if (inserted) super_insert(g, bx, by, bz);
-    if (bucket < 0) return false;
-    const unsigned long long old =
-        atomicMax(g.stamp + bucket, ((unsigned long long)epoch << kEpochShift) | pack_coords(bx, by, bz));
-    return (uint32_t)(old >> kEpochShift) != epoch;
+// largest packed coordinate of the call). Most visits find the block in its
+// home bucket, already stamped by an earlier tile: the home bucket's key and
+// stamp (and, with a side array, the block's word of it) are loaded together,
+// so such a visit costs one round trip to L2 and no atomic. A stamp that
+// already holds this call's value or a larger one would not change, and its
+// epoch says "not first", so skipping the atomicMax then changes nothing.
+// With a side array (words per bucket `side_stride`), the block's word
+// `side_word` gets `side_bit` ORed in (a load first: it is usually set).
+template <bool kSide = false>
+__device__ __forceinline__ bool find_and_stamp(const GridView &g, uint32_t epoch, int bx, int by, int bz, int &bucket,
+                                               uint32_t *side = nullptr, int side_stride = 0, int side_word = 0,
+                                               uint32_t side_bit = 0) {
+    const unsigned long long key = prime_hash(bx, by, bz);
+    const unsigned long long val = ((unsigned long long)epoch << kEpochShift) | pack_coords(bx, by, bz);
+    const uint32_t home = home_bucket(key, g.mask);
+    const unsigned long long k0 = ld_relaxed(g.keys + home);
+    const unsigned long long s0 = ld_relaxed(g.stamp + home);
+    uint32_t m0 = 0;
+    if (kSide) m0 = ld_relaxed_u32(side + (size_t)home * side_stride + side_word);
+    bool append = false;
+    if (k0 == key) {
+        bucket = (int)home;
+        if (s0 < val) append = (uint32_t)(atomicMax(g.stamp + home, val) >> kEpochShift) != epoch;
+    } else {
+        bool inserted = false;
+        bucket = table_find_or_insert(g, key, &inserted);
+        if (inserted) super_insert(g, bx, by, bz);
+        if (bucket < 0) return false;
+        append = (uint32_t)(atomicMax(g.stamp + bucket, val) >> kEpochShift) != epoch;
+        if (kSide) m0 = ld_relaxed_u32(side + (size_t)bucket * side_stride + side_word);
+    }
+    if (kSide && !(m0 & side_bit)) atomicOr(side + (size_t)bucket * side_stride + side_word, side_bit);
+    return append;
 }
 
 }  // namespace ss

@@ -546,6 +546,7 @@ ss_status ss_grid_create(const ss_params *p, ss_grid **out) {
     g->v.mask = p->hash_buckets - 1;
     g->v.vl = p->voxel_length;
     g->v.vbl = kEdge * p->voxel_length;  // GPUVoxelGrid.cpp:15
+    g->v.rvbl = 1.0f / g->v.vbl;
     g->v.trunc = p->truncation;
     g->v.rmin = p->rmin;
     g->v.d_max = p->d_max;

@@ -96,6 +96,7 @@ struct GridView {
     uint32_t sbmask;            // sb_buckets - 1
     uint32_t mask;              // buckets - 1
     float vl, vbl, trunc, rmin, d_max, max_weight;
+    float rvbl;  // RN(1 / vbl), computed on the host
     int resi, resj;
     Intr in;
     // getPoint's per-column and per-row quotients (j - cj) / fx and
@@ -153,8 +154,16 @@ __device__ __forceinline__ F3 get_point(const Intr &in, int i, int j, float d) {
             __fmul_rn(__fdiv_rn(__fsub_rn((float)i, in.ci), in.fy), d), d};
 }
 
-// (float)(depth) / 1000 (GPUVoxelGrid.h:306)
-__device__ __forceinline__ float depth_m(uint16_t d) { return __fdiv_rn((float)d, 1000.f); }
+// (float)(depth) / 1000 (GPUVoxelGrid.h:306), the IEEE quotient, as
+// q0 = RN(d y) with y = RN(1/1000), then one residual correction
+// q = RN(q0 + RN(d - q0 1000) y) (the remainder d - q0 1000 is exact in one
+// fma). Equal to the correctly rounded quotient for every u16 d: the whole
+// input range is checked in exact arithmetic (tests/test_device_arith.py).
+__device__ __forceinline__ float depth_m(uint16_t d) {
+    const float a = (float)d, y = 1.0e-3f;
+    const float q0 = __fmul_rn(a, y);
+    return __fmaf_rn(__fmaf_rn(-q0, 1000.f, a), y, q0);
+}
 
 // Index rule of getIndeces / getVBIndeces / getVinVBIndeces
 // (GPUVoxelGrid.h:131-221): a >= 0 ? (int)(a/len) : (int)(a/len - 1).
@@ -215,6 +224,11 @@ __device__ __forceinline__ uint32_t home_bucket(unsigned long long key, uint32_t
 __device__ __forceinline__ unsigned long long ld_relaxed(const unsigned long long *p) {
     unsigned long long v;
     asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ uint32_t ld_relaxed_u32(const uint32_t *p) {
+    uint32_t v;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
     return v;
 }
 

@@ -27,8 +27,9 @@
 namespace ss {
 
 // A block visited by the batched collection in one phase: find or insert,
-// set the phase's bit in the block's mask (a plain load first: other tiles of
-// the phase have mostly set it already), stamp with the batch's epoch.
+// stamp with the batch's epoch, set the phase's bit in the block's mask (a
+// load first, with the home bucket's key and stamp: other tiles of the phase
+// have mostly set it already).
 struct RefuseVisit {
     GridView g;
     uint32_t epoch;
@@ -36,12 +37,7 @@ struct RefuseVisit {
     int word;
     uint32_t bit;
     __device__ __forceinline__ bool operator()(int bx, int by, int bz, int &bucket) {
-        const bool append = find_and_stamp(g, epoch, bx, by, bz, bucket);
-        if (bucket >= 0) {
-            uint32_t *w = phase_mask + (size_t)bucket * kPhaseWords + word;
-            if (!(*(volatile uint32_t *)w & bit)) atomicOr(w, bit);
-        }
-        return append;
+        return find_and_stamp<true>(g, epoch, bx, by, bz, bucket, phase_mask, kPhaseWords, word, bit);
     }
 };
 
