@@ -76,13 +76,11 @@ __device__ __forceinline__ void tile_fill_set(const GridView &g, const uint16_t 
             F3 pt = xform(E, p);
             F3 t{g.trunc, g.trunc, g.trunc};
             F3 lo = f3sub(pt, t), hi = f3add(pt, t);
-            const float rvbl = g.rvbl;
-            lox = idx_rule_r(lo.x, g.vbl, rvbl);
-            loy = idx_rule_r(lo.y, g.vbl, rvbl);
-            loz = idx_rule_r(lo.z, g.vbl, rvbl);
-            nx = idx_rule_r(hi.x, g.vbl, rvbl) - lox + 1;
-            ny = idx_rule_r(hi.y, g.vbl, rvbl) - loy + 1;
-            nz = idx_rule_r(hi.z, g.vbl, rvbl) - loz + 1;
+            int hix, hiy, hiz;
+            block_range(lo, hi, g.vbl, g.rvbl, lox, loy, loz, hix, hiy, hiz);
+            nx = hix - lox + 1;
+            ny = hiy - loy + 1;
+            nz = hiz - loz + 1;
             if (nx < 1 || ny < 1 || nz < 1 || nx > 8 || ny > 8 || nz > 8) {
                 atomicOr(&g.ctr->status, kStRange);  // non-finite pose or truncation > 3.5 blocks
                 nx = ny = nz = 0;

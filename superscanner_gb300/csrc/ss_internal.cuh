@@ -178,15 +178,32 @@ __device__ __forceinline__ int idx_rule(float a, float len) {
 // q = RN(a / len) (u = 2^-24: three roundings), and RN(q - 1) within a
 // further u (|q1| + 1) of q - 1, so when q1 lies more than 5 u (|q1| + 1)
 // from every integer, no integer separates q from q1 or RN(q - 1) from
-// RN(q1 - 1), and the truncations agree. Otherwise (and for zero, huge or
-// non-finite values) the IEEE division decides. One multiply instead of a
-// division in all but a few cases per million.
-__device__ __forceinline__ int idx_rule_r(float a, float len, float rlen) {
+// RN(q1 - 1), and the truncations agree; both are then floor(q1) (a >= 0:
+// q1 >= 0 is no integer; a < 0: neither is RN(q1 - 1), which truncates to
+// floor(q1)). idx_fast returns false where q1 is too close to an integer (and
+// for zero, huge or non-finite values): there the IEEE division decides.
+__device__ __forceinline__ bool idx_fast(float a, float rlen, int &out) {
     const float q1 = __fmul_rn(a, rlen);
-    const float margin = 3.0e-7f * (fabsf(q1) + 1.f);  // > 5 * 2^-24 (|q1| + 1)
-    if (fabsf(q1 - rintf(q1)) > margin)
-        return a >= 0.f ? __float2int_rz(q1) : __float2int_rz(__fsub_rn(q1, 1.f));
-    return idx_rule(a, len);
+    out = __float2int_rd(q1);
+    return fabsf(__fsub_rn(q1, rintf(q1))) > __fmaf_rn(fabsf(q1), 3.0e-7f, 3.0e-7f);  // > 5 u (|q1| + 1)
+}
+
+// The block range of a point's truncation band: idx_rule of its corners lo
+// and hi, six multiplications and one check for all six; the six IEEE
+// divisions only when some quotient is too close to an integer (a few
+// pixels per million).
+__device__ __forceinline__ void block_range(F3 lo, F3 hi, float len, float rlen, int &lx, int &ly, int &lz, int &hx,
+                                            int &hy, int &hz) {
+    const bool ok = idx_fast(lo.x, rlen, lx) & idx_fast(lo.y, rlen, ly) & idx_fast(lo.z, rlen, lz) &
+                    idx_fast(hi.x, rlen, hx) & idx_fast(hi.y, rlen, hy) & idx_fast(hi.z, rlen, hz);
+    if (!ok) {
+        lx = idx_rule(lo.x, len);
+        ly = idx_rule(lo.y, len);
+        lz = idx_rule(lo.z, len);
+        hx = idx_rule(hi.x, len);
+        hy = idx_rule(hi.y, len);
+        hz = idx_rule(hi.z, len);
+    }
 }
 
 // getPrimeHash (GPUVoxelGrid.h:124-128), int wrap, sign-extended to u64.

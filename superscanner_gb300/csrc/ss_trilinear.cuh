@@ -65,42 +65,30 @@ __device__ __forceinline__ TriSample trilinear(const GridView &g, float px, floa
         if (!c.cok) return r;
 #pragma unroll
         for (int k = 0; k < 8; k++) s[k] = c.cs[k];
-    } else if ((ix & 7) != 7 && (iy & 7) != 7 && (iz & 7) != 7) {
-        // all 8 corners in one block: one lookup, fixed offsets +1, +8, +64
-        c.cx = ix, c.cy = iy, c.cz = iz, c.cok = false;
-        const int b = cached_lookup(g, c, ix >> 3, iy >> 3, iz >> 3);
-        if (b < 0) return r;
-        const int v0 = (ix & 7) + 8 * (iy & 7) + 64 * (iz & 7);
-        float2 sw[8];
-#pragma unroll
-        for (int k = 0; k < 8; k++) sw[k] = voxel_sw<kStorage>(g, b, v0 + (k & 1) + 8 * ((k >> 1) & 1) + 64 * (k >> 2));
-        c.voxels += 8;
-        bool ok = true;
-#pragma unroll
-        for (int k = 0; k < 8; k++) {
-            ok &= sw[k].y > 0.f;
-            s[k] = sw[k].x;
-            c.cs[k] = s[k];
-        }
-        c.cok = ok;
-        if (!ok) return r;
     } else {
-        // the cell straddles block faces: each distinct block is looked up once
-        // (corner (a, b, c) lies in block offset (a sx, b sy, c sz))
+        // The cell's 8 corners: one lookup of the cell's lowest block, and,
+        // for a cell straddling block faces, one find of each further block
+        // (corner (a, b, c) lies in block offset (a sx, b sy, c sz)). One code
+        // path for both kinds of cell, so that the corner loads of a warp
+        // whose lanes hold both kinds are issued together.
         c.cx = ix, c.cy = iy, c.cz = iz, c.cok = false;
         const int bx0 = ix >> 3, by0 = iy >> 3, bz0 = iz >> 3;
         const bool sx = (ix & 7) == 7, sy = (iy & 7) == 7, sz = (iz & 7) == 7;
         int bk[8];
         bk[0] = cached_lookup(g, c, bx0, by0, bz0);
         if (bk[0] < 0) return r;
-        bk[1] = sx ? block_find(g, c, bx0 + 1, by0, bz0) : bk[0];
-        bk[2] = sy ? block_find(g, c, bx0, by0 + 1, bz0) : bk[0];
-        bk[4] = sz ? block_find(g, c, bx0, by0, bz0 + 1) : bk[0];
-        bk[3] = (sx && sy) ? block_find(g, c, bx0 + 1, by0 + 1, bz0) : (sx ? bk[1] : bk[2]);
-        bk[5] = (sx && sz) ? block_find(g, c, bx0 + 1, by0, bz0 + 1) : (sx ? bk[1] : bk[4]);
-        bk[6] = (sy && sz) ? block_find(g, c, bx0, by0 + 1, bz0 + 1) : (sy ? bk[2] : bk[4]);
-        bk[7] = (sx && sy && sz) ? block_find(g, c, bx0 + 1, by0 + 1, bz0 + 1)
-                                 : (sx && sy ? bk[3] : (sx && sz ? bk[5] : (sy && sz ? bk[6] : (sx ? bk[1] : (sy ? bk[2] : bk[4])))));
+#pragma unroll
+        for (int k = 1; k < 8; k++) bk[k] = bk[0];
+        if (sx | sy | sz) {
+            if (sx) bk[1] = block_find(g, c, bx0 + 1, by0, bz0);
+            if (sy) bk[2] = block_find(g, c, bx0, by0 + 1, bz0);
+            if (sz) bk[4] = block_find(g, c, bx0, by0, bz0 + 1);
+            bk[3] = (sx && sy) ? block_find(g, c, bx0 + 1, by0 + 1, bz0) : (sx ? bk[1] : bk[2]);
+            bk[5] = (sx && sz) ? block_find(g, c, bx0 + 1, by0, bz0 + 1) : (sx ? bk[1] : bk[4]);
+            bk[6] = (sy && sz) ? block_find(g, c, bx0, by0 + 1, bz0 + 1) : (sy ? bk[2] : bk[4]);
+            bk[7] = (sx && sy && sz) ? block_find(g, c, bx0 + 1, by0 + 1, bz0 + 1)
+                                     : (sx && sy ? bk[3] : (sx && sz ? bk[5] : (sy && sz ? bk[6] : (sx ? bk[1] : (sy ? bk[2] : bk[4])))));
+        }
         bool ok = true;
 #pragma unroll
         for (int k = 0; k < 8; k++) ok &= bk[k] >= 0;
