@@ -140,7 +140,9 @@ ss_status ss_integrate_fast(ss_grid *g, const uint16_t *depth, const uint8_t *rg
  * array of n device pointers to [resi][resj] u16 images; T_old, T_new: n x 16
  * row-major floats (host). Depth only. exact != 0 uses ss_integrate's
  * arithmetic, else ss_integrate_fast's; the volume equals the 2n sequential
- * calls bit for bit. */
+ * calls bit for bit. The first call on a grid allocates the batch buffers
+ * (64 bytes per hash bucket); n = 0 only allocates them, so that a caller can
+ * keep allocation out of a later re-fusion. */
 ss_status ss_refuse_batch(ss_grid *g, int32_t n, const uint16_t *const *depths, const float *T_old,
                           const float *T_new, int32_t exact, ss_stream_t s);
 

@@ -62,29 +62,36 @@ __device__ __forceinline__ void visit_one(const GridView &g, int bx, int by, int
     else atomicOr(&g.ctr->status, kStListOverflow);
 }
 
-// Phase 1 for pixel (i, j) of the tile (every thread of the CTA calls it; the
-// set must be cleared and the CTA synced before).
+// The camera-frame point of pixel (i, j) (depthToPcdTag, GPUVoxelGrid.h:303-307)
+// and whether it takes part (inside the image, z > rmin): the part of a
+// pixel's collection that does not depend on the pose.
+__device__ __forceinline__ bool tile_point(const GridView &g, const uint16_t *__restrict__ depth, int i, int j, F3 &p) {
+    p = F3{0.f, 0.f, 0.f};
+    if (!(i < g.resi && j < g.resj)) return false;
+    p = get_point_t(g, i, j, depth_m(__ldg(depth + (size_t)i * g.resj + j)));
+    return p.z > g.rmin;
+}
+
+// Phase 1 for a pixel of the tile with camera-frame point p (valid: from
+// tile_point) at pose E (every thread of the CTA calls it; the set must be
+// cleared and the CTA synced before).
 template <class Visit>
-__device__ __forceinline__ void tile_fill_set(const GridView &g, const uint16_t *__restrict__ depth, const Mat34 &E,
-                                              int i, int j, unsigned *cset, int slots, int cbx, int cby, int cbz,
-                                              Visit &visit) {
+__device__ __forceinline__ void tile_fill_set(const GridView &g, F3 p, bool valid, const Mat34 &E, unsigned *cset,
+                                              int slots, int cbx, int cby, int cbz, Visit &visit) {
     const unsigned FULL = 0xffffffffu;
     int lox = 0, loy = 0, loz = 0, nx = 0, ny = 0, nz = 0;
-    if (i < g.resi && j < g.resj) {
-        F3 p = get_point_t(g, i, j, depth_m(__ldg(depth + (size_t)i * g.resj + j)));
-        if (p.z > g.rmin) {
-            F3 pt = xform(E, p);
-            F3 t{g.trunc, g.trunc, g.trunc};
-            F3 lo = f3sub(pt, t), hi = f3add(pt, t);
-            int hix, hiy, hiz;
-            block_range(lo, hi, g.vbl, g.rvbl, lox, loy, loz, hix, hiy, hiz);
-            nx = hix - lox + 1;
-            ny = hiy - loy + 1;
-            nz = hiz - loz + 1;
-            if (nx < 1 || ny < 1 || nz < 1 || nx > 8 || ny > 8 || nz > 8) {
-                atomicOr(&g.ctr->status, kStRange);  // non-finite pose or truncation > 3.5 blocks
-                nx = ny = nz = 0;
-            }
+    if (valid) {
+        const F3 pt = xform(E, p);
+        const F3 t{g.trunc, g.trunc, g.trunc};
+        const F3 lo = f3sub(pt, t), hi = f3add(pt, t);
+        int hix, hiy, hiz;
+        block_range(lo, hi, g.vbl, g.rvbl, lox, loy, loz, hix, hiy, hiz);
+        nx = hix - lox + 1;
+        ny = hiy - loy + 1;
+        nz = hiz - loz + 1;
+        if (nx < 1 || ny < 1 || nz < 1 || nx > 8 || ny > 8 || nz > 8) {
+            atomicOr(&g.ctr->status, kStRange);  // non-finite pose or truncation > 3.5 blocks
+            nx = ny = nz = 0;
         }
     }
     const int total = nx * ny * nz;

@@ -149,8 +149,9 @@ __global__ void __launch_bounds__(256, 8) collect_kernel(GridView g, const uint1
     camera_block(g, E, cbx, cby, cbz);
     SS_CT(0);
     __syncthreads();
-    tile_fill_set(g, depth, E, blockIdx.y * blockDim.y + threadIdx.y, blockIdx.x * 32 + threadIdx.x, cset, slots, cbx,
-                  cby, cbz, visit);
+    F3 p;
+    const bool valid = tile_point(g, depth, blockIdx.y * blockDim.y + threadIdx.y, blockIdx.x * 32 + threadIdx.x, p);
+    tile_fill_set(g, p, valid, E, cset, slots, cbx, cby, cbz, visit);
     SS_CT(2);
     __syncthreads();
     SS_CT(3);

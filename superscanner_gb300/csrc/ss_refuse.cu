@@ -5,8 +5,8 @@
 // each with a block collection, a D2H count read and a device fence).
 //
 // Two launches for the whole batch:
-//  1. refuse_collect_kernel, grid (tiles, phases): phase 2k deintegrates and
-//     2k+1 integrates keyframe k. Each tile's candidate blocks are
+//  1. refuse_collect_kernel, grid (tiles, keyframes): phase 2k deintegrates
+//     and 2k+1 integrates keyframe k. Each tile's candidate blocks are
 //     deduplicated in shared memory and found or inserted as in
 //     collect_kernel (ss_collect.cuh); the first visitor of the batch appends
 //     the block to the list, and every phase ORs its bit into the block's
@@ -41,28 +41,37 @@ struct RefuseVisit {
     }
 };
 
-// Grid (tiles, tiles, phases): the tile phases of collect_kernel (ss_collect.cuh)
-// for the depth and pose of one phase. Registers capped as in collect_kernel.
+// Grid (tiles, tiles, keyframes): the tile phases of collect_kernel
+// (ss_collect.cuh) for both phases of one keyframe, which share its depth
+// image: the tile's depth and camera-frame points are read once, then the
+// deintegration phase (old pose) and the integration phase (new pose) each
+// fill and flush the tile's set. Registers capped as in collect_kernel.
 __global__ void __launch_bounds__(256, 8) refuse_collect_kernel(GridView g, const uint16_t *const *__restrict__ depths,
                                                                 const FramePose *__restrict__ poses,
                                                                 uint32_t *__restrict__ phase_mask) {
     extern __shared__ unsigned cset[];  // [slots] keys, then [slots] per-warp lists
     const int slots = kSetSlotsPerRow * blockDim.y;
     const int tid = threadIdx.y * blockDim.x + threadIdx.x, nthreads = blockDim.x * blockDim.y;
-    for (int q = tid; q < slots; q += nthreads) cset[q] = kSetEmpty;
-    const int phase = blockIdx.z;
-    const uint16_t *depth = depths[phase >> 1];
-    Mat34 E;
+    F3 p;
+    const bool valid =
+        tile_point(g, depths[blockIdx.z], blockIdx.y * blockDim.y + threadIdx.y, blockIdx.x * 32 + threadIdx.x, p);
+    const uint32_t epoch = *(volatile uint32_t *)&g.ctr->epoch;
+#pragma unroll 1
+    for (int h = 0; h < 2; h++) {
+        const int phase = 2 * blockIdx.z + h;
+        if (h) __syncthreads();  // the first phase's flush has read the set
+        for (int q = tid; q < slots; q += nthreads) cset[q] = kSetEmpty;
+        Mat34 E;
 #pragma unroll
-    for (int k = 0; k < 12; k++) E.m[k] = __ldg(&poses[phase].E.m[k]);
-    RefuseVisit visit{g, *(volatile uint32_t *)&g.ctr->epoch, phase_mask, phase >> 5, 1u << (phase & 31)};
-    int cbx, cby, cbz;
-    camera_block(g, E, cbx, cby, cbz);
-    __syncthreads();
-    tile_fill_set(g, depth, E, blockIdx.y * blockDim.y + threadIdx.y, blockIdx.x * 32 + threadIdx.x, cset, slots, cbx,
-                  cby, cbz, visit);
-    __syncthreads();
-    tile_flush_set(g, cset, slots, cbx, cby, cbz, visit);
+        for (int k = 0; k < 12; k++) E.m[k] = __ldg(&poses[phase].E.m[k]);
+        RefuseVisit visit{g, epoch, phase_mask, phase >> 5, 1u << (phase & 31)};
+        int cbx, cby, cbz;
+        camera_block(g, E, cbx, cby, cbz);
+        __syncthreads();
+        tile_fill_set(g, p, valid, E, cset, slots, cbx, cby, cbz, visit);
+        __syncthreads();
+        tile_flush_set(g, cset, slots, cbx, cby, cbz, visit);
+    }
 }
 
 template <int kStorage, bool kExact>
@@ -179,7 +188,6 @@ extern "C" ss_status ss_refuse_batch(ss_grid *g, int32_t n, const uint16_t *cons
     if (!g || n < 0 || (n > 0 && (!depths || !T_old || !T_new))) return SS_ERR_ARG;
     if (!g->intr_set) return SS_ERR_STATE;
     if (2 * n > kMaxPhases) return SS_ERR_DIMS;
-    if (n == 0) return SS_OK;
     for (int k = 0; k < n; k++) {
         if (!depths[k]) return SS_ERR_ARG;
         for (int q = 0; q < 16; q++)
@@ -196,6 +204,7 @@ extern "C" ss_status ss_refuse_batch(ss_grid *g, int32_t n, const uint16_t *cons
         }
         SS_CUDA_TRY(cudaMemsetAsync(g->phase_mask, 0, B * kPhaseWords * sizeof(uint32_t), s));
     }
+    if (n == 0) return SS_OK;
     if (g->host_epoch >= kEpochMax) {
         ss_status st = rebase_epoch(g, s);
         if (st != SS_OK) return st;
@@ -209,7 +218,7 @@ extern "C" ss_status ss_refuse_batch(ss_grid *g, int32_t n, const uint16_t *cons
     SS_CUDA_TRY(cudaMemcpyAsync(g->batch_depths, depths, n * sizeof(uint16_t *), cudaMemcpyHostToDevice, s));
     SS_CUDA_TRY(cudaMemsetAsync(&g->v.ctr->work, 0, sizeof(int), s));
     constexpr int kRows = 4;
-    const dim3 cblk(32, kRows), cgrid((g->p.resj + 31) / 32, (g->p.resi + kRows - 1) / kRows, 2 * n);
+    const dim3 cblk(32, kRows), cgrid((g->p.resj + 31) / 32, (g->p.resi + kRows - 1) / kRows, n);
     refuse_collect_kernel<<<cgrid, cblk, tile_set_bytes(kRows), s>>>(g->v, g->batch_depths, g->batch_poses,
                                                                      g->phase_mask);
     SS_LAUNCH_CHECK();

@@ -107,7 +107,8 @@ class GPUVoxelGrid:
 
     def refuse_batch(self, depths, T_old, T_new, exact: bool = False, stream=None) -> None:
         """Re-fuse keyframes: for each k, deintegrate depths[k] at T_old[k] and integrate it at T_new[k]
-        (in order), in one collection and one persistent apply launch."""
+        (in order), in one collection and one persistent apply launch. With no keyframes it only
+        allocates the batch buffers (the first call on a grid does that otherwise)."""
         n = len(depths)
         for d in depths:
             _dev_ptr(d, 2, (self.resi, self.resj), "depth")

@@ -40,6 +40,8 @@ def test_batched_refusion_equals_sequential(storage, exact):
         g = GPUVoxelGrid(int(1e9), 0.016, 0.004, 480, 640, storage=storage, with_color=False,
                          hash_buckets=1 << 18, max_weight=255)
         g.setIntrinsic(*INTR)
+        if batched:
+            g.refuse_batch([], [], [])  # no keyframes: allocates the batch buffers, changes nothing
         for k in range(40):
             if exact:
                 g.integrate(None, dev[k], P[k].astype(np.float32), withColor=False)
