@@ -9,59 +9,41 @@
 namespace ss {
 
 // One voxel of integrationCore[Color]Tag / deIntegrationCore[Color]Tag
-// (GPUVoxelGrid.cpp:345-469, 516-550). Returns true when the voxel changes;
-// pixel (cori, corj) and the observed sdf come back through the references.
-template <bool kExact>
+// (GPUVoxelGrid.cpp:345-469, 516-550) in the reference's arithmetic. Returns
+// true when the voxel changes; pixel (cori, corj) and the observed sdf come
+// back through the references.
 __device__ __forceinline__ bool voxel_observe(const GridView &g, const uint16_t *__restrict__ depth, const Mat34 &E,
                                               const Mat34 &Einv, const F3 &Ez, F3 vm, float &sdf, int &pix) {
-    F3 q;
-    float c0, c1;
-    if (kExact) {
-        q = xform(Einv, vm);
-        c0 = __fadd_rn(__fdiv_rn(__fmul_rn(q.y, g.in.fy), q.z), g.in.ci);  // getCoordinate (GPUVoxelGrid.h:234-237)
-        c1 = __fadd_rn(__fdiv_rn(__fmul_rn(q.x, g.in.fx), q.z), g.in.cj);
-    } else {
-        q.x = fmaf(vm.x, Einv.m[0], fmaf(vm.y, Einv.m[1], fmaf(vm.z, Einv.m[2], Einv.m[3])));
-        q.y = fmaf(vm.x, Einv.m[4], fmaf(vm.y, Einv.m[5], fmaf(vm.z, Einv.m[6], Einv.m[7])));
-        q.z = fmaf(vm.x, Einv.m[8], fmaf(vm.y, Einv.m[9], fmaf(vm.z, Einv.m[10], Einv.m[11])));
-        float rz;  // the pixel choice only needs the projection to ~1 ulp
-        asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(rz) : "f"(q.z));
-        c0 = fmaf(q.y * g.in.fy, rz, g.in.ci);
-        c1 = fmaf(q.x * g.in.fx, rz, g.in.cj);
-    }
-    // exact: the reference's (int) cast (GPUVoxelGrid.cpp:348-349), which picks the pixel half a pixel
-    // off the projection; fast: the nearest pixel (the truncation makes frame-to-model tracking drift)
-    const int cori = kExact ? __float2int_rz(c0) : __float2int_rd(c0 + 0.5f);
-    const int corj = kExact ? __float2int_rz(c1) : __float2int_rd(c1 + 0.5f);
+    const F3 q = xform(Einv, vm);
+    const float c0 = __fadd_rn(__fdiv_rn(__fmul_rn(q.y, g.in.fy), q.z), g.in.ci);  // getCoordinate (GPUVoxelGrid.h:234-237)
+    const float c1 = __fadd_rn(__fdiv_rn(__fmul_rn(q.x, g.in.fx), q.z), g.in.cj);
+    // the reference's (int) cast (GPUVoxelGrid.cpp:348-349), which picks the pixel half a pixel off the projection
+    const int cori = __float2int_rz(c0);
+    const int corj = __float2int_rz(c1);
     if (!(cori < g.resi && corj < g.resj && cori >= 0 && corj >= 0)) return false;
     pix = cori * g.resj + corj;
-    const uint16_t dmm = __ldg(depth + pix);
-    if (kExact) {
-        F3 vpt = get_point(g.in, cori, corj, depth_m(dmm));
-        if (!(vpt.z > g.rmin)) return false;
-        vpt = xform(E, vpt);
-        sdf = f3dot(f3sub(vpt, vm), Ez);
-    } else {
-        const float d = (float)dmm * 1.0e-3f;
-        if (!(d > g.rmin)) return false;
-        // (E p - vm) . Ez with p the pixel's point at depth d: for a rigid E
-        // this is d - q.z (q = E^-1 vm), the projective distance along the
-        // camera axis; a voxel behind the camera gets d + |q.z| > trunc
-        sdf = d - q.z;
-    }
+    F3 vpt = get_point(g.in, cori, corj, depth_m(__ldg(depth + pix)));
+    if (!(vpt.z > g.rmin)) return false;
+    vpt = xform(E, vpt);
+    sdf = f3dot(f3sub(vpt, vm), Ez);
     return fabsf(sdf) < g.trunc;
 }
 
 // The fast path's observation of a voxel from its camera-frame point q =
-// Einv vm: the nearest pixel (within the image), its depth d > rmin, and the
-// projective sdf d - q.z within the truncation (the expression of
-// voxel_observe<false> after its projection).
+// Einv vm: the nearest pixel (the reference's truncation picks the pixel half
+// a pixel off the projection, which makes frame-to-model tracking drift),
+// within the image, with the half pixel of the rounding folded into the
+// principal point and the projection from an approximate reciprocal (the
+// pixel choice only needs it to ~1 ulp); its depth d > rmin; and the
+// projective sdf d - q.z within the truncation: for a rigid E, (E p - vm) . Ez
+// with p the pixel's point at depth d is d - q.z, the distance along the
+// camera axis (a voxel behind the camera gets d + |q.z| > trunc).
 __device__ __forceinline__ bool observe_fast(const GridView &g, const uint16_t *__restrict__ depth, F3 q, float &sdf,
                                              int &pix) {
     float rz;
     asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(rz) : "f"(q.z));
-    const int cori = __float2int_rd(fmaf(q.y * g.in.fy, rz, g.in.ci) + 0.5f);
-    const int corj = __float2int_rd(fmaf(q.x * g.in.fx, rz, g.in.cj) + 0.5f);
+    const int cori = __float2int_rd(fmaf(q.y * g.in.fy, rz, g.in.ci + 0.5f));
+    const int corj = __float2int_rd(fmaf(q.x * g.in.fx, rz, g.in.cj + 0.5f));
     if (!(cori < g.resi && corj < g.resj && cori >= 0 && corj >= 0)) return false;
     pix = cori * g.resj + corj;
     const float d = (float)__ldg(depth + pix) * 1.0e-3f;

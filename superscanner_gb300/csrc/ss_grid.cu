@@ -219,7 +219,7 @@ __global__ void __launch_bounds__(256, 8) fuse_kernel(GridView g, const uint16_t
             const size_t vi = (size_t)bucket * kBlockVoxels + v;
             float obs;
             int pix;
-            if (kExact ? !voxel_observe<true>(g, depth, E, Einv, Ez, vm, obs, pix)
+            if (kExact ? !voxel_observe(g, depth, E, Einv, Ez, vm, obs, pix)
                        : !observe_fast(g, depth, qf[rr], obs, pix))
                 continue;
             float s, w;

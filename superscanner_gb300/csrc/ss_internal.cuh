@@ -64,7 +64,7 @@ struct Mat34 {
 // calls pass it by value; the per-frame pipeline keeps it in device memory
 // (written by the tracker) and passes a pointer, so no host round trip is
 // needed between tracking and fusion.
-struct FramePose {
+struct __align__(16) FramePose {  // 16-byte aligned: a kernel loads E or Einv as three float4
     Mat34 E;     // camera -> world, float (the reference's E view)
     Mat34 Einv;  // world -> camera, float (E_inv)
     float Ez[3]; // normalized third column of E

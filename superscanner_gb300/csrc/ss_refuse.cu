@@ -128,7 +128,7 @@ __global__ void __launch_bounds__(256) refuse_apply_kernel(GridView g, const uin
                 for (int rr = 0; rr < 4; rr++) {
                     float obs;
                     int pix;
-                    if (kExact ? !voxel_observe<true>(g, depth, fp.E, fp.Einv, F3{fp.Ez[0], fp.Ez[1], fp.Ez[2]}, vm[rr],
+                    if (kExact ? !voxel_observe(g, depth, fp.E, fp.Einv, F3{fp.Ez[0], fp.Ez[1], fp.Ez[2]}, vm[rr],
                                                       obs, pix)
                                : !observe_fast(g, depth, qf[rr], obs, pix))
                         continue;
