@@ -288,13 +288,18 @@ def se3_delta(rng, deg=2.0, cm=3.0):
     return D
 
 
-def run_refusion(torch, depth, P, stream, n_kf: int = 200, launch=None, modes=("sequential", "batched"), calls=1):
+def run_refusion(torch, depth, P, stream, n_kf: int = 200, launch=None, modes=("sequential", "batched"), calls=1,
+                 peak=None):
     """Config 4: the volume of the sequence (keyframes fused with seeded
     rectangular occlusions, 20-100 % coverage), then n_kf keyframes re-fused
     at poses corrected by seeded SE(3) deltas (<= 2 deg / 3 cm): one batched
     ss_refuse_batch call vs the 2 n_kf sequential calls, same volume state.
     With calls > 1 the re-fusion is repeated on the same volume, old and new
-    poses swapped between calls, and each call is timed."""
+    poses swapped between calls, and each call is timed. With the sequential
+    mode, the integrate/deintegrate algorithmic bytes of the first call
+    (every call's touched blocks x 512 voxels x 4 B read + 4 B written, plus
+    its depth image, from the grid's counters) give both modes' achieved
+    bandwidth, and its fraction of `peak` (GB/s)."""
     from superscanner_gb300 import GPUVoxelGrid, synth
     n = len(depth)
     n_kf = min(n_kf, n)
@@ -319,6 +324,7 @@ def run_refusion(torch, depth, P, stream, n_kf: int = 200, launch=None, modes=("
             if mode == "batched":
                 g.refuse_batch([], [], [], stream=stream)  # the batch buffers, allocated outside the timing
             torch.cuda.synchronize()
+            touched0 = g.counters(stream)["touched_total"]
             call_ms = []
             for c in range(calls):
                 old, new = (P[:n_kf], T_new) if c % 2 == 0 else (T_new, P[:n_kf])
@@ -333,6 +339,8 @@ def run_refusion(torch, depth, P, stream, n_kf: int = 200, launch=None, modes=("
                 ev1.record(stream)
                 torch.cuda.synchronize()
                 call_ms.append(ev0.elapsed_time(ev1))
+                if c == 0 and mode == "sequential":  # blocks touched by the 2 n_kf calls, summed over calls
+                    block_calls = g.counters(stream)["touched_total"] - touched0
         g.sync(stream)
         ms = call_ms[0]
         res[mode] = {"ms": round(ms, 3), "keyframes_per_s": round(n_kf / (ms * 1e-3), 1)}
@@ -342,6 +350,16 @@ def run_refusion(torch, depth, P, stream, n_kf: int = 200, launch=None, modes=("
         g.close()
     res["keyframes"] = n_kf
     res["coverage_min_max"] = [round(float(cover.min()), 3), round(float(cover.max()), 3)]
+    if "sequential" in res:
+        alg = block_calls * 512 * 4 * 2 + 2 * n_kf * ROWS * COLS * 2
+        res["algorithmic_bytes"] = {"value": int(alg), "block_calls": int(block_calls),
+                                    "note": "sum over the 2 n_kf integrate/deintegrate calls of touched blocks x "
+                                            "512 x (4 B read + 4 B written), plus each call's depth image"}
+        for m in modes:
+            gbs = alg / (res[m]["ms"] * 1e-3) / 1e9
+            res[m]["achieved_gbs"] = round(gbs, 1)
+            if peak:
+                res[m]["frac_of_peak"] = round(gbs / peak, 4)
     if len(dumps) < 2:
         return res
     a, b = dumps["sequential"], dumps["batched"]
@@ -705,7 +723,7 @@ def main_ours(args):
     if traffic is not None:
         roof["traffic_source"] = "ncu capture, " + tf.name
 
-    refusion = run_refusion(torch, depth, P, stream, launch=tuned) if rank == 0 else None
+    refusion = run_refusion(torch, depth, P, stream, launch=tuned, peak=peak) if rank == 0 else None
     precision = (run_precision_form(torch, depth, P, stream, n_frames=args.precision_frames, launch=tuned)
                  if rank == 0 and args.precision_frames > 1 else None)
     refinement = (run_pose_refinement(torch, depth, P, stream, n_frames=args.refine_frames)
