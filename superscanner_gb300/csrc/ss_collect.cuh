@@ -25,9 +25,13 @@
 // per distinct block per tile). 8 bytes of shared memory per slot (set and
 // per-warp lists) and 512 bytes per warp for its cubes: 6 KB per 4-row tile.
 //
-// A visitor is a callable bool (int bx, int by, int bz, int &bucket): it finds
-// or inserts the block, marks it, and returns true when this visit is the
-// one that appends bucket to the list.
+// A visitor is a callable bool (int bx, int by, int bz, unsigned tag, int
+// &bucket): it finds or inserts the block, marks it, and returns true when
+// this visit is the one that appends bucket to the list. A tagged set (the
+// batched re-fusion's) keeps per slot the OR of the tags (2 bits) of the
+// fills that entered the key, so several fills of one tile (a keyframe's two
+// phases) share the set and each distinct block is visited once with the tags
+// of all of them.
 #pragma once
 
 #include "ss_internal.cuh"
@@ -39,9 +43,15 @@ constexpr int kSetSlotsPerRow = 128;
 constexpr int kSetOff = 512;  // key offsets per axis: [-kSetOff, kSetOff) blocks
 
 // Dynamic shared memory of a tile of `rows` pixel rows (rows warps): the
-// set, the per-warp lists, and per warp 32 cube entries of 16 bytes.
-inline size_t tile_set_bytes(int rows) {
-    return (size_t)kSetSlotsPerRow * rows * 2 * sizeof(unsigned) + (size_t)rows * 32 * sizeof(int4);
+// set, the per-warp lists, per warp 32 cube entries of 16 bytes, and for a
+// tagged set the slots' tags.
+inline size_t tile_set_bytes(int rows, bool tagged = false) {
+    return (size_t)kSetSlotsPerRow * rows * (tagged ? 3 : 2) * sizeof(unsigned) + (size_t)rows * 32 * sizeof(int4);
+}
+
+// The slots' tags of a tagged set (after the cube entries).
+__device__ __forceinline__ unsigned *tile_tags(unsigned *cset, int slots) {
+    return cset + 2 * slots + blockDim.y * 32 * 4;
 }
 
 // The camera's block, about (the origin of the set's keys) of pose E: any
@@ -54,9 +64,9 @@ __device__ __forceinline__ void camera_block(const GridView &g, const Mat34 &E, 
 
 // One visit outside the tile's set, with its own append.
 template <class Visit>
-__device__ __forceinline__ void visit_one(const GridView &g, int bx, int by, int bz, Visit &visit) {
+__device__ __forceinline__ void visit_one(const GridView &g, int bx, int by, int bz, unsigned tag, Visit &visit) {
     int bucket = -1;
-    if (!visit(bx, by, bz, bucket)) return;
+    if (!visit(bx, by, bz, tag, bucket)) return;
     const int idx = atomicAdd(&g.ctr->list_count, 1);
     if (idx <= (int)g.mask) g.list[idx] = bucket;
     else atomicOr(&g.ctr->status, kStListOverflow);
@@ -73,12 +83,14 @@ __device__ __forceinline__ bool tile_point(const GridView &g, const uint16_t *__
 }
 
 // Phase 1 for a pixel of the tile with camera-frame point p (valid: from
-// tile_point) at pose E (every thread of the CTA calls it; the set must be
-// cleared and the CTA synced before).
-template <class Visit>
+// tile_point) at pose E (every thread of the CTA calls it; the set, and a
+// tagged set's tags, must be cleared and the CTA synced before; fills of a
+// tagged set may follow one another without a barrier).
+template <bool kTagged, class Visit>
 __device__ __forceinline__ void tile_fill_set(const GridView &g, F3 p, bool valid, const Mat34 &E, unsigned *cset,
-                                              int slots, int cbx, int cby, int cbz, Visit &visit) {
+                                              int slots, int cbx, int cby, int cbz, unsigned tag, Visit &visit) {
     const unsigned FULL = 0xffffffffu;
+    __syncwarp();  // the warp's lanes are done with its cube entries of an earlier fill
     int lox = 0, loy = 0, loz = 0, nx = 0, ny = 0, nz = 0;
     if (valid) {
         const F3 pt = xform(E, p);
@@ -159,27 +171,33 @@ __device__ __forceinline__ void tile_fill_set(const GridView &g, F3 p, bool vali
                 }
             }
         }
-        if (direct) visit_one(g, cx, cy, cz, visit);  // outside the key range
+        if (direct) visit_one(g, cx, cy, cz, tag, visit);  // outside the key range
         if (key == kSetEmpty) continue;
         // most blocks are already in the set (another warp or step put them
         // there): a plain load finds those without an atomic
         uint32_t h = (key * 0x9E3779B1u) >> hshift;  // the product's top bits (multiplicative hashing)
-        bool placed = false;
-        for (int probe = 0; probe < slots / 2 && !placed; probe++) {
+        int at = -1;
+        for (int probe = 0; probe < slots / 2 && at < 0; probe++) {
             h &= hmask;
             unsigned cur = ((volatile unsigned *)cset)[h];
             if (cur == kSetEmpty) cur = atomicCAS(cset + h, kSetEmpty, key);
-            placed = cur == kSetEmpty || cur == key;
+            if (cur == kSetEmpty || cur == key) at = (int)h;
             h++;
         }
-        if (!placed) visit_one(g, cx, cy, cz, visit);  // set too crowded
+        if (at < 0) {
+            visit_one(g, cx, cy, cz, tag, visit);  // set too crowded
+        } else if (kTagged) {
+            unsigned *tg = tile_tags(cset, slots) + at;
+            if ((*(volatile unsigned *)tg & tag) != tag) atomicOr(tg, tag);
+        }
     }
 }
 
 // Phase 2 (every thread of the CTA calls it after a CTA barrier that follows
-// phase 1): warp w compacts slots [w per, (w + 1) per) into its list and
-// visits its distinct blocks, appending with one atomic per warp step.
-template <class Visit>
+// phase 1): warp w compacts slots [w per, (w + 1) per) into its list (a key
+// has 30 bits; a tagged set's tag rides in the top two) and visits its
+// distinct blocks, appending with one atomic per warp step.
+template <bool kTagged, class Visit>
 __device__ __forceinline__ void tile_flush_set(const GridView &g, unsigned *cset, int slots, int cbx, int cby,
                                                int cbz, Visit &visit) {
     const unsigned FULL = 0xffffffffu;
@@ -192,7 +210,8 @@ __device__ __forceinline__ void tile_flush_set(const GridView &g, unsigned *cset
         const unsigned key = cset[wid * per + r + lane];
         const bool present = key != kSetEmpty;
         const unsigned b = __ballot_sync(FULL, present);
-        if (present) wlist[cnt + __popc(b & lt)] = key;
+        if (present)
+            wlist[cnt + __popc(b & lt)] = kTagged ? key | tile_tags(cset, slots)[wid * per + r + lane] << 30 : key;
         cnt += __popc(b);
     }
     __syncwarp();
@@ -202,8 +221,8 @@ __device__ __forceinline__ void tile_flush_set(const GridView &g, unsigned *cset
         int bucket = -1;
         if (e < cnt) {
             const unsigned key = wlist[e];
-            append = visit(cbx + (int)(key >> 20) - kSetOff, cby + (int)((key >> 10) & 1023u) - kSetOff,
-                           cbz + (int)(key & 1023u) - kSetOff, bucket);
+            append = visit(cbx + (int)((key >> 20) & 1023u) - kSetOff, cby + (int)((key >> 10) & 1023u) - kSetOff,
+                           cbz + (int)(key & 1023u) - kSetOff, kTagged ? key >> 30 : 1u, bucket);
         }
         const unsigned ap = __ballot_sync(FULL, append);
         if (ap) {
@@ -231,7 +250,8 @@ __device__ __forceinline__ void tile_flush_set(const GridView &g, unsigned *cset
 // already holds this call's value or a larger one would not change, and its
 // epoch says "not first", so skipping the atomicMax then changes nothing.
 // With a side array (words per bucket `side_stride`), the block's word
-// `side_word` gets `side_bit` ORed in (a load first: it is usually set).
+// `side_word` gets the bits `side_bit` ORed in (a load first: they are
+// usually set; the atomic unless all of them are).
 template <bool kSide = false>
 __device__ __forceinline__ bool find_and_stamp(const GridView &g, uint32_t epoch, int bx, int by, int bz, int &bucket,
                                                uint32_t *side = nullptr, int side_stride = 0, int side_word = 0,
@@ -255,7 +275,7 @@ __device__ __forceinline__ bool find_and_stamp(const GridView &g, uint32_t epoch
         append = (uint32_t)(atomicMax(g.stamp + bucket, val) >> kEpochShift) != epoch;
         if (kSide) m0 = ld_relaxed_u32(side + (size_t)bucket * side_stride + side_word);
     }
-    if (kSide && !(m0 & side_bit)) atomicOr(side + (size_t)bucket * side_stride + side_word, side_bit);
+    if (kSide && (m0 & side_bit) != side_bit) atomicOr(side + (size_t)bucket * side_stride + side_word, side_bit);
     return append;
 }
 

@@ -129,7 +129,7 @@ extern "C" int ss_debug_collect_timing(unsigned long long *out) {
 struct CollectVisit {
     GridView g;
     uint32_t epoch;
-    __device__ __forceinline__ bool operator()(int bx, int by, int bz, int &bucket) {
+    __device__ __forceinline__ bool operator()(int bx, int by, int bz, unsigned, int &bucket) {
         return find_and_stamp(g, epoch, bx, by, bz, bucket);
     }
 };
@@ -151,11 +151,11 @@ __global__ void __launch_bounds__(256, 8) collect_kernel(GridView g, const uint1
     __syncthreads();
     F3 p;
     const bool valid = tile_point(g, depth, blockIdx.y * blockDim.y + threadIdx.y, blockIdx.x * 32 + threadIdx.x, p);
-    tile_fill_set(g, p, valid, E, cset, slots, cbx, cby, cbz, visit);
+    tile_fill_set<false>(g, p, valid, E, cset, slots, cbx, cby, cbz, 1u, visit);
     SS_CT(2);
     __syncthreads();
     SS_CT(3);
-    tile_flush_set(g, cset, slots, cbx, cby, cbz, visit);
+    tile_flush_set<false>(g, cset, slots, cbx, cby, cbz, visit);
     SS_CT(4);
 }
 

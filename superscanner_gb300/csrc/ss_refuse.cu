@@ -26,52 +26,56 @@
 
 namespace ss {
 
-// A block visited by the batched collection in one phase: find or insert,
-// stamp with the batch's epoch, set the phase's bit in the block's mask (a
-// load first, with the home bucket's key and stamp: other tiles of the phase
-// have mostly set it already).
+// A block visited by the batched collection for one or both phases of a
+// keyframe (tag bit 0: phase 2k, bit 1: phase 2k + 1, the same mask word):
+// find or insert, stamp with the batch's epoch, OR the phases' bits into the
+// block's mask (a load first, with the home bucket's key and stamp: other
+// tiles have mostly set them already).
 struct RefuseVisit {
     GridView g;
     uint32_t epoch;
     uint32_t *phase_mask;
-    int word;
-    uint32_t bit;
-    __device__ __forceinline__ bool operator()(int bx, int by, int bz, int &bucket) {
-        return find_and_stamp<true>(g, epoch, bx, by, bz, bucket, phase_mask, kPhaseWords, word, bit);
+    int word, shift;  // phase 2k's word and bit
+    __device__ __forceinline__ bool operator()(int bx, int by, int bz, unsigned tag, int &bucket) {
+        return find_and_stamp<true>(g, epoch, bx, by, bz, bucket, phase_mask, kPhaseWords, word, tag << shift);
     }
 };
 
 // Grid (tiles, tiles, keyframes): the tile phases of collect_kernel
 // (ss_collect.cuh) for both phases of one keyframe, which share its depth
-// image: the tile's depth and camera-frame points are read once, then the
-// deintegration phase (old pose) and the integration phase (new pose) each
-// fill and flush the tile's set. Registers capped as in collect_kernel.
+// image: the tile's depth and camera-frame points are read once, the
+// deintegration phase (old pose) and the integration phase (new pose) fill one
+// tagged set (keys relative to the old pose's camera block), and each distinct
+// block is visited once with the bits of the phases that reach it. Registers
+// capped as in collect_kernel.
 __global__ void __launch_bounds__(256, 8) refuse_collect_kernel(GridView g, const uint16_t *const *__restrict__ depths,
                                                                 const FramePose *__restrict__ poses,
                                                                 uint32_t *__restrict__ phase_mask) {
-    extern __shared__ unsigned cset[];  // [slots] keys, then [slots] per-warp lists
+    extern __shared__ unsigned cset[];  // [slots] keys, [slots] per-warp lists, cube entries, [slots] tags
     const int slots = kSetSlotsPerRow * blockDim.y;
     const int tid = threadIdx.y * blockDim.x + threadIdx.x, nthreads = blockDim.x * blockDim.y;
+    unsigned *tags = tile_tags(cset, slots);
+    for (int q = tid; q < slots; q += nthreads) {
+        cset[q] = kSetEmpty;
+        tags[q] = 0u;
+    }
+    const int phase0 = 2 * blockIdx.z;
     F3 p;
     const bool valid =
         tile_point(g, depths[blockIdx.z], blockIdx.y * blockDim.y + threadIdx.y, blockIdx.x * 32 + threadIdx.x, p);
-    const uint32_t epoch = *(volatile uint32_t *)&g.ctr->epoch;
-#pragma unroll 1
-    for (int h = 0; h < 2; h++) {
-        const int phase = 2 * blockIdx.z + h;
-        if (h) __syncthreads();  // the first phase's flush has read the set
-        for (int q = tid; q < slots; q += nthreads) cset[q] = kSetEmpty;
-        Mat34 E;
+    RefuseVisit visit{g, *(volatile uint32_t *)&g.ctr->epoch, phase_mask, phase0 >> 5, phase0 & 31};
+    Mat34 E;
 #pragma unroll
-        for (int k = 0; k < 12; k++) E.m[k] = __ldg(&poses[phase].E.m[k]);
-        RefuseVisit visit{g, epoch, phase_mask, phase >> 5, 1u << (phase & 31)};
-        int cbx, cby, cbz;
-        camera_block(g, E, cbx, cby, cbz);
-        __syncthreads();
-        tile_fill_set(g, p, valid, E, cset, slots, cbx, cby, cbz, visit);
-        __syncthreads();
-        tile_flush_set(g, cset, slots, cbx, cby, cbz, visit);
-    }
+    for (int k = 0; k < 12; k++) E.m[k] = __ldg(&poses[phase0].E.m[k]);
+    int cbx, cby, cbz;
+    camera_block(g, E, cbx, cby, cbz);
+    __syncthreads();
+    tile_fill_set<true>(g, p, valid, E, cset, slots, cbx, cby, cbz, 1u, visit);
+#pragma unroll
+    for (int k = 0; k < 12; k++) E.m[k] = __ldg(&poses[phase0 + 1].E.m[k]);
+    tile_fill_set<true>(g, p, valid, E, cset, slots, cbx, cby, cbz, 2u, visit);
+    __syncthreads();
+    tile_flush_set<true>(g, cset, slots, cbx, cby, cbz, visit);
 }
 
 template <int kStorage, bool kExact>
@@ -219,7 +223,7 @@ extern "C" ss_status ss_refuse_batch(ss_grid *g, int32_t n, const uint16_t *cons
     SS_CUDA_TRY(cudaMemsetAsync(&g->v.ctr->work, 0, sizeof(int), s));
     constexpr int kRows = 4;
     const dim3 cblk(32, kRows), cgrid((g->p.resj + 31) / 32, (g->p.resi + kRows - 1) / kRows, n);
-    refuse_collect_kernel<<<cgrid, cblk, tile_set_bytes(kRows), s>>>(g->v, g->batch_depths, g->batch_poses,
+    refuse_collect_kernel<<<cgrid, cblk, tile_set_bytes(kRows, true), s>>>(g->v, g->batch_depths, g->batch_poses,
                                                                      g->phase_mask);
     SS_LAUNCH_CHECK();
     const int ctas = persistent_ctas(g, g->lc.refuse_ctas_per_sm);
