@@ -98,3 +98,39 @@ def test_batched_refusion_scattered_depths():
     assert len(a["keys"]) > 10000
     assert np.array_equal(a["keys"], b["keys"]) and np.array_equal(a["coords"], b["coords"])
     assert np.array_equal(a["w"], b["w"]) and np.array_equal(a["sdf"], b["sdf"])
+
+
+def test_batched_refusion_far_new_pose():
+    """Keyframes re-fused at poses 25 m from the old ones: the new phase's
+    blocks lie outside the tile set's key range (keys are offsets from the old
+    pose's camera block), so they are visited one by one with that phase's bit;
+    the volume still equals the sequential calls' bit for bit."""
+    rows, cols = 48, 64
+    rng = np.random.default_rng(12)
+    depth = rng.integers(500, 4000, size=(6, rows, cols)).astype(np.uint16)
+    dev = [torch.from_numpy(np.ascontiguousarray(d.view(np.int16))).cuda() for d in depth]
+    intr = (52.5, 52.5, (cols - 1) / 2.0, (rows - 1) / 2.0)
+    P = np.stack([np.eye(4)] * 6)
+    P[:, 1, 3] = np.linspace(0, 0.2, 6)
+    T_new = np.stack([delta(rng) @ P[k] for k in range(6)])
+    T_new[::2, 0, 3] += 25.0  # keyframes 0, 2, 4 move 25 m along x
+    out = []
+    for batched in (False, True):
+        g = GPUVoxelGrid(int(1e9), 0.016, 0.004, rows, cols, storage="f16", with_color=False, hash_buckets=1 << 18,
+                         max_weight=255)
+        g.setIntrinsic(*intr)
+        for k in range(6):
+            g.integrate_fast(dev[k], P[k].astype(np.float32))
+        if batched:
+            g.refuse_batch(dev, P, T_new)
+        else:
+            for k in range(6):
+                g.integrate_fast(dev[k], P[k].astype(np.float32), deint=True)
+                g.integrate_fast(dev[k], T_new[k].astype(np.float32))
+        g.sync()
+        out.append(g.export_blocks(with_color=False))
+        g.close()
+    a, b = out
+    assert (a["coords"][:, 0] > 500).sum() > 100  # blocks near the moved poses (x > 16 m)
+    assert np.array_equal(a["keys"], b["keys"]) and np.array_equal(a["coords"], b["coords"])
+    assert np.array_equal(a["w"], b["w"]) and np.array_equal(a["sdf"], b["sdf"])
