@@ -234,6 +234,14 @@ __device__ __forceinline__ bool ray_search(const GridView &g, float ox, float oy
             if (sm.f >= 0.f) {
                 mode = kRayForward;
                 prev_valid = true;
+                // a valid sample's corner blocks exist, so the super-block of its
+                // point is occupied: the first forward step needs no probe for it
+                // (should rounding put the point in a neighbouring block, the march
+                // only falls back from a super-block skip to a block skip)
+                csx = (int)floorf(px * inv_vbl) >> kSuperShift;
+                csy = (int)floorf(py * inv_vbl) >> kSuperShift;
+                csz = (int)floorf(pz * inv_vbl) >> kSuperShift;
+                cocc = true;
                 t += fmaxf(vl, 0.8f * sm.f) * inv_len;
             } else {
                 mode = kBack;
