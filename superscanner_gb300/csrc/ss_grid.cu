@@ -140,6 +140,10 @@ __global__ void __launch_bounds__(256, 8) collect_kernel(GridView g, const uint1
     const int slots = kSetSlotsPerRow * blockDim.y;
     const int tid = threadIdx.y * blockDim.x + threadIdx.x, nthreads = blockDim.x * blockDim.y;
     for (int q = tid; q < slots; q += nthreads) cset[q] = kSetEmpty;
+    // the frame's depth is an input, not an output of the kernel before this one
+    F3 p;
+    const bool valid = tile_point(g, depth, blockIdx.y * blockDim.y + threadIdx.y, blockIdx.x * 32 + threadIdx.x, p);
+    pdl_wait();  // the pose (tracker) and the table (previous calls)
     if (pose) {
 #pragma unroll
         for (int k = 0; k < 12; k++) E.m[k] = __ldg(&pose->E.m[k]);
@@ -149,10 +153,9 @@ __global__ void __launch_bounds__(256, 8) collect_kernel(GridView g, const uint1
     camera_block(g, E, cbx, cby, cbz);
     SS_CT(0);
     __syncthreads();
-    F3 p;
-    const bool valid = tile_point(g, depth, blockIdx.y * blockDim.y + threadIdx.y, blockIdx.x * 32 + threadIdx.x, p);
     tile_fill_set<false>(g, p, valid, E, cset, slots, cbx, cby, cbz, 1u, visit);
     SS_CT(2);
+    pdl_trigger();  // the fuse kernel may launch once every tile has filled its set
     __syncthreads();
     SS_CT(3);
     tile_flush_set<false>(g, cset, slots, cbx, cby, cbz, visit);
@@ -176,6 +179,8 @@ template <int kStorage, bool kColor, bool kDeint, bool kExact>
 __global__ void __launch_bounds__(256, 8) fuse_kernel(GridView g, const uint16_t *__restrict__ depth,
                                                    const uint8_t *__restrict__ rgb, Mat34 E, Mat34 Einv, F3 Ez,
                                                    const FramePose *__restrict__ pose) {
+    pdl_wait();     // the block list (collection) and the pose (tracker)
+    pdl_trigger();  // the raycast may launch: its CTAs take the SMs this grid leaves
     if (pose) load_pose(pose, E, Einv, Ez.x, Ez.y, Ez.z);
     const int lane = threadIdx.x & 31;
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -422,11 +427,11 @@ ss_status launch_fuse(ss_grid *g, const uint16_t *depth, const uint8_t *rgb, con
     const dim3 cblk(32, cr), cgrid((g->p.resj + 31) / 32, (g->p.resi + cr - 1) / cr);
     // shared set of packed coordinates + the list of its distinct entries
     const size_t csmem = tile_set_bytes(cr);  // <= 8 KB
-    collect_kernel<<<cgrid, cblk, csmem, s>>>(g->v, depth, E, dpose);
-    SS_LAUNCH_CHECK();
+    SS_CUDA_TRY(launch_kernel(collect_kernel, cgrid, cblk, csmem, s, g->pdl, g->v, depth, E, dpose));
     if (after_collect) SS_CUDA_TRY(cudaEventRecord(after_collect, s));
     const int ctas = persistent_ctas(g, g->lc.fuse_ctas_per_sm);
-#define SS_FUSE(ST, C, D, X) fuse_kernel<ST, C, D, X><<<ctas, 256, 0, s>>>(g->v, depth, rgb, E, Einv, Ez, dpose)
+#define SS_FUSE(ST, C, D, X) \
+    SS_CUDA_TRY(launch_kernel(fuse_kernel<ST, C, D, X>, dim3(ctas), dim3(256), 0, s, g->pdl, g->v, depth, rgb, E, Einv, Ez, dpose))
 #define SS_FUSE_X(ST, C, D) \
     do {                    \
         if (exact) SS_FUSE(ST, C, D, true); else SS_FUSE(ST, C, D, false); \

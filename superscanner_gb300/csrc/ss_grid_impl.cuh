@@ -22,6 +22,9 @@ struct ss_grid {
     ss::FramePose *batch_poses = nullptr;  // [kMaxPhases]
     const uint16_t **batch_depths = nullptr;  // [kMaxPhases / 2] device pointers
     unsigned long long *mesh_count = nullptr;  // triangle counter of ss_grid_extract_mesh (first call)
+    // launch collect, fuse and raycast as programmatic dependents of the kernel
+    // before them (set by the per-frame pipeline while it captures its graph)
+    bool pdl = false;
 };
 
 namespace ss {
@@ -53,6 +56,25 @@ ss_status status_from_bits(int bits);
             return SS_ERR_CUDA;                            \
         }                                                  \
     } while (0)
+
+// Launches kernel<<<grid, block, smem, s>>>(args...), as a programmatic
+// dependent of the previous kernel in s when pdl is set (the kernel must call
+// pdl_wait() before it touches that kernel's outputs).
+template <class... K, class... A>
+cudaError_t launch_kernel(void (*kernel)(K...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, bool pdl,
+                          A &&...args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = pdl ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, kernel, static_cast<A &&>(args)...);
+}
 
 Mat34 mat34_from(const float E[16]);
 FramePose frame_pose_from(const float extr[16]);

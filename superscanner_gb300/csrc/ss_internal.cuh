@@ -351,4 +351,14 @@ __device__ __forceinline__ bool super_occupied(const GridView &g, int sx, int sy
 
 __device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }
 
+// Programmatic dependent launch. A kernel launched with the programmatic
+// stream-serialization attribute may start while the kernel before it in the
+// stream is still running; pdl_wait() then blocks until that kernel has
+// completed and its memory is visible, so a kernel calls it before it reads
+// (or writes) anything the previous kernel writes (or reads). pdl_trigger()
+// lets the next kernel launch once every CTA of this one has called it or
+// exited. Both are no-ops for an ordinary launch.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 }  // namespace ss

@@ -304,7 +304,11 @@ ss_status ss_pipeline_frame(ss_pipeline *P, const uint16_t *depth, int32_t track
     } else if (P->p.use_graph) {
         if (!P->exec[b]) {
             SS_CUDA_TRY(cudaStreamBeginCapture(P->cap, cudaStreamCaptureModeThreadLocal));
+            // collect, fuse and raycast as programmatic dependents: each launches
+            // while the kernel before it drains and waits for it in-kernel
+            g->pdl = true;
             st = enqueue_frame(P, in, P->cap);
+            g->pdl = false;
             cudaGraph_t graph = nullptr;
             cudaError_t e = cudaStreamEndCapture(P->cap, &graph);
             if (st != SS_OK) {

@@ -247,7 +247,6 @@ __global__ void __launch_bounds__(256, 4) raycast_maps_kernel(GridView g, Mat34 
                                                            unsigned long long *__restrict__ counters,
                                                            const uint16_t *__restrict__ hint, float hint_margin,
                                                            Counters *end) {
-    if (end && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0 && threadIdx.y == 0) end_call(end);
     const int j = blockIdx.x * 32 + threadIdx.x;
     const int i = blockIdx.y * blockDim.y + threadIdx.y;
     const bool inside = i < g.resi && j < g.resj;
@@ -269,6 +268,10 @@ __global__ void __launch_bounds__(256, 4) raycast_maps_kernel(GridView g, Mat34 
         const unsigned dl = __shfl_sync(full, own, li), dr = __shfl_sync(full, own, ri);
         hint_mm = own ? own : (left && right ? min(dl, dr) : (left ? dl : (right ? dr : 0u)));
     }
+    // the hint is the frame's depth, an input; the volume, the pose and the
+    // call's counters come from the kernels before this one
+    pdl_wait();
+    if (end && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0 && threadIdx.y == 0) end_call(end);
     SS_RT_NOW(rt1);
     long long rt2 = 0;
     if (inside) {
@@ -344,12 +347,11 @@ ss_status launch_raycast_maps(ss_grid *g, const Mat34 &T, const FramePose *dpose
     const int rr = g->lc.raycast_rows;
     const dim3 blk(32, rr), grid((g->p.resj + 31) / 32, (g->p.resi + rr - 1) / rr);
     if (g->p.storage == SS_STORAGE_F32)
-        raycast_maps_kernel<SS_STORAGE_F32><<<grid, blk, 0, s>>>(g->v, T, dpose, max_steps, t_min, t_max, vmap, nmap,
-                                                                 counters, hint, hint_margin, end);
+        SS_CUDA_TRY(launch_kernel(raycast_maps_kernel<SS_STORAGE_F32>, grid, blk, 0, s, g->pdl, g->v, T, dpose, max_steps,
+                                  t_min, t_max, vmap, nmap, counters, hint, hint_margin, end));
     else
-        raycast_maps_kernel<SS_STORAGE_F16><<<grid, blk, 0, s>>>(g->v, T, dpose, max_steps, t_min, t_max, vmap, nmap,
-                                                                 counters, hint, hint_margin, end);
-    SS_LAUNCH_CHECK();
+        SS_CUDA_TRY(launch_kernel(raycast_maps_kernel<SS_STORAGE_F16>, grid, blk, 0, s, g->pdl, g->v, T, dpose, max_steps,
+                                  t_min, t_max, vmap, nmap, counters, hint, hint_margin, end));
     return SS_OK;
 }
 

@@ -706,6 +706,7 @@ __global__ void __launch_bounds__(256) track_frame_kernel(const uint16_t *__rest
             abuf = abuf == kTrackAccBuffers - 1 ? 0 : abuf + 1;
         }
     }
+    pdl_trigger();  // the collection may launch; it waits for this grid before it reads the pose
     if (blockIdx.x == 0 && threadIdx.x < 32) {
         // the result and its FramePose (float pose, float inverse, unit z column)
         const int lane = threadIdx.x;
