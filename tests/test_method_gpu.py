@@ -113,8 +113,11 @@ def test_tracking_solve_vs_fp64():
 
 @pytest.mark.parametrize("persistent", [False, True])
 def test_pipeline_graph_replay_equals_direct_launches(persistent):
+    """The captured graph (collect, fuse and raycast as programmatic dependent
+    launches) gives the poses, model maps and volume of direct launches bit
+    for bit."""
     P, depth = seq(16)
-    poses = {}
+    res = {}
     for graph in (False, True):
         g = GPUVoxelGrid(int(1e9), TRUNC, VL, 480, 640, storage="f16", with_color=False, hash_buckets=1 << 18,
                          max_weight=255)
@@ -125,9 +128,14 @@ def test_pipeline_graph_replay_equals_direct_launches(persistent):
         for k in range(16):
             pipe.frame(dev(depth[k]), track=(k > 0))
             out.append(pipe.pose())
+        v, n = pipe.maps_tensors()
         g.sync()
-        poses[graph] = np.stack(out)
-    assert np.array_equal(poses[False], poses[True])
+        res[graph] = (np.stack(out), v.cpu().numpy(), n.cpu().numpy(), g.export_blocks(with_color=False))
+    (pa, va, na, ba), (pb, vb, nb, bb) = res[False], res[True]
+    assert np.array_equal(pa, pb)
+    assert np.array_equal(va, vb) and np.array_equal(na, nb)
+    assert np.array_equal(ba["keys"], bb["keys"]) and np.array_equal(ba["sdf"], bb["sdf"])
+    assert np.array_equal(ba["w"], bb["w"])
 
 
 @pytest.mark.parametrize("storage", ["f32", "f16"])
