@@ -23,7 +23,8 @@
 // The set of allocated blocks is the union of every pixel's candidates, as in
 // the reference; only the number of global probes and atomics changes (one
 // per distinct block per tile). 8 bytes of shared memory per slot (set and
-// per-warp lists) and 512 bytes per warp for its cubes: 6 KB per 4-row tile.
+// per-warp lists; 12 with a tagged set's tags) and 512 bytes per warp for its
+// cubes: 6 KB per 4-row tile (8 KB tagged).
 //
 // A visitor is a callable bool (int bx, int by, int bz, unsigned tag, int
 // &bucket): it finds or inserts the block, marks it, and returns true when
