@@ -82,7 +82,7 @@ def dist_env():
 
 
 def make_sequence(n: int):
-    from superscanner_gb300 import synth
+    import synth
     sc = synth.Scene(2, SCENE_SEED)
     P = sc.trajectory(n, TRAJ_SEED)
     depth, _ = sc.render(P, ROWS, COLS, INTR, noise=True, noise_seed=NOISE_SEED, color=False)
@@ -300,7 +300,8 @@ def run_refusion(torch, depth, P, stream, n_kf: int = 200, launch=None, modes=("
     (every call's touched blocks x 512 voxels x 4 B read + 4 B written, plus
     its depth image, from the grid's counters) give both modes' achieved
     bandwidth, and its fraction of `peak` (GB/s)."""
-    from superscanner_gb300 import GPUVoxelGrid, synth
+    import synth
+    from superscanner_gb300 import GPUVoxelGrid
     n = len(depth)
     n_kf = min(n_kf, n)
     masks = synth.occlusion_masks(n_kf, ROWS, COLS, seed=99)

@@ -3,7 +3,8 @@
 Loads ``oracle/_build/libss_oracle.so`` (built from ss_oracle.cpp by the
 Makefile beside it). Only tests/, __graft_entry__.smoke() and bench.py's CPU
 baseline legs use this module; the product package never imports it.
-Parity status: unpinned by the reference (see ss_oracle.cpp's header).
+Parity status: pinned by the reference's own code (oracle/_ref, see
+ss_oracle.cpp's header and tests/test_ref_pinned.py).
 """
 from __future__ import annotations
 

@@ -4,13 +4,18 @@
 // __graft_entry__.smoke() and bench.py's cpu_baseline / reference legs load it.
 // The product path (superscanner_gb300/) never links or calls it.
 //
-// Parity status: UNPINNED by the reference. The reference path cannot be
-// built here (it needs Kokkos, Eigen, Open3D; every launch is hard-wired to
-// Kokkos::Cuda) and its own tests hold no golden vector for this path (the
-// only device test, exe/Test.cpp:117-181, checks a 4x4 float matrix-vector
-// product against Eigen, which tests/test_oracle.py restates). The restatement
-// is pinned instead by analytic known-answer cases (planes, spheres, rigid
-// transforms) in tests/test_oracle.py and by the golden dumps in tests/golden/.
+// Parity status: PINNED by the reference's own code. The reference's
+// hot-path sources (GPUVoxelGrid.cpp, kokkosICP.cpp, imageutil.cpp,
+// kokkosUtil.cpp, kokkosFunctions.cpp) compile unchanged on the host against
+// the stand-ins of ref_stub/ (Kokkos, Eigen, Open3D and OpenCV are absent):
+// `make ref` builds them into _ref/libss_ref.so, tests/golden/ref_*.npz hold
+// their outputs on the config-1 and config-2 sequences of tests/refcases.py,
+// and tests/test_ref_pinned.py checks that this restatement reproduces every
+// block, voxel, raycast row and kokkosICP pose of those fixtures bit for bit
+// (and equals the live reference build on further cases). What the pin does
+// not reach: the third-party arithmetic the stand-ins restate (Eigen's 4x4
+// inverse and JacobiSVD, Kokkos' hash-map slot layout) and the reference
+// binary's FMA contraction (ref_stub/ss_ref_stub.h, oracle/Makefile).
 //
 // Semantics follow the reference source statement by statement, in IEEE
 // single precision with no floating-point contraction (build with
@@ -20,7 +25,7 @@
 // conversion the reference actually ran (truncate toward zero, saturate,
 // NaN -> 0), see f2i() below.
 //
-// Two behaviours of the reference are data races or undefined; the oracle
+// Three behaviours of the reference are data races or undefined; the oracle
 // and the CUDA path share one canonical resolution for each:
 //  * Blocks whose prime hashes collide alias one map entry and the entry's
 //    pzero/vbInd are written by every visitor (GPUVoxelGrid.cpp:500-502, last
@@ -30,6 +35,11 @@
 //    the reference calls value_at(find(..)) on an invalid index
 //    (GPUVoxelGrid.cpp:669-672). Canonical rule: that voxel reads as empty
 //    (w = 0, sdf = 0, colour 0).
+//  * kokkosICP's correspondence view is never zeroed before the first
+//    iteration (kokkosICP.cpp:43; Kvec3f's default constructor,
+//    kokkosFunctions.h:149, writes nothing), so pixels without a
+//    correspondence hold whatever the device memory held. Canonical rule: it
+//    starts at zero, as freshly allocated device memory reads.
 
 #include <algorithm>
 #include <cmath>

@@ -7,7 +7,6 @@ operator interface on top of it:
 * :class:`GPUVoxelGrid` — ``GPUVoxelGrid`` of src/VoxelGrid/GPUVoxelGrid.h
   (integrate, deIntegrate, raycast, setIntrinsic, cleanMemory).
 * :func:`kokkos_icp` — ``kokkosICP`` of src/postprocessing/kokkosICP.h.
-* :mod:`superscanner_gb300.synth` — seeded synthetic RGB-D sequences.
 
 There is no CPU fallback: importing the package loads the native library and
 raises if it is missing.

@@ -2,7 +2,7 @@
 
 ``build_native()`` compiles every ``csrc/*.cu`` for sm_103a in parallel and
 links ``superscanner_gb300/libss.so`` (static CUDA runtime, C-ABI of
-``include/ss_abi.h``), plus the synthetic-scene library ``libss_synth.so``.
+``include/ss_abi.h``).
 Objects are rebuilt only when a source or header is newer than the library.
 Host code is compiled with ``-ffp-contract=off`` so that the host-side pose
 arithmetic (inverse, normalisation) rounds the same on x86 and Arm.
@@ -22,8 +22,6 @@ CSRC = PKG / "csrc"
 INCLUDE = ROOT / "include"
 BUILD = PKG / "_build"
 LIB = PKG / "libss.so"
-SYNTH_SRC = PKG / "synth" / "ss_synth.cpp"
-SYNTH_LIB = PKG / "libss_synth.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = [
@@ -70,16 +68,6 @@ def build_cuda(force: bool = False, verbose: bool = False) -> Path:
     return LIB
 
 
-def build_synth(force: bool = False) -> Path:
-    if not force and SYNTH_LIB.exists() and SYNTH_LIB.stat().st_mtime >= _newest([SYNTH_SRC, Path(__file__)]):
-        return SYNTH_LIB
-    tmp = SYNTH_LIB.with_suffix(".so.tmp")
-    _run(["g++", "-O3", "-std=c++17", "-fPIC", "-fopenmp", "-ffp-contract=off", "-shared",
-          "-o", str(tmp), str(SYNTH_SRC)])
-    os.replace(tmp, SYNTH_LIB)
-    return SYNTH_LIB
-
-
 SHIM_SRC = ROOT / "tests" / "cpp" / "shim_roundtrip.cpp"
 SHIM_BIN = BUILD / "shim_roundtrip"
 
@@ -98,11 +86,7 @@ def build_shim_test(force: bool = False) -> Path:
 
 
 def build_native(force: bool = False, verbose: bool = False) -> None:
-    with cf.ThreadPoolExecutor(max_workers=2) as ex:
-        a = ex.submit(build_cuda, force, verbose)
-        b = ex.submit(build_synth, force)
-        a.result()
-        b.result()
+    build_cuda(force, verbose)
     build_shim_test(force)
 
 

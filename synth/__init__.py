@@ -4,17 +4,37 @@ Stand-ins for the reference's recorded scenes, which are not available:
 config-1 style rooms (2x2x2 m, 6 spheres + 4 boxes) and config-2 style rooms
 (4x4x3 m, 40 primitives), smooth seeded trajectories, exact depth in uint16
 millimetres with optional depth-dependent Gaussian noise and 5 % dropout.
+
+Input data for tests and benchmarks, kept apart from the library package so
+that loading it loads no part of the product. The C++ generator
+(ss_synth.cpp) is compiled into _build/libss_synth.so on first import (or by
+build()) with -ffp-contract=off, so x86 and Arm render the same frames.
 """
 from __future__ import annotations
 
 import ctypes as C
+import os
+import subprocess
 from pathlib import Path
 
 import numpy as np
 
-_LIB_PATH = Path(__file__).resolve().parent.parent / "libss_synth.so"
-if not _LIB_PATH.exists():
-    raise ImportError(f"{_LIB_PATH} is missing: run the package build first")
+_DIR = Path(__file__).resolve().parent
+_SRC = _DIR / "ss_synth.cpp"
+_LIB_PATH = _DIR / "_build" / "libss_synth.so"
+
+
+def build(force: bool = False) -> Path:
+    if force or not _LIB_PATH.exists() or _LIB_PATH.stat().st_mtime < _SRC.stat().st_mtime:
+        _LIB_PATH.parent.mkdir(exist_ok=True)
+        tmp = _LIB_PATH.with_suffix(f".so.tmp{os.getpid()}")
+        subprocess.run(["g++", "-O3", "-std=c++17", "-fPIC", "-fopenmp", "-ffp-contract=off", "-shared",
+                        "-o", str(tmp), str(_SRC)], check=True)
+        os.replace(tmp, _LIB_PATH)
+    return _LIB_PATH
+
+
+build()
 _lib = C.CDLL(str(_LIB_PATH))
 _lib.synth_scene_new.restype = C.c_void_p
 _lib.synth_scene_new.argtypes = [C.c_int, C.c_uint64]

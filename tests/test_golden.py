@@ -1,5 +1,7 @@
-"""Golden fixtures (tests/golden/, written by make_golden.py from the oracle):
-the oracle must keep reproducing them, and the GPU path must match them."""
+"""Golden fixtures of tests/golden/: ref_fusion.npz comes from the reference's
+own code (make_ref_golden.py, oracle/_ref), method.npz from the FP64 method
+oracle (make_golden.py). The oracle must keep reproducing them, and the GPU
+path must match them."""
 from pathlib import Path
 
 import numpy as np

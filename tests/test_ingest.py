@@ -48,7 +48,8 @@ def test_ingested_frames_drive_the_pipeline(tmp_path):
     """Depth frames written as PNGs, read back into pinned memory and fed to
     the pipeline (asynchronous upload) track like the same frames on the GPU."""
     import torch
-    from superscanner_gb300 import GPUVoxelGrid, synth
+    import synth
+    from superscanner_gb300 import GPUVoxelGrid
     from superscanner_gb300.pipeline import Pipeline
     INTR = (525.0, 525.0, 319.5, 239.5)
     sc = synth.Scene(2, 1234)

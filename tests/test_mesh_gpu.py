@@ -6,7 +6,8 @@ import torch
 
 import oracle
 from scenes import wavy_wall, VL as WVL, TRUNC as WTRUNC
-from superscanner_gb300 import GPUVoxelGrid, synth
+import synth
+from superscanner_gb300 import GPUVoxelGrid
 from superscanner_gb300.mesh import extract_triangles
 
 pytestmark = pytest.mark.gpu

@@ -7,7 +7,8 @@ import pytest
 import torch
 
 import oracle
-from superscanner_gb300 import GPUVoxelGrid, synth
+import synth
+from superscanner_gb300 import GPUVoxelGrid
 from superscanner_gb300.pipeline import Pipeline, raycast_maps
 
 pytestmark = pytest.mark.gpu

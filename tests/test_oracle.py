@@ -5,7 +5,7 @@ import numpy as np
 import pytest
 
 import oracle
-from superscanner_gb300 import synth
+import synth
 
 INTR = (525.0, 525.0, 319.5, 239.5)
 

@@ -7,7 +7,8 @@ import pytest
 import torch
 
 import oracle
-from superscanner_gb300 import GPUVoxelGrid, depth_to_pcd, kokkos_icp, normals_from_pcd, synth
+import synth
+from superscanner_gb300 import GPUVoxelGrid, depth_to_pcd, kokkos_icp, normals_from_pcd
 from superscanner_gb300._native import SS_ERR_ARG, SS_ERR_STATE, SS_ERR_TABLE_FULL, SSError
 
 pytestmark = pytest.mark.gpu

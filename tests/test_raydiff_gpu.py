@@ -8,7 +8,8 @@ import pytest
 import torch
 
 import oracle
-from superscanner_gb300 import GPUVoxelGrid, synth
+import synth
+from superscanner_gb300 import GPUVoxelGrid
 from superscanner_gb300.raydiff import raycast_loss, raycast_loss_grad, se3_exp
 from scenes import wavy_wall, VL as WVL, TRUNC as WTRUNC
 

@@ -5,7 +5,8 @@ import numpy as np
 import pytest
 import torch
 
-from superscanner_gb300 import GPUVoxelGrid, synth
+import synth
+from superscanner_gb300 import GPUVoxelGrid
 
 pytestmark = pytest.mark.gpu
 

@@ -20,7 +20,7 @@ INTR = (525.0, 525.0, 319.5, 239.5)
 
 def test_no_alloc_kokkos_icp_matches_allocating_entry_point():
     import torch
-    from superscanner_gb300 import synth
+    import synth
     from superscanner_gb300._native import SS_ERR_DIMS, f64x16, lib
     sc = synth.Scene(1, 1234)
     P = sc.trajectory(20, 42)
