@@ -14,8 +14,12 @@ kernels launched one by one) is timed on the same frames. ``e2e`` is the
 chosen form through the public API with host-pinned input frames copied in
 and the pose read back every step. ``l2_flushed`` is the chosen form with
 L2 evicted (a 512 MB write) before every frame, each frame timed alone.
-``--impl reference`` times the reference semantics restated on the CPU
-(oracle/).
+``dropin`` is the reference's own call surface on the GPU (ss_integrate,
+ss_raycast, ss_kokkos_icp per frame: the reference's algorithm and
+rounding), beside ``cpu_baseline``, the same work on the host cores.
+``--impl reference`` times that CPU work alone: the reference semantics
+restated in C++ (oracle/), which tests/test_ref_pinned.py holds bit-exact to
+the reference's own sources compiled on the host.
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
@@ -53,6 +57,7 @@ WORKLOAD = ("synthetic 4x4x3 m room, 40 primitives, 640x480 noisy uint16 depth (
 # kernels per frame of the chosen form: the cooperative tracker (all GN iterations), collect, fuse, raycast (which
 # also ends the integrate call)
 KERNELS_PER_FRAME = 1 + 2 + 1
+LONG_FRAMES = 206  # config 4 re-fuses 200 keyframes, config 5 refines 50 frames
 
 
 def parse():
@@ -370,6 +375,122 @@ def run_refusion(torch, depth, P, stream, n_kf: int = 200, launch=None, modes=("
     return res
 
 
+def run_dropin(torch, depth_dev, P, W: int, K: int, stream, peak: float, host_pinned=None):
+    """The reference's call surface on the GPU: per frame ss_integrate (FP32,
+    the reference's rounding, depth only), ss_raycast (nearest voxel, to 10 m)
+    and ss_kokkos_icp (point-to-plane, frame k against k-1 at the ground-truth
+    poses, 10 iterations) — the work `--impl reference` and `cpu_baseline` time
+    on the CPU, on the same frames. Returns frames/s (frames resident in HBM),
+    the same with every frame uploaded from pinned host memory (e2e), per-call
+    CUDA-event times, and the roofline of raycast_ref_kernel and
+    icp_ref_iter_kernel (algorithmic bytes from the raycast's work counters and
+    the ICP's per-iteration image reads)."""
+    from superscanner_gb300 import GPUVoxelGrid, depth_to_pcd, kokkos_icp, normals_from_pcd, PointToPlane
+    E = P.astype(np.float32)
+    npix = ROWS * COLS
+
+    def grid():
+        g = GPUVoxelGrid(int(1e9), TRUNC, VL, ROWS, COLS, storage="f32", with_color=False, hash_buckets=BUCKETS)
+        g.setIntrinsic(*INTR)
+        return g
+
+    def frame(g, k, cur, prev, ev=None):
+        if ev:
+            ev[0].record(stream)
+        g.integrate(None, cur, E[k], False, stream)
+        if ev:
+            ev[1].record(stream)
+        g.raycast(E[k], stream, with_color=False)
+        if ev:
+            ev[2].record(stream)
+        T, rmse = kokkos_icp(cur, prev, P[k], P[k - 1], PointToPlane, INTR, stream)
+        if ev:
+            ev[3].record(stream)
+        return T
+
+    out = {}
+    g = grid()
+    with torch.cuda.stream(stream):
+        g.integrate(None, depth_dev[0], E[0], False, stream)
+        for k in range(1, 1 + W):
+            frame(g, k, depth_dev[k], depth_dev[k - 1])
+        torch.cuda.synchronize()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        for k in range(1 + W, 1 + W + K):
+            frame(g, k, depth_dev[k], depth_dev[k - 1])
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        ms = ev0.elapsed_time(ev1)
+        out["value"] = round(K / (ms * 1e-3), 2)
+        out["ms_per_frame"] = round(ms / K, 4)
+        # per-call times on a fresh volume built the same way
+        g.close()
+        g = grid()
+        g.integrate(None, depth_dev[0], E[0], False, stream)
+        for k in range(1, 1 + W):
+            frame(g, k, depth_dev[k], depth_dev[k - 1])
+        torch.cuda.synchronize()
+        rc0 = g.raycast_counters(stream)
+        evs = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(K)]
+        for q, k in enumerate(range(1 + W, 1 + W + K)):
+            frame(g, k, depth_dev[k], depth_dev[k - 1], evs[q])
+        torch.cuda.synchronize()
+        rc1 = g.raycast_counters(stream)
+        per = np.array([[e[0].elapsed_time(e[1]), e[1].elapsed_time(e[2]), e[2].elapsed_time(e[3])] for e in evs])
+        # the ICP call's point-cloud / normal kernels, timed alone on the same frames
+        pe = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        pe[0].record(stream)
+        for k in range(1 + W, 1 + W + K):
+            x = depth_to_pcd(depth_dev[k], *INTR, stream=stream)
+            y = depth_to_pcd(depth_dev[k - 1], *INTR, stream=stream)
+            normals_from_pcd(y, stream=stream)
+        pe[1].record(stream)
+        torch.cuda.synchronize()
+        prep_ms = pe[0].elapsed_time(pe[1]) / K
+    g.close()
+    m = per.mean(axis=0)
+    out["ms_per_call"] = {"integrate": round(float(m[0]), 4), "raycast": round(float(m[1]), 4),
+                          "kokkos_icp": round(float(m[2]), 4)}
+    finds = (rc1["finds"] - rc0["finds"]) / K
+    voxels = (rc1["voxels"] - rc0["voxels"]) / K
+    ray_bytes = finds * 8 + voxels * 8 + 12 * npix  # 8-byte keys, float2 (sdf, w), float3 points
+    icp_iter_ms = max(float(m[2]) - prep_ms, 1e-6) / 10
+    icp_bytes = 36 * npix  # per iteration: source points, target points and normals (12 B each)
+    roof = {}
+    for name, b, t, extra in (("raycast_ref_kernel", ray_bytes, float(m[1]), {"finds_per_frame": round(finds),
+                                                                             "voxel_reads_per_frame": round(voxels)}),
+                              ("icp_ref_iter_kernel", icp_bytes, icp_iter_ms,
+                               {"launches_per_frame": 10, "pcd_and_normal_kernels_ms": round(prep_ms, 4)})):
+        gbs = b / (t * 1e-3) / 1e9
+        roof[name] = {"bytes_per_launch": int(b), "ms_per_launch": round(t, 5), "achieved_gbs": round(gbs, 1),
+                      "frac": round(gbs / peak, 4), **extra}
+    out["roofline"] = roof
+    if host_pinned is not None:
+        g = grid()
+        ring = torch.empty((2, ROWS, COLS), dtype=torch.int16, device="cuda")
+        with torch.cuda.stream(stream):
+            ring[0].copy_(host_pinned[0], non_blocking=True)
+            g.integrate(None, ring[0], E[0], False, stream)
+            for k in range(1, 1 + W):
+                ring[k & 1].copy_(host_pinned[k], non_blocking=True)
+                frame(g, k, ring[k & 1], ring[(k - 1) & 1])
+            torch.cuda.synchronize()
+            ev0.record(stream)
+            t0 = time.perf_counter()
+            for k in range(1 + W, 1 + W + K):
+                ring[k & 1].copy_(host_pinned[k], non_blocking=True)
+                frame(g, k, ring[k & 1], ring[(k - 1) & 1])
+            ev1.record(stream)
+            torch.cuda.synchronize()
+            wall = time.perf_counter() - t0
+        g.close()
+        out["e2e"] = {"value": round(K / (ev0.elapsed_time(ev1) * 1e-3), 2), "unit": "frames/s",
+                      "h2d_bytes_per_step": npix * 2, "d2h_bytes_per_step": 16 * 8 + 4,
+                      "wall_frames_per_s": round(K / wall, 2)}
+    return out
+
+
 def rand_perturb(rng, max_deg=5.0, max_m=0.05):
     """Seeded SE(3) perturbation: rotation about a uniformly random axis by an
     angle ~ U(0, max_deg), translation along a uniformly random direction by a
@@ -624,13 +745,15 @@ def main_reference(args):
     cores = oracle.threads()
     sample = (f"frames {1 + W}..{W + K} of the workload, full 640x480, volume state built from frames 0..{W} "
               f"first; reference semantics restated in C++ (oracle/ss_oracle.cpp, OpenMP {cores} threads, "
-              f"{cpu_model()})")
+              f"{cpu_model()}), bit-exact with the reference's own sources compiled on the host "
+              f"(tests/test_ref_pinned.py)")
     line = {
         "metric": METRIC, "value": round(fps, 4), "unit": "frames/s", "n_gpus": args.gpus, "steps": K,
         "warmup": W, "ms_per_step": round(1e3 * s / K, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "form": "reference semantics on CPU: integrate + nearest-voxel raycast "
-                   "(to 10 m) + kokkosICP point-to-plane (10 iterations, frame-to-frame)"},
+        "config": {"workload": WORKLOAD},
+        "form": {"value": "reference semantics on CPU: integrate + nearest-voxel raycast (to 10 m) + kokkosICP "
+                          "point-to-plane (10 iterations, frame-to-frame); the same work as the GPU arm's dropin leg"},
         "impl": "reference",
         "cpu_baseline": {"value": round(fps, 4), "unit": "frames/s", "cores": cores, "kind": "port",
                          "sample": sample},
@@ -705,6 +828,7 @@ def main_ours(args):
 
     host = torch.from_numpy(depth.view(np.int16)).pin_memory()
     e2e = run_e2e(torch, host, P, W, K, stream, launch=tuned)
+    dropin = run_dropin(torch, depth_dev, P, W, K, stream, peak, host_pinned=host)
     k_flush = min(K, 100)
     flushed_ms = run_l2_flushed(torch, depth_dev, P, W, k_flush, stream, launch=tuned)
     e2e_fps = K / (e2e["ms"] * 1e-3) * world
@@ -724,10 +848,14 @@ def main_ours(args):
     if traffic is not None:
         roof["traffic_source"] = "ncu capture, " + tf.name
 
-    refusion = run_refusion(torch, depth, P, stream, launch=tuned, peak=peak) if rank == 0 else None
+    # config 4 (200 keyframes) and config 5 (50 frames) need a longer sequence than a short timed run
+    P_long, depth_long = (P, depth) if n >= LONG_FRAMES else make_sequence(LONG_FRAMES)
+    refusion = run_refusion(torch, depth_long, P_long, stream, launch=tuned, peak=peak) if rank == 0 else None
     precision = (run_precision_form(torch, depth, P, stream, n_frames=args.precision_frames, launch=tuned)
                  if rank == 0 and args.precision_frames > 1 else None)
-    refinement = (run_pose_refinement(torch, depth, P, stream, n_frames=args.refine_frames)
+    if precision:
+        precision.pop("per_frame")  # the line keeps the per-frame maxima only
+    refinement = (run_pose_refinement(torch, depth_long, P_long, stream, n_frames=args.refine_frames)
                   if rank == 0 and args.refine_frames > 0 else None)
 
     # accuracy: tracked poses vs ground truth, chosen vs plain, depth vs the FP64 oracle
@@ -757,15 +885,20 @@ def main_ours(args):
 
     if rank == 0:
         clocks = sampler.summary() if sampler else None
+        if cpu:
+            dropin["cpu_reference_frames_per_s"] = cpu["value"]
+            dropin["over_cpu_reference"] = round(dropin["value"] / cpu["value"], 2)
+            if "e2e" in dropin:
+                dropin["e2e_over_cpu_reference"] = round(dropin["e2e"]["value"] / cpu["value"], 2)
         line = {
             "metric": METRIC, "value": round(fps_c, 2), "unit": "frames/s", "n_gpus": world, "steps": K,
             "warmup": W, "ms_per_step": round(ms_c / K, 4), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "form": "chosen: FP16 TSDF + u16 weight (FP32 math), persistent "
-                       "cooperative tracker, per-frame CUDA graph, autotuned launch shapes", "storage": "f16",
-                       "launch": tuned, "parallelism": f"replicas x{world}",
+            "config": {"workload": WORKLOAD, "parallelism": f"replicas x{world}",
                        "l2": "no flush: inputs exceed L2 (TSDF pool 2.1 GB f16 / 4.3 GB f32, depth sequence "
                              f"{depth.nbytes / 1e6:.0f} MB)"},
+            "form": {"value": "chosen: FP16 TSDF + u16 weight (FP32 math), persistent cooperative tracker, "
+                              "per-frame CUDA graph, autotuned launch shapes", "launch": tuned},
             "plain_form": {"value": round(fps_p, 2), "unit": "frames/s", "ms_per_step": round(ms_p / K, 4),
                            "storage": "f32", "graph": False, "tracker": "one launch per iteration",
                            "launch": "default shapes"},
@@ -784,6 +917,7 @@ def main_ours(args):
             "e2e": {"value": round(e2e_fps, 2), "unit": "frames/s", "h2d_bytes_per_step": ROWS * COLS * 2,
                     "d2h_bytes_per_step": 16 * 8, "wall_s": round(e2e["wall_s"], 4)},
             "gpu_launches": KERNELS_PER_FRAME * K,
+            "dropin": dropin,
             "accuracy": accuracy,
             "refusion": refusion,
             "mesh": mesh,

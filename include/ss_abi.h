@@ -94,7 +94,8 @@ ss_status ss_params_default(ss_params *p, uint32_t capacity_voxels, float trunc,
 ss_status ss_grid_create(const ss_params *p, ss_grid **out);
 ss_status ss_grid_destroy(ss_grid *g);
 ss_status ss_grid_get_launch_config(const ss_grid *g, ss_launch_config *c);
-/* Takes effect for later launches; a pipeline reads it when it is created. */
+/* Takes effect for later launches, also of a pipeline over this grid (its
+ * captured per-frame graphs are re-captured with the new shapes). */
 ss_status ss_grid_set_launch_config(ss_grid *g, const ss_launch_config *c);
 
 /* Resets the volume to empty (all buckets free, all payload zero). */
@@ -237,6 +238,26 @@ ss_status ss_grid_sync(ss_grid *g, ss_stream_t s);
  * status bits, epoch}. No reference counterpart. */
 ss_status ss_grid_counters(ss_grid *g, ss_stream_t s, int64_t out[6]);
 
+/* Synchronises the stream and copies the work counters of ss_raycast summed
+ * over all its calls on this grid: out = {hash finds, voxel reads}. They give
+ * the raycast's algorithmic bytes (8 B per find, the voxel size per read).
+ * No reference counterpart. */
+ss_status ss_grid_raycast_counters(ss_grid *g, ss_stream_t s, int64_t out[2]);
+
+/* Test hooks of the failure paths (no reference counterpart); they make a
+ * bounded device loop run out without faulting or hanging anything.
+ * ss_grid_test_raycast_cap: ss_raycast's per-ray iteration cap (default 2^20,
+ * far above the longest march) becomes cap; rays that reach it end without a
+ * hit and ss_grid_sync returns SS_ERR_TIMEOUT. cap = 0 restores the default.
+ * ss_pipeline_test_wait_timeout: the next tracked frame's persistent tracker
+ * waits for one contribution more than its CTAs make, for at most `polls`
+ * polls (the default limit is 2^22, about a second): every CTA gives up, the
+ * frame keeps its start pose and is fused there, and ss_grid_sync returns
+ * SS_ERR_TIMEOUT. That frame runs without the captured graph. SS_ERR_STATE
+ * when the pipeline's tracker is not persistent (declared with the pipeline
+ * below). */
+ss_status ss_grid_test_raycast_cap(ss_grid *g, int32_t cap);
+
 /* Text of the last CUDA error seen by this thread (for SS_ERR_CUDA). */
 const char *ss_last_error(void);
 
@@ -286,8 +307,10 @@ ss_status ss_kokkos_icp(const uint16_t *d1, const uint16_t *d2, int32_t rows, in
  * memory belongs to its own pool allocator). Its scratch is a fixed 11.2 MB
  * device array that every GPU loading the library holds until exit; rows *
  * cols above 640 x 480 return SS_ERR_DIMS. The first call on a device looks up
- * the array's address and should come before any stream capture. Calls share
- * the array: calls that overlap on the GPU race and must be serialised. */
+ * the array's address and should come before any stream capture; the address
+ * is kept for the life of the process, so after a cudaDeviceReset the entry
+ * point must not be called on that device again. Calls share the array:
+ * calls that overlap on the GPU race and must be serialised. */
 ss_status ss_kokkos_icp_noalloc(const uint16_t *d1, const uint16_t *d2, int32_t rows, int32_t cols,
                                 float fx, float fy, float cx, float cy, const double tx[16],
                                 const double ty[16], int32_t icp_type, double txy_out[16],
@@ -391,6 +414,8 @@ ss_status ss_pipeline_stage_ms(ss_pipeline *p, double ms[5], int64_t *frames, in
                                ss_stream_t s);
 /* Tracker inliers and residual RMS per level of the last tracked frame. */
 ss_status ss_pipeline_stats(ss_pipeline *p, int32_t inliers[4], float rmse[4], ss_stream_t s);
+/* Test hook of the tracker's bounded wait (see ss_grid_test_raycast_cap above). */
+ss_status ss_pipeline_test_wait_timeout(ss_pipeline *p, int32_t polls);
 
 #ifdef __cplusplus
 }

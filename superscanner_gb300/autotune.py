@@ -75,13 +75,23 @@ def _refuse_ms(depth_dev, poses, frames: int, grid_kw: dict, intr, cfg: dict) ->
 
 
 def autotune(depth_dev, poses, grid_kw: dict, intr, *, frames: int = 8, pipe_kw: dict | None = None,
-             cache: str | Path | None = None) -> dict:
+             cache: str | Path | None = None, stage_timer=None, refuse_timer=None) -> dict:
     """Returns the launch configuration (GPUVoxelGrid.set_launch_config keywords).
 
     depth_dev: CUDA tensor [n, rows, cols] of frames along poses [n, 4, 4] (n >= frames).
     grid_kw: GPUVoxelGrid constructor keywords of the grid the result is for.
+    Coordinate descent: the knobs are tuned one after the other in the order of
+    CANDIDATES, each timed with the best values found so far for the earlier
+    knobs and the defaults for the later ones; ties keep the first candidate.
+    stage_timer(cfg) -> {stage: ms per frame} and refuse_timer(cfg) -> ms
+    replace the GPU timings (the pipeline's stage profiler, one
+    ss_refuse_batch call) when given.
     """
     pipe_kw = dict(pipe_kw or {})
+    if stage_timer is None:
+        stage_timer = lambda cfg: _stage_ms(depth_dev, poses, frames, grid_kw, intr, cfg, pipe_kw)  # noqa: E731
+    if refuse_timer is None:
+        refuse_timer = lambda cfg: _refuse_ms(depth_dev, poses, frames, grid_kw, intr, cfg)  # noqa: E731
     rows, cols = int(grid_kw["resi_"]), int(grid_kw["resj_"])
     key = _cache_key(rows, cols, grid_kw.get("storage", "f32"))
     if cache is not None and Path(cache).exists():
@@ -95,9 +105,9 @@ def autotune(depth_dev, poses, grid_kw: dict, intr, *, frames: int = 8, pipe_kw:
         for v in values:
             cfg = dict(best, **{knob: v})
             if knob == "refuse_ctas_per_sm":
-                t[v] = _refuse_ms(depth_dev, poses, frames, grid_kw, intr, cfg)
+                t[v] = refuse_timer(cfg)
             else:
-                t[v] = _stage_ms(depth_dev, poses, frames, grid_kw, intr, cfg, pipe_kw)[STAGE[knob]]
+                t[v] = stage_timer(cfg)[STAGE[knob]]
         best[knob] = min(t, key=t.get)
         timings[knob] = {str(k): round(v, 5) for k, v in t.items()}
     if cache is not None:

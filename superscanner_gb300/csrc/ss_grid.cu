@@ -498,6 +498,7 @@ ss_status ss_grid_set_launch_config(ss_grid *g, const ss_launch_config *c) {
         c->refuse_ctas_per_sm > 32 || c->track_ctas_per_sm < 1 || c->track_ctas_per_sm > 2)
         return SS_ERR_ARG;
     g->lc = *c;
+    g->launch_gen++;
     return SS_OK;
 }
 
@@ -692,6 +693,16 @@ ss_status ss_grid_counters(ss_grid *g, ss_stream_t stream, int64_t out[6]) {
     out[3] = (int64_t)c.calls;
     out[4] = c.status;
     out[5] = c.epoch;
+    return SS_OK;
+}
+
+ss_status ss_grid_raycast_counters(ss_grid *g, ss_stream_t stream, int64_t out[2]) {
+    if (!g || !out) return SS_ERR_ARG;
+    SS_CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
+    Counters c;
+    SS_CUDA_TRY(cudaMemcpy(&c, g->v.ctr, sizeof(c), cudaMemcpyDeviceToHost));
+    out[0] = (int64_t)c.ray_finds;
+    out[1] = (int64_t)c.ray_voxels;
     return SS_OK;
 }
 

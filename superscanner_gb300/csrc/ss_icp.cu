@@ -407,7 +407,9 @@ static __device__ __align__(256) unsigned char g_icp_noalloc_scratch[kNoAllocByt
 
 // Device address of the array on each device (the host-side symbol is only a
 // stand-in and must never be handed to a kernel). Filled on the first call
-// made with that device current.
+// made with that device current and kept for the life of the process: a
+// cudaDeviceReset would leave a stale address here, so callers do not reset a
+// device they call this entry point on.
 static std::mutex g_noalloc_mutex;
 static unsigned char *g_noalloc_addr[64] = {};
 

@@ -48,7 +48,9 @@ struct Counters {
     int last_touched;                 // list_count of the previous call
     unsigned long long touched_total; // sum of list_count over all calls
     unsigned long long calls;         // integrate/deintegrate calls finalized
-    int pad[22];
+    unsigned long long ray_finds;     // hash finds of the reference-semantics raycast (all calls)
+    unsigned long long ray_voxels;    // voxel (sdf, w) reads of the reference-semantics raycast (all calls)
+    int pad[18];
 };
 static_assert(sizeof(Counters) == 128, "Counters is one 128-byte line");
 

@@ -45,6 +45,9 @@ struct ss_pipeline {
     std::vector<cudaEvent_t> events;
     size_t used = 0;
     unsigned long long *rc_counters = nullptr;  // raycast traffic counters (device u64[4])
+    int test_wait_polls = 0;  // one-shot test hook: the next tracked frame's tracker wait runs out
+    unsigned exec_gen[2] = {0u, 0u};  // the grid's launch-config generation each graph was captured with
+    unsigned lc_gen = 0;              // the generation track_ctas was computed for
 };
 
 namespace {
@@ -80,10 +83,15 @@ ss_status enqueue_fuse_raycast(ss_pipeline *P, const uint16_t *in, cudaStream_t 
     return SS_OK;
 }
 
-ss_status enqueue_frame(ss_pipeline *P, const uint16_t *in, cudaStream_t s, bool prof = false) {
+ss_status enqueue_frame(ss_pipeline *P, const uint16_t *in, cudaStream_t s, bool prof = false, int wait_polls = 0) {
     ss_grid *g = P->g;
     if (prof) SS_CUDA_TRY(cudaEventRecord(next_event(P), s));
     TrackLaunch L{};
+    L.grid_status = &g->v.ctr->status;
+    if (wait_polls > 0) {
+        L.wait_polls = wait_polls;
+        L.wait_extra = 1;
+    }
     L.depth = in;
     L.rows = g->p.resi;
     L.cols = g->p.resj;
@@ -154,6 +162,7 @@ ss_status ss_pipeline_create(ss_grid *g, const ss_pipeline_params *params, ss_pi
     P->p = *params;
     P->ctas = g->num_sms * 2;
     P->track_ctas = persistent_track_ctas(g->num_sms, g->lc.track_ctas_per_sm);
+    P->lc_gen = g->launch_gen;
     const int slot_ctas = P->ctas > 2 * g->num_sms ? P->ctas : 2 * g->num_sms;
     const size_t npix = (size_t)g->p.resi * g->p.resj;
     bool ok = cudaMalloc(&P->st, sizeof(TrackState)) == cudaSuccess &&
@@ -294,6 +303,10 @@ ss_status ss_pipeline_frame(ss_pipeline *P, const uint16_t *depth, int32_t track
         }
     }
     const uint16_t *in = P->inbuf[b];
+    if (P->lc_gen != g->launch_gen) {  // launch shapes changed: new tracker grid, graphs recaptured below
+        P->track_ctas = persistent_track_ctas(g->num_sms, g->lc.track_ctas_per_sm);
+        P->lc_gen = g->launch_gen;
+    }
     ss_status st = epoch_guard(P, s);
     if (st != SS_OK) return st;
     if (!track || !P->have_model) {
@@ -301,7 +314,13 @@ ss_status ss_pipeline_frame(ss_pipeline *P, const uint16_t *depth, int32_t track
         if (st == SS_OK) st = enqueue_fuse_raycast(P, in, s);
         if (st != SS_OK) return st;
         P->have_model = true;
-    } else if (P->p.use_graph) {
+    } else if (P->p.use_graph && P->test_wait_polls == 0) {
+        if (P->exec[b] && P->exec_gen[b] != g->launch_gen) {  // launch shapes changed since the capture
+            cudaGraphExecDestroy(P->exec[b]);
+            cudaGraphDestroy(P->graph[b]);
+            P->exec[b] = nullptr;
+            P->graph[b] = nullptr;
+        }
         if (!P->exec[b]) {
             SS_CUDA_TRY(cudaStreamBeginCapture(P->cap, cudaStreamCaptureModeThreadLocal));
             // collect, fuse and raycast as programmatic dependents: each launches
@@ -321,15 +340,24 @@ ss_status ss_pipeline_frame(ss_pipeline *P, const uint16_t *depth, int32_t track
             }
             P->graph[b] = graph;
             SS_CUDA_TRY(cudaGraphInstantiate(&P->exec[b], P->graph[b], 0));
+            P->exec_gen[b] = g->launch_gen;
         }
         SS_CUDA_TRY(cudaGraphLaunch(P->exec[b], s));
     } else {
-        st = enqueue_frame(P, in, s, P->profile);
+        st = enqueue_frame(P, in, s, P->profile, P->test_wait_polls);
+        P->test_wait_polls = 0;
         if (st != SS_OK) return st;
     }
     SS_CUDA_TRY(cudaEventRecord(P->ev_done[b], s));
     g->host_epoch++;
     P->frames++;
+    return SS_OK;
+}
+
+ss_status ss_pipeline_test_wait_timeout(ss_pipeline *P, int32_t polls) {
+    if (!P || polls < 0) return SS_ERR_ARG;
+    if (!P->p.persistent_track) return SS_ERR_STATE;
+    P->test_wait_polls = polls;
     return SS_OK;
 }
 

@@ -52,13 +52,14 @@ __device__ __forceinline__ F3 voxel_mid(const GridView &g, int v, int bx, int by
             __fmaf_rn((float)vz + 0.5f, g.vl, __fmul_rn((float)bz, g.vbl))};
 }
 
-__device__ __forceinline__ int find_block(const GridView &g, int bx, int by, int bz) {
+__device__ __forceinline__ int find_block(const GridView &g, int bx, int by, int bz, int &finds) {
+    finds++;
     return table_find(g, prime_hash(bx, by, bz));
 }
 
 template <int kStorage>
 __global__ void __launch_bounds__(256) raycast_ref_kernel(GridView g, Mat34 Er, float *__restrict__ out_pcd,
-                                                          float *__restrict__ out_col) {
+                                                          float *__restrict__ out_col, int iter_cap) {
     const int j = blockIdx.x * 32 + threadIdx.x;
     const int i = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= g.resi || j >= g.resj) return;
@@ -71,20 +72,20 @@ __global__ void __launch_bounds__(256) raycast_ref_kernel(GridView g, Mat34 Er, 
     rv = f3sub(rv, f3smul(__fsub_rn(1.f, l), dir));
 
     bool done = false, Fn = false, Lp = false;
-    int guard = 0;
+    int guard = 0, finds = 0, voxels = 0;  // work counters: hash finds, voxel reads
     F3 hit{0.f, 0.f, 0.f};
     float cr = 0.f, cg = 0.f, cb = 0.f;
 
     while (!done && !Fn && l < dmax) {
         int bx, by, bz;
         block_of(g, rv, bx, by, bz);
-        int bucket = find_block(g, bx, by, bz);
+        int bucket = find_block(g, bx, by, bz, finds);
         int count = 0;
-        while (bucket < 0 && l < dmax && guard < kRaycastIterCap) {
+        while (bucket < 0 && l < dmax && guard < iter_cap) {
             rv = f3add(rv, f3smul(vbl, dir));
             l = __fadd_rn(l, vbl);
             block_of(g, rv, bx, by, bz);
-            bucket = find_block(g, bx, by, bz);
+            bucket = find_block(g, bx, by, bz, finds);
             count++;
             guard++;
         }
@@ -94,24 +95,25 @@ __global__ void __launch_bounds__(256) raycast_ref_kernel(GridView g, Mat34 Er, 
             rv = f3sub(rv, f3smul(back, dir));
             l = __fsub_rn(l, back);
             block_of(g, rv, bx, by, bz);
-            bucket = find_block(g, bx, by, bz);
-            while (bucket < 0 && l < dmax && guard < kRaycastIterCap) {
+            bucket = find_block(g, bx, by, bz, finds);
+            while (bucket < 0 && l < dmax && guard < iter_cap) {
                 rv = f3add(rv, f3smul(dtr, dir));
                 l = __fadd_rn(l, dtr);
                 block_of(g, rv, bx, by, bz);
-                bucket = find_block(g, bx, by, bz);
+                bucket = find_block(g, bx, by, bz, finds);
                 guard++;
             }
         }
         if (l >= dmax) break;
-        if (guard >= kRaycastIterCap) break;
+        if (guard >= iter_cap) break;
         // vb = value_at(index); oldvbInd = vbInd (GPUVoxelGrid.cpp:633-635)
         const int cur = bucket;
         const int ox = bx, oy = by, oz = bz;
         int v = voxel_in_block(g, rv, bx, by, bz);
         while (!done && l < dmax && ox == bx && oy == by && oz == bz && !Fn) {
-            if (++guard >= kRaycastIterCap) break;
+            if (++guard >= iter_cap) break;
             const VoxelRead cv = read_voxel<kStorage>(g, cur, v);
+            voxels++;
             if (cv.w > 0) {
                 if (cv.sdf > 0) {
                     Lp = true;
@@ -128,11 +130,12 @@ __global__ void __launch_bounds__(256) raycast_ref_kernel(GridView g, Mat34 Er, 
                     block_of(g, rv, qx, qy, qz);
                     const int vo = voxel_in_block(g, rv, qx, qy, qz);
                     const F3 vm_out = voxel_mid(g, vo, qx, qy, qz);
-                    const int ob = (qx == ox && qy == oy && qz == oz) ? cur : find_block(g, qx, qy, qz);
+                    const int ob = (qx == ox && qy == oy && qz == oz) ? cur : find_block(g, qx, qy, qz, finds);
                     VoxelRead o{0.f, 0.f};
                     float orr = 0.f, og = 0.f, obb = 0.f;
                     if (ob >= 0) {  // missing block: reads as an empty voxel (reference: value_at(invalid))
                         o = read_voxel<kStorage>(g, ob, vo);
+                        voxels++;
                         if (out_col && g.rgb) {
                             const float *pl = g.rgb + (size_t)ob * 3 * kBlockVoxels + vo;
                             orr = pl[0];
@@ -164,9 +167,17 @@ __global__ void __launch_bounds__(256) raycast_ref_kernel(GridView g, Mat34 Er, 
                 v = voxel_in_block(g, rv, bx, by, bz);
             }
         }
-        if (guard >= kRaycastIterCap) break;
+        if (guard >= iter_cap) break;
     }
-    if (guard >= kRaycastIterCap) atomicOr(&g.ctr->status, kStTimeout);
+    if (guard >= iter_cap) atomicOr(&g.ctr->status, kStTimeout);
+    {  // the warp's work counts, one atomic pair per warp
+        const unsigned m = __activemask();
+        const unsigned f = __reduce_add_sync(m, (unsigned)finds), vx = __reduce_add_sync(m, (unsigned)voxels);
+        if ((threadIdx.x & 31) == __ffs(m) - 1) {
+            atomicAdd(&g.ctr->ray_finds, (unsigned long long)f);
+            atomicAdd(&g.ctr->ray_voxels, (unsigned long long)vx);
+        }
+    }
     const size_t pix = (size_t)i * g.resj + j;
     if (!done) hit = F3{0.f, 0.f, 0.f};
     out_pcd[pix * 3 + 0] = hit.x;
@@ -368,11 +379,18 @@ extern "C" ss_status ss_raycast(ss_grid *g, const float extr[16], float *ray_pcd
     cudaStream_t s = (cudaStream_t)stream;
     const dim3 blk(32, 8), grid((g->p.resj + 31) / 32, (g->p.resi + 7) / 8);
     const Mat34 Er = mat34_from(extr);
+    const int cap = g->raycast_cap > 0 ? g->raycast_cap : kRaycastIterCap;
     if (g->p.storage == SS_STORAGE_F32)
-        raycast_ref_kernel<SS_STORAGE_F32><<<grid, blk, 0, s>>>(g->v, Er, ray_pcd, ray_color);
+        raycast_ref_kernel<SS_STORAGE_F32><<<grid, blk, 0, s>>>(g->v, Er, ray_pcd, ray_color, cap);
     else
-        raycast_ref_kernel<SS_STORAGE_F16><<<grid, blk, 0, s>>>(g->v, Er, ray_pcd, ray_color);
+        raycast_ref_kernel<SS_STORAGE_F16><<<grid, blk, 0, s>>>(g->v, Er, ray_pcd, ray_color, cap);
     SS_LAUNCH_CHECK();
+    return SS_OK;
+}
+
+extern "C" ss_status ss_grid_test_raycast_cap(ss_grid *g, int32_t cap) {
+    if (!g || cap < 0) return SS_ERR_ARG;
+    g->raycast_cap = cap;
     return SS_OK;
 }
 

@@ -405,21 +405,22 @@ __device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long
     return v;
 }
 
-// Warp 0: waits until all words of a buffer hold gridDim.x new contributions
-// (relaxed loads, back-off, at most 2^22 polls: about a second), then returns
+// Warp 0: waits until all words of a buffer hold gridDim.x (+ extra) new
+// contributions (relaxed loads, back-off, at most `polls` polls: 2^22 by
+// default, about a second), then returns
 // in lane v < kTrackAccValues value v of this use in FP64, in units of
 // 2^-kTrackFixShift (the chunk increments recombined exactly into a 128-bit
 // integer t = h 2^64 + l with l signed, then fma(h, 2^64, l): exact for
 // |t| < 2^63, else within two roundings). prev: the buffer's 90 words as read
 // at its previous use (shared), updated here. False on timeout.
 __device__ __forceinline__ bool track_acc_wait(const unsigned long long *__restrict__ acc, unsigned long long *prev,
-                                               double &value) {
+                                               double &value, int polls, int extra) {
     const int v = threadIdx.x & 31;
     const bool mine = v < kTrackAccValues;
     const unsigned long long *w = acc + (size_t)(mine ? v : 0) * kTrackAccChunks * kTrackAccStride;
     const unsigned long long p0 = mine ? prev[3 * v] : 0ull, p1 = mine ? prev[3 * v + 1] : 0ull,
                              p2 = mine ? prev[3 * v + 2] : 0ull;
-    const unsigned long long want = (unsigned long long)gridDim.x;
+    const unsigned long long want = (unsigned long long)gridDim.x + (unsigned long long)extra;
     unsigned long long w0 = 0, w1 = 0, w2 = 0;
     bool done = false;
     int spins = 0;
@@ -436,7 +437,7 @@ __device__ __forceinline__ bool track_acc_wait(const unsigned long long *__restr
         done = __all_sync(0xffffffffu, complete);
         if (done) break;
         __nanosleep(32);
-    } while (++spins < (1 << 22));
+    } while (++spins < polls);
     if (!done) return false;
     value = 0.0;
     if (mine) {
@@ -667,10 +668,11 @@ __global__ void __launch_bounds__(256) track_frame_kernel(const uint16_t *__rest
             SS_TC(barriers, 0);
             barriers++;
             double v = 0.0;
-            if (threadIdx.x < 32 && !track_acc_wait(buf, prevw[abuf], v)) {
+            if (threadIdx.x < 32 && !track_acc_wait(buf, prevw[abuf], v, L.wait_polls, L.wait_extra)) {
                 if (threadIdx.x == 0) {
                     abort_run = 1;
                     atomicOr(&st->status, kStTimeout);
+                    if (L.grid_status) atomicOr(L.grid_status, kStTimeout);
                 }
             } else if (threadIdx.x < 32) {
                 SS_TT(barriers - 1, 3);

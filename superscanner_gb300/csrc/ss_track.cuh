@@ -51,6 +51,13 @@ struct TrackLaunch {
     float dist[kMaxLevels];
     float rmin, dmax;
     bool persistent;  // one cooperative launch for all iterations (else one launch per iteration)
+    // The persistent tracker's wait for the other CTAs' sums: at most wait_polls
+    // polls; it waits for wait_extra contributions more than there are CTAs
+    // (0; a test sets 1 to make the wait run out). On a timeout the status bit
+    // is also set in *grid_status (the grid's status word, read by ss_grid_sync).
+    int wait_polls = 1 << 22;
+    int wait_extra = 0;
+    int *grid_status = nullptr;
 };
 
 ss_status launch_track(const TrackLaunch &L, cudaStream_t s);

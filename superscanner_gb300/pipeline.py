@@ -134,3 +134,8 @@ class Pipeline:
         rm = (C.c_float * 4)()
         check(lib.ss_pipeline_stats(self._h, inl, rm, _stream_ptr(stream)), "pipeline_stats")
         return list(inl), list(rm)
+
+    def test_wait_timeout(self, polls: int = 1000):
+        """Test hook: the next tracked frame's tracker wait runs out after `polls` polls
+        (SS_ERR_TIMEOUT at the next sync; the frame keeps its start pose)."""
+        check(lib.ss_pipeline_test_wait_timeout(self._h, int(polls)), "pipeline_test_wait_timeout")

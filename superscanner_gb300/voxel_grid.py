@@ -160,6 +160,16 @@ class GPUVoxelGrid:
         return dict(live_blocks=a[0], last_touched=a[1], touched_total=a[2], calls=a[3], status=a[4],
                     epoch=a[5])
 
+    def test_raycast_cap(self, cap: int) -> None:
+        """Test hook: ss_raycast's per-ray iteration cap (0 restores the default)."""
+        check(lib.ss_grid_test_raycast_cap(self._h, int(cap)), "test_raycast_cap")
+
+    def raycast_counters(self, stream=None) -> dict:
+        """Hash finds and voxel reads of every raycast call on this grid so far."""
+        a = (C.c_int64 * 2)()
+        check(lib.ss_grid_raycast_counters(self._h, _stream_ptr(stream), a), "raycast_counters")
+        return dict(finds=a[0], voxels=a[1])
+
     def export_blocks(self, stream=None, with_color: bool = True) -> dict:
         """Canonical dump sorted by key (the host copy of marchingCubesHost, :204-206)."""
         n = C.c_int32()
