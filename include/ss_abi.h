@@ -205,6 +205,19 @@ ss_status ss_scheduler_frame(ss_scheduler *s, int64_t id, int32_t *integrated, d
  * with a larger buffer). Synchronises s. */
 ss_status ss_grid_extract_mesh(ss_grid *g, int64_t max_triangles, float *triangles, int64_t *count, ss_stream_t s);
 
+/* The same mesh by marching cubes, in the cube conventions of the Open3D
+ * extraction marchingCubesHost hands the blocks to (GPUVoxelGrid.cpp:200-251:
+ * each unit's voxel (x, y, z) is the block's voxel x + 8y + 64z; a cube of 8
+ * voxel centres counts when all 8 weights are non-zero; corner bit set for
+ * sdf < 0; one vertex per sign-changing edge, interpolated linearly from the
+ * edge's lower end). The case table is derived in code (ss_mc_table.h): its
+ * polygons equal the classic table's except on cube faces with four
+ * crossings (each negative corner cut off), and polygons are fanned from
+ * their first vertex. Triangles face from negative to positive sdf; same
+ * buffer protocol as ss_grid_extract_mesh. Synchronises s. */
+ss_status ss_grid_extract_mesh_cubes(ss_grid *g, int64_t max_triangles, float *triangles, int64_t *count,
+                                     ss_stream_t s);
+
 /* Frame ingest help (src/cameras/DataCam.cpp:10-100 reads depth PNGs): undoes
  * the PNG row filters (types 0..4) of rows x (1 + row_bytes) filtered bytes
  * into rows x row_bytes (bpp: bytes per pixel). Host memory, host code. */
@@ -304,7 +317,7 @@ ss_status ss_kokkos_icp(const uint16_t *d1, const uint16_t *d2, int32_t rows, in
 /* No counterpart in the reference. Same computation, arguments and results as
  * ss_kokkos_icp, but it allocates nothing: for callers that cannot call
  * cudaMalloc while tracking (a real-time thread, or a process whose device
- * memory belongs to its own pool allocator). Its scratch is a fixed 11.2 MB
+ * memory belongs to its own pool allocator). Its scratch is a fixed 11.7 MB
  * device array that every GPU loading the library holds until exit; rows *
  * cols above 640 x 480 return SS_ERR_DIMS. The first call on a device looks up
  * the array's address and should come before any stream capture; the address

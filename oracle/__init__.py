@@ -57,6 +57,7 @@ for name, res, args in [
     ("orm_grid_add_voxel", _i, [_p, _i, _i, _i, _i, C.c_double]),
     ("orm_raycast_loss_grad", C.c_double, [_p, _p, _p, C.c_double, C.c_double, _i, C.c_double, C.c_double, _p, _p]),
     ("orm_extract_mesh", C.c_longlong, [_p, C.c_longlong, _p]),
+    ("orm_extract_mesh_cubes", C.c_longlong, [_p, C.c_longlong, _p]),
     ("orm_raycast_loss", C.c_double, [_p, _p, _p, C.c_double, C.c_double, _i, C.c_double, C.c_double, _p]),
     ("orm_track", _i, [_p, _i, _i, _f, _f, _f, _f, _p, _p, _p, _p, _i, _p, _p, C.c_double, C.c_double]),
 ]:
@@ -236,11 +237,12 @@ class MethodGrid64:
                                           _ptr(grad), _ptr(gvox))
         return (loss, grad, gvox) if voxels else (loss, grad)
 
-    def extract_mesh(self) -> np.ndarray:
-        """Marching-tetrahedra triangle soup [n, 3, 3] (FP64)."""
-        n = _lib.orm_extract_mesh(self._h, 0, C.c_void_p())
+    def extract_mesh(self, method: str = "tetrahedra") -> np.ndarray:
+        """Triangle soup [n, 3, 3] (FP64) by marching tetrahedra or marching cubes."""
+        fn = _lib.orm_extract_mesh_cubes if method == "cubes" else _lib.orm_extract_mesh
+        n = fn(self._h, 0, C.c_void_p())
         out = np.zeros((max(n, 1), 3, 3))
-        _lib.orm_extract_mesh(self._h, n, _ptr(out))
+        fn(self._h, n, _ptr(out))
         return out[:n]
 
     def export(self) -> dict:

@@ -839,6 +839,126 @@ void tetra64(std::vector<double> &out, const P3 *p, const double *s, const int *
 }
 }  // namespace
 
+// ---- marching cubes (the GPU's ss_grid_extract_mesh_cubes) in FP64 ----
+// Cube corners m = 0..7 at (0,0,0) (1,0,0) (1,1,0) (0,1,0) (0,0,1) (1,0,1)
+// (1,1,1) (0,1,1), edges 0-3 / 4-7 around the z = 0 / z = 1 faces, 8-11
+// upwards; corner bit set when sdf < 0. A case's polygons: per cube face the
+// sign-changing edges are paired (two: one segment; four: each negative
+// corner's two edges), segments chain into loops, a loop is oriented by its
+// Newell normal through the edge midpoints against the negative -> positive
+// corner directions, and fanned from its first vertex.
+namespace {
+const int kMcEdge[12][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 0}, {4, 5}, {5, 6}, {6, 7}, {7, 4}, {0, 4}, {1, 5}, {2, 6}, {3, 7}};
+const int kMcPos[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0}, {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
+const int kMcFaceCorner[6][4] = {{0, 1, 2, 3}, {4, 5, 6, 7}, {0, 1, 5, 4}, {3, 2, 6, 7}, {0, 3, 7, 4}, {1, 2, 6, 5}};
+const int kMcFaceEdge[6][4] = {{0, 1, 2, 3}, {4, 5, 6, 7}, {0, 9, 4, 8}, {2, 10, 6, 11}, {3, 11, 7, 8}, {1, 10, 5, 9}};
+
+std::vector<int> mc_case(int cs) {
+    std::vector<int> adj[12];
+    bool cross[12];
+    for (int e = 0; e < 12; e++) cross[e] = ((cs >> kMcEdge[e][0]) & 1) != ((cs >> kMcEdge[e][1]) & 1);
+    for (int f = 0; f < 6; f++) {
+        std::vector<int> cr;
+        for (int q = 0; q < 4; q++)
+            if (cross[kMcFaceEdge[f][q]]) cr.push_back(q);
+        if (cr.size() == 2) {
+            adj[kMcFaceEdge[f][cr[0]]].push_back(kMcFaceEdge[f][cr[1]]);
+            adj[kMcFaceEdge[f][cr[1]]].push_back(kMcFaceEdge[f][cr[0]]);
+        } else if (cr.size() == 4) {
+            for (int q = 0; q < 4; q++) {
+                if (!((cs >> kMcFaceCorner[f][q]) & 1)) continue;
+                const int a = kMcFaceEdge[f][q], b = kMcFaceEdge[f][(q + 3) % 4];
+                adj[a].push_back(b);
+                adj[b].push_back(a);
+            }
+        }
+    }
+    std::vector<int> tri;
+    bool used[12] = {};
+    for (int e = 0; e < 12; e++) {
+        if (!cross[e] || used[e]) continue;
+        std::vector<int> loop;
+        int prev = -1, cur = e;
+        while (!used[cur]) {
+            used[cur] = true;
+            loop.push_back(cur);
+            const int nx = adj[cur][0] != prev ? adj[cur][0] : adj[cur][1];
+            prev = cur;
+            cur = nx;
+        }
+        long n[3] = {0, 0, 0}, d[3] = {0, 0, 0};
+        for (size_t k = 0; k < loop.size(); k++) {
+            const int ea = loop[k], eb = loop[(k + 1) % loop.size()];
+            long pa[3], pb[3];
+            for (int c = 0; c < 3; c++) {
+                pa[c] = kMcPos[kMcEdge[ea][0]][c] + kMcPos[kMcEdge[ea][1]][c];
+                pb[c] = kMcPos[kMcEdge[eb][0]][c] + kMcPos[kMcEdge[eb][1]][c];
+            }
+            n[0] += (pa[1] - pb[1]) * (pa[2] + pb[2]);
+            n[1] += (pa[2] - pb[2]) * (pa[0] + pb[0]);
+            n[2] += (pa[0] - pb[0]) * (pa[1] + pb[1]);
+            const int c0 = kMcEdge[ea][0], c1 = kMcEdge[ea][1];
+            const int neg = ((cs >> c0) & 1) ? c0 : c1, pos = neg == c0 ? c1 : c0;
+            for (int c = 0; c < 3; c++) d[c] += kMcPos[pos][c] - kMcPos[neg][c];
+        }
+        const bool flip = n[0] * d[0] + n[1] * d[1] + n[2] * d[2] < 0;
+        for (size_t k = 1; k + 1 < loop.size(); k++) {
+            tri.push_back(loop[0]);
+            tri.push_back(flip ? loop[k + 1] : loop[k]);
+            tri.push_back(flip ? loop[k] : loop[k + 1]);
+        }
+    }
+    return tri;
+}
+}  // namespace
+
+// Marching-cubes triangles (9 doubles each) into tris (up to cap); returns the total count.
+extern "C" long long orm_extract_mesh_cubes(void *h, long long cap, double *tris) {
+    const Grid64 &g = *(Grid64 *)h;
+    static const int kCell[8] = {0, 1, 3, 2, 4, 5, 7, 6};  // table corner -> cell corner dx + 2 dy + 4 dz
+    std::vector<std::vector<int>> table(256);
+    for (int cs = 0; cs < 256; cs++) table[cs] = mc_case(cs);
+    std::vector<double> out;
+    Cache cache;
+    for (const Block64 *blk : g.blocks) {
+        const int bx = blk->vb[0], by = blk->vb[1], bz = blk->vb[2];
+        for (int c = 0; c < kVox; c++) {
+            const int i = c & 7, j = (c >> 3) & 7, k = c >> 6;
+            P3 p[8];
+            double s[8];
+            bool ok = true;
+            int cs = 0;
+            for (int m = 0; m < 8 && ok; m++) {
+                const int n = kCell[m];
+                const int vi = i + (n & 1), vj = j + ((n >> 1) & 1), vk = k + (n >> 2);
+                const Block64 *b = cached(g, cache, bx + (vi >> 3), by + (vj >> 3), bz + (vk >> 3));
+                const int v = (vi & 7) + 8 * (vj & 7) + 64 * (vk & 7);
+                if (!b || !(b->w[v] > 0)) {
+                    ok = false;
+                    break;
+                }
+                s[m] = b->sdf[v];
+                if (s[m] < 0) cs |= 1 << m;
+                p[m] = {((double)(bx * 8 + vi) + 0.5) * g.vl, ((double)(by * 8 + vj) + 0.5) * g.vl,
+                        ((double)(bz * 8 + vk) + 0.5) * g.vl};
+            }
+            if (!ok || cs == 0 || cs == 255) continue;
+            for (int e : table[cs]) {
+                // from the edge's lower-coordinate end
+                int a = kMcEdge[e][0], b = kMcEdge[e][1];
+                if (kMcPos[a][0] + kMcPos[a][1] + kMcPos[a][2] > kMcPos[b][0] + kMcPos[b][1] + kMcPos[b][2]) std::swap(a, b);
+                const P3 q = edge64(p[a], s[a], p[b], s[b]);
+                out.push_back(q.x);
+                out.push_back(q.y);
+                out.push_back(q.z);
+            }
+        }
+    }
+    const long long n = (long long)out.size() / 9;
+    if (tris) std::memcpy(tris, out.data(), (size_t)std::min(n, cap) * 9 * sizeof(double));
+    return n;
+}
+
 // Triangles (9 doubles each) into tris (up to cap); returns the total count.
 extern "C" long long orm_extract_mesh(void *h, long long cap, double *tris) {
     const Grid64 &g = *(Grid64 *)h;

@@ -80,6 +80,7 @@ SIGNATURES = {
     "ss_clean_memory": (_st, [_p, _p]),
     "ss_refuse_batch": (_st, [_p, _i32, _p, _p, _p, _i32, _p]),
     "ss_grid_extract_mesh": (_st, [_p, C.c_int64, _p, C.POINTER(C.c_int64), _p]),
+    "ss_grid_extract_mesh_cubes": (_st, [_p, C.c_int64, _p, C.POINTER(C.c_int64), _p]),
     "ss_png_unfilter": (_st, [_p, _i32, _i32, _i32, _p]),
     "ss_jpeg_create": (_st, [C.POINTER(_p)]),
     "ss_jpeg_destroy": (_st, [_p]),

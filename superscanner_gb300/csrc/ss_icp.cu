@@ -8,6 +8,7 @@
 // (warp shuffles, then one slot per CTA) and the last CTA to finish reduces
 // the CTA slots in a fixed order, runs a one-sided Jacobi SVD of H in double
 // and writes the next Txy, so the 10 iterations run without a host round trip.
+#include <climits>
 #include <mutex>
 
 #include "ss_grid_impl.cuh"
@@ -126,80 +127,229 @@ __device__ __forceinline__ double warp_sum(double v) {
     return v;
 }
 
+// Orthogonal polar factor R of A = H^T (A = R P, P symmetric positive
+// semidefinite), by one warp: the scaled Newton iteration X <- (g X + (g X)^-T) / 2
+// (Higham, "Computing the polar decomposition with applications", SIAM J. Sci.
+// Stat. Comput. 7, 1986), lane r*3+c holding X[r][c] in FP64, X^-T from the
+// cofactors, g = (|X^-1|_F / |X|_F)^(1/2) in FP32 (the scaling only sets the
+// speed, not the fixed point). For a full-rank H = U S V^T, R = V U^T: the
+// rotation kokkosICP takes from its SVD (kokkosICP.cpp:173-176), without its
+// sign and order conventions. Returns false for a (nearly) rank-deficient H;
+// R is then left unset. Every lane of the warp calls it.
+__device__ bool polar3_warp(const double *H, double *R) {
+    const int lane = threadIdx.x & 31;
+    const bool mine = lane < 9;
+    const int r = mine ? lane / 3 : 0, c = mine ? lane % 3 : 0;
+    double x = mine ? H[c * 3 + r] : 0.0;  // A = H^T
+    // exact power-of-two normalisation (the polar factor does not depend on scale)
+    double mx = fabs(x);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if (!(mx > 0.0) || !isfinite(mx)) return false;
+    x = ldexp(x, -ilogb(mx));
+    const int r1 = (r + 1) % 3, r2 = (r + 2) % 3, c1 = (c + 1) % 3, c2 = (c + 2) % 3;
+    bool ok = true;
+    for (int it = 0; it < 24; it++) {
+        // signed cofactor of (r, c) by the cyclic rule
+        const double a11 = __shfl_sync(0xffffffffu, x, r1 * 3 + c1), a22 = __shfl_sync(0xffffffffu, x, r2 * 3 + c2);
+        const double a12 = __shfl_sync(0xffffffffu, x, r1 * 3 + c2), a21 = __shfl_sync(0xffffffffu, x, r2 * 3 + c1);
+        const double cof = mine ? fma(a11, a22, -a12 * a21) : 0.0;
+        // det = sum_c X[0][c] C[0][c] (lanes 0..2)
+        double dterm = lane < 3 ? x * cof : 0.0;
+        dterm += __shfl_down_sync(0xffffffffu, dterm, 1);
+        dterm += __shfl_down_sync(0xffffffffu, dterm, 2);
+        const double det = __shfl_sync(0xffffffffu, dterm, 0);
+        double fx = x * x, fc = cof * cof;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            fx += __shfl_xor_sync(0xffffffffu, fx, o);
+            fc += __shfl_xor_sync(0xffffffffu, fc, o);
+        }
+        // |det| well below |X|^3: rank-deficient (relative 1e-10)
+        if (!(fabs(det) > 1e-10 * fx * sqrt(fx))) {
+            ok = false;
+            break;
+        }
+        const float q = (float)fc / ((float)(det * det) * (float)fx);
+        const double g = (double)sqrtf(sqrtf(q));
+        // 1 / (g det) in FP64: FP32 seed, two Newton steps
+        const double a = g * det;
+        double y = (double)(1.0f / (float)a);
+        y = fma(y, fma(-a, y, 1.0), y);
+        y = fma(y, fma(-a, y, 1.0), y);
+        const double xn = 0.5 * fma(g, x, cof * y);
+        double dlt = fabs(xn - x);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) dlt = fmax(dlt, __shfl_xor_sync(0xffffffffu, dlt, o));
+        x = xn;
+        if (dlt <= 4e-16) break;
+    }
+    if (!ok) return false;
+    if (mine) R[lane] = x;
+    __syncwarp();
+    return true;
+}
+
+// Target pixels staged per CTA: a tile's 10 x 10 windows (kokkosICP.cpp:81-83)
+// usually fall inside a region of some 42 x 18 pixels; up to this many are
+// staged, larger regions are read from global memory.
+constexpr int kIcpStage = 1536;
+
 // One kokkosICP iteration: Closest Point Kernel (kokkosICP.cpp:69-115) fused
-// with the host sums (:121-171) and, in the last CTA, the SVD update (:173-185).
+// with the host sums (:121-171) and, in the last CTA, the rotation update
+// (:173-185). One thread per source pixel of a 32 x 8 tile. The target points
+// and normals under the tile's windows are staged in shared memory first, a
+// tap that the reference skips (py.z == 0, or n.x == 0 point-to-plane) holding
+// NaN so that its distance fails every comparison; the search then keeps the
+// reference's scan order and strict comparisons (starting from max_dist: the
+// accepted taps of `dist < smallest && dist < max_dist` are exactly those of
+// `dist < min(smallest, max_dist)`), remembers the best tap and forms the
+// correspondence from it afterwards.
 template <int kType>
 __global__ void __launch_bounds__(256) icp_ref_iter_kernel(const float *__restrict__ xp, const float *__restrict__ yp,
                                                            const float *__restrict__ yn, int rows, int cols, Intr in,
                                                            IcpState *st, double *partials) {
+    __shared__ float4 sA[kIcpStage];  // target (x, y, z, nx)
+    __shared__ float2 sB[kIcpStage];  // target (ny, nz)
     __shared__ double red[8][kIcpSums];
+    __shared__ int box[4];
     __shared__ bool last;
     const int n_search = 5;
     const float max_dist = 0.075f;
     Mat34 T;
 #pragma unroll
     for (int k = 0; k < 12; k++) T.m[k] = st->Txy[k];
-    double Td[12];
-#pragma unroll
-    for (int k = 0; k < 12; k++) Td[k] = st->Txy_d[k];
+    const int j = blockIdx.x * 32 + (threadIdx.x & 31), i = blockIdx.y * 8 + (threadIdx.x >> 5);
+    const size_t p = (size_t)i * cols + j;
+    const bool inside = i < rows && j < cols;
+    const F3 x = inside ? ld3(xp, p) : F3{0.f, 0.f, 0.f};
+    const bool has_x = x.z != 0;
+    F3 px{0.f, 0.f, 0.f};
+    int ci = 0, cj = 0;
+    bool search = false;
+    if (has_x) {
+        px = xform(T, x);
+        const float c0 = __fadd_rn(__fdiv_rn(__fmul_rn(px.y, in.fy), px.z), in.ci);
+        const float c1 = __fadd_rn(__fdiv_rn(__fmul_rn(px.x, in.fx), px.z), in.cj);
+        ci = __float2int_rz(c0);
+        cj = __float2int_rz(c1);
+        search = ci > n_search && ci < rows - n_search && cj > n_search && cj < cols - n_search;
+    }
+    // the tile's window region [r0, r1) x [q0, q1)
+    if (threadIdx.x == 0) {
+        box[0] = INT_MAX;
+        box[1] = INT_MIN;
+        box[2] = INT_MAX;
+        box[3] = INT_MIN;
+    }
+    __syncthreads();
+    {
+        int lo_i = search ? ci : INT_MAX, hi_i = search ? ci : INT_MIN;
+        int lo_j = search ? cj : INT_MAX, hi_j = search ? cj : INT_MIN;
+        lo_i = __reduce_min_sync(0xffffffffu, lo_i);
+        hi_i = __reduce_max_sync(0xffffffffu, hi_i);
+        lo_j = __reduce_min_sync(0xffffffffu, lo_j);
+        hi_j = __reduce_max_sync(0xffffffffu, hi_j);
+        if ((threadIdx.x & 31) == 0 && lo_i != INT_MAX) {
+            atomicMin(&box[0], lo_i);
+            atomicMax(&box[1], hi_i);
+            atomicMin(&box[2], lo_j);
+            atomicMax(&box[3], hi_j);
+        }
+    }
+    __syncthreads();
+    const bool any = box[0] != INT_MAX;
+    const int r0 = box[0] - n_search, q0 = box[2] - n_search;
+    const int W = any ? box[3] + n_search - q0 : 0, H = any ? box[1] + n_search - r0 : 0;
+    const bool staged = any && W * H <= kIcpStage;
+    if (staged) {
+        // inside the image: the border test keeps every window within rows x cols
+        for (int t = threadIdx.x; t < W * H; t += blockDim.x) {
+            const int k = r0 + t / W, l = q0 + t % W;
+            const size_t q = (size_t)k * cols + l;
+            F3 py = ld3(yp, q), nn{0.f, 0.f, 0.f};
+            bool ok = py.z != 0;
+            if (kType == SS_ICP_POINT_TO_PLANE) {
+                nn = ld3(yn, q);
+                ok = ok && nn.x != 0;
+            }
+            if (!ok) py.x = __int_as_float(0x7fc00000);
+            sA[t] = make_float4(py.x, py.y, py.z, nn.x);
+            sB[t] = make_float2(nn.y, nn.z);
+        }
+    }
+    __syncthreads();
 
     double acc[kIcpSums];
 #pragma unroll
     for (int k = 0; k < kIcpSums; k++) acc[k] = 0.0;
-
-    const size_t npix = (size_t)rows * cols;
-    for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < npix; p += (size_t)gridDim.x * blockDim.x) {
-        const F3 x = ld3(xp, p);
-        if (x.z == 0) continue;
-        acc[17] += 1.0;  // n_pointsinX
-        const F3 px = xform(T, x);
-        const float c0 = __fadd_rn(__fdiv_rn(__fmul_rn(px.y, in.fy), px.z), in.ci);
-        const float c1 = __fadd_rn(__fdiv_rn(__fmul_rn(px.x, in.fx), px.z), in.cj);
-        const int ci = __float2int_rz(c0), cj = __float2int_rz(c1);
-        if (!(ci > n_search && ci < rows - n_search && cj > n_search && cj < cols - n_search)) continue;
-        float smallest = 1e6f;
-        F3 best{0.f, 0.f, 0.f};
+    if (has_x) acc[17] = 1.0;  // n_pointsinX
+    if (search) {
+        float smallest = max_dist;
+        int best = -1;
         for (int k = ci - n_search; k < ci + n_search; k++) {
             for (int l = cj - n_search; l < cj + n_search; l++) {
-                const size_t q = (size_t)k * cols + l;
-                const F3 py = ld3(yp, q);
-                if (kType == SS_ICP_POINT_TO_POINT) {
-                    if (py.z != 0) {
-                        const float dist = f3len(f3sub(py, px));
-                        if (dist < smallest && dist < max_dist) {
-                            smallest = dist;
-                            best = py;
-                        }
+                F3 py, nn;
+                int tag;
+                if (staged) {
+                    tag = (k - r0) * W + (l - q0);
+                    const float4 a = sA[tag];
+                    py = F3{a.x, a.y, a.z};
+                    if (kType == SS_ICP_POINT_TO_PLANE) {
+                        const float2 b = sB[tag];
+                        nn = F3{a.w, b.x, b.y};
                     }
                 } else {
-                    const F3 nn = ld3(yn, q);
-                    if (py.z != 0 && nn.x != 0) {
-                        const float d = f3dot(f3sub(py, px), nn);
-                        const float dist = fabsf(d);
-                        if (dist < smallest && dist < max_dist) {
-                            smallest = dist;
-                            best = f3add(px, f3smul(d, nn));
-                        }
+                    tag = k * cols + l;
+                    py = ld3(yp, (size_t)tag);
+                    bool ok = py.z != 0;
+                    if (kType == SS_ICP_POINT_TO_PLANE) {
+                        nn = ld3(yn, (size_t)tag);
+                        ok = ok && nn.x != 0;
                     }
+                    if (!ok) py.x = __int_as_float(0x7fc00000);
+                }
+                const float dist = kType == SS_ICP_POINT_TO_POINT ? f3len(f3sub(py, px)) : fabsf(f3dot(f3sub(py, px), nn));
+                if (dist < smallest) {
+                    smallest = dist;
+                    best = tag;
                 }
             }
         }
-        if (best.z == 0) continue;  // x_nearest(i, j).z == 0: no correspondence
-        const double a0 = x.x, a1 = x.y, a2 = x.z, b0 = best.x, b1 = best.y, b2 = best.z;
-        acc[0] += 1.0;
-        acc[1] += a0; acc[2] += a1; acc[3] += a2;
-        acc[4] += b0; acc[5] += b1; acc[6] += b2;
-        acc[7] += a0 * b0;  acc[8] += a0 * b1;  acc[9] += a0 * b2;
-        acc[10] += a1 * b0; acc[11] += a1 * b1; acc[12] += a1 * b2;
-        acc[13] += a2 * b0; acc[14] += a2 * b1; acc[15] += a2 * b2;
-        // RMSE term: || x_nearest4 - Txy_eigen * x4 || in double, squared in float (kokkosICP.cpp:137-138)
-        const double e0 = b0 - (Td[0] * a0 + Td[1] * a1 + Td[2] * a2 + Td[3]);
-        const double e1 = b1 - (Td[4] * a0 + Td[5] * a1 + Td[6] * a2 + Td[7]);
-        const double e2 = b2 - (Td[8] * a0 + Td[9] * a1 + Td[10] * a2 + Td[11]);
-        const float tmp = (float)sqrt(e0 * e0 + e1 * e1 + e2 * e2);
-        acc[16] += (double)(tmp * tmp);
+        if (best >= 0) {
+            F3 py, nn{0.f, 0.f, 0.f};
+            if (staged) {
+                const float4 a = sA[best];
+                const float2 b = sB[best];
+                py = F3{a.x, a.y, a.z};
+                nn = F3{a.w, b.x, b.y};
+            } else {
+                py = ld3(yp, (size_t)best);
+                if (kType == SS_ICP_POINT_TO_PLANE) nn = ld3(yn, (size_t)best);
+            }
+            const F3 bpt = kType == SS_ICP_POINT_TO_POINT ? py : f3add(px, f3smul(f3dot(f3sub(py, px), nn), nn));
+            if (bpt.z != 0) {  // x_nearest(i, j).z != 0: a correspondence (kokkosICP.cpp:131)
+                const double Td[12] = {st->Txy_d[0], st->Txy_d[1], st->Txy_d[2],  st->Txy_d[3],
+                                       st->Txy_d[4], st->Txy_d[5], st->Txy_d[6],  st->Txy_d[7],
+                                       st->Txy_d[8], st->Txy_d[9], st->Txy_d[10], st->Txy_d[11]};
+                const double a0 = x.x, a1 = x.y, a2 = x.z, b0 = bpt.x, b1 = bpt.y, b2 = bpt.z;
+                acc[0] = 1.0;
+                acc[1] = a0; acc[2] = a1; acc[3] = a2;
+                acc[4] = b0; acc[5] = b1; acc[6] = b2;
+                acc[7] = a0 * b0;  acc[8] = a0 * b1;  acc[9] = a0 * b2;
+                acc[10] = a1 * b0; acc[11] = a1 * b1; acc[12] = a1 * b2;
+                acc[13] = a2 * b0; acc[14] = a2 * b1; acc[15] = a2 * b2;
+                // RMSE term: || x_nearest4 - Txy_eigen * x4 || in double, squared in float (kokkosICP.cpp:137-138)
+                const double e0 = b0 - (Td[0] * a0 + Td[1] * a1 + Td[2] * a2 + Td[3]);
+                const double e1 = b1 - (Td[4] * a0 + Td[5] * a1 + Td[6] * a2 + Td[7]);
+                const double e2 = b2 - (Td[8] * a0 + Td[9] * a1 + Td[10] * a2 + Td[11]);
+                const float tmp = (float)sqrt(e0 * e0 + e1 * e1 + e2 * e2);
+                acc[16] = (double)(tmp * tmp);
+            }
+        }
     }
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const unsigned nctas = gridDim.x * gridDim.y, cta = blockIdx.y * gridDim.x + blockIdx.x;
 #pragma unroll
     for (int k = 0; k < kIcpSums; k++) {
         const double v = warp_sum(acc[k]);
@@ -209,38 +359,44 @@ __global__ void __launch_bounds__(256) icp_ref_iter_kernel(const float *__restri
     if (threadIdx.x < kIcpSums) {  // value-major slots: partials[value][cta]
         double s = 0.0;
         for (int w = 0; w < (int)(blockDim.x >> 5); w++) s += red[w][threadIdx.x];
-        partials[(size_t)threadIdx.x * gridDim.x + blockIdx.x] = s;
+        partials[(size_t)threadIdx.x * nctas + cta] = s;
     }
     __threadfence();
     __syncthreads();
-    if (threadIdx.x == 0) last = atomicAdd(&st->ticket, 1) == (int)gridDim.x - 1;
+    if (threadIdx.x == 0) last = atomicAdd(&st->ticket, 1) == (int)nctas - 1;
     __syncthreads();
     if (!last) return;
     __threadfence();
     // last CTA: one warp per sum, lanes stride over the CTA slots, fixed shuffle tree (deterministic)
     __shared__ double tot[kIcpSums];
+    __shared__ double Hs[9], Rs[9];
     for (int v = wid; v < kIcpSums; v += (int)(blockDim.x >> 5)) {
         double s = 0.0;
-        for (unsigned b = lane; b < gridDim.x; b += 32) s += __ldcg(partials + (size_t)v * gridDim.x + b);
+        for (unsigned b = lane; b < nctas; b += 32) s += __ldcg(partials + (size_t)v * nctas + b);
         s = warp_sum(s);
         if (lane == 0) tot[v] = s;
     }
     __syncthreads();
-    if (threadIdx.x != 0) return;
+    if (threadIdx.x >= 32) return;
     const double n = tot[0];
     const double cx[3] = {tot[1] / n, tot[2] / n, tot[3] / n}, cy[3] = {tot[4] / n, tot[5] / n, tot[6] / n};
+    // H = sum (x - cx)(y - cy)^T = sum x y^T - n cx cy^T
+    if (lane < 9) Hs[lane] = tot[7 + lane] - n * cx[lane / 3] * cy[lane % 3];
+    __syncwarp();
+    if (!polar3_warp(Hs, Rs) && lane == 0) {  // rank-deficient H: the SVD's own completion of U
+        double U[9], S[3], V[9];
+        svd3_jacobi(Hs, U, S, V);
+        for (int r = 0; r < 3; r++)
+            for (int c = 0; c < 3; c++)
+                Rs[r * 3 + c] = V[r * 3] * U[c * 3] + V[r * 3 + 1] * U[c * 3 + 1] + V[r * 3 + 2] * U[c * 3 + 2];
+    }
+    __syncwarp();
+    if (lane != 0) return;
     float rsme = (float)tot[16];
     rsme /= (float)n;
     rsme = sqrtf(rsme);
     const float fitness = (float)n / (float)tot[17];
-    // H = sum (x - cx)(y - cy)^T = sum x y^T - n cx cy^T
-    double H[9];
-    for (int r = 0; r < 3; r++)
-        for (int c = 0; c < 3; c++) H[r * 3 + c] = tot[7 + r * 3 + c] - n * cx[r] * cy[c];
-    double U[9], S[3], V[9], R[9];
-    svd3_jacobi(H, U, S, V);
-    for (int r = 0; r < 3; r++)
-        for (int c = 0; c < 3; c++) R[r * 3 + c] = V[r * 3] * U[c * 3] + V[r * 3 + 1] * U[c * 3 + 1] + V[r * 3 + 2] * U[c * 3 + 2];
+    const double *R = Rs;
     double Tn[16];
     for (int k = 0; k < 16; k++) Tn[k] = (k % 5 == 0) ? 1.0 : 0.0;
     for (int r = 0; r < 3; r++) {
@@ -268,6 +424,10 @@ __global__ void __launch_bounds__(256) icp_ref_iter_kernel(const float *__restri
     st->iteration = it + 1;
     st->ticket = 0;
 }
+
+// The iteration kernel's grid: one CTA per 32 x 8 tile of source pixels.
+static inline int icp_tiles_x(int cols) { return (cols + 31) / 32; }
+static inline int icp_tiles_y(int rows) { return (rows + 7) / 8; }
 
 // Scratch of ss_kokkos_icp, one per device, grown on demand.
 struct IcpWorkspace {
@@ -367,11 +527,12 @@ ss_status icp_ref_run(const uint16_t *d1, const uint16_t *d2, int rows, int cols
     h.lowest = 1e6f;
     h.best_fitness = 0.f;
     SS_CUDA_TRY(cudaMemcpyAsync(state, &h, sizeof(h), cudaMemcpyHostToDevice, s));
+    const dim3 tiles(icp_tiles_x(cols), icp_tiles_y(rows));  // ctas == tiles.x * tiles.y
     for (int it = 0; it < kIcpIters; it++) {
         if (type == SS_ICP_POINT_TO_POINT)
-            icp_ref_iter_kernel<SS_ICP_POINT_TO_POINT><<<ctas, 256, 0, s>>>(xp, yp, yn, rows, cols, in, state, partials);
+            icp_ref_iter_kernel<SS_ICP_POINT_TO_POINT><<<tiles, 256, 0, s>>>(xp, yp, yn, rows, cols, in, state, partials);
         else
-            icp_ref_iter_kernel<SS_ICP_POINT_TO_PLANE><<<ctas, 256, 0, s>>>(xp, yp, yn, rows, cols, in, state, partials);
+            icp_ref_iter_kernel<SS_ICP_POINT_TO_PLANE><<<tiles, 256, 0, s>>>(xp, yp, yn, rows, cols, in, state, partials);
         SS_LAUNCH_CHECK();
     }
     SS_CUDA_TRY(cudaMemcpyAsync(&h, state, sizeof(h), cudaMemcpyDeviceToHost, s));
@@ -397,7 +558,7 @@ static ss_status icp_check_args(const uint16_t *d1, const uint16_t *d2, int rows
 // the library is loaded, so the entry point never calls cudaMalloc. Every GPU
 // that loads the library holds these bytes until the process exits.
 constexpr size_t kNoAllocMaxPixels = 640 * 480;  // largest rows * cols accepted
-constexpr int kNoAllocCtas = 608;                // fixed upper bound of the iteration grid
+constexpr int kNoAllocCtas = 4096;  // iteration-grid CTAs (32 x 8 tiles): any rows x cols <= 640 x 480 needs <= 3200
 constexpr size_t kAlign256(size_t n) { return (n + 255) / 256 * 256; }
 constexpr size_t kNoAllocImage = kAlign256(kNoAllocMaxPixels * 3 * sizeof(float));
 constexpr size_t kNoAllocPartials = kAlign256((size_t)kNoAllocCtas * kIcpSums * sizeof(double));
@@ -455,10 +616,13 @@ ss_status ss_kokkos_icp_noalloc(const uint16_t *d1, const uint16_t *d2, int32_t 
         set_last_error_text("ss_kokkos_icp_noalloc: rows * cols exceeds the 640 x 480 scratch");
         return SS_ERR_DIMS;
     }
-    int dev = 0, sms = 0;
+    int dev = 0;
     SS_CUDA_TRY(cudaGetDevice(&dev));
-    SS_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    const int ctas = sms * 4 < kNoAllocCtas ? sms * 4 : kNoAllocCtas;
+    const int ctas = icp_tiles_x(cols) * icp_tiles_y(rows);  // <= 3200 for any image of at most 640 x 480 pixels
+    if (ctas > kNoAllocCtas) {
+        set_last_error_text("ss_kokkos_icp_noalloc: more 32 x 8 tiles than the scratch holds");
+        return SS_ERR_DIMS;
+    }
     unsigned char *base = nullptr;
     st = noalloc_scratch(dev, &base);
     if (st != SS_OK) return st;
@@ -492,10 +656,9 @@ ss_status ss_kokkos_icp(const uint16_t *d1, const uint16_t *d2, int32_t rows, in
                         double txy_out[16], float *rmse_out, ss_stream_t stream) {
     ss_status st = icp_check_args(d1, d2, rows, cols, fx, fy, tx, ty, icp_type, txy_out);
     if (st != SS_OK) return st;
-    int dev = 0, sms = 0;
+    int dev = 0;
     SS_CUDA_TRY(cudaGetDevice(&dev));
-    SS_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    const int ctas = sms * 4;
+    const int ctas = icp_tiles_x(cols) * icp_tiles_y(rows);
     std::lock_guard<std::mutex> lock(g_icp_mutex);
     IcpWorkspace *w = nullptr;
     st = icp_workspace(dev, (size_t)rows * cols, ctas, &w);

@@ -18,6 +18,7 @@
 // neighbouring blocks a block's last row of cells reaches into are looked up
 // once per CTA. Each triangle is appended with one atomic on the counter.
 #include "ss_grid_impl.cuh"
+#include "ss_mc_table.h"
 #include "ss_trilinear.cuh"
 
 namespace ss {
@@ -128,9 +129,109 @@ __global__ void __launch_bounds__(256) mesh_kernel(GridView g, MeshOut o) {
     }
 }
 
+// ---------------------------------------------------------- marching cubes
+// The case table (ss_mc_table.h) in global memory, read through the
+// read-only cache (the lanes of a warp hold different cases).
+__device__ const McTable g_mc_table = kMcTable;
+
+// Marching cubes over the same cells as mesh_kernel: corner m of the table
+// (x + y, ... order of ss_mc_table.h) is cell corner n = dx + 2 dy + 4 dz.
+__constant__ int kMcCornerCell[8] = {0, 1, 3, 2, 4, 5, 7, 6};
+// The end of each table edge with the lower coordinate: a vertex is
+// interpolated from that end, so the cubes sharing an edge compute it alike.
+__constant__ int kMcEdgeLo[12] = {0, 1, 3, 0, 4, 5, 7, 4, 0, 1, 2, 3};
+__constant__ int kMcEdgeHi[12] = {1, 2, 2, 3, 5, 6, 6, 7, 4, 5, 6, 7};
+
+template <int kStorage>
+__global__ void __launch_bounds__(256) mesh_mc_kernel(GridView g, MeshOut o) {
+    __shared__ int nb[8];
+    __shared__ int bc[3];
+    for (uint32_t bucket = blockIdx.x; bucket <= g.mask; bucket += gridDim.x) {
+        const unsigned long long key = g.keys[bucket];
+        if (key == kEmptyKey || key == kTombKey) continue;  // uniform over the CTA
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int x, y, z;
+            unpack_coords(g.stamp[bucket] & ((1ull << kEpochShift) - 1ull), x, y, z);
+            bc[0] = x, bc[1] = y, bc[2] = z;
+            nb[0] = (int)bucket;
+        }
+        __syncthreads();
+        if (threadIdx.x >= 1 && threadIdx.x < 8) {
+            const int n = threadIdx.x, x = bc[0] + (n & 1), y = bc[1] + ((n >> 1) & 1), z = bc[2] + (n >> 2);
+            nb[n] = packable(x, y, z) ? table_find(g, prime_hash(x, y, z)) : -1;
+        }
+        __syncthreads();
+        for (int c = threadIdx.x; c < kBlockVoxels; c += blockDim.x) {
+            const int i = c & 7, j = (c >> 3) & 7, k = c >> 6;
+            F3 p[8];
+            float s[8];
+            bool ok = true;
+            int cs = 0;
+#pragma unroll
+            for (int m = 0; m < 8; m++) {
+                const int n = kMcCornerCell[m];
+                const int vi = i + (n & 1), vj = j + ((n >> 1) & 1), vk = k + (n >> 2);
+                const int b = nb[(vi >> 3) + 2 * (vj >> 3) + 4 * (vk >> 3)];
+                if (b < 0) {
+                    ok = false;
+                    break;
+                }
+                const float2 sw = voxel_sw<kStorage>(g, b, (vi & 7) + 8 * (vj & 7) + 64 * (vk & 7));
+                if (!(sw.y > 0.f)) {  // a corner without observations: no cube (weight 0)
+                    ok = false;
+                    break;
+                }
+                s[m] = sw.x;
+                if (sw.x < 0.f) cs |= 1 << m;
+                p[m] = F3{((float)(bc[0] * 8 + vi) + 0.5f) * g.vl, ((float)(bc[1] * 8 + vj) + 0.5f) * g.vl,
+                          ((float)(bc[2] * 8 + vk) + 0.5f) * g.vl};
+            }
+            if (!ok || cs == 0 || cs == 255) continue;
+            const signed char *tri = g_mc_table.tri[cs];
+            for (int q = 0; q < kMcMaxTris * 3; q += 3) {
+                const int e0 = __ldg(tri + q);
+                if (e0 < 0) break;
+                const int es[3] = {e0, __ldg(tri + q + 1), __ldg(tri + q + 2)};
+                F3 v[3];
+#pragma unroll
+                for (int u = 0; u < 3; u++) {
+                    const int a = kMcEdgeLo[es[u]], b = kMcEdgeHi[es[u]];
+                    v[u] = edge_point(p[a], s[a], p[b], s[b]);
+                }
+                const unsigned long long at = atomicAdd(o.count, 1ull);
+                if (at >= o.cap) continue;
+                float *d = o.tris + at * 9;
+                d[0] = v[0].x, d[1] = v[0].y, d[2] = v[0].z, d[3] = v[1].x, d[4] = v[1].y, d[5] = v[1].z;
+                d[6] = v[2].x, d[7] = v[2].y, d[8] = v[2].z;
+            }
+        }
+    }
+}
+
 }  // namespace ss
 
 using namespace ss;
+
+extern "C" ss_status ss_grid_extract_mesh_cubes(ss_grid *g, int64_t max_triangles, float *triangles, int64_t *count,
+                                                ss_stream_t stream) {
+    if (!g || !count || max_triangles < 0 || (max_triangles > 0 && !triangles)) return SS_ERR_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (!g->mesh_count) SS_CUDA_TRY(cudaMalloc(&g->mesh_count, sizeof(unsigned long long)));
+    SS_CUDA_TRY(cudaMemsetAsync(g->mesh_count, 0, sizeof(unsigned long long), s));
+    MeshOut o{triangles, g->mesh_count, (unsigned long long)max_triangles};
+    const int ctas = g->num_sms * 8;
+    if (g->p.storage == SS_STORAGE_F32)
+        mesh_mc_kernel<SS_STORAGE_F32><<<ctas, 256, 0, s>>>(g->v, o);
+    else
+        mesh_mc_kernel<SS_STORAGE_F16><<<ctas, 256, 0, s>>>(g->v, o);
+    SS_LAUNCH_CHECK();
+    unsigned long long n = 0;
+    SS_CUDA_TRY(cudaMemcpyAsync(&n, g->mesh_count, sizeof(n), cudaMemcpyDeviceToHost, s));
+    SS_CUDA_TRY(cudaStreamSynchronize(s));
+    *count = (int64_t)n;
+    return SS_OK;
+}
 
 extern "C" ss_status ss_grid_extract_mesh(ss_grid *g, int64_t max_triangles, float *triangles, int64_t *count,
                                           ss_stream_t stream) {

@@ -1,6 +1,7 @@
 """Mesh export of the TSDF on the GPU (the reference meshes on the host:
-marchingCubesHost, GPUVoxelGrid.cpp:200-251): marching tetrahedra over the
-observed cells, then vertices welded on the host and written as PLY."""
+marchingCubesHost, GPUVoxelGrid.cpp:200-251): marching cubes (or marching
+tetrahedra) over the observed cells, then vertices welded on the host and
+written as PLY."""
 from __future__ import annotations
 
 import ctypes as C
@@ -12,15 +13,17 @@ from ._native import check, lib
 from .voxel_grid import GPUVoxelGrid, _stream_ptr
 
 
-def extract_triangles(grid: GPUVoxelGrid, stream=None) -> torch.Tensor:
+def extract_triangles(grid: GPUVoxelGrid, stream=None, method: str = "cubes") -> torch.Tensor:
     """Triangle soup as a CUDA tensor [n, 3, 3] (world coordinates; each
-    triangle faces from negative to positive TSDF)."""
+    triangle faces from negative to positive TSDF), by marching cubes (the
+    cube conventions of the Open3D extraction the reference runs) or by
+    marching tetrahedra (method="tetrahedra")."""
+    fn = lib.ss_grid_extract_mesh_cubes if method == "cubes" else lib.ss_grid_extract_mesh
     n = C.c_int64()
-    check(lib.ss_grid_extract_mesh(grid.handle, 0, None, C.byref(n), _stream_ptr(stream)), "extract_mesh")
+    check(fn(grid.handle, 0, None, C.byref(n), _stream_ptr(stream)), "extract_mesh")
     cap = n.value
     out = torch.empty((max(cap, 1), 3, 3), dtype=torch.float32, device=grid.device)
-    check(lib.ss_grid_extract_mesh(grid.handle, cap, C.c_void_p(out.data_ptr()), C.byref(n), _stream_ptr(stream)),
-          "extract_mesh")
+    check(fn(grid.handle, cap, C.c_void_p(out.data_ptr()), C.byref(n), _stream_ptr(stream)), "extract_mesh")
     return out[:min(cap, n.value)]
 
 

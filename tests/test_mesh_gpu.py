@@ -1,5 +1,6 @@
-"""GPU mesh extraction against the FP64 oracle's marching tetrahedra on the
-same volume: the same triangles (count, centroids within 10 um, orientation)."""
+"""GPU mesh extraction against the FP64 oracle's on the same volume, by
+marching cubes and by marching tetrahedra: the same triangles (count,
+centroids within 10 um, orientation)."""
 import numpy as np
 import pytest
 import torch
@@ -13,12 +14,12 @@ from superscanner_gb300.mesh import extract_triangles
 pytestmark = pytest.mark.gpu
 
 
-def compare(g, vl, trunc):
+def compare(g, vl, trunc, method):
     d = g.export_blocks(with_color=False)
     o = oracle.MethodGrid64(vl, trunc, g.resi, g.resj)
     o.import_blocks(d["coords"], d["sdf"], d["w"])
-    t64 = o.extract_mesh()
-    t32 = extract_triangles(g).cpu().numpy().astype(np.float64)
+    t64 = o.extract_mesh(method)
+    t32 = extract_triangles(g, method=method).cpu().numpy().astype(np.float64)
     assert len(t32) == len(t64) and len(t32) > 1000
     from scipy.spatial import cKDTree
     c32, c64 = t32.mean(axis=1), t64.mean(axis=1)
@@ -35,17 +36,19 @@ def compare(g, vl, trunc):
     return len(t32)
 
 
-def test_mesh_of_the_analytic_wall():
+@pytest.mark.parametrize("method", ["cubes", "tetrahedra"])
+def test_mesh_of_the_analytic_wall(method):
     coords, sdf, w, obs, intr = wavy_wall()
     g = GPUVoxelGrid(int(1e9), WTRUNC, WVL, obs.shape[0], obs.shape[1], storage="f32", with_color=False,
                      hash_buckets=1 << 17)
     g.setIntrinsic(*intr)
     g.import_blocks(coords, sdf, w)
     g.sync()
-    compare(g, WVL, WTRUNC)
+    compare(g, WVL, WTRUNC, method)
 
 
-def test_mesh_of_a_fused_room_f16():
+@pytest.mark.parametrize("method", ["cubes", "tetrahedra"])
+def test_mesh_of_a_fused_room_f16(method):
     INTR = (525.0, 525.0, 319.5, 239.5)
     sc = synth.Scene(2, 1234)
     P = sc.trajectory(10, 42)
@@ -57,5 +60,5 @@ def test_mesh_of_a_fused_room_f16():
         g.integrate_fast(torch.from_numpy(np.ascontiguousarray(depth[k].view(np.int16))).cuda(),
                          P[k].astype(np.float32))
     g.sync()
-    n = compare(g, 0.004, 0.016)
+    n = compare(g, 0.004, 0.016, method)
     assert n > 100000

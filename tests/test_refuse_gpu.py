@@ -67,6 +67,39 @@ def test_batched_refusion_equals_sequential(storage, exact):
     assert np.array_equal(a["sdf"], b["sdf"])
 
 
+def test_batched_refusion_matches_oracle():
+    """The exact batched re-fusion against the CPU oracle's sequential
+    deIntegrate(old pose) + integrate(new pose) per keyframe (the reference's
+    re-fusion, src/core/integrate.cpp:109-113, with reference arithmetic):
+    block set, weights and TSDF bit for bit (FP32 storage, no weight cap)."""
+    import oracle
+    sc = synth.Scene(2, 1234)
+    P = sc.trajectory(24, 42)
+    depth, _ = sc.render(P, 480, 640, INTR, noise=True, noise_seed=7, color=False)
+    masks = synth.occlusion_masks(24, 480, 640, seed=99)
+    depth = np.where(masks, depth, 0).astype(np.uint16)
+    dev = [torch.from_numpy(np.ascontiguousarray(d.view(np.int16))).cuda() for d in depth]
+    rng = np.random.default_rng(5)
+    kf = list(range(0, 24, 2))
+    T_new = np.stack([delta(rng) @ P[k] for k in kf])
+    g = GPUVoxelGrid(int(1e9), 0.016, 0.004, 480, 640, storage="f32", with_color=False, hash_buckets=1 << 18)
+    g.setIntrinsic(*INTR)
+    o = oracle.OracleGrid(0.004, 0.016, 480, 640, intr=INTR)
+    for k in range(24):
+        g.integrate(None, dev[k], P[k].astype(np.float32), withColor=False)
+        o.integrate(depth[k], None, P[k].astype(np.float32), with_color=False)
+    g.refuse_batch([dev[k] for k in kf], P[kf], T_new, exact=True)
+    for q, k in enumerate(kf):
+        o.deintegrate(depth[k], None, P[k].astype(np.float32), with_color=False)
+        o.integrate(depth[k], None, T_new[q].astype(np.float32), with_color=False)
+    g.sync()
+    a, b = g.export_blocks(with_color=False), o.export()
+    g.close()
+    assert np.array_equal(a["keys"], b["keys"]) and np.array_equal(a["coords"], b["coords"])
+    assert np.array_equal(a["w"], b["w"])
+    assert np.array_equal(a["sdf"], b["sdf"])
+
+
 def test_batched_refusion_scattered_depths():
     """The batched collection off its common path (random depths up to 40 m:
     blocks beyond the tile set's key range, crowded tile sets) still gives the
