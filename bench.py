@@ -804,7 +804,7 @@ def main_ours(args):
                               "unit": "frames/s", "steps": K, "warmup": W, "only": "chosen"}), flush=True)
         return
     mesh = None
-    if rank == 0:  # mesh export of the chosen form's volume (GPU marching tetrahedra)
+    if rank == 0:  # mesh export of the chosen form's volume (GPU marching cubes)
         from superscanner_gb300.mesh import extract_triangles
         extract_triangles(chosen["grid"], stream=stream)
         t0 = time.perf_counter()

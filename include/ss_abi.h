@@ -366,6 +366,14 @@ ss_status ss_raycast_loss(ss_grid *g, const double T[16], const uint16_t *depth_
 ss_status ss_raycast_loss_grad(ss_grid *g, const double T[16], const uint16_t *depth_obs, float lambda_n,
                                float r_max, int32_t max_steps, double *loss, double grad_pose[6],
                                float *grad_voxels, int64_t *valid_pixels, ss_stream_t s);
+/* The same restricted to the pixels whose pixel_mask byte ([resi][resj] u8,
+ * device) is non-zero (a pixel must also be valid as above): the loss over a
+ * fixed pixel set, e.g. to compare the adjoint with finite differences
+ * taken with that set frozen. */
+ss_status ss_raycast_loss_grad_masked(ss_grid *g, const double T[16], const uint16_t *depth_obs,
+                                      const uint8_t *pixel_mask, float lambda_n, float r_max, int32_t max_steps,
+                                      double *loss, double grad_pose[6], float *grad_voxels, int64_t *valid_pixels,
+                                      ss_stream_t s);
 
 typedef struct ss_pipeline ss_pipeline;
 

@@ -119,6 +119,8 @@ SIGNATURES = {
     "ss_raycast_loss": (_st, [_p, _D16, _p, _f, _f, _i32, C.POINTER(C.c_double), C.POINTER(C.c_int64), _p, _p]),
     "ss_raycast_loss_grad": (_st, [_p, _D16, _p, _f, _f, _i32, C.POINTER(C.c_double), C.POINTER(C.c_double), _p,
                                    C.POINTER(C.c_int64), _p]),
+    "ss_raycast_loss_grad_masked": (_st, [_p, _D16, _p, _p, _f, _f, _i32, C.POINTER(C.c_double),
+                                          C.POINTER(C.c_double), _p, C.POINTER(C.c_int64), _p]),
     "ss_pipeline_params_default": (_st, [C.POINTER(SSPipelineParams)]),
     "ss_pipeline_create": (_st, [_p, C.POINTER(SSPipelineParams), C.POINTER(_p)]),
     "ss_pipeline_destroy": (_st, [_p]),

@@ -92,7 +92,8 @@ __global__ void __launch_bounds__(256) raydiff_kernel(GridView g, Mat34 T, const
                                                       int max_steps, float t_min, float t_max, float lambda_n,
                                                       float r_max, float2 *__restrict__ slots, double *result,
                                                       int *ticket, float *__restrict__ grad_vox,
-                                                      float *__restrict__ depth_out) {
+                                                      float *__restrict__ depth_out,
+                                                      const uint8_t *__restrict__ mask) {
     const int j = blockIdx.x * 32 + threadIdx.x;
     const int i = blockIdx.y * blockDim.y + threadIdx.y;
     float acc[kDiffSums];
@@ -135,7 +136,7 @@ __global__ void __launch_bounds__(256) raydiff_kernel(GridView g, Mat34 T, const
         const size_t pix = (size_t)i * g.resj + j;
         if (depth_out) depth_out[pix] = cs.valid ? t : 0.f;
         const float d_obs = (float)__ldg(obs + pix) * 1e-3f;
-        if (cs.valid && d_obs > g.rmin) {
+        if (cs.valid && d_obs > g.rmin && (!mask || __ldg(mask + pix))) {
             const float gn = sqrtf(cs.g[0] * cs.g[0] + cs.g[1] * cs.g[1] + cs.g[2] * cs.g[2]);
             const float n[3] = {cs.g[0] / gn, cs.g[1] / gn, cs.g[2] / gn};
             const float d[3] = {dx, dy, dz};
@@ -246,7 +247,7 @@ static ss_status diff_scratch(ss_grid *g, int nb, DiffScratch **out) {
 
 static ss_status raydiff(ss_grid *g, const double T[16], const uint16_t *obs, float lambda_n, float r_max,
                          int32_t max_steps, bool backward, double *loss, double grad[6], int64_t *valid,
-                         float *grad_vox, float *depth_out, cudaStream_t s) {
+                         float *grad_vox, float *depth_out, cudaStream_t s, const uint8_t *mask = nullptr) {
     if (!g || !T || !obs || !loss || max_steps <= 0 || !(r_max > 0.f)) return SS_ERR_ARG;
     if (backward && !grad) return SS_ERR_ARG;
     if (!g->intr_set) return SS_ERR_STATE;
@@ -263,7 +264,7 @@ static ss_status raydiff(ss_grid *g, const double T[16], const uint16_t *obs, fl
     const float t_min = g->p.rmin, t_max = g->p.d_max;
 #define SS_RD(ST, BW)                                                                                           \
     raydiff_kernel<ST, BW><<<grid, blk, 0, s>>>(g->v, M, obs, max_steps, t_min, t_max, lambda_n, r_max, d->slots, \
-                                                d->result, d->ticket, grad_vox, depth_out)
+                                                d->result, d->ticket, grad_vox, depth_out, mask)
     if (g->p.storage == SS_STORAGE_F32) {
         if (backward) SS_RD(SS_STORAGE_F32, true); else SS_RD(SS_STORAGE_F32, false);
     } else {
@@ -292,6 +293,15 @@ ss_status ss_raycast_loss(ss_grid *g, const double T[16], const uint16_t *depth_
                           ss_stream_t s) {
     return raydiff(g, T, depth_obs, lambda_n, r_max, max_steps, false, loss, nullptr, valid_pixels, nullptr,
                    depth_out, (cudaStream_t)s);
+}
+
+ss_status ss_raycast_loss_grad_masked(ss_grid *g, const double T[16], const uint16_t *depth_obs,
+                                      const uint8_t *pixel_mask, float lambda_n, float r_max, int32_t max_steps,
+                                      double *loss, double grad_pose[6], float *grad_voxels, int64_t *valid_pixels,
+                                      ss_stream_t s) {
+    if (!pixel_mask) return SS_ERR_ARG;
+    return raydiff(g, T, depth_obs, lambda_n, r_max, max_steps, true, loss, grad_pose, valid_pixels, grad_voxels,
+                   nullptr, (cudaStream_t)s, pixel_mask);
 }
 
 ss_status ss_raycast_loss_grad(ss_grid *g, const double T[16], const uint16_t *depth_obs, float lambda_n,

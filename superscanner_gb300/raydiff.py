@@ -39,6 +39,20 @@ def raycast_loss_grad(grid: GPUVoxelGrid, T, depth_obs, lambda_n: float = 1.0, r
     return loss.value, np.array(grad[:]), valid.value
 
 
+def raycast_loss_grad_masked(grid: GPUVoxelGrid, T, depth_obs, pixel_mask, lambda_n: float = 1.0,
+                             r_max: float = 0.05, max_steps: int = 128, stream=None):
+    """raycast_loss_grad over the pixels whose pixel_mask (CUDA uint8 [rows, cols]) is non-zero."""
+    loss = C.c_double()
+    valid = C.c_int64()
+    grad = (C.c_double * 6)()
+    d = _dev_ptr(depth_obs, 2, (grid.resi, grid.resj), "depth_obs")
+    m = _dev_ptr(pixel_mask, 1, (grid.resi, grid.resj), "pixel_mask")
+    check(lib.ss_raycast_loss_grad_masked(grid.handle, f64x16(T), d, m, float(lambda_n), float(r_max),
+                                          int(max_steps), C.byref(loss), grad, C.c_void_p(), C.byref(valid),
+                                          _stream_ptr(stream)), "raycast_loss_grad_masked")
+    return loss.value, np.array(grad[:]), valid.value
+
+
 def se3_exp(xi) -> np.ndarray:
     """exp of a twist (omega, upsilon) as a 4x4 matrix (left increment)."""
     w, v = np.asarray(xi[:3], float), np.asarray(xi[3:], float)

@@ -1,8 +1,9 @@
 """Differentiable raycast: GPU forward loss against the FP64 oracle, and the
 hand-written adjoint (pose se(3) and voxel TSDF gradients) against the FP64
-adjoint on a fused scene and against FP64 central finite differences
+adjoint on a fused scene, against FP64 central finite differences
 (h = 1e-4 on the pose twist, 1e-3 of the truncation on voxels) on a smooth
-analytic wall."""
+analytic wall, and against FP64 pose differences on the fused FP16 room with
+the pixel set frozen."""
 import numpy as np
 import pytest
 import torch
@@ -120,6 +121,39 @@ def test_adjoint_matches_fp64_finite_differences(storage, tol):
         print("voxel", b, v, "gpu", gvn[b, v], "fd", fdv)
         rel.append(abs(gvn[b, v] - fdv) / max(abs(fdv), 1e-12))
     assert np.median(rel) < tol and max(rel) < 4 * tol
+
+
+def test_pose_adjoint_matches_fp64_differences_with_frozen_pixels():
+    """Config 5's check on the fused FP16 room: FP64 central differences
+    (h = 1e-4 on the pose twist) of the loss over a frozen pixel set against
+    the GPU adjoint over the same pixels (ss_raycast_loss_grad_masked). The set
+    keeps the pixels that are valid at the pose and at all twelve perturbed
+    poses and whose loss term changes smoothly there (second difference below
+    1 % of the first), so no pixel enters or leaves the loss between the
+    evaluations and no ray's hit jumps to another surface."""
+    from superscanner_gb300.raydiff import raycast_loss_grad_masked
+    g, o, d, P, depth, dev = setup("f16")
+    T = se3_exp([0.004, -0.003, 0.002, 0.006, -0.004, 0.003]) @ P[7]
+    h = 1e-4
+    base = o.raycast_loss_pixels(T, depth[7])
+    plus, minus = [], []
+    for i in range(6):
+        e = np.zeros(6)
+        e[i] = h
+        plus.append(o.raycast_loss_pixels(se3_exp(e) @ T, depth[7]))
+        minus.append(o.raycast_loss_pixels(se3_exp(-e) @ T, depth[7]))
+    Lp, Lm = np.stack(plus), np.stack(minus)
+    with np.errstate(invalid="ignore"):
+        ok = np.isfinite(base) & np.isfinite(Lp).all(0) & np.isfinite(Lm).all(0)
+        smooth = ok & (np.abs(Lp + Lm - 2 * base) <= 0.01 * np.abs(Lp - Lm) + 1e-15).all(0)
+    frozen = smooth.astype(np.uint8)
+    assert frozen.sum() > 0.5 * np.isfinite(base).sum()
+    fd = np.where(smooth, Lp - Lm, 0.0).sum(axis=(1, 2)) / (2 * h)
+    L, grad, nv = raycast_loss_grad_masked(g, T, dev[7], torch.from_numpy(frozen).cuda())
+    print("frozen pixels", int(frozen.sum()), "gpu valid among them", nv)
+    print("pose grad gpu", grad, "\n      fp64 fd", fd)
+    assert nv >= 0.999 * frozen.sum()
+    assert np.abs(grad - fd).max() <= 0.02 * np.abs(fd).max()
 
 
 def test_pose_refinement_through_the_adjoint():
