@@ -73,9 +73,10 @@ def parse():
                     help="frames of the gradient-based pose refinement through the raycast adjoint (0: skip)")
     ap.add_argument("--buckets", type=int, default=BUCKETS,
                     help="hash buckets (profiler captures use a smaller table to keep device memory small)")
-    ap.add_argument("--only", choices=["all", "chosen", "refusion"], default="all",
+    ap.add_argument("--only", choices=["all", "chosen", "refusion", "dropin"], default="all",
                     help="chosen: time the chosen form alone; refusion: time the batched re-fusion alone, "
-                         "three calls with the poses swapped between calls (both for profiler captures)")
+                         "three calls with the poses swapped between calls; dropin: the reference's call "
+                         "surface alone (all for profiler captures)")
     return ap.parse_args()
 
 
@@ -358,9 +359,8 @@ def run_refusion(torch, depth, P, stream, n_kf: int = 200, launch=None, modes=("
     res["coverage_min_max"] = [round(float(cover.min()), 3), round(float(cover.max()), 3)]
     if "sequential" in res:
         alg = block_calls * 512 * 4 * 2 + 2 * n_kf * ROWS * COLS * 2
-        res["algorithmic_bytes"] = {"value": int(alg), "block_calls": int(block_calls),
-                                    "note": "sum over the 2 n_kf integrate/deintegrate calls of touched blocks x "
-                                            "512 x (4 B read + 4 B written), plus each call's depth image"}
+        # the 2 n_kf calls' touched blocks x 512 x (4 B read + 4 B written), plus each call's depth image
+        res["algorithmic_bytes"] = int(alg)
         for m in modes:
             gbs = alg / (res[m]["ms"] * 1e-3) / 1e9
             res[m]["achieved_gbs"] = round(gbs, 1)
@@ -778,6 +778,13 @@ def main_ours(args):
     depth_dev = torch.from_numpy(depth.view(np.int16)).cuda()
     stream = torch.cuda.Stream()
     peak, peak_kind = measured_peaks()
+    if args.only == "dropin":
+        if rank == 0:
+            torch.cuda.nvtx.range_push("dropin")
+            res = run_dropin(torch, depth_dev, P, W, K, stream, peak)
+            torch.cuda.nvtx.range_pop()
+            print(json.dumps({"metric": "dropin_frames_per_s", "impl": "ours", "dropin": res}))
+        return
     if args.only == "refusion":
         if rank == 0:
             res = run_refusion(torch, depth, P, stream, modes=("batched",), calls=3)
@@ -810,8 +817,7 @@ def main_ours(args):
         t0 = time.perf_counter()
         tris = extract_triangles(chosen["grid"], stream=stream)
         mesh = {"triangles": int(tris.shape[0]), "live_blocks": int(chosen["live"]),
-                "ms": round((time.perf_counter() - t0) * 1e3, 3),
-                "note": "two calls (count, then extract) incl. host sync; world-space triangle soup"}
+                "ms": round((time.perf_counter() - t0) * 1e3, 3), "method": "marching cubes"}
         del tris
     plain = run_form(torch, "plain", depth_dev, P, W, K, stream, barrier)
     prof = run_form(torch, "chosen", depth_dev, P, W, K, stream, lambda: None, profile=True, launch=tuned)
@@ -905,15 +911,13 @@ def main_ours(args):
             "autotune_ms": tune_ms,
             "chosen_over_plain": round(fps_c / fps_p, 3),
             "roofline": roof,
-            "stages": table,
+            "stages": {k: {"ms": v["ms_per_frame"], "frac": v["frac"]} for k, v in table.items()},
             "raycast_counters_per_frame": {k: round(v / max(prof["prof_frames"], 1), 1) for k, v in prof["rc"].items()},
             "touched_blocks_per_frame": round(prof["touched"] / max(prof["prof_frames"], 1), 1),
             "live_blocks": chosen["live"],
             "cpu_baseline": cpu,
             "l2_flushed": {"value": round(world * k_flush / (flushed_ms * 1e-3), 2), "unit": "frames/s",
-                           "ms_per_step": round(flushed_ms / k_flush, 4), "frames": k_flush,
-                           "note": "chosen form, 512 MB written before every frame outside the timed window "
-                                   "(L2 129 MB), CUDA events around each frame alone"},
+                           "frames": k_flush},
             "e2e": {"value": round(e2e_fps, 2), "unit": "frames/s", "h2d_bytes_per_step": ROWS * COLS * 2,
                     "d2h_bytes_per_step": 16 * 8, "wall_s": round(e2e["wall_s"], 4)},
             "gpu_launches": KERNELS_PER_FRAME * K,

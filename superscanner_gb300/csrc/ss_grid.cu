@@ -13,6 +13,7 @@
 //   list   i32[B]          buckets touched by the current call (deduplicated)
 // One 8^3 block is 4 KB (plain) or 2 KB (precision) contiguous: a warp reads a
 // whole block as 16 fully coalesced 256/128-byte rows.
+#include <climits>
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -307,6 +308,14 @@ __global__ void __launch_bounds__(256) clean_kernel(GridView g) {
     }
 }
 
+// Empties the super-blocks' bounding box (before a rebuild re-derives it).
+__global__ void super_bbox_reset_kernel(Counters *c) {
+    if (threadIdx.x < 3) {
+        c->sb_lo[threadIdx.x] = INT_MAX;
+        c->sb_hi[threadIdx.x] = INT_MIN;
+    }
+}
+
 // Re-derives the super-block set from the live blocks (after clean).
 __global__ void super_rebuild_kernel(GridView g) {
     for (size_t b = blockIdx.x * (size_t)blockDim.x + threadIdx.x; b <= g.mask; b += (size_t)gridDim.x * blockDim.x) {
@@ -516,6 +525,10 @@ ss_status ss_grid_reset(ss_grid *g, ss_stream_t stream) {
     Counters c;
     std::memset(&c, 0, sizeof(c));
     c.epoch = 1;
+    for (int a = 0; a < 3; a++) {
+        c.sb_lo[a] = INT_MAX;
+        c.sb_hi[a] = INT_MIN;
+    }
     SS_CUDA_TRY(cudaMemcpyAsync(g->v.ctr, &c, sizeof(c), cudaMemcpyHostToDevice, s));
     SS_CUDA_TRY(cudaStreamSynchronize(s));
     g->host_epoch = 1;
@@ -560,6 +573,7 @@ ss_status ss_grid_create(const ss_params *p, ss_grid **out) {
     g->v.vl = p->voxel_length;
     g->v.vbl = kEdge * p->voxel_length;  // GPUVoxelGrid.cpp:15
     g->v.rvbl = 1.0f / g->v.vbl;
+    g->v.rvl = 1.0f / g->v.vl;
     g->v.trunc = p->truncation;
     g->v.rmin = p->rmin;
     g->v.d_max = p->d_max;
@@ -656,6 +670,7 @@ ss_status ss_clean_memory(ss_grid *g, ss_stream_t stream) {
     else clean_kernel<SS_STORAGE_F16><<<persistent_ctas(g, 8), 256, 0, s>>>(g->v);
     SS_LAUNCH_CHECK();
     fill_u64_kernel<<<persistent_ctas(g, 1), 256, 0, s>>>(g->v.sbkeys, (size_t)g->v.sbmask + 1, kSuperEmpty);
+    super_bbox_reset_kernel<<<1, 32, 0, s>>>(g->v.ctr);
     super_rebuild_kernel<<<persistent_ctas(g, 4), 256, 0, s>>>(g->v);
     SS_LAUNCH_CHECK();
     return SS_OK;

@@ -50,7 +50,8 @@ struct Counters {
     unsigned long long calls;         // integrate/deintegrate calls finalized
     unsigned long long ray_finds;     // hash finds of the reference-semantics raycast (all calls)
     unsigned long long ray_voxels;    // voxel (sdf, w) reads of the reference-semantics raycast (all calls)
-    int pad[18];
+    int sb_lo[3], sb_hi[3];           // bounding box of the marked super-blocks (empty: lo > hi)
+    int pad[12];
 };
 static_assert(sizeof(Counters) == 128, "Counters is one 128-byte line");
 
@@ -99,6 +100,7 @@ struct GridView {
     uint32_t mask;              // buckets - 1
     float vl, vbl, trunc, rmin, d_max, max_weight;
     float rvbl;  // RN(1 / vbl), computed on the host
+    float rvl;   // RN(1 / vl), computed on the host
     int resi, resj;
     Intr in;
     // getPoint's per-column and per-row quotients (j - cj) / fx and
@@ -188,6 +190,12 @@ __device__ __forceinline__ bool idx_fast(float a, float rlen, int &out) {
     const float q1 = __fmul_rn(a, rlen);
     out = __float2int_rd(q1);
     return fabsf(__fsub_rn(q1, rintf(q1))) > __fmaf_rn(fabsf(q1), 3.0e-7f, 3.0e-7f);  // > 5 u (|q1| + 1)
+}
+
+// idx_rule(a, len) through idx_fast where that is decisive (rlen = RN(1 / len)).
+__device__ __forceinline__ int idx_rule_fast(float a, float len, float rlen) {
+    int o;
+    return idx_fast(a, rlen, o) ? o : idx_rule(a, len);
 }
 
 // The block range of a point's truncation band: idx_rule of its corners lo
@@ -333,7 +341,17 @@ __device__ __forceinline__ void super_insert(const GridView &g, int bx, int by, 
         if (k == key) return;
         if (k == kSuperEmpty) {
             const unsigned long long old = atomicCAS(g.sbkeys + b, kSuperEmpty, key);
-            if (old == kSuperEmpty || old == key) return;
+            if (old == kSuperEmpty) {  // a new super-block: grow the bounding box
+                const int sx = bx >> kSuperShift, sy = by >> kSuperShift, sz = bz >> kSuperShift;
+                atomicMin(&g.ctr->sb_lo[0], sx);
+                atomicMin(&g.ctr->sb_lo[1], sy);
+                atomicMin(&g.ctr->sb_lo[2], sz);
+                atomicMax(&g.ctr->sb_hi[0], sx);
+                atomicMax(&g.ctr->sb_hi[1], sy);
+                atomicMax(&g.ctr->sb_hi[2], sz);
+                return;
+            }
+            if (old == key) return;
         }
         b = (b + 1) & g.sbmask;
     }

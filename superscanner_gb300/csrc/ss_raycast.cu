@@ -30,16 +30,19 @@ __device__ __forceinline__ VoxelRead read_voxel(const GridView &g, int bucket, i
     }
 }
 
+// getVBIndeces (GPUVoxelGrid.h:162-189): the index rule of each coordinate
+// (by multiplication where that is provably the IEEE quotient's result).
 __device__ __forceinline__ void block_of(const GridView &g, F3 p, int &bx, int &by, int &bz) {
-    bx = idx_rule(p.x, g.vbl);
-    by = idx_rule(p.y, g.vbl);
-    bz = idx_rule(p.z, g.vbl);
+    bx = idx_rule_fast(p.x, g.vbl, g.rvbl);
+    by = idx_rule_fast(p.y, g.vbl, g.rvbl);
+    bz = idx_rule_fast(p.z, g.vbl, g.rvbl);
 }
 
 // getVinVBIndeces (GPUVoxelGrid.h:192-221): p - vbl * vbInd, then the index rule.
 __device__ __forceinline__ int voxel_in_block(const GridView &g, F3 p, int bx, int by, int bz) {
     const F3 q = f3sub(p, F3{__fmul_rn(g.vbl, (float)bx), __fmul_rn(g.vbl, (float)by), __fmul_rn(g.vbl, (float)bz)});
-    const int vx = idx_rule(q.x, g.vl), vy = idx_rule(q.y, g.vl), vz = idx_rule(q.z, g.vl);
+    const int vx = idx_rule_fast(q.x, g.vl, g.rvl), vy = idx_rule_fast(q.y, g.vl, g.rvl),
+              vz = idx_rule_fast(q.z, g.vl, g.rvl);
     return vx + kEdge * vy + kEdge * kEdge * vz;
 }
 
@@ -52,10 +55,40 @@ __device__ __forceinline__ F3 voxel_mid(const GridView &g, int v, int bx, int by
             __fmaf_rn((float)vz + 0.5f, g.vl, __fmul_rn((float)bz, g.vbl))};
 }
 
-__device__ __forceinline__ int find_block(const GridView &g, int bx, int by, int bz, int &finds) {
+// Block finds of the reference raycast (UnorderedMap::find of the prime hash,
+// GPUVoxelGrid.cpp:590-630). When `skip` holds, a block whose super-block
+// holds no allocated block is known to be absent without a table probe: the
+// super-block is looked up once per super-block the ray enters. That is exact
+// only where no prime-hash collision can make another block answer the find
+// (see raycast_ref_kernel).
+struct SuperCache {
+    int sx = INT_MIN, sy = INT_MIN, sz = INT_MIN;
+    bool occ = false;
+};
+
+__device__ __forceinline__ int find_block(const GridView &g, int bx, int by, int bz, int &finds, bool skip,
+                                          SuperCache &sc) {
+    if (skip) {
+        const int sx = bx >> kSuperShift, sy = by >> kSuperShift, sz = bz >> kSuperShift;
+        if (sx != sc.sx || sy != sc.sy || sz != sc.sz) {
+            sc.sx = sx;
+            sc.sy = sy;
+            sc.sz = sz;
+            sc.occ = super_occupied(g, sx, sy, sz);
+            finds++;
+        }
+        if (!sc.occ) return -1;
+    }
     finds++;
     return table_find(g, prime_hash(bx, by, bz));
 }
+
+// The shortest difference between two block coordinates with the same prime
+// hash (73856093 dx + 19349669 dy + 83492791 dz = 0 mod 2^32, dx, dy, dz not
+// all zero) is 951 blocks along some axis (exhaustive search of |dx|, |dy| <=
+// 3000 for the dz that solves it): blocks within 950 of each other along
+// every axis never share a key.
+constexpr int kHashCollisionFree = 950;
 
 template <int kStorage>
 __global__ void __launch_bounds__(256) raycast_ref_kernel(GridView g, Mat34 Er, float *__restrict__ out_pcd,
@@ -72,20 +105,47 @@ __global__ void __launch_bounds__(256) raycast_ref_kernel(GridView g, Mat34 Er, 
     rv = f3sub(rv, f3smul(__fsub_rn(1.f, l), dir));
 
     bool done = false, Fn = false, Lp = false;
-    int guard = 0, finds = 0, voxels = 0;  // work counters: hash finds, voxel reads
+    int guard = 0, finds = 0, voxels = 0;  // work counters: hash and super-block finds, voxel reads
+
+    // Skip the table probe in empty super-blocks when this ray's blocks and
+    // every allocated block (within the super-blocks' bounding box) lie within
+    // the collision-free extent: then a find answers only for the block itself.
+    bool skip = false;
+    {
+        const int lo0 = __ldcg(&g.ctr->sb_lo[0]), lo1 = __ldcg(&g.ctr->sb_lo[1]), lo2 = __ldcg(&g.ctr->sb_lo[2]);
+        const int hi0 = __ldcg(&g.ctr->sb_hi[0]), hi1 = __ldcg(&g.ctr->sb_hi[1]), hi2 = __ldcg(&g.ctr->sb_hi[2]);
+        const float reach = dmax + 2.f * vbl;  // the march ends within d_max plus a step of the start
+        const float e[3] = {Er.m[3] + reach * dir.x, Er.m[7] + reach * dir.y, Er.m[11] + reach * dir.z};
+        const float c[3] = {Er.m[3], Er.m[7], Er.m[11]};
+        const int lo[3] = {lo0, lo1, lo2}, hi[3] = {hi0, hi1, hi2};
+        skip = true;
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            const float mn = fminf(c[a], e[a]), mx = fmaxf(c[a], e[a]);
+            if (!(fabsf(mn) < 1e6f && fabsf(mx) < 1e6f)) skip = false;
+            const long long rb_lo = (long long)floorf(mn / vbl) - 1, rb_hi = (long long)floorf(mx / vbl) + 1;
+            long long bl = rb_lo, bh = rb_hi;
+            if (lo[a] <= hi[a]) {  // allocated blocks lie in super-blocks lo..hi
+                bl = min(bl, (long long)lo[a] * 8);
+                bh = max(bh, (long long)hi[a] * 8 + 7);
+            }
+            if (bh - bl > kHashCollisionFree) skip = false;
+        }
+    }
+    SuperCache sc;
     F3 hit{0.f, 0.f, 0.f};
     float cr = 0.f, cg = 0.f, cb = 0.f;
 
     while (!done && !Fn && l < dmax) {
         int bx, by, bz;
         block_of(g, rv, bx, by, bz);
-        int bucket = find_block(g, bx, by, bz, finds);
+        int bucket = find_block(g, bx, by, bz, finds, skip, sc);
         int count = 0;
         while (bucket < 0 && l < dmax && guard < iter_cap) {
             rv = f3add(rv, f3smul(vbl, dir));
             l = __fadd_rn(l, vbl);
             block_of(g, rv, bx, by, bz);
-            bucket = find_block(g, bx, by, bz, finds);
+            bucket = find_block(g, bx, by, bz, finds, skip, sc);
             count++;
             guard++;
         }
@@ -95,12 +155,12 @@ __global__ void __launch_bounds__(256) raycast_ref_kernel(GridView g, Mat34 Er, 
             rv = f3sub(rv, f3smul(back, dir));
             l = __fsub_rn(l, back);
             block_of(g, rv, bx, by, bz);
-            bucket = find_block(g, bx, by, bz, finds);
+            bucket = find_block(g, bx, by, bz, finds, skip, sc);
             while (bucket < 0 && l < dmax && guard < iter_cap) {
                 rv = f3add(rv, f3smul(dtr, dir));
                 l = __fadd_rn(l, dtr);
                 block_of(g, rv, bx, by, bz);
-                bucket = find_block(g, bx, by, bz, finds);
+                bucket = find_block(g, bx, by, bz, finds, skip, sc);
                 guard++;
             }
         }
@@ -130,7 +190,7 @@ __global__ void __launch_bounds__(256) raycast_ref_kernel(GridView g, Mat34 Er, 
                     block_of(g, rv, qx, qy, qz);
                     const int vo = voxel_in_block(g, rv, qx, qy, qz);
                     const F3 vm_out = voxel_mid(g, vo, qx, qy, qz);
-                    const int ob = (qx == ox && qy == oy && qz == oz) ? cur : find_block(g, qx, qy, qz, finds);
+                    const int ob = (qx == ox && qy == oy && qz == oz) ? cur : find_block(g, qx, qy, qz, finds, skip, sc);
                     VoxelRead o{0.f, 0.f};
                     float orr = 0.f, og = 0.f, obb = 0.f;
                     if (ob >= 0) {  // missing block: reads as an empty voxel (reference: value_at(invalid))
