@@ -375,7 +375,7 @@ def run_refusion(torch, depth, P, stream, n_kf: int = 200, launch=None, modes=("
     return res
 
 
-def run_dropin(torch, depth_dev, P, W: int, K: int, stream, peak: float, host_pinned=None):
+def run_dropin(torch, depth_dev, P, W: int, K: int, stream, peak: float, host_pinned=None, buckets: int = BUCKETS):
     """The reference's call surface on the GPU: per frame ss_integrate (FP32,
     the reference's rounding, depth only), ss_raycast (nearest voxel, to 10 m)
     and ss_kokkos_icp (point-to-plane, frame k against k-1 at the ground-truth
@@ -390,7 +390,7 @@ def run_dropin(torch, depth_dev, P, W: int, K: int, stream, peak: float, host_pi
     npix = ROWS * COLS
 
     def grid():
-        g = GPUVoxelGrid(int(1e9), TRUNC, VL, ROWS, COLS, storage="f32", with_color=False, hash_buckets=BUCKETS)
+        g = GPUVoxelGrid(int(1e9), TRUNC, VL, ROWS, COLS, storage="f32", with_color=False, hash_buckets=buckets)
         g.setIntrinsic(*INTR)
         return g
 
@@ -781,7 +781,7 @@ def main_ours(args):
     if args.only == "dropin":
         if rank == 0:
             torch.cuda.nvtx.range_push("dropin")
-            res = run_dropin(torch, depth_dev, P, W, K, stream, peak)
+            res = run_dropin(torch, depth_dev, P, W, K, stream, peak, buckets=args.buckets)
             torch.cuda.nvtx.range_pop()
             print(json.dumps({"metric": "dropin_frames_per_s", "impl": "ours", "dropin": res}))
         return
