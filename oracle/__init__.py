@@ -60,7 +60,7 @@ for name, res, args in [
     ("orm_extract_mesh_cubes", C.c_longlong, [_p, C.c_longlong, _p]),
     ("orm_raycast_loss", C.c_double, [_p, _p, _p, C.c_double, C.c_double, _i, C.c_double, C.c_double, _p]),
     ("orm_raycast_loss_pixels", C.c_double, [_p, _p, _p, C.c_double, C.c_double, _i, C.c_double, C.c_double, _p,
-                                             _p]),
+                                             _p, _p]),
     ("orm_track", _i, [_p, _i, _i, _f, _f, _f, _f, _p, _p, _p, _p, _i, _p, _p, C.c_double, C.c_double]),
 ]:
     fn = getattr(_lib, name)
@@ -229,12 +229,14 @@ class MethodGrid64:
         return loss, int(valid[0])
 
     def raycast_loss_pixels(self, T, obs, lambda_n=1.0, r_max=0.05, max_steps=128, t_min=0.2, t_max=10.0):
-        """Per-pixel loss terms [rows, cols] (NaN where a pixel is not valid)."""
+        """(per-pixel loss terms, per-pixel hit depths t*), [rows, cols] each, NaN where a pixel is not valid."""
         out = np.zeros((self.resi, self.resj))
+        hit = np.zeros((self.resi, self.resj))
         obs = np.ascontiguousarray(obs, np.uint16)
         _lib.orm_raycast_loss_pixels(self._h, _ptr(np.ascontiguousarray(T, np.float64)), _ptr(obs), float(lambda_n),
-                                     float(r_max), int(max_steps), float(t_min), float(t_max), C.c_void_p(), _ptr(out))
-        return out
+                                     float(r_max), int(max_steps), float(t_min), float(t_max), C.c_void_p(), _ptr(out),
+                                     _ptr(hit))
+        return out, hit
 
     def raycast_loss_grad(self, T, obs, lambda_n=1.0, r_max=0.05, max_steps=128, t_min=0.2, t_max=10.0,
                           voxels=False):

@@ -466,22 +466,27 @@ int orm_grid_add_voxel(void *h, int x, int y, int z, int v, double delta) {
 // trilinear march from t_min, Newton steps to the root of the trilinear field,
 // L = sum of r^2 + lambda (r n.d)^2 over valid pixels (r = t* - d_obs).
 double orm_raycast_loss_pixels(void *h, const double *T, const uint16_t *obs, double lambda_n, double r_max,
-                               int max_steps, double t_min, double t_max, long long *valid_out, double *per_pixel);
+                               int max_steps, double t_min, double t_max, long long *valid_out, double *per_pixel,
+                               double *hit_depth);
 
 double orm_raycast_loss(void *h, const double *T, const uint16_t *obs, double lambda_n, double r_max,
                         int max_steps, double t_min, double t_max, long long *valid_out) {
-    return orm_raycast_loss_pixels(h, T, obs, lambda_n, r_max, max_steps, t_min, t_max, valid_out, nullptr);
+    return orm_raycast_loss_pixels(h, T, obs, lambda_n, r_max, max_steps, t_min, t_max, valid_out, nullptr,
+                                   nullptr);
 }
 
-// orm_raycast_loss with each pixel's term in per_pixel ([resi][resj], NaN where
-// the pixel is not valid) when per_pixel is given.
+// orm_raycast_loss with each pixel's term in per_pixel and its hit depth t* in
+// hit_depth ([resi][resj] each, NaN where the pixel is not valid), each when given.
 double orm_raycast_loss_pixels(void *h, const double *T, const uint16_t *obs, double lambda_n, double r_max,
-                               int max_steps, double t_min, double t_max, long long *valid_out, double *per_pixel) {
+                               int max_steps, double t_min, double t_max, long long *valid_out, double *per_pixel,
+                               double *hit_depth) {
     const Grid64 &g = *(Grid64 *)h;
     double total = 0;
     long long valid = 0;
-    if (per_pixel)
-        for (size_t q = 0; q < (size_t)g.resi * g.resj; q++) per_pixel[q] = std::nan("");
+    for (size_t q = 0; q < (size_t)g.resi * g.resj; q++) {
+        if (per_pixel) per_pixel[q] = std::nan("");
+        if (hit_depth) hit_depth[q] = std::nan("");
+    }
 #pragma omp parallel for schedule(dynamic, 2) reduction(+ : total, valid)
     for (int i = 0; i < g.resi; i++) {
         Cache cache;
@@ -527,6 +532,7 @@ double orm_raycast_loss_pixels(void *h, const double *T, const uint16_t *obs, do
             const double term = r * r + lambda_n * (r * c) * (r * c);
             total += term;
             if (per_pixel) per_pixel[(size_t)i * g.resj + j] = term;
+            if (hit_depth) hit_depth[(size_t)i * g.resj + j] = t;
             valid++;
         }
     }

@@ -287,32 +287,49 @@ __global__ void __launch_bounds__(256) icp_ref_iter_kernel(const float *__restri
     if (search) {
         float smallest = max_dist;
         int best = -1;
-        for (int k = ci - n_search; k < ci + n_search; k++) {
-            for (int l = cj - n_search; l < cj + n_search; l++) {
-                F3 py, nn;
-                int tag;
-                if (staged) {
-                    tag = (k - r0) * W + (l - q0);
-                    const float4 a = sA[tag];
-                    py = F3{a.x, a.y, a.z};
-                    if (kType == SS_ICP_POINT_TO_PLANE) {
-                        const float2 b = sB[tag];
-                        nn = F3{a.w, b.x, b.y};
+        if (staged) {
+            // rows of the window in scan order (k outer, l inner); a row's ten
+            // taps are loaded before its comparisons
+            const int base = (ci - n_search - r0) * W + (cj - n_search - q0);
+#pragma unroll 1
+            for (int dk = 0; dk < 2 * n_search; dk++) {
+                const int row = base + dk * W;
+                float4 a[2 * n_search];
+                float2 b[2 * n_search];
+#pragma unroll
+                for (int dl = 0; dl < 2 * n_search; dl++) {
+                    a[dl] = sA[row + dl];
+                    if (kType == SS_ICP_POINT_TO_PLANE) b[dl] = sB[row + dl];
+                }
+#pragma unroll
+                for (int dl = 0; dl < 2 * n_search; dl++) {
+                    const F3 py{a[dl].x, a[dl].y, a[dl].z};
+                    const float dist = kType == SS_ICP_POINT_TO_POINT
+                                           ? f3len(f3sub(py, px))
+                                           : fabsf(f3dot(f3sub(py, px), F3{a[dl].w, b[dl].x, b[dl].y}));
+                    if (dist < smallest) {
+                        smallest = dist;
+                        best = row + dl;
                     }
-                } else {
-                    tag = k * cols + l;
-                    py = ld3(yp, (size_t)tag);
+                }
+            }
+        } else {
+            for (int k = ci - n_search; k < ci + n_search; k++) {
+                for (int l = cj - n_search; l < cj + n_search; l++) {
+                    const int tag = k * cols + l;
+                    F3 py = ld3(yp, (size_t)tag), nn{0.f, 0.f, 0.f};
                     bool ok = py.z != 0;
                     if (kType == SS_ICP_POINT_TO_PLANE) {
                         nn = ld3(yn, (size_t)tag);
                         ok = ok && nn.x != 0;
                     }
                     if (!ok) py.x = __int_as_float(0x7fc00000);
-                }
-                const float dist = kType == SS_ICP_POINT_TO_POINT ? f3len(f3sub(py, px)) : fabsf(f3dot(f3sub(py, px), nn));
-                if (dist < smallest) {
-                    smallest = dist;
-                    best = tag;
+                    const float dist = kType == SS_ICP_POINT_TO_POINT ? f3len(f3sub(py, px))
+                                                                      : fabsf(f3dot(f3sub(py, px), nn));
+                    if (dist < smallest) {
+                        smallest = dist;
+                        best = tag;
+                    }
                 }
             }
         }

@@ -130,7 +130,8 @@ class GPUVoxelGrid:
         check(lib.ss_clean_memory(self._h, _stream_ptr(stream)), "cleanMemory")
 
     # -- additions of the C-ABI
-    LAUNCH_FIELDS = ("collect_rows", "raycast_rows", "fuse_ctas_per_sm", "refuse_ctas_per_sm", "track_ctas_per_sm")
+    LAUNCH_FIELDS = ("collect_rows", "raycast_rows", "fuse_ctas_per_sm", "refuse_ctas_per_sm", "track_ctas_per_sm",
+                     "raycast_rays")
 
     def launch_config(self) -> dict:
         c = SSLaunchConfig()

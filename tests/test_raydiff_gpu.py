@@ -126,33 +126,46 @@ def test_adjoint_matches_fp64_finite_differences(storage, tol):
 def test_pose_adjoint_matches_fp64_differences_with_frozen_pixels():
     """Config 5's check on the fused FP16 room: FP64 central differences
     (h = 1e-4 on the pose twist) of the loss over a frozen pixel set against
-    the GPU adjoint over the same pixels (ss_raycast_loss_grad_masked). The set
-    keeps the pixels that are valid at the pose and at all twelve perturbed
-    poses and whose loss term changes smoothly there (second difference below
-    1 % of the first), so no pixel enters or leaves the loss between the
-    evaluations and no ray's hit jumps to another surface."""
+    the GPU adjoint over the same pixels (ss_raycast_loss_grad_masked). The
+    per-pixel loss is smooth only while its hit stays in one trilinear cell
+    (the field's gradient, and so the normal term, changes across cell faces),
+    so the set keeps the pixels that are valid at the pose and at all twelve
+    perturbed poses, whose hit stays in the same cell in all of them, and whose
+    second difference is small (no jump to another crossing)."""
     from superscanner_gb300.raydiff import raycast_loss_grad_masked
     g, o, d, P, depth, dev = setup("f16")
     T = se3_exp([0.004, -0.003, 0.002, 0.006, -0.004, 0.003]) @ P[7]
     h = 1e-4
-    base = o.raycast_loss_pixels(T, depth[7])
+    vl = float(np.float32(VL))
+    jj, ii = np.meshgrid(np.arange(640), np.arange(480))
+
+    def cells(Tm, t):
+        dcx, dcy = (jj - INTR[2]) / INTR[0], (ii - (480 - INTR[3])) / INTR[1]
+        dd = np.stack([Tm[r, 0] * dcx + Tm[r, 1] * dcy + Tm[r, 2] for r in range(3)], -1)
+        with np.errstate(invalid="ignore"):
+            return np.floor((Tm[:3, 3] + t[..., None] * dd) / vl - 0.5)
+
+    base, t0 = o.raycast_loss_pixels(T, depth[7])
+    frozen = np.isfinite(base)
+    c0 = cells(T, t0)
     plus, minus = [], []
     for i in range(6):
-        e = np.zeros(6)
-        e[i] = h
-        plus.append(o.raycast_loss_pixels(se3_exp(e) @ T, depth[7]))
-        minus.append(o.raycast_loss_pixels(se3_exp(-e) @ T, depth[7]))
+        for sgn, out in ((1.0, plus), (-1.0, minus)):
+            e = np.zeros(6)
+            e[i] = sgn * h
+            Te = se3_exp(e) @ T
+            L, t = o.raycast_loss_pixels(Te, depth[7])
+            frozen &= np.isfinite(L) & (cells(Te, t) == c0).all(-1)
+            out.append(L)
     Lp, Lm = np.stack(plus), np.stack(minus)
     with np.errstate(invalid="ignore"):
-        ok = np.isfinite(base) & np.isfinite(Lp).all(0) & np.isfinite(Lm).all(0)
-        smooth = ok & (np.abs(Lp + Lm - 2 * base) <= 0.01 * np.abs(Lp - Lm) + 1e-15).all(0)
-    frozen = smooth.astype(np.uint8)
+        frozen &= (np.abs(Lp + Lm - 2 * base) <= 2e-6).all(0)
     assert frozen.sum() > 0.5 * np.isfinite(base).sum()
-    fd = np.where(smooth, Lp - Lm, 0.0).sum(axis=(1, 2)) / (2 * h)
-    L, grad, nv = raycast_loss_grad_masked(g, T, dev[7], torch.from_numpy(frozen).cuda())
+    fd = np.where(frozen, Lp - Lm, 0.0).sum(axis=(1, 2)) / (2 * h)
+    L, grad, nv = raycast_loss_grad_masked(g, T, dev[7], torch.from_numpy(frozen.astype(np.uint8)).cuda())
     print("frozen pixels", int(frozen.sum()), "gpu valid among them", nv)
     print("pose grad gpu", grad, "\n      fp64 fd", fd)
-    assert nv >= 0.999 * frozen.sum()
+    assert nv >= 0.995 * frozen.sum()
     assert np.abs(grad - fd).max() <= 0.02 * np.abs(fd).max()
 
 
