@@ -48,45 +48,32 @@ Mat34 mat34_from(const float E[16]) {
     return m;
 }
 
-// Inverse of a 4x4 float matrix by cofactors in double, rounded to float
-// (GPUVoxelGrid.cpp:55 inverts with Eigen in float; Eigen is not available).
+// Inverse of a 4x4 float matrix, row-major: the adjugate over the
+// determinant, each cofactor a 3x3 minor expanded along its first row, all in
+// double, rounded to float once (GPUVoxelGrid.cpp:55 inverts with Eigen in
+// float; Eigen is not available).
+static double det3_rowmajor(const double a[9]) {
+    return a[0] * (a[4] * a[8] - a[5] * a[7]) - a[1] * (a[3] * a[8] - a[5] * a[6]) +
+           a[2] * (a[3] * a[7] - a[4] * a[6]);
+}
+
 void inverse4_rounded(const float Ef[16], float out[16]) {
-    double m[16], inv[16];
+    double m[16], cof[16];
     for (int k = 0; k < 16; k++) m[k] = Ef[k];
-    inv[0] = m[5] * m[10] * m[15] - m[5] * m[11] * m[14] - m[9] * m[6] * m[15] + m[9] * m[7] * m[14] +
-             m[13] * m[6] * m[11] - m[13] * m[7] * m[10];
-    inv[4] = -m[4] * m[10] * m[15] + m[4] * m[11] * m[14] + m[8] * m[6] * m[15] - m[8] * m[7] * m[14] -
-             m[12] * m[6] * m[11] + m[12] * m[7] * m[10];
-    inv[8] = m[4] * m[9] * m[15] - m[4] * m[11] * m[13] - m[8] * m[5] * m[15] + m[8] * m[7] * m[13] +
-             m[12] * m[5] * m[11] - m[12] * m[7] * m[9];
-    inv[12] = -m[4] * m[9] * m[14] + m[4] * m[10] * m[13] + m[8] * m[5] * m[14] - m[8] * m[6] * m[13] -
-              m[12] * m[5] * m[10] + m[12] * m[6] * m[9];
-    inv[1] = -m[1] * m[10] * m[15] + m[1] * m[11] * m[14] + m[9] * m[2] * m[15] - m[9] * m[3] * m[14] -
-             m[13] * m[2] * m[11] + m[13] * m[3] * m[10];
-    inv[5] = m[0] * m[10] * m[15] - m[0] * m[11] * m[14] - m[8] * m[2] * m[15] + m[8] * m[3] * m[14] +
-             m[12] * m[2] * m[11] - m[12] * m[3] * m[10];
-    inv[9] = -m[0] * m[9] * m[15] + m[0] * m[11] * m[13] + m[8] * m[1] * m[15] - m[8] * m[3] * m[13] -
-             m[12] * m[1] * m[11] + m[12] * m[3] * m[9];
-    inv[13] = m[0] * m[9] * m[14] - m[0] * m[10] * m[13] - m[8] * m[1] * m[14] + m[8] * m[2] * m[13] +
-              m[12] * m[1] * m[10] - m[12] * m[2] * m[9];
-    inv[2] = m[1] * m[6] * m[15] - m[1] * m[7] * m[14] - m[5] * m[2] * m[15] + m[5] * m[3] * m[14] +
-             m[13] * m[2] * m[7] - m[13] * m[3] * m[6];
-    inv[6] = -m[0] * m[6] * m[15] + m[0] * m[7] * m[14] + m[4] * m[2] * m[15] - m[4] * m[3] * m[14] -
-             m[12] * m[2] * m[7] + m[12] * m[3] * m[6];
-    inv[10] = m[0] * m[5] * m[15] - m[0] * m[7] * m[13] - m[4] * m[1] * m[15] + m[4] * m[3] * m[13] +
-              m[12] * m[1] * m[7] - m[12] * m[3] * m[5];
-    inv[14] = -m[0] * m[5] * m[14] + m[0] * m[6] * m[13] + m[4] * m[1] * m[14] - m[4] * m[2] * m[13] -
-              m[12] * m[1] * m[6] + m[12] * m[2] * m[5];
-    inv[3] = -m[1] * m[6] * m[11] + m[1] * m[7] * m[10] + m[5] * m[2] * m[11] - m[5] * m[3] * m[10] -
-             m[9] * m[2] * m[7] + m[9] * m[3] * m[6];
-    inv[7] = m[0] * m[6] * m[11] - m[0] * m[7] * m[10] - m[4] * m[2] * m[11] + m[4] * m[3] * m[10] +
-             m[8] * m[2] * m[7] - m[8] * m[3] * m[6];
-    inv[11] = -m[0] * m[5] * m[11] + m[0] * m[7] * m[9] + m[4] * m[1] * m[11] - m[4] * m[3] * m[9] -
-              m[8] * m[1] * m[7] + m[8] * m[3] * m[5];
-    inv[15] = m[0] * m[5] * m[10] - m[0] * m[6] * m[9] - m[4] * m[1] * m[10] + m[4] * m[2] * m[9] +
-              m[8] * m[1] * m[6] - m[8] * m[2] * m[5];
-    double det = m[0] * inv[0] + m[1] * inv[4] + m[2] * inv[8] + m[3] * inv[12];
-    for (int k = 0; k < 16; k++) out[k] = (float)(inv[k] / det);
+    for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 4; j++) {
+            double sub[9];
+            int n = 0;
+            for (int r = 0; r < 4; r++)
+                if (r != i)
+                    for (int c = 0; c < 4; c++)
+                        if (c != j) sub[n++] = m[4 * r + c];
+            const double d = det3_rowmajor(sub);
+            cof[4 * i + j] = ((i + j) & 1) ? -d : d;
+        }
+    const double det = m[0] * cof[0] + m[1] * cof[1] + m[2] * cof[2] + m[3] * cof[3];
+    for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 4; j++) out[4 * j + i] = (float)(cof[4 * i + j] / det);
 }
 
 int persistent_ctas(const ss_grid *g, int per_sm) { return g->num_sms * per_sm; }
@@ -435,7 +422,7 @@ ss_status launch_fuse(ss_grid *g, const uint16_t *depth, const uint8_t *rgb, con
     const int cr = g->lc.collect_rows;
     const dim3 cblk(32, cr), cgrid((g->p.resj + 31) / 32, (g->p.resi + cr - 1) / cr);
     // shared set of packed coordinates + the list of its distinct entries
-    const size_t csmem = tile_set_bytes(cr);  // <= 8 KB
+    const size_t csmem = tile_set_bytes(cr);  // <= 12 KB (8 rows)
     SS_CUDA_TRY(launch_kernel(collect_kernel, cgrid, cblk, csmem, s, g->pdl, g->v, depth, E, dpose));
     if (after_collect) SS_CUDA_TRY(cudaEventRecord(after_collect, s));
     const int ctas = persistent_ctas(g, g->lc.fuse_ctas_per_sm);

@@ -3,8 +3,10 @@
 //   -> integrate at the tracked pose -> raycast the model view at that pose.
 //
 // All state (pose, model maps, hash table) stays in device memory; a frame
-// needs no host synchronisation. With use_graph the whole frame (about 25
-// kernels) is captured once as a CUDA graph and replayed per frame.
+// needs no host synchronisation. With use_graph a tracked frame (4 kernels:
+// the persistent tracker, then collect, fuse and raycast as programmatic
+// dependent launches) is captured once per input buffer as a CUDA graph and
+// replayed; a change of the grid's launch shapes re-captures it.
 // The reference has no such pipeline object: its integration thread
 // (src/core/integrate.cpp:47-209) calls GPUVoxelGrid::integrate with poses
 // from the keypoint tracker, and raycast is called by the GUI loop
