@@ -23,12 +23,11 @@ CANDIDATES = {
     "fuse_ctas_per_sm": (4, 8, 16),
     "track_ctas_per_sm": (1, 2),
     "refuse_ctas_per_sm": (4, 8, 16),
-    "raycast_rays": (1, 2),
 }
 STAGE = {"raycast_rows": "raycast", "collect_rows": "collect", "fuse_ctas_per_sm": "fuse",
-         "track_ctas_per_sm": "track", "raycast_rays": "raycast"}
+         "track_ctas_per_sm": "track"}
 DEFAULT = {"collect_rows": 8, "raycast_rows": 8, "fuse_ctas_per_sm": 8, "refuse_ctas_per_sm": 8,
-           "track_ctas_per_sm": 2, "raycast_rays": 1}
+           "track_ctas_per_sm": 2}
 
 
 def _cache_key(rows: int, cols: int, storage: str) -> str:

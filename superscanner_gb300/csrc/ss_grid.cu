@@ -492,7 +492,7 @@ ss_status ss_grid_set_launch_config(ss_grid *g, const ss_launch_config *c) {
     if (c->collect_rows < 1 || c->collect_rows > 8 || c->raycast_rows < 1 || c->raycast_rows > 8 ||
         c->fuse_ctas_per_sm < 1 || c->fuse_ctas_per_sm > 32 || c->refuse_ctas_per_sm < 1 ||
         c->refuse_ctas_per_sm > 32 || c->track_ctas_per_sm < 1 || c->track_ctas_per_sm > 2 ||
-        c->raycast_rays < 1 || c->raycast_rays > 2 || c->ref_raycast_rays < 1 || c->ref_raycast_rays > 2)
+        c->ref_raycast_rays < 1 || c->ref_raycast_rays > 2)
         return SS_ERR_ARG;
     g->lc = *c;
     g->launch_gen++;

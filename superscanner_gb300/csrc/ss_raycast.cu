@@ -628,109 +628,10 @@ __global__ void __launch_bounds__(256, 4) raycast_maps_kernel(GridView g, Mat34 
     }
 }
 
-// The same model view with kRays rays per thread (rows i0, i0 + rows per
-// tile, ...), each thread walking its rays through the ray_step state
-// machine: a lane whose ray ends early starts its next ray while the others
-// finish theirs, and all lanes keep sampling through one trilinear call site,
-// so a warp takes about the mean of its rays' step counts per ray instead of
-// their maximum. The outputs are those of raycast_maps_kernel bit for bit.
-template <int kStorage, int kRays>
-__global__ void __launch_bounds__(256, 3) raycast_maps_multi_kernel(GridView g, Mat34 T,
-                                                                 const FramePose *__restrict__ pose, int max_steps,
-                                                                 float t_min, float t_max, float4 *__restrict__ vmap,
-                                                                 float4 *__restrict__ nmap,
-                                                                 unsigned long long *__restrict__ counters,
-                                                                 const uint16_t *__restrict__ hint, float hint_margin,
-                                                                 Counters *end) {
-    const int j = blockIdx.x * 32 + threadIdx.x;
-    const int i0 = blockIdx.y * (blockDim.y * kRays) + threadIdx.y;
-    const unsigned full = 0xffffffffu;
-    const int lane = threadIdx.x & 31;
-    unsigned hint_mm[kRays];
-#pragma unroll
-    for (int q = 0; q < kRays; q++) {  // per ray as raycast_maps_kernel (warp-collective)
-        const int i = i0 + q * (int)blockDim.y;
-        hint_mm[q] = 0u;
-        if (hint) {
-            const bool inside = i < g.resi && j < g.resj;
-            const unsigned own = inside ? (unsigned)__ldg(hint + (size_t)i * g.resj + j) : 0u;
-            const unsigned have = __ballot_sync(full, own != 0u);
-            const unsigned left = have & ((1u << lane) - 1u), right = lane < 31 ? have & (full << (lane + 1)) : 0u;
-            const int li = left ? 31 - __clz(left) : lane, ri = right ? __ffs(right) - 1 : lane;
-            const unsigned dl = __shfl_sync(full, own, li), dr = __shfl_sync(full, own, ri);
-            hint_mm[q] = own ? own : (left && right ? min(dl, dr) : (left ? dl : (right ? dr : 0u)));
-        }
-    }
-    pdl_wait();
-    if (end && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0 && threadIdx.y == 0) end_call(end);
-    if (pose) {
-#pragma unroll
-        for (int k = 0; k < 12; k++) T.m[k] = __ldg(&pose->E.m[k]);
-    }
-    BlockCache cache{INT_MIN, INT_MIN, INT_MIN, -1, 0u, 0u};
-    unsigned steps = 0, hits = 0;
-    RayState r;
-    int q = 0;
-    // starts ray q if its pixel is inside the image
-    auto start = [&](int qq) -> bool {
-        const int i = i0 + qq * (int)blockDim.y;
-        if (!(i < g.resi && j < g.resj)) return false;
-        const float dcx = ((float)j - g.in.cj) / g.in.fx, dcy = ((float)i - g.in.ci) / g.in.fy;
-        const float dx = fmaf(T.m[0], dcx, fmaf(T.m[1], dcy, T.m[2]));
-        const float dy = fmaf(T.m[4], dcx, fmaf(T.m[5], dcy, T.m[6]));
-        const float dz = fmaf(T.m[8], dcx, fmaf(T.m[9], dcy, T.m[10]));
-        const float inv_len = rsqrtf(fmaf(dx, dx, fmaf(dy, dy, dz * dz)));
-        unsigned hm = hint_mm[0];
-#pragma unroll
-        for (int u = 1; u < kRays; u++)
-            if (qq == u) hm = hint_mm[u];
-        const float t_hint = (float)hm * 1e-3f - hint_margin;
-        if (hint && t_hint > t_min)
-            ray_begin(r, T.m[3], T.m[7], T.m[11], dx, dy, dz, inv_len, kRaySeek, t_hint + hint_margin, t_hint,
-                      fminf(t_max, t_hint + 2.f * hint_margin));
-        else
-            ray_begin(r, T.m[3], T.m[7], T.m[11], dx, dy, dz, inv_len, kRayForward, t_min, t_min, t_max);
-        return true;
-    };
-    while (q < kRays && !start(q)) q++;
-    while (q < kRays) {
-        ray_step<kStorage>(g, r, max_steps, cache);
-        if (r.mode == kRayDone) {
-            const size_t pix = (size_t)(i0 + q * (int)blockDim.y) * g.resj + j;
-            vmap[pix] = r.v;
-            nmap[pix] = r.n;
-            steps += (unsigned)r.steps;
-            hits += r.hit ? 1u : 0u;
-            q++;
-            while (q < kRays && !start(q)) q++;
-        }
-    }
-    if (counters) {  // algorithmic-traffic counters (profiling only), one atomic per warp and field
-        const unsigned l = __reduce_add_sync(full, cache.lookups), vx = __reduce_add_sync(full, cache.voxels);
-        const unsigned st = __reduce_add_sync(full, steps), h = __reduce_add_sync(full, hits);
-        if (lane == 0) {
-            atomicAdd(counters + 0, (unsigned long long)l);
-            atomicAdd(counters + 1, (unsigned long long)vx);
-            atomicAdd(counters + 2, (unsigned long long)st);
-            atomicAdd(counters + 3, (unsigned long long)h);
-        }
-    }
-}
-
 ss_status launch_raycast_maps(ss_grid *g, const Mat34 &T, const FramePose *dpose, int max_steps, float t_min,
                               float t_max, float4 *vmap, float4 *nmap, cudaStream_t s, unsigned long long *counters,
                               const uint16_t *hint, float hint_margin, Counters *end) {
     const int rr = g->lc.raycast_rows;
-    if (g->lc.raycast_rays == 2) {
-        const dim3 blk(32, rr), grid((g->p.resj + 31) / 32, (g->p.resi + 2 * rr - 1) / (2 * rr));
-        if (g->p.storage == SS_STORAGE_F32)
-            SS_CUDA_TRY(launch_kernel(raycast_maps_multi_kernel<SS_STORAGE_F32, 2>, grid, blk, 0, s, g->pdl, g->v, T,
-                                      dpose, max_steps, t_min, t_max, vmap, nmap, counters, hint, hint_margin, end));
-        else
-            SS_CUDA_TRY(launch_kernel(raycast_maps_multi_kernel<SS_STORAGE_F16, 2>, grid, blk, 0, s, g->pdl, g->v, T,
-                                      dpose, max_steps, t_min, t_max, vmap, nmap, counters, hint, hint_margin, end));
-        return SS_OK;
-    }
     const dim3 blk(32, rr), grid((g->p.resj + 31) / 32, (g->p.resi + rr - 1) / rr);
     if (g->p.storage == SS_STORAGE_F32)
         SS_CUDA_TRY(launch_kernel(raycast_maps_kernel<SS_STORAGE_F32>, grid, blk, 0, s, g->pdl, g->v, T, dpose, max_steps,

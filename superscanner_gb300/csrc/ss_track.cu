@@ -107,31 +107,19 @@ __global__ void pose_prep_kernel(TrackState *st) {
 // a group adds at most kTrackGroup - 1 roundings).
 constexpr int kTrackGroup = 4;
 
-// Pixel m of this thread at a level (m = 0, 1, ...): warp w of CTA c takes the
-// 32-pixel chunks w * gridDim.x + c + m * (nthreads / 32), so the warps of one
-// CTA sample the whole image instead of one band of it, which evens out the
-// CTAs' share of valid pixels (and so their arrival at the cross-CTA sums).
-// Covers every pixel once per nthreads-pixel slab; a warp's loads stay
-// contiguous. Needs blockDim.x == 256.
-__device__ __forceinline__ int track_pixel(int m, int nthreads) {
-    const int chunk = (threadIdx.x >> 5) * (int)gridDim.x + (int)blockIdx.x + m * (nthreads >> 5);
-    return chunk * 32 + (threadIdx.x & 31);
-}
-
 __device__ __forceinline__ void track_accumulate(const uint16_t *__restrict__ depth, int rows, int cols, Intr in,
                                                  const float4 *__restrict__ vmap, const float4 *__restrict__ nmap,
                                                  const float *T, const float *Pi, int level, float dist2, float rmin,
                                                  float dmax, int tid, int nthreads, float *s, float *c) {
     const int lr = (rows + (1 << level) - 1) >> level, lc = (cols + (1 << level) - 1) >> level;
     const int npix = lr * lc;
-    const int m_count = (npix + nthreads - 1) / nthreads;
     const float rfx = 1.f / in.fx, rfy = 1.f / in.fy;
-    for (int m0 = 0; m0 < m_count; m0 += kTrackGroup) {
+    for (int base = tid; base < npix; base += kTrackGroup * nthreads) {
         float d[kTrackGroup];
         int pi[kTrackGroup], pj[kTrackGroup];
 #pragma unroll
         for (int g = 0; g < kTrackGroup; g++) {
-            const int p = track_pixel(m0 + g, nthreads);
+            const int p = base + g * nthreads;
             pi[g] = (p / lc) << level;
             pj[g] = (p % lc) << level;
             d[g] = p < npix ? (float)__ldg(depth + (size_t)pi[g] * cols + pj[g]) * 1e-3f : 0.f;
@@ -213,7 +201,7 @@ __device__ __forceinline__ void track_fill_cam(const uint16_t *__restrict__ dept
 #pragma unroll
     for (int m = 0; m < kCamCache; m++) {
         if (m >= m_count) break;
-        const int p = track_pixel(m, nthreads);
+        const int p = tid + m * nthreads;
         float4 cp = make_float4(0.f, 0.f, 0.f, 0.f);
         if (p < npix) {
             const int i = (p / lc) << level, j = (p % lc) << level;

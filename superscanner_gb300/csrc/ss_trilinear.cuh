@@ -268,175 +268,6 @@ __device__ __forceinline__ bool ray_search(const GridView &g, float ox, float oy
     return found;
 }
 
-// ray_search, refine_crossing and the final sample with the gradient as one
-// resumable state machine: each call of ray_step takes one sample (or one
-// empty-space skip, or one bookkeeping transition), so that lanes of a warp
-// working on different rays, or on different phases of their rays, still run
-// one instruction stream with one trilinear call site. Decisions, arithmetic
-// and their order are those of ray_search / refine_crossing, and the final
-// sample is the one raycast_maps_kernel takes at the hit (gradients are
-// computed at every sample; the value f does not depend on that).
-constexpr int kRayBack = 2, kRayRefine = 3, kRayFinal = 4, kRayDone = 5;
-
-struct RayState {
-    float ox, oy, oz, dx, dy, dz, inv_len;
-    float t, t_lo, t_hi;
-    float t_prev, f_prev, ta, fa, tb, fb;
-    int mode, steps, refine;
-    bool prev_valid;
-    int csx, csy, csz;
-    bool cocc;
-    // result (valid once mode == kRayDone)
-    bool hit;
-    float4 v, n;
-};
-
-__device__ __forceinline__ void ray_begin(RayState &r, float ox, float oy, float oz, float dx, float dy, float dz,
-                                          float inv_len, int mode, float t0, float t_lo, float t_hi) {
-    r.ox = ox, r.oy = oy, r.oz = oz, r.dx = dx, r.dy = dy, r.dz = dz, r.inv_len = inv_len;
-    r.t = t0, r.t_lo = t_lo, r.t_hi = t_hi;
-    r.t_prev = r.f_prev = r.ta = r.fa = r.tb = r.fb = 0.f;
-    r.mode = mode, r.steps = 0, r.refine = 0;
-    r.prev_valid = false;
-    r.csx = r.csy = r.csz = INT_MIN;
-    r.cocc = false;
-    r.hit = false;
-    r.v = r.n = make_float4(0.f, 0.f, 0.f, 0.f);
-}
-
-// The search has ended: a bracket goes to refinement, else the ray has no hit.
-__device__ __forceinline__ void ray_search_end(RayState &r, bool found) {
-    r.mode = found ? kRayRefine : kRayDone;
-}
-
-template <int kStorage>
-__device__ __forceinline__ void ray_step(const GridView &g, RayState &r, int max_steps, BlockCache &cache) {
-    const float vl = g.vl, inv_vl = 1.f / g.vl;
-    float ts = r.t;  // the sample's ray parameter
-    if (r.mode <= kRayBack) {  // search (ray_search's loop)
-        if (!(r.steps < max_steps) || (r.mode == kRayForward && !(r.t < r.t_hi))) {
-            ray_search_end(r, false);
-            return;
-        }
-        r.steps++;
-        if (r.mode == kRayForward) {
-            const float px = fmaf(r.t, r.dx, r.ox), py = fmaf(r.t, r.dy, r.oy), pz = fmaf(r.t, r.dz, r.oz);
-            const float inv_vbl = 1.f / g.vbl;
-            const int bx = (int)floorf(px * inv_vbl), by = (int)floorf(py * inv_vbl), bz = (int)floorf(pz * inv_vbl);
-            const int sx = bx >> kSuperShift, sy = by >> kSuperShift, sz = bz >> kSuperShift;
-            if (sx != r.csx || sy != r.csy || sz != r.csz) {
-                r.csx = sx;
-                r.csy = sy;
-                r.csz = sz;
-                r.cocc = super_occupied(g, sx, sy, sz);
-                cache.lookups++;
-            }
-            const bool empty_super = !r.cocc;
-            if (empty_super || cached_lookup(g, cache, bx, by, bz) < 0) {
-                const float sbl = g.vbl * (float)(1 << kSuperShift);
-                const float box = empty_super ? sbl : g.vbl;
-                const int cx = empty_super ? sx : bx, cy = empty_super ? sy : by, cz = empty_super ? sz : bz;
-                const float rdx = 1.f / r.dx, rdy = 1.f / r.dy, rdz = 1.f / r.dz;
-                const float ex = ((float)(cx + (r.dx > 0.f)) * box - r.ox) * rdx;
-                const float ey = ((float)(cy + (r.dy > 0.f)) * box - r.oy) * rdy;
-                const float ez = ((float)(cz + (r.dz > 0.f)) * box - r.oz) * rdz;
-                const float te = fminf(fminf(r.dx != 0.f ? ex : INFINITY, r.dy != 0.f ? ey : INFINITY),
-                                       r.dz != 0.f ? ez : INFINITY);
-                r.t = fmaxf(te, r.t) + 1e-4f * vl * r.inv_len;
-                r.prev_valid = false;
-                return;
-            }
-        }
-    } else if (r.mode == kRayRefine) {
-        ts = r.ta + (r.tb - r.ta) * r.fa / (r.fa - r.fb);
-    }
-    const TriSample sm =
-        trilinear<kStorage, true>(g, fmaf(ts, r.dx, r.ox), fmaf(ts, r.dy, r.oy), fmaf(ts, r.dz, r.oz), inv_vl, cache);
-    if (r.mode == kRayForward) {
-        if (!sm.valid) {
-            r.prev_valid = false;
-            r.t += vl * r.inv_len;
-            return;
-        }
-        if (sm.f < 0.f) {
-            const bool found = r.prev_valid && r.f_prev > 0.f;
-            r.ta = r.t_prev;
-            r.fa = r.f_prev;
-            r.tb = r.t;
-            r.fb = sm.f;
-            ray_search_end(r, found);
-            return;
-        }
-        r.prev_valid = true;
-        r.t_prev = r.t;
-        r.f_prev = sm.f;
-        r.t += fmaxf(vl, 0.8f * sm.f) * r.inv_len;
-    } else if (r.mode == kRaySeek) {
-        if (!sm.valid) {
-            ray_search_end(r, false);
-            return;
-        }
-        r.t_prev = r.t;
-        r.f_prev = sm.f;
-        if (sm.f >= 0.f) {
-            r.mode = kRayForward;
-            r.prev_valid = true;
-            const float inv_vbl = 1.f / g.vbl;
-            const float px = fmaf(r.t, r.dx, r.ox), py = fmaf(r.t, r.dy, r.oy), pz = fmaf(r.t, r.dz, r.oz);
-            r.csx = (int)floorf(px * inv_vbl) >> kSuperShift;
-            r.csy = (int)floorf(py * inv_vbl) >> kSuperShift;
-            r.csz = (int)floorf(pz * inv_vbl) >> kSuperShift;
-            r.cocc = true;
-            r.t += fmaxf(vl, 0.8f * sm.f) * r.inv_len;
-        } else {
-            r.mode = kRayBack;
-            r.t -= fmaxf(vl, -0.8f * sm.f) * r.inv_len;
-            if (r.t < r.t_lo) ray_search_end(r, false);
-        }
-    } else if (r.mode == kRayBack) {
-        if (sm.valid && sm.f > 0.f) {
-            r.ta = r.t;
-            r.fa = sm.f;
-            r.tb = r.t_prev;
-            r.fb = r.f_prev;
-            ray_search_end(r, true);
-            return;
-        }
-        if (!sm.valid) {
-            ray_search_end(r, false);
-            return;
-        }
-        r.t_prev = r.t;
-        r.f_prev = sm.f;
-        r.t -= fmaxf(vl, -0.8f * sm.f) * r.inv_len;
-        if (r.t < r.t_lo) ray_search_end(r, false);
-    } else if (r.mode == kRayRefine) {  // refine_crossing: two regula-falsi steps, then the secant root
-        bool last = !sm.valid;
-        if (sm.valid) {
-            if (sm.f > 0.f) {
-                r.ta = ts;
-                r.fa = sm.f;
-            } else {
-                r.tb = ts;
-                r.fb = sm.f;
-            }
-            last = ++r.refine == 2;
-        }
-        if (last) {
-            r.t = r.ta + (r.tb - r.ta) * r.fa / (r.fa - r.fb);
-            r.mode = kRayFinal;
-        }
-    } else {  // kRayFinal: the sample at the hit, with the gradient
-        const float gn = sm.valid ? sqrtf(sm.gx * sm.gx + sm.gy * sm.gy + sm.gz * sm.gz) : 0.f;
-        r.hit = true;
-        if (gn > 0.f) {
-            r.v = make_float4(fmaf(ts, r.dx, r.ox), fmaf(ts, r.dy, r.oy), fmaf(ts, r.dz, r.oz), ts);
-            r.n = make_float4(sm.gx / gn, sm.gy / gn, sm.gz / gn, 0.f);
-        }
-        r.mode = kRayDone;
-    }
-}
-
 // One forward ray march from t0 to t_max; returns true on a zero crossing (t = hit depth).
 template <int kStorage>
 __device__ __forceinline__ bool march(const GridView &g, float ox, float oy, float oz, float dx, float dy, float dz,

@@ -131,7 +131,7 @@ class GPUVoxelGrid:
 
     # -- additions of the C-ABI
     LAUNCH_FIELDS = ("collect_rows", "raycast_rows", "fuse_ctas_per_sm", "refuse_ctas_per_sm", "track_ctas_per_sm",
-                     "raycast_rays", "ref_raycast_rays")
+                     "ref_raycast_rays")
 
     def launch_config(self) -> dict:
         c = SSLaunchConfig()

@@ -9,7 +9,7 @@ from superscanner_gb300 import autotune as at
 
 GRID_KW = dict(c=int(1e9), trunc=0.016, voxlength=0.004, resi_=480, resj_=640, storage="f16")
 FASTEST = {"raycast_rows": 4, "collect_rows": 2, "fuse_ctas_per_sm": 16, "track_ctas_per_sm": 1,
-           "refuse_ctas_per_sm": 4, "raycast_rays": 2}
+           "refuse_ctas_per_sm": 4}
 
 
 def _fake(seen):
@@ -51,8 +51,7 @@ def test_coordinate_descent_picks_each_knobs_fastest_value(tmp_path):
             for later in order[q + 1:]:
                 assert cfg[later] == at.DEFAULT[later]
     assert set(timings) == set(order)
-    assert timings["raycast_rows"]["4"] == pytest.approx(
-        1.0 + abs(at.DEFAULT["raycast_rays"] - FASTEST["raycast_rays"]) + 0.5 * at.DEFAULT["collect_rows"])
+    assert timings["raycast_rows"]["4"] == pytest.approx(1.0 + 0.5 * at.DEFAULT["collect_rows"])
 
     # the cache holds the result under this GPU / size / storage key and is used next time
     stored = json.loads(cache.read_text())

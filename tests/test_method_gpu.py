@@ -59,29 +59,6 @@ def test_raycast_maps_vs_fp64(storage, margin):
     assert np.median(cos) > 0.9999
 
 
-@pytest.mark.parametrize("storage,margin", [("f16", 0.0), ("f16", 0.04), ("f32", 0.04)])
-def test_two_rays_per_thread_equal_one(storage, margin):
-    """raycast_rays = 2 (two rays per thread through the ray state machine)
-    renders the same maps bit for bit as one ray per thread, with and
-    without the depth hint, at two tile heights, with the same work counts."""
-    from superscanner_gb300.pipeline import Pipeline
-    P, depth = seq(6, 2)
-    g = GPUVoxelGrid(int(1e9), TRUNC, VL, 480, 640, storage=storage, with_color=False, hash_buckets=1 << 18,
-                     max_weight=255)
-    g.setIntrinsic(*INTR)
-    for k in range(6):
-        g.integrate_fast(dev(depth[k]), P[k].astype(np.float32))
-    hint = dev(depth[5]) if margin > 0 else None
-    out = []
-    for rays, rows in ((1, 8), (2, 8), (2, 3)):
-        g.set_launch_config(raycast_rays=rays, raycast_rows=rows)
-        v, n = raycast_maps(g, P[5].astype(np.float32), hint_depth=hint, hint_margin=margin)
-        g.sync()
-        out.append((v.cpu().numpy(), n.cpu().numpy()))
-    for v, n in out[1:]:
-        assert np.array_equal(v, out[0][0]) and np.array_equal(n, out[0][1])
-
-
 @pytest.mark.parametrize("storage", ["f32", "f16"])
 def test_fast_fusion_vs_fp64(storage):
     """The method's fusion (nearest pixel, running average in FP32) against
