@@ -84,7 +84,6 @@ typedef struct ss_launch_config {
     int32_t fuse_ctas_per_sm;   /* integrate / deintegrate, 1..32 (default 8) */
     int32_t refuse_ctas_per_sm; /* batched re-fusion apply, 1..32 (default 8) */
     int32_t track_ctas_per_sm;  /* persistent tracker, 1..2, capped by occupancy (default 2) */
-    int32_t ref_raycast_rays;   /* ss_raycast rays per thread, 1 or 2 (default 1) */
 } ss_launch_config;
 
 /* Fills the reference defaults of GPUVoxelGrid(c, trunc, voxlength, resi, resj)

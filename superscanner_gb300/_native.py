@@ -50,8 +50,7 @@ _D16 = C.POINTER(C.c_double)
 
 class SSLaunchConfig(C.Structure):
     _fields_ = [("collect_rows", C.c_int32), ("raycast_rows", C.c_int32), ("fuse_ctas_per_sm", C.c_int32),
-                ("refuse_ctas_per_sm", C.c_int32), ("track_ctas_per_sm", C.c_int32),
-                ("ref_raycast_rays", C.c_int32)]
+                ("refuse_ctas_per_sm", C.c_int32), ("track_ctas_per_sm", C.c_int32)]
 
 
 class SSPipelineParams(C.Structure):

@@ -13,7 +13,7 @@ struct ss_grid {
     ss::GridView v;
     bool intr_set = false;
     float fx = 0, fy = 0, cx = 0, cy = 0;
-    ss_launch_config lc{8, 8, 8, 8, 2, 1};  // launch shapes (autotuner)
+    ss_launch_config lc{8, 8, 8, 8, 2};  // launch shapes (autotuner)
     unsigned launch_gen = 0;               // bumped by every ss_grid_set_launch_config
     int raycast_cap = 0;                   // test hook: ss_raycast's iteration cap (0: the default)
     uint32_t host_epoch = 1;  // mirror of Counters::epoch for wrap handling

@@ -190,6 +190,52 @@ __device__ bool polar3_warp(const double *H, double *R) {
     return true;
 }
 
+// Float pairs (hi, lo) holding hi + lo: the per-pixel terms of kokkosICP's
+// double sums are exact in this form (x and y coordinates are floats; a
+// product of two floats is hi = RN(a b), lo = the exact rounding error), and
+// pairs add with an error-free TwoSum, so the CTA sums keep double-like
+// accuracy without FP64 instructions (one FP64 warp instruction occupies an
+// SM sub-partition's FP64 pipe for tens of cycles on this part).
+__device__ __forceinline__ void fp2_add(float &h, float &l, float h2, float l2) {
+    const float s = __fadd_rn(h, h2);
+    const float bb = __fsub_rn(s, h);
+    const float e = __fadd_rn(__fsub_rn(h, __fsub_rn(s, bb)), __fsub_rn(h2, bb));
+    const float t = __fadd_rn(__fadd_rn(l, l2), e);
+    h = __fadd_rn(s, t);
+    l = __fsub_rn(t, __fsub_rn(h, s));
+}
+
+// The CTA's 18 sums: each lane's pairs, a warp transpose-reduce (at offset o a
+// lane keeps the half of its values selected by lane bit o and adds the other
+// lane's; after offsets 16..1 lane v holds the warp's pair of value v), then
+// the warps' pairs in a fixed order; thread v < kIcpSums returns value v of
+// the CTA as a double (hi + lo, exact).
+__device__ __forceinline__ double icp_cta_sum(float *vh, float *vl, float2 (*red)[kIcpSums]) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) {
+        const bool upper = (lane & o) != 0;
+#pragma unroll
+        for (int k = 0; k < o; k++) {
+            const float sh = upper ? vh[k] : vh[k + o], sl = upper ? vl[k] : vl[k + o];
+            float kh = upper ? vh[k + o] : vh[k], kl = upper ? vl[k + o] : vl[k];
+            const float rh = __shfl_xor_sync(0xffffffffu, sh, o), rl = __shfl_xor_sync(0xffffffffu, sl, o);
+            fp2_add(kh, kl, rh, rl);
+            vh[k] = kh;
+            vl[k] = kl;
+        }
+    }
+    if (lane < kIcpSums) red[wid][lane] = make_float2(vh[0], vl[0]);
+    __syncthreads();
+    double out = 0.0;
+    if (threadIdx.x < kIcpSums) {
+        float h = 0.f, l = 0.f;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) fp2_add(h, l, red[w][threadIdx.x].x, red[w][threadIdx.x].y);
+        out = (double)h + (double)l;
+    }
+    return out;
+}
+
 // Target pixels staged per CTA: a tile's 10 x 10 windows (kokkosICP.cpp:81-83)
 // usually fall inside a region of some 42 x 18 pixels; up to this many are
 // staged, larger regions are read from global memory.
@@ -211,7 +257,7 @@ __global__ void __launch_bounds__(256) icp_ref_iter_kernel(const float *__restri
                                                            IcpState *st, double *partials) {
     __shared__ float4 sA[kIcpStage];  // target (x, y, z, nx)
     __shared__ float2 sB[kIcpStage];  // target (ny, nz)
-    __shared__ double red[8][kIcpSums];
+    __shared__ float2 red[8][kIcpSums];
     __shared__ int box[4];
     __shared__ bool last;
     const int n_search = 5;
@@ -280,10 +326,11 @@ __global__ void __launch_bounds__(256) icp_ref_iter_kernel(const float *__restri
     }
     __syncthreads();
 
-    double acc[kIcpSums];
+    // this pixel's terms as float pairs, padded to 32 for the transpose-reduce
+    float vh[32], vl[32];
 #pragma unroll
-    for (int k = 0; k < kIcpSums; k++) acc[k] = 0.0;
-    if (has_x) acc[17] = 1.0;  // n_pointsinX
+    for (int k = 0; k < 32; k++) vh[k] = vl[k] = 0.f;
+    if (has_x) vh[17] = 1.f;  // n_pointsinX
     if (search) {
         float smallest = max_dist;
         int best = -1;
@@ -346,38 +393,33 @@ __global__ void __launch_bounds__(256) icp_ref_iter_kernel(const float *__restri
             }
             const F3 bpt = kType == SS_ICP_POINT_TO_POINT ? py : f3add(px, f3smul(f3dot(f3sub(py, px), nn), nn));
             if (bpt.z != 0) {  // x_nearest(i, j).z != 0: a correspondence (kokkosICP.cpp:131)
-                const double Td[12] = {st->Txy_d[0], st->Txy_d[1], st->Txy_d[2],  st->Txy_d[3],
-                                       st->Txy_d[4], st->Txy_d[5], st->Txy_d[6],  st->Txy_d[7],
-                                       st->Txy_d[8], st->Txy_d[9], st->Txy_d[10], st->Txy_d[11]};
-                const double a0 = x.x, a1 = x.y, a2 = x.z, b0 = bpt.x, b1 = bpt.y, b2 = bpt.z;
-                acc[0] = 1.0;
-                acc[1] = a0; acc[2] = a1; acc[3] = a2;
-                acc[4] = b0; acc[5] = b1; acc[6] = b2;
-                acc[7] = a0 * b0;  acc[8] = a0 * b1;  acc[9] = a0 * b2;
-                acc[10] = a1 * b0; acc[11] = a1 * b1; acc[12] = a1 * b2;
-                acc[13] = a2 * b0; acc[14] = a2 * b1; acc[15] = a2 * b2;
-                // RMSE term: || x_nearest4 - Txy_eigen * x4 || in double, squared in float (kokkosICP.cpp:137-138)
-                const double e0 = b0 - (Td[0] * a0 + Td[1] * a1 + Td[2] * a2 + Td[3]);
-                const double e1 = b1 - (Td[4] * a0 + Td[5] * a1 + Td[6] * a2 + Td[7]);
-                const double e2 = b2 - (Td[8] * a0 + Td[9] * a1 + Td[10] * a2 + Td[11]);
-                const float tmp = (float)sqrt(e0 * e0 + e1 * e1 + e2 * e2);
-                acc[16] = (double)(tmp * tmp);
+                const float a[3] = {x.x, x.y, x.z}, b[3] = {bpt.x, bpt.y, bpt.z};
+                vh[0] = 1.f;
+#pragma unroll
+                for (int r = 0; r < 3; r++) {
+                    vh[1 + r] = a[r];
+                    vh[4 + r] = b[r];
+#pragma unroll
+                    for (int c = 0; c < 3; c++) {  // x y^T, exact as a pair
+                        const float p = __fmul_rn(a[r], b[c]);
+                        vh[7 + 3 * r + c] = p;
+                        vl[7 + 3 * r + c] = fmaf(a[r], b[c], -p);
+                    }
+                }
+                // RMSE term || x_nearest - Txy x || squared in float (kokkosICP.cpp:137-138; the
+                // reference evaluates the norm in double, this in FP32 with the float Txy)
+                const float e0 = b[0] - fmaf(T.m[0], a[0], fmaf(T.m[1], a[1], fmaf(T.m[2], a[2], T.m[3])));
+                const float e1 = b[1] - fmaf(T.m[4], a[0], fmaf(T.m[5], a[1], fmaf(T.m[6], a[2], T.m[7])));
+                const float e2 = b[2] - fmaf(T.m[8], a[0], fmaf(T.m[9], a[1], fmaf(T.m[10], a[2], T.m[11])));
+                const float tmp = sqrtf(fmaf(e0, e0, fmaf(e1, e1, e2 * e2)));
+                vh[16] = tmp * tmp;
             }
         }
     }
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const unsigned nctas = gridDim.x * gridDim.y, cta = blockIdx.y * gridDim.x + blockIdx.x;
-#pragma unroll
-    for (int k = 0; k < kIcpSums; k++) {
-        const double v = warp_sum(acc[k]);
-        if (lane == 0) red[wid][k] = v;
-    }
-    __syncthreads();
-    if (threadIdx.x < kIcpSums) {  // value-major slots: partials[value][cta]
-        double s = 0.0;
-        for (int w = 0; w < (int)(blockDim.x >> 5); w++) s += red[w][threadIdx.x];
-        partials[(size_t)threadIdx.x * nctas + cta] = s;
-    }
+    const double csum = icp_cta_sum(vh, vl, red);
+    if (threadIdx.x < kIcpSums) partials[(size_t)threadIdx.x * nctas + cta] = csum;  // value-major slots
     __threadfence();
     __syncthreads();
     if (threadIdx.x == 0) last = atomicAdd(&st->ticket, 1) == (int)nctas - 1;

@@ -57,12 +57,14 @@ __device__ __forceinline__ F3 voxel_mid(const GridView &g, int v, int bx, int by
 
 // Block finds of the reference raycast (UnorderedMap::find of the prime hash,
 // GPUVoxelGrid.cpp:590-630). When `skip` holds, a block whose super-block
-// holds no allocated block is known to be absent without a table probe: the
-// super-block is looked up once per super-block the ray enters. That is exact
-// only where no prime-hash collision can make another block answer the find
-// (see raycast_ref_kernel).
+// holds no allocated block, or whose bit in its super-block's mask is clear,
+// is known to be absent without a table probe: the super-block is looked up
+// once per super-block the ray enters. That is exact only where no
+// prime-hash collision can make another block answer the find (see
+// raycast_ref_kernel). Every find counts once in `finds`, probe or not.
 struct SuperCache {
     int sx = INT_MIN, sy = INT_MIN, sz = INT_MIN;
+    int slot = -1;  // the super-block's slot, -1: empty
     bool occ = false;
 };
 
@@ -74,13 +76,43 @@ __device__ __forceinline__ int find_block(const GridView &g, int bx, int by, int
             sc.sx = sx;
             sc.sy = sy;
             sc.sz = sz;
-            sc.occ = super_occupied(g, sx, sy, sz);
+            sc.slot = super_slot(g, sx, sy, sz);
+            sc.occ = sc.slot >= 0;
             finds++;
         }
         if (!sc.occ) return -1;
+        finds++;
+        // no block inserted at these coordinates: absent without a probe
+        if (!super_has_block(g, sc.slot, bx, by, bz)) return -1;
+        return table_find(g, prime_hash(bx, by, bz));
     }
     finds++;
     return table_find(g, prime_hash(bx, by, bz));
+}
+
+// Block-skip steps (rv <- rv + st, st = RN(vbl dir)) that certainly keep rv
+// in the ray's current super-block sc: on each axis the distance to the face
+// the ray moves towards, less a margin of 32 units of 2^-24 |rv| (the
+// roundings of up to 14 steps — a step advances at least vbl / sqrt(3) along
+// the ray's main axis, a super-block is 8 vbl wide — of the face and of the
+// index rule's quotient), over the step, minus one. Such steps move rv
+// monotonically on every axis and never cross that face, so each one's block
+// lies in sc: where sc is empty its find is -1 and no super-block lookup
+// happens, and the step reduces to its additions.
+__device__ __forceinline__ int empty_steps(const GridView &g, F3 rv, F3 st, const SuperCache &sc) {
+    const float vbl = g.vbl;
+    const float p[3] = {rv.x, rv.y, rv.z}, d[3] = {st.x, st.y, st.z};
+    const int sb[3] = {sc.sx, sc.sy, sc.sz};
+    float n = 1e30f;
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        if (d[a] == 0.f) continue;
+        const float face = (float)((sb[a] + (d[a] > 0.f ? 1 : 0)) * 8) * vbl;
+        const float margin = 0x1p-19f * (fabsf(p[a]) + 16.f * vbl);
+        const float room = fabsf(face - p[a]) - margin;
+        n = fminf(n, room / fabsf(d[a]));
+    }
+    return n >= 16.f ? 15 : (n > 1.f ? (int)n - 1 : 0);
 }
 
 // The shortest difference between two block coordinates with the same prime
@@ -141,8 +173,18 @@ __global__ void __launch_bounds__(256) raycast_ref_kernel(GridView g, Mat34 Er, 
         block_of(g, rv, bx, by, bz);
         int bucket = find_block(g, bx, by, bz, finds, skip, sc);
         int count = 0;
+        const F3 st = f3smul(vbl, dir);
         while (bucket < 0 && l < dmax && guard < iter_cap) {
-            rv = f3add(rv, f3smul(vbl, dir));
+            if (skip && !sc.occ) {  // through an empty super-block: the steps without their finds
+                for (int n = empty_steps(g, rv, st, sc); n > 0 && l < dmax && guard < iter_cap; n--) {
+                    rv = f3add(rv, st);
+                    l = __fadd_rn(l, vbl);
+                    count++;
+                    guard++;
+                }
+                if (!(l < dmax && guard < iter_cap)) break;
+            }
+            rv = f3add(rv, st);
             l = __fadd_rn(l, vbl);
             block_of(g, rv, bx, by, bz);
             bucket = find_block(g, bx, by, bz, finds, skip, sc);
@@ -247,222 +289,6 @@ __global__ void __launch_bounds__(256) raycast_ref_kernel(GridView g, Mat34 Er, 
         out_col[pix * 3 + 0] = done ? cr : 0.f;
         out_col[pix * 3 + 1] = done ? cg : 0.f;
         out_col[pix * 3 + 2] = done ? cb : 0.f;
-    }
-}
-
-
-// raycastingTag's march (the loops of raycast_ref_kernel) as a resumable
-// state machine: each call of ref_ray_step is one iteration of one of the
-// loops (block skip, truncation-stride re-advance, voxel march) or one of the
-// transitions between them, with the same conditions, arithmetic and guard
-// counting in the same order, so a thread can walk several rays and the lanes
-// of a warp keep stepping together while their rays are in different loops.
-enum : int { kRefOuter = 0, kRefSkip, kRefTrunc, kRefEnter, kRefVoxel, kRefEnd };
-
-struct RefRay {
-    F3 rv, dir;
-    float l;
-    int phase, guard, count;
-    bool done, Fn, Lp, skip;
-    int bx, by, bz, bucket;  // the block at rv and its find result
-    int cur, ox, oy, oz, v;  // the entered block and the voxel in it
-    F3 hit;
-    float cr, cg, cb;
-    SuperCache sc;
-};
-
-__device__ __forceinline__ void ref_ray_begin(const GridView &g, const Mat34 &Er, int i, int j, RefRay &r) {
-    const F3 np = f3normalized(get_point(g.in, i, j, 1.0f));
-    F3 rv = xform(Er, np);
-    r.dir = f3sub(rv, F3{Er.m[3], Er.m[7], Er.m[11]});
-    r.l = 0.1f;
-    r.rv = f3sub(rv, f3smul(__fsub_rn(1.f, r.l), r.dir));
-    r.phase = kRefOuter;
-    r.guard = r.count = 0;
-    r.done = r.Fn = r.Lp = false;
-    r.bucket = -1;
-    r.hit = F3{0.f, 0.f, 0.f};
-    r.cr = r.cg = r.cb = 0.f;
-    r.sc = SuperCache{};
-    // the super-block skip condition of raycast_ref_kernel
-    const float vbl = g.vbl, reach = g.d_max + 2.f * vbl;
-    const float e[3] = {Er.m[3] + reach * r.dir.x, Er.m[7] + reach * r.dir.y, Er.m[11] + reach * r.dir.z};
-    const float c[3] = {Er.m[3], Er.m[7], Er.m[11]};
-    r.skip = true;
-#pragma unroll
-    for (int a = 0; a < 3; a++) {
-        const int lo = __ldcg(&g.ctr->sb_lo[a]), hi = __ldcg(&g.ctr->sb_hi[a]);
-        const float mn = fminf(c[a], e[a]), mx = fmaxf(c[a], e[a]);
-        if (!(fabsf(mn) < 1e6f && fabsf(mx) < 1e6f)) r.skip = false;
-        long long bl = (long long)floorf(mn / vbl) - 1, bh = (long long)floorf(mx / vbl) + 1;
-        if (lo <= hi) {
-            bl = min(bl, (long long)lo * 8);
-            bh = max(bh, (long long)hi * 8 + 7);
-        }
-        if (bh - bl > kHashCollisionFree) r.skip = false;
-    }
-}
-
-template <int kStorage>
-__device__ __forceinline__ void ref_ray_step(const GridView &g, RefRay &r, int cap, bool want_col, int &finds,
-                                             int &voxels) {
-    const float vl = g.vl, vbl = g.vbl, dtr = g.trunc, dmax = g.d_max;
-    if (r.phase == kRefOuter) {
-        if (!(!r.done && !r.Fn && r.l < dmax)) {
-            r.phase = kRefEnd;
-            return;
-        }
-        block_of(g, r.rv, r.bx, r.by, r.bz);
-        r.bucket = find_block(g, r.bx, r.by, r.bz, finds, r.skip, r.sc);
-        r.count = 0;
-        r.phase = kRefSkip;
-    } else if (r.phase == kRefSkip) {
-        if (r.bucket < 0 && r.l < dmax && r.guard < cap) {
-            r.rv = f3add(r.rv, f3smul(vbl, r.dir));
-            r.l = __fadd_rn(r.l, vbl);
-            block_of(g, r.rv, r.bx, r.by, r.bz);
-            r.bucket = find_block(g, r.bx, r.by, r.bz, finds, r.skip, r.sc);
-            r.count++;
-            r.guard++;
-            return;
-        }
-        if (r.l >= dmax) {
-            r.phase = kRefEnd;
-        } else if (r.count > 0) {
-            const float back = __fsub_rn(vbl, dtr);
-            r.rv = f3sub(r.rv, f3smul(back, r.dir));
-            r.l = __fsub_rn(r.l, back);
-            block_of(g, r.rv, r.bx, r.by, r.bz);
-            r.bucket = find_block(g, r.bx, r.by, r.bz, finds, r.skip, r.sc);
-            r.phase = kRefTrunc;
-        } else {
-            r.phase = kRefEnter;
-        }
-    } else if (r.phase == kRefTrunc) {
-        if (r.bucket < 0 && r.l < dmax && r.guard < cap) {
-            r.rv = f3add(r.rv, f3smul(dtr, r.dir));
-            r.l = __fadd_rn(r.l, dtr);
-            block_of(g, r.rv, r.bx, r.by, r.bz);
-            r.bucket = find_block(g, r.bx, r.by, r.bz, finds, r.skip, r.sc);
-            r.guard++;
-            return;
-        }
-        r.phase = kRefEnter;
-    } else if (r.phase == kRefEnter) {
-        if (r.l >= dmax || r.guard >= cap) {
-            r.phase = kRefEnd;
-            return;
-        }
-        r.cur = r.bucket;
-        r.ox = r.bx, r.oy = r.by, r.oz = r.bz;
-        r.v = voxel_in_block(g, r.rv, r.bx, r.by, r.bz);
-        r.phase = kRefVoxel;
-    } else if (r.phase == kRefVoxel) {
-        if (!(!r.done && r.l < dmax && r.ox == r.bx && r.oy == r.by && r.oz == r.bz && !r.Fn)) {
-            r.phase = r.guard >= cap ? kRefEnd : kRefOuter;
-            return;
-        }
-        if (++r.guard >= cap) {
-            r.phase = kRefEnd;
-            return;
-        }
-        const VoxelRead cv = read_voxel<kStorage>(g, r.cur, r.v);
-        voxels++;
-        if (cv.w > 0) {
-            if (cv.sdf > 0) {
-                r.Lp = true;
-                r.rv = f3add(r.rv, f3smul(vl, r.dir));
-                r.l = __fadd_rn(r.l, vl);
-                block_of(g, r.rv, r.bx, r.by, r.bz);
-                r.v = voxel_in_block(g, r.rv, r.bx, r.by, r.bz);
-            } else if (r.Lp) {
-                r.done = true;  // zero crossing (GPUVoxelGrid.cpp:655-689)
-                const F3 vm_in = voxel_mid(g, r.v, r.bx, r.by, r.bz);
-                r.rv = f3sub(r.rv, f3smul(vl, r.dir));
-                r.l = __fsub_rn(r.l, vl);
-                int qx, qy, qz;
-                block_of(g, r.rv, qx, qy, qz);
-                const int vo = voxel_in_block(g, r.rv, qx, qy, qz);
-                const F3 vm_out = voxel_mid(g, vo, qx, qy, qz);
-                const int ob = (qx == r.ox && qy == r.oy && qz == r.oz) ? r.cur
-                                                                       : find_block(g, qx, qy, qz, finds, r.skip, r.sc);
-                VoxelRead o{0.f, 0.f};
-                float orr = 0.f, og = 0.f, obb = 0.f;
-                if (ob >= 0) {  // missing block: reads as an empty voxel (reference: value_at(invalid))
-                    o = read_voxel<kStorage>(g, ob, vo);
-                    voxels++;
-                    if (want_col) {
-                        const float *pl = g.rgb + (size_t)ob * 3 * kBlockVoxels + vo;
-                        orr = pl[0];
-                        og = pl[kBlockVoxels];
-                        obb = pl[2 * kBlockVoxels];
-                    }
-                }
-                const float x = __fdiv_rn(
-                    __fadd_rn(__fdiv_rn(__fmul_rn(o.w, o.sdf), vl), __fmul_rn(cv.w, __fsub_rn(1.f, __fdiv_rn(cv.sdf, vl)))),
-                    __fadd_rn(cv.w, o.w));
-                const F3 p = f3add(vm_out, f3smul(x, f3sub(vm_in, vm_out)));
-                const float sproj = __fsub_rn(f3dot(p, r.dir), f3dot(r.rv, r.dir));
-                r.hit = f3add(r.rv, f3smul(sproj, r.dir));
-                if (want_col) {
-                    const float *pl = g.rgb + (size_t)r.cur * 3 * kBlockVoxels + r.v;
-                    r.cr = (float)((0.5 * (double)orr + 0.5 * (double)pl[0]) / 255.0);
-                    r.cg = (float)((0.5 * (double)og + 0.5 * (double)pl[kBlockVoxels]) / 255.0);
-                    r.cb = (float)((0.5 * (double)obb + 0.5 * (double)pl[2 * kBlockVoxels]) / 255.0);
-                }
-            } else {
-                r.Fn = true;
-            }
-        } else {
-            r.Lp = false;
-            r.rv = f3add(r.rv, f3smul(vl, r.dir));
-            r.l = __fadd_rn(r.l, vl);
-            block_of(g, r.rv, r.bx, r.by, r.bz);
-            r.v = voxel_in_block(g, r.rv, r.bx, r.by, r.bz);
-        }
-    }
-}
-
-// raycast_ref_kernel with kRays rays per thread (rows i0, i0 + tile rows,
-// ...) through ref_ray_step: the same outputs, status and counters.
-template <int kStorage, int kRays>
-__global__ void __launch_bounds__(256) raycast_ref_multi_kernel(GridView g, Mat34 Er, float *__restrict__ out_pcd,
-                                                                float *__restrict__ out_col, int iter_cap) {
-    const int j = blockIdx.x * 32 + threadIdx.x;
-    const int i0 = blockIdx.y * (blockDim.y * kRays) + threadIdx.y;
-    const bool want_col = out_col && g.rgb;
-    int finds = 0, voxels = 0;
-    bool timed_out = false;
-    RefRay r;
-    int q = 0;
-    auto inside = [&](int qq) { return i0 + qq * (int)blockDim.y < g.resi && j < g.resj; };
-    while (q < kRays && !inside(q)) q++;
-    if (q < kRays) ref_ray_begin(g, Er, i0 + q * (int)blockDim.y, j, r);
-    while (q < kRays) {
-        ref_ray_step<kStorage>(g, r, iter_cap, want_col, finds, voxels);
-        if (r.phase == kRefEnd) {
-            timed_out |= r.guard >= iter_cap;
-            const size_t pix = (size_t)(i0 + q * (int)blockDim.y) * g.resj + j;
-            const F3 hit = r.done ? r.hit : F3{0.f, 0.f, 0.f};
-            out_pcd[pix * 3 + 0] = hit.x;
-            out_pcd[pix * 3 + 1] = hit.y;
-            out_pcd[pix * 3 + 2] = hit.z;
-            if (out_col) {
-                out_col[pix * 3 + 0] = r.done ? r.cr : 0.f;
-                out_col[pix * 3 + 1] = r.done ? r.cg : 0.f;
-                out_col[pix * 3 + 2] = r.done ? r.cb : 0.f;
-            }
-            q++;
-            while (q < kRays && !inside(q)) q++;
-            if (q < kRays) ref_ray_begin(g, Er, i0 + q * (int)blockDim.y, j, r);
-        }
-    }
-    if (timed_out) atomicOr(&g.ctr->status, kStTimeout);
-    const unsigned m = __activemask();
-    const unsigned f = __reduce_add_sync(m, (unsigned)finds), vx = __reduce_add_sync(m, (unsigned)voxels);
-    if ((threadIdx.x & 31) == __ffs(m) - 1) {
-        atomicAdd(&g.ctr->ray_finds, (unsigned long long)f);
-        atomicAdd(&g.ctr->ray_voxels, (unsigned long long)vx);
     }
 }
 
@@ -656,13 +482,7 @@ extern "C" ss_status ss_raycast(ss_grid *g, const float extr[16], float *ray_pcd
     const dim3 blk(32, 8), grid((g->p.resj + 31) / 32, (g->p.resi + 7) / 8);
     const Mat34 Er = mat34_from(extr);
     const int cap = g->raycast_cap > 0 ? g->raycast_cap : kRaycastIterCap;
-    if (g->lc.ref_raycast_rays == 2) {
-        const dim3 grid2((g->p.resj + 31) / 32, (g->p.resi + 15) / 16);
-        if (g->p.storage == SS_STORAGE_F32)
-            raycast_ref_multi_kernel<SS_STORAGE_F32, 2><<<grid2, blk, 0, s>>>(g->v, Er, ray_pcd, ray_color, cap);
-        else
-            raycast_ref_multi_kernel<SS_STORAGE_F16, 2><<<grid2, blk, 0, s>>>(g->v, Er, ray_pcd, ray_color, cap);
-    } else if (g->p.storage == SS_STORAGE_F32) {
+    if (g->p.storage == SS_STORAGE_F32) {
         raycast_ref_kernel<SS_STORAGE_F32><<<grid, blk, 0, s>>>(g->v, Er, ray_pcd, ray_color, cap);
     } else {
         raycast_ref_kernel<SS_STORAGE_F16><<<grid, blk, 0, s>>>(g->v, Er, ray_pcd, ray_color, cap);

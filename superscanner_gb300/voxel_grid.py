@@ -130,8 +130,7 @@ class GPUVoxelGrid:
         check(lib.ss_clean_memory(self._h, _stream_ptr(stream)), "cleanMemory")
 
     # -- additions of the C-ABI
-    LAUNCH_FIELDS = ("collect_rows", "raycast_rows", "fuse_ctas_per_sm", "refuse_ctas_per_sm", "track_ctas_per_sm",
-                     "ref_raycast_rays")
+    LAUNCH_FIELDS = ("collect_rows", "raycast_rows", "fuse_ctas_per_sm", "refuse_ctas_per_sm", "track_ctas_per_sm")
 
     def launch_config(self) -> dict:
         c = SSLaunchConfig()

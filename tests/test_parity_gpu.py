@@ -112,39 +112,6 @@ def test_raycast_matches_oracle():
         assert np.abs(gc[both] - oc[both]).max() <= 1e-6
 
 
-@pytest.mark.parametrize("cap", [0, 40])
-def test_two_rays_per_thread_reference_raycast_equals_one(cap):
-    """ss_raycast with two rays per thread (ref_raycast_rays = 2, the march as
-    a state machine) writes the same points and colours bit for bit as one
-    ray per thread, counts the same work, and runs out of iterations on the
-    same rays under a small cap (cap 40: SS_ERR_TIMEOUT from both)."""
-    from superscanner_gb300._native import SS_ERR_TIMEOUT
-    P, depth, rgb, intr = frames(n=4, noise=True)
-    g, _ = make_pair(480, 640, intr)
-    for k in range(4):
-        g.integrate(dev(rgb[k]), dev(depth[k]), P[k].astype(np.float32))
-    g.sync()
-    g.test_raycast_cap(cap)
-    out = []
-    for rays in (1, 2):
-        g.set_launch_config(ref_raycast_rays=rays)
-        c0 = g.raycast_counters()
-        pcd, col = g.raycast(P[1].astype(np.float32))
-        pcd, col = pcd.cpu().numpy(), col.cpu().numpy()
-        if cap:
-            with pytest.raises(SSError) as ei:
-                g.sync()
-            assert ei.value.code == SS_ERR_TIMEOUT
-        else:
-            g.sync()
-        c1 = g.raycast_counters()
-        out.append((pcd, col, c1["finds"] - c0["finds"], c1["voxels"] - c0["voxels"]))
-    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
-    assert out[0][2:] == out[1][2:]
-    if not cap:
-        assert (out[0][0][..., 2] != 0).mean() > 0.9
-
-
 def test_pcd_and_normals_match_oracle():
     _, depth, _, intr = frames(n=1, noise=True)
     d = dev(depth[0])
