@@ -505,7 +505,6 @@ ss_status ss_grid_reset(ss_grid *g, ss_stream_t stream) {
     fill_u64_kernel<<<persistent_ctas(g, 4), 256, 0, s>>>(g->v.keys, B, kEmptyKey);
     fill_u64_kernel<<<persistent_ctas(g, 1), 256, 0, s>>>(g->v.sbkeys, (size_t)g->v.sbmask + 1, kSuperEmpty);
     SS_LAUNCH_CHECK();
-    SS_CUDA_TRY(cudaMemsetAsync(g->v.sbbits, 0, ((size_t)g->v.sbmask + 1) * 64, s));
     SS_CUDA_TRY(cudaMemsetAsync(g->v.stamp, 0, B * 8, s));
     if (g->v.vox32) SS_CUDA_TRY(cudaMemsetAsync(g->v.vox32, 0, B * kBlockVoxels * sizeof(float2), s));
     if (g->v.vox16) SS_CUDA_TRY(cudaMemsetAsync(g->v.vox16, 0, B * kBlockVoxels * sizeof(uint32_t), s));
@@ -545,7 +544,6 @@ ss_status ss_grid_create(const ss_params *p, ss_grid **out) {
     // super-block of its own); at least 4096
     const size_t SB = std::max<size_t>(4096, B);
     if (ok) ok = cudaMalloc(&g->v.sbkeys, SB * 8) == cudaSuccess;
-    if (ok) ok = cudaMalloc(&g->v.sbbits, SB * 64) == cudaSuccess;
     g->v.sbmask = (uint32_t)(SB - 1);
     if (ok && p->storage == SS_STORAGE_F32)
         ok = cudaMalloc(&g->v.vox32, B * kBlockVoxels * sizeof(float2)) == cudaSuccess;
@@ -588,7 +586,6 @@ ss_status ss_grid_destroy(ss_grid *g) {
     cudaFree(g->v.vox16);
     cudaFree(g->v.rgb);
     cudaFree(g->v.sbkeys);
-    cudaFree(g->v.sbbits);
     cudaFree((void *)g->v.ray_u);
     cudaFree((void *)g->v.ray_v);
     cudaFree(g->phase_mask);
@@ -660,7 +657,6 @@ ss_status ss_clean_memory(ss_grid *g, ss_stream_t stream) {
     else clean_kernel<SS_STORAGE_F16><<<persistent_ctas(g, 8), 256, 0, s>>>(g->v);
     SS_LAUNCH_CHECK();
     fill_u64_kernel<<<persistent_ctas(g, 1), 256, 0, s>>>(g->v.sbkeys, (size_t)g->v.sbmask + 1, kSuperEmpty);
-    SS_CUDA_TRY(cudaMemsetAsync(g->v.sbbits, 0, ((size_t)g->v.sbmask + 1) * 64, s));
     super_bbox_reset_kernel<<<1, 32, 0, s>>>(g->v.ctr);
     super_rebuild_kernel<<<persistent_ctas(g, 4), 256, 0, s>>>(g->v);
     SS_LAUNCH_CHECK();

@@ -190,6 +190,59 @@ __device__ bool polar3_warp(const double *H, double *R) {
     return true;
 }
 
+// The same polar factor in FP32 (one warp, lane r*3+c holding X[r][c]):
+// the scaled Newton iteration on A = H^T normalised by a power of two, until
+// an update changes no entry by more than 1e-4, then one more (the error
+// squares each step), R written as doubles. It is used where
+// |det X| > 1e-4 |X|_F^3 at every step: then the two smaller singular values
+// of H sum to more than 0.02 times the largest, and the FP32 roundings move
+// R by at most a few 1e-6 rad (the polar factor's sensitivity to a
+// perturbation of A is below 2 / (s_i + s_j) for the singular values
+// s_i, s_j of the rotation's plane). Returns false otherwise (R unset): the
+// FP64 iteration then decides. Every lane of the warp calls it.
+__device__ bool polar3_warp_f32(const double *H, double *R) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const bool mine = lane < 9;
+    const int r = mine ? lane / 3 : 0, c = mine ? lane % 3 : 0;
+    float x = mine ? (float)H[c * 3 + r] : 0.f;  // A = H^T
+    float mx = fabsf(x);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(full, mx, o));
+    if (!(mx > 0.f) || !isfinite(mx)) return false;
+    x = ldexpf(x, -ilogbf(mx));
+    const int r1 = (r + 1) % 3, r2 = (r + 2) % 3, c1 = (c + 1) % 3, c2 = (c + 2) % 3;
+    bool last = false;
+    for (int it = 0; it < 24; it++) {
+        const float a11 = __shfl_sync(full, x, r1 * 3 + c1), a22 = __shfl_sync(full, x, r2 * 3 + c2);
+        const float a12 = __shfl_sync(full, x, r1 * 3 + c2), a21 = __shfl_sync(full, x, r2 * 3 + c1);
+        const float cof = mine ? fmaf(a11, a22, -a12 * a21) : 0.f;
+        float dterm = lane < 3 ? x * cof : 0.f;
+        dterm += __shfl_down_sync(full, dterm, 1);
+        dterm += __shfl_down_sync(full, dterm, 2);
+        const float det = __shfl_sync(full, dterm, 0);
+        float fx = x * x, fc = cof * cof;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            fx += __shfl_xor_sync(full, fx, o);
+            fc += __shfl_xor_sync(full, fc, o);
+        }
+        if (!(fabsf(det) > 1e-4f * fx * sqrtf(fx))) return false;
+        const float g = sqrtf(sqrtf(fc / (det * det * fx)));
+        const float xn = 0.5f * fmaf(g, x, cof / (g * det));
+        float dlt = fabsf(xn - x);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) dlt = fmaxf(dlt, __shfl_xor_sync(full, dlt, o));
+        x = xn;
+        if (last) break;
+        last = dlt <= 1e-4f;
+    }
+    if (!last) return false;
+    if (mine) R[lane] = (double)x;
+    __syncwarp();
+    return true;
+}
+
 // Float pairs (hi, lo) holding hi + lo: the per-pixel terms of kokkosICP's
 // double sums are exact in this form (x and y coordinates are floats; a
 // product of two floats is hi = RN(a b), lo = the exact rounding error), and
@@ -208,9 +261,9 @@ __device__ __forceinline__ void fp2_add(float &h, float &l, float h2, float l2) 
 // The CTA's 18 sums: each lane's pairs, a warp transpose-reduce (at offset o a
 // lane keeps the half of its values selected by lane bit o and adds the other
 // lane's; after offsets 16..1 lane v holds the warp's pair of value v), then
-// the warps' pairs in a fixed order; thread v < kIcpSums returns value v of
-// the CTA as a double (hi + lo, exact).
-__device__ __forceinline__ double icp_cta_sum(float *vh, float *vl, float2 (*red)[kIcpSums]) {
+// the warps' pairs in a fixed order; thread v < kIcpSums returns the CTA's
+// pair of value v.
+__device__ __forceinline__ float2 icp_cta_sum(float *vh, float *vl, float2 (*red)[kIcpSums]) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
     for (int o = 16; o >= 1; o >>= 1) {
@@ -227,13 +280,10 @@ __device__ __forceinline__ double icp_cta_sum(float *vh, float *vl, float2 (*red
     }
     if (lane < kIcpSums) red[wid][lane] = make_float2(vh[0], vl[0]);
     __syncthreads();
-    double out = 0.0;
-    if (threadIdx.x < kIcpSums) {
-        float h = 0.f, l = 0.f;
+    float h = 0.f, l = 0.f;
+    if (threadIdx.x < kIcpSums)
         for (int w = 0; w < (int)(blockDim.x >> 5); w++) fp2_add(h, l, red[w][threadIdx.x].x, red[w][threadIdx.x].y);
-        out = (double)h + (double)l;
-    }
-    return out;
+    return make_float2(h, l);
 }
 
 // Target pixels staged per CTA: a tile's 10 x 10 windows (kokkosICP.cpp:81-83)
@@ -250,11 +300,12 @@ constexpr int kIcpStage = 1536;
 // reference's scan order and strict comparisons (starting from max_dist: the
 // accepted taps of `dist < smallest && dist < max_dist` are exactly those of
 // `dist < min(smallest, max_dist)`), remembers the best tap and forms the
-// correspondence from it afterwards.
+// correspondence from it afterwards. 64 registers (four CTAs per SM; only the
+// rank-deficient fallback of the last CTA spills).
 template <int kType>
-__global__ void __launch_bounds__(256) icp_ref_iter_kernel(const float *__restrict__ xp, const float *__restrict__ yp,
+__global__ void __launch_bounds__(256, 4) icp_ref_iter_kernel(const float *__restrict__ xp, const float *__restrict__ yp,
                                                            const float *__restrict__ yn, int rows, int cols, Intr in,
-                                                           IcpState *st, double *partials) {
+                                                           IcpState *st, float2 *partials) {
     __shared__ float4 sA[kIcpStage];  // target (x, y, z, nx)
     __shared__ float2 sB[kIcpStage];  // target (ny, nz)
     __shared__ float2 red[8][kIcpSums];
@@ -336,29 +387,47 @@ __global__ void __launch_bounds__(256) icp_ref_iter_kernel(const float *__restri
         int best = -1;
         if (staged) {
             // rows of the window in scan order (k outer, l inner); a row's ten
-            // taps are loaded before its comparisons
+            // taps are loaded before its comparisons. The even and the odd
+            // columns keep separate minima (two independent compare chains);
+            // the first tap of the scan with the smallest distance is then
+            // the one of the smaller minimum, on a tie the earlier tap (a
+            // smaller staged index: the staged rows are in scan order).
             const int base = (ci - n_search - r0) * W + (cj - n_search - q0);
+            float s1 = max_dist;
+            int b1 = -1;
 #pragma unroll 1
             for (int dk = 0; dk < 2 * n_search; dk++) {
-                const int row = base + dk * W;
-                float4 a[2 * n_search];
-                float2 b[2 * n_search];
 #pragma unroll
-                for (int dl = 0; dl < 2 * n_search; dl++) {
+              for (int half = 0; half < 2; half++) {  // a half row's taps are loaded before their comparisons
+                const int row = base + dk * W + half * n_search;
+                float4 a[n_search];
+                float2 b[n_search];
+#pragma unroll
+                for (int dl = 0; dl < n_search; dl++) {
                     a[dl] = sA[row + dl];
                     if (kType == SS_ICP_POINT_TO_PLANE) b[dl] = sB[row + dl];
                 }
 #pragma unroll
-                for (int dl = 0; dl < 2 * n_search; dl++) {
+                for (int dl = 0; dl < n_search; dl++) {
                     const F3 py{a[dl].x, a[dl].y, a[dl].z};
                     const float dist = kType == SS_ICP_POINT_TO_POINT
                                            ? f3len(f3sub(py, px))
                                            : fabsf(f3dot(f3sub(py, px), F3{a[dl].w, b[dl].x, b[dl].y}));
-                    if (dist < smallest) {
+                    if ((dl + half * n_search) & 1) {  // an odd column of the window
+                        if (dist < s1) {
+                            s1 = dist;
+                            b1 = row + dl;
+                        }
+                    } else if (dist < smallest) {
                         smallest = dist;
                         best = row + dl;
                     }
                 }
+              }
+            }
+            if (s1 < smallest || (s1 == smallest && b1 < best)) {
+                smallest = s1;
+                best = b1;
             }
         } else {
             for (int k = ci - n_search; k < ci + n_search; k++) {
@@ -418,7 +487,7 @@ __global__ void __launch_bounds__(256) icp_ref_iter_kernel(const float *__restri
     }
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const unsigned nctas = gridDim.x * gridDim.y, cta = blockIdx.y * gridDim.x + blockIdx.x;
-    const double csum = icp_cta_sum(vh, vl, red);
+    const float2 csum = icp_cta_sum(vh, vl, red);
     if (threadIdx.x < kIcpSums) partials[(size_t)threadIdx.x * nctas + cta] = csum;  // value-major slots
     __threadfence();
     __syncthreads();
@@ -426,23 +495,48 @@ __global__ void __launch_bounds__(256) icp_ref_iter_kernel(const float *__restri
     __syncthreads();
     if (!last) return;
     __threadfence();
-    // last CTA: one warp per sum, lanes stride over the CTA slots, fixed shuffle tree (deterministic)
+    // last CTA: warp w sums values w, w + 8, w + 16 (interleaved chains), its
+    // lanes striding over the CTA slots, then a fixed shuffle tree: float
+    // pairs throughout (deterministic), the totals as doubles (hi + lo)
     __shared__ double tot[kIcpSums];
-    __shared__ double Hs[9], Rs[9];
-    for (int v = wid; v < kIcpSums; v += (int)(blockDim.x >> 5)) {
-        double s = 0.0;
-        for (unsigned b = lane; b < nctas; b += 32) s += __ldcg(partials + (size_t)v * nctas + b);
-        s = warp_sum(s);
-        if (lane == 0) tot[v] = s;
+    __shared__ double Hs[9], Rs[9], cxy[6];
+    {
+        constexpr int kPer = (kIcpSums + 7) / 8;
+        float h[kPer], l[kPer];
+#pragma unroll
+        for (int k = 0; k < kPer; k++) h[k] = l[k] = 0.f;
+        for (unsigned b = lane; b < nctas; b += 32) {
+#pragma unroll
+            for (int k = 0; k < kPer; k++) {
+                const int v = wid + 8 * k;
+                if (v < kIcpSums) {
+                    const float2 q = __ldcg(partials + (size_t)v * nctas + b);
+                    fp2_add(h[k], l[k], q.x, q.y);
+                }
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < kPer; k++) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const float h2 = __shfl_down_sync(0xffffffffu, h[k], o), l2 = __shfl_down_sync(0xffffffffu, l[k], o);
+                fp2_add(h[k], l[k], h2, l2);
+            }
+            const int v = wid + 8 * k;
+            if (lane == 0 && v < kIcpSums) tot[v] = (double)h[k] + (double)l[k];
+        }
     }
     __syncthreads();
     if (threadIdx.x >= 32) return;
     const double n = tot[0];
-    const double cx[3] = {tot[1] / n, tot[2] / n, tot[3] / n}, cy[3] = {tot[4] / n, tot[5] / n, tot[6] / n};
+    if (lane < 6) cxy[lane] = tot[1 + lane] / n;  // centerx (0..2), centery (3..5)
+    __syncwarp();
+    const double *cx = cxy, *cy = cxy + 3;
     // H = sum (x - cx)(y - cy)^T = sum x y^T - n cx cy^T
     if (lane < 9) Hs[lane] = tot[7 + lane] - n * cx[lane / 3] * cy[lane % 3];
     __syncwarp();
-    if (!polar3_warp(Hs, Rs) && lane == 0) {  // rank-deficient H: the SVD's own completion of U
+    if (!polar3_warp_f32(Hs, Rs) && !polar3_warp(Hs, Rs) && lane == 0) {
+        // rank-deficient H: the SVD's own completion of U
         double U[9], S[3], V[9];
         svd3_jacobi(Hs, U, S, V);
         for (int r = 0; r < 3; r++)
@@ -450,29 +544,26 @@ __global__ void __launch_bounds__(256) icp_ref_iter_kernel(const float *__restri
                 Rs[r * 3 + c] = V[r * 3] * U[c * 3] + V[r * 3 + 1] * U[c * 3 + 1] + V[r * 3 + 2] * U[c * 3 + 2];
     }
     __syncwarp();
-    if (lane != 0) return;
+    // the new Txy_eigen, one entry per lane: [R | centery - R centerx] (kokkosICP.cpp:177-179)
+    double tn = (lane % 5 == 0) ? 1.0 : 0.0;
+    if (lane < 12) {
+        const int r = lane >> 2, c = lane & 3;
+        tn = c < 3 ? Rs[r * 3 + c] : cy[r] - (Rs[r * 3] * cx[0] + Rs[r * 3 + 1] * cx[1] + Rs[r * 3 + 2] * cx[2]);
+    }
+    if (lane < 16) {
+        st->Txy_d[lane] = tn;
+        st->Txy[lane] = (float)tn;
+    }
     float rsme = (float)tot[16];
     rsme /= (float)n;
     rsme = sqrtf(rsme);
     const float fitness = (float)n / (float)tot[17];
-    const double *R = Rs;
-    double Tn[16];
-    for (int k = 0; k < 16; k++) Tn[k] = (k % 5 == 0) ? 1.0 : 0.0;
-    for (int r = 0; r < 3; r++) {
-        for (int c = 0; c < 3; c++) Tn[r * 4 + c] = R[r * 3 + c];
-        Tn[r * 4 + 3] = cy[r] - (R[r * 3] * cx[0] + R[r * 3 + 1] * cx[1] + R[r * 3 + 2] * cx[2]);
-    }
-    for (int k = 0; k < 16; k++) {
-        st->Txy_d[k] = Tn[k];
-        st->Txy[k] = (float)Tn[k];
-    }
+    const bool became_best = rsme < st->lowest;  // kokkosICP.cpp:181-185 (every lane reads it before lane 0 writes)
+    __syncwarp();
+    if (became_best && lane < 16) st->best[lane] = tn;
+    if (lane != 0) return;
+    if (became_best) st->lowest = rsme;
     const int it = st->iteration;
-    bool became_best = false;
-    if (rsme < st->lowest) {  // kokkosICP.cpp:181-185
-        st->lowest = rsme;
-        for (int k = 0; k < 16; k++) st->best[k] = Tn[k];
-        became_best = true;
-    }
     if (fitness > st->best_fitness) st->best_fitness = fitness;
     if (it < kIcpIters) {
         st->stats[it * 4 + 0] = n;
@@ -558,6 +649,29 @@ static void inverse4d(const double *m, double *out) {
         for (int c = 0; c < 4; c++) out[r * 4 + c] = a[r][c + 4];
 }
 
+// The rotation block of a 4x4 pose (row-major) made orthogonal to double
+// precision: Newton's iteration X <- (X + X^-T) / 2 (X^-T = cofactors / det)
+// from the device's polar factor, which the FP32 iteration leaves orthogonal
+// to about 1e-7; each step squares the deviation, three are plenty.
+static void orthonormalize_rotation(double *T) {
+    double X[9];
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 3; c++) X[r * 3 + c] = T[r * 4 + c];
+    for (int it = 0; it < 3; it++) {
+        double C[9];
+        for (int r = 0; r < 3; r++)
+            for (int c = 0; c < 3; c++) {
+                const int r1 = (r + 1) % 3, r2 = (r + 2) % 3, c1 = (c + 1) % 3, c2 = (c + 2) % 3;
+                C[r * 3 + c] = X[r1 * 3 + c1] * X[r2 * 3 + c2] - X[r1 * 3 + c2] * X[r2 * 3 + c1];
+            }
+        const double det = X[0] * C[0] + X[1] * C[1] + X[2] * C[2];
+        if (!(std::fabs(det) > 0.5)) return;  // not near a rotation: leave it
+        for (int k = 0; k < 9; k++) X[k] = 0.5 * (X[k] + C[k] / det);
+    }
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 3; c++) T[r * 4 + c] = X[r * 3 + c];
+}
+
 // Runs the 10 iterations on prepared point clouds; shared by the entry points.
 ss_status icp_ref_run(const uint16_t *d1, const uint16_t *d2, int rows, int cols, Intr in, const double tx[16],
                       const double ty[16], int type, float *xp, float *yp, float *yn, double *partials, int ctas,
@@ -587,16 +701,27 @@ ss_status icp_ref_run(const uint16_t *d1, const uint16_t *d2, int rows, int cols
     h.best_fitness = 0.f;
     SS_CUDA_TRY(cudaMemcpyAsync(state, &h, sizeof(h), cudaMemcpyHostToDevice, s));
     const dim3 tiles(icp_tiles_x(cols), icp_tiles_y(rows));  // ctas == tiles.x * tiles.y
+    float2 *slots = reinterpret_cast<float2 *>(partials);        // 8 bytes per CTA and value, as a double
+    // four CTAs per SM (64 registers, 38 KB of shared memory each) need the
+    // largest shared-memory carveout; a hint, so its status is not fatal
+    if (type == SS_ICP_POINT_TO_POINT)
+        cudaFuncSetAttribute(icp_ref_iter_kernel<SS_ICP_POINT_TO_POINT>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             (int)cudaSharedmemCarveoutMaxShared);
+    else
+        cudaFuncSetAttribute(icp_ref_iter_kernel<SS_ICP_POINT_TO_PLANE>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             (int)cudaSharedmemCarveoutMaxShared);
+    cudaGetLastError();
     for (int it = 0; it < kIcpIters; it++) {
         if (type == SS_ICP_POINT_TO_POINT)
-            icp_ref_iter_kernel<SS_ICP_POINT_TO_POINT><<<tiles, 256, 0, s>>>(xp, yp, yn, rows, cols, in, state, partials);
+            icp_ref_iter_kernel<SS_ICP_POINT_TO_POINT><<<tiles, 256, 0, s>>>(xp, yp, yn, rows, cols, in, state, slots);
         else
-            icp_ref_iter_kernel<SS_ICP_POINT_TO_PLANE><<<tiles, 256, 0, s>>>(xp, yp, yn, rows, cols, in, state, partials);
+            icp_ref_iter_kernel<SS_ICP_POINT_TO_PLANE><<<tiles, 256, 0, s>>>(xp, yp, yn, rows, cols, in, state, slots);
         SS_LAUNCH_CHECK();
     }
     SS_CUDA_TRY(cudaMemcpyAsync(&h, state, sizeof(h), cudaMemcpyDeviceToHost, s));
     SS_CUDA_TRY(cudaStreamSynchronize(s));
     for (int k = 0; k < 16; k++) txy_out[k] = h.best[k];
+    orthonormalize_rotation(txy_out);
     if (rmse_out) *rmse_out = h.lowest;
     return SS_OK;
 }

@@ -96,7 +96,6 @@ struct GridView {
     int *list;                  // [buckets] touched bucket indices
     Counters *ctr;
     unsigned long long *sbkeys; // [sb_buckets] occupied super-blocks (8^3 blocks) for empty-space skipping
-    uint32_t *sbbits;           // [sb_buckets][16] per entry, bit x + 8y + 64z: a block inserted at (x, y, z) in it
     uint32_t sbmask;            // sb_buckets - 1
     uint32_t mask;              // buckets - 1
     float vl, vbl, trunc, rmin, d_max, max_weight;
@@ -322,11 +321,6 @@ __device__ __forceinline__ int table_find_or_insert(const GridView &g, unsigned 
 // holding at least one allocated block lets a ray skip 8 blocks at a time
 // through empty space. Kept as a small open-addressing set of packed
 // coordinates; inserts are idempotent, entries are only removed by a rebuild.
-// Each entry also carries a 512-bit mask of the block coordinates inserted in
-// it, so a ray in an occupied super-block tests a bit before it probes the
-// table. A bit is set by every insertion and cleared only by a rebuild: a set
-// bit may be stale (a removed block: the probe then answers), a clear bit
-// means no block with those coordinates was inserted.
 constexpr int kSuperShift = 3;
 constexpr unsigned long long kSuperEmpty = ~0ull;
 
@@ -339,23 +333,12 @@ __device__ __forceinline__ uint32_t super_home(unsigned long long key, uint32_t 
     h ^= h >> 15;
     return h & mask;
 }
-__device__ __forceinline__ uint32_t super_bit(int bx, int by, int bz) {
-    return (uint32_t)((bx & 7) | (by & 7) << 3 | (bz & 7) << 6);
-}
-__device__ __forceinline__ void super_mark(const GridView &g, uint32_t slot, int bx, int by, int bz) {
-    const uint32_t v = super_bit(bx, by, bz);
-    uint32_t *w = g.sbbits + (size_t)slot * 16 + (v >> 5);
-    if (!((ld_relaxed_u32(w) >> (v & 31)) & 1u)) atomicOr(w, 1u << (v & 31));
-}
 __device__ __forceinline__ void super_insert(const GridView &g, int bx, int by, int bz) {
     const unsigned long long key = super_key(bx >> kSuperShift, by >> kSuperShift, bz >> kSuperShift);
     uint32_t b = super_home(key, g.sbmask);
     for (uint32_t probe = 0; probe <= g.sbmask; probe++) {
         const unsigned long long k = ld_relaxed(g.sbkeys + b);
-        if (k == key) {
-            super_mark(g, b, bx, by, bz);
-            return;
-        }
+        if (k == key) return;
         if (k == kSuperEmpty) {
             const unsigned long long old = atomicCAS(g.sbkeys + b, kSuperEmpty, key);
             if (old == kSuperEmpty) {  // a new super-block: grow the bounding box
@@ -366,37 +349,24 @@ __device__ __forceinline__ void super_insert(const GridView &g, int bx, int by, 
                 atomicMax(&g.ctr->sb_hi[0], sx);
                 atomicMax(&g.ctr->sb_hi[1], sy);
                 atomicMax(&g.ctr->sb_hi[2], sz);
-                super_mark(g, b, bx, by, bz);
                 return;
             }
-            if (old == key) {
-                super_mark(g, b, bx, by, bz);
-                return;
-            }
+            if (old == key) return;
         }
         b = (b + 1) & g.sbmask;
     }
     atomicOr(&g.ctr->status, kStTableFull);
 }
-// The slot of super-block (sx, sy, sz), or -1 when it holds no block.
-__device__ __forceinline__ int super_slot(const GridView &g, int sx, int sy, int sz) {
+__device__ __forceinline__ bool super_occupied(const GridView &g, int sx, int sy, int sz) {
     const unsigned long long key = super_key(sx, sy, sz);
     uint32_t b = super_home(key, g.sbmask);
     for (uint32_t probe = 0; probe <= g.sbmask; probe++) {
         const unsigned long long k = __ldg(g.sbkeys + b);
-        if (k == key) return (int)b;
-        if (k == kSuperEmpty) return -1;
+        if (k == key) return true;
+        if (k == kSuperEmpty) return false;
         b = (b + 1) & g.sbmask;
     }
-    return -1;
-}
-__device__ __forceinline__ bool super_occupied(const GridView &g, int sx, int sy, int sz) {
-    return super_slot(g, sx, sy, sz) >= 0;
-}
-// Whether a block was inserted at (bx, by, bz), a block of the super-block in `slot`.
-__device__ __forceinline__ bool super_has_block(const GridView &g, int slot, int bx, int by, int bz) {
-    const uint32_t v = super_bit(bx, by, bz);
-    return (__ldg(g.sbbits + (size_t)slot * 16 + (v >> 5)) >> (v & 31)) & 1u;
+    return false;
 }
 
 __device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }

@@ -57,14 +57,12 @@ __device__ __forceinline__ F3 voxel_mid(const GridView &g, int v, int bx, int by
 
 // Block finds of the reference raycast (UnorderedMap::find of the prime hash,
 // GPUVoxelGrid.cpp:590-630). When `skip` holds, a block whose super-block
-// holds no allocated block, or whose bit in its super-block's mask is clear,
-// is known to be absent without a table probe: the super-block is looked up
-// once per super-block the ray enters. That is exact only where no
-// prime-hash collision can make another block answer the find (see
-// raycast_ref_kernel). Every find counts once in `finds`, probe or not.
+// holds no allocated block is known to be absent without a table probe: the
+// super-block is looked up once per super-block the ray enters. That is exact
+// only where no prime-hash collision can make another block answer the find
+// (see raycast_ref_kernel).
 struct SuperCache {
     int sx = INT_MIN, sy = INT_MIN, sz = INT_MIN;
-    int slot = -1;  // the super-block's slot, -1: empty
     bool occ = false;
 };
 
@@ -76,43 +74,13 @@ __device__ __forceinline__ int find_block(const GridView &g, int bx, int by, int
             sc.sx = sx;
             sc.sy = sy;
             sc.sz = sz;
-            sc.slot = super_slot(g, sx, sy, sz);
-            sc.occ = sc.slot >= 0;
+            sc.occ = super_occupied(g, sx, sy, sz);
             finds++;
         }
         if (!sc.occ) return -1;
-        finds++;
-        // no block inserted at these coordinates: absent without a probe
-        if (!super_has_block(g, sc.slot, bx, by, bz)) return -1;
-        return table_find(g, prime_hash(bx, by, bz));
     }
     finds++;
     return table_find(g, prime_hash(bx, by, bz));
-}
-
-// Block-skip steps (rv <- rv + st, st = RN(vbl dir)) that certainly keep rv
-// in the ray's current super-block sc: on each axis the distance to the face
-// the ray moves towards, less a margin of 32 units of 2^-24 |rv| (the
-// roundings of up to 14 steps — a step advances at least vbl / sqrt(3) along
-// the ray's main axis, a super-block is 8 vbl wide — of the face and of the
-// index rule's quotient), over the step, minus one. Such steps move rv
-// monotonically on every axis and never cross that face, so each one's block
-// lies in sc: where sc is empty its find is -1 and no super-block lookup
-// happens, and the step reduces to its additions.
-__device__ __forceinline__ int empty_steps(const GridView &g, F3 rv, F3 st, const SuperCache &sc) {
-    const float vbl = g.vbl;
-    const float p[3] = {rv.x, rv.y, rv.z}, d[3] = {st.x, st.y, st.z};
-    const int sb[3] = {sc.sx, sc.sy, sc.sz};
-    float n = 1e30f;
-#pragma unroll
-    for (int a = 0; a < 3; a++) {
-        if (d[a] == 0.f) continue;
-        const float face = (float)((sb[a] + (d[a] > 0.f ? 1 : 0)) * 8) * vbl;
-        const float margin = 0x1p-19f * (fabsf(p[a]) + 16.f * vbl);
-        const float room = fabsf(face - p[a]) - margin;
-        n = fminf(n, room / fabsf(d[a]));
-    }
-    return n >= 16.f ? 15 : (n > 1.f ? (int)n - 1 : 0);
 }
 
 // The shortest difference between two block coordinates with the same prime
@@ -173,18 +141,8 @@ __global__ void __launch_bounds__(256) raycast_ref_kernel(GridView g, Mat34 Er, 
         block_of(g, rv, bx, by, bz);
         int bucket = find_block(g, bx, by, bz, finds, skip, sc);
         int count = 0;
-        const F3 st = f3smul(vbl, dir);
         while (bucket < 0 && l < dmax && guard < iter_cap) {
-            if (skip && !sc.occ) {  // through an empty super-block: the steps without their finds
-                for (int n = empty_steps(g, rv, st, sc); n > 0 && l < dmax && guard < iter_cap; n--) {
-                    rv = f3add(rv, st);
-                    l = __fadd_rn(l, vbl);
-                    count++;
-                    guard++;
-                }
-                if (!(l < dmax && guard < iter_cap)) break;
-            }
-            rv = f3add(rv, st);
+            rv = f3add(rv, f3smul(vbl, dir));
             l = __fadd_rn(l, vbl);
             block_of(g, rv, bx, by, bz);
             bucket = find_block(g, bx, by, bz, finds, skip, sc);

@@ -399,6 +399,28 @@ __device__ __forceinline__ void track_cta_to_acc(float *s, float *c, float2 (*re
     }
 }
 
+// t rounded to the nearest double (ties to even), by integer operations (the
+// FP64 pipe's conversions cost as much latency as an FMA); |t| < 2^127.
+__device__ __forceinline__ double f64_rn_of_i128(__int128 t) {
+    if (t == 0) return 0.0;
+    const bool neg = t < 0;
+    unsigned __int128 m = neg ? (unsigned __int128)(-t) : (unsigned __int128)t;
+    const unsigned long long mh = (unsigned long long)(m >> 64), ml = (unsigned long long)m;
+    const int lz = mh ? __clzll((long long)mh) : 64 + __clzll((long long)ml);
+    m <<= lz;  // the leading one at bit 127
+    const unsigned long long th = (unsigned long long)(m >> 64), tl = (unsigned long long)m;
+    unsigned long long mant = th >> 11;  // 53 bits
+    int ex = 127 - lz + 1023;
+    if (((th >> 10) & 1ull) && ((th & 0x3ffull) || tl || (mant & 1ull))) {
+        if (++mant >> 53) {
+            mant >>= 1;
+            ex++;
+        }
+    }
+    return __longlong_as_double((long long)((neg ? 0x8000000000000000ull : 0ull) | ((unsigned long long)ex << 52) |
+                                            (mant & 0xfffffffffffffull)));
+}
+
 __device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long *p) {
     unsigned long long v;
     asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
@@ -410,8 +432,7 @@ __device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long
 // default, about a second), then returns
 // in lane v < kTrackAccValues value v of this use in FP64, in units of
 // 2^-kTrackFixShift (the chunk increments recombined exactly into a 128-bit
-// integer t = h 2^64 + l with l signed, then fma(h, 2^64, l): exact for
-// |t| < 2^63, else within two roundings). prev: the buffer's 90 words as read
+// integer, then rounded once to the nearest double). prev: the buffer's 90 words as read
 // at its previous use (shared), updated here. False on timeout.
 __device__ __forceinline__ bool track_acc_wait(const unsigned long long *__restrict__ acc, unsigned long long *prev,
                                                double &value, int polls, int extra) {
@@ -448,9 +469,7 @@ __device__ __forceinline__ bool track_acc_wait(const unsigned long long *__restr
         const long long s0 = (long long)(w0 - p0 - counted), s1 = (long long)(w1 - p1 - counted),
                         s2 = (long long)(w2 - p2 - counted);
         const __int128 t = (__int128)s2 * ((__int128)1 << 64) + (__int128)s1 * ((__int128)1 << 32) + (__int128)s0;
-        const long long l = (long long)(unsigned long long)t;  // t mod 2^64, signed
-        const long long h = (long long)((t - (__int128)l) >> 64);
-        value = fma((double)h, 0x1p64, (double)l);
+        value = f64_rn_of_i128(t);
     }
     return true;
 }

@@ -15,6 +15,7 @@
 //   so a_ik = a_ki serves the rows below the pivot); the rows above the pivot
 //   are cleared too, so no back substitution is needed. Each step updates
 //   every other row in fraction-free form, a_ij <- p' a_ij - a_ik (a_kj 2^-e),
+//   rounded as fma(-a_ik, a_kj 2^-e, RN(p' a_ij)),
 //   with the pivot p = p' 2^e split exactly into p' in [1, 2) and a power of
 //   two by integer operations: each row is scaled by a factor in [1, 2) per
 //   step, and no division sits on the elimination's critical path;
@@ -65,13 +66,39 @@ __device__ __forceinline__ double scale_pow2(double x, int e) {
     return __hiloint2double((hi & 0x800fffff) | (nx << 20), lo);
 }
 
+// Conversions by integer operations, off the FP64 pipe (whose conversion
+// instructions cost as much latency as an FMA): m in [1, 2) to the float of
+// its leading 23 mantissa bits (truncated), and a normal float to its exact
+// double.
+__device__ __forceinline__ float f32_of_unit_mantissa(double m) {
+    const unsigned hi = (unsigned)__double2hiint(m), lo = (unsigned)__double2loint(m);
+    return __uint_as_float(0x3f800000u | ((hi & 0xfffffu) << 3) | (lo >> 29));
+}
+__device__ __forceinline__ double f64_of_normal_f32(float f) {
+    const unsigned u = __float_as_uint(f);
+    const unsigned hi = (u & 0x80000000u) | ((((u >> 23) & 0xffu) + 896u) << 20) | ((u & 0x7fffffu) >> 3);
+    return __hiloint2double((int)hi, (int)(u << 29));
+}
+
+// (float)d, rounded to nearest even, by integer operations where the result
+// is a normal float (other values: the conversion instruction).
+__device__ __forceinline__ float f32_rn_of_f64(double d) {
+    const unsigned hi = (unsigned)__double2hiint(d), lo = (unsigned)__double2loint(d);
+    const int e = (int)((hi >> 20) & 0x7ffu) - 1023;
+    if (e < -126 || e > 127) return (float)d;
+    const unsigned top = ((hi & 0xfffffu) << 3) | (lo >> 29), rest = lo & 0x1fffffffu;
+    unsigned bits = ((unsigned)(e + 127) << 23) | top;
+    if (rest > 0x10000000u || (rest == 0x10000000u && (top & 1u))) bits += 1u;  // a carry moves into the exponent
+    return __uint_as_float(bits | (hi & 0x80000000u));
+}
+
 // 1 / x for finite normal x > 0: FP32 seed on the mantissa, two Newton-Raphson steps in FP64.
 __device__ __forceinline__ double rcp_pos(double x) {
     int e;
     const double m = split_pow2(x, e);
     float sf;
-    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(sf) : "f"((float)m));
-    double r = (double)sf;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(sf) : "f"(f32_of_unit_mantissa(m)));
+    double r = f64_of_normal_f32(sf);  // sf in [0.5, 1]
     double t = fma(-m, r, 1.0);
     r = fma(r, t, r);
     t = fma(-m, r, 1.0);
@@ -148,7 +175,8 @@ __device__ __forceinline__ bool warp_solve6_aug(double a, double x[6], double pi
         const double aik = __shfl_sync(full, a, !upd ? 0 : (i < k ? aug_lane(i, k) : aug_lane(k, i)));
         // a_kj 2^-e of this lane's column (columns left of the pivot are cleared: 0)
         const double akj = __shfl_sync(full, ahat, (upd && j >= k) ? aug_lane(k, j) : 0);
-        if (upd) a = fma(ph, a, -(aik * (j >= k ? akj : 0.0)));
+        // ph a needs only the pivot, so it overlaps the shuffles of a_kj
+        if (upd) a = fma(-aik, j >= k ? akj : 0.0, ph * a);
     }
     // row i is now u_ii x_i = c_i: reciprocals on the diagonal lanes, x_i on lanes (i, 6)
     const bool diag = live && i == j;
@@ -240,7 +268,7 @@ __device__ __forceinline__ float warp_se3_left_update(const double xi[6], const 
     if (nl && c == 3) nv += tr;
     if (nl) {
         Tout[lane] = nv;
-        Tfout[lane] = (float)nv;
+        Tfout[lane] = f32_rn_of_f64(nv);
     }
     // |xi|^2 in FP32: lane k < 6 converts xi[k], then a sum over 8 lanes
     const int k6 = lane & 7;

@@ -178,7 +178,7 @@ __device__ __forceinline__ bool ray_search(const GridView &g, float ox, float oy
     float t_prev = 0.f, f_prev = 0.f;  // forward: last valid sample; back: last (negative) sample
     float ta = 0.f, fa = 0.f, tb = 0.f, fb = 0.f;  // bracket: f(ta) > 0 > f(tb)
     int csx = INT_MIN, csy = INT_MIN, csz = INT_MIN;
-    int cslot = -1;  // the current super-block's slot; -1: empty; -2: occupied, slot not looked up
+    bool cocc = false;
     while (steps < max_steps) {
         if (mode == kRayForward && !(t < t_hi)) break;
         const float px = fmaf(t, dx, ox), py = fmaf(t, dy, oy), pz = fmaf(t, dz, oz);
@@ -190,13 +190,11 @@ __device__ __forceinline__ bool ray_search(const GridView &g, float ox, float oy
                 csx = sx;
                 csy = sy;
                 csz = sz;
-                cslot = super_slot(g, sx, sy, sz);
+                cocc = super_occupied(g, sx, sy, sz);
                 cache.lookups++;
             }
-            const bool empty_super = cslot == -1;
-            // a block never inserted at (bx, by, bz) is skipped without a table probe
-            if (empty_super || (cslot >= 0 && !super_has_block(g, cslot, bx, by, bz)) ||
-                cached_lookup(g, cache, bx, by, bz) < 0) {
+            const bool empty_super = !cocc;
+            if (empty_super || cached_lookup(g, cache, bx, by, bz) < 0) {
                 // exit of the empty super-block's (or block's) box along the ray
                 const float box = empty_super ? sbl : g.vbl;
                 const int cx = empty_super ? sx : bx, cy = empty_super ? sy : by, cz = empty_super ? sz : bz;
@@ -243,7 +241,7 @@ __device__ __forceinline__ bool ray_search(const GridView &g, float ox, float oy
                 csx = (int)floorf(px * inv_vbl) >> kSuperShift;
                 csy = (int)floorf(py * inv_vbl) >> kSuperShift;
                 csz = (int)floorf(pz * inv_vbl) >> kSuperShift;
-                cslot = -2;
+                cocc = true;
                 t += fmaxf(vl, 0.8f * sm.f) * inv_len;
             } else {
                 mode = kBack;
