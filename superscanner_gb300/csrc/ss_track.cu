@@ -213,20 +213,24 @@ __device__ __forceinline__ void track_fill_cam(const uint16_t *__restrict__ dept
     }
 }
 
-// track_accumulate over the cached camera points (groups of kTrackGroup:
-// all model-map loads of a group before its sums). A group's terms are summed
+// track_accumulate over the cached camera points (groups of kG: all
+// model-map loads of a group before its sums). A group's terms are summed
 // with plain FMAs, then added to the Kahan pairs once per group (the running
-// sums stay compensated; a group adds at most kTrackGroup - 1 roundings).
+// sums stay compensated; a group adds at most kG - 1 roundings). With
+// kG = kCamCache the thread's points are one group: every gather of the
+// iteration is in flight at once (one memory round trip), and the pairs are
+// the group's sums with zero compensation.
+template <int kG>
 __device__ __forceinline__ void track_accumulate_cam(const float4 (*cam)[256], int m_count, int rows, int cols,
                                                      Intr in, const float4 *__restrict__ vmap,
                                                      const float4 *__restrict__ nmap, const float *T, const float *Pi,
                                                      float dist2, float *s, float *c) {
-    for (int m0 = 0; m0 < m_count; m0 += kTrackGroup) {
-        float wv[kTrackGroup][3];
-        float4 n[kTrackGroup], v[kTrackGroup];
-        bool ok[kTrackGroup];
+    for (int m0 = 0; m0 < m_count; m0 += kG) {
+        float wv[kG][3];
+        float4 n[kG], v[kG];
+        bool ok[kG];
 #pragma unroll
-        for (int g = 0; g < kTrackGroup; g++) {
+        for (int g = 0; g < kG; g++) {
             const float4 cp = (m0 + g < m_count) ? cam[m0 + g][threadIdx.x] : make_float4(0.f, 0.f, 0.f, 0.f);
             const float cx = cp.x, cy = cp.y, dd = cp.z;
             const float wx = fmaf(T[0], cx, fmaf(T[1], cy, fmaf(T[2], dd, T[3])));
@@ -256,7 +260,7 @@ __device__ __forceinline__ void track_accumulate_cam(const float4 (*cam)[256], i
         for (int q = 0; q < kTrackSums - 1; q++) t[q] = 0.f;
         bool any = false;
 #pragma unroll
-        for (int g = 0; g < kTrackGroup; g++) {
+        for (int g = 0; g < kG; g++) {
             if (!ok[g]) continue;
             const float4 nn = n[g], vv = v[g];
             if (nn.x == 0.f && nn.y == 0.f && nn.z == 0.f) continue;
@@ -276,7 +280,10 @@ __device__ __forceinline__ void track_accumulate_cam(const float4 (*cam)[256], i
             s[28] += 1.f;  // counts stay exact far below 2^24
             any = true;
         }
-        if (any) {
+        if (kG >= kCamCache) {  // the only group
+#pragma unroll
+            for (int q = 0; q < kTrackSums - 1; q++) s[q] = t[q];
+        } else if (any) {
 #pragma unroll
             for (int q = 0; q < kTrackSums - 1; q++) kahan_add(s[q], c[q], t[q]);
         }
@@ -676,7 +683,10 @@ __global__ void __launch_bounds__(256) track_frame_kernel(const uint16_t *__rest
                 P[k] = Pi[k];
             }
             if (cached)
-                track_accumulate_cam(cam, m_count, rows, cols, in, vmap, nmap, T, P, dist2, s, c);
+                if (m_count > kTrackGroup)
+                    track_accumulate_cam<kCamCache>(cam, m_count, rows, cols, in, vmap, nmap, T, P, dist2, s, c);
+                else
+                    track_accumulate_cam<kTrackGroup>(cam, m_count, rows, cols, in, vmap, nmap, T, P, dist2, s, c);
             else
                 track_accumulate(depth, rows, cols, in, vmap, nmap, T, P, level, dist2, L.rmin, L.dmax, tid, nthreads,
                                  s, c);
