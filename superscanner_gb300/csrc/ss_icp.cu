@@ -4,9 +4,10 @@
 // The reference runs the 10x10-window correspondence search on the GPU and
 // then copies both point clouds and the correspondences to the host every
 // iteration for centroids, RMSE, H and an Eigen JacobiSVD. Here one kernel
-// per iteration does the search, reduces the 18 sums in double
+// per iteration does the search, reduces the 18 sums as exact float pairs
 // (warp shuffles, then one slot per CTA) and the last CTA to finish reduces
-// the CTA slots in a fixed order, runs a one-sided Jacobi SVD of H in double
+// the CTA slots in a fixed order, takes the rotation as the polar factor of
+// H^T (the SVD's V U^T for a full-rank H; a one-sided Jacobi SVD otherwise)
 // and writes the next Txy, so the 10 iterations run without a host round trip.
 #include <climits>
 #include <mutex>
@@ -496,24 +497,31 @@ __global__ void __launch_bounds__(256, 4) icp_ref_iter_kernel(const float *__res
     if (!last) return;
     __threadfence();
     // last CTA: warp w sums values w, w + 8, w + 16 (interleaved chains), its
-    // lanes striding over the CTA slots, then a fixed shuffle tree: float
-    // pairs throughout (deterministic), the totals as doubles (hi + lo)
+    // lanes striding over the CTA slots (four slots per value loaded before
+    // their additions: one L2 round trip per four, not per slot; a missing
+    // slot adds an exact zero), then a fixed shuffle tree: float pairs
+    // throughout (deterministic), the totals as doubles (hi + lo)
     __shared__ double tot[kIcpSums];
     __shared__ double Hs[9], Rs[9], cxy[6];
     {
-        constexpr int kPer = (kIcpSums + 7) / 8;
+        constexpr int kPer = (kIcpSums + 7) / 8, kBatch = 4;
         float h[kPer], l[kPer];
 #pragma unroll
         for (int k = 0; k < kPer; k++) h[k] = l[k] = 0.f;
-        for (unsigned b = lane; b < nctas; b += 32) {
+        for (unsigned b0 = lane; b0 < nctas; b0 += 32 * kBatch) {
+            float2 q[kPer][kBatch];
 #pragma unroll
-            for (int k = 0; k < kPer; k++) {
-                const int v = wid + 8 * k;
-                if (v < kIcpSums) {
-                    const float2 q = __ldcg(partials + (size_t)v * nctas + b);
-                    fp2_add(h[k], l[k], q.x, q.y);
+            for (int k = 0; k < kPer; k++)
+#pragma unroll
+                for (int i = 0; i < kBatch; i++) {
+                    const int v = wid + 8 * k;
+                    const unsigned b = b0 + 32u * i;
+                    q[k][i] = (v < kIcpSums && b < nctas) ? __ldcg(partials + (size_t)v * nctas + b) : make_float2(0.f, 0.f);
                 }
-            }
+#pragma unroll
+            for (int k = 0; k < kPer; k++)
+#pragma unroll
+                for (int i = 0; i < kBatch; i++) fp2_add(h[k], l[k], q[k][i].x, q[k][i].y);
         }
 #pragma unroll
         for (int k = 0; k < kPer; k++) {
