@@ -191,7 +191,7 @@ __device__ bool polar3_warp(const double *H, double *R) {
     return true;
 }
 
-// The same polar factor in FP32 (one warp, lane r*3+c holding X[r][c]):
+// The same polar factor in FP32, by every lane of the warp at once:
 // the scaled Newton iteration on A = H^T normalised by a power of two, until
 // an update changes no entry by more than 1e-4, then one more (the error
 // squares each step), R written as doubles. It is used where
@@ -202,44 +202,54 @@ __device__ bool polar3_warp(const double *H, double *R) {
 // s_i, s_j of the rotation's plane). Returns false otherwise (R unset): the
 // FP64 iteration then decides. Every lane of the warp calls it.
 __device__ bool polar3_warp_f32(const double *H, double *R) {
-    const unsigned full = 0xffffffffu;
-    const int lane = threadIdx.x & 31;
-    const bool mine = lane < 9;
-    const int r = mine ? lane / 3 : 0, c = mine ? lane % 3 : 0;
-    float x = mine ? (float)H[c * 3 + r] : 0.f;  // A = H^T
-    float mx = fabsf(x);
+    // every lane iterates the whole 3 x 3 in its registers (no shuffles on
+    // the dependent chain); the lanes compute identical values
+    float X[9];
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(full, mx, o));
+    for (int r = 0; r < 3; r++)
+#pragma unroll
+        for (int c = 0; c < 3; c++) X[r * 3 + c] = (float)H[c * 3 + r];  // A = H^T
+    float mx = 0.f;
+#pragma unroll
+    for (int k = 0; k < 9; k++) mx = fmaxf(mx, fabsf(X[k]));
     if (!(mx > 0.f) || !isfinite(mx)) return false;
-    x = ldexpf(x, -ilogbf(mx));
-    const int r1 = (r + 1) % 3, r2 = (r + 2) % 3, c1 = (c + 1) % 3, c2 = (c + 2) % 3;
+    const int ex = ilogbf(mx);
+#pragma unroll
+    for (int k = 0; k < 9; k++) X[k] = ldexpf(X[k], -ex);
     bool last = false;
     for (int it = 0; it < 24; it++) {
-        const float a11 = __shfl_sync(full, x, r1 * 3 + c1), a22 = __shfl_sync(full, x, r2 * 3 + c2);
-        const float a12 = __shfl_sync(full, x, r1 * 3 + c2), a21 = __shfl_sync(full, x, r2 * 3 + c1);
-        const float cof = mine ? fmaf(a11, a22, -a12 * a21) : 0.f;
-        float dterm = lane < 3 ? x * cof : 0.f;
-        dterm += __shfl_down_sync(full, dterm, 1);
-        dterm += __shfl_down_sync(full, dterm, 2);
-        const float det = __shfl_sync(full, dterm, 0);
-        float fx = x * x, fc = cof * cof;
+        float cof[9];
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            fx += __shfl_xor_sync(full, fx, o);
-            fc += __shfl_xor_sync(full, fc, o);
+        for (int r = 0; r < 3; r++)
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                const int r1 = (r + 1) % 3, r2 = (r + 2) % 3, c1 = (c + 1) % 3, c2 = (c + 2) % 3;
+                cof[r * 3 + c] = fmaf(X[r1 * 3 + c1], X[r2 * 3 + c2], -X[r1 * 3 + c2] * X[r2 * 3 + c1]);
+            }
+        const float det = fmaf(X[0], cof[0], fmaf(X[1], cof[1], X[2] * cof[2]));
+        float fx = 0.f, fc = 0.f;
+#pragma unroll
+        for (int k = 0; k < 9; k++) {
+            fx = fmaf(X[k], X[k], fx);
+            fc = fmaf(cof[k], cof[k], fc);
         }
         if (!(fabsf(det) > 1e-4f * fx * sqrtf(fx))) return false;
         const float g = sqrtf(sqrtf(fc / (det * det * fx)));
-        const float xn = 0.5f * fmaf(g, x, cof / (g * det));
-        float dlt = fabsf(xn - x);
+        const float y = 1.f / (g * det);
+        float dlt = 0.f;
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) dlt = fmaxf(dlt, __shfl_xor_sync(full, dlt, o));
-        x = xn;
+        for (int k = 0; k < 9; k++) {
+            const float xn = 0.5f * fmaf(g, X[k], cof[k] * y);
+            dlt = fmaxf(dlt, fabsf(xn - X[k]));
+            X[k] = xn;
+        }
         if (last) break;
         last = dlt <= 1e-4f;
     }
     if (!last) return false;
-    if (mine) R[lane] = (double)x;
+    if ((threadIdx.x & 31) == 0)
+#pragma unroll
+        for (int k = 0; k < 9; k++) R[k] = (double)X[k];
     __syncwarp();
     return true;
 }
@@ -361,19 +371,32 @@ __global__ void __launch_bounds__(256, 4) icp_ref_iter_kernel(const float *__res
     const int W = any ? box[3] + n_search - q0 : 0, H = any ? box[1] + n_search - r0 : 0;
     const bool staged = any && W * H <= kIcpStage;
     if (staged) {
-        // inside the image: the border test keeps every window within rows x cols
-        for (int t = threadIdx.x; t < W * H; t += blockDim.x) {
-            const int k = r0 + t / W, l = q0 + t % W;
-            const size_t q = (size_t)k * cols + l;
-            F3 py = ld3(yp, q), nn{0.f, 0.f, 0.f};
-            bool ok = py.z != 0;
-            if (kType == SS_ICP_POINT_TO_PLANE) {
-                nn = ld3(yn, q);
-                ok = ok && nn.x != 0;
+        // inside the image: the border test keeps every window within rows x cols.
+        // Three entries per thread and round: their loads are issued before the first store.
+        constexpr int kStageRound = 3;
+        for (int t0 = threadIdx.x; t0 < W * H; t0 += kStageRound * blockDim.x) {
+            F3 py[kStageRound], nn[kStageRound];
+#pragma unroll
+            for (int u = 0; u < kStageRound; u++) {
+                const int t = t0 + u * (int)blockDim.x;
+                py[u] = F3{0.f, 0.f, 0.f};
+                nn[u] = F3{0.f, 0.f, 0.f};
+                if (t < W * H) {
+                    const size_t q = (size_t)(r0 + t / W) * cols + (q0 + t % W);
+                    py[u] = ld3(yp, q);
+                    if (kType == SS_ICP_POINT_TO_PLANE) nn[u] = ld3(yn, q);
+                }
             }
-            if (!ok) py.x = __int_as_float(0x7fc00000);
-            sA[t] = make_float4(py.x, py.y, py.z, nn.x);
-            sB[t] = make_float2(nn.y, nn.z);
+#pragma unroll
+            for (int u = 0; u < kStageRound; u++) {
+                const int t = t0 + u * (int)blockDim.x;
+                if (t >= W * H) break;
+                bool ok = py[u].z != 0;
+                if (kType == SS_ICP_POINT_TO_PLANE) ok = ok && nn[u].x != 0;
+                const float px0 = ok ? py[u].x : __int_as_float(0x7fc00000);
+                sA[t] = make_float4(px0, py[u].y, py[u].z, nn[u].x);
+                sB[t] = make_float2(nn[u].y, nn[u].z);
+            }
         }
     }
     __syncthreads();
@@ -497,14 +520,14 @@ __global__ void __launch_bounds__(256, 4) icp_ref_iter_kernel(const float *__res
     if (!last) return;
     __threadfence();
     // last CTA: warp w sums values w, w + 8, w + 16 (interleaved chains), its
-    // lanes striding over the CTA slots (four slots per value loaded before
-    // their additions: one L2 round trip per four, not per slot; a missing
+    // lanes striding over the CTA slots (eight slots per value loaded before
+    // their additions: one L2 round trip per eight, not per slot; a missing
     // slot adds an exact zero), then a fixed shuffle tree: float pairs
     // throughout (deterministic), the totals as doubles (hi + lo)
     __shared__ double tot[kIcpSums];
     __shared__ double Hs[9], Rs[9], cxy[6];
     {
-        constexpr int kPer = (kIcpSums + 7) / 8, kBatch = 4;
+        constexpr int kPer = (kIcpSums + 7) / 8, kBatch = 8;
         float h[kPer], l[kPer];
 #pragma unroll
         for (int k = 0; k < kPer; k++) h[k] = l[k] = 0.f;
