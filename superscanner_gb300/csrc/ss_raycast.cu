@@ -1,8 +1,8 @@
 // ss_raycast.cu — reference-semantics raycast (raycastingTag,
 // src/VoxelGrid/GPUVoxelGrid.cpp:561-715) and its C-ABI entry point.
 //
-// One thread per pixel, 32x8 pixel tiles (a warp marches 32 neighbouring rays
-// of one row, which stay coherent through the block-skip loop). The unit ray
+// One thread per pixel, 32x8 pixel tiles, each warp an 8 x 4 patch of
+// neighbouring rays, which stay coherent through the block-skip loop. The unit ray
 // table normPcd (createNormPcdTag, :717-722) is recomputed in registers
 // instead of being read from a 3.7 MB image.
 #include <climits>
@@ -93,8 +93,12 @@ constexpr int kHashCollisionFree = 950;
 template <int kStorage>
 __global__ void __launch_bounds__(256) raycast_ref_kernel(GridView g, Mat34 Er, float *__restrict__ out_pcd,
                                                           float *__restrict__ out_col, int iter_cap) {
-    const int j = blockIdx.x * 32 + threadIdx.x;
-    const int i = blockIdx.y * blockDim.y + threadIdx.y;
+    // warp w of the 32 x 8 tile marches an 8 x 4 pixel patch: neighbouring rays
+    // in both directions take more similar paths than a 32-pixel row segment
+    // (0.351 vs 0.388 ms per call at 640 x 480)
+    const int w = threadIdx.y, ln = threadIdx.x;
+    const int j = blockIdx.x * 32 + (w & 3) * 8 + (ln & 7);
+    const int i = blockIdx.y * blockDim.y + (w >> 2) * 4 + (ln >> 3);
     if (i >= g.resi || j >= g.resj) return;
     const float vl = g.vl, vbl = g.vbl, dtr = g.trunc, dmax = g.d_max;
 
