@@ -324,13 +324,17 @@ __global__ void __launch_bounds__(256, 4) icp_ref_iter_kernel(const float *__res
     __shared__ bool last;
     const int n_search = 5;
     const float max_dist = 0.075f;
-    Mat34 T;
-#pragma unroll
-    for (int k = 0; k < 12; k++) T.m[k] = st->Txy[k];
     const int j = blockIdx.x * 32 + (threadIdx.x & 31), i = blockIdx.y * 8 + (threadIdx.x >> 5);
     const size_t p = (size_t)i * cols + j;
     const bool inside = i < rows && j < cols;
+    // the source point does not change between iterations (written before the
+    // first one): loaded before this launch waits for the previous iteration,
+    // whose last CTA is still forming Txy and reading the CTA slots
     const F3 x = inside ? ld3(xp, p) : F3{0.f, 0.f, 0.f};
+    pdl_wait();
+    Mat34 T;
+#pragma unroll
+    for (int k = 0; k < 12; k++) T.m[k] = st->Txy[k];
     const bool has_x = x.z != 0;
     F3 px{0.f, 0.f, 0.f};
     int ci = 0, cj = 0;
@@ -517,6 +521,7 @@ __global__ void __launch_bounds__(256, 4) icp_ref_iter_kernel(const float *__res
     __syncthreads();
     if (threadIdx.x == 0) last = atomicAdd(&st->ticket, 1) == (int)nctas - 1;
     __syncthreads();
+    pdl_trigger();  // the next iteration may launch (it waits for this grid before reading anything it writes)
     if (!last) return;
     __threadfence();
     // last CTA: warp w sums values w, w + 8, w + 16 (interleaved chains), its
@@ -742,12 +747,15 @@ ss_status icp_ref_run(const uint16_t *d1, const uint16_t *d2, int rows, int cols
         cudaFuncSetAttribute(icp_ref_iter_kernel<SS_ICP_POINT_TO_PLANE>, cudaFuncAttributePreferredSharedMemoryCarveout,
                              (int)cudaSharedmemCarveoutMaxShared);
     cudaGetLastError();
+    // programmatic dependent launches: an iteration's CTAs start while the
+    // previous one's last CTA forms the transform
     for (int it = 0; it < kIcpIters; it++) {
         if (type == SS_ICP_POINT_TO_POINT)
-            icp_ref_iter_kernel<SS_ICP_POINT_TO_POINT><<<tiles, 256, 0, s>>>(xp, yp, yn, rows, cols, in, state, slots);
+            SS_CUDA_TRY(launch_kernel(icp_ref_iter_kernel<SS_ICP_POINT_TO_POINT>, tiles, dim3(256), 0, s, true, xp, yp, yn,
+                                      rows, cols, in, state, slots));
         else
-            icp_ref_iter_kernel<SS_ICP_POINT_TO_PLANE><<<tiles, 256, 0, s>>>(xp, yp, yn, rows, cols, in, state, slots);
-        SS_LAUNCH_CHECK();
+            SS_CUDA_TRY(launch_kernel(icp_ref_iter_kernel<SS_ICP_POINT_TO_PLANE>, tiles, dim3(256), 0, s, true, xp, yp, yn,
+                                      rows, cols, in, state, slots));
     }
     SS_CUDA_TRY(cudaMemcpyAsync(&h, state, sizeof(h), cudaMemcpyDeviceToHost, s));
     SS_CUDA_TRY(cudaStreamSynchronize(s));
