@@ -61,16 +61,34 @@ __global__ void normals_kernel(const float *__restrict__ pcd, int rows, int cols
 constexpr int kIcpSums = 18;  // n_cors, sum x (3), sum y (3), sum x y^T (9), sum tmp^2, n_x
 constexpr int kIcpIters = 10; // n_it (kokkosICP.cpp:54)
 
+// The iteration kernel's CTA slots are summed in two stages: the last CTA of
+// each group of CTAs sums the group's slots into a group slot, the last group
+// sums the group slots (a fixed order throughout). Groups of kIcpGroup CTAs,
+// larger where that would make more than kIcpMaxGroups groups.
+constexpr int kIcpGroup = 32;
+constexpr int kIcpMaxGroups = 128;
+
+static inline int icp_group_size(int ctas) {
+    const int g = (ctas + kIcpMaxGroups - 1) / kIcpMaxGroups;
+    return g > kIcpGroup ? g : kIcpGroup;
+}
+
 struct IcpState {
     float Txy[16];      // float copy used by the search (EigentoKmat4f(Txy.cast<float>()))
     double Txy_d[16];   // double Txy_eigen
     double best[16];    // bestTxy_eigen
     float lowest;       // lowestRSME
     float best_fitness;
-    int ticket;
+    int ticket;         // groups done
     int iteration;
     double stats[kIcpIters * 4];
+    int gticket[kIcpMaxGroups];  // CTAs done, per group
 };
+
+// Bytes of CTA and group slots (8 per slot and value) for `ctas` iteration CTAs.
+static inline size_t icp_slot_bytes(int ctas) {
+    return (size_t)(ctas + kIcpMaxGroups) * kIcpSums * 8;
+}
 
 __device__ void svd3_jacobi(const double *H, double *U, double *S, double *V) {
     double A[9];
@@ -316,7 +334,7 @@ constexpr int kIcpStage = 1536;
 template <int kType>
 __global__ void __launch_bounds__(256, 4) icp_ref_iter_kernel(const float *__restrict__ xp, const float *__restrict__ yp,
                                                            const float *__restrict__ yn, int rows, int cols, Intr in,
-                                                           IcpState *st, float2 *partials) {
+                                                           IcpState *st, float2 *partials, int gsz) {
     __shared__ float4 sA[kIcpStage];  // target (x, y, z, nx)
     __shared__ float2 sB[kIcpStage];  // target (ny, nz)
     __shared__ float2 red[8][kIcpSums];
@@ -519,24 +537,53 @@ __global__ void __launch_bounds__(256, 4) icp_ref_iter_kernel(const float *__res
     if (threadIdx.x < kIcpSums) partials[(size_t)threadIdx.x * nctas + cta] = csum;  // value-major slots
     __threadfence();
     __syncthreads();
-    if (threadIdx.x == 0) last = atomicAdd(&st->ticket, 1) == (int)nctas - 1;
+    constexpr int kPer = (kIcpSums + 7) / 8;  // values per warp: w, w + 8, w + 16
+    const unsigned grp = cta / gsz, gbase = grp * gsz, ngroups = (nctas + gsz - 1) / gsz;
+    const unsigned gsize = min((unsigned)gsz, nctas - gbase);
+    if (threadIdx.x == 0) last = atomicAdd(&st->gticket[grp], 1) == (int)gsize - 1;
+    __syncthreads();
+    if (!last) return;  // (a CTA's exit lets the next iteration launch)
+    __threadfence();
+    // the group's last CTA: lane b of warp w adds slots gbase + b, + 32, ...
+    // of values w, w + 8, w + 16, then a fixed shuffle tree into the group slot
+    float2 *gslots = partials + (size_t)kIcpSums * nctas;  // [value][group]
+#pragma unroll
+    for (int k = 0; k < kPer; k++) {
+        const int v = wid + 8 * k;
+        float h = 0.f, l = 0.f;
+        if (v < kIcpSums)
+            for (unsigned b = lane; b < gsize; b += 32) {
+                const float2 q = __ldcg(partials + (size_t)v * nctas + gbase + b);
+                fp2_add(h, l, q.x, q.y);
+            }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const float h2 = __shfl_down_sync(0xffffffffu, h, o), l2 = __shfl_down_sync(0xffffffffu, l, o);
+            fp2_add(h, l, h2, l2);
+        }
+        if (lane == 0 && v < kIcpSums) gslots[(size_t)v * ngroups + grp] = make_float2(h, l);
+    }
+    if (threadIdx.x == 0) st->gticket[grp] = 0;  // every CTA of the group has taken its ticket
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(&st->ticket, 1) == (int)ngroups - 1;
     __syncthreads();
     pdl_trigger();  // the next iteration may launch (it waits for this grid before reading anything it writes)
     if (!last) return;
     __threadfence();
     // last CTA: warp w sums values w, w + 8, w + 16 (interleaved chains), its
-    // lanes striding over the CTA slots (eight slots per value loaded before
-    // their additions: one L2 round trip per eight, not per slot; a missing
-    // slot adds an exact zero), then a fixed shuffle tree: float pairs
-    // throughout (deterministic), the totals as doubles (hi + lo)
+    // lanes striding over the group slots (eight slots per value loaded before
+    // their additions; a missing slot adds an exact zero), then a fixed
+    // shuffle tree: float pairs throughout (deterministic), the totals as
+    // doubles (hi + lo)
     __shared__ double tot[kIcpSums];
     __shared__ double Hs[9], Rs[9], cxy[6];
     {
-        constexpr int kPer = (kIcpSums + 7) / 8, kBatch = 8;
+        constexpr int kBatch = 4;
         float h[kPer], l[kPer];
 #pragma unroll
         for (int k = 0; k < kPer; k++) h[k] = l[k] = 0.f;
-        for (unsigned b0 = lane; b0 < nctas; b0 += 32 * kBatch) {
+        for (unsigned b0 = lane; b0 < ngroups; b0 += 32 * kBatch) {
             float2 q[kPer][kBatch];
 #pragma unroll
             for (int k = 0; k < kPer; k++)
@@ -544,7 +591,7 @@ __global__ void __launch_bounds__(256, 4) icp_ref_iter_kernel(const float *__res
                 for (int i = 0; i < kBatch; i++) {
                     const int v = wid + 8 * k;
                     const unsigned b = b0 + 32u * i;
-                    q[k][i] = (v < kIcpSums && b < nctas) ? __ldcg(partials + (size_t)v * nctas + b) : make_float2(0.f, 0.f);
+                    q[k][i] = (v < kIcpSums && b < ngroups) ? __ldcg(gslots + (size_t)v * ngroups + b) : make_float2(0.f, 0.f);
                 }
 #pragma unroll
             for (int k = 0; k < kPer; k++)
@@ -648,7 +695,7 @@ static ss_status icp_workspace(int dev, size_t npix, int ctas, IcpWorkspace **ou
         w.partials = nullptr;
         w.state = nullptr;
         w.ctas = 0;
-        if (cudaMalloc(&w.partials, (size_t)ctas * kIcpSums * sizeof(double)) != cudaSuccess ||
+        if (cudaMalloc(&w.partials, icp_slot_bytes(ctas)) != cudaSuccess ||
             cudaMalloc(&w.state, sizeof(IcpState)) != cudaSuccess) {
             cudaGetLastError();
             return SS_ERR_NOMEM;
@@ -737,7 +784,8 @@ ss_status icp_ref_run(const uint16_t *d1, const uint16_t *d2, int rows, int cols
     h.best_fitness = 0.f;
     SS_CUDA_TRY(cudaMemcpyAsync(state, &h, sizeof(h), cudaMemcpyHostToDevice, s));
     const dim3 tiles(icp_tiles_x(cols), icp_tiles_y(rows));  // ctas == tiles.x * tiles.y
-    float2 *slots = reinterpret_cast<float2 *>(partials);        // 8 bytes per CTA and value, as a double
+    float2 *slots = reinterpret_cast<float2 *>(partials);        // 8 bytes per slot and value, as a double
+    const int gsz = icp_group_size((int)(tiles.x * tiles.y));
     // four CTAs per SM (64 registers, 38 KB of shared memory each) need the
     // largest shared-memory carveout; a hint, so its status is not fatal
     if (type == SS_ICP_POINT_TO_POINT)
@@ -752,10 +800,10 @@ ss_status icp_ref_run(const uint16_t *d1, const uint16_t *d2, int rows, int cols
     for (int it = 0; it < kIcpIters; it++) {
         if (type == SS_ICP_POINT_TO_POINT)
             SS_CUDA_TRY(launch_kernel(icp_ref_iter_kernel<SS_ICP_POINT_TO_POINT>, tiles, dim3(256), 0, s, true, xp, yp, yn,
-                                      rows, cols, in, state, slots));
+                                      rows, cols, in, state, slots, gsz));
         else
             SS_CUDA_TRY(launch_kernel(icp_ref_iter_kernel<SS_ICP_POINT_TO_PLANE>, tiles, dim3(256), 0, s, true, xp, yp, yn,
-                                      rows, cols, in, state, slots));
+                                      rows, cols, in, state, slots, gsz));
     }
     SS_CUDA_TRY(cudaMemcpyAsync(&h, state, sizeof(h), cudaMemcpyDeviceToHost, s));
     SS_CUDA_TRY(cudaStreamSynchronize(s));
@@ -784,7 +832,7 @@ constexpr size_t kNoAllocMaxPixels = 640 * 480;  // largest rows * cols accepted
 constexpr int kNoAllocCtas = 4096;  // iteration-grid CTAs (32 x 8 tiles): any rows x cols <= 640 x 480 needs <= 3200
 constexpr size_t kAlign256(size_t n) { return (n + 255) / 256 * 256; }
 constexpr size_t kNoAllocImage = kAlign256(kNoAllocMaxPixels * 3 * sizeof(float));
-constexpr size_t kNoAllocPartials = kAlign256((size_t)kNoAllocCtas * kIcpSums * sizeof(double));
+constexpr size_t kNoAllocPartials = kAlign256((size_t)(kNoAllocCtas + kIcpMaxGroups) * kIcpSums * 8);  // CTA and group slots
 constexpr size_t kNoAllocBytes = 3 * kNoAllocImage + kNoAllocPartials + kAlign256(sizeof(IcpState));
 
 static __device__ __align__(256) unsigned char g_icp_noalloc_scratch[kNoAllocBytes];
