@@ -183,7 +183,7 @@ __global__ void __launch_bounds__(256) raydiff_kernel(GridView g, Mat34 T, const
             }
         }
     }
-    // CTA reduction into value-major slots, last CTA sums them in FP64
+    // CTA reduction into value-major slots, the last CTA sums them in FP64
     __shared__ float red[8][kDiffSums];
     __shared__ bool last;
     const int lane = (threadIdx.y * blockDim.x + threadIdx.x) & 31, wid = (threadIdx.y * blockDim.x + threadIdx.x) >> 5;
@@ -208,10 +208,25 @@ __global__ void __launch_bounds__(256) raydiff_kernel(GridView g, Mat34 T, const
     __syncthreads();
     if (!last) return;
     __threadfence();
-    if (tid < kDiffSums) {
-        double v = 0.0;
-        for (int q = 0; q < nb; q++) v += (double)__ldcg(slots + (size_t)tid * nb + q).x;
-        result[tid] = v;
+    // warp w sums value w: its lanes stride over the CTA slots, four slots per
+    // round loaded before their additions into four FP64 partial sums (not one
+    // dependent chain of nb additions), then a fixed shuffle tree
+    for (int v = wid; v < kDiffSums; v += (int)((blockDim.x * blockDim.y) >> 5)) {
+        double a[4] = {0.0, 0.0, 0.0, 0.0};
+        for (int q0 = lane; q0 < nb; q0 += 32 * 4) {
+            float s[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const int q = q0 + 32 * u;
+                s[u] = q < nb ? __ldcg(slots + (size_t)v * nb + q).x : 0.f;
+            }
+#pragma unroll
+            for (int u = 0; u < 4; u++) a[u] += (double)s[u];
+        }
+        double t = (a[0] + a[1]) + (a[2] + a[3]);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+        if (lane == 0) result[v] = t;
     }
     if (tid == 0) *ticket = 0;
 }
