@@ -306,9 +306,11 @@ ss_status ss_normals_from_pcd(const float *pcd, int32_t rows, int32_t cols, floa
 /* kokkosICP(View d1, View d2, tx, ty, type, rmse) (kokkosICP.cpp:25-210):
  * aligns depth d1 (pose tx) to depth d2 (pose ty); returns the best relative
  * transform Txy (4x4 row-major, host) and its RMSE. Correspondence search,
- * reductions and the 3x3 SVD all run on the device; the call synchronises s
- * once at the end to return the result. Scratch memory is allocated on the
- * first call per device and reused. */
+ * reductions and the rotation (the polar factor of H^T, which is the SVD's
+ * V U^T for a full-rank H) all run on the device; the returned rotation is
+ * orthonormal to double precision. The call synchronises s once at the end to
+ * return the result. Scratch memory is allocated on the first call per device
+ * and reused. */
 ss_status ss_kokkos_icp(const uint16_t *d1, const uint16_t *d2, int32_t rows, int32_t cols,
                         float fx, float fy, float cx, float cy, const double tx[16],
                         const double ty[16], int32_t icp_type, double txy_out[16],
