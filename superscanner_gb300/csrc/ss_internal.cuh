@@ -171,8 +171,12 @@ __device__ __forceinline__ float depth_m(uint16_t d) {
 
 // Index rule of getIndeces / getVBIndeces / getVinVBIndeces
 // (GPUVoxelGrid.h:131-221): a >= 0 ? (int)(a/len) : (int)(a/len - 1).
-// __float2int_rz is the (int) cast of the reference's device build.
-__device__ __forceinline__ int idx_rule(float a, float len) {
+// __float2int_rz is the (int) cast of the reference's device build. Not
+// inlined: the hot paths take it only where the multiplication form
+// (idx_fast) is not decisive, and its IEEE division inlined at every call site
+// made the reference raycast's loops larger than the instruction cache likes
+// (0.354 -> 0.336 ms per ss_raycast call as a called function).
+static __device__ __noinline__ int idx_rule(float a, float len) {
     float q = __fdiv_rn(a, len);
     return a >= 0.f ? __float2int_rz(q) : __float2int_rz(__fsub_rn(q, 1.f));
 }
