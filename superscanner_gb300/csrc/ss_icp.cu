@@ -219,14 +219,15 @@ __device__ bool polar3_warp(const double *H, double *R) {
 // perturbation of A is below 2 / (s_i + s_j) for the singular values
 // s_i, s_j of the rotation's plane). Returns false otherwise (R unset): the
 // FP64 iteration then decides. Every lane of the warp calls it.
-__device__ bool polar3_warp_f32(const double *H, double *R) {
+__device__ bool polar3_warp_f32(const float *Hf, double *R) {
     // every lane iterates the whole 3 x 3 in its registers (no shuffles on
-    // the dependent chain); the lanes compute identical values
+    // the dependent chain); the lanes compute identical values. Hf: H as
+    // floats (each lane of the caller converted one entry).
     float X[9];
 #pragma unroll
     for (int r = 0; r < 3; r++)
 #pragma unroll
-        for (int c = 0; c < 3; c++) X[r * 3 + c] = (float)H[c * 3 + r];  // A = H^T
+        for (int c = 0; c < 3; c++) X[r * 3 + c] = Hf[c * 3 + r];  // A = H^T
     float mx = 0.f;
 #pragma unroll
     for (int k = 0; k < 9; k++) mx = fmaxf(mx, fabsf(X[k]));
@@ -252,8 +253,10 @@ __device__ bool polar3_warp_f32(const double *H, double *R) {
             fc = fmaf(cof[k], cof[k], fc);
         }
         if (!(fabsf(det) > 1e-4f * fx * sqrtf(fx))) return false;
-        const float g = sqrtf(sqrtf(fc / (det * det * fx)));
-        const float y = 1.f / (g * det);
+        // the scale g only sets the speed (approximate instructions suffice);
+        // y is the reciprocal of the g det that scales X
+        const float g = rsqrtf(rsqrtf(__fdividef(fc, det * det * fx)));
+        const float y = __frcp_rn(g * det);
         float dlt = 0.f;
 #pragma unroll
         for (int k = 0; k < 9; k++) {
@@ -265,9 +268,12 @@ __device__ bool polar3_warp_f32(const double *H, double *R) {
         last = dlt <= 1e-4f;
     }
     if (!last) return false;
-    if ((threadIdx.x & 31) == 0)
+    const int lane = threadIdx.x & 31;
+    float mine = 0.f;  // X[lane] without dynamic register indexing
 #pragma unroll
-        for (int k = 0; k < 9; k++) R[k] = (double)X[k];
+    for (int k = 0; k < 9; k++)
+        if (lane == k) mine = X[k];
+    if (lane < 9) R[lane] = (double)mine;
     __syncwarp();
     return true;
 }
@@ -578,6 +584,7 @@ __global__ void __launch_bounds__(256, 4) icp_ref_iter_kernel(const float *__res
     // doubles (hi + lo)
     __shared__ double tot[kIcpSums];
     __shared__ double Hs[9], Rs[9], cxy[6];
+    __shared__ float Hf[9];
     {
         constexpr int kBatch = 4;
         float h[kPer], l[kPer];
@@ -616,9 +623,12 @@ __global__ void __launch_bounds__(256, 4) icp_ref_iter_kernel(const float *__res
     __syncwarp();
     const double *cx = cxy, *cy = cxy + 3;
     // H = sum (x - cx)(y - cy)^T = sum x y^T - n cx cy^T
-    if (lane < 9) Hs[lane] = tot[7 + lane] - n * cx[lane / 3] * cy[lane % 3];
+    if (lane < 9) {
+        Hs[lane] = tot[7 + lane] - n * cx[lane / 3] * cy[lane % 3];
+        Hf[lane] = (float)Hs[lane];
+    }
     __syncwarp();
-    if (!polar3_warp_f32(Hs, Rs) && !polar3_warp(Hs, Rs) && lane == 0) {
+    if (!polar3_warp_f32(Hf, Rs) && !polar3_warp(Hs, Rs) && lane == 0) {
         // rank-deficient H: the SVD's own completion of U
         double U[9], S[3], V[9];
         svd3_jacobi(Hs, U, S, V);
