@@ -80,7 +80,7 @@ typedef struct ss_grid ss_grid;
  * row); persistent kernels run ctas_per_sm x SM-count CTAs of 256 threads. */
 typedef struct ss_launch_config {
     int32_t collect_rows;       /* block collection tile rows, 1..8 (default 8) */
-    int32_t raycast_rows;       /* model-view raycast tile rows, 1..8 (default 8) */
+    int32_t raycast_rows;       /* model-view raycast tile rows, 1..16 (default 8) */
     int32_t fuse_ctas_per_sm;   /* integrate / deintegrate, 1..32 (default 8) */
     int32_t refuse_ctas_per_sm; /* batched re-fusion apply, 1..32 (default 8) */
     int32_t track_ctas_per_sm;  /* persistent tracker, 1..2, capped by occupancy (default 2) */

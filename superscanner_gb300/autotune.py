@@ -18,7 +18,7 @@ from .pipeline import Pipeline
 from .voxel_grid import GPUVoxelGrid
 
 CANDIDATES = {
-    "raycast_rows": (2, 4, 8),
+    "raycast_rows": (2, 4, 8, 16),
     "collect_rows": (2, 4, 8),
     "fuse_ctas_per_sm": (4, 8, 16),
     "track_ctas_per_sm": (1, 2),

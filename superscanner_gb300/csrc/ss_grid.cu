@@ -489,7 +489,7 @@ ss_status ss_grid_get_launch_config(const ss_grid *g, ss_launch_config *c) {
 
 ss_status ss_grid_set_launch_config(ss_grid *g, const ss_launch_config *c) {
     if (!g || !c) return SS_ERR_ARG;
-    if (c->collect_rows < 1 || c->collect_rows > 8 || c->raycast_rows < 1 || c->raycast_rows > 8 ||
+    if (c->collect_rows < 1 || c->collect_rows > 8 || c->raycast_rows < 1 || c->raycast_rows > 16 ||
         c->fuse_ctas_per_sm < 1 || c->fuse_ctas_per_sm > 32 || c->refuse_ctas_per_sm < 1 ||
         c->refuse_ctas_per_sm > 32 || c->track_ctas_per_sm < 1 || c->track_ctas_per_sm > 2)
         return SS_ERR_ARG;

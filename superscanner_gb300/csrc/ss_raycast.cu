@@ -316,7 +316,7 @@ extern "C" int ss_debug_raycast_timing(unsigned long long *out, int reset) {
 #endif
 
 template <int kStorage>
-__global__ void __launch_bounds__(256, 4) raycast_maps_kernel(GridView g, Mat34 T, const FramePose *__restrict__ pose,
+__global__ void __launch_bounds__(512, 2) raycast_maps_kernel(GridView g, Mat34 T, const FramePose *__restrict__ pose,
                                                            int max_steps, float t_min, float t_max,
                                                            float4 *__restrict__ vmap, float4 *__restrict__ nmap,
                                                            unsigned long long *__restrict__ counters,

@@ -262,3 +262,23 @@ def test_host_frames_and_pose_readback():
         pipe.close()
         g.close()
     assert np.array_equal(poses["host"], poses["device"])
+
+
+def test_raycast_tile_rows_do_not_change_the_maps():
+    """The model-view raycast's tile height (autotuned, 1..16 rows) changes
+    only the launch shape: every ray, and the dropout fallback of its 32-pixel
+    row segment, is the same, so the maps are bit-identical."""
+    P, depth = seq(4, 2)
+    g = GPUVoxelGrid(int(1e9), TRUNC, VL, 480, 640, storage="f16", with_color=False, hash_buckets=1 << 18,
+                     max_weight=255)
+    g.setIntrinsic(*INTR)
+    for k in range(4):
+        g.integrate_fast(dev(depth[k]), P[k].astype(np.float32))
+    out = {}
+    for rows in (2, 8, 16):
+        g.set_launch_config(raycast_rows=rows)
+        v, n = raycast_maps(g, P[3].astype(np.float32), hint_depth=dev(depth[3]), hint_margin=0.04)
+        g.sync()
+        out[rows] = (v.cpu().numpy(), n.cpu().numpy())
+    for rows in (2, 16):
+        assert np.array_equal(out[rows][0], out[8][0]) and np.array_equal(out[rows][1], out[8][1])
