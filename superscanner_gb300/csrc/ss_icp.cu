@@ -296,7 +296,7 @@ __device__ __forceinline__ void fp2_add(float &h, float &l, float h2, float l2) 
 // The CTA's 18 sums: each lane's pairs, a warp transpose-reduce (at offset o a
 // lane keeps the half of its values selected by lane bit o and adds the other
 // lane's; after offsets 16..1 lane v holds the warp's pair of value v), then
-// the warps' pairs in a fixed order; thread v < kIcpSums returns the CTA's
+// the warps' pairs by a fixed tree; thread v < kIcpSums returns the CTA's
 // pair of value v.
 __device__ __forceinline__ float2 icp_cta_sum(float *vh, float *vl, float2 (*red)[kIcpSums]) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -316,8 +316,17 @@ __device__ __forceinline__ float2 icp_cta_sum(float *vh, float *vl, float2 (*red
     if (lane < kIcpSums) red[wid][lane] = make_float2(vh[0], vl[0]);
     __syncthreads();
     float h = 0.f, l = 0.f;
-    if (threadIdx.x < kIcpSums)
-        for (int w = 0; w < (int)(blockDim.x >> 5); w++) fp2_add(h, l, red[w][threadIdx.x].x, red[w][threadIdx.x].y);
+    if (threadIdx.x < kIcpSums) {  // the eight warps' pairs by a tree, three additions deep
+        float2 p[8];
+#pragma unroll
+        for (int w = 0; w < 8; w++) p[w] = red[w][threadIdx.x];
+#pragma unroll
+        for (int st = 1; st < 8; st <<= 1)
+#pragma unroll
+            for (int w = 0; w < 8; w += 2 * st) fp2_add(p[w].x, p[w].y, p[w + st].x, p[w + st].y);
+        h = p[0].x;
+        l = p[0].y;
+    }
     return make_float2(h, l);
 }
 

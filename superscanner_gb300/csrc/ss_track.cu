@@ -295,8 +295,8 @@ __device__ __forceinline__ void track_accumulate_cam(const float4 (*cam)[256], i
 // each lane keeps the half of its remaining values selected by lane bit o and
 // trades the other half with lane ^ o, adding with TwoSum, so after offsets
 // 16, 8, 4, 2, 1 lane l holds the warp's pair of value l (31 exchanges per
-// lane instead of 5 per value). Warps then combine through shared memory in a
-// fixed order.
+// lane instead of 5 per value). Warps then combine through shared memory by a
+// fixed tree (eight warps: three additions deep).
 __device__ __forceinline__ float2 track_cta_pairs(float *s, float *c, float2 (*red)[kTrackSums]) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     float vs[32], vc[32];
@@ -321,8 +321,21 @@ __device__ __forceinline__ float2 track_cta_pairs(float *s, float *c, float2 (*r
     if (lane < kTrackSums) red[wid][lane] = make_float2(vs[0], vc[0]);
     __syncthreads();
     float a = 0.f, b = 0.f;
-    if (threadIdx.x < kTrackSums)
-        for (int w = 0; w < (int)(blockDim.x >> 5); w++) pair_add(a, b, red[w][threadIdx.x].x, red[w][threadIdx.x].y);
+    if (threadIdx.x < kTrackSums) {
+        if (blockDim.x == 256) {  // the eight warps' pairs by a tree, three additions deep
+            float2 p[8];
+#pragma unroll
+            for (int w = 0; w < 8; w++) p[w] = red[w][threadIdx.x];
+#pragma unroll
+            for (int st = 1; st < 8; st <<= 1)
+#pragma unroll
+                for (int w = 0; w < 8; w += 2 * st) pair_add(p[w].x, p[w].y, p[w + st].x, p[w + st].y);
+            a = p[0].x;
+            b = p[0].y;
+        } else {
+            for (int w = 0; w < (int)(blockDim.x >> 5); w++) pair_add(a, b, red[w][threadIdx.x].x, red[w][threadIdx.x].y);
+        }
+    }
     return make_float2(a, b);
 }
 
