@@ -384,8 +384,9 @@ def run_dropin(torch, depth_dev, P, W: int, K: int, stream, peak: float, host_pi
     the same with every frame uploaded from pinned host memory (e2e), per-call
     CUDA-event times, and the roofline of raycast_ref_kernel and
     icp_ref_iter_kernel (algorithmic bytes from the raycast's work counters and
-    the ICP's per-iteration image reads)."""
-    from superscanner_gb300 import GPUVoxelGrid, depth_to_pcd, kokkos_icp, normals_from_pcd, PointToPlane
+    the ICP's per-iteration image reads; the ICP's time per iteration is the
+    whole call's over its 10 iterations, an upper bound)."""
+    from superscanner_gb300 import GPUVoxelGrid, kokkos_icp, PointToPlane
     E = P.astype(np.float32)
     npix = ROWS * COLS
 
@@ -440,16 +441,6 @@ def run_dropin(torch, depth_dev, P, W: int, K: int, stream, peak: float, host_pi
         torch.cuda.synchronize()
         rc1 = g.raycast_counters(stream)
         per = np.array([[e[0].elapsed_time(e[1]), e[1].elapsed_time(e[2]), e[2].elapsed_time(e[3])] for e in evs])
-        # the ICP call's point-cloud / normal kernels, timed alone on the same frames
-        pe = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
-        pe[0].record(stream)
-        for k in range(1 + W, 1 + W + K):
-            x = depth_to_pcd(depth_dev[k], *INTR, stream=stream)
-            y = depth_to_pcd(depth_dev[k - 1], *INTR, stream=stream)
-            normals_from_pcd(y, stream=stream)
-        pe[1].record(stream)
-        torch.cuda.synchronize()
-        prep_ms = pe[0].elapsed_time(pe[1]) / K
     g.close()
     m = per.mean(axis=0)
     out["ms_per_call"] = {"integrate": round(float(m[0]), 4), "raycast": round(float(m[1]), 4),
@@ -457,13 +448,15 @@ def run_dropin(torch, depth_dev, P, W: int, K: int, stream, peak: float, host_pi
     finds = (rc1["finds"] - rc0["finds"]) / K
     voxels = (rc1["voxels"] - rc0["voxels"]) / K
     ray_bytes = finds * 8 + voxels * 8 + 12 * npix  # 8-byte keys, float2 (sdf, w), float3 points
-    icp_iter_ms = max(float(m[2]) - prep_ms, 1e-6) / 10
+    # per iteration: the whole call over its 10 iterations (its point-cloud /
+    # normal kernel and state copies included: an upper bound on the kernel's time)
+    icp_iter_ms = float(m[2]) / 10
     icp_bytes = 36 * npix  # per iteration: source points, target points and normals (12 B each)
     roof = {}
     for name, b, t, extra in (("raycast_ref_kernel", ray_bytes, float(m[1]), {"finds_per_frame": round(finds),
                                                                              "voxel_reads_per_frame": round(voxels)}),
                               ("icp_ref_iter_kernel", icp_bytes, icp_iter_ms,
-                               {"launches_per_frame": 10, "pcd_and_normal_kernels_ms": round(prep_ms, 4)})):
+                               {"launches_per_frame": 10, "ms_per_launch_from": "ss_kokkos_icp call / 10"})):
         gbs = b / (t * 1e-3) / 1e9
         roof[name] = {"bytes_per_launch": int(b), "ms_per_launch": round(t, 5), "achieved_gbs": round(gbs, 1),
                       "frac": round(gbs / peak, 4), **extra}

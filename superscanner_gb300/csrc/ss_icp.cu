@@ -57,6 +57,47 @@ __global__ void normals_kernel(const float *__restrict__ pcd, int rows, int cols
     out[p * 3 + 2] = n.z;
 }
 
+// depth_to_pcd_kernel for both of kokkosICP's depth images and normals_kernel
+// for the second, in one launch: a pixel's column and row quotients of
+// getPoint are shared by its points, and its neighbours' points are
+// recomputed from their depths with the same roundings, so the three images
+// equal those of the three separate launches bit for bit.
+__global__ void icp_prep_kernel(const uint16_t *__restrict__ d1, const uint16_t *__restrict__ d2, int rows, int cols,
+                                Intr in, float *__restrict__ xp, float *__restrict__ yp, float *__restrict__ yn) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y;
+    if (j >= cols || i >= rows) return;
+    const size_t p = (size_t)i * cols + j;
+    const float qx = __fdiv_rn(__fsub_rn((float)j, in.cj), in.fx), qy = __fdiv_rn(__fsub_rn((float)i, in.ci), in.fy);
+    auto pt = [](float ux, float uy, float d) { return F3{__fmul_rn(ux, d), __fmul_rn(uy, d), d}; };
+    const F3 x = pt(qx, qy, depth_m(__ldg(d1 + p)));
+    const F3 c = pt(qx, qy, depth_m(__ldg(d2 + p)));
+    xp[p * 3 + 0] = x.x;
+    xp[p * 3 + 1] = x.y;
+    xp[p * 3 + 2] = x.z;
+    yp[p * 3 + 0] = c.x;
+    yp[p * 3 + 1] = c.y;
+    yp[p * 3 + 2] = c.z;
+    F3 n{0.f, 0.f, 1.f};
+    if (i >= 1 && i < rows - 1 && j >= 1 && j < cols - 1) {
+        const float qxl = __fdiv_rn(__fsub_rn((float)(j - 1), in.cj), in.fx);
+        const float qxr = __fdiv_rn(__fsub_rn((float)(j + 1), in.cj), in.fx);
+        const float qyd = __fdiv_rn(__fsub_rn((float)(i - 1), in.ci), in.fy);
+        const float qyu = __fdiv_rn(__fsub_rn((float)(i + 1), in.ci), in.fy);
+        const F3 up = pt(qx, qyu, depth_m(__ldg(d2 + p + cols))), dn = pt(qx, qyd, depth_m(__ldg(d2 + p - cols)));
+        const F3 rt = pt(qxr, qy, depth_m(__ldg(d2 + p + 1))), lf = pt(qxl, qy, depth_m(__ldg(d2 + p - 1)));
+        if (c.z != 0 && up.z != 0 && dn.z != 0 && rt.z != 0 && lf.z != 0) {  // as normals_kernel
+            const F3 n1 = f3cross(f3sub(up, c), f3sub(rt, c));
+            const F3 n2 = f3cross(f3sub(lf, c), f3sub(up, c));
+            const F3 n3 = f3cross(f3sub(rt, c), f3sub(dn, c));
+            const F3 n4 = f3cross(f3sub(dn, c), f3sub(lf, c));
+            n = f3normalized(f3add(f3add(f3add(n1, n2), n3), n4));
+        }
+    }
+    yn[p * 3 + 0] = n.x;
+    yn[p * 3 + 1] = n.y;
+    yn[p * 3 + 2] = n.z;
+}
+
 // ----------------------------------------------------------------- kokkosICP
 constexpr int kIcpSums = 18;  // n_cors, sum x (3), sum y (3), sum x y^T (9), sum tmp^2, n_x
 constexpr int kIcpIters = 10; // n_it (kokkosICP.cpp:54)
@@ -779,9 +820,7 @@ ss_status icp_ref_run(const uint16_t *d1, const uint16_t *d2, int rows, int cols
                       const double ty[16], int type, float *xp, float *yp, float *yn, double *partials, int ctas,
                       IcpState *state, double txy_out[16], float *rmse_out, cudaStream_t s) {
     const dim3 blk(128), grid((cols + 127) / 128, rows);
-    depth_to_pcd_kernel<<<grid, blk, 0, s>>>(d1, rows, cols, in, xp);
-    depth_to_pcd_kernel<<<grid, blk, 0, s>>>(d2, rows, cols, in, yp);
-    normals_kernel<<<grid, blk, 0, s>>>(yp, rows, cols, yn);
+    icp_prep_kernel<<<grid, blk, 0, s>>>(d1, d2, rows, cols, in, xp, yp, yn);
     SS_LAUNCH_CHECK();
     // Txy = ty^-1 * tx (kokkosICP.cpp:57), float copy for the search
     double tyi[16], T[16];
@@ -815,14 +854,15 @@ ss_status icp_ref_run(const uint16_t *d1, const uint16_t *d2, int rows, int cols
                              (int)cudaSharedmemCarveoutMaxShared);
     cudaGetLastError();
     // programmatic dependent launches: an iteration's CTAs start while the
-    // previous one's last CTA forms the transform
+    // previous one's last CTA forms the transform (not the first: it loads the
+    // source points that the launch before it writes before it waits)
     for (int it = 0; it < kIcpIters; it++) {
         if (type == SS_ICP_POINT_TO_POINT)
-            SS_CUDA_TRY(launch_kernel(icp_ref_iter_kernel<SS_ICP_POINT_TO_POINT>, tiles, dim3(256), 0, s, true, xp, yp, yn,
-                                      rows, cols, in, state, slots, gsz));
+            SS_CUDA_TRY(launch_kernel(icp_ref_iter_kernel<SS_ICP_POINT_TO_POINT>, tiles, dim3(256), 0, s, it > 0, xp, yp,
+                                      yn, rows, cols, in, state, slots, gsz));
         else
-            SS_CUDA_TRY(launch_kernel(icp_ref_iter_kernel<SS_ICP_POINT_TO_PLANE>, tiles, dim3(256), 0, s, true, xp, yp, yn,
-                                      rows, cols, in, state, slots, gsz));
+            SS_CUDA_TRY(launch_kernel(icp_ref_iter_kernel<SS_ICP_POINT_TO_PLANE>, tiles, dim3(256), 0, s, it > 0, xp, yp,
+                                      yn, rows, cols, in, state, slots, gsz));
     }
     SS_CUDA_TRY(cudaMemcpyAsync(&h, state, sizeof(h), cudaMemcpyDeviceToHost, s));
     SS_CUDA_TRY(cudaStreamSynchronize(s));
