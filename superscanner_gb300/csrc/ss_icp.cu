@@ -61,9 +61,15 @@ __global__ void normals_kernel(const float *__restrict__ pcd, int rows, int cols
 // for the second, in one launch: a pixel's column and row quotients of
 // getPoint are shared by its points, and its neighbours' points are
 // recomputed from their depths with the same roundings, so the three images
-// equal those of the three separate launches bit for bit.
+// equal those of the three separate launches bit for bit. The source points
+// go out as float triples; the target point and normal of a pixel as one
+// 16-byte (x, y, z, nx) and one 8-byte (ny, nz) entry, the layout the
+// iteration kernel stages in shared memory, x holding NaN where the
+// reference's search skips the tap (py.z == 0, or n.x == 0 point-to-plane:
+// kokkosICP.cpp:89,100) so that its distance fails every comparison.
 __global__ void icp_prep_kernel(const uint16_t *__restrict__ d1, const uint16_t *__restrict__ d2, int rows, int cols,
-                                Intr in, float *__restrict__ xp, float *__restrict__ yp, float *__restrict__ yn) {
+                                Intr in, int type, float *__restrict__ xp, float4 *__restrict__ ya,
+                                float2 *__restrict__ yb) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y;
     if (j >= cols || i >= rows) return;
     const size_t p = (size_t)i * cols + j;
@@ -74,9 +80,6 @@ __global__ void icp_prep_kernel(const uint16_t *__restrict__ d1, const uint16_t 
     xp[p * 3 + 0] = x.x;
     xp[p * 3 + 1] = x.y;
     xp[p * 3 + 2] = x.z;
-    yp[p * 3 + 0] = c.x;
-    yp[p * 3 + 1] = c.y;
-    yp[p * 3 + 2] = c.z;
     F3 n{0.f, 0.f, 1.f};
     if (i >= 1 && i < rows - 1 && j >= 1 && j < cols - 1) {
         const float qxl = __fdiv_rn(__fsub_rn((float)(j - 1), in.cj), in.fx);
@@ -93,10 +96,20 @@ __global__ void icp_prep_kernel(const uint16_t *__restrict__ d1, const uint16_t 
             n = f3normalized(f3add(f3add(f3add(n1, n2), n3), n4));
         }
     }
-    yn[p * 3 + 0] = n.x;
-    yn[p * 3 + 1] = n.y;
-    yn[p * 3 + 2] = n.z;
+    const bool tap = c.z != 0 && (type == SS_ICP_POINT_TO_POINT || n.x != 0);
+    ya[p] = make_float4(tap ? c.x : __int_as_float(0x7fc00000), c.y, c.z, n.x);
+    yb[p] = make_float2(n.y, n.z);
 }
+
+// 16- and 8-byte asynchronous copies from global to shared memory (no
+// registers held while they are in flight).
+__device__ __forceinline__ void cp_async16(unsigned dst, const void *src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async8(unsigned dst, const void *src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
 // ----------------------------------------------------------------- kokkosICP
 constexpr int kIcpSums = 18;  // n_cors, sum x (3), sum y (3), sum x y^T (9), sum tmp^2, n_x
@@ -379,17 +392,18 @@ constexpr int kIcpStage = 1536;
 // One kokkosICP iteration: Closest Point Kernel (kokkosICP.cpp:69-115) fused
 // with the host sums (:121-171) and, in the last CTA, the rotation update
 // (:173-185). One thread per source pixel of a 32 x 8 tile. The target points
-// and normals under the tile's windows are staged in shared memory first, a
-// tap that the reference skips (py.z == 0, or n.x == 0 point-to-plane) holding
-// NaN so that its distance fails every comparison; the search then keeps the
+// and normals under the tile's windows are staged in shared memory first by
+// asynchronous copies of icp_prep_kernel's entries (a tap that the reference
+// skips holding NaN, so that its distance fails every comparison); the search then keeps the
 // reference's scan order and strict comparisons (starting from max_dist: the
 // accepted taps of `dist < smallest && dist < max_dist` are exactly those of
 // `dist < min(smallest, max_dist)`), remembers the best tap and forms the
 // correspondence from it afterwards. 64 registers (four CTAs per SM; only the
 // rank-deficient fallback of the last CTA spills).
 template <int kType>
-__global__ void __launch_bounds__(256, 4) icp_ref_iter_kernel(const float *__restrict__ xp, const float *__restrict__ yp,
-                                                           const float *__restrict__ yn, int rows, int cols, Intr in,
+__global__ void __launch_bounds__(256, 4) icp_ref_iter_kernel(const float *__restrict__ xp,
+                                                           const float4 *__restrict__ ya,
+                                                           const float2 *__restrict__ yb, int rows, int cols, Intr in,
                                                            IcpState *st, float2 *partials, int gsz) {
     __shared__ float4 sA[kIcpStage];  // target (x, y, z, nx)
     __shared__ float2 sB[kIcpStage];  // target (ny, nz)
@@ -449,33 +463,20 @@ __global__ void __launch_bounds__(256, 4) icp_ref_iter_kernel(const float *__res
     const int W = any ? box[3] + n_search - q0 : 0, H = any ? box[1] + n_search - r0 : 0;
     const bool staged = any && W * H <= kIcpStage;
     if (staged) {
-        // inside the image: the border test keeps every window within rows x cols.
-        // Three entries per thread and round: their loads are issued before the first store.
-        constexpr int kStageRound = 3;
-        for (int t0 = threadIdx.x; t0 < W * H; t0 += kStageRound * blockDim.x) {
-            F3 py[kStageRound], nn[kStageRound];
-#pragma unroll
-            for (int u = 0; u < kStageRound; u++) {
-                const int t = t0 + u * (int)blockDim.x;
-                py[u] = F3{0.f, 0.f, 0.f};
-                nn[u] = F3{0.f, 0.f, 0.f};
-                if (t < W * H) {
-                    const size_t q = (size_t)(r0 + t / W) * cols + (q0 + t % W);
-                    py[u] = ld3(yp, q);
-                    if (kType == SS_ICP_POINT_TO_PLANE) nn[u] = ld3(yn, q);
-                }
-            }
-#pragma unroll
-            for (int u = 0; u < kStageRound; u++) {
-                const int t = t0 + u * (int)blockDim.x;
-                if (t >= W * H) break;
-                bool ok = py[u].z != 0;
-                if (kType == SS_ICP_POINT_TO_PLANE) ok = ok && nn[u].x != 0;
-                const float px0 = ok ? py[u].x : __int_as_float(0x7fc00000);
-                sA[t] = make_float4(px0, py[u].y, py[u].z, nn[u].x);
-                sB[t] = make_float2(nn[u].y, nn[u].z);
+        // inside the image (the border test keeps every window within rows x
+        // cols): warp w copies rows w, w + 8, ... of the region, its lanes the
+        // columns, the entries in the layout icp_prep_kernel wrote them in
+        const unsigned sa = (unsigned)__cvta_generic_to_shared(sA), sb = (unsigned)__cvta_generic_to_shared(sB);
+        const int ln = threadIdx.x & 31;
+        for (int r = threadIdx.x >> 5; r < H; r += 8) {
+            const size_t q = (size_t)(r0 + r) * cols + q0;
+            for (int c = ln; c < W; c += 32) {
+                const int t = r * W + c;
+                cp_async16(sa + 16u * t, ya + q + c);
+                if (kType == SS_ICP_POINT_TO_PLANE) cp_async8(sb + 8u * t, yb + q + c);
             }
         }
+        cp_async_wait_all();
     }
     __syncthreads();
 
@@ -535,13 +536,9 @@ __global__ void __launch_bounds__(256, 4) icp_ref_iter_kernel(const float *__res
             for (int k = ci - n_search; k < ci + n_search; k++) {
                 for (int l = cj - n_search; l < cj + n_search; l++) {
                     const int tag = k * cols + l;
-                    F3 py = ld3(yp, (size_t)tag), nn{0.f, 0.f, 0.f};
-                    bool ok = py.z != 0;
-                    if (kType == SS_ICP_POINT_TO_PLANE) {
-                        nn = ld3(yn, (size_t)tag);
-                        ok = ok && nn.x != 0;
-                    }
-                    if (!ok) py.x = __int_as_float(0x7fc00000);
+                    const float4 a = __ldg(ya + tag);
+                    const float2 b = kType == SS_ICP_POINT_TO_PLANE ? __ldg(yb + tag) : make_float2(0.f, 0.f);
+                    const F3 py{a.x, a.y, a.z}, nn{a.w, b.x, b.y};
                     const float dist = kType == SS_ICP_POINT_TO_POINT ? f3len(f3sub(py, px))
                                                                       : fabsf(f3dot(f3sub(py, px), nn));
                     if (dist < smallest) {
@@ -559,8 +556,12 @@ __global__ void __launch_bounds__(256, 4) icp_ref_iter_kernel(const float *__res
                 py = F3{a.x, a.y, a.z};
                 nn = F3{a.w, b.x, b.y};
             } else {
-                py = ld3(yp, (size_t)best);
-                if (kType == SS_ICP_POINT_TO_PLANE) nn = ld3(yn, (size_t)best);
+                const float4 a = __ldg(ya + best);
+                py = F3{a.x, a.y, a.z};
+                if (kType == SS_ICP_POINT_TO_PLANE) {
+                    const float2 b = __ldg(yb + best);
+                    nn = F3{a.w, b.x, b.y};
+                }
             }
             const F3 bpt = kType == SS_ICP_POINT_TO_POINT ? py : f3add(px, f3smul(f3dot(f3sub(py, px), nn), nn));
             if (bpt.z != 0) {  // x_nearest(i, j).z != 0: a correspondence (kokkosICP.cpp:131)
@@ -724,7 +725,9 @@ static inline int icp_tiles_y(int rows) { return (rows + 7) / 8; }
 
 // Scratch of ss_kokkos_icp, one per device, grown on demand.
 struct IcpWorkspace {
-    float *xp = nullptr, *yp = nullptr, *yn = nullptr;
+    float *xp = nullptr;
+    float4 *ya = nullptr;
+    float2 *yb = nullptr;
     double *partials = nullptr;
     IcpState *state = nullptr;
     size_t npix = 0;
@@ -738,12 +741,14 @@ static ss_status icp_workspace(int dev, size_t npix, int ctas, IcpWorkspace **ou
     IcpWorkspace &w = g_icp_ws[dev];
     if (w.npix < npix) {
         cudaFree(w.xp);
-        cudaFree(w.yp);
-        cudaFree(w.yn);
-        w.xp = w.yp = w.yn = nullptr;
+        cudaFree(w.ya);
+        cudaFree(w.yb);
+        w.xp = nullptr;
+        w.ya = nullptr;
+        w.yb = nullptr;
         w.npix = 0;
-        if (cudaMalloc(&w.xp, npix * 12) != cudaSuccess || cudaMalloc(&w.yp, npix * 12) != cudaSuccess ||
-            cudaMalloc(&w.yn, npix * 12) != cudaSuccess) {
+        if (cudaMalloc(&w.xp, npix * 12) != cudaSuccess || cudaMalloc(&w.ya, npix * 16) != cudaSuccess ||
+            cudaMalloc(&w.yb, npix * 8) != cudaSuccess) {
             cudaGetLastError();
             return SS_ERR_NOMEM;
         }
@@ -817,10 +822,10 @@ static void orthonormalize_rotation(double *T) {
 
 // Runs the 10 iterations on prepared point clouds; shared by the entry points.
 ss_status icp_ref_run(const uint16_t *d1, const uint16_t *d2, int rows, int cols, Intr in, const double tx[16],
-                      const double ty[16], int type, float *xp, float *yp, float *yn, double *partials, int ctas,
+                      const double ty[16], int type, float *xp, float4 *ya, float2 *yb, double *partials, int ctas,
                       IcpState *state, double txy_out[16], float *rmse_out, cudaStream_t s) {
     const dim3 blk(128), grid((cols + 127) / 128, rows);
-    icp_prep_kernel<<<grid, blk, 0, s>>>(d1, d2, rows, cols, in, xp, yp, yn);
+    icp_prep_kernel<<<grid, blk, 0, s>>>(d1, d2, rows, cols, in, type, xp, ya, yb);
     SS_LAUNCH_CHECK();
     // Txy = ty^-1 * tx (kokkosICP.cpp:57), float copy for the search
     double tyi[16], T[16];
@@ -858,11 +863,11 @@ ss_status icp_ref_run(const uint16_t *d1, const uint16_t *d2, int rows, int cols
     // source points that the launch before it writes before it waits)
     for (int it = 0; it < kIcpIters; it++) {
         if (type == SS_ICP_POINT_TO_POINT)
-            SS_CUDA_TRY(launch_kernel(icp_ref_iter_kernel<SS_ICP_POINT_TO_POINT>, tiles, dim3(256), 0, s, it > 0, xp, yp,
-                                      yn, rows, cols, in, state, slots, gsz));
+            SS_CUDA_TRY(launch_kernel(icp_ref_iter_kernel<SS_ICP_POINT_TO_POINT>, tiles, dim3(256), 0, s, it > 0, xp, ya,
+                                      yb, rows, cols, in, state, slots, gsz));
         else
-            SS_CUDA_TRY(launch_kernel(icp_ref_iter_kernel<SS_ICP_POINT_TO_PLANE>, tiles, dim3(256), 0, s, it > 0, xp, yp,
-                                      yn, rows, cols, in, state, slots, gsz));
+            SS_CUDA_TRY(launch_kernel(icp_ref_iter_kernel<SS_ICP_POINT_TO_PLANE>, tiles, dim3(256), 0, s, it > 0, xp, ya,
+                                      yb, rows, cols, in, state, slots, gsz));
     }
     SS_CUDA_TRY(cudaMemcpyAsync(&h, state, sizeof(h), cudaMemcpyDeviceToHost, s));
     SS_CUDA_TRY(cudaStreamSynchronize(s));
@@ -890,9 +895,12 @@ static ss_status icp_check_args(const uint16_t *d1, const uint16_t *d2, int rows
 constexpr size_t kNoAllocMaxPixels = 640 * 480;  // largest rows * cols accepted
 constexpr int kNoAllocCtas = 4096;  // iteration-grid CTAs (32 x 8 tiles): any rows x cols <= 640 x 480 needs <= 3200
 constexpr size_t kAlign256(size_t n) { return (n + 255) / 256 * 256; }
-constexpr size_t kNoAllocImage = kAlign256(kNoAllocMaxPixels * 3 * sizeof(float));
+constexpr size_t kNoAllocSource = kAlign256(kNoAllocMaxPixels * 12);  // source points
+constexpr size_t kNoAllocTargetA = kAlign256(kNoAllocMaxPixels * 16);  // target (x, y, z, nx)
+constexpr size_t kNoAllocTargetB = kAlign256(kNoAllocMaxPixels * 8);   // target (ny, nz)
+constexpr size_t kNoAllocImages = kNoAllocSource + kNoAllocTargetA + kNoAllocTargetB;
 constexpr size_t kNoAllocPartials = kAlign256((size_t)(kNoAllocCtas + kIcpMaxGroups) * kIcpSums * 8);  // CTA and group slots
-constexpr size_t kNoAllocBytes = 3 * kNoAllocImage + kNoAllocPartials + kAlign256(sizeof(IcpState));
+constexpr size_t kNoAllocBytes = kNoAllocImages + kNoAllocPartials + kAlign256(sizeof(IcpState));
 
 static __device__ __align__(256) unsigned char g_icp_noalloc_scratch[kNoAllocBytes];
 
@@ -956,11 +964,13 @@ ss_status ss_kokkos_icp_noalloc(const uint16_t *d1, const uint16_t *d2, int32_t 
     unsigned char *base = nullptr;
     st = noalloc_scratch(dev, &base);
     if (st != SS_OK) return st;
-    float *xp = (float *)base, *yp = (float *)(base + kNoAllocImage), *yn = (float *)(base + 2 * kNoAllocImage);
-    double *partials = (double *)(base + 3 * kNoAllocImage);
-    IcpState *state = (IcpState *)(base + 3 * kNoAllocImage + kNoAllocPartials);
+    float *xp = (float *)base;
+    float4 *ya = (float4 *)(base + kNoAllocSource);
+    float2 *yb = (float2 *)(base + kNoAllocSource + kNoAllocTargetA);
+    double *partials = (double *)(base + kNoAllocImages);
+    IcpState *state = (IcpState *)(base + kNoAllocImages + kNoAllocPartials);
     const Intr in{fx, fy, (float)rows - cy, cx};
-    return icp_ref_run(d1, d2, rows, cols, in, tx, ty, icp_type, xp, yp, yn, partials, ctas, state, txy_out,
+    return icp_ref_run(d1, d2, rows, cols, in, tx, ty, icp_type, xp, ya, yb, partials, ctas, state, txy_out,
                        rmse_out, (cudaStream_t)stream);
 }
 
@@ -994,7 +1004,7 @@ ss_status ss_kokkos_icp(const uint16_t *d1, const uint16_t *d2, int32_t rows, in
     st = icp_workspace(dev, (size_t)rows * cols, ctas, &w);
     if (st != SS_OK) return st;
     const Intr in{fx, fy, (float)rows - cy, cx};  // ci = resi - cy, cj = cx (kokkosICP.cpp:48-49)
-    return icp_ref_run(d1, d2, rows, cols, in, tx, ty, icp_type, w->xp, w->yp, w->yn, w->partials, ctas, w->state,
+    return icp_ref_run(d1, d2, rows, cols, in, tx, ty, icp_type, w->xp, w->ya, w->yb, w->partials, ctas, w->state,
                        txy_out, rmse_out, (cudaStream_t)stream);
 }
 
