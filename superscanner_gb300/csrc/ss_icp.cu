@@ -385,21 +385,152 @@ __device__ __forceinline__ float2 icp_cta_sum(float *vh, float *vl, float2 (*red
 }
 
 // Target pixels staged per CTA: a tile's 10 x 10 windows (kokkosICP.cpp:81-83)
-// usually fall inside a region of some 42 x 18 pixels; up to this many are
+// usually fall inside a region of some 42 x 26 pixels; up to this many are
 // staged, larger regions are read from global memory.
 constexpr int kIcpStage = 1536;
+constexpr int kIcpSearch = 5;         // n_search (kokkosICP.cpp:53)
+constexpr float kIcpMaxDist = 0.075f; // max_dist (kokkosICP.cpp:55)
+
+// The transformed source point px = Txy x and its window centre
+// (kokkosICP.cpp:72-76); true when the reference searches (x.z != 0 and the
+// window inside the image, :79).
+__device__ __forceinline__ bool icp_center(const Mat34 &T, F3 x, Intr in, int rows, int cols, F3 &px, int &ci,
+                                           int &cj) {
+    px = F3{0.f, 0.f, 0.f};
+    ci = cj = 0;
+    if (x.z == 0) return false;
+    px = xform(T, x);
+    const float c0 = __fadd_rn(__fdiv_rn(__fmul_rn(px.y, in.fy), px.z), in.ci);
+    const float c1 = __fadd_rn(__fdiv_rn(__fmul_rn(px.x, in.fx), px.z), in.cj);
+    ci = __float2int_rz(c0);
+    cj = __float2int_rz(c1);
+    return ci > kIcpSearch && ci < rows - kIcpSearch && cj > kIcpSearch && cj < cols - kIcpSearch;
+}
+
+// A tap's distance (kokkosICP.cpp:91,101-102) from its (x, y, z, nx) and
+// (ny, nz) entries; NaN for a tap the reference skips.
+template <int kType>
+__device__ __forceinline__ float icp_tap_dist(const float4 a, const float2 b, F3 px) {
+    const F3 py{a.x, a.y, a.z};
+    return kType == SS_ICP_POINT_TO_POINT ? f3len(f3sub(py, px)) : fabsf(f3dot(f3sub(py, px), F3{a.w, b.x, b.y}));
+}
+
+// The search state of one window: the even and the odd columns keep separate
+// minima (two independent compare chains) with their taps' indices (staged
+// or image indices, increasing in the window's scan order); the first tap of
+// the scan with the smallest distance is then the one of the smaller
+// minimum, on a tie the earlier tap. Starting from max_dist, the accepted
+// taps of `dist < smallest && dist < max_dist` are exactly those of
+// `dist < min(smallest, max_dist)`.
+struct IcpBest {
+    float s0 = kIcpMaxDist, s1 = kIcpMaxDist;
+    int b0 = -1, b1 = -1;
+    __device__ __forceinline__ void take(bool odd, float dist, int idx) {
+        if (odd) {
+            if (dist < s1) {
+                s1 = dist;
+                b1 = idx;
+            }
+        } else if (dist < s0) {
+            s0 = dist;
+            b0 = idx;
+        }
+    }
+    __device__ __forceinline__ int best() const { return (s1 < s0 || (s1 == s0 && b1 < b0)) ? b1 : b0; }
+};
+
+// One window row of staged taps [row, row + 10) for up to two windows that
+// contain it (a vertical pixel pair's windows share nine of their rows): a
+// half row's taps are loaded once, before their comparisons, and compared
+// with each window that uses the row.
+template <int kType>
+__device__ __forceinline__ void icp_scan_row(const float4 *sA, const float2 *sB, int row, F3 pa, bool ua, IcpBest &ba,
+                                             F3 pb, bool ub, IcpBest &bb) {
+#pragma unroll
+    for (int half = 0; half < 2; half++) {
+        float4 a[kIcpSearch];
+        float2 b[kIcpSearch];
+#pragma unroll
+        for (int dl = 0; dl < kIcpSearch; dl++) {
+            a[dl] = sA[row + half * kIcpSearch + dl];
+            b[dl] = kType == SS_ICP_POINT_TO_PLANE ? sB[row + half * kIcpSearch + dl] : make_float2(0.f, 0.f);
+        }
+#pragma unroll
+        for (int dl = 0; dl < kIcpSearch; dl++) {
+            const bool odd = ((dl + half * kIcpSearch) & 1) != 0;
+            const int idx = row + half * kIcpSearch + dl;
+            if (ua) ba.take(odd, icp_tap_dist<kType>(a[dl], b[dl], pa), idx);
+            if (ub) bb.take(odd, icp_tap_dist<kType>(a[dl], b[dl], pb), idx);
+        }
+    }
+}
+
+// A window read from global memory (a tile whose window region does not fit
+// the stage): image indices, the reference's loops.
+template <int kType>
+__device__ __forceinline__ int icp_search_global(const float4 *__restrict__ ya, const float2 *__restrict__ yb, int cols,
+                                                 int ci, int cj, F3 px) {
+    IcpBest bt;
+    for (int k = ci - kIcpSearch; k < ci + kIcpSearch; k++)
+        for (int l = cj - kIcpSearch; l < cj + kIcpSearch; l++) {
+            const int tag = k * cols + l;
+            const float2 b = kType == SS_ICP_POINT_TO_PLANE ? __ldg(yb + tag) : make_float2(0.f, 0.f);
+            bt.take(false, icp_tap_dist<kType>(__ldg(ya + tag), b, px), tag);
+        }
+    return bt.best();
+}
+
+// Adds one source pixel's terms of the host sums (kokkosICP.cpp:121-171) to
+// the lane's float pairs: for a correspondence (x_nearest.z != 0) the count,
+// x, x_nearest, x x_nearest^T (each product exact as a pair) and the RMSE
+// term. best indexes the staged region (staged) or the image.
+template <int kType>
+__device__ __forceinline__ void icp_add_terms(F3 x, const Mat34 &T, int best, bool staged, const float4 *sA,
+                                              const float2 *sB, const float4 *__restrict__ ya,
+                                              const float2 *__restrict__ yb, float *vh, float *vl) {
+    if (best < 0) return;
+    const F3 px = xform(T, x);
+    const float4 a = staged ? sA[best] : __ldg(ya + best);
+    const float2 b = kType == SS_ICP_POINT_TO_PLANE ? (staged ? sB[best] : __ldg(yb + best)) : make_float2(0.f, 0.f);
+    const F3 py{a.x, a.y, a.z}, nn{a.w, b.x, b.y};
+    const F3 bpt = kType == SS_ICP_POINT_TO_POINT ? py : f3add(px, f3smul(f3dot(f3sub(py, px), nn), nn));
+    if (bpt.z == 0) return;  // x_nearest(i, j).z == 0: no correspondence (kokkosICP.cpp:131)
+    const float xa[3] = {x.x, x.y, x.z}, xb[3] = {bpt.x, bpt.y, bpt.z};
+    fp2_add(vh[0], vl[0], 1.f, 0.f);
+#pragma unroll
+    for (int r = 0; r < 3; r++) {
+        fp2_add(vh[1 + r], vl[1 + r], xa[r], 0.f);
+        fp2_add(vh[4 + r], vl[4 + r], xb[r], 0.f);
+#pragma unroll
+        for (int c = 0; c < 3; c++) {  // x y^T, each product exact as a pair
+            const float q = __fmul_rn(xa[r], xb[c]);
+            fp2_add(vh[7 + 3 * r + c], vl[7 + 3 * r + c], q, fmaf(xa[r], xb[c], -q));
+        }
+    }
+    // RMSE term || x_nearest - Txy x || squared in float (kokkosICP.cpp:137-138; the
+    // reference evaluates the norm in double, this in FP32 with the float Txy)
+    const float e0 = xb[0] - fmaf(T.m[0], xa[0], fmaf(T.m[1], xa[1], fmaf(T.m[2], xa[2], T.m[3])));
+    const float e1 = xb[1] - fmaf(T.m[4], xa[0], fmaf(T.m[5], xa[1], fmaf(T.m[6], xa[2], T.m[7])));
+    const float e2 = xb[2] - fmaf(T.m[8], xa[0], fmaf(T.m[9], xa[1], fmaf(T.m[10], xa[2], T.m[11])));
+    const float tmp = sqrtf(fmaf(e0, e0, fmaf(e1, e1, e2 * e2)));
+    fp2_add(vh[16], vl[16], tmp * tmp, 0.f);
+}
 
 // One kokkosICP iteration: Closest Point Kernel (kokkosICP.cpp:69-115) fused
 // with the host sums (:121-171) and, in the last CTA, the rotation update
-// (:173-185). One thread per source pixel of a 32 x 8 tile. The target points
-// and normals under the tile's windows are staged in shared memory first by
-// asynchronous copies of icp_prep_kernel's entries (a tap that the reference
-// skips holding NaN, so that its distance fails every comparison); the search then keeps the
-// reference's scan order and strict comparisons (starting from max_dist: the
-// accepted taps of `dist < smallest && dist < max_dist` are exactly those of
-// `dist < min(smallest, max_dist)`), remembers the best tap and forms the
-// correspondence from it afterwards. 64 registers (four CTAs per SM; only the
-// rank-deficient fallback of the last CTA spills).
+// (:173-185). A CTA covers a 32 x 16 tile of source pixels, each thread a
+// vertical pair (rows 2w and 2w + 1 of warp w's lane column). The target
+// points and normals under the tile's windows are staged in shared memory
+// first by asynchronous copies of icp_prep_kernel's entries (a tap that the
+// reference skips holding NaN, so that its distance fails every comparison).
+// The search keeps the reference's scan order and strict comparisons for
+// each window, remembers the best tap and forms the correspondence from it
+// afterwards. When the two windows lie in the same columns at most two rows
+// apart (the usual case: neighbouring pixels project to neighbouring centres,
+// one row apart), the thread scans their union, loading each tap once for
+// both; otherwise it scans the lower window on its own after the upper one.
+// 64 registers (four CTAs per SM; only the rank-deficient fallback of the
+// last CTA spills).
 template <int kType>
 __global__ void __launch_bounds__(256, 4) icp_ref_iter_kernel(const float *__restrict__ xp,
                                                            const float4 *__restrict__ ya,
@@ -410,31 +541,21 @@ __global__ void __launch_bounds__(256, 4) icp_ref_iter_kernel(const float *__res
     __shared__ float2 red[8][kIcpSums];
     __shared__ int box[4];
     __shared__ bool last;
-    const int n_search = 5;
-    const float max_dist = 0.075f;
-    const int j = blockIdx.x * 32 + (threadIdx.x & 31), i = blockIdx.y * 8 + (threadIdx.x >> 5);
-    const size_t p = (size_t)i * cols + j;
-    const bool inside = i < rows && j < cols;
-    // the source point does not change between iterations (written before the
+    const int j = blockIdx.x * 32 + (threadIdx.x & 31), i0 = blockIdx.y * 16 + 2 * (threadIdx.x >> 5);
+    const size_t p0 = (size_t)i0 * cols + j, p1 = p0 + cols;
+    // the source points do not change between iterations (written before the
     // first one): loaded before this launch waits for the previous iteration,
     // whose last CTA is still forming Txy and reading the CTA slots
-    const F3 x = inside ? ld3(xp, p) : F3{0.f, 0.f, 0.f};
+    const F3 x0 = j < cols && i0 < rows ? ld3(xp, p0) : F3{0.f, 0.f, 0.f};
+    const F3 x1 = j < cols && i0 + 1 < rows ? ld3(xp, p1) : F3{0.f, 0.f, 0.f};
     pdl_wait();
     Mat34 T;
 #pragma unroll
     for (int k = 0; k < 12; k++) T.m[k] = st->Txy[k];
-    const bool has_x = x.z != 0;
-    F3 px{0.f, 0.f, 0.f};
-    int ci = 0, cj = 0;
-    bool search = false;
-    if (has_x) {
-        px = xform(T, x);
-        const float c0 = __fadd_rn(__fdiv_rn(__fmul_rn(px.y, in.fy), px.z), in.ci);
-        const float c1 = __fadd_rn(__fdiv_rn(__fmul_rn(px.x, in.fx), px.z), in.cj);
-        ci = __float2int_rz(c0);
-        cj = __float2int_rz(c1);
-        search = ci > n_search && ci < rows - n_search && cj > n_search && cj < cols - n_search;
-    }
+    F3 pa, pb;
+    int ca_i, ca_j, cb_i, cb_j;
+    const bool sa = icp_center(T, x0, in, rows, cols, pa, ca_i, ca_j);
+    const bool sb = icp_center(T, x1, in, rows, cols, pb, cb_i, cb_j);
     // the tile's window region [r0, r1) x [q0, q1)
     if (threadIdx.x == 0) {
         box[0] = INT_MAX;
@@ -444,8 +565,14 @@ __global__ void __launch_bounds__(256, 4) icp_ref_iter_kernel(const float *__res
     }
     __syncthreads();
     {
-        int lo_i = search ? ci : INT_MAX, hi_i = search ? ci : INT_MIN;
-        int lo_j = search ? cj : INT_MAX, hi_j = search ? cj : INT_MIN;
+        int lo_i = sa ? ca_i : INT_MAX, hi_i = sa ? ca_i : INT_MIN;
+        int lo_j = sa ? ca_j : INT_MAX, hi_j = sa ? ca_j : INT_MIN;
+        if (sb) {
+            lo_i = min(lo_i, cb_i);
+            hi_i = max(hi_i, cb_i);
+            lo_j = min(lo_j, cb_j);
+            hi_j = max(hi_j, cb_j);
+        }
         lo_i = __reduce_min_sync(0xffffffffu, lo_i);
         hi_i = __reduce_max_sync(0xffffffffu, hi_i);
         lo_j = __reduce_min_sync(0xffffffffu, lo_j);
@@ -459,135 +586,70 @@ __global__ void __launch_bounds__(256, 4) icp_ref_iter_kernel(const float *__res
     }
     __syncthreads();
     const bool any = box[0] != INT_MAX;
-    const int r0 = box[0] - n_search, q0 = box[2] - n_search;
-    const int W = any ? box[3] + n_search - q0 : 0, H = any ? box[1] + n_search - r0 : 0;
+    const int r0 = box[0] - kIcpSearch, q0 = box[2] - kIcpSearch;
+    const int W = any ? box[3] + kIcpSearch - q0 : 0, H = any ? box[1] + kIcpSearch - r0 : 0;
     const bool staged = any && W * H <= kIcpStage;
     if (staged) {
         // inside the image (the border test keeps every window within rows x
         // cols): warp w copies rows w, w + 8, ... of the region, its lanes the
         // columns, the entries in the layout icp_prep_kernel wrote them in
-        const unsigned sa = (unsigned)__cvta_generic_to_shared(sA), sb = (unsigned)__cvta_generic_to_shared(sB);
+        const unsigned sa_s = (unsigned)__cvta_generic_to_shared(sA), sb_s = (unsigned)__cvta_generic_to_shared(sB);
         const int ln = threadIdx.x & 31;
         for (int r = threadIdx.x >> 5; r < H; r += 8) {
             const size_t q = (size_t)(r0 + r) * cols + q0;
             for (int c = ln; c < W; c += 32) {
                 const int t = r * W + c;
-                cp_async16(sa + 16u * t, ya + q + c);
-                if (kType == SS_ICP_POINT_TO_PLANE) cp_async8(sb + 8u * t, yb + q + c);
+                cp_async16(sa_s + 16u * t, ya + q + c);
+                if (kType == SS_ICP_POINT_TO_PLANE) cp_async8(sb_s + 8u * t, yb + q + c);
             }
         }
         cp_async_wait_all();
     }
     __syncthreads();
 
-    // this pixel's terms as float pairs, padded to 32 for the transpose-reduce
+    int best0 = -1, best1 = -1;
+    if (staged) {
+        // the thread's windows: the upper one leads, and the other joins it
+        // when it lies dr = 0..2 rows below in the same columns (its rows are
+        // then the lead's rows dr..dr + 9); a lower window that does not join
+        // is scanned on its own afterwards
+        int dr = 0;
+        bool joined = false, swap = !sa && sb;  // swap: the lower pixel leads
+        if (sa && sb && ca_j == cb_j && abs(cb_i - ca_i) <= 2) {
+            joined = true;
+            dr = abs(cb_i - ca_i);
+            swap = cb_i < ca_i;
+        }
+        const F3 pl = swap ? pb : pa, pm = swap ? pa : pb;
+        IcpBest bl, bm;
+        if (sa || sb) {
+            const int li = swap ? cb_i : ca_i, lj = swap ? cb_j : ca_j;
+            const int base = (li - kIcpSearch - r0) * W + (lj - kIcpSearch - q0);
+            const int nr = 2 * kIcpSearch + dr;
+#pragma unroll 1
+            for (int dk = 0; dk < nr; dk++)
+                icp_scan_row<kType>(sA, sB, base + dk * W, pl, dk < 2 * kIcpSearch, bl, pm, joined && dk >= dr, bm);
+        }
+        if (sa && sb && !joined) {  // the lower window on its own (the upper one led)
+            const int base = (cb_i - kIcpSearch - r0) * W + (cb_j - kIcpSearch - q0);
+#pragma unroll 1
+            for (int dk = 0; dk < 2 * kIcpSearch; dk++)
+                icp_scan_row<kType>(sA, sB, base + dk * W, pb, true, bm, pa, false, bl);
+        }
+        best0 = swap ? bm.best() : bl.best();
+        best1 = swap ? bl.best() : bm.best();
+    } else {
+        if (sa) best0 = icp_search_global<kType>(ya, yb, cols, ca_i, ca_j, pa);
+        if (sb) best1 = icp_search_global<kType>(ya, yb, cols, cb_i, cb_j, pb);
+    }
+
+    // this thread's terms as float pairs, padded to 32 for the transpose-reduce
     float vh[32], vl[32];
 #pragma unroll
     for (int k = 0; k < 32; k++) vh[k] = vl[k] = 0.f;
-    if (has_x) vh[17] = 1.f;  // n_pointsinX
-    if (search) {
-        float smallest = max_dist;
-        int best = -1;
-        if (staged) {
-            // rows of the window in scan order (k outer, l inner); a row's ten
-            // taps are loaded before its comparisons. The even and the odd
-            // columns keep separate minima (two independent compare chains);
-            // the first tap of the scan with the smallest distance is then
-            // the one of the smaller minimum, on a tie the earlier tap (a
-            // smaller staged index: the staged rows are in scan order).
-            const int base = (ci - n_search - r0) * W + (cj - n_search - q0);
-            float s1 = max_dist;
-            int b1 = -1;
-#pragma unroll 1
-            for (int dk = 0; dk < 2 * n_search; dk++) {
-#pragma unroll
-              for (int half = 0; half < 2; half++) {  // a half row's taps are loaded before their comparisons
-                const int row = base + dk * W + half * n_search;
-                float4 a[n_search];
-                float2 b[n_search];
-#pragma unroll
-                for (int dl = 0; dl < n_search; dl++) {
-                    a[dl] = sA[row + dl];
-                    if (kType == SS_ICP_POINT_TO_PLANE) b[dl] = sB[row + dl];
-                }
-#pragma unroll
-                for (int dl = 0; dl < n_search; dl++) {
-                    const F3 py{a[dl].x, a[dl].y, a[dl].z};
-                    const float dist = kType == SS_ICP_POINT_TO_POINT
-                                           ? f3len(f3sub(py, px))
-                                           : fabsf(f3dot(f3sub(py, px), F3{a[dl].w, b[dl].x, b[dl].y}));
-                    if ((dl + half * n_search) & 1) {  // an odd column of the window
-                        if (dist < s1) {
-                            s1 = dist;
-                            b1 = row + dl;
-                        }
-                    } else if (dist < smallest) {
-                        smallest = dist;
-                        best = row + dl;
-                    }
-                }
-              }
-            }
-            if (s1 < smallest || (s1 == smallest && b1 < best)) {
-                smallest = s1;
-                best = b1;
-            }
-        } else {
-            for (int k = ci - n_search; k < ci + n_search; k++) {
-                for (int l = cj - n_search; l < cj + n_search; l++) {
-                    const int tag = k * cols + l;
-                    const float4 a = __ldg(ya + tag);
-                    const float2 b = kType == SS_ICP_POINT_TO_PLANE ? __ldg(yb + tag) : make_float2(0.f, 0.f);
-                    const F3 py{a.x, a.y, a.z}, nn{a.w, b.x, b.y};
-                    const float dist = kType == SS_ICP_POINT_TO_POINT ? f3len(f3sub(py, px))
-                                                                      : fabsf(f3dot(f3sub(py, px), nn));
-                    if (dist < smallest) {
-                        smallest = dist;
-                        best = tag;
-                    }
-                }
-            }
-        }
-        if (best >= 0) {
-            F3 py, nn{0.f, 0.f, 0.f};
-            if (staged) {
-                const float4 a = sA[best];
-                const float2 b = sB[best];
-                py = F3{a.x, a.y, a.z};
-                nn = F3{a.w, b.x, b.y};
-            } else {
-                const float4 a = __ldg(ya + best);
-                py = F3{a.x, a.y, a.z};
-                if (kType == SS_ICP_POINT_TO_PLANE) {
-                    const float2 b = __ldg(yb + best);
-                    nn = F3{a.w, b.x, b.y};
-                }
-            }
-            const F3 bpt = kType == SS_ICP_POINT_TO_POINT ? py : f3add(px, f3smul(f3dot(f3sub(py, px), nn), nn));
-            if (bpt.z != 0) {  // x_nearest(i, j).z != 0: a correspondence (kokkosICP.cpp:131)
-                const float a[3] = {x.x, x.y, x.z}, b[3] = {bpt.x, bpt.y, bpt.z};
-                vh[0] = 1.f;
-#pragma unroll
-                for (int r = 0; r < 3; r++) {
-                    vh[1 + r] = a[r];
-                    vh[4 + r] = b[r];
-#pragma unroll
-                    for (int c = 0; c < 3; c++) {  // x y^T, exact as a pair
-                        const float p = __fmul_rn(a[r], b[c]);
-                        vh[7 + 3 * r + c] = p;
-                        vl[7 + 3 * r + c] = fmaf(a[r], b[c], -p);
-                    }
-                }
-                // RMSE term || x_nearest - Txy x || squared in float (kokkosICP.cpp:137-138; the
-                // reference evaluates the norm in double, this in FP32 with the float Txy)
-                const float e0 = b[0] - fmaf(T.m[0], a[0], fmaf(T.m[1], a[1], fmaf(T.m[2], a[2], T.m[3])));
-                const float e1 = b[1] - fmaf(T.m[4], a[0], fmaf(T.m[5], a[1], fmaf(T.m[6], a[2], T.m[7])));
-                const float e2 = b[2] - fmaf(T.m[8], a[0], fmaf(T.m[9], a[1], fmaf(T.m[10], a[2], T.m[11])));
-                const float tmp = sqrtf(fmaf(e0, e0, fmaf(e1, e1, e2 * e2)));
-                vh[16] = tmp * tmp;
-            }
-        }
-    }
+    vh[17] = (float)((x0.z != 0) + (x1.z != 0));  // n_pointsinX
+    icp_add_terms<kType>(x0, T, best0, staged, sA, sB, ya, yb, vh, vl);
+    icp_add_terms<kType>(x1, T, best1, staged, sA, sB, ya, yb, vh, vl);
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const unsigned nctas = gridDim.x * gridDim.y, cta = blockIdx.y * gridDim.x + blockIdx.x;
     const float2 csum = icp_cta_sum(vh, vl, red);
@@ -719,9 +781,9 @@ __global__ void __launch_bounds__(256, 4) icp_ref_iter_kernel(const float *__res
     st->ticket = 0;
 }
 
-// The iteration kernel's grid: one CTA per 32 x 8 tile of source pixels.
+// The iteration kernel's grid: one CTA per 32 x 16 tile of source pixels.
 static inline int icp_tiles_x(int cols) { return (cols + 31) / 32; }
-static inline int icp_tiles_y(int rows) { return (rows + 7) / 8; }
+static inline int icp_tiles_y(int rows) { return (rows + 15) / 16; }
 
 // Scratch of ss_kokkos_icp, one per device, grown on demand.
 struct IcpWorkspace {
@@ -893,7 +955,7 @@ static ss_status icp_check_args(const uint16_t *d1, const uint16_t *d2, int rows
 // the library is loaded, so the entry point never calls cudaMalloc. Every GPU
 // that loads the library holds these bytes until the process exits.
 constexpr size_t kNoAllocMaxPixels = 640 * 480;  // largest rows * cols accepted
-constexpr int kNoAllocCtas = 4096;  // iteration-grid CTAs (32 x 8 tiles): any rows x cols <= 640 x 480 needs <= 3200
+constexpr int kNoAllocCtas = 4096;  // iteration-grid CTAs (32 x 16 tiles): any rows x cols <= 640 x 480 needs <= 1600
 constexpr size_t kAlign256(size_t n) { return (n + 255) / 256 * 256; }
 constexpr size_t kNoAllocSource = kAlign256(kNoAllocMaxPixels * 12);  // source points
 constexpr size_t kNoAllocTargetA = kAlign256(kNoAllocMaxPixels * 16);  // target (x, y, z, nx)
@@ -956,9 +1018,9 @@ ss_status ss_kokkos_icp_noalloc(const uint16_t *d1, const uint16_t *d2, int32_t 
     }
     int dev = 0;
     SS_CUDA_TRY(cudaGetDevice(&dev));
-    const int ctas = icp_tiles_x(cols) * icp_tiles_y(rows);  // <= 3200 for any image of at most 640 x 480 pixels
+    const int ctas = icp_tiles_x(cols) * icp_tiles_y(rows);  // <= 1600 for any image of at most 640 x 480 pixels
     if (ctas > kNoAllocCtas) {
-        set_last_error_text("ss_kokkos_icp_noalloc: more 32 x 8 tiles than the scratch holds");
+        set_last_error_text("ss_kokkos_icp_noalloc: more 32 x 16 tiles than the scratch holds");
         return SS_ERR_DIMS;
     }
     unsigned char *base = nullptr;
