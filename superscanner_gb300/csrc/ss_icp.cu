@@ -439,13 +439,62 @@ struct IcpBest {
     __device__ __forceinline__ int best() const { return (s1 < s0 || (s1 == s0 && b1 < b0)) ? b1 : b0; }
 };
 
+// Packed pairs of floats (a 64-bit register pair: lane 0 in the low half)
+// and the paired FP32 instructions of this architecture: each half rounded to
+// nearest as the scalar instruction would, so one instruction evaluates a
+// tap's arithmetic for both windows of a pixel pair.
+typedef unsigned long long f32x2;
+__device__ __forceinline__ f32x2 f2_pack(float lo, float hi) {
+    f32x2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ void f2_unpack(f32x2 v, float &lo, float &hi) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ f32x2 f2_sub(f32x2 a, f32x2 b) {
+    f32x2 r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f32x2 f2_mul(f32x2 a, f32x2 b) {
+    f32x2 r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f32x2 f2_add(f32x2 a, f32x2 b) {
+    f32x2 r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+
+// The distances of one tap to two transformed source points (packed x, y and
+// z of both): icp_tap_dist for each, the same roundings in the same order.
+template <int kType>
+__device__ __forceinline__ void icp_tap_dist2(const float4 a, const float2 b, f32x2 px, f32x2 py, f32x2 pz, float &da,
+                                              float &db) {
+    const f32x2 dx = f2_sub(f2_pack(a.x, a.x), px), dy = f2_sub(f2_pack(a.y, a.y), py),
+                dz = f2_sub(f2_pack(a.z, a.z), pz);
+    if (kType == SS_ICP_POINT_TO_POINT) {
+        f2_unpack(f2_add(f2_add(f2_mul(dx, dx), f2_mul(dy, dy)), f2_mul(dz, dz)), da, db);
+        da = __fsqrt_rn(da);
+        db = __fsqrt_rn(db);
+    } else {
+        f2_unpack(f2_add(f2_add(f2_mul(dx, f2_pack(a.w, a.w)), f2_mul(dy, f2_pack(b.x, b.x))), f2_mul(dz, f2_pack(b.y, b.y))),
+                  da, db);
+        da = fabsf(da);
+        db = fabsf(db);
+    }
+}
+
 // One window row of staged taps [row, row + 10) for up to two windows that
 // contain it (a vertical pixel pair's windows share nine of their rows): a
-// half row's taps are loaded once, before their comparisons, and compared
-// with each window that uses the row.
+// half row's taps are loaded once, before their comparisons, and each tap's
+// distances to both source points are evaluated together (packed pairs pa, pb
+// of the two points' coordinates: x, y, z).
 template <int kType>
-__device__ __forceinline__ void icp_scan_row(const float4 *sA, const float2 *sB, int row, F3 pa, bool ua, IcpBest &ba,
-                                             F3 pb, bool ub, IcpBest &bb) {
+__device__ __forceinline__ void icp_scan_row(const float4 *sA, const float2 *sB, int row, f32x2 px, f32x2 py,
+                                             f32x2 pz, bool ua, IcpBest &ba, bool ub, IcpBest &bb) {
 #pragma unroll
     for (int half = 0; half < 2; half++) {
         float4 a[kIcpSearch];
@@ -459,8 +508,10 @@ __device__ __forceinline__ void icp_scan_row(const float4 *sA, const float2 *sB,
         for (int dl = 0; dl < kIcpSearch; dl++) {
             const bool odd = ((dl + half * kIcpSearch) & 1) != 0;
             const int idx = row + half * kIcpSearch + dl;
-            if (ua) ba.take(odd, icp_tap_dist<kType>(a[dl], b[dl], pa), idx);
-            if (ub) bb.take(odd, icp_tap_dist<kType>(a[dl], b[dl], pb), idx);
+            float da, db;
+            icp_tap_dist2<kType>(a[dl], b[dl], px, py, pz, da, db);
+            if (ua) ba.take(odd, da, idx);
+            if (ub) bb.take(odd, db, idx);
         }
     }
 }
@@ -621,6 +672,7 @@ __global__ void __launch_bounds__(256, 4) icp_ref_iter_kernel(const float *__res
             swap = cb_i < ca_i;
         }
         const F3 pl = swap ? pb : pa, pm = swap ? pa : pb;
+        const f32x2 qx = f2_pack(pl.x, pm.x), qy = f2_pack(pl.y, pm.y), qz = f2_pack(pl.z, pm.z);
         IcpBest bl, bm;
         if (sa || sb) {
             const int li = swap ? cb_i : ca_i, lj = swap ? cb_j : ca_j;
@@ -628,13 +680,14 @@ __global__ void __launch_bounds__(256, 4) icp_ref_iter_kernel(const float *__res
             const int nr = 2 * kIcpSearch + dr;
 #pragma unroll 1
             for (int dk = 0; dk < nr; dk++)
-                icp_scan_row<kType>(sA, sB, base + dk * W, pl, dk < 2 * kIcpSearch, bl, pm, joined && dk >= dr, bm);
+                icp_scan_row<kType>(sA, sB, base + dk * W, qx, qy, qz, dk < 2 * kIcpSearch, bl, joined && dk >= dr, bm);
         }
         if (sa && sb && !joined) {  // the lower window on its own (the upper one led)
             const int base = (cb_i - kIcpSearch - r0) * W + (cb_j - kIcpSearch - q0);
+            const f32x2 ux = f2_pack(pb.x, pb.x), uy = f2_pack(pb.y, pb.y), uz = f2_pack(pb.z, pb.z);
 #pragma unroll 1
             for (int dk = 0; dk < 2 * kIcpSearch; dk++)
-                icp_scan_row<kType>(sA, sB, base + dk * W, pb, true, bm, pa, false, bl);
+                icp_scan_row<kType>(sA, sB, base + dk * W, ux, uy, uz, true, bm, false, bl);
         }
         best0 = swap ? bm.best() : bl.best();
         best1 = swap ? bl.best() : bm.best();
