@@ -129,13 +129,12 @@ static inline int icp_group_size(int ctas) {
 
 struct IcpState {
     float Txy[16];      // float copy used by the search (EigentoKmat4f(Txy.cast<float>()))
-    double Txy_d[16];   // double Txy_eigen
-    double best[16];    // bestTxy_eigen
+    float2 best[16];    // bestTxy_eigen, each entry a float pair (hi + lo)
     float lowest;       // lowestRSME
     float best_fitness;
     int ticket;         // groups done
     int iteration;
-    double stats[kIcpIters * 4];
+    float stats[kIcpIters * 4];  // per iteration: correspondences, RMSE, fitness, became best
     int gticket[kIcpMaxGroups];  // CTAs done, per group
 };
 
@@ -273,7 +272,7 @@ __device__ bool polar3_warp(const double *H, double *R) {
 // perturbation of A is below 2 / (s_i + s_j) for the singular values
 // s_i, s_j of the rotation's plane). Returns false otherwise (R unset): the
 // FP64 iteration then decides. Every lane of the warp calls it.
-__device__ bool polar3_warp_f32(const float *Hf, double *R) {
+__device__ bool polar3_warp_f32(const float *Hf, float *R) {
     // every lane iterates the whole 3 x 3 in its registers (no shuffles on
     // the dependent chain); the lanes compute identical values. Hf: H as
     // floats (each lane of the caller converted one entry).
@@ -327,7 +326,7 @@ __device__ bool polar3_warp_f32(const float *Hf, double *R) {
 #pragma unroll
     for (int k = 0; k < 9; k++)
         if (lane == k) mine = X[k];
-    if (lane < 9) R[lane] = (double)mine;
+    if (lane < 9) R[lane] = mine;
     __syncwarp();
     return true;
 }
@@ -567,6 +566,29 @@ __device__ __forceinline__ void icp_add_terms(F3 x, const Mat34 &T, int best, bo
     fp2_add(vh[16], vl[16], tmp * tmp, 0.f);
 }
 
+// Copies the target entries of rows [r0, r0 + h) x columns [q0, q0 + w) of
+// the image into the stage (row pitch w) with asynchronous copies: warp k
+// copies rows k, k + 8, ..., its lanes the columns, the entries in the layout
+// icp_prep_kernel wrote them in. The caller waits for them.
+template <int kType>
+__device__ __forceinline__ void icp_stage(float4 *sA, float2 *sB, const float4 *__restrict__ ya,
+                                          const float2 *__restrict__ yb, int cols, int r0, int q0, int w, int h) {
+    const unsigned sa_s = (unsigned)__cvta_generic_to_shared(sA), sb_s = (unsigned)__cvta_generic_to_shared(sB);
+    const int ln = threadIdx.x & 31;
+    for (int r = threadIdx.x >> 5; r < h; r += 8) {
+        const size_t q = (size_t)(r0 + r) * cols + q0;
+        for (int c = ln; c < w; c += 32) {
+            const int t = r * w + c;
+            cp_async16(sa_s + 16u * t, ya + q + c);
+            if (kType == SS_ICP_POINT_TO_PLANE) cp_async8(sb_s + 8u * t, yb + q + c);
+        }
+    }
+}
+
+// Pixels by which an iteration widens the region its CTA needed in the
+// iteration before when it stages that region ahead of its wait.
+constexpr int kIcpMargin = 2;
+
 // One kokkosICP iteration: Closest Point Kernel (kokkosICP.cpp:69-115) fused
 // with the host sums (:121-171) and, in the last CTA, the rotation update
 // (:173-185). A CTA covers a 32 x 16 tile of source pixels, each thread a
@@ -576,7 +598,12 @@ __device__ __forceinline__ void icp_add_terms(F3 x, const Mat34 &T, int best, bo
 // reference skips holding NaN, so that its distance fails every comparison).
 // The search keeps the reference's scan order and strict comparisons for
 // each window, remembers the best tap and forms the correspondence from it
-// afterwards. When the two windows lie in the same columns at most two rows
+// afterwards. Every iteration after the first stages, before it waits for
+// the previous one, the region its CTA needed there widened by kIcpMargin
+// (regions[cta]: rows r0.., columns q0.., width, height), and keeps it when
+// it holds every window of this iteration (the centres move little between
+// iterations); the images are constant, so any staged region is valid and
+// only its bounds matter. When the two windows lie in the same columns at most two rows
 // apart (the usual case: neighbouring pixels project to neighbouring centres,
 // one row apart), the thread scans their union, loading each tap once for
 // both; otherwise it scans the lower window on its own after the upper one.
@@ -586,12 +613,15 @@ template <int kType>
 __global__ void __launch_bounds__(256, 4) icp_ref_iter_kernel(const float *__restrict__ xp,
                                                            const float4 *__restrict__ ya,
                                                            const float2 *__restrict__ yb, int rows, int cols, Intr in,
-                                                           IcpState *st, float2 *partials, int gsz) {
+                                                           IcpState *st, float2 *partials, int gsz,
+                                                           int4 *__restrict__ regions, int prestage) {
     __shared__ float4 sA[kIcpStage];  // target (x, y, z, nx)
     __shared__ float2 sB[kIcpStage];  // target (ny, nz)
     __shared__ float2 red[8][kIcpSums];
     __shared__ int box[4];
+    __shared__ int4 pre;
     __shared__ bool last;
+    const unsigned nctas = gridDim.x * gridDim.y, cta = blockIdx.y * gridDim.x + blockIdx.x;
     const int j = blockIdx.x * 32 + (threadIdx.x & 31), i0 = blockIdx.y * 16 + 2 * (threadIdx.x >> 5);
     const size_t p0 = (size_t)i0 * cols + j, p1 = p0 + cols;
     // the source points do not change between iterations (written before the
@@ -599,6 +629,28 @@ __global__ void __launch_bounds__(256, 4) icp_ref_iter_kernel(const float *__res
     // whose last CTA is still forming Txy and reading the CTA slots
     const F3 x0 = j < cols && i0 < rows ? ld3(xp, p0) : F3{0.f, 0.f, 0.f};
     const F3 x1 = j < cols && i0 + 1 < rows ? ld3(xp, p1) : F3{0.f, 0.f, 0.f};
+    int4 P = make_int4(0, 0, 0, 0);  // the region staged before the wait: r0, q0, width, height
+    if (prestage) {
+        if (threadIdx.x == 0) {
+            // the region written by this CTA's previous iteration (a stale
+            // read only costs the restaging: it is checked to lie in the image)
+            const int4 R = __ldcg(regions + cta);
+            int4 q = make_int4(0, 0, 0, 0);
+            if (R.z > 0 && R.w > 0 && R.x >= 0 && R.y >= 0 && R.w <= rows - R.x && R.z <= cols - R.y)
+                for (int m = kIcpMargin; m >= 0; m--) {
+                    const int a0 = max(R.x - m, 0), b0 = max(R.y - m, 0);
+                    const int a1 = min(R.x + R.w + m, rows), b1 = min(R.y + R.z + m, cols);
+                    if ((a1 - a0) * (b1 - b0) <= kIcpStage) {
+                        q = make_int4(a0, b0, b1 - b0, a1 - a0);
+                        break;
+                    }
+                }
+            pre = q;
+        }
+        __syncthreads();
+        P = pre;
+        if (P.w > 0) icp_stage<kType>(sA, sB, ya, yb, cols, P.x, P.y, P.z, P.w);
+    }
     pdl_wait();
     Mat34 T;
 #pragma unroll
@@ -639,23 +691,22 @@ __global__ void __launch_bounds__(256, 4) icp_ref_iter_kernel(const float *__res
     const bool any = box[0] != INT_MAX;
     const int r0 = box[0] - kIcpSearch, q0 = box[2] - kIcpSearch;
     const int W = any ? box[3] + kIcpSearch - q0 : 0, H = any ? box[1] + kIcpSearch - r0 : 0;
-    const bool staged = any && W * H <= kIcpStage;
-    if (staged) {
-        // inside the image (the border test keeps every window within rows x
-        // cols): warp w copies rows w, w + 8, ... of the region, its lanes the
-        // columns, the entries in the layout icp_prep_kernel wrote them in
-        const unsigned sa_s = (unsigned)__cvta_generic_to_shared(sA), sb_s = (unsigned)__cvta_generic_to_shared(sB);
-        const int ln = threadIdx.x & 31;
-        for (int r = threadIdx.x >> 5; r < H; r += 8) {
-            const size_t q = (size_t)(r0 + r) * cols + q0;
-            for (int c = ln; c < W; c += 32) {
-                const int t = r * W + c;
-                cp_async16(sa_s + 16u * t, ya + q + c);
-                if (kType == SS_ICP_POINT_TO_PLANE) cp_async8(sb_s + 8u * t, yb + q + c);
-            }
+    // the staged region: the one staged before the wait when it holds every
+    // window (its origin and row pitch sr0, sq0, sw), else this one
+    const bool reuse =
+        any && P.w > 0 && r0 >= P.x && q0 >= P.y && r0 + H <= P.x + P.w && q0 + W <= P.y + P.z;
+    bool staged = reuse || (any && W * H <= kIcpStage);
+    const int sr0 = reuse ? P.x : r0, sq0 = reuse ? P.y : q0, sw = reuse ? P.z : W;
+    if (!reuse && staged) {
+        if (P.w > 0) {  // the early copies land before their entries are overwritten
+            cp_async_wait_all();
+            __syncthreads();
         }
-        cp_async_wait_all();
+        // inside the image: the border test keeps every window within rows x cols
+        icp_stage<kType>(sA, sB, ya, yb, cols, r0, q0, W, H);
     }
+    cp_async_wait_all();
+    if (threadIdx.x == 0) regions[cta] = any ? make_int4(r0, q0, W, H) : make_int4(0, 0, 0, 0);
     __syncthreads();
 
     int best0 = -1, best1 = -1;
@@ -676,18 +727,18 @@ __global__ void __launch_bounds__(256, 4) icp_ref_iter_kernel(const float *__res
         IcpBest bl, bm;
         if (sa || sb) {
             const int li = swap ? cb_i : ca_i, lj = swap ? cb_j : ca_j;
-            const int base = (li - kIcpSearch - r0) * W + (lj - kIcpSearch - q0);
+            const int base = (li - kIcpSearch - sr0) * sw + (lj - kIcpSearch - sq0);
             const int nr = 2 * kIcpSearch + dr;
 #pragma unroll 1
             for (int dk = 0; dk < nr; dk++)
-                icp_scan_row<kType>(sA, sB, base + dk * W, qx, qy, qz, dk < 2 * kIcpSearch, bl, joined && dk >= dr, bm);
+                icp_scan_row<kType>(sA, sB, base + dk * sw, qx, qy, qz, dk < 2 * kIcpSearch, bl, joined && dk >= dr, bm);
         }
         if (sa && sb && !joined) {  // the lower window on its own (the upper one led)
-            const int base = (cb_i - kIcpSearch - r0) * W + (cb_j - kIcpSearch - q0);
+            const int base = (cb_i - kIcpSearch - sr0) * sw + (cb_j - kIcpSearch - sq0);
             const f32x2 ux = f2_pack(pb.x, pb.x), uy = f2_pack(pb.y, pb.y), uz = f2_pack(pb.z, pb.z);
 #pragma unroll 1
             for (int dk = 0; dk < 2 * kIcpSearch; dk++)
-                icp_scan_row<kType>(sA, sB, base + dk * W, ux, uy, uz, true, bm, false, bl);
+                icp_scan_row<kType>(sA, sB, base + dk * sw, ux, uy, uz, true, bm, false, bl);
         }
         best0 = swap ? bm.best() : bl.best();
         best1 = swap ? bl.best() : bm.best();
@@ -704,18 +755,23 @@ __global__ void __launch_bounds__(256, 4) icp_ref_iter_kernel(const float *__res
     icp_add_terms<kType>(x0, T, best0, staged, sA, sB, ya, yb, vh, vl);
     icp_add_terms<kType>(x1, T, best1, staged, sA, sB, ya, yb, vh, vl);
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const unsigned nctas = gridDim.x * gridDim.y, cta = blockIdx.y * gridDim.x + blockIdx.x;
     const float2 csum = icp_cta_sum(vh, vl, red);
     if (threadIdx.x < kIcpSums) partials[(size_t)threadIdx.x * nctas + cta] = csum;  // value-major slots
-    __threadfence();
-    __syncthreads();
     constexpr int kPer = (kIcpSums + 7) / 8;  // values per warp: w, w + 8, w + 16
     const unsigned grp = cta / gsz, gbase = grp * gsz, ngroups = (nctas + gsz - 1) / gsz;
     const unsigned gsize = min((unsigned)gsz, nctas - gbase);
-    if (threadIdx.x == 0) last = atomicAdd(&st->gticket[grp], 1) == (int)gsize - 1;
+    // the CTA's slot writes, ordered by the barrier, are released by thread
+    // 0's fence before its ticket; the group's last CTA acquires the others'
+    // by a fence after its ticket (then the barrier) and reads them from L2
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        const bool l = atomicAdd(&st->gticket[grp], 1) == (int)gsize - 1;
+        if (l) __threadfence();
+        last = l;
+    }
     __syncthreads();
     if (!last) return;  // (a CTA's exit lets the next iteration launch)
-    __threadfence();
     // the group's last CTA: lane b of warp w adds slots gbase + b, + 32, ...
     // of values w, w + 8, w + 16, then a fixed shuffle tree into the group slot
     float2 *gslots = partials + (size_t)kIcpSums * nctas;  // [value][group]
@@ -735,22 +791,26 @@ __global__ void __launch_bounds__(256, 4) icp_ref_iter_kernel(const float *__res
         }
         if (lane == 0 && v < kIcpSums) gslots[(size_t)v * ngroups + grp] = make_float2(h, l);
     }
-    if (threadIdx.x == 0) st->gticket[grp] = 0;  // every CTA of the group has taken its ticket
-    __threadfence();
     __syncthreads();
-    if (threadIdx.x == 0) last = atomicAdd(&st->ticket, 1) == (int)ngroups - 1;
+    if (threadIdx.x == 0) {
+        st->gticket[grp] = 0;  // every CTA of the group has taken its ticket
+        __threadfence();
+        const bool l = atomicAdd(&st->ticket, 1) == (int)ngroups - 1;
+        if (l) __threadfence();
+        last = l;
+    }
     __syncthreads();
     pdl_trigger();  // the next iteration may launch (it waits for this grid before reading anything it writes)
     if (!last) return;
-    __threadfence();
+    // the best RMSE so far, loaded while the group slots are summed
+    const float lowest = threadIdx.x < 32 ? *(volatile float *)&st->lowest : 0.f;
     // last CTA: warp w sums values w, w + 8, w + 16 (interleaved chains), its
     // lanes striding over the group slots (eight slots per value loaded before
     // their additions; a missing slot adds an exact zero), then a fixed
-    // shuffle tree: float pairs throughout (deterministic), the totals as
-    // doubles (hi + lo)
-    __shared__ double tot[kIcpSums];
-    __shared__ double Hs[9], Rs[9], cxy[6];
-    __shared__ float Hf[9];
+    // shuffle tree: float pairs throughout (deterministic)
+    __shared__ float2 tot[kIcpSums];
+    __shared__ double Hs[9], Rs[9];
+    __shared__ float Hf[9], Rf[9];
     {
         constexpr int kBatch = 4;
         float h[kPer], l[kPer];
@@ -779,46 +839,85 @@ __global__ void __launch_bounds__(256, 4) icp_ref_iter_kernel(const float *__res
                 fp2_add(h[k], l[k], h2, l2);
             }
             const int v = wid + 8 * k;
-            if (lane == 0 && v < kIcpSums) tot[v] = (double)h[k] + (double)l[k];
+            if (lane == 0 && v < kIcpSums) tot[v] = make_float2(h[k], l[k]);
         }
     }
     __syncthreads();
     if (threadIdx.x >= 32) return;
-    const double n = tot[0];
-    if (lane < 6) cxy[lane] = tot[1 + lane] / n;  // centerx (0..2), centery (3..5)
-    __syncwarp();
-    const double *cx = cxy, *cy = cxy + 3;
-    // H = sum (x - cx)(y - cy)^T = sum x y^T - n cx cy^T
-    if (lane < 9) {
-        Hs[lane] = tot[7 + lane] - n * cx[lane / 3] * cy[lane % 3];
-        Hf[lane] = (float)Hs[lane];
+    // the update in float pairs (no FP64 instruction on this serial path; the
+    // reference forms it in double, kokkosICP.cpp:121-185): n is an exact count
+    const unsigned FULL = 0xffffffffu;
+    const float n = tot[0].x;
+    float ch = 0.f, cl = 0.f;  // lane k < 6: centerx (k < 3), centery (k >= 3) = sum / n
+    if (lane < 6) {
+        const float2 t = tot[1 + lane];
+        ch = __fdiv_rn(t.x, n);
+        cl = __fdiv_rn(fmaf(-ch, n, t.x) + t.y, n);  // the remainder t.x - ch n is exact
+        const float q = ch + cl;
+        cl -= q - ch;
+        ch = q;
+    }
+    // H = sum (x - cx)(y - cy)^T = sum x y^T - n cx cy^T, lane 3 r + c: entry (r, c)
+    {
+        const int hr = min(lane / 3, 2), hc = lane % 3;
+        const float xh = __shfl_sync(FULL, ch, hr), xl = __shfl_sync(FULL, cl, hr);
+        const float yh = __shfl_sync(FULL, ch, 3 + hc), yl = __shfl_sync(FULL, cl, 3 + hc);
+        const float ph = xh * yh, pl = fmaf(xh, yh, -ph) + fmaf(xh, yl, xl * yh);
+        const float qh = n * ph, ql = fmaf(n, ph, -qh) + n * pl;
+        if (lane < 9) {
+            float hh = tot[7 + lane].x, hl = tot[7 + lane].y;
+            fp2_add(hh, hl, -qh, -ql);
+            Hf[lane] = hh;
+            Hs[lane] = (double)hh + (double)hl;  // for the rank-deficient fallback
+        }
     }
     __syncwarp();
-    if (!polar3_warp_f32(Hf, Rs) && !polar3_warp(Hs, Rs) && lane == 0) {
-        // rank-deficient H: the SVD's own completion of U
-        double U[9], S[3], V[9];
-        svd3_jacobi(Hs, U, S, V);
-        for (int r = 0; r < 3; r++)
-            for (int c = 0; c < 3; c++)
-                Rs[r * 3 + c] = V[r * 3] * U[c * 3] + V[r * 3 + 1] * U[c * 3 + 1] + V[r * 3 + 2] * U[c * 3 + 2];
+    if (!polar3_warp_f32(Hf, Rf)) {  // the same outcome in every lane
+        if (!polar3_warp(Hs, Rs) && lane == 0) {
+            // rank-deficient H: the SVD's own completion of U
+            double U[9], S[3], V[9];
+            svd3_jacobi(Hs, U, S, V);
+            for (int r = 0; r < 3; r++)
+                for (int c = 0; c < 3; c++)
+                    Rs[r * 3 + c] = V[r * 3] * U[c * 3] + V[r * 3 + 1] * U[c * 3 + 1] + V[r * 3 + 2] * U[c * 3 + 2];
+        }
+        __syncwarp();
+        if (lane < 9) Rf[lane] = (float)Rs[lane];
+        __syncwarp();
     }
-    __syncwarp();
     // the new Txy_eigen, one entry per lane: [R | centery - R centerx] (kokkosICP.cpp:177-179)
-    double tn = (lane % 5 == 0) ? 1.0 : 0.0;
-    if (lane < 12) {
-        const int r = lane >> 2, c = lane & 3;
-        tn = c < 3 ? Rs[r * 3 + c] : cy[r] - (Rs[r * 3] * cx[0] + Rs[r * 3 + 1] * cx[1] + Rs[r * 3 + 2] * cx[2]);
+    float2 tn = make_float2((lane % 5 == 0) ? 1.f : 0.f, 0.f);
+    {
+        const int r = min(lane >> 2, 2);
+        float cxh[3], cxl[3];
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            cxh[k] = __shfl_sync(FULL, ch, k);
+            cxl[k] = __shfl_sync(FULL, cl, k);
+        }
+        const float cyh = __shfl_sync(FULL, ch, 3 + r), cyl = __shfl_sync(FULL, cl, 3 + r);
+        if (lane < 12) {
+            if ((lane & 3) < 3) {
+                tn = make_float2(Rf[r * 3 + (lane & 3)], 0.f);
+            } else {
+                float sh = 0.f, sl = 0.f;  // R centerx as a pair
+#pragma unroll
+                for (int k = 0; k < 3; k++) {
+                    const float a = Rf[r * 3 + k], p = a * cxh[k];
+                    fp2_add(sh, sl, p, fmaf(a, cxh[k], -p) + a * cxl[k]);
+                }
+                float th = cyh, tl = cyl;
+                fp2_add(th, tl, -sh, -sl);
+                tn = make_float2(th, tl);
+            }
+        }
     }
-    if (lane < 16) {
-        st->Txy_d[lane] = tn;
-        st->Txy[lane] = (float)tn;
-    }
-    float rsme = (float)tot[16];
-    rsme /= (float)n;
+    if (lane < 16) st->Txy[lane] = tn.x;
+    float rsme = tot[16].x;
+    rsme /= n;
     rsme = sqrtf(rsme);
-    const float fitness = (float)n / (float)tot[17];
-    const bool became_best = rsme < st->lowest;  // kokkosICP.cpp:181-185 (every lane reads it before lane 0 writes)
-    __syncwarp();
+    const float fitness = n / tot[17].x;
+    const bool became_best = rsme < lowest;  // kokkosICP.cpp:181-185
     if (became_best && lane < 16) st->best[lane] = tn;
     if (lane != 0) return;
     if (became_best) st->lowest = rsme;
@@ -828,7 +927,7 @@ __global__ void __launch_bounds__(256, 4) icp_ref_iter_kernel(const float *__res
         st->stats[it * 4 + 0] = n;
         st->stats[it * 4 + 1] = rsme;
         st->stats[it * 4 + 2] = fitness;
-        st->stats[it * 4 + 3] = became_best ? 1.0 : 0.0;
+        st->stats[it * 4 + 3] = became_best ? 1.f : 0.f;
     }
     st->iteration = it + 1;
     st->ticket = 0;
@@ -844,6 +943,7 @@ struct IcpWorkspace {
     float4 *ya = nullptr;
     float2 *yb = nullptr;
     double *partials = nullptr;
+    int4 *regions = nullptr;
     IcpState *state = nullptr;
     size_t npix = 0;
     int ctas = 0;
@@ -871,11 +971,14 @@ static ss_status icp_workspace(int dev, size_t npix, int ctas, IcpWorkspace **ou
     }
     if (w.ctas < ctas || !w.state) {
         cudaFree(w.partials);
+        cudaFree(w.regions);
         cudaFree(w.state);
         w.partials = nullptr;
+        w.regions = nullptr;
         w.state = nullptr;
         w.ctas = 0;
         if (cudaMalloc(&w.partials, icp_slot_bytes(ctas)) != cudaSuccess ||
+            cudaMalloc(&w.regions, (size_t)ctas * sizeof(int4)) != cudaSuccess ||
             cudaMalloc(&w.state, sizeof(IcpState)) != cudaSuccess) {
             cudaGetLastError();
             return SS_ERR_NOMEM;
@@ -938,7 +1041,7 @@ static void orthonormalize_rotation(double *T) {
 // Runs the 10 iterations on prepared point clouds; shared by the entry points.
 ss_status icp_ref_run(const uint16_t *d1, const uint16_t *d2, int rows, int cols, Intr in, const double tx[16],
                       const double ty[16], int type, float *xp, float4 *ya, float2 *yb, double *partials, int ctas,
-                      IcpState *state, double txy_out[16], float *rmse_out, cudaStream_t s) {
+                      int4 *regions, IcpState *state, double txy_out[16], float *rmse_out, cudaStream_t s) {
     const dim3 blk(128), grid((cols + 127) / 128, rows);
     icp_prep_kernel<<<grid, blk, 0, s>>>(d1, d2, rows, cols, in, type, xp, ya, yb);
     SS_LAUNCH_CHECK();
@@ -954,9 +1057,8 @@ ss_status icp_ref_run(const uint16_t *d1, const uint16_t *d2, int rows, int cols
     IcpState h;
     std::memset(&h, 0, sizeof(h));
     for (int k = 0; k < 16; k++) {
-        h.Txy_d[k] = T[k];
         h.Txy[k] = (float)T[k];
-        h.best[k] = (k % 5 == 0) ? 1.0 : 0.0;
+        h.best[k] = make_float2((k % 5 == 0) ? 1.f : 0.f, 0.f);
     }
     h.lowest = 1e6f;
     h.best_fitness = 0.f;
@@ -979,14 +1081,14 @@ ss_status icp_ref_run(const uint16_t *d1, const uint16_t *d2, int rows, int cols
     for (int it = 0; it < kIcpIters; it++) {
         if (type == SS_ICP_POINT_TO_POINT)
             SS_CUDA_TRY(launch_kernel(icp_ref_iter_kernel<SS_ICP_POINT_TO_POINT>, tiles, dim3(256), 0, s, it > 0, xp, ya,
-                                      yb, rows, cols, in, state, slots, gsz));
+                                      yb, rows, cols, in, state, slots, gsz, regions, (int)(it > 0)));
         else
             SS_CUDA_TRY(launch_kernel(icp_ref_iter_kernel<SS_ICP_POINT_TO_PLANE>, tiles, dim3(256), 0, s, it > 0, xp, ya,
-                                      yb, rows, cols, in, state, slots, gsz));
+                                      yb, rows, cols, in, state, slots, gsz, regions, (int)(it > 0)));
     }
     SS_CUDA_TRY(cudaMemcpyAsync(&h, state, sizeof(h), cudaMemcpyDeviceToHost, s));
     SS_CUDA_TRY(cudaStreamSynchronize(s));
-    for (int k = 0; k < 16; k++) txy_out[k] = h.best[k];
+    for (int k = 0; k < 16; k++) txy_out[k] = (double)h.best[k].x + (double)h.best[k].y;
     orthonormalize_rotation(txy_out);
     if (rmse_out) *rmse_out = h.lowest;
     return SS_OK;
@@ -1015,7 +1117,8 @@ constexpr size_t kNoAllocTargetA = kAlign256(kNoAllocMaxPixels * 16);  // target
 constexpr size_t kNoAllocTargetB = kAlign256(kNoAllocMaxPixels * 8);   // target (ny, nz)
 constexpr size_t kNoAllocImages = kNoAllocSource + kNoAllocTargetA + kNoAllocTargetB;
 constexpr size_t kNoAllocPartials = kAlign256((size_t)(kNoAllocCtas + kIcpMaxGroups) * kIcpSums * 8);  // CTA and group slots
-constexpr size_t kNoAllocBytes = kNoAllocImages + kNoAllocPartials + kAlign256(sizeof(IcpState));
+constexpr size_t kNoAllocRegions = kAlign256((size_t)kNoAllocCtas * sizeof(int4));  // staged region per CTA
+constexpr size_t kNoAllocBytes = kNoAllocImages + kNoAllocPartials + kNoAllocRegions + kAlign256(sizeof(IcpState));
 
 static __device__ __align__(256) unsigned char g_icp_noalloc_scratch[kNoAllocBytes];
 
@@ -1083,9 +1186,10 @@ ss_status ss_kokkos_icp_noalloc(const uint16_t *d1, const uint16_t *d2, int32_t 
     float4 *ya = (float4 *)(base + kNoAllocSource);
     float2 *yb = (float2 *)(base + kNoAllocSource + kNoAllocTargetA);
     double *partials = (double *)(base + kNoAllocImages);
-    IcpState *state = (IcpState *)(base + kNoAllocImages + kNoAllocPartials);
+    int4 *regions = (int4 *)(base + kNoAllocImages + kNoAllocPartials);
+    IcpState *state = (IcpState *)(base + kNoAllocImages + kNoAllocPartials + kNoAllocRegions);
     const Intr in{fx, fy, (float)rows - cy, cx};
-    return icp_ref_run(d1, d2, rows, cols, in, tx, ty, icp_type, xp, ya, yb, partials, ctas, state, txy_out,
+    return icp_ref_run(d1, d2, rows, cols, in, tx, ty, icp_type, xp, ya, yb, partials, ctas, regions, state, txy_out,
                        rmse_out, (cudaStream_t)stream);
 }
 
@@ -1119,7 +1223,7 @@ ss_status ss_kokkos_icp(const uint16_t *d1, const uint16_t *d2, int32_t rows, in
     st = icp_workspace(dev, (size_t)rows * cols, ctas, &w);
     if (st != SS_OK) return st;
     const Intr in{fx, fy, (float)rows - cy, cx};  // ci = resi - cy, cj = cx (kokkosICP.cpp:48-49)
-    return icp_ref_run(d1, d2, rows, cols, in, tx, ty, icp_type, w->xp, w->ya, w->yb, w->partials, ctas, w->state,
+    return icp_ref_run(d1, d2, rows, cols, in, tx, ty, icp_type, w->xp, w->ya, w->yb, w->partials, ctas, w->regions, w->state,
                        txy_out, rmse_out, (cudaStream_t)stream);
 }
 
