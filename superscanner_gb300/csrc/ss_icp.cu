@@ -57,50 +57,6 @@ __global__ void normals_kernel(const float *__restrict__ pcd, int rows, int cols
     out[p * 3 + 2] = n.z;
 }
 
-// depth_to_pcd_kernel for both of kokkosICP's depth images and normals_kernel
-// for the second, in one launch: a pixel's column and row quotients of
-// getPoint are shared by its points, and its neighbours' points are
-// recomputed from their depths with the same roundings, so the three images
-// equal those of the three separate launches bit for bit. The source points
-// go out as float triples; the target point and normal of a pixel as one
-// 16-byte (x, y, z, nx) and one 8-byte (ny, nz) entry, the layout the
-// iteration kernel stages in shared memory, x holding NaN where the
-// reference's search skips the tap (py.z == 0, or n.x == 0 point-to-plane:
-// kokkosICP.cpp:89,100) so that its distance fails every comparison.
-__global__ void icp_prep_kernel(const uint16_t *__restrict__ d1, const uint16_t *__restrict__ d2, int rows, int cols,
-                                Intr in, int type, float *__restrict__ xp, float4 *__restrict__ ya,
-                                float2 *__restrict__ yb) {
-    const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y;
-    if (j >= cols || i >= rows) return;
-    const size_t p = (size_t)i * cols + j;
-    const float qx = __fdiv_rn(__fsub_rn((float)j, in.cj), in.fx), qy = __fdiv_rn(__fsub_rn((float)i, in.ci), in.fy);
-    auto pt = [](float ux, float uy, float d) { return F3{__fmul_rn(ux, d), __fmul_rn(uy, d), d}; };
-    const F3 x = pt(qx, qy, depth_m(__ldg(d1 + p)));
-    const F3 c = pt(qx, qy, depth_m(__ldg(d2 + p)));
-    xp[p * 3 + 0] = x.x;
-    xp[p * 3 + 1] = x.y;
-    xp[p * 3 + 2] = x.z;
-    F3 n{0.f, 0.f, 1.f};
-    if (i >= 1 && i < rows - 1 && j >= 1 && j < cols - 1) {
-        const float qxl = __fdiv_rn(__fsub_rn((float)(j - 1), in.cj), in.fx);
-        const float qxr = __fdiv_rn(__fsub_rn((float)(j + 1), in.cj), in.fx);
-        const float qyd = __fdiv_rn(__fsub_rn((float)(i - 1), in.ci), in.fy);
-        const float qyu = __fdiv_rn(__fsub_rn((float)(i + 1), in.ci), in.fy);
-        const F3 up = pt(qx, qyu, depth_m(__ldg(d2 + p + cols))), dn = pt(qx, qyd, depth_m(__ldg(d2 + p - cols)));
-        const F3 rt = pt(qxr, qy, depth_m(__ldg(d2 + p + 1))), lf = pt(qxl, qy, depth_m(__ldg(d2 + p - 1)));
-        if (c.z != 0 && up.z != 0 && dn.z != 0 && rt.z != 0 && lf.z != 0) {  // as normals_kernel
-            const F3 n1 = f3cross(f3sub(up, c), f3sub(rt, c));
-            const F3 n2 = f3cross(f3sub(lf, c), f3sub(up, c));
-            const F3 n3 = f3cross(f3sub(rt, c), f3sub(dn, c));
-            const F3 n4 = f3cross(f3sub(dn, c), f3sub(lf, c));
-            n = f3normalized(f3add(f3add(f3add(n1, n2), n3), n4));
-        }
-    }
-    const bool tap = c.z != 0 && (type == SS_ICP_POINT_TO_POINT || n.x != 0);
-    ya[p] = make_float4(tap ? c.x : __int_as_float(0x7fc00000), c.y, c.z, n.x);
-    yb[p] = make_float2(n.y, n.z);
-}
-
 // 16- and 8-byte asynchronous copies from global to shared memory (no
 // registers held while they are in flight).
 __device__ __forceinline__ void cp_async16(unsigned dst, const void *src) {
@@ -138,10 +94,83 @@ struct IcpState {
     int gticket[kIcpMaxGroups];  // CTAs done, per group
 };
 
+// The starting transform of a call (Txy as floats), passed by value to the
+// prep kernel, which initialises the state with it.
+struct IcpInit {
+    float Txy[16];
+};
+
+// A call's result as the final iteration's last CTA writes it (into host
+// memory mapped into the device's address space, where the caller has some).
+struct IcpOut {
+    float2 best[16];  // bestTxy_eigen as float pairs
+    float lowest;     // lowestRSME
+};
+
 // Bytes of CTA and group slots (8 per slot and value) for `ctas` iteration CTAs.
 static inline size_t icp_slot_bytes(int ctas) {
     return (size_t)(ctas + kIcpMaxGroups) * kIcpSums * 8;
 }
+
+// depth_to_pcd_kernel for both of kokkosICP's depth images and normals_kernel
+// for the second, in one launch: a pixel's column and row quotients of
+// getPoint are shared by its points, and its neighbours' points are
+// recomputed from their depths with the same roundings, so the three images
+// equal those of the three separate launches bit for bit. The source points
+// go out as float triples; the target point and normal of a pixel as one
+// 16-byte (x, y, z, nx) and one 8-byte (ny, nz) entry, the layout the
+// iteration kernel stages in shared memory, x holding NaN where the
+// reference's search skips the tap (py.z == 0, or n.x == 0 point-to-plane:
+// kokkosICP.cpp:89,100) so that its distance fails every comparison.
+__global__ void icp_prep_kernel(const uint16_t *__restrict__ d1, const uint16_t *__restrict__ d2, int rows, int cols,
+                                Intr in, int type, float *__restrict__ xp, float4 *__restrict__ ya,
+                                float2 *__restrict__ yb, IcpInit ini, IcpState *__restrict__ st) {
+    if (blockIdx.x == 0 && blockIdx.y == 0) {  // the call's state: Txy, identity best, counters cleared
+        const int t = threadIdx.x;
+        if (t < 16) {
+            st->Txy[t] = ini.Txy[t];
+            st->best[t] = make_float2(t % 5 == 0 ? 1.f : 0.f, 0.f);
+        }
+        for (int k = t; k < kIcpMaxGroups; k += blockDim.x) st->gticket[k] = 0;
+        for (int k = t; k < kIcpIters * 4; k += blockDim.x) st->stats[k] = 0.f;
+        if (t == 0) {
+            st->lowest = 1e6f;  // lowestRSME (kokkosICP.cpp:59)
+            st->best_fitness = 0.f;
+            st->ticket = 0;
+            st->iteration = 0;
+        }
+    }
+    const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y;
+    if (j >= cols || i >= rows) return;
+    const size_t p = (size_t)i * cols + j;
+    const float qx = __fdiv_rn(__fsub_rn((float)j, in.cj), in.fx), qy = __fdiv_rn(__fsub_rn((float)i, in.ci), in.fy);
+    auto pt = [](float ux, float uy, float d) { return F3{__fmul_rn(ux, d), __fmul_rn(uy, d), d}; };
+    const F3 x = pt(qx, qy, depth_m(__ldg(d1 + p)));
+    const F3 c = pt(qx, qy, depth_m(__ldg(d2 + p)));
+    xp[p * 3 + 0] = x.x;
+    xp[p * 3 + 1] = x.y;
+    xp[p * 3 + 2] = x.z;
+    F3 n{0.f, 0.f, 1.f};
+    if (i >= 1 && i < rows - 1 && j >= 1 && j < cols - 1) {
+        const float qxl = __fdiv_rn(__fsub_rn((float)(j - 1), in.cj), in.fx);
+        const float qxr = __fdiv_rn(__fsub_rn((float)(j + 1), in.cj), in.fx);
+        const float qyd = __fdiv_rn(__fsub_rn((float)(i - 1), in.ci), in.fy);
+        const float qyu = __fdiv_rn(__fsub_rn((float)(i + 1), in.ci), in.fy);
+        const F3 up = pt(qx, qyu, depth_m(__ldg(d2 + p + cols))), dn = pt(qx, qyd, depth_m(__ldg(d2 + p - cols)));
+        const F3 rt = pt(qxr, qy, depth_m(__ldg(d2 + p + 1))), lf = pt(qxl, qy, depth_m(__ldg(d2 + p - 1)));
+        if (c.z != 0 && up.z != 0 && dn.z != 0 && rt.z != 0 && lf.z != 0) {  // as normals_kernel
+            const F3 n1 = f3cross(f3sub(up, c), f3sub(rt, c));
+            const F3 n2 = f3cross(f3sub(lf, c), f3sub(up, c));
+            const F3 n3 = f3cross(f3sub(rt, c), f3sub(dn, c));
+            const F3 n4 = f3cross(f3sub(dn, c), f3sub(lf, c));
+            n = f3normalized(f3add(f3add(f3add(n1, n2), n3), n4));
+        }
+    }
+    const bool tap = c.z != 0 && (type == SS_ICP_POINT_TO_POINT || n.x != 0);
+    ya[p] = make_float4(tap ? c.x : __int_as_float(0x7fc00000), c.y, c.z, n.x);
+    yb[p] = make_float2(n.y, n.z);
+}
+
 
 __device__ void svd3_jacobi(const double *H, double *U, double *S, double *V) {
     double A[9];
@@ -614,7 +643,7 @@ __global__ void __launch_bounds__(256, 4) icp_ref_iter_kernel(const float *__res
                                                            const float4 *__restrict__ ya,
                                                            const float2 *__restrict__ yb, int rows, int cols, Intr in,
                                                            IcpState *st, float2 *partials, int gsz,
-                                                           int4 *__restrict__ regions, int prestage) {
+                                                           int4 *__restrict__ regions, int prestage, IcpOut *out) {
     __shared__ float4 sA[kIcpStage];  // target (x, y, z, nx)
     __shared__ float2 sB[kIcpStage];  // target (ny, nz)
     __shared__ float2 red[8][kIcpSums];
@@ -919,6 +948,10 @@ __global__ void __launch_bounds__(256, 4) icp_ref_iter_kernel(const float *__res
     const float fitness = n / tot[17].x;
     const bool became_best = rsme < lowest;  // kokkosICP.cpp:181-185
     if (became_best && lane < 16) st->best[lane] = tn;
+    if (out) {  // the final iteration, with a host-mapped result
+        if (lane < 16) out->best[lane] = became_best ? tn : st->best[lane];
+        if (lane == 0) out->lowest = became_best ? rsme : lowest;
+    }
     if (lane != 0) return;
     if (became_best) st->lowest = rsme;
     const int it = st->iteration;
@@ -945,6 +978,7 @@ struct IcpWorkspace {
     double *partials = nullptr;
     int4 *regions = nullptr;
     IcpState *state = nullptr;
+    IcpOut *out_host = nullptr, *out_dev = nullptr;  // pinned, mapped
     size_t npix = 0;
     int ctas = 0;
 };
@@ -984,6 +1018,15 @@ static ss_status icp_workspace(int dev, size_t npix, int ctas, IcpWorkspace **ou
             return SS_ERR_NOMEM;
         }
         w.ctas = ctas;
+    }
+    if (!w.out_host) {
+        if (cudaHostAlloc(&w.out_host, sizeof(IcpOut), cudaHostAllocMapped) != cudaSuccess ||
+            cudaHostGetDevicePointer(&w.out_dev, w.out_host, 0) != cudaSuccess) {
+            cudaGetLastError();
+            if (w.out_host) cudaFreeHost(w.out_host);
+            w.out_host = w.out_dev = nullptr;
+            return SS_ERR_NOMEM;
+        }
     }
     *out = &w;
     return SS_OK;
@@ -1039,12 +1082,13 @@ static void orthonormalize_rotation(double *T) {
 }
 
 // Runs the 10 iterations on prepared point clouds; shared by the entry points.
+// With a host-mapped result (out_host, out_dev) the final iteration writes
+// it there and the call ends with a stream synchronisation; without, the
+// state is copied back.
 ss_status icp_ref_run(const uint16_t *d1, const uint16_t *d2, int rows, int cols, Intr in, const double tx[16],
                       const double ty[16], int type, float *xp, float4 *ya, float2 *yb, double *partials, int ctas,
-                      int4 *regions, IcpState *state, double txy_out[16], float *rmse_out, cudaStream_t s) {
-    const dim3 blk(128), grid((cols + 127) / 128, rows);
-    icp_prep_kernel<<<grid, blk, 0, s>>>(d1, d2, rows, cols, in, type, xp, ya, yb);
-    SS_LAUNCH_CHECK();
+                      int4 *regions, IcpState *state, IcpOut *out_host, IcpOut *out_dev, double txy_out[16],
+                      float *rmse_out, cudaStream_t s) {
     // Txy = ty^-1 * tx (kokkosICP.cpp:57), float copy for the search
     double tyi[16], T[16];
     inverse4d(ty, tyi);
@@ -1054,15 +1098,11 @@ ss_status icp_ref_run(const uint16_t *d1, const uint16_t *d2, int rows, int cols
             for (int k = 0; k < 4; k++) acc += tyi[r * 4 + k] * tx[k * 4 + c];
             T[r * 4 + c] = acc;
         }
-    IcpState h;
-    std::memset(&h, 0, sizeof(h));
-    for (int k = 0; k < 16; k++) {
-        h.Txy[k] = (float)T[k];
-        h.best[k] = make_float2((k % 5 == 0) ? 1.f : 0.f, 0.f);
-    }
-    h.lowest = 1e6f;
-    h.best_fitness = 0.f;
-    SS_CUDA_TRY(cudaMemcpyAsync(state, &h, sizeof(h), cudaMemcpyHostToDevice, s));
+    IcpInit ini;
+    for (int k = 0; k < 16; k++) ini.Txy[k] = (float)T[k];
+    const dim3 blk(128), grid((cols + 127) / 128, rows);
+    icp_prep_kernel<<<grid, blk, 0, s>>>(d1, d2, rows, cols, in, type, xp, ya, yb, ini, state);
+    SS_LAUNCH_CHECK();
     const dim3 tiles(icp_tiles_x(cols), icp_tiles_y(rows));  // ctas == tiles.x * tiles.y
     float2 *slots = reinterpret_cast<float2 *>(partials);        // 8 bytes per slot and value, as a double
     const int gsz = icp_group_size((int)(tiles.x * tiles.y));
@@ -1079,18 +1119,31 @@ ss_status icp_ref_run(const uint16_t *d1, const uint16_t *d2, int rows, int cols
     // previous one's last CTA forms the transform (not the first: it loads the
     // source points that the launch before it writes before it waits)
     for (int it = 0; it < kIcpIters; it++) {
+        IcpOut *o = it == kIcpIters - 1 ? out_dev : nullptr;
         if (type == SS_ICP_POINT_TO_POINT)
             SS_CUDA_TRY(launch_kernel(icp_ref_iter_kernel<SS_ICP_POINT_TO_POINT>, tiles, dim3(256), 0, s, it > 0, xp, ya,
-                                      yb, rows, cols, in, state, slots, gsz, regions, (int)(it > 0)));
+                                      yb, rows, cols, in, state, slots, gsz, regions, (int)(it > 0), o));
         else
             SS_CUDA_TRY(launch_kernel(icp_ref_iter_kernel<SS_ICP_POINT_TO_PLANE>, tiles, dim3(256), 0, s, it > 0, xp, ya,
-                                      yb, rows, cols, in, state, slots, gsz, regions, (int)(it > 0)));
+                                      yb, rows, cols, in, state, slots, gsz, regions, (int)(it > 0), o));
     }
-    SS_CUDA_TRY(cudaMemcpyAsync(&h, state, sizeof(h), cudaMemcpyDeviceToHost, s));
-    SS_CUDA_TRY(cudaStreamSynchronize(s));
-    for (int k = 0; k < 16; k++) txy_out[k] = (double)h.best[k].x + (double)h.best[k].y;
+    float2 best[16];
+    float lowest;
+    if (out_host) {
+        SS_CUDA_TRY(cudaStreamSynchronize(s));
+        const volatile IcpOut *o = out_host;
+        for (int k = 0; k < 16; k++) best[k] = make_float2(o->best[k].x, o->best[k].y);
+        lowest = o->lowest;
+    } else {
+        IcpState h;
+        SS_CUDA_TRY(cudaMemcpyAsync(&h, state, sizeof(h), cudaMemcpyDeviceToHost, s));
+        SS_CUDA_TRY(cudaStreamSynchronize(s));
+        for (int k = 0; k < 16; k++) best[k] = h.best[k];
+        lowest = h.lowest;
+    }
+    for (int k = 0; k < 16; k++) txy_out[k] = (double)best[k].x + (double)best[k].y;
     orthonormalize_rotation(txy_out);
-    if (rmse_out) *rmse_out = h.lowest;
+    if (rmse_out) *rmse_out = lowest;
     return SS_OK;
 }
 
@@ -1189,7 +1242,8 @@ ss_status ss_kokkos_icp_noalloc(const uint16_t *d1, const uint16_t *d2, int32_t 
     int4 *regions = (int4 *)(base + kNoAllocImages + kNoAllocPartials);
     IcpState *state = (IcpState *)(base + kNoAllocImages + kNoAllocPartials + kNoAllocRegions);
     const Intr in{fx, fy, (float)rows - cy, cx};
-    return icp_ref_run(d1, d2, rows, cols, in, tx, ty, icp_type, xp, ya, yb, partials, ctas, regions, state, txy_out,
+    return icp_ref_run(d1, d2, rows, cols, in, tx, ty, icp_type, xp, ya, yb, partials, ctas, regions, state, nullptr,
+                       nullptr, txy_out,
                        rmse_out, (cudaStream_t)stream);
 }
 
@@ -1223,7 +1277,8 @@ ss_status ss_kokkos_icp(const uint16_t *d1, const uint16_t *d2, int32_t rows, in
     st = icp_workspace(dev, (size_t)rows * cols, ctas, &w);
     if (st != SS_OK) return st;
     const Intr in{fx, fy, (float)rows - cy, cx};  // ci = resi - cy, cj = cx (kokkosICP.cpp:48-49)
-    return icp_ref_run(d1, d2, rows, cols, in, tx, ty, icp_type, w->xp, w->ya, w->yb, w->partials, ctas, w->regions, w->state,
+    return icp_ref_run(d1, d2, rows, cols, in, tx, ty, icp_type, w->xp, w->ya, w->yb, w->partials, ctas, w->regions,
+                       w->state, w->out_host, w->out_dev,
                        txy_out, rmse_out, (cudaStream_t)stream);
 }
 
