@@ -248,8 +248,12 @@ __global__ void __launch_bounds__(256, 8) fuse_kernel(GridView g, const uint16_t
     }
 }
 
-// Ends a call: remembers and resets the list, advances the epoch.
-__global__ void finalize_kernel(Counters *ctr) { end_call(ctr); }
+// Ends a call: remembers and resets the list, advances the epoch (after the
+// fuse kernel, of which it may be a programmatic dependent).
+__global__ void finalize_kernel(Counters *ctr) {
+    pdl_wait();
+    end_call(ctr);
+}
 
 // Clears the epoch field of every stamp (run when the epoch counter wraps).
 __global__ void rebase_epoch_kernel(GridView g) {
@@ -423,11 +427,17 @@ ss_status launch_fuse(ss_grid *g, const uint16_t *depth, const uint8_t *rgb, con
     const dim3 cblk(32, cr), cgrid((g->p.resj + 31) / 32, (g->p.resi + cr - 1) / cr);
     // shared set of packed coordinates + the list of its distinct entries
     const size_t csmem = tile_set_bytes(cr);  // <= 12 KB (8 rows)
+    // The collection reads the depth before it waits for the kernel before it,
+    // so it is a programmatic dependent only where that kernel is known not to
+    // write the depth (g->pdl: the per-frame pipeline); the fuse and finalize
+    // kernels wait before they read anything and follow this call's own
+    // kernels, so they always are (unless an event sits between).
     SS_CUDA_TRY(launch_kernel(collect_kernel, cgrid, cblk, csmem, s, g->pdl, g->v, depth, E, dpose));
     if (after_collect) SS_CUDA_TRY(cudaEventRecord(after_collect, s));
     const int ctas = persistent_ctas(g, g->lc.fuse_ctas_per_sm);
+    const bool fuse_pdl = g->pdl || !after_collect;
 #define SS_FUSE(ST, C, D, X) \
-    SS_CUDA_TRY(launch_kernel(fuse_kernel<ST, C, D, X>, dim3(ctas), dim3(256), 0, s, g->pdl, g->v, depth, rgb, E, Einv, Ez, dpose))
+    SS_CUDA_TRY(launch_kernel(fuse_kernel<ST, C, D, X>, dim3(ctas), dim3(256), 0, s, fuse_pdl, g->v, depth, rgb, E, Einv, Ez, dpose))
 #define SS_FUSE_X(ST, C, D) \
     do {                    \
         if (exact) SS_FUSE(ST, C, D, true); else SS_FUSE(ST, C, D, false); \
@@ -446,10 +456,7 @@ ss_status launch_fuse(ss_grid *g, const uint16_t *depth, const uint8_t *rgb, con
 #undef SS_FUSE
     SS_LAUNCH_CHECK();
     if (after_fuse) SS_CUDA_TRY(cudaEventRecord(after_fuse, s));
-    if (finalize) {
-        finalize_kernel<<<1, 1, 0, s>>>(g->v.ctr);
-        SS_LAUNCH_CHECK();
-    }
+    if (finalize) SS_CUDA_TRY(launch_kernel(finalize_kernel, dim3(1), dim3(1), 0, s, !after_fuse, g->v.ctr));
     if (manage_epoch) g->host_epoch++;
     return SS_OK;
 }
