@@ -4,9 +4,9 @@
 // The reference runs the 10x10-window correspondence search on the GPU and
 // then copies both point clouds and the correspondences to the host every
 // iteration for centroids, RMSE, H and an Eigen JacobiSVD. Here one kernel
-// per iteration does the search, reduces the 18 sums as exact float pairs
-// (warp shuffles, then one slot per CTA) and the last CTA to finish reduces
-// the CTA slots in a fixed order, takes the rotation as the polar factor of
+// per iteration does the search, reduces the 18 sums per CTA as float pairs
+// (warp shuffles), adds the CTA's totals exactly in fixed point with integer
+// atomics, and the last CTA to finish takes the totals, the rotation as the polar factor of
 // H^T (the SVD's V U^T for a full-rank H; a one-sided Jacobi SVD otherwise)
 // and writes the next Txy, so the 10 iterations run without a host round trip.
 #include <climits>
@@ -71,27 +71,28 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 constexpr int kIcpSums = 18;  // n_cors, sum x (3), sum y (3), sum x y^T (9), sum tmp^2, n_x
 constexpr int kIcpIters = 10; // n_it (kokkosICP.cpp:54)
 
-// The iteration kernel's CTA slots are summed in two stages: the last CTA of
-// each group of CTAs sums the group's slots into a group slot, the last group
-// sums the group slots (a fixed order throughout). Groups of kIcpGroup CTAs,
-// larger where that would make more than kIcpMaxGroups groups.
-constexpr int kIcpGroup = 32;
-constexpr int kIcpMaxGroups = 128;
-
-static inline int icp_group_size(int ctas) {
-    const int g = (ctas + kIcpMaxGroups - 1) / kIcpMaxGroups;
-    return g > kIcpGroup ? g : kIcpGroup;
-}
+// Cross-CTA sums of an iteration in fixed point: a CTA's pair (hi, lo) of
+// value v is converted exactly, to a resolution of 2^-kIcpFix, into a signed
+// integer below 2^95 in magnitude (values below 2^47: every sum of a 640 x 480
+// image is far below), split into three 32-bit chunks (two unsigned, the top
+// one signed) and each chunk added with a 64-bit integer atomic into its own
+// word: fewer than 2^10 CTAs add less than 2^42 to a word, so no carry leaves
+// it. The totals are exact and do not depend on the order in which the CTAs
+// arrive; the last CTA (by ticket) recombines each into a 128-bit integer and
+// takes it as a float pair.
+constexpr int kIcpFix = 48;
+constexpr int kIcpAccWords = 3 * kIcpSums;
 
 struct IcpState {
     float Txy[16];      // float copy used by the search (EigentoKmat4f(Txy.cast<float>()))
     float2 best[16];    // bestTxy_eigen, each entry a float pair (hi + lo)
     float lowest;       // lowestRSME
     float best_fitness;
-    int ticket;         // groups done
+    int ticket;         // CTAs done with the iteration
     int iteration;
+    int overflow;       // a CTA value out of the fixed-point range (or NaN) this iteration
     float stats[kIcpIters * 4];  // per iteration: correspondences, RMSE, fitness, became best
-    int gticket[kIcpMaxGroups];  // CTAs done, per group
+    unsigned long long acc[kIcpAccWords];  // value v: chunk words 3 v, 3 v + 1, 3 v + 2
 };
 
 // The starting transform of a call (Txy as floats), passed by value to the
@@ -107,9 +108,44 @@ struct IcpOut {
     float lowest;     // lowestRSME
 };
 
-// Bytes of CTA and group slots (8 per slot and value) for `ctas` iteration CTAs.
-static inline size_t icp_slot_bytes(int ctas) {
-    return (size_t)(ctas + kIcpMaxGroups) * kIcpSums * 8;
+// f 2^kIcpFix truncated toward zero, for |f| < 2^47 (false otherwise, NaN
+// included), by integer operations.
+__device__ __forceinline__ bool icp_fixed_of_float(float f, __int128 &q) {
+    q = 0;
+    if (!(fabsf(f) < 0x1p47f)) return false;
+    const unsigned u = __float_as_uint(f);
+    const int ex = (int)((u >> 23) & 0xffu);
+    if (ex == 0) return true;  // zero or subnormal: below the resolution
+    const unsigned long long m = (u & 0x7fffffu) | 0x800000u;  // f = m 2^(ex - 150)
+    const int sh = ex - 150 + kIcpFix;                         // < 71: m 2^sh < 2^95
+    __int128 mag = 0;
+    if (sh >= 0)
+        mag = (__int128)m << sh;
+    else if (sh > -24)
+        mag = (__int128)(m >> -sh);
+    q = (u >> 31) ? -mag : mag;
+    return true;
+}
+
+// t 2^-kIcpFix rounded to the nearest float (ties to even), |t| < 2^127, by
+// integer operations (every such value is a normal float).
+__device__ __forceinline__ float icp_float_of_fixed(__int128 t) {
+    if (t == 0) return 0.f;
+    const bool neg = t < 0;
+    unsigned __int128 m = neg ? (unsigned __int128)(-t) : (unsigned __int128)t;
+    const unsigned long long mh = (unsigned long long)(m >> 64), ml = (unsigned long long)m;
+    const int lz = mh ? __clzll((long long)mh) : 64 + __clzll((long long)ml);
+    m <<= lz;  // the leading one at bit 127
+    const unsigned long long th = (unsigned long long)(m >> 64), tl = (unsigned long long)m;
+    unsigned mant = (unsigned)(th >> 40);  // 24 bits
+    int ex = 127 - lz - kIcpFix;           // value in [2^ex, 2^(ex + 1))
+    if (((th >> 39) & 1ull) && ((th & ((1ull << 39) - 1ull)) || tl || (mant & 1u))) {
+        if (++mant >> 24) {
+            mant >>= 1;
+            ex++;
+        }
+    }
+    return __uint_as_float((neg ? 0x80000000u : 0u) | ((unsigned)(ex + 127) << 23) | (mant & 0x7fffffu));
 }
 
 // depth_to_pcd_kernel for both of kokkosICP's depth images and normals_kernel
@@ -131,13 +167,14 @@ __global__ void icp_prep_kernel(const uint16_t *__restrict__ d1, const uint16_t 
             st->Txy[t] = ini.Txy[t];
             st->best[t] = make_float2(t % 5 == 0 ? 1.f : 0.f, 0.f);
         }
-        for (int k = t; k < kIcpMaxGroups; k += blockDim.x) st->gticket[k] = 0;
+        for (int k = t; k < kIcpAccWords; k += blockDim.x) st->acc[k] = 0ull;
         for (int k = t; k < kIcpIters * 4; k += blockDim.x) st->stats[k] = 0.f;
         if (t == 0) {
             st->lowest = 1e6f;  // lowestRSME (kokkosICP.cpp:59)
             st->best_fitness = 0.f;
             st->ticket = 0;
             st->iteration = 0;
+            st->overflow = 0;
         }
     }
     const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y;
@@ -642,7 +679,7 @@ template <int kType>
 __global__ void __launch_bounds__(256, 4) icp_ref_iter_kernel(const float *__restrict__ xp,
                                                            const float4 *__restrict__ ya,
                                                            const float2 *__restrict__ yb, int rows, int cols, Intr in,
-                                                           IcpState *st, float2 *partials, int gsz,
+                                                           IcpState *st,
                                                            int4 *__restrict__ regions, int prestage, IcpOut *out) {
     __shared__ float4 sA[kIcpStage];  // target (x, y, z, nx)
     __shared__ float2 sB[kIcpStage];  // target (ny, nz)
@@ -655,7 +692,7 @@ __global__ void __launch_bounds__(256, 4) icp_ref_iter_kernel(const float *__res
     const size_t p0 = (size_t)i0 * cols + j, p1 = p0 + cols;
     // the source points do not change between iterations (written before the
     // first one): loaded before this launch waits for the previous iteration,
-    // whose last CTA is still forming Txy and reading the CTA slots
+    // whose last CTA is still forming Txy from the totals
     const F3 x0 = j < cols && i0 < rows ? ld3(xp, p0) : F3{0.f, 0.f, 0.f};
     const F3 x1 = j < cols && i0 + 1 < rows ? ld3(xp, p1) : F3{0.f, 0.f, 0.f};
     int4 P = make_int4(0, 0, 0, 0);  // the region staged before the wait: r0, q0, width, height
@@ -783,96 +820,55 @@ __global__ void __launch_bounds__(256, 4) icp_ref_iter_kernel(const float *__res
     vh[17] = (float)((x0.z != 0) + (x1.z != 0));  // n_pointsinX
     icp_add_terms<kType>(x0, T, best0, staged, sA, sB, ya, yb, vh, vl);
     icp_add_terms<kType>(x1, T, best1, staged, sA, sB, ya, yb, vh, vl);
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
     const float2 csum = icp_cta_sum(vh, vl, red);
-    if (threadIdx.x < kIcpSums) partials[(size_t)threadIdx.x * nctas + cta] = csum;  // value-major slots
-    constexpr int kPer = (kIcpSums + 7) / 8;  // values per warp: w, w + 8, w + 16
-    const unsigned grp = cta / gsz, gbase = grp * gsz, ngroups = (nctas + gsz - 1) / gsz;
-    const unsigned gsize = min((unsigned)gsz, nctas - gbase);
-    // the CTA's slot writes, ordered by the barrier, are released by thread
-    // 0's fence before its ticket; the group's last CTA acquires the others'
-    // by a fence after its ticket (then the barrier) and reads them from L2
+    // the CTA's sums into the fixed-point words (thread v < kIcpSums: value v)
+    if (threadIdx.x < kIcpSums) {
+        __int128 qh, ql;
+        const bool ok = icp_fixed_of_float(csum.x, qh) & icp_fixed_of_float(csum.y, ql);
+        if (!ok) atomicOr(&st->overflow, 1);
+        const __int128 q = ok ? qh + ql : (__int128)0;
+        unsigned long long *w = st->acc + 3 * threadIdx.x;
+        atomicAdd(w, (unsigned long long)q & 0xffffffffull);
+        atomicAdd(w + 1, (unsigned long long)(q >> 32) & 0xffffffffull);
+        atomicAdd(w + 2, (unsigned long long)(long long)(q >> 64));
+    }
+    // the additions, ordered by the barrier, are released by thread 0's fence
+    // before its ticket; the last CTA acquires everyone's by a fence after its
+    // ticket and reads the words from L2
     __syncthreads();
     if (threadIdx.x == 0) {
         __threadfence();
-        const bool l = atomicAdd(&st->gticket[grp], 1) == (int)gsize - 1;
+        const bool l = atomicAdd(&st->ticket, 1) == (int)nctas - 1;
         if (l) __threadfence();
         last = l;
     }
     __syncthreads();
     if (!last) return;  // (a CTA's exit lets the next iteration launch)
-    // the group's last CTA: lane b of warp w adds slots gbase + b, + 32, ...
-    // of values w, w + 8, w + 16, then a fixed shuffle tree into the group slot
-    float2 *gslots = partials + (size_t)kIcpSums * nctas;  // [value][group]
-#pragma unroll
-    for (int k = 0; k < kPer; k++) {
-        const int v = wid + 8 * k;
-        float h = 0.f, l = 0.f;
-        if (v < kIcpSums)
-            for (unsigned b = lane; b < gsize; b += 32) {
-                const float2 q = __ldcg(partials + (size_t)v * nctas + gbase + b);
-                fp2_add(h, l, q.x, q.y);
-            }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            const float h2 = __shfl_down_sync(0xffffffffu, h, o), l2 = __shfl_down_sync(0xffffffffu, l, o);
-            fp2_add(h, l, h2, l2);
-        }
-        if (lane == 0 && v < kIcpSums) gslots[(size_t)v * ngroups + grp] = make_float2(h, l);
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        st->gticket[grp] = 0;  // every CTA of the group has taken its ticket
-        __threadfence();
-        const bool l = atomicAdd(&st->ticket, 1) == (int)ngroups - 1;
-        if (l) __threadfence();
-        last = l;
-    }
-    __syncthreads();
-    pdl_trigger();  // the next iteration may launch (it waits for this grid before reading anything it writes)
-    if (!last) return;
-    // the best RMSE so far, loaded while the group slots are summed
-    const float lowest = threadIdx.x < 32 ? *(volatile float *)&st->lowest : 0.f;
-    // last CTA: warp w sums values w, w + 8, w + 16 (interleaved chains), its
-    // lanes striding over the group slots (eight slots per value loaded before
-    // their additions; a missing slot adds an exact zero), then a fixed
-    // shuffle tree: float pairs throughout (deterministic)
+    pdl_trigger();      // the next iteration may launch (it waits for this grid before reading anything it writes)
+    if (threadIdx.x >= 32) return;
+    // last CTA, warp 0: lane v < kIcpSums takes total v as a float pair and
+    // clears its words for the next iteration
+    const float lowest = *(volatile float *)&st->lowest;  // the best RMSE so far
     __shared__ float2 tot[kIcpSums];
     __shared__ double Hs[9], Rs[9];
     __shared__ float Hf[9], Rf[9];
-    {
-        constexpr int kBatch = 4;
-        float h[kPer], l[kPer];
-#pragma unroll
-        for (int k = 0; k < kPer; k++) h[k] = l[k] = 0.f;
-        for (unsigned b0 = lane; b0 < ngroups; b0 += 32 * kBatch) {
-            float2 q[kPer][kBatch];
-#pragma unroll
-            for (int k = 0; k < kPer; k++)
-#pragma unroll
-                for (int i = 0; i < kBatch; i++) {
-                    const int v = wid + 8 * k;
-                    const unsigned b = b0 + 32u * i;
-                    q[k][i] = (v < kIcpSums && b < ngroups) ? __ldcg(gslots + (size_t)v * ngroups + b) : make_float2(0.f, 0.f);
-                }
-#pragma unroll
-            for (int k = 0; k < kPer; k++)
-#pragma unroll
-                for (int i = 0; i < kBatch; i++) fp2_add(h[k], l[k], q[k][i].x, q[k][i].y);
-        }
-#pragma unroll
-        for (int k = 0; k < kPer; k++) {
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                const float h2 = __shfl_down_sync(0xffffffffu, h[k], o), l2 = __shfl_down_sync(0xffffffffu, l[k], o);
-                fp2_add(h[k], l[k], h2, l2);
-            }
-            const int v = wid + 8 * k;
-            if (lane == 0 && v < kIcpSums) tot[v] = make_float2(h[k], l[k]);
-        }
+    if (lane < kIcpSums) {
+        unsigned long long *w = st->acc + 3 * lane;
+        const unsigned long long s0 = __ldcg(w), s1 = __ldcg(w + 1), s2 = __ldcg(w + 2);
+        w[0] = 0ull;
+        w[1] = 0ull;
+        w[2] = 0ull;
+        const __int128 t = (__int128)(long long)s2 * ((__int128)1 << 64) + (__int128)s1 * ((__int128)1 << 32) +
+                           (__int128)s0;
+        const float h = icp_float_of_fixed(t);
+        __int128 hq;
+        icp_fixed_of_float(h, hq);
+        float2 v = make_float2(h, icp_float_of_fixed(t - hq));
+        if (*(volatile int *)&st->overflow) v = make_float2(__int_as_float(0x7fc00000), 0.f);  // as the reference's NaNs
+        tot[lane] = v;
     }
-    __syncthreads();
-    if (threadIdx.x >= 32) return;
+    __syncwarp();
     // the update in float pairs (no FP64 instruction on this serial path; the
     // reference forms it in double, kokkosICP.cpp:121-185): n is an exact count
     const unsigned FULL = 0xffffffffu;
@@ -964,6 +960,7 @@ __global__ void __launch_bounds__(256, 4) icp_ref_iter_kernel(const float *__res
     }
     st->iteration = it + 1;
     st->ticket = 0;
+    st->overflow = 0;
 }
 
 // The iteration kernel's grid: one CTA per 32 x 16 tile of source pixels.
@@ -975,7 +972,6 @@ struct IcpWorkspace {
     float *xp = nullptr;
     float4 *ya = nullptr;
     float2 *yb = nullptr;
-    double *partials = nullptr;
     int4 *regions = nullptr;
     IcpState *state = nullptr;
     IcpOut *out_host = nullptr, *out_dev = nullptr;  // pinned, mapped
@@ -1004,15 +1000,12 @@ static ss_status icp_workspace(int dev, size_t npix, int ctas, IcpWorkspace **ou
         w.npix = npix;
     }
     if (w.ctas < ctas || !w.state) {
-        cudaFree(w.partials);
         cudaFree(w.regions);
         cudaFree(w.state);
-        w.partials = nullptr;
         w.regions = nullptr;
         w.state = nullptr;
         w.ctas = 0;
-        if (cudaMalloc(&w.partials, icp_slot_bytes(ctas)) != cudaSuccess ||
-            cudaMalloc(&w.regions, (size_t)ctas * sizeof(int4)) != cudaSuccess ||
+        if (cudaMalloc(&w.regions, (size_t)ctas * sizeof(int4)) != cudaSuccess ||
             cudaMalloc(&w.state, sizeof(IcpState)) != cudaSuccess) {
             cudaGetLastError();
             return SS_ERR_NOMEM;
@@ -1086,7 +1079,7 @@ static void orthonormalize_rotation(double *T) {
 // it there and the call ends with a stream synchronisation; without, the
 // state is copied back.
 ss_status icp_ref_run(const uint16_t *d1, const uint16_t *d2, int rows, int cols, Intr in, const double tx[16],
-                      const double ty[16], int type, float *xp, float4 *ya, float2 *yb, double *partials, int ctas,
+                      const double ty[16], int type, float *xp, float4 *ya, float2 *yb, int ctas,
                       int4 *regions, IcpState *state, IcpOut *out_host, IcpOut *out_dev, double txy_out[16],
                       float *rmse_out, cudaStream_t s) {
     // Txy = ty^-1 * tx (kokkosICP.cpp:57), float copy for the search
@@ -1104,8 +1097,6 @@ ss_status icp_ref_run(const uint16_t *d1, const uint16_t *d2, int rows, int cols
     icp_prep_kernel<<<grid, blk, 0, s>>>(d1, d2, rows, cols, in, type, xp, ya, yb, ini, state);
     SS_LAUNCH_CHECK();
     const dim3 tiles(icp_tiles_x(cols), icp_tiles_y(rows));  // ctas == tiles.x * tiles.y
-    float2 *slots = reinterpret_cast<float2 *>(partials);        // 8 bytes per slot and value, as a double
-    const int gsz = icp_group_size((int)(tiles.x * tiles.y));
     // four CTAs per SM (64 registers, 38 KB of shared memory each) need the
     // largest shared-memory carveout; a hint, so its status is not fatal
     if (type == SS_ICP_POINT_TO_POINT)
@@ -1122,10 +1113,10 @@ ss_status icp_ref_run(const uint16_t *d1, const uint16_t *d2, int rows, int cols
         IcpOut *o = it == kIcpIters - 1 ? out_dev : nullptr;
         if (type == SS_ICP_POINT_TO_POINT)
             SS_CUDA_TRY(launch_kernel(icp_ref_iter_kernel<SS_ICP_POINT_TO_POINT>, tiles, dim3(256), 0, s, it > 0, xp, ya,
-                                      yb, rows, cols, in, state, slots, gsz, regions, (int)(it > 0), o));
+                                      yb, rows, cols, in, state, regions, (int)(it > 0), o));
         else
             SS_CUDA_TRY(launch_kernel(icp_ref_iter_kernel<SS_ICP_POINT_TO_PLANE>, tiles, dim3(256), 0, s, it > 0, xp, ya,
-                                      yb, rows, cols, in, state, slots, gsz, regions, (int)(it > 0), o));
+                                      yb, rows, cols, in, state, regions, (int)(it > 0), o));
     }
     float2 best[16];
     float lowest;
@@ -1157,8 +1148,8 @@ static ss_status icp_check_args(const uint16_t *d1, const uint16_t *d2, int rows
 }
 
 // ------------------------------------------------- allocation-free variant
-// Scratch of ss_kokkos_icp_noalloc: the same three point / normal images, CTA
-// slots and solver state that ss_kokkos_icp takes from its lazily allocated
+// Scratch of ss_kokkos_icp_noalloc: the same three point / normal images, staged
+// regions and solver state that ss_kokkos_icp takes from its lazily allocated
 // workspace, but in one statically sized device array that exists as soon as
 // the library is loaded, so the entry point never calls cudaMalloc. Every GPU
 // that loads the library holds these bytes until the process exits.
@@ -1169,9 +1160,8 @@ constexpr size_t kNoAllocSource = kAlign256(kNoAllocMaxPixels * 12);  // source 
 constexpr size_t kNoAllocTargetA = kAlign256(kNoAllocMaxPixels * 16);  // target (x, y, z, nx)
 constexpr size_t kNoAllocTargetB = kAlign256(kNoAllocMaxPixels * 8);   // target (ny, nz)
 constexpr size_t kNoAllocImages = kNoAllocSource + kNoAllocTargetA + kNoAllocTargetB;
-constexpr size_t kNoAllocPartials = kAlign256((size_t)(kNoAllocCtas + kIcpMaxGroups) * kIcpSums * 8);  // CTA and group slots
 constexpr size_t kNoAllocRegions = kAlign256((size_t)kNoAllocCtas * sizeof(int4));  // staged region per CTA
-constexpr size_t kNoAllocBytes = kNoAllocImages + kNoAllocPartials + kNoAllocRegions + kAlign256(sizeof(IcpState));
+constexpr size_t kNoAllocBytes = kNoAllocImages + kNoAllocRegions + kAlign256(sizeof(IcpState));
 
 static __device__ __align__(256) unsigned char g_icp_noalloc_scratch[kNoAllocBytes];
 
@@ -1238,11 +1228,10 @@ ss_status ss_kokkos_icp_noalloc(const uint16_t *d1, const uint16_t *d2, int32_t 
     float *xp = (float *)base;
     float4 *ya = (float4 *)(base + kNoAllocSource);
     float2 *yb = (float2 *)(base + kNoAllocSource + kNoAllocTargetA);
-    double *partials = (double *)(base + kNoAllocImages);
-    int4 *regions = (int4 *)(base + kNoAllocImages + kNoAllocPartials);
-    IcpState *state = (IcpState *)(base + kNoAllocImages + kNoAllocPartials + kNoAllocRegions);
+    int4 *regions = (int4 *)(base + kNoAllocImages);
+    IcpState *state = (IcpState *)(base + kNoAllocImages + kNoAllocRegions);
     const Intr in{fx, fy, (float)rows - cy, cx};
-    return icp_ref_run(d1, d2, rows, cols, in, tx, ty, icp_type, xp, ya, yb, partials, ctas, regions, state, nullptr,
+    return icp_ref_run(d1, d2, rows, cols, in, tx, ty, icp_type, xp, ya, yb, ctas, regions, state, nullptr,
                        nullptr, txy_out,
                        rmse_out, (cudaStream_t)stream);
 }
@@ -1277,7 +1266,7 @@ ss_status ss_kokkos_icp(const uint16_t *d1, const uint16_t *d2, int32_t rows, in
     st = icp_workspace(dev, (size_t)rows * cols, ctas, &w);
     if (st != SS_OK) return st;
     const Intr in{fx, fy, (float)rows - cy, cx};  // ci = resi - cy, cj = cx (kokkosICP.cpp:48-49)
-    return icp_ref_run(d1, d2, rows, cols, in, tx, ty, icp_type, w->xp, w->ya, w->yb, w->partials, ctas, w->regions,
+    return icp_ref_run(d1, d2, rows, cols, in, tx, ty, icp_type, w->xp, w->ya, w->yb, ctas, w->regions,
                        w->state, w->out_host, w->out_dev,
                        txy_out, rmse_out, (cudaStream_t)stream);
 }
