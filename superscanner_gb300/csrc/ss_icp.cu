@@ -80,7 +80,7 @@ constexpr int kIcpIters = 10; // n_it (kokkosICP.cpp:54)
 // it. The totals are exact and do not depend on the order in which the CTAs
 // arrive; the last CTA (by ticket) recombines each into a 128-bit integer and
 // takes it as a float pair.
-constexpr int kIcpFix = 48;
+constexpr int kIcpFix = kFix48;
 constexpr int kIcpAccWords = 3 * kIcpSums;
 
 struct IcpState {
@@ -107,25 +107,6 @@ struct IcpOut {
     float2 best[16];  // bestTxy_eigen as float pairs
     float lowest;     // lowestRSME
 };
-
-// f 2^kIcpFix truncated toward zero, for |f| < 2^47 (false otherwise, NaN
-// included), by integer operations.
-__device__ __forceinline__ bool icp_fixed_of_float(float f, __int128 &q) {
-    q = 0;
-    if (!(fabsf(f) < 0x1p47f)) return false;
-    const unsigned u = __float_as_uint(f);
-    const int ex = (int)((u >> 23) & 0xffu);
-    if (ex == 0) return true;  // zero or subnormal: below the resolution
-    const unsigned long long m = (u & 0x7fffffu) | 0x800000u;  // f = m 2^(ex - 150)
-    const int sh = ex - 150 + kIcpFix;                         // < 71: m 2^sh < 2^95
-    __int128 mag = 0;
-    if (sh >= 0)
-        mag = (__int128)m << sh;
-    else if (sh > -24)
-        mag = (__int128)(m >> -sh);
-    q = (u >> 31) ? -mag : mag;
-    return true;
-}
 
 // t 2^-kIcpFix rounded to the nearest float (ties to even), |t| < 2^127, by
 // integer operations (every such value is a normal float).
@@ -825,13 +806,10 @@ __global__ void __launch_bounds__(256, 4) icp_ref_iter_kernel(const float *__res
     // the CTA's sums into the fixed-point words (thread v < kIcpSums: value v)
     if (threadIdx.x < kIcpSums) {
         __int128 qh, ql;
-        const bool ok = icp_fixed_of_float(csum.x, qh) & icp_fixed_of_float(csum.y, ql);
+        const bool ok = fixed48_of_float(csum.x, qh) & fixed48_of_float(csum.y, ql);
         if (!ok) atomicOr(&st->overflow, 1);
         const __int128 q = ok ? qh + ql : (__int128)0;
-        unsigned long long *w = st->acc + 3 * threadIdx.x;
-        atomicAdd(w, (unsigned long long)q & 0xffffffffull);
-        atomicAdd(w + 1, (unsigned long long)(q >> 32) & 0xffffffffull);
-        atomicAdd(w + 2, (unsigned long long)(long long)(q >> 64));
+        fixed48_add(st->acc + 3 * threadIdx.x, q);
     }
     // the additions, ordered by the barrier, are released by thread 0's fence
     // before its ticket; the last CTA acquires everyone's by a fence after its
@@ -859,11 +837,10 @@ __global__ void __launch_bounds__(256, 4) icp_ref_iter_kernel(const float *__res
         w[0] = 0ull;
         w[1] = 0ull;
         w[2] = 0ull;
-        const __int128 t = (__int128)(long long)s2 * ((__int128)1 << 64) + (__int128)s1 * ((__int128)1 << 32) +
-                           (__int128)s0;
+        const __int128 t = fixed48_total(s0, s1, s2);
         const float h = icp_float_of_fixed(t);
         __int128 hq;
-        icp_fixed_of_float(h, hq);
+        fixed48_of_float(h, hq);
         float2 v = make_float2(h, icp_float_of_fixed(t - hq));
         if (*(volatile int *)&st->overflow) v = make_float2(__int_as_float(0x7fc00000), 0.f);  // as the reference's NaNs
         tot[lane] = v;

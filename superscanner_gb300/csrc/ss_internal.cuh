@@ -385,4 +385,66 @@ __device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 __device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 
+// Exact cross-CTA sums in fixed point (resolution 2^-48): a CTA's float
+// value becomes a signed integer below 2^95 in magnitude, added as three
+// 32-bit chunks (two unsigned, the top one signed) into three 64-bit words
+// with integer atomics, so the total does not depend on the order in which
+// the CTAs arrive (fewer than 2^10 CTAs add less than 2^42 to a word: no
+// carry leaves it). All by integer operations: this part's FP64 pipe takes
+// conversions at FMA latency.
+constexpr int kFix48 = 48;
+
+// f 2^48 truncated toward zero, for |f| < 2^47 (false otherwise, NaN included).
+__device__ __forceinline__ bool fixed48_of_float(float f, __int128 &q) {
+    q = 0;
+    if (!(fabsf(f) < 0x1p47f)) return false;
+    const unsigned u = __float_as_uint(f);
+    const int ex = (int)((u >> 23) & 0xffu);
+    if (ex == 0) return true;  // zero or subnormal: below the resolution
+    const unsigned long long m = (u & 0x7fffffu) | 0x800000u;  // f = m 2^(ex - 150)
+    const int sh = ex - 150 + kFix48;                          // < 71: m 2^sh < 2^95
+    __int128 mag = 0;
+    if (sh >= 0)
+        mag = (__int128)m << sh;
+    else if (sh > -24)
+        mag = (__int128)(m >> -sh);
+    q = (u >> 31) ? -mag : mag;
+    return true;
+}
+
+// Adds the fixed-point value q into its three words w[0..2].
+__device__ __forceinline__ void fixed48_add(unsigned long long *w, __int128 q) {
+    atomicAdd(w, (unsigned long long)q & 0xffffffffull);
+    atomicAdd(w + 1, (unsigned long long)(q >> 32) & 0xffffffffull);
+    atomicAdd(w + 2, (unsigned long long)(long long)(q >> 64));
+}
+
+// The total held by three words (their sums of chunks) as a 128-bit integer.
+__device__ __forceinline__ __int128 fixed48_total(unsigned long long s0, unsigned long long s1,
+                                                  unsigned long long s2) {
+    const unsigned __int128 u = ((unsigned __int128)(__int128)(long long)s2 << 64) + ((unsigned __int128)s1 << 32) + s0;
+    return (__int128)u;  // two's complement: the top word's sign
+}
+
+// t 2^-48 rounded to the nearest double (ties to even), |t| < 2^127.
+__device__ __forceinline__ double f64_of_fixed48(__int128 t) {
+    if (t == 0) return 0.0;
+    const bool neg = t < 0;
+    unsigned __int128 m = neg ? (unsigned __int128)(-t) : (unsigned __int128)t;
+    const unsigned long long mh = (unsigned long long)(m >> 64), ml = (unsigned long long)m;
+    const int lz = mh ? __clzll((long long)mh) : 64 + __clzll((long long)ml);
+    m <<= lz;  // the leading one at bit 127
+    const unsigned long long th = (unsigned long long)(m >> 64), tl = (unsigned long long)m;
+    unsigned long long mant = th >> 11;  // 53 bits
+    int ex = 127 - lz - kFix48 + 1023;
+    if (((th >> 10) & 1ull) && ((th & 0x3ffull) || tl || (mant & 1ull))) {
+        if (++mant >> 53) {
+            mant >>= 1;
+            ex++;
+        }
+    }
+    return __longlong_as_double((long long)((neg ? 0x8000000000000000ull : 0ull) | ((unsigned long long)ex << 52) |
+                                            (mant & 0xfffffffffffffull)));
+}
+
 }  // namespace ss

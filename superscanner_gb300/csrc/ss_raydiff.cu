@@ -20,9 +20,10 @@
 //   dL/d omega   = -e (p x g) + b (p x h + d x n)
 //   dL/d upsilon = -e g + b h
 //   dL/d s_k     = -e w_k + b (m . grad w_k)
-// The pose gradient is reduced per CTA into slots (FP32), the last CTA sums
-// the slots in FP64; voxel gradients are scattered with atomicAdd into a
-// caller buffer laid out like the TSDF payload ([buckets][512] floats).
+// The pose gradient is reduced per CTA (FP32), the CTAs' values added exactly
+// in fixed point with integer atomics (order-independent), the last CTA
+// takes the totals as doubles; voxel gradients are scattered with atomicAdd
+// into a caller buffer laid out like the TSDF payload ([buckets][512] floats).
 #include "ss_grid_impl.cuh"
 #include "ss_trilinear.cuh"
 
@@ -90,8 +91,9 @@ __device__ __forceinline__ void cell_sample(const GridView &g, float px, float p
 template <int kStorage, bool kBackward>
 __global__ void __launch_bounds__(256) raydiff_kernel(GridView g, Mat34 T, const uint16_t *__restrict__ obs,
                                                       int max_steps, float t_min, float t_max, float lambda_n,
-                                                      float r_max, float2 *__restrict__ slots, double *result,
-                                                      int *ticket, float *__restrict__ grad_vox,
+                                                      float r_max, unsigned long long *__restrict__ facc,
+                                                      double *result, double *result_host, int *ticket,
+                                                      float *__restrict__ grad_vox,
                                                       float *__restrict__ depth_out,
                                                       const uint8_t *__restrict__ mask) {
     const int j = blockIdx.x * 32 + threadIdx.x;
@@ -183,12 +185,13 @@ __global__ void __launch_bounds__(256) raydiff_kernel(GridView g, Mat34 T, const
             }
         }
     }
-    // CTA reduction into value-major slots, the last CTA sums them in FP64
+    // CTA reduction, the CTAs' values added in fixed point (words 3 v, 3 v + 1,
+    // 3 v + 2 of value v; word 3 kDiffSums counts values out of range)
     __shared__ float red[8][kDiffSums];
     __shared__ bool last;
     const int lane = (threadIdx.y * blockDim.x + threadIdx.x) & 31, wid = (threadIdx.y * blockDim.x + threadIdx.x) >> 5;
     const int tid = threadIdx.y * blockDim.x + threadIdx.x;
-    const int nb = gridDim.x * gridDim.y, bid = blockIdx.y * gridDim.x + blockIdx.x;
+    const int nb = gridDim.x * gridDim.y;
 #pragma unroll
     for (int k = 0; k < kDiffSums; k++) {
         float v = acc[k];
@@ -200,61 +203,69 @@ __global__ void __launch_bounds__(256) raydiff_kernel(GridView g, Mat34 T, const
     if (tid < kDiffSums) {
         float v = 0.f;
         for (int w = 0; w < 8; w++) v += red[w][tid];
-        slots[(size_t)tid * nb + bid] = make_float2(v, 0.f);
+        __int128 q;
+        if (fixed48_of_float(v, q)) fixed48_add(facc + 3 * tid, q);
+        else atomicAdd(facc + 3 * kDiffSums, 1ull);
     }
-    __threadfence();
+    // the additions, ordered by the barrier, are released by thread 0's fence
+    // before its ticket; the last CTA acquires them by a fence after its own
     __syncthreads();
-    if (tid == 0) last = atomicAdd(ticket, 1) == nb - 1;
-    __syncthreads();
-    if (!last) return;
-    __threadfence();
-    // warp w sums value w: its lanes stride over the CTA slots, four slots per
-    // round loaded before their additions into four FP64 partial sums (not one
-    // dependent chain of nb additions), then a fixed shuffle tree
-    for (int v = wid; v < kDiffSums; v += (int)((blockDim.x * blockDim.y) >> 5)) {
-        double a[4] = {0.0, 0.0, 0.0, 0.0};
-        for (int q0 = lane; q0 < nb; q0 += 32 * 4) {
-            float s[4];
-#pragma unroll
-            for (int u = 0; u < 4; u++) {
-                const int q = q0 + 32 * u;
-                s[u] = q < nb ? __ldcg(slots + (size_t)v * nb + q).x : 0.f;
-            }
-#pragma unroll
-            for (int u = 0; u < 4; u++) a[u] += (double)s[u];
-        }
-        double t = (a[0] + a[1]) + (a[2] + a[3]);
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
-        if (lane == 0) result[v] = t;
+    if (tid == 0) {
+        __threadfence();
+        const bool l = atomicAdd(ticket, 1) == nb - 1;
+        if (l) __threadfence();
+        last = l;
     }
-    if (tid == 0) *ticket = 0;
+    __syncthreads();
+    if (!last || tid >= 32) return;
+    // lane v < kDiffSums: total v as a double; the words cleared for the next call
+    const bool bad = __ldcg(facc + 3 * kDiffSums) != 0ull;
+    if (lane < kDiffSums) {
+        unsigned long long *w = facc + 3 * lane;
+        const unsigned long long s0 = __ldcg(w), s1 = __ldcg(w + 1), s2 = __ldcg(w + 2);
+        w[0] = 0ull;
+        w[1] = 0ull;
+        w[2] = 0ull;
+        const double t = bad ? __longlong_as_double(0x7ff8000000000000ll) : f64_of_fixed48(fixed48_total(s0, s1, s2));
+        result[lane] = t;
+        if (result_host) result_host[lane] = t;
+    }
+    __syncwarp();
+    if (lane == 0) {
+        facc[3 * kDiffSums] = 0ull;
+        *ticket = 0;
+    }
 }
 
 struct DiffScratch {
-    float2 *slots = nullptr;
+    unsigned long long *facc = nullptr;  // 3 kDiffSums fixed-point words and the out-of-range count
     double *result = nullptr;
+    double *result_host = nullptr, *result_mapped = nullptr;  // pinned, mapped
     int *ticket = nullptr;
-    int nb = 0;
 };
 
-static ss_status diff_scratch(ss_grid *g, int nb, DiffScratch **out) {
+static ss_status diff_scratch(ss_grid *g, DiffScratch **out) {
     static DiffScratch per_device[64];
     if (g->device < 0 || g->device >= 64) return SS_ERR_ARG;
     DiffScratch &d = per_device[g->device];
-    if (d.nb < nb) {
-        cudaFree(d.slots);
-        cudaFree(d.result);
-        cudaFree(d.ticket);
-        d = DiffScratch{};
-        if (cudaMalloc(&d.slots, (size_t)nb * kDiffSums * sizeof(float2)) != cudaSuccess ||
+    if (!d.facc) {
+        const size_t words = 3 * kDiffSums + 1;
+        if (cudaMalloc(&d.facc, words * sizeof(unsigned long long)) != cudaSuccess ||
             cudaMalloc(&d.result, kDiffSums * sizeof(double)) != cudaSuccess ||
-            cudaMalloc(&d.ticket, sizeof(int)) != cudaSuccess) {
+            cudaMalloc(&d.ticket, sizeof(int)) != cudaSuccess ||
+            cudaHostAlloc(&d.result_host, kDiffSums * sizeof(double), cudaHostAllocMapped) != cudaSuccess ||
+            cudaHostGetDevicePointer(&d.result_mapped, d.result_host, 0) != cudaSuccess) {
             cudaGetLastError();
+            cudaFree(d.facc);
+            cudaFree(d.result);
+            cudaFree(d.ticket);
+            if (d.result_host) cudaFreeHost(d.result_host);
+            d = DiffScratch{};
             return SS_ERR_NOMEM;
         }
-        if (cudaMemset(d.ticket, 0, sizeof(int)) != cudaSuccess) return SS_ERR_CUDA;
-        d.nb = nb;
+        if (cudaMemset(d.facc, 0, words * sizeof(unsigned long long)) != cudaSuccess ||
+            cudaMemset(d.ticket, 0, sizeof(int)) != cudaSuccess)
+            return SS_ERR_CUDA;
     }
     *out = &d;
     return SS_OK;
@@ -273,13 +284,13 @@ static ss_status raydiff(ss_grid *g, const double T[16], const uint16_t *obs, fl
     }
     const dim3 blk(32, 8), grid((g->p.resj + 31) / 32, (g->p.resi + 7) / 8);
     DiffScratch *d = nullptr;
-    ss_status st = diff_scratch(g, grid.x * grid.y, &d);
+    ss_status st = diff_scratch(g, &d);
     if (st != SS_OK) return st;
     const Mat34 M = mat34_from(Tf);
     const float t_min = g->p.rmin, t_max = g->p.d_max;
 #define SS_RD(ST, BW)                                                                                           \
-    raydiff_kernel<ST, BW><<<grid, blk, 0, s>>>(g->v, M, obs, max_steps, t_min, t_max, lambda_n, r_max, d->slots, \
-                                                d->result, d->ticket, grad_vox, depth_out, mask)
+    raydiff_kernel<ST, BW><<<grid, blk, 0, s>>>(g->v, M, obs, max_steps, t_min, t_max, lambda_n, r_max, d->facc, \
+                                                d->result, d->result_mapped, d->ticket, grad_vox, depth_out, mask)
     if (g->p.storage == SS_STORAGE_F32) {
         if (backward) SS_RD(SS_STORAGE_F32, true); else SS_RD(SS_STORAGE_F32, false);
     } else {
@@ -287,9 +298,9 @@ static ss_status raydiff(ss_grid *g, const double T[16], const uint16_t *obs, fl
     }
 #undef SS_RD
     SS_LAUNCH_CHECK();
+    SS_CUDA_TRY(cudaStreamSynchronize(s));  // the last CTA wrote the totals into mapped host memory
     double h[kDiffSums];
-    SS_CUDA_TRY(cudaMemcpyAsync(h, d->result, sizeof(h), cudaMemcpyDeviceToHost, s));
-    SS_CUDA_TRY(cudaStreamSynchronize(s));
+    for (int k = 0; k < kDiffSums; k++) h[k] = ((volatile double *)d->result_host)[k];
     *loss = h[0];
     if (backward)
         for (int k = 0; k < 6; k++) grad[k] = h[1 + k];
