@@ -319,7 +319,7 @@ ss_status ss_kokkos_icp(const uint16_t *d1, const uint16_t *d2, int32_t rows, in
 /* No counterpart in the reference. Same computation, arguments and results as
  * ss_kokkos_icp, but it allocates nothing: for callers that cannot call
  * cudaMalloc while tracking (a real-time thread, or a process whose device
- * memory belongs to its own pool allocator). Its scratch is a fixed 11.7 MB
+ * memory belongs to its own pool allocator). Its scratch is a fixed 11.1 MB
  * device array that every GPU loading the library holds until exit; rows *
  * cols above 640 x 480 return SS_ERR_DIMS. The first call on a device looks up
  * the array's address and should come before any stream capture; the address
