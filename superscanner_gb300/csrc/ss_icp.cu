@@ -485,35 +485,6 @@ struct IcpBest {
     __device__ __forceinline__ int best() const { return (s1 < s0 || (s1 == s0 && b1 < b0)) ? b1 : b0; }
 };
 
-// Packed pairs of floats (a 64-bit register pair: lane 0 in the low half)
-// and the paired FP32 instructions of this architecture: each half rounded to
-// nearest as the scalar instruction would, so one instruction evaluates a
-// tap's arithmetic for both windows of a pixel pair.
-typedef unsigned long long f32x2;
-__device__ __forceinline__ f32x2 f2_pack(float lo, float hi) {
-    f32x2 r;
-    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
-    return r;
-}
-__device__ __forceinline__ void f2_unpack(f32x2 v, float &lo, float &hi) {
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
-}
-__device__ __forceinline__ f32x2 f2_sub(f32x2 a, f32x2 b) {
-    f32x2 r;
-    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-__device__ __forceinline__ f32x2 f2_mul(f32x2 a, f32x2 b) {
-    f32x2 r;
-    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-__device__ __forceinline__ f32x2 f2_add(f32x2 a, f32x2 b) {
-    f32x2 r;
-    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-
 // The distances of one tap to two transformed source points (packed x, y and
 // z of both): icp_tap_dist for each, the same roundings in the same order.
 template <int kType>

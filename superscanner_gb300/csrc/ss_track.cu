@@ -42,6 +42,16 @@ __device__ __forceinline__ void pair_add(float &s, float &c, float s2, float c2)
     c = c + c2 - e;  // compensation holds the negated error (kahan convention: value = s - c)
 }
 
+// pair_add of two independent pairs at once (packed: value 0 in the low
+// halves), the same operations in the same order on each half.
+__device__ __forceinline__ void pair_add2(f32x2 &s, f32x2 &c, f32x2 s2, f32x2 c2) {
+    const f32x2 t = f2_add(s, s2);
+    const f32x2 bp = f2_sub(t, s);
+    const f32x2 e = f2_add(f2_sub(s, f2_sub(t, bp)), f2_sub(s2, bp));
+    s = t;
+    c = f2_sub(f2_add(c, c2), e);
+}
+
 __device__ void mat_from_T(const double *T, float *m) {
     for (int k = 0; k < 12; k++) m[k] = (float)T[k];
 }
@@ -308,14 +318,31 @@ __device__ __forceinline__ float2 track_cta_pairs(float *s, float *c, float2 (*r
 #pragma unroll
     for (int o = 16; o >= 1; o >>= 1) {
         const bool upper = (lane & o) != 0;
+        if (o >= 2) {  // two values per step in paired instructions (the same roundings)
 #pragma unroll
-        for (int k = 0; k < o; k++) {
-            const float ss = upper ? vs[k] : vs[k + o], sc = upper ? vc[k] : vc[k + o];
-            float ks = upper ? vs[k + o] : vs[k], kc = upper ? vc[k + o] : vc[k];
-            const float rs = __shfl_xor_sync(0xffffffffu, ss, o), rc = __shfl_xor_sync(0xffffffffu, sc, o);
+            for (int k = 0; k < o; k += 2) {
+                float ss[2], sc[2], ks[2], kc[2], rs[2], rc[2];
+#pragma unroll
+                for (int u = 0; u < 2; u++) {
+                    ss[u] = upper ? vs[k + u] : vs[k + u + o];
+                    sc[u] = upper ? vc[k + u] : vc[k + u + o];
+                    ks[u] = upper ? vs[k + u + o] : vs[k + u];
+                    kc[u] = upper ? vc[k + u + o] : vc[k + u];
+                    rs[u] = __shfl_xor_sync(0xffffffffu, ss[u], o);
+                    rc[u] = __shfl_xor_sync(0xffffffffu, sc[u], o);
+                }
+                f32x2 ps = f2_pack(ks[0], ks[1]), pc = f2_pack(kc[0], kc[1]);
+                pair_add2(ps, pc, f2_pack(rs[0], rs[1]), f2_pack(rc[0], rc[1]));
+                f2_unpack(ps, vs[k], vs[k + 1]);
+                f2_unpack(pc, vc[k], vc[k + 1]);
+            }
+        } else {
+            const float ss = upper ? vs[0] : vs[1], sc = upper ? vc[0] : vc[1];
+            float ks = upper ? vs[1] : vs[0], kc = upper ? vc[1] : vc[0];
+            const float rs = __shfl_xor_sync(0xffffffffu, ss, 1), rc = __shfl_xor_sync(0xffffffffu, sc, 1);
             pair_add(ks, kc, rs, rc);
-            vs[k] = ks;
-            vc[k] = kc;
+            vs[0] = ks;
+            vc[0] = kc;
         }
     }
     if (lane < kTrackSums) red[wid][lane] = make_float2(vs[0], vc[0]);
