@@ -393,6 +393,17 @@ __device__ __forceinline__ void fp2_add(float &h, float &l, float h2, float l2) 
     l = __fsub_rn(t, __fsub_rn(h, s));
 }
 
+// fp2_add of two independent pairs at once (packed: value 0 in the low
+// halves), the same operations in the same order on each half.
+__device__ __forceinline__ void fp2_add2(f32x2 &h, f32x2 &l, f32x2 h2, f32x2 l2) {
+    const f32x2 s = f2_add(h, h2);
+    const f32x2 bb = f2_sub(s, h);
+    const f32x2 e = f2_add(f2_sub(h, f2_sub(s, bb)), f2_sub(h2, bb));
+    const f32x2 t = f2_add(f2_add(l, l2), e);
+    h = f2_add(s, t);
+    l = f2_sub(t, f2_sub(h, s));
+}
+
 // The CTA's 18 sums: each lane's pairs, a warp transpose-reduce (at offset o a
 // lane keeps the half of its values selected by lane bit o and adds the other
 // lane's; after offsets 16..1 lane v holds the warp's pair of value v), then
@@ -403,14 +414,30 @@ __device__ __forceinline__ float2 icp_cta_sum(float *vh, float *vl, float2 (*red
 #pragma unroll
     for (int o = 16; o >= 1; o >>= 1) {
         const bool upper = (lane & o) != 0;
+        if (o >= 2) {  // two values per step in paired instructions (the same roundings)
 #pragma unroll
-        for (int k = 0; k < o; k++) {
-            const float sh = upper ? vh[k] : vh[k + o], sl = upper ? vl[k] : vl[k + o];
-            float kh = upper ? vh[k + o] : vh[k], kl = upper ? vl[k + o] : vl[k];
-            const float rh = __shfl_xor_sync(0xffffffffu, sh, o), rl = __shfl_xor_sync(0xffffffffu, sl, o);
+            for (int k = 0; k < o; k += 2) {
+                float kh[2], kl[2], rh[2], rl[2];
+#pragma unroll
+                for (int u = 0; u < 2; u++) {
+                    const float sh = upper ? vh[k + u] : vh[k + u + o], sl = upper ? vl[k + u] : vl[k + u + o];
+                    kh[u] = upper ? vh[k + u + o] : vh[k + u];
+                    kl[u] = upper ? vl[k + u + o] : vl[k + u];
+                    rh[u] = __shfl_xor_sync(0xffffffffu, sh, o);
+                    rl[u] = __shfl_xor_sync(0xffffffffu, sl, o);
+                }
+                f32x2 ph = f2_pack(kh[0], kh[1]), pl = f2_pack(kl[0], kl[1]);
+                fp2_add2(ph, pl, f2_pack(rh[0], rh[1]), f2_pack(rl[0], rl[1]));
+                f2_unpack(ph, vh[k], vh[k + 1]);
+                f2_unpack(pl, vl[k], vl[k + 1]);
+            }
+        } else {
+            const float sh = upper ? vh[0] : vh[1], sl = upper ? vl[0] : vl[1];
+            float kh = upper ? vh[1] : vh[0], kl = upper ? vl[1] : vl[0];
+            const float rh = __shfl_xor_sync(0xffffffffu, sh, 1), rl = __shfl_xor_sync(0xffffffffu, sl, 1);
             fp2_add(kh, kl, rh, rl);
-            vh[k] = kh;
-            vl[k] = kl;
+            vh[0] = kh;
+            vl[0] = kl;
         }
     }
     if (lane < kIcpSums) red[wid][lane] = make_float2(vh[0], vl[0]);
