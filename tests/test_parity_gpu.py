@@ -137,6 +137,31 @@ def test_kokkos_icp_matches_oracle(kind):
     assert rmse == pytest.approx(rmse_o, rel=1e-3)
 
 
+def test_kokkos_icp_is_bit_reproducible():
+    """The CTAs' totals are added exactly in fixed point, so the result does
+    not depend on the order in which the CTAs finish: repeated calls, and the
+    allocation-free entry point, return the same bits."""
+    import ctypes as C
+    from superscanner_gb300._native import f64x16, lib
+    sc = synth.Scene(1, 1234)
+    P = sc.trajectory(40, 42)
+    depth, _ = sc.render(P[[10, 13]], 480, 640, INTR, noise=True, color=False)
+    a, b = dev(depth[0]), dev(depth[1])
+    stream = torch.cuda.current_stream().cuda_stream
+
+    def call(fn):
+        out = (C.c_double * 16)()
+        rmse = C.c_float()
+        st = fn(C.c_void_p(a.data_ptr()), C.c_void_p(b.data_ptr()), 480, 640, *INTR, f64x16(P[10]), f64x16(P[13]), 1,
+                out, C.byref(rmse), C.c_void_p(stream))
+        assert st == 0, st
+        return np.array(out[:]), rmse.value
+
+    runs = [call(lib.ss_kokkos_icp) for _ in range(3)] + [call(lib.ss_kokkos_icp_noalloc)]
+    for T, r in runs[1:]:
+        assert np.array_equal(T, runs[0][0]) and r == runs[0][1]
+
+
 def test_ragged_image_and_empty_frame():
     rows, cols = 97, 131
     P, depth, rgb, intr = frames(n=3, rows=rows, cols=cols)

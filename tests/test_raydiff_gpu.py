@@ -74,6 +74,16 @@ def wall_grid(storage):
     return g, o, coords, obs
 
 
+def test_pose_loss_and_gradient_are_bit_reproducible():
+    """The CTAs' loss and pose-gradient values are added exactly in fixed
+    point: repeated evaluations return the same bits."""
+    g, o, d, P, depth, dev = setup()
+    T = se3_exp([0.004, -0.003, 0.002, 0.006, -0.004, 0.003]) @ P[7]
+    runs = [raycast_loss_grad(g, T, dev[7]) for _ in range(3)]
+    for L, grad, nv in runs[1:]:
+        assert L == runs[0][0] and np.array_equal(grad, runs[0][1]) and nv == runs[0][2]
+
+
 @pytest.mark.parametrize("storage,tol", [("f32", 0.01), ("f16", 0.01)])
 def test_adjoint_matches_fp64_finite_differences(storage, tol):
     """GPU pose and voxel gradients against FP64 central differences (h = 1e-4
