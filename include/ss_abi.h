@@ -309,8 +309,10 @@ ss_status ss_normals_from_pcd(const float *pcd, int32_t rows, int32_t cols, floa
  * reductions and the rotation (the polar factor of H^T, which is the SVD's
  * V U^T for a full-rank H) all run on the device; the returned rotation is
  * orthonormal to double precision. The call synchronises s once at the end to
- * return the result. Scratch memory is allocated on the first call per device
- * and reused. */
+ * return the result, which the last iteration writes into pinned host memory
+ * mapped into the device's address space (no copy). Scratch memory (device,
+ * and that small pinned buffer) is allocated on the first call per device and
+ * reused. The result is bit-reproducible: the cross-CTA sums are exact. */
 ss_status ss_kokkos_icp(const uint16_t *d1, const uint16_t *d2, int32_t rows, int32_t cols,
                         float fx, float fy, float cx, float cy, const double tx[16],
                         const double ty[16], int32_t icp_type, double txy_out[16],
