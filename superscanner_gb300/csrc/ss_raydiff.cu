@@ -92,7 +92,7 @@ template <int kStorage, bool kBackward>
 __global__ void __launch_bounds__(256) raydiff_kernel(GridView g, Mat34 T, const uint16_t *__restrict__ obs,
                                                       int max_steps, float t_min, float t_max, float lambda_n,
                                                       float r_max, unsigned long long *__restrict__ facc,
-                                                      double *result, double *result_host, int *ticket,
+                                                      double *result, int *ticket,
                                                       float *__restrict__ grad_vox,
                                                       float *__restrict__ depth_out,
                                                       const uint8_t *__restrict__ mask) {
@@ -218,7 +218,8 @@ __global__ void __launch_bounds__(256) raydiff_kernel(GridView g, Mat34 T, const
     }
     __syncthreads();
     if (!last || tid >= 32) return;
-    // lane v < kDiffSums: total v as a double; the words cleared for the next call
+    // lane v < kDiffSums: total v as a double into the mapped host result; the
+    // words cleared for the next call
     const bool bad = __ldcg(facc + 3 * kDiffSums) != 0ull;
     if (lane < kDiffSums) {
         unsigned long long *w = facc + 3 * lane;
@@ -228,7 +229,6 @@ __global__ void __launch_bounds__(256) raydiff_kernel(GridView g, Mat34 T, const
         w[2] = 0ull;
         const double t = bad ? __longlong_as_double(0x7ff8000000000000ll) : f64_of_fixed48(fixed48_total(s0, s1, s2));
         result[lane] = t;
-        if (result_host) result_host[lane] = t;
     }
     __syncwarp();
     if (lane == 0) {
@@ -239,8 +239,7 @@ __global__ void __launch_bounds__(256) raydiff_kernel(GridView g, Mat34 T, const
 
 struct DiffScratch {
     unsigned long long *facc = nullptr;  // 3 kDiffSums fixed-point words and the out-of-range count
-    double *result = nullptr;
-    double *result_host = nullptr, *result_mapped = nullptr;  // pinned, mapped
+    double *result_host = nullptr, *result_mapped = nullptr;  // the totals: pinned host memory, mapped
     int *ticket = nullptr;
 };
 
@@ -251,13 +250,11 @@ static ss_status diff_scratch(ss_grid *g, DiffScratch **out) {
     if (!d.facc) {
         const size_t words = 3 * kDiffSums + 1;
         if (cudaMalloc(&d.facc, words * sizeof(unsigned long long)) != cudaSuccess ||
-            cudaMalloc(&d.result, kDiffSums * sizeof(double)) != cudaSuccess ||
             cudaMalloc(&d.ticket, sizeof(int)) != cudaSuccess ||
             cudaHostAlloc(&d.result_host, kDiffSums * sizeof(double), cudaHostAllocMapped) != cudaSuccess ||
             cudaHostGetDevicePointer(&d.result_mapped, d.result_host, 0) != cudaSuccess) {
             cudaGetLastError();
             cudaFree(d.facc);
-            cudaFree(d.result);
             cudaFree(d.ticket);
             if (d.result_host) cudaFreeHost(d.result_host);
             d = DiffScratch{};
@@ -290,7 +287,7 @@ static ss_status raydiff(ss_grid *g, const double T[16], const uint16_t *obs, fl
     const float t_min = g->p.rmin, t_max = g->p.d_max;
 #define SS_RD(ST, BW)                                                                                           \
     raydiff_kernel<ST, BW><<<grid, blk, 0, s>>>(g->v, M, obs, max_steps, t_min, t_max, lambda_n, r_max, d->facc, \
-                                                d->result, d->result_mapped, d->ticket, grad_vox, depth_out, mask)
+                                                d->result_mapped, d->ticket, grad_vox, depth_out, mask)
     if (g->p.storage == SS_STORAGE_F32) {
         if (backward) SS_RD(SS_STORAGE_F32, true); else SS_RD(SS_STORAGE_F32, false);
     } else {
