@@ -271,6 +271,14 @@ ss_status ss_grid_raycast_counters(ss_grid *g, ss_stream_t s, int64_t out[2]);
  * below). */
 ss_status ss_grid_test_raycast_cap(ss_grid *g, int32_t cap);
 
+/* Test hook of the exact cross-CTA sums that kokkosICP and the differentiable
+ * raycast use (no reference counterpart): the n floats at values (device) are
+ * added, each truncated to a multiple of 2^-48, in fixed point by integer
+ * atomics from many CTAs; out[0] is the total rounded once to double, out[1]
+ * and out[2] the float pair (hi, lo) kokkosICP takes from it. Synchronises s.
+ * SS_ERR_ARG for n < 0 or a value of magnitude 2^47 or more. */
+ss_status ss_test_fixed48_sum(const float *values, int32_t n, double out[3], ss_stream_t s);
+
 /* Text of the last CUDA error seen by this thread (for SS_ERR_CUDA). */
 const char *ss_last_error(void);
 

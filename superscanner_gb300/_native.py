@@ -105,6 +105,7 @@ SIGNATURES = {
     "ss_grid_counters": (_st, [_p, _p, C.POINTER(C.c_int64)]),
     "ss_grid_raycast_counters": (_st, [_p, _p, C.POINTER(C.c_int64)]),
     "ss_grid_test_raycast_cap": (_st, [_p, C.c_int32]),
+    "ss_test_fixed48_sum": (_st, [_p, _i32, C.POINTER(C.c_double), _p]),
     "ss_pipeline_test_wait_timeout": (_st, [_p, C.c_int32]),
     "ss_grid_export_blocks": (_st, [_p, _p, _i32, _p, _p, _p, _p, _p, C.POINTER(_i32)]),
     "ss_grid_export_buckets": (_st, [_p, _p, _i32, _p, C.POINTER(_i32)]),

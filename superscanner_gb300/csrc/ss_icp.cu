@@ -1164,11 +1164,61 @@ static ss_status noalloc_scratch(int dev, unsigned char **out) {
     return SS_OK;
 }
 
+// Test hook kernel: every thread adds its values into the three words; the
+// last CTA (by ticket) forms the total like the kokkosICP and differentiable
+// raycast last CTAs do.
+__global__ void fixed48_sum_kernel(const float *__restrict__ values, int n, unsigned long long *acc, int *ticket,
+                                   double *out) {
+    __shared__ bool last;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        __int128 q;
+        if (fixed48_of_float(values[k], q)) fixed48_add(acc, q);
+        else atomicAdd(acc + 3, 1ull);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        const bool l = atomicAdd(ticket, 1) == (int)gridDim.x - 1;
+        if (l) __threadfence();
+        last = l;
+    }
+    __syncthreads();
+    if (!last || threadIdx.x != 0) return;
+    const __int128 t = fixed48_total(__ldcg(acc), __ldcg(acc + 1), __ldcg(acc + 2));
+    const float h = icp_float_of_fixed(t);
+    __int128 hq;
+    fixed48_of_float(h, hq);
+    out[0] = f64_of_fixed48(t);
+    out[1] = h;
+    out[2] = icp_float_of_fixed(t - hq);
+    out[3] = (double)__ldcg(acc + 3);
+}
+
 }  // namespace ss
 
 using namespace ss;
 
 extern "C" {
+
+ss_status ss_test_fixed48_sum(const float *values, int32_t n, double out[3], ss_stream_t stream) {
+    if (n < 0 || !out || (n > 0 && !values)) return SS_ERR_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    unsigned char *scratch = nullptr;  // 4 words (the chunks, out-of-range count), a ticket, 4 doubles
+    SS_CUDA_TRY(cudaMallocAsync((void **)&scratch, 96, s));
+    SS_CUDA_TRY(cudaMemsetAsync(scratch, 0, 96, s));
+    fixed48_sum_kernel<<<64, 256, 0, s>>>(values, n, (unsigned long long *)scratch, (int *)(scratch + 32),
+                                          (double *)(scratch + 64));
+    SS_LAUNCH_CHECK();
+    double h[4];
+    SS_CUDA_TRY(cudaMemcpyAsync(h, scratch + 64, 4 * sizeof(double), cudaMemcpyDeviceToHost, s));
+    SS_CUDA_TRY(cudaFreeAsync(scratch, s));
+    SS_CUDA_TRY(cudaStreamSynchronize(s));
+    if (h[3] != 0.0) return SS_ERR_ARG;
+    out[0] = h[0];
+    out[1] = h[1];
+    out[2] = h[2];
+    return SS_OK;
+}
 
 // Same computation and arguments as ss_kokkos_icp, for callers that cannot
 // allocate device memory while they run: a tracking thread with a real-time

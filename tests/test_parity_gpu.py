@@ -316,3 +316,27 @@ def test_collection_tile_rows_match_oracle(rows):
         o.integrate(depth[k], rgb[k], E, with_color=False)
     g.sync()
     assert compare(g, o, 0.02, color=False) == 1.0
+
+
+def test_fixed48_sums_are_exact():
+    """The fixed-point cross-CTA sums (kokkosICP, differentiable raycast):
+    the total of each value truncated to a multiple of 2^-48, over values
+    spread across 60 binary orders of magnitude and both signs, is exact, its
+    double is the nearest one, and the float pair is (RN(total), RN(rest))."""
+    import ctypes as C
+    from fractions import Fraction
+    from superscanner_gb300._native import SS_ERR_ARG, lib
+    rng = np.random.default_rng(11)
+    v = (rng.standard_normal(200000) * np.exp2(rng.integers(-40, 20, 200000))).astype(np.float32)
+    v[:5] = [0.0, -0.0, 3.0e-30, 1.0e13, -1.0e13]
+    dv = torch.from_numpy(v).cuda()
+    out = (C.c_double * 3)()
+    assert lib.ss_test_fixed48_sum(C.c_void_p(dv.data_ptr()), len(v), out, None) == 0
+    unit = Fraction(1, 2 ** 48)
+    exact = sum((Fraction(float(x)) / unit).__trunc__() for x in v) * unit
+    assert out[0] == float(exact)  # the nearest double
+    h, l = out[1], out[2]
+    assert h == float(np.float32(float(exact))) or abs(Fraction(h) - exact) <= abs(Fraction(float(np.float32(float(exact)))) - exact)
+    assert abs(Fraction(h) + Fraction(l) - exact) <= abs(exact) * Fraction(1, 2 ** 46) + unit
+    big = torch.tensor([1.0, 2.0 ** 47], dtype=torch.float32, device="cuda")
+    assert lib.ss_test_fixed48_sum(C.c_void_p(big.data_ptr()), 2, out, None) == SS_ERR_ARG
